@@ -1,0 +1,140 @@
+/* tmvg.h -- C ABI of the GB300 (sm_103a) implementation of TMV's dense hot
+ * path: the blocked matrix product and the partial-pivoting LU factor/solve.
+ *
+ * Plain pointers and sizes only.  Matrices are IEEE double (or float where a
+ * name says f32), addressed like a tmv::MatrixView by (stepi, stepj) strides
+ * in elements; "lda"/"ldb" name the stride between columns of a column-major
+ * matrix.  Pivots are int64 (ptrdiff_t on LP64), 0-based, in TMV's (and
+ * LAPACK's) interchange form: at step j row j was swapped with row P[j].
+ *
+ * Functions without "_host" take DEVICE pointers and are stream-ordered on the
+ * handle's stream; they return once the work is enqueued unless stated.
+ * Functions with "_host" take HOST pointers and are synchronous, like the TMV
+ * calls they replace; they copy inputs to the device and results back.
+ *
+ * Each entry point names the TMV 0.76 routine it replaces (file:line in the
+ * TMV source tree).  The drop-in shim (tmv_gb300/shim/tmv_gpu_shim.cpp)
+ * defines those routines' explicit instantiations over this ABI.
+ */
+#ifndef TMVG_H
+#define TMVG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+typedef enum tmvg_status {
+    TMVG_OK = 0,
+    TMVG_SINGULAR = 1,       /* a zero U(j,j) was met while solving (TMV throws
+                                SingularUpperTriMatrix, src/TMV_TriDiv_M.cpp:78-84) */
+    TMVG_NOT_CONVERGED = 2,  /* iterative refinement missed its tolerance */
+    TMVG_BAD_ARG = 3,
+    TMVG_OOM = 4,            /* TMV: std::bad_alloc */
+    TMVG_TIMEOUT = 5,        /* a bounded device-side wait gave up */
+    TMVG_CUDA_ERROR = 6,
+    TMVG_NO_DEVICE = 7,
+    TMVG_UNSUPPORTED = 8
+} tmvg_status;
+
+typedef struct tmvg_context* tmvg_handle;
+
+/* ---- context -------------------------------------------------------- */
+int tmvg_version(void);
+const char* tmvg_status_string(tmvg_status s);
+/* Create a context on `device` (its current CUDA context, default stream). */
+tmvg_status tmvg_create(tmvg_handle* h, int device);
+tmvg_status tmvg_destroy(tmvg_handle h);
+/* Use this cudaStream_t for all later calls (NULL = legacy default stream). */
+tmvg_status tmvg_set_stream(tmvg_handle h, void* cuda_stream);
+tmvg_status tmvg_synchronize(tmvg_handle h);
+/* Text of the last error on this handle ("" if none). */
+const char* tmvg_last_error(tmvg_handle h);
+/* Number of kernels this handle has launched since creation. */
+int64_t tmvg_launch_count(tmvg_handle h);
+
+/* ---- MultMM ----------------------------------------------------------
+ * C (+)= alpha * A * B;  A m x k, B k x n, C m x n.  add = 0: C = alpha*A*B,
+ * add = 1: C += alpha*A*B.  A and B may each be column-major (stepi == 1) or
+ * row-major (stepj == 1): the CCC, CRC, RCC (and RRC) layouts; a row-major C
+ * is computed as C^T = B^T A^T.  Operands must not overlap C.
+ * Replaces: template void tmv::MultMM<add,double,double,double>
+ *           (src/TMV_MultMM.cpp:405-477; declared
+ *            include/tmv/TMV_MatrixArithFunc.h:55-58). */
+tmvg_status tmvg_multmm_f64(tmvg_handle h, int add, double alpha,
+                            int64_t m, int64_t n, int64_t k,
+                            const double* A, int64_t sAi, int64_t sAj,
+                            const double* B, int64_t sBi, int64_t sBj,
+                            double* C, int64_t sCi, int64_t sCj);
+tmvg_status tmvg_multmm_f64_host(tmvg_handle h, int add, double alpha,
+                                 int64_t m, int64_t n, int64_t k,
+                                 const double* A, int64_t sAi, int64_t sAj,
+                                 const double* B, int64_t sBi, int64_t sBj,
+                                 double* C, int64_t sCi, int64_t sCj);
+
+/* ---- LU_Decompose ----------------------------------------------------
+ * In-place P A = L U of an n x n column-major matrix (leading dim lda):
+ * L unit lower below the diagonal, U on and above it, P[0..n) interchanges.
+ * Pivot rule as TMV: first index of the strict maximum |a|; a column whose
+ * largest |a|^2 underflows DBL_MIN is zeroed with P[j] = j.  Never fails on
+ * singular input.
+ * Replaces: template void tmv::LU_Decompose(MatrixView<double>, ptrdiff_t*)
+ *           (src/TMV_LUDecompose.cpp:514-559). */
+tmvg_status tmvg_lu_decompose_f64(tmvg_handle h, int64_t n, double* A,
+                                  int64_t lda, int64_t* P);
+/* Host variant; A may be column- or row-major (stepi/stepj), as TMV allows. */
+tmvg_status tmvg_lu_decompose_f64_host(tmvg_handle h, int64_t n, double* A,
+                                       int64_t sAi, int64_t sAj, int64_t* P);
+
+/* ---- LU_LDivEq / LU_RDivEq -------------------------------------------
+ * LDivEq: B := (P L U)^-1 B, B n x nrhs column-major (ldb).
+ * RDivEq: B := B (P L U)^-1, B nrows x n column-major (ldb).
+ * Return TMVG_SINGULAR when a zero U(j,j) divides a nonzero entry.
+ * Replace: template void tmv::LU_LDivEq / LU_RDivEq<double,double>
+ *          (src/TMV_LUDiv.cpp:186-226, 370-411; declared src/TMV_LUDiv.h:30-35). */
+tmvg_status tmvg_lu_ldiveq_f64(tmvg_handle h, int64_t n, const double* LU,
+                               int64_t lda, const int64_t* P, int64_t nrhs,
+                               double* B, int64_t ldb);
+tmvg_status tmvg_lu_rdiveq_f64(tmvg_handle h, int64_t n, const double* LU,
+                               int64_t lda, const int64_t* P, int64_t nrows,
+                               double* B, int64_t ldb);
+tmvg_status tmvg_lu_ldiveq_f64_host(tmvg_handle h, int64_t n, const double* LU,
+                                    int64_t lda, const int64_t* P, int64_t nrhs,
+                                    double* B, int64_t sBi, int64_t sBj);
+tmvg_status tmvg_lu_rdiveq_f64_host(tmvg_handle h, int64_t n, const double* LU,
+                                    int64_t lda, const int64_t* P, int64_t nrows,
+                                    double* B, int64_t sBi, int64_t sBj);
+
+/* ---- m.divideUsing(tmv::LU); X = B/m --------------------------------
+ * Factor a copy of A (column-major n x n) and solve X = A^-1 B (n x nrhs).
+ * LU and P receive the factors (kept by the caller for later solves, the
+ * saveDiv() behaviour).  Replaces the LUDiv<double> construction + doLDiv
+ * (src/TMV_LUD.cpp:74-120). */
+tmvg_status tmvg_divide_f64(tmvg_handle h, int64_t n, const double* A,
+                            int64_t lda, int64_t nrhs, const double* B,
+                            int64_t ldb, double* X, int64_t ldx, double* LU,
+                            int64_t* P);
+tmvg_status tmvg_divide_f64_host(tmvg_handle h, int64_t n, const double* A,
+                                 int64_t nrhs, const double* B, double* X,
+                                 double* LU, int64_t* P);
+
+/* det / logDet of stored factors (LUDiv::det, logDet: src/TMV_LUD.cpp:132-156). */
+tmvg_status tmvg_lu_det_f64(tmvg_handle h, int64_t n, const double* LU,
+                            int64_t lda, const int64_t* P, double* det,
+                            double* logdet, double* sign);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TMVG_H */

@@ -1,0 +1,222 @@
+"""CPU checkers for the GPU path -- TEST INFRASTRUCTURE ONLY.
+
+Two interchangeable backends with one numpy interface:
+
+* ``port()``  -- oracle/_build/liboracle.so, the C restatement of TMV's
+  MultMM / LU_Decompose / LU_LDivEq / LU_RDivEq (tmv_oracle.c).  Builds on any
+  machine with gcc (``make -C oracle port``).
+* ``ref()``   -- oracle/_ref/libtmvref.so, TMV 0.76 itself compiled from the
+  reference sources (``make -C oracle ref``; only where those sources exist).
+  ``ref(generic=True)`` uses TMV's generic (non-SSE) product kernels, the ones
+  an aarch64 build runs.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs use this
+package.  The product (tmv_gb300/) never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+PORT_LIB = HERE / "_build" / "liboracle.so"
+REF_LIB = HERE / "_ref" / "libtmvref.so"
+REF_GENERIC_LIB = HERE / "_ref" / "libtmvref_generic.so"
+
+i64 = C.c_int64
+vp = C.c_void_p
+dbl = C.c_double
+
+SINGULAR = 1
+
+
+class OracleSingular(RuntimeError):
+    pass
+
+
+def build_port() -> Path:
+    subprocess.run(["make", "-s", "-C", str(HERE), "port"], check=True)
+    return PORT_LIB
+
+
+def build_ref(reference: str = "/root/reference") -> Path | None:
+    if not Path(reference, "src", "TMV_LUDecompose.cpp").exists():
+        return None
+    subprocess.run(["make", "-s", "-j8", "-C", str(HERE), "ref", f"REF={reference}"], check=True)
+    return REF_LIB
+
+
+def _p(a: np.ndarray) -> vp:
+    return vp(a.ctypes.data)
+
+
+def _strides(a: np.ndarray):
+    it = a.itemsize
+    if a.ndim == 1:
+        return a.strides[0] // it, a.size * (a.strides[0] // it)
+    return a.strides[0] // it, a.strides[1] // it
+
+
+class _Backend:
+    prefix = ""
+
+    def __init__(self, path: Path):
+        if not path.exists():
+            raise FileNotFoundError(f"{path} not built")
+        self.lib = C.CDLL(str(path))
+        self.path = path
+
+    def _f(self, name, res, args):
+        f = getattr(self.lib, self.prefix + name)
+        f.restype = res
+        f.argtypes = args
+        return f
+
+    # numpy-level interface -------------------------------------------------
+    def multmm(self, add: bool, alpha: float, A: np.ndarray, B: np.ndarray, Cm: np.ndarray) -> None:
+        m, k = A.shape
+        n = B.shape[1]
+        f = self._f("multmm", C.c_int, [C.c_int, dbl, i64, i64, i64, vp, i64, i64, vp, i64, i64,
+                                        vp, i64, i64])
+        rc = f(int(add), alpha, m, n, k, _p(A), *_strides(A), _p(B), *_strides(B), _p(Cm),
+               *_strides(Cm))
+        if rc:
+            raise RuntimeError(f"multmm rc={rc}")
+
+    def lu_decompose(self, A: np.ndarray) -> np.ndarray:
+        """In place; returns P (int64)."""
+        n = A.shape[0]
+        P = np.zeros(min(A.shape), dtype=np.int64)
+        rc = self._lu(A, P)
+        if rc:
+            raise RuntimeError(f"lu rc={rc}")
+        return P
+
+    def ldiveq(self, LU: np.ndarray, P: np.ndarray, B: np.ndarray) -> None:
+        n = LU.shape[0]
+        Bv = B.reshape(n, -1) if B.ndim == 1 else B
+        f = self._f("lu_ldiveq", C.c_int, [i64, vp, i64, vp, i64, vp, i64, i64])
+        rc = f(n, _p(LU), LU.strides[1] // 8, _p(P), Bv.shape[1], _p(Bv), *_strides(Bv))
+        if rc == SINGULAR:
+            raise OracleSingular("singular")
+        if rc:
+            raise RuntimeError(f"ldiveq rc={rc}")
+
+    def rdiveq(self, LU: np.ndarray, P: np.ndarray, B: np.ndarray) -> None:
+        n = LU.shape[0]
+        Bv = B.reshape(1, n) if B.ndim == 1 else B
+        f = self._f("lu_rdiveq", C.c_int, [i64, vp, i64, vp, i64, vp, i64, i64])
+        rc = f(n, _p(LU), LU.strides[1] // 8, _p(P), Bv.shape[0], _p(Bv), *_strides(Bv))
+        if rc == SINGULAR:
+            raise OracleSingular("singular")
+        if rc:
+            raise RuntimeError(f"rdiveq rc={rc}")
+
+    def divide(self, A: np.ndarray, B: np.ndarray):
+        """X = B / A with A column-major; returns (X, LU, P)."""
+        n = A.shape[0]
+        A = np.asfortranarray(A)
+        B2 = np.asfortranarray(B.reshape(n, -1))
+        X = np.zeros_like(B2, order="F")
+        LU = np.zeros((n, n), order="F")
+        P = np.zeros(n, dtype=np.int64)
+        rc = self._divide(n, A, B2, X, LU, P)
+        if rc == SINGULAR:
+            raise OracleSingular("singular")
+        if rc:
+            raise RuntimeError(f"divide rc={rc}")
+        return X, LU, P
+
+    def batched_divide(self, n, nrhs, a_off, b_off, A, B) -> np.ndarray:
+        cnt = len(n)
+        st = np.zeros(cnt, dtype=np.int32)
+        f = self._f("batched_divide", C.c_int, [i64, vp, vp, vp, vp, vp, vp, vp])
+        n = np.ascontiguousarray(n, dtype=np.int64)
+        nrhs = np.ascontiguousarray(nrhs, dtype=np.int64)
+        a_off = np.ascontiguousarray(a_off, dtype=np.int64)
+        b_off = np.ascontiguousarray(b_off, dtype=np.int64)
+        f(cnt, _p(n), _p(nrhs), _p(a_off), _p(b_off), _p(A), _p(B), _p(st))
+        return st
+
+    def set_threads(self, t: int) -> None:
+        self._f("set_threads", None, [C.c_int])(t)
+
+    def max_threads(self) -> int:
+        return int(self._f("max_threads", C.c_int, [])())
+
+
+class Port(_Backend):
+    prefix = "oracle_"
+
+    def _lu(self, A, P):
+        f = self._f("lu_decompose", C.c_int, [i64, i64, vp, i64, i64, vp])
+        return f(A.shape[0], A.shape[1], _p(A), *_strides(A), _p(P))
+
+    def _divide(self, n, A, B, X, LU, P):
+        f = self._f("divide", C.c_int, [i64, vp, i64, vp, vp, vp, vp])
+        return f(n, _p(A), B.shape[1], _p(B), _p(X), _p(LU), _p(P))
+
+    def det(self, LU: np.ndarray, P: np.ndarray):
+        d, ld, s = dbl(), dbl(), dbl()
+        f = self._f("lu_det", None, [i64, vp, i64, vp, C.POINTER(dbl), C.POINTER(dbl),
+                                     C.POINTER(dbl)])
+        f(LU.shape[0], _p(LU), LU.strides[1] // 8, _p(P), C.byref(d), C.byref(ld), C.byref(s))
+        return d.value, ld.value, s.value
+
+
+class Ref(_Backend):
+    prefix = "tmvref_"
+
+    def _lu(self, A, P):
+        if A.shape[0] != A.shape[1]:
+            raise ValueError("ref binding factors square matrices")
+        f = self._f("lu_decompose", C.c_int, [i64, vp, i64, i64, vp])
+        return f(A.shape[0], _p(A), *_strides(A), _p(P))
+
+    def _divide(self, n, A, B, X, LU, P):
+        f = self._f("divide", C.c_int, [i64, C.c_int, vp, i64, vp, vp, vp, vp])
+        return f(n, 0, _p(A), B.shape[1], _p(B), _p(X), _p(LU), _p(P))
+
+    def rdivide(self, A: np.ndarray, W: np.ndarray) -> np.ndarray:
+        """X = W % A (X A = W), W nrows x n."""
+        n = A.shape[0]
+        A = np.asfortranarray(A)
+        W = np.asfortranarray(W)
+        X = np.zeros_like(W, order="F")
+        f = self._f("rdivide", C.c_int, [i64, vp, i64, vp, vp])
+        rc = f(n, _p(A), W.shape[0], _p(W), _p(X))
+        if rc:
+            raise RuntimeError(f"rdivide rc={rc}")
+        return X
+
+    def det_of(self, A: np.ndarray):
+        d, ld, s = dbl(), dbl(), dbl()
+        A = np.asfortranarray(A)
+        f = self._f("det", C.c_int, [i64, vp, C.POINTER(dbl), C.POINTER(dbl), C.POINTER(dbl)])
+        rc = f(A.shape[0], _p(A), C.byref(d), C.byref(ld), C.byref(s))
+        if rc:
+            raise RuntimeError(f"det rc={rc}")
+        return d.value, ld.value, s.value
+
+
+_port = None
+
+
+def port() -> Port:
+    global _port
+    if _port is None:
+        if not PORT_LIB.exists():
+            build_port()
+        _port = Port(PORT_LIB)
+    return _port
+
+
+def ref(generic: bool = False) -> Ref:
+    return Ref(REF_GENERIC_LIB if generic else REF_LIB)
+
+
+def ref_available() -> bool:
+    return REF_LIB.exists()

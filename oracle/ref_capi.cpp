@@ -1,0 +1,189 @@
+// ref_capi.cpp -- extern "C" binding of TMV 0.76's own public surface.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is compiled together with the TMV
+// reference sources into oracle/_ref/libtmvref.so by oracle/Makefile, and is
+// loaded only by the fixture generator (tests/golden/make_golden.py) and by the
+// CPU tests that pin the C restatement (oracle/tmv_oracle.c) against TMV itself.
+// Nothing in the product links it.
+//
+// Every entry point reaches TMV through the calls a TMV user (or TMV's own
+// LUDiv) makes:
+//   tmvref_multmm        C = alpha*A*B / C += alpha*A*B  (tmv::Matrix expression
+//                        surface -> ProdMM::assignToM -> MultMM<add>,
+//                        include/tmv/TMV_MatrixArith.h:701-810, src/TMV_MultMM.cpp:405)
+//   tmvref_lu_decompose  LU_Decompose(MatrixView<T>, ptrdiff_t*) (src/TMV_LUDecompose.cpp:514)
+//   tmvref_lu_ldiveq     LU_LDivEq (src/TMV_LUDiv.cpp:186)
+//   tmvref_lu_rdiveq     LU_RDivEq (src/TMV_LUDiv.cpp:370)
+//   tmvref_divide        m.divideUsing(tmv::LU); m.saveDiv(); X = B/m (src/TMV_LUD.cpp:74-120)
+//   tmvref_rdivide       X = B % m (LUDiv::doRDiv, src/TMV_LUD.cpp:122-130)
+//   tmvref_det           m.det(), m.logDet(&s) (src/TMV_LUD.cpp:132-190)
+//   tmvref_batched_divide  one B_i/A_i per system, OpenMP over systems.
+//
+// Status: 0 ok, 1 tmv::Singular thrown, 2 other tmv::Error, 3 other exception.
+
+#include "TMV.h"
+#include "TMV_LUDiv.h"
+#include <omp.h>
+#include <cstring>
+
+namespace {
+
+template <class F>
+int guarded(F f)
+{
+    try {
+        f();
+    } catch (tmv::Singular&) {
+        return 1;
+    } catch (tmv::Error&) {
+        return 2;
+    } catch (...) {
+        return 3;
+    }
+    return 0;
+}
+
+tmv::StorageType stor_of(int rowmajor)
+{ return rowmajor ? tmv::RowMajor : tmv::ColMajor; }
+
+}  // namespace
+
+extern "C" {
+
+int tmvref_version(void) { return 76; }
+
+void tmvref_set_threads(int n) { if (n > 0) omp_set_num_threads(n); }
+
+int tmvref_max_threads(void) { return omp_get_max_threads(); }
+
+int tmvref_multmm(int add, double alpha, ptrdiff_t m, ptrdiff_t n, ptrdiff_t k,
+                  const double* A, ptrdiff_t sAi, ptrdiff_t sAj,
+                  const double* B, ptrdiff_t sBi, ptrdiff_t sBj,
+                  double* C, ptrdiff_t sCi, ptrdiff_t sCj)
+{
+    return guarded([&] {
+        tmv::ConstMatrixView<double> Av = tmv::MatrixViewOf(A, m, k, sAi, sAj);
+        tmv::ConstMatrixView<double> Bv = tmv::MatrixViewOf(B, k, n, sBi, sBj);
+        tmv::MatrixView<double> Cv = tmv::MatrixViewOf(C, m, n, sCi, sCj);
+        if (add) Cv += alpha * Av * Bv;
+        else Cv = alpha * Av * Bv;
+    });
+}
+
+int tmvref_lu_decompose(ptrdiff_t n, double* A, ptrdiff_t sAi, ptrdiff_t sAj,
+                        ptrdiff_t* P)
+{
+    return guarded([&] {
+        tmv::MatrixView<double> Av = tmv::MatrixViewOf(A, n, n, sAi, sAj);
+        tmv::LU_Decompose(Av, P);
+    });
+}
+
+int tmvref_lu_ldiveq(ptrdiff_t n, const double* LU, ptrdiff_t lda,
+                     const ptrdiff_t* P, ptrdiff_t nrhs,
+                     double* B, ptrdiff_t sBi, ptrdiff_t sBj)
+{
+    return guarded([&] {
+        tmv::ConstMatrixView<double> LUv = tmv::MatrixViewOf(LU, n, n, 1, lda);
+        tmv::MatrixView<double> Bv = tmv::MatrixViewOf(B, n, nrhs, sBi, sBj);
+        tmv::LU_LDivEq(LUv, P, Bv);
+    });
+}
+
+int tmvref_lu_rdiveq(ptrdiff_t n, const double* LU, ptrdiff_t lda,
+                     const ptrdiff_t* P, ptrdiff_t nrows,
+                     double* B, ptrdiff_t sBi, ptrdiff_t sBj)
+{
+    return guarded([&] {
+        tmv::ConstMatrixView<double> LUv = tmv::MatrixViewOf(LU, n, n, 1, lda);
+        tmv::MatrixView<double> Bv = tmv::MatrixViewOf(B, nrows, n, sBi, sBj);
+        tmv::LU_RDivEq(LUv, P, Bv);
+    });
+}
+
+// A: n x n, storage rowmajor?RM:CM (dense).  B, X: n x nrhs column-major.
+// LU_out (n*n, the stored factor in LUDiv's own storage order, i.e. the
+// factor of A for column-major input and of A^T for row-major input) and
+// P_out (n) may be null.
+int tmvref_divide(ptrdiff_t n, int rowmajor, const double* A, ptrdiff_t nrhs,
+                  const double* B, double* X, double* LU_out, ptrdiff_t* P_out)
+{
+    return guarded([&] {
+        if (rowmajor) {
+            tmv::Matrix<double, tmv::RowMajor> m(
+                tmv::MatrixViewOf(A, n, n, tmv::RowMajor));
+            m.divideUsing(tmv::LU);
+            m.saveDiv();
+            m.setDiv();
+            tmv::Matrix<double, tmv::ColMajor> Bm(
+                tmv::MatrixViewOf(B, n, nrhs, tmv::ColMajor));
+            tmv::MatrixViewOf(X, n, nrhs, tmv::ColMajor) = Bm / m;
+            if (LU_out) tmv::MatrixViewOf(LU_out, n, n, tmv::ColMajor) = m.lud().getLU();
+            if (P_out) std::memcpy(P_out, m.lud().getP().getValues(), n * sizeof(ptrdiff_t));
+        } else {
+            tmv::Matrix<double, tmv::ColMajor> m(
+                tmv::MatrixViewOf(A, n, n, tmv::ColMajor));
+            m.divideUsing(tmv::LU);
+            m.saveDiv();
+            m.setDiv();
+            tmv::Matrix<double, tmv::ColMajor> Bm(
+                tmv::MatrixViewOf(B, n, nrhs, tmv::ColMajor));
+            tmv::MatrixViewOf(X, n, nrhs, tmv::ColMajor) = Bm / m;
+            if (LU_out) tmv::MatrixViewOf(LU_out, n, n, tmv::ColMajor) = m.lud().getLU();
+            if (P_out) std::memcpy(P_out, m.lud().getP().getValues(), n * sizeof(ptrdiff_t));
+        }
+    });
+}
+
+// X = W % A  (X A = W): W, X are nrows x n column-major, A n x n column-major.
+int tmvref_rdivide(ptrdiff_t n, const double* A, ptrdiff_t nrows,
+                   const double* W, double* X)
+{
+    return guarded([&] {
+        tmv::Matrix<double, tmv::ColMajor> m(
+            tmv::MatrixViewOf(A, n, n, tmv::ColMajor));
+        m.divideUsing(tmv::LU);
+        m.saveDiv();
+        tmv::Matrix<double, tmv::ColMajor> Wm(
+            tmv::MatrixViewOf(W, nrows, n, tmv::ColMajor));
+        tmv::MatrixViewOf(X, nrows, n, tmv::ColMajor) = Wm % m;
+    });
+}
+
+int tmvref_det(ptrdiff_t n, const double* A, double* det, double* logdet,
+               double* sign)
+{
+    return guarded([&] {
+        tmv::Matrix<double, tmv::ColMajor> m(
+            tmv::MatrixViewOf(A, n, n, tmv::ColMajor));
+        m.divideUsing(tmv::LU);
+        m.saveDiv();
+        *det = m.det();
+        double s = 0;
+        *logdet = m.logDet(&s);
+        *sign = s;
+    });
+}
+
+// Ragged batch: system i has order n[i], nrhs[i] right-hand sides, A_i at
+// A + a_off[i] (column-major n_i x n_i), B_i at B + b_off[i] (column-major
+// n_i x nrhs_i).  X_i = B_i / A_i is written over B_i.  status[i] per system.
+int tmvref_batched_divide(ptrdiff_t count, const ptrdiff_t* n, const ptrdiff_t* nrhs,
+                          const ptrdiff_t* a_off, const ptrdiff_t* b_off,
+                          const double* A, double* B, int* status)
+{
+#pragma omp parallel for schedule(dynamic, 16)
+    for (ptrdiff_t i = 0; i < count; ++i) {
+        const ptrdiff_t ni = n[i], ri = nrhs[i];
+        status[i] = guarded([&] {
+            tmv::Matrix<double, tmv::ColMajor> m(
+                tmv::MatrixViewOf(A + a_off[i], ni, ni, tmv::ColMajor));
+            tmv::MatrixView<double> Bv =
+                tmv::MatrixViewOf(B + b_off[i], ni, ri, tmv::ColMajor);
+            Bv /= m;
+        });
+    }
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,125 @@
+"""ctypes binding of libtmvg.so (the C ABI declared in include/tmvg.h).
+
+The library is built in-tree by tmv_gb300/build.py (or __graft_entry__.build()).
+There is no fallback: if the shared library is missing, importing the binding
+raises, so nothing silently runs on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "_build" / "libtmvg.so"
+
+i64 = C.c_int64
+dbl = C.c_double
+vp = C.c_void_p
+
+STATUS = {
+    0: "ok", 1: "singular", 2: "not converged", 3: "bad argument", 4: "out of memory",
+    5: "device wait timed out", 6: "cuda error", 7: "no cuda device", 8: "unsupported",
+}
+
+
+class TmvgError(RuntimeError):
+    """Raised for a non-OK tmvg_status; .status holds the code."""
+
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class SingularError(TmvgError):
+    """A zero U(j,j) was met while solving (TMV's SingularUpperTriMatrix)."""
+
+
+# name -> (restype, argtypes)
+_SIGS = {
+    "tmvg_version": (C.c_int, []),
+    "tmvg_status_string": (C.c_char_p, [C.c_int]),
+    "tmvg_create": (C.c_int, [C.POINTER(vp), C.c_int]),
+    "tmvg_destroy": (C.c_int, [vp]),
+    "tmvg_set_stream": (C.c_int, [vp, vp]),
+    "tmvg_synchronize": (C.c_int, [vp]),
+    "tmvg_last_error": (C.c_char_p, [vp]),
+    "tmvg_launch_count": (i64, [vp]),
+    "tmvg_multmm_f64": (C.c_int, [vp, C.c_int, dbl, i64, i64, i64, vp, i64, i64, vp, i64, i64,
+                                  vp, i64, i64]),
+    "tmvg_multmm_f64_host": (C.c_int, [vp, C.c_int, dbl, i64, i64, i64, vp, i64, i64, vp, i64,
+                                       i64, vp, i64, i64]),
+    "tmvg_lu_decompose_f64": (C.c_int, [vp, i64, vp, i64, vp]),
+    "tmvg_lu_decompose_f64_host": (C.c_int, [vp, i64, vp, i64, i64, vp]),
+    "tmvg_lu_ldiveq_f64": (C.c_int, [vp, i64, vp, i64, vp, i64, vp, i64]),
+    "tmvg_lu_rdiveq_f64": (C.c_int, [vp, i64, vp, i64, vp, i64, vp, i64]),
+    "tmvg_lu_ldiveq_f64_host": (C.c_int, [vp, i64, vp, i64, vp, i64, vp, i64, i64]),
+    "tmvg_lu_rdiveq_f64_host": (C.c_int, [vp, i64, vp, i64, vp, i64, vp, i64, i64]),
+    "tmvg_divide_f64": (C.c_int, [vp, i64, vp, i64, i64, vp, i64, vp, i64, vp, vp]),
+    "tmvg_divide_f64_host": (C.c_int, [vp, i64, vp, i64, vp, vp, vp, vp]),
+    "tmvg_lu_det_f64": (C.c_int, [vp, i64, vp, i64, vp, C.POINTER(dbl), C.POINTER(dbl),
+                                  C.POINTER(dbl)]),
+}
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Load libtmvg.so once and attach the signatures of every entry point."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise ImportError(
+            f"{LIB_PATH} is missing: build the CUDA library first "
+            "(python -c 'import __graft_entry__ as g; g.build()')")
+    lib = C.CDLL(str(LIB_PATH))
+    for name, (res, args) in _SIGS.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def declared_symbols() -> list[str]:
+    return list(_SIGS)
+
+
+class Handle:
+    """Owns one tmvg context; check() turns a status into an exception."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = vp()
+        st = self.lib.tmvg_create(C.byref(h), device)
+        if st != 0:
+            raise TmvgError(st, "tmvg_create failed")
+        self.h = h
+        self.device = device
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.tmvg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr: int) -> None:
+        self.check(self.lib.tmvg_set_stream(self.h, vp(stream_ptr)))
+
+    def check(self, st: int, what: str = "") -> None:
+        if st == 0:
+            return
+        msg = (self.lib.tmvg_last_error(self.h) or b"").decode() or what
+        if st == 1:
+            raise SingularError(st, msg)
+        raise TmvgError(st, msg)
+
+    def launches(self) -> int:
+        return int(self.lib.tmvg_launch_count(self.h))
+
+    def call(self, name: str, *args) -> int:
+        return getattr(self.lib, name)(self.h, *args)

@@ -1,0 +1,517 @@
+// capi.cu -- extern "C" entry points (include/tmvg.h) and context plumbing.
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "lu.cuh"
+
+namespace tmvg {
+
+tmvg_status set_error(Context* c, tmvg_status s, const std::string& msg)
+{
+    if (c) c->last_error = msg;
+    return s;
+}
+
+tmvg_status check_cuda(Context* c, cudaError_t e, const char* what)
+{
+    if (e == cudaSuccess) return TMVG_OK;
+    if (e == cudaErrorMemoryAllocation)
+        return set_error(c, TMVG_OOM, std::string(what) + ": " + cudaGetErrorString(e));
+    return set_error(c, TMVG_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+void* workspace(Context* c, size_t bytes)
+{
+    if (bytes <= c->work_bytes) return c->work;
+    if (c->work) {
+        cudaStreamSynchronize(c->stream);
+        cudaFree(c->work);
+        c->work = nullptr;
+        c->work_bytes = 0;
+    }
+    size_t want = bytes + bytes / 4 + 4096;
+    if (cudaMalloc(&c->work, want) != cudaSuccess) {
+        cudaGetLastError();
+        c->work = nullptr;
+        set_error(c, TMVG_OOM, "workspace allocation failed");
+        return nullptr;
+    }
+    c->work_bytes = want;
+    return c->work;
+}
+
+tmvg_status collect_device_error(Context* c, const char* what)
+{
+    tmvg_status st = check_cuda(
+        c, cudaMemcpyAsync(c->hflags, c->dflags, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream),
+        what);
+    if (st) return st;
+    st = check_cuda(c, cudaStreamSynchronize(c->stream), what);
+    if (st) return st;
+    const int code = c->hflags[0];
+    if (code == kDevOk) return TMVG_OK;
+    cudaMemsetAsync(c->dflags, 0, 2 * sizeof(int), c->stream);
+    cudaStreamSynchronize(c->stream);
+    if (code == kDevSingular)
+        return set_error(c, TMVG_SINGULAR, std::string(what) + ": singular triangular factor");
+    if (code == kDevTimeout)
+        return set_error(c, TMVG_TIMEOUT, std::string(what) + ": a device-side wait timed out");
+    return set_error(c, TMVG_CUDA_ERROR, std::string(what) + ": device error word set");
+}
+
+// RAII stream-ordered device buffer for the host-pointer entry points.
+struct DevBuf {
+    Context* c;
+    void* p = nullptr;
+    DevBuf(Context* ctx, size_t bytes) : c(ctx)
+    {
+        if (bytes == 0) bytes = 16;
+        if (cudaMallocAsync(&p, bytes, c->stream) != cudaSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+        }
+    }
+    ~DevBuf()
+    {
+        if (p) cudaFreeAsync(p, c->stream);
+    }
+    template <typename T>
+    T* as() { return static_cast<T*>(p); }
+};
+
+// 32x32 tiled transpose: out (cols x rows, column-major) = in^T where in is
+// rows x cols column-major.
+template <typename T>
+__global__ void transpose_kernel(int64_t rows, int64_t cols, const T* __restrict__ in,
+                                 int64_t ldi, T* __restrict__ out, int64_t ldo)
+{
+    __shared__ T tile[32][33];
+    const int64_t i0 = (int64_t)blockIdx.x * 32, j0 = (int64_t)blockIdx.y * 32;
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int64_t i = i0 + threadIdx.x, j = j0 + r;
+        if (i < rows && j < cols) tile[r][threadIdx.x] = in[i + j * ldi];
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int64_t j = j0 + threadIdx.x, i = i0 + r;
+        if (i < rows && j < cols) out[j + i * ldo] = tile[threadIdx.x][r];
+    }
+}
+
+template <typename T>
+static tmvg_status transpose(Context* c, int64_t rows, int64_t cols, const T* in, int64_t ldi,
+                             T* out, int64_t ldo)
+{
+    if (rows <= 0 || cols <= 0) return TMVG_OK;
+    dim3 grid((unsigned)ceil_div(rows, 32), (unsigned)ceil_div(cols, 32));
+    transpose_kernel<T><<<grid, dim3(32, 8), 0, c->stream>>>(rows, cols, in, ldi, out, ldo);
+    ++c->launches;
+    return check_cuda(c, cudaGetLastError(), "transpose launch");
+}
+
+// Copy a strided host matrix (rows x cols, element (i,j) at p[i*si + j*sj])
+// into a dense column-major device buffer, and back.  Column- and row-major
+// host layouts move with one 2-D copy; anything else is packed on the host.
+static tmvg_status h2d_matrix(Context* c, double* dst, const double* src, int64_t rows,
+                              int64_t cols, int64_t si, int64_t sj, double* tmp_dev)
+{
+    if (rows <= 0 || cols <= 0) return TMVG_OK;
+    if (si == 1 || cols == 1) {
+        const int64_t ld = cols == 1 ? rows : sj;
+        return check_cuda(c,
+                          cudaMemcpy2DAsync(dst, rows * sizeof(double), src, ld * sizeof(double),
+                                            rows * sizeof(double), cols, cudaMemcpyHostToDevice,
+                                            c->stream),
+                          "h2d");
+    }
+    if (sj == 1 || rows == 1) {
+        const int64_t ld = rows == 1 ? cols : si;
+        tmvg_status st = check_cuda(
+            c,
+            cudaMemcpy2DAsync(tmp_dev, cols * sizeof(double), src, ld * sizeof(double),
+                              cols * sizeof(double), rows, cudaMemcpyHostToDevice, c->stream),
+            "h2d");
+        if (st) return st;
+        return transpose<double>(c, cols, rows, tmp_dev, cols, dst, rows);
+    }
+    return set_error(c, TMVG_BAD_ARG, "host matrix must be column- or row-major");
+}
+
+static tmvg_status d2h_matrix(Context* c, double* dst, const double* src, int64_t rows,
+                              int64_t cols, int64_t si, int64_t sj, double* tmp_dev)
+{
+    if (rows <= 0 || cols <= 0) return TMVG_OK;
+    if (si == 1 || cols == 1) {
+        const int64_t ld = cols == 1 ? rows : sj;
+        return check_cuda(c,
+                          cudaMemcpy2DAsync(dst, ld * sizeof(double), src, rows * sizeof(double),
+                                            rows * sizeof(double), cols, cudaMemcpyDeviceToHost,
+                                            c->stream),
+                          "d2h");
+    }
+    if (sj == 1 || rows == 1) {
+        const int64_t ld = rows == 1 ? cols : si;
+        tmvg_status st = transpose<double>(c, rows, cols, src, rows, tmp_dev, cols);
+        if (st) return st;
+        return check_cuda(c,
+                          cudaMemcpy2DAsync(dst, ld * sizeof(double), tmp_dev, cols * sizeof(double),
+                                            cols * sizeof(double), rows, cudaMemcpyDeviceToHost,
+                                            c->stream),
+                          "d2h");
+    }
+    return set_error(c, TMVG_BAD_ARG, "host matrix must be column- or row-major");
+}
+
+}  // namespace tmvg
+
+using namespace tmvg;
+
+#define CTX_OR_BAIL(h)                                     \
+    Context* c = reinterpret_cast<Context*>(h);            \
+    if (!c) return TMVG_BAD_ARG;                           \
+    c->last_error.clear();                                 \
+    if (cudaSetDevice(c->device) != cudaSuccess)           \
+        return set_error(c, TMVG_CUDA_ERROR, "cudaSetDevice failed");
+
+extern "C" {
+
+int tmvg_version(void) { return 1; }
+
+const char* tmvg_status_string(tmvg_status s)
+{
+    switch (s) {
+        case TMVG_OK: return "ok";
+        case TMVG_SINGULAR: return "singular";
+        case TMVG_NOT_CONVERGED: return "not converged";
+        case TMVG_BAD_ARG: return "bad argument";
+        case TMVG_OOM: return "out of memory";
+        case TMVG_TIMEOUT: return "device wait timed out";
+        case TMVG_CUDA_ERROR: return "cuda error";
+        case TMVG_NO_DEVICE: return "no cuda device";
+        case TMVG_UNSUPPORTED: return "unsupported";
+    }
+    return "unknown";
+}
+
+tmvg_status tmvg_create(tmvg_handle* h, int device)
+{
+    if (!h) return TMVG_BAD_ARG;
+    *h = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) {
+        cudaGetLastError();
+        return TMVG_NO_DEVICE;
+    }
+    if (device < 0 || device >= count) return TMVG_BAD_ARG;
+    Context* c = new (std::nothrow) Context();
+    if (!c) return TMVG_OOM;
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+        cudaMalloc(&c->dflags, 64 * sizeof(int)) != cudaSuccess ||
+        cudaMallocHost(&c->hflags, 64 * sizeof(int)) != cudaSuccess ||
+        cudaMemset(c->dflags, 0, 64 * sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        if (c->dflags) cudaFree(c->dflags);
+        if (c->hflags) cudaFreeHost(c->hflags);
+        delete c;
+        return TMVG_CUDA_ERROR;
+    }
+    c->dbar = reinterpret_cast<unsigned*>(c->dflags + 16);
+    *h = reinterpret_cast<tmvg_handle>(c);
+    return TMVG_OK;
+}
+
+tmvg_status tmvg_destroy(tmvg_handle h)
+{
+    Context* c = reinterpret_cast<Context*>(h);
+    if (!c) return TMVG_OK;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    if (c->work) cudaFree(c->work);
+    if (c->dflags) cudaFree(c->dflags);
+    if (c->hflags) cudaFreeHost(c->hflags);
+    delete c;
+    return TMVG_OK;
+}
+
+tmvg_status tmvg_set_stream(tmvg_handle h, void* stream)
+{
+    CTX_OR_BAIL(h);
+    c->stream = reinterpret_cast<cudaStream_t>(stream);
+    return TMVG_OK;
+}
+
+tmvg_status tmvg_synchronize(tmvg_handle h)
+{
+    CTX_OR_BAIL(h);
+    return check_cuda(c, cudaStreamSynchronize(c->stream), "synchronize");
+}
+
+const char* tmvg_last_error(tmvg_handle h)
+{
+    Context* c = reinterpret_cast<Context*>(h);
+    return c ? c->last_error.c_str() : "";
+}
+
+int64_t tmvg_launch_count(tmvg_handle h)
+{
+    Context* c = reinterpret_cast<Context*>(h);
+    return c ? c->launches : 0;
+}
+
+tmvg_status tmvg_multmm_f64(tmvg_handle h, int add, double alpha, int64_t m, int64_t n, int64_t k,
+                            const double* A, int64_t sAi, int64_t sAj, const double* B,
+                            int64_t sBi, int64_t sBj, double* C, int64_t sCi, int64_t sCj)
+{
+    CTX_OR_BAIL(h);
+    return gemm<double>(c, m, n, k, alpha, Mat<const double>{A, sAi, sAj},
+                        Mat<const double>{B, sBi, sBj}, add ? 1.0 : 0.0, Mat<double>{C, sCi, sCj});
+}
+
+tmvg_status tmvg_multmm_f64_host(tmvg_handle h, int add, double alpha, int64_t m, int64_t n,
+                                 int64_t k, const double* A, int64_t sAi, int64_t sAj,
+                                 const double* B, int64_t sBi, int64_t sBj, double* C,
+                                 int64_t sCi, int64_t sCj)
+{
+    CTX_OR_BAIL(h);
+    if (m < 0 || n < 0 || k < 0) return set_error(c, TMVG_BAD_ARG, "multmm: negative size");
+    if (m == 0 || n == 0) return TMVG_OK;
+    DevBuf dA(c, sizeof(double) * m * k), dB(c, sizeof(double) * k * n),
+        dC(c, sizeof(double) * m * n),
+        tmp(c, sizeof(double) * std::max(std::max(m * k, k * n), m * n));
+    if (!dA.p || !dB.p || !dC.p || !tmp.p) return set_error(c, TMVG_OOM, "multmm: device buffers");
+    tmvg_status st = h2d_matrix(c, dA.as<double>(), A, m, k, sAi, sAj, tmp.as<double>());
+    if (!st) st = h2d_matrix(c, dB.as<double>(), B, k, n, sBi, sBj, tmp.as<double>());
+    if (!st && add) st = h2d_matrix(c, dC.as<double>(), C, m, n, sCi, sCj, tmp.as<double>());
+    if (!st)
+        st = gemm<double>(c, m, n, k, alpha, Mat<const double>{dA.as<double>(), 1, m},
+                          Mat<const double>{dB.as<double>(), 1, k}, add ? 1.0 : 0.0,
+                          Mat<double>{dC.as<double>(), 1, m});
+    if (!st) st = d2h_matrix(c, C, dC.as<double>(), m, n, sCi, sCj, tmp.as<double>());
+    if (!st) st = check_cuda(c, cudaStreamSynchronize(c->stream), "multmm sync");
+    return st;
+}
+
+tmvg_status tmvg_lu_decompose_f64(tmvg_handle h, int64_t n, double* A, int64_t lda, int64_t* P)
+{
+    CTX_OR_BAIL(h);
+    return lu_factor<double>(c, n, A, lda, P);
+}
+
+tmvg_status tmvg_lu_decompose_f64_host(tmvg_handle h, int64_t n, double* A, int64_t sAi,
+                                       int64_t sAj, int64_t* P)
+{
+    CTX_OR_BAIL(h);
+    if (n < 0) return set_error(c, TMVG_BAD_ARG, "lu: negative n");
+    if (n == 0) return TMVG_OK;
+    DevBuf dA(c, sizeof(double) * n * n), tmp(c, sizeof(double) * n * n),
+        dP(c, sizeof(int64_t) * n);
+    if (!dA.p || !tmp.p || !dP.p) return set_error(c, TMVG_OOM, "lu: device buffers");
+    tmvg_status st = h2d_matrix(c, dA.as<double>(), A, n, n, sAi, sAj, tmp.as<double>());
+    if (!st) st = lu_factor<double>(c, n, dA.as<double>(), n, dP.as<int64_t>());
+    if (!st) st = d2h_matrix(c, A, dA.as<double>(), n, n, sAi, sAj, tmp.as<double>());
+    if (!st)
+        st = check_cuda(c,
+                        cudaMemcpyAsync(P, dP.p, sizeof(int64_t) * n, cudaMemcpyDeviceToHost,
+                                        c->stream),
+                        "lu: pivots d2h");
+    if (!st) st = check_cuda(c, cudaStreamSynchronize(c->stream), "lu sync");
+    return st;
+}
+
+tmvg_status tmvg_lu_ldiveq_f64(tmvg_handle h, int64_t n, const double* LU, int64_t lda,
+                               const int64_t* P, int64_t nrhs, double* B, int64_t ldb)
+{
+    CTX_OR_BAIL(h);
+    if (n < 0 || nrhs < 0 || lda < std::max<int64_t>(n, 1) || ldb < std::max<int64_t>(n, 1))
+        return set_error(c, TMVG_BAD_ARG, "ldiveq: bad sizes");
+    return lu_ldiveq<double>(c, n, LU, lda, P, nrhs, B, 1, ldb);
+}
+
+tmvg_status tmvg_lu_rdiveq_f64(tmvg_handle h, int64_t n, const double* LU, int64_t lda,
+                               const int64_t* P, int64_t nrows, double* B, int64_t ldb)
+{
+    CTX_OR_BAIL(h);
+    if (n < 0 || nrows < 0 || lda < std::max<int64_t>(n, 1) || ldb < std::max<int64_t>(nrows, 1))
+        return set_error(c, TMVG_BAD_ARG, "rdiveq: bad sizes");
+    return lu_rdiveq<double>(c, n, LU, lda, P, nrows, B, 1, ldb);
+}
+
+static tmvg_status div_host(Context* c, bool right, int64_t n, const double* LU, int64_t lda,
+                            const int64_t* P, int64_t other, double* B, int64_t sBi, int64_t sBj)
+{
+    if (n < 0 || other < 0 || lda < std::max<int64_t>(n, 1))
+        return set_error(c, TMVG_BAD_ARG, "div: bad sizes");
+    if (n == 0 || other == 0) return TMVG_OK;
+    const int64_t rows = right ? other : n, cols = right ? n : other;
+    DevBuf dLU(c, sizeof(double) * n * n), dP(c, sizeof(int64_t) * n),
+        dB(c, sizeof(double) * rows * cols), tmp(c, sizeof(double) * rows * cols);
+    if (!dLU.p || !dP.p || !dB.p || !tmp.p) return set_error(c, TMVG_OOM, "div: device buffers");
+    tmvg_status st = check_cuda(
+        c,
+        cudaMemcpy2DAsync(dLU.p, n * sizeof(double), LU, lda * sizeof(double), n * sizeof(double),
+                          n, cudaMemcpyHostToDevice, c->stream),
+        "div: LU h2d");
+    if (!st)
+        st = check_cuda(c,
+                        cudaMemcpyAsync(dP.p, P, sizeof(int64_t) * n, cudaMemcpyHostToDevice,
+                                        c->stream),
+                        "div: P h2d");
+    if (!st) st = h2d_matrix(c, dB.as<double>(), B, rows, cols, sBi, sBj, tmp.as<double>());
+    if (!st)
+        st = right ? lu_rdiveq<double>(c, n, dLU.as<double>(), n, dP.as<int64_t>(), other,
+                                       dB.as<double>(), 1, rows)
+                   : lu_ldiveq<double>(c, n, dLU.as<double>(), n, dP.as<int64_t>(), other,
+                                       dB.as<double>(), 1, rows);
+    if (st == TMVG_OK || st == TMVG_SINGULAR) {
+        tmvg_status st2 = d2h_matrix(c, B, dB.as<double>(), rows, cols, sBi, sBj, tmp.as<double>());
+        if (!st2) st2 = check_cuda(c, cudaStreamSynchronize(c->stream), "div sync");
+        if (st2) return st2;
+    }
+    return st;
+}
+
+tmvg_status tmvg_lu_ldiveq_f64_host(tmvg_handle h, int64_t n, const double* LU, int64_t lda,
+                                    const int64_t* P, int64_t nrhs, double* B, int64_t sBi,
+                                    int64_t sBj)
+{
+    CTX_OR_BAIL(h);
+    return div_host(c, false, n, LU, lda, P, nrhs, B, sBi, sBj);
+}
+
+tmvg_status tmvg_lu_rdiveq_f64_host(tmvg_handle h, int64_t n, const double* LU, int64_t lda,
+                                    const int64_t* P, int64_t nrows, double* B, int64_t sBi,
+                                    int64_t sBj)
+{
+    CTX_OR_BAIL(h);
+    return div_host(c, true, n, LU, lda, P, nrows, B, sBi, sBj);
+}
+
+tmvg_status tmvg_divide_f64(tmvg_handle h, int64_t n, const double* A, int64_t lda, int64_t nrhs,
+                            const double* B, int64_t ldb, double* X, int64_t ldx, double* LU,
+                            int64_t* P)
+{
+    CTX_OR_BAIL(h);
+    if (n < 0 || nrhs < 0 || lda < std::max<int64_t>(n, 1) || ldb < std::max<int64_t>(n, 1) ||
+        ldx < std::max<int64_t>(n, 1))
+        return set_error(c, TMVG_BAD_ARG, "divide: bad sizes");
+    if (n == 0) return TMVG_OK;
+    tmvg_status st = check_cuda(
+        c,
+        cudaMemcpy2DAsync(LU, n * sizeof(double), A, lda * sizeof(double), n * sizeof(double), n,
+                          cudaMemcpyDeviceToDevice, c->stream),
+        "divide: copy A");
+    if (st) return st;
+    st = lu_factor<double>(c, n, LU, n, P);
+    if (st) return st;
+    if (nrhs == 0) return TMVG_OK;
+    st = check_cuda(c,
+                    cudaMemcpy2DAsync(X, ldx * sizeof(double), B, ldb * sizeof(double),
+                                      n * sizeof(double), nrhs, cudaMemcpyDeviceToDevice, c->stream),
+                    "divide: copy B");
+    if (st) return st;
+    return lu_ldiveq<double>(c, n, LU, n, P, nrhs, X, 1, ldx);
+}
+
+tmvg_status tmvg_divide_f64_host(tmvg_handle h, int64_t n, const double* A, int64_t nrhs,
+                                 const double* B, double* X, double* LU, int64_t* P)
+{
+    CTX_OR_BAIL(h);
+    if (n < 0 || nrhs < 0) return set_error(c, TMVG_BAD_ARG, "divide: bad sizes");
+    if (n == 0) return TMVG_OK;
+    DevBuf dA(c, sizeof(double) * n * n), dP(c, sizeof(int64_t) * n),
+        dX(c, sizeof(double) * n * std::max<int64_t>(nrhs, 1));
+    if (!dA.p || !dP.p || !dX.p) return set_error(c, TMVG_OOM, "divide: device buffers");
+    tmvg_status st = check_cuda(
+        c, cudaMemcpyAsync(dA.p, A, sizeof(double) * n * n, cudaMemcpyHostToDevice, c->stream),
+        "divide: A h2d");
+    if (!st && nrhs > 0)
+        st = check_cuda(c,
+                        cudaMemcpyAsync(dX.p, B, sizeof(double) * n * nrhs, cudaMemcpyHostToDevice,
+                                        c->stream),
+                        "divide: B h2d");
+    if (!st) st = lu_factor<double>(c, n, dA.as<double>(), n, dP.as<int64_t>());
+    if (!st && nrhs > 0)
+        st = lu_ldiveq<double>(c, n, dA.as<double>(), n, dP.as<int64_t>(), nrhs, dX.as<double>(),
+                               1, n);
+    if (st == TMVG_OK || st == TMVG_SINGULAR) {
+        tmvg_status st2 = TMVG_OK;
+        if (X && nrhs > 0)
+            st2 = check_cuda(c,
+                             cudaMemcpyAsync(X, dX.p, sizeof(double) * n * nrhs,
+                                             cudaMemcpyDeviceToHost, c->stream),
+                             "divide: X d2h");
+        if (!st2 && LU)
+            st2 = check_cuda(c,
+                             cudaMemcpyAsync(LU, dA.p, sizeof(double) * n * n,
+                                             cudaMemcpyDeviceToHost, c->stream),
+                             "divide: LU d2h");
+        if (!st2 && P)
+            st2 = check_cuda(c,
+                             cudaMemcpyAsync(P, dP.p, sizeof(int64_t) * n, cudaMemcpyDeviceToHost,
+                                             c->stream),
+                             "divide: P d2h");
+        if (!st2) st2 = check_cuda(c, cudaStreamSynchronize(c->stream), "divide sync");
+        if (st2) return st2;
+    }
+    return st;
+}
+
+tmvg_status tmvg_lu_det_f64(tmvg_handle h, int64_t n, const double* LU, int64_t lda,
+                            const int64_t* P, double* det, double* logdet, double* sign)
+{
+    // LUDiv::det / logDet (src/TMV_LUD.cpp:132-156) over GenDiagMatrix::logDet
+    // (src/TMV_DiagMatrix.cpp:59-85): log|U_jj| summed, a zero U_jj gives
+    // sign 0; det = sign * exp(logdet).  O(n) work: the diagonal and P are
+    // read back and reduced on the host in TMV's order.
+    CTX_OR_BAIL(h);
+    if (n < 0 || lda < std::max<int64_t>(n, 1)) return set_error(c, TMVG_BAD_ARG, "det: bad sizes");
+    double* diag = nullptr;
+    int64_t* hp = nullptr;
+    if (cudaMallocHost(&diag, sizeof(double) * std::max<int64_t>(n, 1)) != cudaSuccess ||
+        cudaMallocHost(&hp, sizeof(int64_t) * std::max<int64_t>(n, 1)) != cudaSuccess) {
+        cudaGetLastError();
+        if (diag) cudaFreeHost(diag);
+        return set_error(c, TMVG_OOM, "det: host buffers");
+    }
+    tmvg_status st = TMVG_OK;
+    if (n > 0) {
+        st = check_cuda(c,
+                        cudaMemcpy2DAsync(diag, sizeof(double), LU, (lda + 1) * sizeof(double),
+                                          sizeof(double), n, cudaMemcpyDeviceToHost, c->stream),
+                        "det: diag d2h");
+        if (!st)
+            st = check_cuda(c,
+                            cudaMemcpyAsync(hp, P, sizeof(int64_t) * n, cudaMemcpyDeviceToHost,
+                                            c->stream),
+                            "det: P d2h");
+        if (!st) st = check_cuda(c, cudaStreamSynchronize(c->stream), "det sync");
+    }
+    if (!st) {
+        double ld = 0.0, s = 1.0;
+        int pd = 1;
+        for (int64_t j = 0; j < n; ++j) {
+            const double u = diag[j];
+            if (u == 0.0) {
+                ld = std::log(0.0);
+                s = 0.0;
+            } else {
+                ld += std::log(std::fabs(u));
+                s *= u > 0 ? 1.0 : -1.0;
+            }
+            if (hp[j] != j) pd = -pd;
+        }
+        s *= (double)pd;
+        if (logdet) *logdet = ld;
+        if (sign) *sign = s;
+        if (det) *det = s == 0.0 ? 0.0 : s * std::exp(ld);
+    }
+    cudaFreeHost(diag);
+    cudaFreeHost(hp);
+    return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,131 @@
+// common.cuh -- shared device/host helpers of the sm_103a kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+
+#include "tmvg.h"
+
+namespace tmvg {
+
+// Number of SMs of the device a context runs on is read at creation; these
+// constants only size launch shapes.
+constexpr int kWarp = 32;
+
+// Bounded spin: a device-side wait that exceeds this many polls records an
+// error code and returns instead of hanging the GPU.  At roughly 100-200 ns a
+// poll (with __nanosleep backoff) this is a few seconds.
+constexpr unsigned kSpinLimit = 1u << 24;
+
+// Device error word codes (written by kernels, read by the host).
+enum DevError : int {
+    kDevOk = 0,
+    kDevTimeout = 1,
+    kDevSingular = 2,
+};
+
+// Per-context state shared by the C entry points.
+struct Context {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    // Grow-only device workspace (bytes) for temporaries of one call.
+    void* work = nullptr;
+    size_t work_bytes = 0;
+    // Device words: [0] error code, [1] aux (e.g. index where a wait gave up),
+    // [2..] barrier counters.
+    int* dflags = nullptr;
+    unsigned* dbar = nullptr;
+    int* hflags = nullptr;  // pinned mirror of dflags[0..2)
+    int64_t launches = 0;
+    std::string last_error;
+};
+
+tmvg_status set_error(Context* c, tmvg_status s, const std::string& msg);
+tmvg_status check_cuda(Context* c, cudaError_t e, const char* what);
+// Ensure at least `bytes` of workspace; returns nullptr on failure.
+void* workspace(Context* c, size_t bytes);
+// Reads and clears the device error word (synchronises the stream).
+tmvg_status collect_device_error(Context* c, const char* what);
+
+// ---------------------------------------------------------------------
+// Pivot search keys.
+//
+// TMV's maxAbsElement (src/TMV_Vector.cpp:474-503) scans from the first
+// element with `if (|v_i| > max)`, so ties keep the lowest index and a NaN is
+// chosen only when it is the first element.  A parallel reduction reproduces
+// this with a key per element, compared as (key desc, index asc):
+//   first element: |v|, or +inf when v is NaN ("maxabs" mode), or 0 when v is
+//                  NaN in the second column of TMV's two-column leaf
+//                  (src/TMV_LUDecompose.cpp:306-319), whose scan starts
+//                  from max = 0 ("r2" mode);
+//   other elements: |v|, or -1 when v is NaN.
+// ---------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ double pivot_key(T v, bool first, bool r2mode)
+{
+    double a = fabs((double)v);
+    if (a != a) return first ? (r2mode ? 0.0 : __longlong_as_double(0x7ff0000000000000LL)) : -1.0;
+    return a;
+}
+
+// (key, index) max-reduction with lowest index on ties.
+__device__ __forceinline__ void pivot_combine(double& k, long long& i, double k2, long long i2)
+{
+    if (k2 > k || (k2 == k && i2 < i)) {
+        k = k2;
+        i = i2;
+    }
+}
+
+__device__ __forceinline__ void warp_pivot_reduce(double& k, long long& i)
+{
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        double k2 = __shfl_xor_sync(0xffffffffu, k, off);
+        long long i2 = __shfl_xor_sync(0xffffffffu, i, off);
+        pivot_combine(k, i, k2, i2);
+    }
+}
+
+// TMV_Underflow for a real pivot magnitude (include/tmv/TMV_Base.h:692-696).
+__device__ __forceinline__ bool underflows(double a) { return a * a < 2.2250738585072014e-308; }
+__device__ __forceinline__ bool underflows_f(float a) { return a * a < 1.17549435e-38f; }
+
+// ---------------------------------------------------------------------
+// Grid barrier for cooperative launches (all CTAs co-resident).
+// `counter` is a monotonically increasing word zeroed before the launch; the
+// b-th barrier (0-based) completes when it reaches (b+1)*gridDim.x.  The wait
+// is bounded: on timeout it writes kDevTimeout into err[0] and returns false,
+// and the caller must leave the kernel.
+// ---------------------------------------------------------------------
+__device__ __forceinline__ bool grid_barrier(unsigned* counter, unsigned target, int* err)
+{
+    __syncthreads();
+    __shared__ int ok;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(counter, 1u);
+        unsigned spins = 0;
+        ok = 1;
+        while (true) {
+            unsigned v = *((volatile unsigned*)counter);
+            if (v >= target) break;
+            if (*((volatile int*)err) != kDevOk) { ok = 0; break; }
+            if (++spins > kSpinLimit) {
+                atomicExch(err, (int)kDevTimeout);
+                ok = 0;
+                break;
+            }
+            if (spins > 64) __nanosleep(64);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+}  // namespace tmvg

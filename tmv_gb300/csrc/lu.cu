@@ -1,0 +1,541 @@
+// lu.cu -- partial-pivoting LU factorisation and LU solves on sm_103a.
+//
+// Algorithm (right-looking, blocked; the reference is recursive,
+// src/TMV_LUDecompose.cpp:217-407, and produces the same factors up to the
+// rounding of the trailing updates):
+//   for each panel of kPanel columns starting at k:
+//     1. lu_panel_kernel: factor A[k:n, k:k+nb] column by column with TMV's
+//        pivot rule; the panel lives in the shared memory of up to one CTA
+//        per SM, one bounded grid barrier per column;
+//     2. laswp_kernel: apply the panel's interchanges to the other columns
+//        (TMV: A1.permuteRows(P,0,N1) and A0.permuteRows(P,N1,R));
+//     3. tri_diag_kernel: U12 = L11^-1 A12 (TMV: A01 /= A00.lowerTri(UnitDiag));
+//     4. gemm: A22 -= L21 U12 (TMV: A11 -= A10*A01 -> MultMM<true>(-1,...)).
+//
+// Pivot rule (src/TMV_Vector.cpp:474-503, src/TMV_LUDecompose.cpp:274-383):
+// first index of the strict maximum |a| over the sub-column, NaN handling as
+// described at pivot_key(); a maximum with |a|^2 < DBL_MIN (TMV_Underflow,
+// include/tmv/TMV_Base.h:692-696) zeroes the sub-column and records P[j] = j.
+// The L column is scaled by the reciprocal of the pivot, as TMV's v /= x does
+// (include/tmv/TMV_VectorArith.h:104-106).
+#include "lu.cuh"
+
+#include <algorithm>
+#include <climits>
+#include <vector>
+
+namespace tmvg {
+
+constexpr int kPanelThreads = 256;
+constexpr int kPanelMax = 64;  // largest panel width
+constexpr int kTriBlock = 64;  // diagonal block of the blocked triangular solves
+
+// ---------------------------------------------------------------------
+// Columns that TMV factors as the second column of a two-column leaf of its
+// recursion (split N1 = R/2, rounded down to a multiple of 64 above 64,
+// src/TMV_LUDecompose.cpp:241-245).  Their pivot scan starts from max = 0,
+// which only matters for NaN input.
+// ---------------------------------------------------------------------
+static void leaf_modes(int64_t off, int64_t R, std::vector<unsigned char>& modes)
+{
+    if (R > 2) {
+        int64_t N1 = R / 2;
+        if (N1 > 64) N1 = (N1 / 64) * 64;
+        leaf_modes(off, N1, modes);
+        leaf_modes(off + N1, R - N1, modes);
+    } else if (R == 2) {
+        modes[off + 1] = 1;
+    }
+}
+
+// ---------------------------------------------------------------------
+// Panel factorisation.
+// ---------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(kPanelThreads)
+lu_panel_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int nb,
+                int64_t* __restrict__ P, const unsigned char* __restrict__ modes,
+                int rows_per_cta, double* cand_key, long long* cand_idx,
+                T* cand_rows, T* diag_row, unsigned* bar, int* err)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* rows = reinterpret_cast<T*>(smem_raw);
+    const int ldp = nb + 1;
+    __shared__ double s_key[kPanelThreads / 32];
+    __shared__ long long s_idx[kPanelThreads / 32];
+    __shared__ double w_key;
+    __shared__ long long w_idx;
+    __shared__ T urow[kPanelMax];
+
+    const int G = gridDim.x;
+    const int cta = blockIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t m = n - k;
+    const int64_t r0 = (int64_t)cta * rows_per_cta;
+    const int nr = (int)max((int64_t)0, min((int64_t)rows_per_cta, m - r0));
+
+    for (int t = tid; t < nr * nb; t += kPanelThreads) {
+        const int r = t % nr, cc = t / nr;
+        rows[r * ldp + cc] = A[(k + r0 + r) + (k + cc) * lda];
+    }
+    __syncthreads();
+
+    bool prev_uf = false;
+    for (int jj = 0; jj < nb; ++jj) {
+        const int par = jj & 1;
+        const bool r2 = modes[jj] && !prev_uf;
+
+        // 1. this CTA's best candidate among panel rows >= jj
+        double bk = -INFINITY;
+        long long bi = LLONG_MAX;
+        for (int r = tid; r < nr; r += kPanelThreads) {
+            const int64_t pr = r0 + r;
+            if (pr < jj) continue;
+            pivot_combine(bk, bi, pivot_key(rows[r * ldp + jj], pr == jj, r2), (long long)pr);
+        }
+        warp_pivot_reduce(bk, bi);
+        if (lane == 0) { s_key[warp] = bk; s_idx[warp] = bi; }
+        __syncthreads();
+        if (warp == 0) {
+            bk = lane < kPanelThreads / 32 ? s_key[lane] : -INFINITY;
+            bi = lane < kPanelThreads / 32 ? s_idx[lane] : LLONG_MAX;
+            warp_pivot_reduce(bk, bi);
+            if (lane == 0) {
+                __stcg(&cand_key[par * G + cta], bk);
+                __stcg(&cand_idx[par * G + cta], bi);
+                w_idx = bi;  // local use below
+            }
+        }
+        __syncthreads();
+        // 2. publish the candidate row and (owner only) the diagonal row
+        {
+            const long long mine = w_idx;
+            if (mine != LLONG_MAX) {
+                const int r = (int)(mine - r0);
+                for (int cc = tid; cc < nb; cc += kPanelThreads)
+                    __stcg(&cand_rows[((int64_t)par * G + cta) * kPanelMax + cc], rows[r * ldp + cc]);
+            }
+            if (jj >= r0 && jj < r0 + nr) {
+                const int r = (int)(jj - r0);
+                for (int cc = tid; cc < nb; cc += kPanelThreads)
+                    __stcg(&diag_row[par * kPanelMax + cc], rows[r * ldp + cc]);
+            }
+        }
+        if (!grid_barrier(bar, (unsigned)(jj + 1) * (unsigned)G, err)) return;
+
+        // 3. global winner
+        if (warp == 0) {
+            double kk = -INFINITY;
+            long long ii = LLONG_MAX;
+            for (int g = lane; g < G; g += 32)
+                pivot_combine(kk, ii, __ldcg(&cand_key[par * G + g]), __ldcg(&cand_idx[par * G + g]));
+            warp_pivot_reduce(kk, ii);
+            if (lane == 0) { w_key = kk; w_idx = ii; }
+        }
+        __syncthreads();
+        const double wk = w_key;
+        const long long wi = w_idx;  // panel row of the pivot
+
+        if (underflows(wk)) {
+            if (cta == 0 && tid == 0) P[k + jj] = k + jj;
+            for (int r = tid; r < nr; r += kPanelThreads)
+                if (r0 + r >= jj) rows[r * ldp + jj] = T(0);
+            prev_uf = true;
+        } else {
+            prev_uf = false;
+            if (cta == 0 && tid == 0) P[k + jj] = k + wi;
+            const int wc = (int)(wi / rows_per_cta);
+            for (int cc = tid; cc < nb; cc += kPanelThreads)
+                urow[cc] = __ldcg(&cand_rows[((int64_t)par * G + wc) * kPanelMax + cc]);
+            __syncthreads();
+            if (wi != jj) {
+                if (jj >= r0 && jj < r0 + nr) {
+                    const int r = (int)(jj - r0);
+                    for (int cc = tid; cc < nb; cc += kPanelThreads) rows[r * ldp + cc] = urow[cc];
+                }
+                if (wi >= r0 && wi < r0 + nr) {
+                    const int r = (int)(wi - r0);
+                    for (int cc = tid; cc < nb; cc += kPanelThreads)
+                        rows[r * ldp + cc] = __ldcg(&diag_row[par * kPanelMax + cc]);
+                }
+            }
+            __syncthreads();
+            const T inv = T(1) / urow[jj];
+            for (int r = tid; r < nr; r += kPanelThreads) {
+                if (r0 + r <= jj) continue;
+                T* rw = rows + r * ldp;
+                const T l = rw[jj] * inv;
+                rw[jj] = l;
+                for (int cc = jj + 1; cc < nb; ++cc) rw[cc] -= l * urow[cc];
+            }
+        }
+        __syncthreads();
+    }
+
+    for (int t = tid; t < nr * nb; t += kPanelThreads) {
+        const int r = t % nr, cc = t / nr;
+        A[(k + r0 + r) + (k + cc) * lda] = rows[r * ldp + cc];
+    }
+}
+
+// ---------------------------------------------------------------------
+// Row interchanges.
+// ---------------------------------------------------------------------
+// Interchanges P[k..k+nb) applied to columns [0, ncols) except [skip0, skip1).
+template <typename T>
+__global__ void laswp_kernel(T* __restrict__ A, int64_t lda, int64_t ncols, int64_t k, int nb,
+                             const int64_t* __restrict__ P, int64_t skip0, int64_t skip1)
+{
+    __shared__ int64_t sp[kPanelMax];
+    for (int t = threadIdx.x; t < nb; t += blockDim.x) sp[t] = P[k + t];
+    __syncthreads();
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= ncols || (c >= skip0 && c < skip1)) return;
+    T* col = A + c * lda;
+    for (int t = 0; t < nb; ++t) {
+        const int64_t i = k + t, p = sp[t];
+        if (p != i) {
+            const T a = col[i];
+            col[i] = col[p];
+            col[p] = a;
+        }
+    }
+}
+
+// General interchanges on a strided matrix (one thread per column).
+template <typename T>
+__global__ void pivot_rows_kernel(int64_t ncols, T* __restrict__ B, int64_t bsi, int64_t bsj,
+                                  const int64_t* __restrict__ P, int64_t i1, int64_t i2, bool reverse)
+{
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= ncols) return;
+    T* col = B + c * bsj;
+    if (!reverse) {
+        for (int64_t i = i1; i < i2; ++i) {
+            const int64_t p = P[i];
+            if (p != i) { const T a = col[i * bsi]; col[i * bsi] = col[p * bsi]; col[p * bsi] = a; }
+        }
+    } else {
+        for (int64_t i = i2; i > i1;) {
+            --i;
+            const int64_t p = P[i];
+            if (p != i) { const T a = col[i * bsi]; col[i * bsi] = col[p * bsi]; col[p * bsi] = a; }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------
+// Triangular solve of one diagonal block (w <= kTriBlock rows) for many
+// right-hand sides: each thread substitutes one column, held in shared
+// memory.  Lower: x_i = (b_i - sum_{j<i} T_ij x_j) / T_ii; upper the mirror,
+// with the sums taken in the order TMV's column-oriented vector solve applies
+// its updates (src/TMV_TriDiv_V.cpp:148-236, 322-398).
+// skip_zero reproduces that solve's "if (*bj != 0)" test: a zero diagonal
+// only raises SINGULAR where it would divide a nonzero; the division is then
+// a true division.  Otherwise (TMV's row-major leaves,
+// src/TMV_TriDiv_M.cpp:58-188) every zero diagonal is singular and the row
+// is multiplied by the reciprocal.
+// ---------------------------------------------------------------------
+constexpr int kTriCols = 64;
+template <typename T>
+__global__ void __launch_bounds__(kTriCols)
+tri_diag_kernel(int w, const T* __restrict__ tri, int64_t tsi, int64_t tsj, bool upper,
+                bool unit, int64_t nrhs, T* __restrict__ B, int64_t bsi, int64_t bsj,
+                bool skip_zero, int* err)
+{
+    __shared__ T Ts[kTriBlock][kTriBlock + 1];
+    __shared__ T Xs[kTriBlock][kTriCols + 1];
+    const int tid = threadIdx.x;
+    const int64_t c0 = (int64_t)blockIdx.x * kTriCols;
+    const int ncb = (int)min((int64_t)kTriCols, nrhs - c0);
+
+    for (int t = tid; t < w * w; t += kTriCols) {
+        const int i = t % w, j = t / w;
+        const bool need = upper ? (j >= i) : (i >= j);
+        Ts[i][j] = need ? tri[i * tsi + j * tsj] : T(0);
+    }
+    if (bsi == 1) {
+        for (int t = tid; t < w * ncb; t += kTriCols) {
+            const int i = t % w, cl = t / w;
+            Xs[i][cl] = B[i + (c0 + cl) * bsj];
+        }
+    } else {
+        for (int t = tid; t < w * ncb; t += kTriCols) {
+            const int cl = t % ncb, i = t / ncb;
+            Xs[i][cl] = B[i * bsi + (c0 + cl) * bsj];
+        }
+    }
+    __syncthreads();
+
+    if (tid < ncb) {
+        bool sing = false;
+        if (!upper) {
+            for (int i = 0; i < w; ++i) {
+                T s = Xs[i][tid];
+                for (int j = 0; j < i; ++j) s -= Ts[i][j] * Xs[j][tid];
+                if (!unit) {
+                    const T d = Ts[i][i];
+                    if (skip_zero) {
+                        if (s != T(0)) {
+                            if (d == T(0)) sing = true;
+                            else s = s / d;
+                        }
+                    } else {
+                        if (d == T(0)) sing = true;
+                        else s = s * (T(1) / d);
+                    }
+                }
+                Xs[i][tid] = s;
+            }
+        } else {
+            for (int i = w - 1; i >= 0; --i) {
+                T s = Xs[i][tid];
+                for (int j = w - 1; j > i; --j) s -= Ts[i][j] * Xs[j][tid];
+                if (!unit) {
+                    const T d = Ts[i][i];
+                    if (skip_zero) {
+                        if (s != T(0)) {
+                            if (d == T(0)) sing = true;
+                            else s = s / d;
+                        }
+                    } else {
+                        if (d == T(0)) sing = true;
+                        else s = s * (T(1) / d);
+                    }
+                }
+                Xs[i][tid] = s;
+            }
+        }
+        if (sing) atomicCAS(err, (int)kDevOk, (int)kDevSingular);
+    }
+    __syncthreads();
+    if (bsi == 1) {
+        for (int t = tid; t < w * ncb; t += kTriCols) {
+            const int i = t % w, cl = t / w;
+            B[i + (c0 + cl) * bsj] = Xs[i][cl];
+        }
+    } else {
+        for (int t = tid; t < w * ncb; t += kTriCols) {
+            const int cl = t % ncb, i = t / ncb;
+            B[i * bsi + (c0 + cl) * bsj] = Xs[i][cl];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------
+// Host drivers.
+// ---------------------------------------------------------------------
+template <typename T>
+static tmvg_status launch_tri_diag(Context* c, int w, const T* tri, int64_t tsi, int64_t tsj,
+                                   bool upper, bool unit, int64_t nrhs, T* B, int64_t bsi,
+                                   int64_t bsj, bool skip_zero)
+{
+    if (nrhs <= 0 || w <= 0) return TMVG_OK;
+    const int64_t blocks = ceil_div(nrhs, kTriCols);
+    if (blocks > INT_MAX) return set_error(c, TMVG_UNSUPPORTED, "tri solve: too many columns");
+    tri_diag_kernel<T><<<(unsigned)blocks, kTriCols, 0, c->stream>>>(
+        w, tri, tsi, tsj, upper, unit, nrhs, B, bsi, bsj, skip_zero, c->dflags);
+    ++c->launches;
+    return check_cuda(c, cudaGetLastError(), "tri_diag launch");
+}
+
+template <typename T>
+tmvg_status tri_solve(Context* c, int64_t n, const T* tri, int64_t tsi, int64_t tsj,
+                      bool upper, bool unit, int64_t nrhs, T* B, int64_t bsi, int64_t bsj,
+                      bool skip_zero)
+{
+    if (n <= 0 || nrhs <= 0) return TMVG_OK;
+    tmvg_status st;
+    if (!upper) {
+        for (int64_t kb = 0; kb < n; kb += kTriBlock) {
+            const int w = (int)std::min<int64_t>(kTriBlock, n - kb);
+            st = launch_tri_diag<T>(c, w, tri + kb * tsi + kb * tsj, tsi, tsj, false, unit, nrhs,
+                                    B + kb * bsi, bsi, bsj, skip_zero);
+            if (st) return st;
+            if (kb + w < n) {
+                st = gemm<T>(c, n - kb - w, nrhs, w, T(-1),
+                             Mat<const T>{tri + (kb + w) * tsi + kb * tsj, tsi, tsj},
+                             Mat<const T>{B + kb * bsi, bsi, bsj}, T(1),
+                             Mat<T>{B + (kb + w) * bsi, bsi, bsj});
+                if (st) return st;
+            }
+        }
+    } else {
+        const int64_t last = ((n - 1) / kTriBlock) * kTriBlock;
+        for (int64_t kb = last; kb >= 0; kb -= kTriBlock) {
+            const int w = (int)std::min<int64_t>(kTriBlock, n - kb);
+            st = launch_tri_diag<T>(c, w, tri + kb * tsi + kb * tsj, tsi, tsj, true, unit, nrhs,
+                                    B + kb * bsi, bsi, bsj, skip_zero);
+            if (st) return st;
+            if (kb > 0) {
+                st = gemm<T>(c, kb, nrhs, w, T(-1), Mat<const T>{tri + kb * tsj, tsi, tsj},
+                             Mat<const T>{B + kb * bsi, bsi, bsj}, T(1), Mat<T>{B, bsi, bsj});
+                if (st) return st;
+            }
+        }
+    }
+    return TMVG_OK;
+}
+
+template <typename T>
+tmvg_status apply_pivots(Context* c, int64_t ncols, T* B, int64_t bsi, int64_t bsj,
+                         const int64_t* P, int64_t i1, int64_t i2, bool reverse)
+{
+    if (ncols <= 0 || i2 <= i1) return TMVG_OK;
+    pivot_rows_kernel<T><<<(unsigned)ceil_div(ncols, 128), 128, 0, c->stream>>>(
+        ncols, B, bsi, bsj, P, i1, i2, reverse);
+    ++c->launches;
+    return check_cuda(c, cudaGetLastError(), "pivot_rows launch");
+}
+
+template <typename T>
+tmvg_status lu_factor(Context* c, int64_t n, T* A, int64_t lda, int64_t* P)
+{
+    if (n < 0 || lda < std::max<int64_t>(n, 1)) return set_error(c, TMVG_BAD_ARG, "lu: bad n/lda");
+    if (n == 0) return TMVG_OK;
+    const int nbmax = kPanelMax;
+
+    // Panel geometry: one CTA per 256 rows up to one per SM.
+    const int64_t G_full = std::min<int64_t>(c->num_sms, ceil_div(n, kPanelThreads));
+    const int64_t rows_full = ceil_div(n, G_full);
+    const size_t smem_full = (size_t)rows_full * (nbmax + 1) * sizeof(T);
+    if (smem_full > 200 * 1024)
+        return set_error(c, TMVG_UNSUPPORTED, "lu: matrix too tall for the shared-memory panel");
+
+    // Workspace: modes (n bytes), candidate keys/indices/rows, diag rows.
+    const size_t off_key = 0;
+    const size_t off_idx = off_key + sizeof(double) * 2 * G_full;
+    const size_t off_rows = (off_idx + sizeof(long long) * 2 * G_full + 255) & ~size_t(255);
+    const size_t off_diag = off_rows + sizeof(T) * 2 * G_full * nbmax;
+    const size_t off_modes = (off_diag + sizeof(T) * 2 * nbmax + 255) & ~size_t(255);
+    const size_t bytes = off_modes + (size_t)n;
+    unsigned char* ws = (unsigned char*)workspace(c, bytes);
+    if (!ws) return TMVG_OOM;
+    double* cand_key = (double*)(ws + off_key);
+    long long* cand_idx = (long long*)(ws + off_idx);
+    T* cand_rows = (T*)(ws + off_rows);
+    T* diag_row = (T*)(ws + off_diag);
+    unsigned char* modes = ws + off_modes;
+    {
+        std::vector<unsigned char> hm((size_t)n, 0);
+        leaf_modes(0, n, hm);
+        tmvg_status st = check_cuda(
+            c, cudaMemcpyAsync(modes, hm.data(), (size_t)n, cudaMemcpyHostToDevice, c->stream),
+            "lu: modes upload");
+        if (st) return st;
+        // the host vector must outlive the copy
+        st = check_cuda(c, cudaStreamSynchronize(c->stream), "lu: modes sync");
+        if (st) return st;
+    }
+
+    static bool attr_set[2] = {false, false};
+    const int ai = sizeof(T) == 8 ? 0 : 1;
+    if (!attr_set[ai]) {
+        cudaFuncSetAttribute(lu_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             200 * 1024);
+        attr_set[ai] = true;
+    }
+
+    for (int64_t k = 0; k < n; k += nbmax) {
+        const int nb = (int)std::min<int64_t>(nbmax, n - k);
+        const int64_t m = n - k;
+        const int G = (int)std::min<int64_t>(c->num_sms, ceil_div(m, kPanelThreads));
+        const int rows_per_cta = (int)ceil_div(m, G);
+        const size_t smem = (size_t)rows_per_cta * (nb + 1) * sizeof(T);
+        tmvg_status st = check_cuda(c, cudaMemsetAsync(c->dbar, 0, sizeof(unsigned), c->stream),
+                                    "lu: barrier reset");
+        if (st) return st;
+        T* Ap = A;
+        int64_t* Pp = P;
+        const unsigned char* mp = modes + k;
+        int64_t ldav = lda, nv = n, kv = k;
+        int nbv = nb, rpc = rows_per_cta;
+        unsigned* bar = c->dbar;
+        int* err = c->dflags;
+        void* args[] = {&Ap, &ldav, &nv, &kv, &nbv, &Pp, &mp, &rpc, &cand_key, &cand_idx,
+                        &cand_rows, &diag_row, &bar, &err};
+        st = check_cuda(c,
+                        cudaLaunchCooperativeKernel((const void*)lu_panel_kernel<T>, dim3(G),
+                                                    dim3(kPanelThreads), args, smem, c->stream),
+                        "lu: panel launch");
+        if (st) return st;
+        ++c->launches;
+
+        // interchanges on the other columns
+        if (n > nb) {
+            laswp_kernel<T><<<(unsigned)ceil_div(n, 128), 128, 0, c->stream>>>(A, lda, n, k, nb, P,
+                                                                              k, k + nb);
+            ++c->launches;
+            st = check_cuda(c, cudaGetLastError(), "lu: laswp launch");
+            if (st) return st;
+        }
+        if (k + nb < n) {
+            const int64_t rest = n - k - nb;
+            st = launch_tri_diag<T>(c, nb, A + k + k * lda, 1, lda, false, true, rest,
+                                    A + k + (k + nb) * lda, 1, lda, false);
+            if (st) return st;
+            st = gemm<T>(c, rest, rest, nb, T(-1), Mat<const T>{A + (k + nb) + k * lda, 1, lda},
+                         Mat<const T>{A + k + (k + nb) * lda, 1, lda}, T(1),
+                         Mat<T>{A + (k + nb) + (k + nb) * lda, 1, lda});
+            if (st) return st;
+        }
+    }
+    return collect_device_error(c, "lu_factor");
+}
+
+template <typename T>
+tmvg_status lu_ldiveq(Context* c, int64_t n, const T* LU, int64_t lda, const int64_t* P,
+                      int64_t nrhs, T* B, int64_t bsi, int64_t bsj)
+{
+    // src/TMV_LUDiv.cpp:186-226: m.permuteRows(P); m /= L(unit); m /= U.
+    if (n <= 0 || nrhs <= 0) return TMVG_OK;
+    tmvg_status st = apply_pivots<T>(c, nrhs, B, bsi, bsj, P, 0, n, false);
+    if (st) return st;
+    // Column-major B (or one column) takes TMV's vector path: skip semantics.
+    const bool skip = true;
+    st = tri_solve<T>(c, n, LU, 1, lda, false, true, nrhs, B, bsi, bsj, skip);
+    if (st) return st;
+    st = tri_solve<T>(c, n, LU, 1, lda, true, false, nrhs, B, bsi, bsj, skip);
+    if (st) return st;
+    return collect_device_error(c, "lu_ldiveq");
+}
+
+template <typename T>
+tmvg_status lu_rdiveq(Context* c, int64_t n, const T* LU, int64_t lda, const int64_t* P,
+                      int64_t nrows, T* B, int64_t bsi, int64_t bsj)
+{
+    // src/TMV_LUDiv.cpp:370-411: m %= U; m %= L; m.reversePermuteCols(P), with
+    // m %= T computed as T^T.LDivEq(m^T) (include/tmv/TMV_TriMatrix.h:945-946).
+    if (n <= 0 || nrows <= 0) return TMVG_OK;
+    // m^T is n x nrows: element (i, j) = B[j*bsi + i*bsj].
+    const int64_t tsi = bsj, tsj = bsi;
+    // A single row of m is one vector (skip semantics); otherwise m^T is
+    // row-major and TMV's row-major leaves check every diagonal.
+    const bool skip = (nrows == 1);
+    tmvg_status st = tri_solve<T>(c, n, LU, lda, 1, false, false, nrows, B, tsi, tsj, skip);
+    if (st) return st;
+    st = tri_solve<T>(c, n, LU, lda, 1, true, true, nrows, B, tsi, tsj, skip);
+    if (st) return st;
+    st = apply_pivots<T>(c, nrows, B, tsi, tsj, P, 0, n, true);
+    if (st) return st;
+    return collect_device_error(c, "lu_rdiveq");
+}
+
+template tmvg_status lu_factor<double>(Context*, int64_t, double*, int64_t, int64_t*);
+template tmvg_status lu_factor<float>(Context*, int64_t, float*, int64_t, int64_t*);
+template tmvg_status tri_solve<double>(Context*, int64_t, const double*, int64_t, int64_t, bool,
+                                       bool, int64_t, double*, int64_t, int64_t, bool);
+template tmvg_status tri_solve<float>(Context*, int64_t, const float*, int64_t, int64_t, bool,
+                                      bool, int64_t, float*, int64_t, int64_t, bool);
+template tmvg_status apply_pivots<double>(Context*, int64_t, double*, int64_t, int64_t,
+                                          const int64_t*, int64_t, int64_t, bool);
+template tmvg_status apply_pivots<float>(Context*, int64_t, float*, int64_t, int64_t,
+                                         const int64_t*, int64_t, int64_t, bool);
+template tmvg_status lu_ldiveq<double>(Context*, int64_t, const double*, int64_t, const int64_t*,
+                                       int64_t, double*, int64_t, int64_t);
+template tmvg_status lu_rdiveq<double>(Context*, int64_t, const double*, int64_t, const int64_t*,
+                                       int64_t, double*, int64_t, int64_t);
+template tmvg_status lu_ldiveq<float>(Context*, int64_t, const float*, int64_t, const int64_t*,
+                                      int64_t, float*, int64_t, int64_t);
+
+}  // namespace tmvg

@@ -1,0 +1,143 @@
+"""Tensor-level entry points over the C ABI (device-resident float64 data).
+
+Matrices are torch tensors on a CUDA device.  TMV stores column-major; here a
+column-major n x m matrix is a tensor whose stride is (1, ld) with ld >= n,
+e.g. ``colmajor(x)``.  Each function names the TMV routine it mirrors.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+
+import torch
+
+from . import _lib
+
+_handles: dict[int, _lib.Handle] = {}
+_lock = threading.Lock()
+
+
+def handle(device: int | None = None) -> _lib.Handle:
+    """The per-device context, bound to torch's current stream."""
+    if device is None:
+        device = torch.cuda.current_device()
+    with _lock:
+        h = _handles.get(device)
+        if h is None:
+            h = _lib.Handle(device)
+            _handles[device] = h
+    h.set_stream(torch.cuda.current_stream(device).cuda_stream)
+    return h
+
+
+def colmajor(x: torch.Tensor) -> torch.Tensor:
+    """A column-major (Fortran-order) copy of a 2-D tensor."""
+    return x.t().contiguous().t()
+
+
+def is_colmajor(x: torch.Tensor) -> bool:
+    return x.dim() == 2 and (x.stride(0) == 1 or x.shape[0] <= 1) and (
+        x.shape[1] <= 1 or x.stride(1) >= max(x.shape[0], 1))
+
+
+def _ptr(x: torch.Tensor) -> C.c_void_p:
+    return C.c_void_p(x.data_ptr())
+
+
+def _check_f64_cuda(*ts: torch.Tensor) -> None:
+    for t in ts:
+        if t.dtype != torch.float64 or not t.is_cuda:
+            raise TypeError("expected float64 CUDA tensors")
+
+
+def _ld(x: torch.Tensor) -> int:
+    return max(x.stride(1) if x.shape[1] > 1 else x.shape[0], 1)
+
+
+def multmm(add: bool, alpha: float, A: torch.Tensor, B: torch.Tensor, C_: torch.Tensor) -> None:
+    """C (+)= alpha*A*B in place (tmv::MultMM<add>, src/TMV_MultMM.cpp:405).
+
+    A, B and C are 2-D float64 CUDA tensors with any of TMV's dense layouts
+    (column- or row-major strides)."""
+    _check_f64_cuda(A, B, C_)
+    m, k = A.shape
+    k2, n = B.shape
+    if k2 != k or tuple(C_.shape) != (m, n):
+        raise ValueError("multmm: shape mismatch")
+    h = handle(C_.device.index)
+    h.check(h.call("tmvg_multmm_f64", int(bool(add)), float(alpha), m, n, k,
+                   _ptr(A), A.stride(0), A.stride(1), _ptr(B), B.stride(0), B.stride(1),
+                   _ptr(C_), C_.stride(0), C_.stride(1)), "multmm")
+
+
+def lu_decompose(A: torch.Tensor, P: torch.Tensor | None = None) -> torch.Tensor:
+    """In-place P A = L U of a column-major square A; returns the int64
+    interchange vector (tmv::LU_Decompose, src/TMV_LUDecompose.cpp:514)."""
+    _check_f64_cuda(A)
+    n = A.shape[0]
+    if A.shape[1] != n or not is_colmajor(A):
+        raise ValueError("lu_decompose: A must be square and column-major")
+    if P is None:
+        P = torch.empty(n, dtype=torch.int64, device=A.device)
+    h = handle(A.device.index)
+    h.check(h.call("tmvg_lu_decompose_f64", n, _ptr(A), _ld(A), _ptr(P)), "lu_decompose")
+    return P
+
+
+def lu_ldiveq(LU: torch.Tensor, P: torch.Tensor, B: torch.Tensor) -> None:
+    """B := (P L U)^-1 B in place (tmv::LU_LDivEq, src/TMV_LUDiv.cpp:186)."""
+    _check_f64_cuda(LU, B)
+    n = LU.shape[0]
+    if B.dim() == 1:
+        B = B.view(-1, 1)
+    if B.shape[0] != n or not is_colmajor(B) or not is_colmajor(LU):
+        raise ValueError("lu_ldiveq: B must be column-major n x nrhs")
+    h = handle(LU.device.index)
+    h.check(h.call("tmvg_lu_ldiveq_f64", n, _ptr(LU), _ld(LU), _ptr(P), B.shape[1], _ptr(B),
+                   _ld(B)), "lu_ldiveq")
+
+
+def lu_rdiveq(LU: torch.Tensor, P: torch.Tensor, B: torch.Tensor) -> None:
+    """B := B (P L U)^-1 in place (tmv::LU_RDivEq, src/TMV_LUDiv.cpp:370)."""
+    _check_f64_cuda(LU, B)
+    n = LU.shape[0]
+    if B.dim() == 1:
+        B = B.view(1, -1)
+    if B.shape[1] != n or not is_colmajor(B) or not is_colmajor(LU):
+        raise ValueError("lu_rdiveq: B must be column-major nrows x n")
+    h = handle(LU.device.index)
+    h.check(h.call("tmvg_lu_rdiveq_f64", n, _ptr(LU), _ld(LU), _ptr(P), B.shape[0], _ptr(B),
+                   _ld(B)), "lu_rdiveq")
+
+
+def divide(A: torch.Tensor, B: torch.Tensor):
+    """X = B/A with the LU of a copy of A (LUDiv<double>, src/TMV_LUD.cpp:74-120).
+
+    Returns (X, LU, P); LU and P can be reused for further solves."""
+    _check_f64_cuda(A, B)
+    n = A.shape[0]
+    if B.dim() == 1:
+        B = B.view(-1, 1)
+    nrhs = B.shape[1]
+    if not is_colmajor(A):
+        A = colmajor(A)
+    if not is_colmajor(B):
+        B = colmajor(B)
+    LU = torch.empty((n, n), dtype=torch.float64, device=A.device).t()
+    X = torch.empty((nrhs, n), dtype=torch.float64, device=A.device).t()
+    P = torch.empty(n, dtype=torch.int64, device=A.device)
+    h = handle(A.device.index)
+    h.check(h.call("tmvg_divide_f64", n, _ptr(A), _ld(A), nrhs, _ptr(B), _ld(B), _ptr(X),
+                   max(n, 1), _ptr(LU), _ptr(P)), "divide")
+    return X, LU, P
+
+
+def lu_det(LU: torch.Tensor, P: torch.Tensor):
+    """(det, logdet, sign) of stored factors (LUDiv::det/logDet, src/TMV_LUD.cpp:132-156)."""
+    _check_f64_cuda(LU)
+    n = LU.shape[0]
+    d, ld, s = C.c_double(), C.c_double(), C.c_double()
+    h = handle(LU.device.index)
+    h.check(h.call("tmvg_lu_det_f64", n, _ptr(LU), _ld(LU), _ptr(P), C.byref(d), C.byref(ld),
+                   C.byref(s)), "lu_det")
+    return d.value, ld.value, s.value

@@ -1,0 +1,241 @@
+"""A GPU-resident mirror of the tmv::Matrix<double> product and division surface.
+
+    A = Matrix(a); B = Matrix(b)
+    C = A * B                      # ProdMM -> MultMM<false>  (TMV_MatrixArith.h:701-730)
+    A.divideUsing(LU); A.saveDiv() # DivHelper flags          (src/TMV_BaseMatrix.cpp:215-223)
+    X = B / A                      # QuotMM -> LUDiv::doLDiv  (TMV_MatrixArith.h:1145-1175)
+    Y = W % A                      # RQuotMM -> LUDiv::doRDiv (TMV_MatrixArith.h:1197-1227)
+    A.det(), A.logDet(), A.lud().getP(), A.isSingular()
+
+Storage is column-major float64 on the current CUDA device.  As in TMV, the
+LU divider is created lazily on the first division and destroyed after it
+unless saveDiv() was called (src/TMV_BaseMatrix.cpp:170-190, 273-274).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import torch
+
+from . import linalg
+
+LU = "LU"
+ColMajor = "ColMajor"
+RowMajor = "RowMajor"
+
+
+class LUDiv:
+    """The LU decomposition of a matrix (tmv::LUDiv<double>, include/tmv/TMV_LUD.h:90-161)."""
+
+    def __init__(self, m: "Matrix", inplace: bool = False):
+        src = m.t
+        if inplace:
+            self.LU = src
+        else:
+            self.LU = torch.empty_like(src.t()).t()
+            self.LU.copy_(src)
+        self.P = linalg.lu_decompose(self.LU)
+        self._det = None
+
+    def isTrans(self) -> bool:
+        return False
+
+    def getLU(self) -> torch.Tensor:
+        return self.LU
+
+    def getL(self) -> torch.Tensor:
+        n = self.LU.shape[0]
+        return torch.tril(self.LU, -1) + torch.eye(n, dtype=self.LU.dtype, device=self.LU.device)
+
+    def getU(self) -> torch.Tensor:
+        return torch.triu(self.LU)
+
+    def getP(self) -> np.ndarray:
+        return self.P.cpu().numpy()
+
+    def det(self) -> float:
+        if self._det is None:
+            self._det = linalg.lu_det(self.LU, self.P)
+        return self._det[0]
+
+    def logDet(self):
+        if self._det is None:
+            self._det = linalg.lu_det(self.LU, self.P)
+        return self._det[1], self._det[2]
+
+    def isSingular(self) -> bool:
+        # src/TMV_LUD.cpp:204-209: min |U_jj|^2 <= eps * max |U_jj|^2
+        d2 = torch.diagonal(self.LU) ** 2
+        if d2.numel() == 0:
+            return False
+        return bool(d2.min() <= np.finfo(np.float64).eps * d2.max())
+
+    def ldiv(self, b: torch.Tensor) -> torch.Tensor:
+        x = linalg.colmajor(b)
+        linalg.lu_ldiveq(self.LU, self.P, x)
+        return x
+
+    def rdiv(self, b: torch.Tensor) -> torch.Tensor:
+        x = linalg.colmajor(b)
+        linalg.lu_rdiveq(self.LU, self.P, x)
+        return x
+
+
+class Matrix:
+    """Column-major float64 matrix on a CUDA device (tmv::Matrix<double,ColMajor>)."""
+
+    def __init__(self, data, device=None):
+        if isinstance(data, Matrix):
+            data = data.t
+        if isinstance(data, torch.Tensor):
+            t = data.to(dtype=torch.float64, device=device or data.device if data.is_cuda else "cuda")
+        else:
+            a = np.asarray(data, dtype=np.float64)
+            t = torch.from_numpy(a).to(device or "cuda")
+        if t.dim() == 1:
+            t = t.view(-1, 1)
+        self.t = linalg.colmajor(t)
+        self._divtype = None
+        self._savediv = False
+        self._inplace = False
+        self._div: LUDiv | None = None
+
+    # -- shape -------------------------------------------------------------
+    def colsize(self) -> int:
+        return self.t.shape[0]
+
+    def rowsize(self) -> int:
+        return self.t.shape[1]
+
+    @property
+    def shape(self):
+        return tuple(self.t.shape)
+
+    def numpy(self) -> np.ndarray:
+        return self.t.cpu().numpy()
+
+    # -- product -----------------------------------------------------------
+    def __mul__(self, other):
+        if isinstance(other, (int, float)):
+            return Matrix(self.t * float(other))
+        if not isinstance(other, Matrix):
+            other = Matrix(other)
+        m, k = self.shape
+        k2, n = other.shape
+        if k != k2:
+            raise ValueError("size mismatch in product")
+        out = torch.empty((n, m), dtype=torch.float64, device=self.t.device).t()
+        linalg.multmm(False, 1.0, self.t, other.t, out)
+        return Matrix._wrap(out)
+
+    __matmul__ = __mul__
+
+    @staticmethod
+    def _wrap(t: torch.Tensor) -> "Matrix":
+        m = Matrix.__new__(Matrix)
+        m.t = t
+        m._divtype = None
+        m._savediv = False
+        m._inplace = False
+        m._div = None
+        return m
+
+    # -- division control (DivHelper) ---------------------------------------
+    def divideUsing(self, dt) -> None:
+        if dt != LU:
+            raise NotImplementedError("only tmv::LU is implemented on the GPU")
+        if self._divtype != dt:
+            self._div = None
+        self._divtype = dt
+
+    def saveDiv(self) -> None:
+        self._savediv = True
+
+    def divideInPlace(self) -> None:
+        self._inplace = True
+        self._savediv = True
+
+    def setDiv(self) -> None:
+        if self._div is None:
+            if self.colsize() != self.rowsize():
+                raise NotImplementedError("LU division of non-square matrices is out of scope")
+            self._divtype = self._divtype or LU
+            self._div = LUDiv(self, self._inplace)
+
+    def unsetDiv(self) -> None:
+        self._div = None
+
+    def resetDiv(self) -> None:
+        self.unsetDiv()
+        self.setDiv()
+
+    def lud(self) -> LUDiv:
+        self.divideUsing(LU)
+        self.setDiv()
+        return self._div
+
+    def _done(self) -> None:
+        if not self._savediv:
+            self._div = None
+
+    def _ldiv(self, b: "Matrix") -> "Matrix":
+        self.setDiv()
+        x = self._div.ldiv(b.t)
+        self._done()
+        return Matrix._wrap(x)
+
+    def _rdiv(self, b: "Matrix") -> "Matrix":
+        self.setDiv()
+        bt = b.t if b.t.shape[1] == self.colsize() else b.t.t()
+        x = self._div.rdiv(bt)
+        self._done()
+        return Matrix._wrap(x)
+
+    def __truediv__(self, other):
+        """self / other: for a Matrix `other`, X = other^-1 self (TMV's b/m)."""
+        if isinstance(other, (int, float)):
+            return Matrix(self.t / float(other))
+        if not isinstance(other, Matrix):
+            other = Matrix(other)
+        return other._ldiv(self)
+
+    def __mod__(self, other):
+        """self % other: X = self other^-1 (TMV's b%m)."""
+        if not isinstance(other, Matrix):
+            other = Matrix(other)
+        return other._rdiv(self)
+
+    # -- decomposition queries ------------------------------------------------
+    def det(self) -> float:
+        self.setDiv()
+        d = self._div.det()
+        self._done()
+        return d
+
+    def logDet(self):
+        self.setDiv()
+        r = self._div.logDet()
+        self._done()
+        return r
+
+    def isSingular(self) -> bool:
+        self.setDiv()
+        r = self._div.isSingular()
+        self._done()
+        return r
+
+    def inverse(self) -> "Matrix":
+        n = self.colsize()
+        eye = torch.eye(n, dtype=torch.float64, device=self.t.device)
+        return Matrix._wrap(eye) / self
+
+    def norm(self) -> float:
+        return float(torch.linalg.norm(self.t))
+
+
+def Norm(m: Matrix) -> float:
+    return m.norm() if isinstance(m, Matrix) else float(np.linalg.norm(m))
+
+
+__all__ = ["Matrix", "LUDiv", "LU", "ColMajor", "RowMajor", "Norm", "math"]
