@@ -1,0 +1,357 @@
+"""Benchmark of the LU-solve hot path on GB300.
+
+Headline workload (a "step"): one dense solve x = A^-1 b at n = 8192 with one
+right-hand side, A = U diag(s) V^T, U and V Haar-orthogonal (Q of the QR of a
+seeded Gaussian, columns sign-fixed by diag(R)), s log-spaced from 1 to
+1/cond.  The step runs the mixed-precision path (FP32 factorisation + FP64
+iterative refinement to a normwise backward error <= 1e-12) when it is
+available, otherwise the plain FP64 LU path.  Throughput is reported as
+FP64-equivalent TFLOP/s, (2n^3/3 + 2n^2 nrhs) per solve.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times TMV's CPU algorithm (the oracle's C restatement of
+TMV's LU_Decompose + LU_LDivEq with its OpenMP product) on the host cores on
+the same workload and prints the same JSON line with "impl": "reference".
+Inputs are 512 MiB (A in FP64), larger than the 129 MB L2, so no flush is
+needed between steps.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "n=8192 LU-solve TFLOP/s mixed+IR vs FP64 GPU at 1e-12 rel err; batched solves/s"
+
+
+def lu_solve_flops(n: int, nrhs: int) -> float:
+    return 2.0 * n ** 3 / 3.0 + 2.0 * n * n * nrhs
+
+
+def haar_matrix_torch(n: int, cond: float, seed: int, dev):
+    """A = U diag(s) V^T in FP64 on the device (setup, not timed)."""
+    import torch
+
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(2):
+        g = torch.from_numpy(rng.standard_normal((n, n))).to(dev)
+        q, r = torch.linalg.qr(g)
+        q *= torch.sign(torch.diagonal(r)).unsqueeze(0)
+        out.append(q)
+        del g, r
+    U, V = out
+    s = torch.logspace(0, -np.log10(cond), n, dtype=torch.float64, device=dev)
+    A = (U * s.unsqueeze(0)) @ V.t()
+    b = torch.from_numpy(rng.standard_normal(n)).to(dev)
+    return A, b
+
+
+def haar_matrix_numpy(n: int, cond: float, seed: int):
+    rng = np.random.default_rng(seed)
+    qs = []
+    for _ in range(2):
+        q, r = np.linalg.qr(rng.standard_normal((n, n)))
+        qs.append(q * np.sign(np.diag(r))[None, :])
+    U, V = qs
+    s = np.logspace(0, -np.log10(cond), n)
+    A = (U * s[None, :]) @ V.T
+    b = rng.standard_normal(n)
+    return np.asfortranarray(A), b
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int = 0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        d["_source"] = "measured"
+        return d
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0,
+            "_source": "fallback"}
+
+
+# FP64 DFMA peak of a GB300, measured by a DFMA throughput kernel on this machine
+# (1.19 TFLOP/s at ~1990 MHz; the m8n8k4 DMMA path measured 1.05 TFLOP/s).
+FP64_DFMA_PEAK_TFLOPS = 1.19
+
+
+def run_gpu(args) -> dict:
+    import torch
+
+    from tmv_gb300 import linalg
+    from tmv_gb300 import _lib
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+
+    n, nrhs, cond = args.n, 1, args.cond
+    A, b = haar_matrix_torch(n, cond, seed=3 + rank, dev=dev)
+    Acm = linalg.colmajor(A)
+    del A
+    B = b.view(n, 1).clone()
+    h = linalg.handle(local)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        X, LU, P = linalg.divide(Acm, B)
+        return X
+
+    for _ in range(args.warmup):
+        X = step()
+    torch.cuda.synchronize()
+    launches0 = h.launches()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        X = step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    launches = (h.launches() - launches0) // max(args.steps, 1)
+    ms_step = ms / args.steps
+    flops = lu_solve_flops(n, nrhs)
+    value = flops * world / (ms_step * 1e-3) / 1e12
+
+    # accuracy of the last solve: normwise backward error and relative residual
+    x = X[:, 0]
+    r = B[:, 0] - Acm @ x
+    berr = float(r.abs().max() / (Acm.abs().sum(dim=1).max() * x.abs().max() + B.abs().max()))
+
+    # dominant kernel: the FP64 trailing-update product, timed alone at the
+    # size of the first trailing update of this factorisation.
+    roof = gemm_roofline(dev, n)
+
+    # end to end through the host-pointer C ABI (pinned host buffers)
+    e2e = e2e_host(args, Acm, B, n, nrhs)
+
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(np.asfortranarray(Acm.cpu().numpy()),
+                           B.cpu().numpy(), n, cond)
+    else:
+        cpu = None
+    out = {
+        "metric": METRIC, "value": round(value, 4), "unit": "TFLOP/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms_step, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"dense LU solve n={n}, 1 RHS, cond={cond:g}, FP64 GPU LU path",
+                   "path": "fp64", "n": n, "nrhs": nrhs, "cond": cond,
+                   "l2": "inputs larger than L2 (A is 512 MiB FP64); no flush"},
+        "accuracy": {"backward_error": berr},
+        "roofline": roof, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
+    }
+    if cpu is not None:
+        out["cpu_baseline"] = cpu
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return out if rank == 0 else None
+
+
+def gemm_roofline(dev, n: int) -> dict:
+    import torch
+
+    from tmv_gb300 import linalg
+
+    m = n - 64
+    a = linalg.colmajor(torch.randn(m, 64, dtype=torch.float64, device=dev))
+    bb = linalg.colmajor(torch.randn(64, m, dtype=torch.float64, device=dev))
+    c = linalg.colmajor(torch.randn(m, m, dtype=torch.float64, device=dev))
+    for _ in range(2):
+        linalg.multmm(True, -1.0, a, bb, c)
+    s = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 5
+    e0.record(s)
+    for _ in range(reps):
+        linalg.multmm(True, -1.0, a, bb, c)
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    flop = 2.0 * m * m * 64
+    ach = flop / (ms * 1e-3) / 1e12
+    return {"kernel": "gemm_simt_kernel<double> (trailing update A22 -= L21 U12, K=64)",
+            "bound": "tensor", "achieved": round(ach, 4), "peak": FP64_DFMA_PEAK_TFLOPS,
+            "unit": "TFLOP/s", "frac": round(ach / FP64_DFMA_PEAK_TFLOPS, 4), "traffic": None,
+            "peak_source": "measured FP64 DFMA throughput (no FP64 entry in MEASURED_PEAKS.json)",
+            "algorithmic_flop_per_launch": flop, "ms_per_launch": round(ms, 4)}
+
+
+def e2e_host(args, Acm, B, n, nrhs) -> dict:
+    import ctypes as C
+
+    import torch
+
+    from tmv_gb300 import linalg
+
+    hA = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
+    hA.copy_(Acm.t())  # row-major storage of A^T == column-major storage of A
+    hB = torch.empty((n, nrhs), dtype=torch.float64, pin_memory=True)
+    hB.copy_(B)
+    hX = torch.empty((nrhs, n), dtype=torch.float64, pin_memory=True)
+    h = linalg.handle(Acm.device.index)
+    def call():
+        h.check(h.call("tmvg_divide_f64_host", n, C.c_void_p(hA.data_ptr()), nrhs,
+                       C.c_void_p(hB.data_ptr()), C.c_void_p(hX.data_ptr()), None, None))
+    call()
+    steps = max(1, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        call()
+    dt = (time.perf_counter() - t0) / steps
+    return {"value": round(lu_solve_flops(n, nrhs) / dt / 1e12, 4), "unit": "TFLOP/s",
+            "h2d_bytes_per_step": 8 * n * n + 8 * n * nrhs, "d2h_bytes_per_step": 8 * n * nrhs,
+            "ms_per_step": round(dt * 1e3, 3), "steps": steps}
+
+
+def cpu_baseline(A: np.ndarray, B: np.ndarray, n: int, cond: float) -> dict:
+    """TMV's FP64 LU + solve algorithm (oracle C restatement, OpenMP product)
+    on the host cores: one solve of the same workload (same A and b)."""
+    import oracle
+
+    orc = oracle.port()
+    cores = os.cpu_count() or 1
+    orc.set_threads(cores)
+    t0 = time.perf_counter()
+    X, LU, P = orc.divide(A, B)
+    dt = time.perf_counter() - t0
+    return {"value": round(lu_solve_flops(n, 1) / dt / 1e12, 5), "unit": "TFLOP/s",
+            "cores": cores, "kind": "port",
+            "sample": f"one FP64 LU_Decompose + LU_LDivEq at n={n}, cond={cond:g} ({dt:.1f} s)"}
+
+
+def run_reference(args) -> dict | None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return None
+    import oracle
+
+    orc = oracle.port()
+    cores = os.cpu_count() or 1
+    orc.set_threads(cores)
+    n = args.n
+    A, b = haar_matrix_numpy(n, args.cond, seed=3)
+    B = b.reshape(n, 1)
+    for _ in range(min(args.warmup, 1)):
+        orc.divide(A, B)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        orc.divide(A, B)
+    dt = (time.perf_counter() - t0) / args.steps
+    v = lu_solve_flops(n, 1) / dt / 1e12
+    return {"metric": METRIC, "value": round(v, 5), "unit": "TFLOP/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"dense LU solve n={n}, 1 RHS, cond={args.cond:g}",
+                       "n": n, "nrhs": 1, "cond": args.cond},
+            "cpu_baseline": {"value": round(v, 5), "unit": "TFLOP/s", "cores": cores,
+                             "kind": "port",
+                             "sample": f"{args.steps} FP64 LU solves at n={n} (TMV algorithm, "
+                                       "oracle C restatement; warm-up capped at 1)"},
+            "e2e": {"value": round(v, 5), "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=8192)
+    ap.add_argument("--cond", type=float, default=1e6)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        out = run_reference(args)
+    else:
+        out = run_gpu(args)
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,76 @@
+"""Shared test helpers: seeded inputs in TMV's layouts and device transfers."""
+from __future__ import annotations
+
+import numpy as np
+
+
+def to_dev(a: np.ndarray, dev, layout: str = "F"):
+    """A torch CUDA tensor holding `a` in column-major ("F") or row-major ("C") storage."""
+    import torch
+
+    if layout == "F":
+        t = torch.from_numpy(np.ascontiguousarray(a.T)).to(dev)
+        return t.t()
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+def to_host(t) -> np.ndarray:
+    return t.detach().cpu().numpy()
+
+
+def rel_frob(x: np.ndarray, ref: np.ndarray) -> float:
+    d = np.linalg.norm(ref)
+    return float(np.linalg.norm(x - ref) / (d if d > 0 else 1.0))
+
+
+def arith8_operands(m: int, n: int, k: int):
+    """The integer-valued operands of TMV's real product test
+    (tests/TMV_TestMatrixArith_8.cpp:327-336): ac(i,j) = i+j+5 (m x k),
+    bc(i,j) = 2i-3j+13 (k x n).  Every product is exact in FP64."""
+    i = np.arange(m)[:, None]
+    j = np.arange(k)[None, :]
+    a = (i + j + 5).astype(np.float64)
+    i2 = np.arange(k)[:, None]
+    j2 = np.arange(n)[None, :]
+    b = (2 * i2 - 3 * j2 + 13).astype(np.float64)
+    return a, b
+
+
+def tmv_square4():
+    """TMV's 4x4 known-answer matrix and right-hand side
+    (tests/TMV_TestMatrixDiv.cpp:11-24); det = 28800 (:76)."""
+    m = np.array([[2 + 4 * i - 5 * j for j in range(4)] for i in range(4)], dtype=np.float64)
+    m[0, 0], m[1, 0], m[2, 0], m[3, 0], m[2, 2] = 14, -2, 7, -10, 30
+    b = np.array([2.0, -10.0, 5.0, -5.0])
+    return m, b
+
+
+def tmv_decomp_matrix(mattype: int, N: int = 200) -> np.ndarray:
+    """The square real test matrix of tests/TMV_TestMatrixDecomp.cpp:27-55
+    (mattype 0: well conditioned, 3: singular)."""
+    M = N
+    singular = mattype >= 3
+    i = np.arange(M)[:, None]
+    j = np.arange(N)[None, :]
+    m = (2 + 4 * i - 5 * j).astype(np.float64)
+    if not singular:
+        m /= 10 * N
+    m[3, 3] = 14
+    m[3, 4] = -2
+    m[0, 2] = 7
+    m[M - 1, N - 4] = 23
+    m[M - 1, N - 2] = 13
+    m[M - 1, N - 1] = -10
+    if singular:
+        m[:, 1] = 0
+        m[7, :] = m[6, :]
+    else:
+        m[np.arange(N), np.arange(N)] *= 30 * N
+    return m
+
+
+def diag_shift_matrix(rng, n: int, shift: float) -> np.ndarray:
+    """A_ij ~ N(0,1) plus `shift` on the diagonal (the workloads' LU matrices)."""
+    a = rng.standard_normal((n, n))
+    a[np.arange(n), np.arange(n)] += shift
+    return a

@@ -1,0 +1,239 @@
+"""LU_Decompose / LU_LDivEq / LU_RDivEq on the GPU against the oracle."""
+import numpy as np
+import pytest
+
+from helpers import diag_shift_matrix, rel_frob, tmv_decomp_matrix, tmv_square4, to_dev, to_host
+
+pytestmark = pytest.mark.gpu
+
+SIZES = [1, 2, 3, 4, 5, 17, 31, 32, 33, 63, 64, 65, 100, 127, 128, 129, 200, 255, 256, 257, 500]
+
+
+def gpu_lu(dev, a):
+    import torch
+
+    from tmv_gb300 import linalg
+
+    A = to_dev(a, dev, "F")
+    P = linalg.lu_decompose(A)
+    torch.cuda.synchronize()
+    return to_host(A), to_host(P)
+
+
+def oracle_lu(orc, a):
+    A = np.asfortranarray(a.copy())
+    P = orc.lu_decompose(A)
+    return A, P
+
+
+def reconstruct(LU, P):
+    n = LU.shape[0]
+    L = np.tril(LU, -1) + np.eye(n)
+    U = np.triu(LU)
+    A = L @ U
+    for i in range(n - 1, -1, -1):  # reversePermuteRows
+        p = P[i]
+        if p != i:
+            A[[i, p]] = A[[p, i]]
+    return A
+
+
+@pytest.mark.parametrize("n", SIZES)
+def test_random_pivots_match_oracle(dev, orc, n):
+    rng = np.random.default_rng(1000 + n)
+    a = rng.standard_normal((n, n))
+    lu_g, p_g = gpu_lu(dev, a)
+    lu_o, p_o = oracle_lu(orc, a)
+    assert np.array_equal(p_g, p_o), "pivot sequence differs"
+    scale = max(np.abs(lu_o).max(), 1.0)
+    assert np.abs(lu_g - lu_o).max() <= 1e-11 * scale * max(n, 1)
+    # P L U = A to working accuracy
+    resid = np.linalg.norm(reconstruct(lu_g, p_g) - a) / np.linalg.norm(a)
+    assert resid <= 1e-14 * n + 1e-15
+
+
+def test_diag_shifted_identity_pivots(dev, orc):
+    # the LU workload's matrix family: N(0,1) + 4 sqrt(n) on the diagonal
+    rng = np.random.default_rng(2)
+    n = 1024
+    a = diag_shift_matrix(rng, n, 4 * np.sqrt(n))
+    lu_g, p_g = gpu_lu(dev, a)
+    lu_o, p_o = oracle_lu(orc, a)
+    assert np.array_equal(p_g, p_o)
+    assert np.array_equal(p_g, np.arange(n))
+    assert rel_frob(lu_g, lu_o) <= 1e-14
+
+
+def test_tmv_decomp_matrices(dev, orc):
+    # tests/TMV_TestMatrixDecomp.cpp:27-55,133-150 (mattype 0 and singular 3).
+    # The reference test checks P*L*U == m within eps*norm(m).  The singular
+    # matrix has rank 5 numerically: from step 5 on |U_jj| ~ 1e-13 is
+    # rounding noise and the pivot choice depends on summation order (TMV's
+    # own SSE2 and generic builds already disagree from step 16), so pivots
+    # are compared on the numerically determined prefix only.
+    for mattype in (0, 3):
+        a = tmv_decomp_matrix(mattype)
+        lu_g, p_g = gpu_lu(dev, a)
+        lu_o, p_o = oracle_lu(orc, a)
+        normm = np.linalg.norm(a)
+        noise = np.nonzero(np.abs(np.diag(lu_o))[2:] <= 1e-8 * normm)[0]
+        prefix = int(noise[0]) + 2 if mattype == 3 else len(p_o)
+        if mattype == 3:
+            assert prefix == 5
+        assert np.array_equal(p_g[:prefix], p_o[:prefix]), mattype
+        assert np.linalg.norm(reconstruct(lu_g, p_g) - a) <= 1e-12 * normm, mattype
+
+
+def test_tmv_square4_det(dev, orc):
+    import torch
+
+    from tmv_gb300 import linalg
+
+    m, b = tmv_square4()
+    lu_g, p_g = gpu_lu(dev, m)
+    lu_o, p_o = oracle_lu(orc, m)
+    assert np.array_equal(p_g, p_o)
+    LU = to_dev(lu_g, dev, "F")
+    P = torch.from_numpy(p_g).to(dev)
+    det, logdet, sign = linalg.lu_det(LU, P)
+    assert abs(det - 28800) < 1e-10 * 28800
+    assert abs(logdet - np.log(28800)) < 1e-12 and sign == 1.0
+
+
+def test_zero_and_singular_columns(dev, orc):
+    # an all-zero matrix: every column underflows -> P[j] = j, factor zero
+    n = 70
+    lu_g, p_g = gpu_lu(dev, np.zeros((n, n)))
+    assert np.array_equal(p_g, np.arange(n)) and not lu_g.any()
+    # a zero column in the middle and duplicate rows
+    rng = np.random.default_rng(7)
+    a = rng.standard_normal((n, n))
+    a[:, 9] = 0.0
+    a[40] = a[12]
+    lu_g, p_g = gpu_lu(dev, a)
+    lu_o, p_o = oracle_lu(orc, a)
+    assert np.array_equal(p_g, p_o)
+    assert p_g[9] == 9
+    # underflowing column (|a|^2 < DBL_MIN): zeroed, not pivoted
+    a = rng.standard_normal((n, n))
+    a[:, 5] = 1e-160 * rng.standard_normal(n)
+    lu_g, p_g = gpu_lu(dev, a)
+    lu_o, p_o = oracle_lu(orc, a)
+    assert np.array_equal(p_g, p_o)
+    assert np.array_equal(lu_g[5:, 5], np.zeros(n - 5))
+
+
+def test_ties_take_first_index(dev, orc):
+    # exact ties in the first column: TMV's strict '>' keeps the lowest index
+    n = 40
+    rng = np.random.default_rng(3)
+    a = rng.standard_normal((n, n))
+    a[:, 0] = 0.5
+    a[[7, 20, 33], 0] = [-3.0, 3.0, -3.0]
+    lu_g, p_g = gpu_lu(dev, a)
+    lu_o, p_o = oracle_lu(orc, a)
+    assert p_o[0] == 7 and np.array_equal(p_g, p_o)
+
+
+def test_nan_pivot_rules(dev, orc):
+    # NaN is chosen only when it is the first element of the scanned column
+    n = 9
+    rng = np.random.default_rng(4)
+    for where in [(0, 0), (3, 0), (1, 1), (4, 1), (2, 2)]:
+        a = rng.standard_normal((n, n))
+        a[where] = np.nan
+        lu_g, p_g = gpu_lu(dev, a)
+        lu_o, p_o = oracle_lu(orc, a)
+        assert np.array_equal(p_g, p_o), where
+        assert np.array_equal(np.isnan(lu_g), np.isnan(lu_o)), where
+
+
+@pytest.mark.parametrize("n,nrhs", [(1, 1), (7, 3), (64, 1), (65, 8), (300, 8), (513, 64)])
+def test_ldiveq_rdiveq_vs_oracle(dev, orc, n, nrhs):
+    import torch
+
+    from tmv_gb300 import linalg
+
+    rng = np.random.default_rng(50 + n)
+    a = rng.standard_normal((n, n))
+    lu_o, p_o = oracle_lu(orc, a)
+    b = rng.standard_normal((n, nrhs))
+    w = rng.standard_normal((nrhs, n))
+    x_o = np.asfortranarray(b.copy())
+    orc.ldiveq(lu_o, p_o, x_o)
+    y_o = np.asfortranarray(w.copy())
+    orc.rdiveq(lu_o, p_o, y_o)
+    LU = to_dev(lu_o, dev, "F")
+    P = torch.from_numpy(p_o).to(dev)
+    X = to_dev(b, dev, "F")
+    linalg.lu_ldiveq(LU, P, X)
+    Y = to_dev(w, dev, "F")
+    linalg.lu_rdiveq(LU, P, Y)
+    torch.cuda.synchronize()
+    assert rel_frob(to_host(X), x_o) <= 1e-12
+    assert rel_frob(to_host(Y), y_o) <= 1e-12
+
+
+def test_config2_lu_solve_4096(dev, orc):
+    # FP64 LU factor + solve, n = 4096, N(0,1) + 4 sqrt(n) I, 8 RHS:
+    # pivots identical to the oracle, solution within 1e-12 relative error.
+    from tmv_gb300 import linalg
+
+    rng = np.random.default_rng(4096)
+    n = 4096
+    a = diag_shift_matrix(rng, n, 4 * np.sqrt(n))
+    b = rng.standard_normal((n, 8))
+    x_o, lu_o, p_o = orc.divide(np.asfortranarray(a), np.asfortranarray(b))
+    X, LU, P = linalg.divide(to_dev(a, dev, "F"), to_dev(b, dev, "F"))
+    assert np.array_equal(to_host(P), p_o)
+    assert rel_frob(to_host(X), x_o) <= 1e-12
+
+
+def test_singular_solve_raises(dev, orc):
+    import torch
+
+    from tmv_gb300 import SingularError, linalg
+
+    import oracle
+
+    n = 12
+    rng = np.random.default_rng(9)
+    a = rng.standard_normal((n, n))
+    a[:, 4] = 0.0  # U(4,4) = 0 after factorisation
+    lu_o, p_o = oracle_lu(orc, a)
+    b = rng.standard_normal((n, 2))
+    with pytest.raises(oracle.OracleSingular):
+        orc.ldiveq(lu_o, p_o, np.asfortranarray(b.copy()))
+    LU = to_dev(lu_o, dev, "F")
+    P = torch.from_numpy(p_o).to(dev)
+    with pytest.raises(SingularError):
+        linalg.lu_ldiveq(LU, P, to_dev(b, dev, "F"))
+    # and the context stays usable afterwards
+    X = to_dev(rng.standard_normal((n, 1)), dev, "F")
+    a2 = rng.standard_normal((n, n))
+    lu2, p2 = gpu_lu(dev, a2)
+    linalg.lu_ldiveq(to_dev(lu2, dev, "F"), torch.from_numpy(p2).to(dev), X)
+
+
+def test_matrix_surface(dev, orc):
+    # the tmv::Matrix mirror: C = A*B, A.divideUsing(LU), X = B/A, Y = W%A
+    from tmv_gb300.matrix import LU, Matrix
+
+    rng = np.random.default_rng(21)
+    n = 150
+    a = rng.standard_normal((n, n))
+    b = rng.standard_normal((n, 4))
+    w = rng.standard_normal((3, n))
+    A = Matrix(a)
+    A.divideUsing(LU)
+    A.saveDiv()
+    X = Matrix(b) / A
+    Y = Matrix(w) % A
+    x_o, lu_o, p_o = orc.divide(np.asfortranarray(a), np.asfortranarray(b))
+    y_o = np.asfortranarray(w.copy())
+    orc.rdiveq(lu_o, p_o, y_o)
+    assert rel_frob(X.numpy(), x_o) <= 1e-12
+    assert rel_frob(Y.numpy(), y_o) <= 1e-12
+    assert np.array_equal(A.lud().getP(), p_o)
+    Cm = A * Matrix(b)
+    assert rel_frob(Cm.numpy(), a @ b) <= 1e-13

@@ -27,8 +27,14 @@
 namespace tmvg {
 
 constexpr int kPanelThreads = 256;
-constexpr int kPanelMax = 64;  // largest panel width
-constexpr int kTriBlock = 64;  // diagonal block of the blocked triangular solves
+constexpr int kPanelMax = 128;  // largest panel width (scratch layout)
+constexpr int kTriBlock = 64;   // diagonal block of the blocked triangular solves
+
+// Panel width: 64 columns in FP64, 128 in FP32 (same shared-memory
+// footprint, 256 rows x ~33 KB per CTA; wider FP32 panels halve the number
+// of trailing updates and so the trailing-matrix traffic).
+template <typename T>
+constexpr int panel_width() { return sizeof(T) == 8 ? 64 : 128; }
 
 // ---------------------------------------------------------------------
 // Columns that TMV factors as the second column of a two-column leaf of its
@@ -243,8 +249,12 @@ tri_diag_kernel(int w, const T* __restrict__ tri, int64_t tsi, int64_t tsj, bool
                 bool unit, int64_t nrhs, T* __restrict__ B, int64_t bsi, int64_t bsj,
                 bool skip_zero, int* err)
 {
-    __shared__ T Ts[kTriBlock][kTriBlock + 1];
-    __shared__ T Xs[kTriBlock][kTriCols + 1];
+    // dynamic shared memory: Ts[w][w+1] then Xs[w][kTriCols+1]
+    extern __shared__ __align__(16) unsigned char tri_smem[];
+    T* Tsb = reinterpret_cast<T*>(tri_smem);
+    T* Xsb = Tsb + w * (w + 1);
+#define Ts(i, j) Tsb[(i) * (w + 1) + (j)]
+#define Xs(i, j) Xsb[(i) * (kTriCols + 1) + (j)]
     const int tid = threadIdx.x;
     const int64_t c0 = (int64_t)blockIdx.x * kTriCols;
     const int ncb = (int)min((int64_t)kTriCols, nrhs - c0);
@@ -252,17 +262,17 @@ tri_diag_kernel(int w, const T* __restrict__ tri, int64_t tsi, int64_t tsj, bool
     for (int t = tid; t < w * w; t += kTriCols) {
         const int i = t % w, j = t / w;
         const bool need = upper ? (j >= i) : (i >= j);
-        Ts[i][j] = need ? tri[i * tsi + j * tsj] : T(0);
+        Ts(i, j) = need ? tri[i * tsi + j * tsj] : T(0);
     }
     if (bsi == 1) {
         for (int t = tid; t < w * ncb; t += kTriCols) {
             const int i = t % w, cl = t / w;
-            Xs[i][cl] = B[i + (c0 + cl) * bsj];
+            Xs(i, cl) = B[i + (c0 + cl) * bsj];
         }
     } else {
         for (int t = tid; t < w * ncb; t += kTriCols) {
             const int cl = t % ncb, i = t / ncb;
-            Xs[i][cl] = B[i * bsi + (c0 + cl) * bsj];
+            Xs(i, cl) = B[i * bsi + (c0 + cl) * bsj];
         }
     }
     __syncthreads();
@@ -271,10 +281,10 @@ tri_diag_kernel(int w, const T* __restrict__ tri, int64_t tsi, int64_t tsj, bool
         bool sing = false;
         if (!upper) {
             for (int i = 0; i < w; ++i) {
-                T s = Xs[i][tid];
-                for (int j = 0; j < i; ++j) s -= Ts[i][j] * Xs[j][tid];
+                T s = Xs(i, tid);
+                for (int j = 0; j < i; ++j) s -= Ts(i, j) * Xs(j, tid);
                 if (!unit) {
-                    const T d = Ts[i][i];
+                    const T d = Ts(i, i);
                     if (skip_zero) {
                         if (s != T(0)) {
                             if (d == T(0)) sing = true;
@@ -285,14 +295,14 @@ tri_diag_kernel(int w, const T* __restrict__ tri, int64_t tsi, int64_t tsj, bool
                         else s = s * (T(1) / d);
                     }
                 }
-                Xs[i][tid] = s;
+                Xs(i, tid) = s;
             }
         } else {
             for (int i = w - 1; i >= 0; --i) {
-                T s = Xs[i][tid];
-                for (int j = w - 1; j > i; --j) s -= Ts[i][j] * Xs[j][tid];
+                T s = Xs(i, tid);
+                for (int j = w - 1; j > i; --j) s -= Ts(i, j) * Xs(j, tid);
                 if (!unit) {
-                    const T d = Ts[i][i];
+                    const T d = Ts(i, i);
                     if (skip_zero) {
                         if (s != T(0)) {
                             if (d == T(0)) sing = true;
@@ -303,7 +313,7 @@ tri_diag_kernel(int w, const T* __restrict__ tri, int64_t tsi, int64_t tsj, bool
                         else s = s * (T(1) / d);
                     }
                 }
-                Xs[i][tid] = s;
+                Xs(i, tid) = s;
             }
         }
         if (sing) atomicCAS(err, (int)kDevOk, (int)kDevSingular);
@@ -312,15 +322,17 @@ tri_diag_kernel(int w, const T* __restrict__ tri, int64_t tsi, int64_t tsj, bool
     if (bsi == 1) {
         for (int t = tid; t < w * ncb; t += kTriCols) {
             const int i = t % w, cl = t / w;
-            B[i + (c0 + cl) * bsj] = Xs[i][cl];
+            B[i + (c0 + cl) * bsj] = Xs(i, cl);
         }
     } else {
         for (int t = tid; t < w * ncb; t += kTriCols) {
             const int cl = t % ncb, i = t / ncb;
-            B[i * bsi + (c0 + cl) * bsj] = Xs[i][cl];
+            B[i * bsi + (c0 + cl) * bsj] = Xs(i, cl);
         }
     }
 }
+#undef Ts
+#undef Xs
 
 // ---------------------------------------------------------------------
 // Host drivers.
@@ -333,7 +345,11 @@ static tmvg_status launch_tri_diag(Context* c, int w, const T* tri, int64_t tsi,
     if (nrhs <= 0 || w <= 0) return TMVG_OK;
     const int64_t blocks = ceil_div(nrhs, kTriCols);
     if (blocks > INT_MAX) return set_error(c, TMVG_UNSUPPORTED, "tri solve: too many columns");
-    tri_diag_kernel<T><<<(unsigned)blocks, kTriCols, 0, c->stream>>>(
+    const size_t smem = sizeof(T) * ((size_t)w * (w + 1) + (size_t)w * (kTriCols + 1));
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(tri_diag_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(sizeof(T) * (kTriBlock * (kTriBlock + 1) + kTriBlock * (kTriCols + 1))));
+    tri_diag_kernel<T><<<(unsigned)blocks, kTriCols, smem, c->stream>>>(
         w, tri, tsi, tsj, upper, unit, nrhs, B, bsi, bsj, skip_zero, c->dflags);
     ++c->launches;
     return check_cuda(c, cudaGetLastError(), "tri_diag launch");
@@ -393,7 +409,7 @@ tmvg_status lu_factor(Context* c, int64_t n, T* A, int64_t lda, int64_t* P)
 {
     if (n < 0 || lda < std::max<int64_t>(n, 1)) return set_error(c, TMVG_BAD_ARG, "lu: bad n/lda");
     if (n == 0) return TMVG_OK;
-    const int nbmax = kPanelMax;
+    const int nbmax = panel_width<T>();
 
     // Panel geometry: one CTA per 256 rows up to one per SM.
     const int64_t G_full = std::min<int64_t>(c->num_sms, ceil_div(n, kPanelThreads));
@@ -406,8 +422,8 @@ tmvg_status lu_factor(Context* c, int64_t n, T* A, int64_t lda, int64_t* P)
     const size_t off_key = 0;
     const size_t off_idx = off_key + sizeof(double) * 2 * G_full;
     const size_t off_rows = (off_idx + sizeof(long long) * 2 * G_full + 255) & ~size_t(255);
-    const size_t off_diag = off_rows + sizeof(T) * 2 * G_full * nbmax;
-    const size_t off_modes = (off_diag + sizeof(T) * 2 * nbmax + 255) & ~size_t(255);
+    const size_t off_diag = off_rows + sizeof(T) * 2 * G_full * kPanelMax;
+    const size_t off_modes = (off_diag + sizeof(T) * 2 * kPanelMax + 255) & ~size_t(255);
     const size_t bytes = off_modes + (size_t)n;
     unsigned char* ws = (unsigned char*)workspace(c, bytes);
     if (!ws) return TMVG_OOM;
@@ -471,8 +487,8 @@ tmvg_status lu_factor(Context* c, int64_t n, T* A, int64_t lda, int64_t* P)
         }
         if (k + nb < n) {
             const int64_t rest = n - k - nb;
-            st = launch_tri_diag<T>(c, nb, A + k + k * lda, 1, lda, false, true, rest,
-                                    A + k + (k + nb) * lda, 1, lda, false);
+            st = tri_solve<T>(c, nb, A + k + k * lda, 1, lda, false, true, rest,
+                              A + k + (k + nb) * lda, 1, lda, false);
             if (st) return st;
             st = gemm<T>(c, rest, rest, nb, T(-1), Mat<const T>{A + (k + nb) + k * lda, 1, lda},
                          Mat<const T>{A + k + (k + nb) * lda, 1, lda}, T(1),
