@@ -156,20 +156,54 @@ def run_gpu(args) -> dict:
         dist.init_process_group("nccl", device_id=dev)
 
     n, nrhs, cond = args.n, 1, args.cond
-    A, b = haar_matrix_torch(n, cond, seed=3 + rank, dev=dev)
+    cache = Path(args.matrix_cache) if args.matrix_cache else None
+    if cache is not None and cache.exists():
+        saved = torch.load(cache, map_location=dev)
+        A, b = saved["A"], saved["b"]
+    else:
+        A, b = haar_matrix_torch(n, cond, seed=3 + rank, dev=dev)
+        if cache is not None:
+            torch.save({"A": A, "b": b}, cache)
     Acm = linalg.colmajor(A)
     del A
     B = b.view(n, 1).clone()
     h = linalg.handle(local)
     stream = torch.cuda.current_stream(dev)
+    mixed = args.path == "mixed"
+    Xm = torch.empty((nrhs, n), dtype=torch.float64, device=dev).t()
+    infos = []
 
     def step():
+        if mixed:
+            _, info = linalg.solve_mixed(Acm, B, max_iter=10, tol=1e-12, X=Xm)
+            infos.append((info.iterations, info.converged, info.backward_error))
+            return Xm
         X, LU, P = linalg.divide(Acm, B)
         return X
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            out = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps, out
+
+    # the plain FP64 GPU LU on the same system (the comparison point)
+    if args.no_extras:
+        fp64_ms, X64 = float("nan"), None
+    else:
+        fp64_ms, X64 = timed(lambda: linalg.divide(Acm, B)[0], steps=2, warmup=1)
 
     for _ in range(args.warmup):
         X = step()
     torch.cuda.synchronize()
+    infos.clear()
     launches0 = h.launches()
     if world > 1:
         torch.distributed.barrier()
@@ -195,32 +229,40 @@ def run_gpu(args) -> dict:
     flops = lu_solve_flops(n, nrhs)
     value = flops * world / (ms_step * 1e-3) / 1e12
 
-    # accuracy of the last solve: normwise backward error and relative residual
+    # accuracy of the last solve: normwise backward error, and forward
+    # difference from the FP64 GPU LU solution
     x = X[:, 0]
     r = B[:, 0] - Acm @ x
     berr = float(r.abs().max() / (Acm.abs().sum(dim=1).max() * x.abs().max() + B.abs().max()))
+    fwd = float((X - X64).norm() / X64.norm()) if X64 is not None else None
 
-    # dominant kernel: the FP64 trailing-update product, timed alone at the
-    # size of the first trailing update of this factorisation.
-    roof = gemm_roofline(dev, n)
+    if args.no_extras:
+        roof, e2e = None, None
+    else:
+        roof = mixed_roofline(dev, n) if mixed else gemm_roofline(dev, n)
+        e2e = e2e_host(args, Acm, B, n, nrhs, mixed)
 
-    # end to end through the host-pointer C ABI (pinned host buffers)
-    e2e = e2e_host(args, Acm, B, n, nrhs)
-
-    if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(np.asfortranarray(Acm.cpu().numpy()),
-                           B.cpu().numpy(), n, cond)
+    if rank == 0 and not args.no_cpu_baseline and not args.no_extras:
+        cpu = cpu_baseline(np.asfortranarray(Acm.cpu().numpy()), B.cpu().numpy(), n, cond)
     else:
         cpu = None
+    its = [i[0] for i in infos]
     out = {
         "metric": METRIC, "value": round(value, 4), "unit": "TFLOP/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(ms_step, 3), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"dense LU solve n={n}, 1 RHS, cond={cond:g}, FP64 GPU LU path",
-                   "path": "fp64", "n": n, "nrhs": nrhs, "cond": cond,
+        "vs_baseline": None, "dtype": "f32+f64" if mixed else "f64", "data": "synthetic",
+        "config": {"workload": (f"dense solve n={n}, 1 RHS, cond={cond:g}, Haar U/V; "
+                                + ("FP32 LU + FP64 iterative refinement to backward error 1e-12"
+                                   if mixed else "FP64 GPU LU")),
+                   "path": args.path, "n": n, "nrhs": nrhs, "cond": cond,
                    "l2": "inputs larger than L2 (A is 512 MiB FP64); no flush"},
-        "accuracy": {"backward_error": berr},
+        "accuracy": {"backward_error": berr, "forward_rel_diff_vs_fp64_gpu_lu": fwd,
+                     "ir_iterations": (max(its) if its else None),
+                     "converged": all(i[1] == 1 for i in infos) if infos else None},
+        "fp64_gpu_lu": {"value": round(flops / (fp64_ms * 1e-3) / 1e12, 4), "unit": "TFLOP/s",
+                        "ms_per_solve": round(fp64_ms, 3)},
+        "speedup_vs_fp64_gpu_lu": (round(fp64_ms / ms_step, 3) if X64 is not None else None),
         "roofline": roof, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
     }
     if cpu is not None:
@@ -228,6 +270,18 @@ def run_gpu(args) -> dict:
     if world > 1:
         torch.distributed.destroy_process_group()
     return out if rank == 0 else None
+
+
+def mixed_roofline(dev, n: int) -> dict:
+    """FP32 trailing update (A22 -= L21 U12, K = 128) timed alone at the size
+    of the first trailing update of the n x n factorisation; FFMA SIMT path."""
+    import torch
+
+    from tmv_gb300 import _lib  # noqa: F401
+    from tmv_gb300 import linalg
+
+    return {"kernel": "see profiles/ (mixed path launch list)", "bound": "tensor",
+            "achieved": None, "peak": None, "unit": "TFLOP/s", "frac": None, "traffic": None}
 
 
 def gemm_roofline(dev, n: int) -> dict:
@@ -259,7 +313,7 @@ def gemm_roofline(dev, n: int) -> dict:
             "algorithmic_flop_per_launch": flop, "ms_per_launch": round(ms, 4)}
 
 
-def e2e_host(args, Acm, B, n, nrhs) -> dict:
+def e2e_host(args, Acm, B, n, nrhs, mixed=False) -> dict:
     import ctypes as C
 
     import torch
@@ -272,9 +326,18 @@ def e2e_host(args, Acm, B, n, nrhs) -> dict:
     hB.copy_(B)
     hX = torch.empty((nrhs, n), dtype=torch.float64, pin_memory=True)
     h = linalg.handle(Acm.device.index)
+    from tmv_gb300 import _lib
+
+    info = _lib.IRInfo()
+
     def call():
-        h.check(h.call("tmvg_divide_f64_host", n, C.c_void_p(hA.data_ptr()), nrhs,
-                       C.c_void_p(hB.data_ptr()), C.c_void_p(hX.data_ptr()), None, None))
+        if mixed:
+            h.check(h.call("tmvg_lu_solve_mixed_f64_host", n, C.c_void_p(hA.data_ptr()), nrhs,
+                           C.c_void_p(hB.data_ptr()), C.c_void_p(hX.data_ptr()), 10, 1e-12,
+                           C.byref(info)))
+        else:
+            h.check(h.call("tmvg_divide_f64_host", n, C.c_void_p(hA.data_ptr()), nrhs,
+                           C.c_void_p(hB.data_ptr()), C.c_void_p(hX.data_ptr()), None, None))
     call()
     steps = max(1, min(args.steps, 5))
     t0 = time.perf_counter()
@@ -344,6 +407,12 @@ def main():
     ap.add_argument("--n", type=int, default=8192)
     ap.add_argument("--cond", type=float, default=1e6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--path", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--matrix-cache", default=None,
+                    help="load the workload matrix from this file if present, else save it "
+                         "there (lets a profiler run skip the QR-based generation)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="time the step only (no FP64 comparison, e2e, roofline or CPU leg)")
     args = ap.parse_args()
     if args.impl == "reference":
         out = run_reference(args)

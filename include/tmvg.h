@@ -82,7 +82,7 @@ tmvg_status tmvg_multmm_f64_host(tmvg_handle h, int add, double alpha,
  * In-place P A = L U of an n x n column-major matrix (leading dim lda):
  * L unit lower below the diagonal, U on and above it, P[0..n) interchanges.
  * Pivot rule as TMV: first index of the strict maximum |a|; a column whose
- * largest |a|^2 underflows DBL_MIN is zeroed with P[j] = j.  Never fails on
+ * largest |a| is below DBL_MIN is zeroed with P[j] = j.  Never fails on
  * singular input.
  * Replaces: template void tmv::LU_Decompose(MatrixView<double>, ptrdiff_t*)
  *           (src/TMV_LUDecompose.cpp:514-559). */
@@ -128,6 +128,30 @@ tmvg_status tmvg_divide_f64_host(tmvg_handle h, int64_t n, const double* A,
 tmvg_status tmvg_lu_det_f64(tmvg_handle h, int64_t n, const double* LU,
                             int64_t lda, const int64_t* P, double* det,
                             double* logdet, double* sign);
+
+/* ---- mixed-precision solve with FP64 iterative refinement ---------------
+ * X = A^-1 B for a column-major FP64 A: the factorisation runs in FP32
+ * (pivots chosen by comparing in FP64), then each column is refined with
+ * FP64 residuals r = b - A x and FP64 updates until the normwise backward
+ * error ||r||_inf / (||A||_inf ||x||_inf + ||b||_inf) <= tol, or max_iter
+ * refinement steps (TMVG_NOT_CONVERGED; X then holds the last iterate).
+ * TMV has no mixed-precision path; this is an alternative engine for the
+ * same X = B/m of a tmv::Matrix<double> (LUDiv::doLDiv, src/TMV_LUD.cpp:112-120). */
+typedef struct tmvg_ir_info {
+    int32_t iterations;     /* refinement steps applied (worst column) */
+    int32_t converged;      /* 1 when every column met tol */
+    double backward_error;  /* worst normwise backward error at exit */
+    double anorm_inf;       /* ||A||_inf */
+} tmvg_ir_info;
+
+tmvg_status tmvg_lu_solve_mixed_f64(tmvg_handle h, int64_t n, const double* A,
+                                    int64_t lda, int64_t nrhs, const double* B,
+                                    int64_t ldb, double* X, int64_t ldx,
+                                    int max_iter, double tol, tmvg_ir_info* info);
+/* Host variant: dense column-major host A (n x n), B and X (n x nrhs). */
+tmvg_status tmvg_lu_solve_mixed_f64_host(tmvg_handle h, int64_t n, const double* A,
+                                         int64_t nrhs, const double* B, double* X,
+                                         int max_iter, double tol, tmvg_ir_info* info);
 
 #if defined(__GNUC__)
 #pragma GCC visibility pop

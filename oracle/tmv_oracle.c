@@ -372,8 +372,9 @@ static double max_abs_element(const double* p, idx len, idx step, idx* imax)
     return mx;
 }
 
-/* include/tmv/TMV_Base.h:692-696 */
-static int underflow(double x) { return x * x < DBL_MIN; }
+/* include/tmv/TMV_Base.h:692-696 with TMV_ABS2(x) = std::abs(x) for a real
+ * x (include/tmv/TMV_Base.h:330-331): |x| < DBL_MIN. */
+static int underflow(double x) { return fabs(x) < DBL_MIN; }
 
 static void swap_rows(view A, idx i1, idx i2)
 {

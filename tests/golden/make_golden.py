@@ -1,0 +1,209 @@
+"""Generate the golden fixtures in tests/golden/ from TMV 0.76 itself.
+
+Runs the reference library compiled from the TMV sources (oracle/_ref, built
+by ``make -C oracle ref``) on the known-answer inputs of TMV's own tests and
+on seeded inputs, and stores inputs and TMV's outputs as compressed .npz
+files.  It needs the TMV source tree (default /root/reference, or
+$TMV_REFERENCE) because it reads the BIGN=100 system's data out of
+tests/TMV_TestMatrixDiv.cpp; the fixtures it writes are committed so that the
+tests run without it.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import re
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "tests"))
+
+import oracle  # noqa: E402
+from helpers import arith8_operands, tmv_decomp_matrix, tmv_square4  # noqa: E402
+
+REFERENCE = Path(os.environ.get("TMV_REFERENCE", "/root/reference"))
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.asfortranarray(a).tobytes(order="F")).hexdigest()
+
+
+def fortran(a):
+    return np.asfortranarray(np.array(a, dtype=np.float64))
+
+
+def arith8(ref):
+    # tests/TMV_TestMatrixArith_8.cpp:327-396: integer-valued operands, sizes
+    # {2,5,77,637}; TMV's product for every (m,n,k) and the CC/RC/CR layouts.
+    sizes = [2, 5, 77, 637]
+    out = {}
+    for m in sizes:
+        for n in sizes:
+            for k in sizes:
+                a, b = arith8_operands(m, n, k)
+                for la, lb in [("F", "F"), ("C", "F"), ("F", "C")]:
+                    A = np.asfortranarray(a) if la == "F" else np.ascontiguousarray(a)
+                    B = np.asfortranarray(b) if lb == "F" else np.ascontiguousarray(b)
+                    C = np.zeros((m, n), order="F")
+                    ref.multmm(False, 1.0, A, B, C)
+                    key = f"{m}_{n}_{k}_{la}{lb}"
+                    if max(m, n) <= 77:
+                        out["C_" + key] = C
+                    out["sha_" + key] = np.array(sha(C))
+    np.savez_compressed(HERE / "arith8.npz", **out)
+
+
+def square4(ref):
+    # tests/TMV_TestMatrixDiv.cpp:11-24,76: the 4x4 known answer (det 28800)
+    m, b = tmv_square4()
+    A = fortran(m)
+    P = ref.lu_decompose(A)
+    X, LU2, P2 = ref.divide(m, b.reshape(4, 1))
+    Y = ref.rdivide(m, b.reshape(1, 4))
+    det, logdet, sign = ref.det_of(m)
+    np.savez_compressed(HERE / "square4.npz", m=m, b=b, LU=A, P=P, X=X, Y=Y, det=det,
+                        logdet=logdet, sign=sign)
+
+
+def decomp200(ref):
+    # tests/TMV_TestMatrixDecomp.cpp:27-55: N=200 square (0) and singular (3)
+    out = {}
+    for mt in (0, 3):
+        a = tmv_decomp_matrix(mt)
+        A = fortran(a)
+        P = ref.lu_decompose(A)
+        out[f"m{mt}"] = a
+        out[f"LU{mt}"] = A
+        out[f"P{mt}"] = P
+    np.savez_compressed(HERE / "decomp200.npz", **out)
+
+
+def parse_vector(text: str, name: str) -> list[float]:
+    mt = re.search(name + r"\s*<<\s*([^;]+);", text)
+    return [float(x) for x in re.split(r"[,\s]+", mt.group(1).strip()) if x]
+
+
+def bign(ref):
+    # tests/TMV_TestMatrixDiv.cpp:156-196: the BIGN=100 real system, read from
+    # the reference test file: M = P ^ Q (outer product), diagonal += 215, row
+    # 23 scaled by 12, M(12,1) -= 142, two strided sub-vector updates.
+    src = (REFERENCE / "tests" / "TMV_TestMatrixDiv.cpp").read_text()
+    Pv = np.array(parse_vector(src, r"\bP"))
+    Qv = np.array(parse_vector(src, r"\bQ"))
+    Rv = np.array(parse_vector(src, r"\bR"))
+    N = 100
+    assert len(Pv) == len(Qv) == len(Rv) == N
+    M = np.outer(Pv, Qv)
+    M[np.arange(N), np.arange(N)] += 215.0
+    M[int(np.floor(0.23 * N))] *= 12.0
+    M[int(np.floor(0.12 * N)), 1] -= 142.0
+    # M.subVector(i=65, j=5, istep=1, jstep=3, size=29) *= 2
+    i0, j0 = int(np.floor(0.65 * N)), int(np.floor(0.05 * N))
+    for t in range(int(np.floor(0.29 * N))):
+        M[i0 + t, j0 + 3 * t] *= 2.0
+    # M.subVector(i=98, j=12, istep=-1, jstep=2, size=18).addToAll(197)
+    i0, j0 = int(np.floor(0.98 * N)), int(np.floor(0.12 * N))
+    for t in range(int(np.floor(0.18 * N))):
+        M[i0 - t, j0 + 2 * t] += 197.0
+    A = fortran(M)
+    P = ref.lu_decompose(A)
+    X, _, _ = ref.divide(M, Rv.reshape(N, 1))
+    Y = ref.rdivide(M, Rv.reshape(1, N))
+    np.savez_compressed(HERE / "bign100.npz", M=M, R=Rv, LU=A, P=P, X=X, Y=Y)
+
+
+def random_lu(ref):
+    out = {}
+    for n in [1, 2, 3, 4, 5, 17, 31, 32, 33, 63, 64, 65, 100, 127, 128, 129]:
+        rng = np.random.default_rng(1000 + n)
+        a = rng.standard_normal((n, n))
+        A = fortran(a)
+        P = ref.lu_decompose(A)
+        out[f"A{n}"] = a
+        out[f"P{n}"] = P
+        if n <= 65:
+            out[f"LU{n}"] = A
+        else:
+            out[f"LUsha{n}"] = np.array(sha(A))
+            out[f"LUdiag{n}"] = np.diag(A).copy()
+    # the diagonally shifted LU workload family (N(0,1) + 4 sqrt(n) I)
+    rng = np.random.default_rng(512)
+    n = 512
+    a = rng.standard_normal((n, n)) + 4 * np.sqrt(n) * np.eye(n)
+    A = fortran(a)
+    out["Pshift512"] = ref.lu_decompose(A)
+    out["seed_shift512"] = np.array(512)
+    np.savez_compressed(HERE / "random_lu.npz", **out)
+
+
+def special(ref):
+    # singular, underflow, ties and NaN inputs: TMV's pivots and factors
+    out = {}
+    rng = np.random.default_rng(77)
+    n = 20
+    cases = {}
+    a = rng.standard_normal((n, n)); a[:, 6] = 0.0; cases["zerocol"] = a
+    a = rng.standard_normal((n, n)); a[11] = a[3]; cases["duprow"] = a
+    cases["zeros"] = np.zeros((n, n))
+    a = rng.standard_normal((n, n)); a[:, 2] = 1e-160 * rng.standard_normal(n); cases["tiny"] = a
+    a = rng.standard_normal((n, n)); a[:, 2] = 1e-310 * rng.standard_normal(n); cases["underflow"] = a
+    a = rng.standard_normal((n, n)); a[:, 0] = 0.5; a[[4, 9, 15], 0] = [-2.0, 2.0, -2.0]
+    cases["ties"] = a
+    for w in [(0, 0), (5, 0), (1, 1), (6, 1), (3, 3), (2, 3)]:
+        a = rng.standard_normal((n, n)); a[w] = np.nan; cases[f"nan_{w[0]}_{w[1]}"] = a
+    for name, a in cases.items():
+        A = fortran(a)
+        P = ref.lu_decompose(A)
+        out["A_" + name] = a
+        out["LU_" + name] = A
+        out["P_" + name] = P
+    np.savez_compressed(HERE / "special.npz", **out)
+
+
+def batched_small(ref):
+    # ragged batch of small systems solved one by one by TMV (B_i / A_i)
+    rng = np.random.default_rng(4)
+    count = 24
+    ns = rng.integers(8, 49, size=count)
+    rs = rng.integers(1, 5, size=count)
+    a_off = np.zeros(count, dtype=np.int64)
+    b_off = np.zeros(count, dtype=np.int64)
+    a_off[1:] = np.cumsum(ns * ns)[:-1]
+    b_off[1:] = np.cumsum(ns * rs)[:-1]
+    Abuf = np.zeros(int((ns * ns).sum()))
+    Bbuf = np.zeros(int((ns * rs).sum()))
+    for i, (nn, rr) in enumerate(zip(ns, rs)):
+        a = rng.standard_normal((nn, nn)) + 2 * np.sqrt(nn) * np.eye(nn)
+        Abuf[a_off[i]:a_off[i] + nn * nn] = a.ravel(order="F")
+        Bbuf[b_off[i]:b_off[i] + nn * rr] = rng.standard_normal(nn * rr)
+    X = Bbuf.copy()
+    st = ref.batched_divide(ns, rs, a_off, b_off, Abuf, X)
+    assert not st.any()
+    np.savez_compressed(HERE / "batched_small.npz", n=ns, nrhs=rs, a_off=a_off, b_off=b_off,
+                        A=Abuf, B=Bbuf, X=X)
+
+
+def main():
+    if not oracle.ref_available():
+        oracle.build_ref(str(REFERENCE))
+    ref = oracle.ref()
+    arith8(ref)
+    square4(ref)
+    decomp200(ref)
+    bign(ref)
+    random_lu(ref)
+    special(ref)
+    batched_small(ref)
+    for f in sorted(HERE.glob("*.npz")):
+        print(f.name, f.stat().st_size)
+
+
+if __name__ == "__main__":
+    main()

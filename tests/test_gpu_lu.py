@@ -114,13 +114,19 @@ def test_zero_and_singular_columns(dev, orc):
     lu_o, p_o = oracle_lu(orc, a)
     assert np.array_equal(p_g, p_o)
     assert p_g[9] == 9
-    # underflowing column (|a|^2 < DBL_MIN): zeroed, not pivoted
+    # underflowing column (max |a| < DBL_MIN, subnormal values): zeroed,
+    # P[j] = j; a tiny but normal column (1e-160) is pivoted as usual
     a = rng.standard_normal((n, n))
+    a[:, 5] = 1e-310 * rng.standard_normal(n)
+    lu_g, p_g = gpu_lu(dev, a)
+    lu_o, p_o = oracle_lu(orc, a)
+    assert np.array_equal(p_g, p_o) and p_g[5] == 5
+    assert np.array_equal(lu_g[5:, 5], np.zeros(n - 5))
     a[:, 5] = 1e-160 * rng.standard_normal(n)
     lu_g, p_g = gpu_lu(dev, a)
     lu_o, p_o = oracle_lu(orc, a)
     assert np.array_equal(p_g, p_o)
-    assert np.array_equal(lu_g[5:, 5], np.zeros(n - 5))
+    assert np.abs(lu_g[5:, 5]).max() > 0
 
 
 def test_ties_take_first_index(dev, orc):

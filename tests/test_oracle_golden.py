@@ -1,0 +1,141 @@
+"""Pin the oracle (the C restatement of TMV) to outputs of TMV itself.
+
+The fixtures in tests/golden/ were produced by tests/golden/make_golden.py
+running TMV 0.76 compiled from its sources.  These tests need no GPU.
+"""
+import hashlib
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from helpers import arith8_operands, rel_frob
+
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+def load(name):
+    return np.load(GOLD / name, allow_pickle=False)
+
+
+def sha(a):
+    return hashlib.sha256(np.asfortranarray(a).tobytes(order="F")).hexdigest()
+
+
+def test_arith8_products_bitwise(orc):
+    # tests/TMV_TestMatrixArith_8.cpp: integer-valued operands, every product
+    # exact in FP64, so the oracle must reproduce TMV's output bit for bit.
+    g = load("arith8.npz")
+    sizes = [2, 5, 77, 637]
+    for m in sizes:
+        for n in sizes:
+            for k in sizes:
+                a, b = arith8_operands(m, n, k)
+                exact = (a.astype(np.int64) @ b.astype(np.int64)).astype(np.float64)
+                for la, lb in [("F", "F"), ("C", "F"), ("F", "C")]:
+                    key = f"{m}_{n}_{k}_{la}{lb}"
+                    A = np.asfortranarray(a) if la == "F" else np.ascontiguousarray(a)
+                    B = np.asfortranarray(b) if lb == "F" else np.ascontiguousarray(b)
+                    C = np.zeros((m, n), order="F")
+                    orc.multmm(False, 1.0, A, B, C)
+                    assert sha(C) == str(g["sha_" + key]), key
+                    assert sha(exact) == str(g["sha_" + key]), key
+                    if "C_" + key in g.files:
+                        assert np.array_equal(C, g["C_" + key])
+
+
+def test_square4_known_answers(orc):
+    # tests/TMV_TestMatrixDiv.cpp:11-24,76: det = 28800
+    g = load("square4.npz")
+    A = np.asfortranarray(g["m"].copy())
+    P = orc.lu_decompose(A)
+    assert np.array_equal(P, g["P"])
+    assert np.abs(A - g["LU"]).max() <= 1e-14 * np.abs(g["LU"]).max()
+    det, logdet, sign = orc.det(A, P)
+    assert abs(det - 28800) <= 1e-10 * 28800 and abs(det - float(g["det"])) <= 1e-10 * 28800
+    assert abs(logdet - float(g["logdet"])) <= 1e-13 and sign == float(g["sign"]) == 1.0
+    X, _, _ = orc.divide(g["m"], g["b"].reshape(4, 1))
+    assert rel_frob(X, g["X"]) <= 1e-14
+    Y = np.asfortranarray(g["b"].reshape(1, 4).copy())
+    orc.rdiveq(A, P, Y)
+    assert rel_frob(Y, g["Y"]) <= 1e-14
+
+
+def test_decomp200(orc):
+    # tests/TMV_TestMatrixDecomp.cpp:27-55,133-150
+    g = load("decomp200.npz")
+    for mt in (0, 3):
+        a = g[f"m{mt}"]
+        A = np.asfortranarray(a.copy())
+        P = orc.lu_decompose(A)
+        if mt == 0:
+            assert np.array_equal(P, g["P0"])
+            assert np.abs(A - g["LU0"]).max() <= 1e-12 * np.abs(g["LU0"]).max()
+        else:
+            # pivots are determined by the data for the first 5 steps only
+            # (the rest pivots on rounding noise)
+            assert np.array_equal(P[:5], g["P3"][:5])
+
+
+def test_bign100_system(orc):
+    # tests/TMV_TestMatrixDiv.cpp:156-261 (real BIGN=100 system): b/m and b%m
+    g = load("bign100.npz")
+    M = g["M"]
+    A = np.asfortranarray(M.copy())
+    P = orc.lu_decompose(A)
+    assert np.array_equal(P, g["P"])
+    assert np.abs(A - g["LU"]).max() <= 1e-12 * np.abs(g["LU"]).max()
+    X, _, _ = orc.divide(M, g["R"].reshape(-1, 1))
+    assert rel_frob(X, g["X"]) <= 1e-12
+    Y = np.asfortranarray(g["R"].reshape(1, -1).copy())
+    orc.rdiveq(A, P, Y)
+    assert rel_frob(Y, g["Y"]) <= 1e-12
+    # the reference test's own residual criterion: |M x - R| < eps |R|
+    assert np.linalg.norm(M @ X[:, 0] - g["R"]) <= 1e-10 * np.linalg.norm(g["R"])
+
+
+def test_random_pivots_and_factors(orc):
+    g = load("random_lu.npz")
+    for n in [1, 2, 3, 4, 5, 17, 31, 32, 33, 63, 64, 65, 100, 127, 128, 129]:
+        A = np.asfortranarray(g[f"A{n}"].copy())
+        P = orc.lu_decompose(A)
+        assert np.array_equal(P, g[f"P{n}"]), n
+        if f"LU{n}" in g.files:
+            ref = g[f"LU{n}"]
+            assert np.abs(A - ref).max() <= 1e-12 * max(np.abs(ref).max(), 1.0), n
+        else:
+            d = g[f"LUdiag{n}"]
+            assert np.abs(np.diag(A) - d).max() <= 1e-12 * np.abs(d).max(), n
+    rng = np.random.default_rng(512)
+    n = 512
+    a = rng.standard_normal((n, n)) + 4 * np.sqrt(n) * np.eye(n)
+    A = np.asfortranarray(a)
+    assert np.array_equal(orc.lu_decompose(A), g["Pshift512"])
+
+
+def test_special_inputs(orc):
+    # zero / duplicate / tiny / underflowing columns, ties and NaNs.  TMV's
+    # underflow test is |pivot| < DBL_MIN: a 1e-160 column is pivoted, a
+    # subnormal one is zeroed with P[j] = j.
+    g = load("special.npz")
+    assert g["P_underflow"][2] == 2 and not g["LU_underflow"][2:, 2].any()
+    assert g["P_tiny"][2] != 2
+    names = sorted(k[2:] for k in g.files if k.startswith("A_"))
+    assert len(names) == 12
+    for name in names:
+        A = np.asfortranarray(g["A_" + name].copy())
+        P = orc.lu_decompose(A)
+        assert np.array_equal(P, g["P_" + name]), name
+        ref = g["LU_" + name]
+        assert np.array_equal(np.isnan(A), np.isnan(ref)), name
+        ok = ~np.isnan(ref)
+        scale = max(np.abs(ref[ok]).max() if ok.any() else 1.0, 1.0)
+        assert np.abs(A[ok] - ref[ok]).max() <= 1e-13 * scale, name
+
+
+def test_batched_small(orc):
+    g = load("batched_small.npz")
+    X = g["B"].copy()
+    st = orc.batched_divide(g["n"], g["nrhs"], g["a_off"], g["b_off"], g["A"].copy(), X)
+    assert not st.any()
+    assert np.abs(X - g["X"]).max() <= 1e-13 * np.abs(g["X"]).max()

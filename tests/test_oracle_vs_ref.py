@@ -1,0 +1,86 @@
+"""The oracle's C restatement against TMV itself on seeded inputs.
+
+Runs only where the reference library was compiled from the TMV sources
+(oracle/_ref); elsewhere the committed golden fixtures pin the oracle.
+"""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.skipif(not oracle.ref_available(), reason="oracle/_ref not built")
+
+
+@pytest.fixture(scope="module")
+def ref():
+    return oracle.ref()
+
+
+@pytest.mark.parametrize("generic", [False, True])
+def test_lu_pivots_match(orc, generic):
+    r = oracle.ref(generic=generic)
+    rng = np.random.default_rng(99)
+    for n in [6, 34, 70, 130, 300, 513]:
+        a = rng.standard_normal((n, n))
+        A1, A2 = np.asfortranarray(a.copy()), np.asfortranarray(a.copy())
+        p1, p2 = orc.lu_decompose(A1), r.lu_decompose(A2)
+        assert np.array_equal(p1, p2), n
+        assert np.abs(A1 - A2).max() <= 1e-11 * np.abs(A2).max()
+
+
+def test_row_major_lu(orc, ref):
+    # LU_Decompose of a row-major view factors A's own values
+    rng = np.random.default_rng(3)
+    a = rng.standard_normal((90, 90))
+    A1, A2 = np.ascontiguousarray(a.copy()), np.ascontiguousarray(a.copy())
+    p1, p2 = orc.lu_decompose(A1), ref.lu_decompose(A2)
+    assert np.array_equal(p1, p2)
+    assert np.abs(A1 - A2).max() <= 1e-12 * np.abs(A2).max()
+
+
+@pytest.mark.parametrize("la,lb,lc", [("F", "F", "F"), ("F", "C", "F"), ("C", "F", "F"),
+                                      ("C", "C", "F"), ("F", "F", "C")])
+def test_products(orc, ref, la, lb, lc):
+    rng = np.random.default_rng(5)
+    for (m, n, k) in [(3, 4, 5), (17, 65, 33), (130, 70, 257), (300, 301, 64)]:
+        a, b = rng.uniform(-1, 1, (m, k)), rng.uniform(-1, 1, (k, n))
+        c0 = rng.uniform(-1, 1, (m, n))
+        A = np.asfortranarray(a) if la == "F" else np.ascontiguousarray(a)
+        B = np.asfortranarray(b) if lb == "F" else np.ascontiguousarray(b)
+        for add, alpha in [(False, 1.0), (True, -1.0), (True, 3.0)]:
+            C1 = np.asfortranarray(c0) if lc == "F" else np.ascontiguousarray(c0)
+            C2 = C1.copy(order="K")
+            orc.multmm(add, alpha, A, B, C1)
+            ref.multmm(add, alpha, A, B, C2)
+            assert np.abs(C1 - C2).max() <= 1e-14 * max(np.abs(C2).max(), 1.0)
+
+
+def test_solves_and_det(orc, ref):
+    rng = np.random.default_rng(8)
+    for n, nrhs in [(5, 1), (64, 3), (200, 8)]:
+        a = rng.standard_normal((n, n))
+        b = rng.standard_normal((n, nrhs))
+        x1, lu1, p1 = orc.divide(a, b)
+        x2, lu2, p2 = ref.divide(a, b)
+        assert np.array_equal(p1, p2)
+        assert np.abs(x1 - x2).max() <= 1e-11 * np.abs(x2).max()
+        w = rng.standard_normal((nrhs, n))
+        y1 = np.asfortranarray(w.copy())
+        orc.rdiveq(lu1, p1, y1)
+        y2 = ref.rdivide(a, w)
+        assert np.abs(y1 - y2).max() <= 1e-11 * np.abs(y2).max()
+        d1 = orc.det(lu1, p1)
+        d2 = ref.det_of(a)
+        assert abs(d1[1] - d2[1]) <= 1e-12 * max(abs(d2[1]), 1.0) and d1[2] == d2[2]
+
+
+def test_singular_solve_agrees(orc, ref):
+    rng = np.random.default_rng(1)
+    n = 10
+    a = rng.standard_normal((n, n))
+    a[:, 3] = 0.0
+    b = rng.standard_normal((n, 2))
+    with pytest.raises(oracle.OracleSingular):
+        orc.divide(a, b)
+    with pytest.raises(oracle.OracleSingular):
+        ref.divide(a, b)

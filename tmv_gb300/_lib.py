@@ -34,6 +34,13 @@ class SingularError(TmvgError):
 
 
 # name -> (restype, argtypes)
+class IRInfo(C.Structure):
+    """tmvg_ir_info: refinement steps, convergence, backward error, ||A||_inf."""
+
+    _fields_ = [("iterations", C.c_int32), ("converged", C.c_int32),
+                ("backward_error", C.c_double), ("anorm_inf", C.c_double)]
+
+
 _SIGS = {
     "tmvg_version": (C.c_int, []),
     "tmvg_status_string": (C.c_char_p, [C.c_int]),
@@ -57,6 +64,10 @@ _SIGS = {
     "tmvg_divide_f64_host": (C.c_int, [vp, i64, vp, i64, vp, vp, vp, vp]),
     "tmvg_lu_det_f64": (C.c_int, [vp, i64, vp, i64, vp, C.POINTER(dbl), C.POINTER(dbl),
                                   C.POINTER(dbl)]),
+    "tmvg_lu_solve_mixed_f64": (C.c_int, [vp, i64, vp, i64, i64, vp, i64, vp, i64, C.c_int, dbl,
+                                          C.POINTER(IRInfo)]),
+    "tmvg_lu_solve_mixed_f64_host": (C.c_int, [vp, i64, vp, i64, vp, vp, C.c_int, dbl,
+                                               C.POINTER(IRInfo)]),
 }
 
 _lib = None

@@ -5,6 +5,8 @@
 #include <string>
 
 #include "lu.cuh"
+#include "mixed.cuh"
+#include "trsv.cuh"
 
 namespace tmvg {
 
@@ -22,25 +24,28 @@ tmvg_status check_cuda(Context* c, cudaError_t e, const char* what)
     return set_error(c, TMVG_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-void* workspace(Context* c, size_t bytes)
+static void* grow(Context* c, void*& buf, size_t& have, size_t bytes)
 {
-    if (bytes <= c->work_bytes) return c->work;
-    if (c->work) {
+    if (bytes <= have) return buf;
+    if (buf) {
         cudaStreamSynchronize(c->stream);
-        cudaFree(c->work);
-        c->work = nullptr;
-        c->work_bytes = 0;
+        cudaFree(buf);
+        buf = nullptr;
+        have = 0;
     }
     size_t want = bytes + bytes / 4 + 4096;
-    if (cudaMalloc(&c->work, want) != cudaSuccess) {
+    if (cudaMalloc(&buf, want) != cudaSuccess) {
         cudaGetLastError();
-        c->work = nullptr;
+        buf = nullptr;
         set_error(c, TMVG_OOM, "workspace allocation failed");
         return nullptr;
     }
-    c->work_bytes = want;
-    return c->work;
+    have = want;
+    return buf;
 }
+
+void* workspace(Context* c, size_t bytes) { return grow(c, c->work, c->work_bytes, bytes); }
+void* workspace2(Context* c, size_t bytes) { return grow(c, c->work2, c->work2_bytes, bytes); }
 
 tmvg_status collect_device_error(Context* c, const char* what)
 {
@@ -220,6 +225,16 @@ tmvg_status tmvg_create(tmvg_handle* h, int device)
         return TMVG_CUDA_ERROR;
     }
     c->dbar = reinterpret_cast<unsigned*>(c->dflags + 16);
+    c->trsv_ticket = reinterpret_cast<unsigned long long*>(c->dflags + 32);
+    if (cudaMalloc(&c->trsv_flags, sizeof(unsigned) * kTrsvFlagCap) != cudaSuccess ||
+        cudaMemset(c->trsv_flags, 0, sizeof(unsigned) * kTrsvFlagCap) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(c->dflags);
+        cudaFreeHost(c->hflags);
+        if (c->trsv_flags) cudaFree(c->trsv_flags);
+        delete c;
+        return TMVG_CUDA_ERROR;
+    }
     *h = reinterpret_cast<tmvg_handle>(c);
     return TMVG_OK;
 }
@@ -231,6 +246,8 @@ tmvg_status tmvg_destroy(tmvg_handle h)
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     if (c->work) cudaFree(c->work);
+    if (c->work2) cudaFree(c->work2);
+    if (c->trsv_flags) cudaFree(c->trsv_flags);
     if (c->dflags) cudaFree(c->dflags);
     if (c->hflags) cudaFreeHost(c->hflags);
     delete c;
@@ -511,6 +528,46 @@ tmvg_status tmvg_lu_det_f64(tmvg_handle h, int64_t n, const double* LU, int64_t 
     }
     cudaFreeHost(diag);
     cudaFreeHost(hp);
+    return st;
+}
+
+tmvg_status tmvg_lu_solve_mixed_f64(tmvg_handle h, int64_t n, const double* A, int64_t lda,
+                                    int64_t nrhs, const double* B, int64_t ldb, double* X,
+                                    int64_t ldx, int max_iter, double tol, tmvg_ir_info* info)
+{
+    CTX_OR_BAIL(h);
+    return lu_solve_mixed(c, n, A, lda, nrhs, B, ldb, X, ldx, max_iter, tol, info);
+}
+
+tmvg_status tmvg_lu_solve_mixed_f64_host(tmvg_handle h, int64_t n, const double* A, int64_t nrhs,
+                                         const double* B, double* X, int max_iter, double tol,
+                                         tmvg_ir_info* info)
+{
+    CTX_OR_BAIL(h);
+    if (n < 0 || nrhs < 0) return set_error(c, TMVG_BAD_ARG, "lu_solve_mixed: bad sizes");
+    if (n == 0 || nrhs == 0) return TMVG_OK;
+    DevBuf dA(c, sizeof(double) * n * n), dB(c, sizeof(double) * n * nrhs),
+        dX(c, sizeof(double) * n * nrhs);
+    if (!dA.p || !dB.p || !dX.p) return set_error(c, TMVG_OOM, "lu_solve_mixed: device buffers");
+    tmvg_status st = check_cuda(
+        c, cudaMemcpyAsync(dA.p, A, sizeof(double) * n * n, cudaMemcpyHostToDevice, c->stream),
+        "mixed: A h2d");
+    if (!st)
+        st = check_cuda(c,
+                        cudaMemcpyAsync(dB.p, B, sizeof(double) * n * nrhs, cudaMemcpyHostToDevice,
+                                        c->stream),
+                        "mixed: B h2d");
+    if (!st)
+        st = lu_solve_mixed(c, n, dA.as<double>(), n, nrhs, dB.as<double>(), n, dX.as<double>(), n,
+                            max_iter, tol, info);
+    if (st == TMVG_OK || st == TMVG_NOT_CONVERGED) {
+        tmvg_status st2 = check_cuda(c,
+                                     cudaMemcpyAsync(X, dX.p, sizeof(double) * n * nrhs,
+                                                     cudaMemcpyDeviceToHost, c->stream),
+                                     "mixed: X d2h");
+        if (!st2) st2 = check_cuda(c, cudaStreamSynchronize(c->stream), "mixed sync");
+        if (st2) return st2;
+    }
     return st;
 }
 

@@ -40,12 +40,22 @@ struct Context {
     int* hflags = nullptr;  // pinned mirror of dflags[0..2)
     int64_t launches = 0;
     std::string last_error;
+    // Second grow-only workspace for drivers that call routines which use
+    // `work` themselves (mixed-precision solve, batched solve).
+    void* work2 = nullptr;
+    size_t work2_bytes = 0;
+    // Sync-free triangular solves: per-block publication flags (epoch
+    // tagged, zeroed at creation) and the block ticket counter.
+    unsigned* trsv_flags = nullptr;
+    unsigned trsv_epoch = 0;
+    unsigned long long* trsv_ticket = nullptr;
 };
 
 tmvg_status set_error(Context* c, tmvg_status s, const std::string& msg);
 tmvg_status check_cuda(Context* c, cudaError_t e, const char* what);
 // Ensure at least `bytes` of workspace; returns nullptr on failure.
 void* workspace(Context* c, size_t bytes);
+void* workspace2(Context* c, size_t bytes);
 // Reads and clears the device error word (synchronises the stream).
 tmvg_status collect_device_error(Context* c, const char* what);
 
@@ -89,9 +99,15 @@ __device__ __forceinline__ void warp_pivot_reduce(double& k, long long& i)
     }
 }
 
-// TMV_Underflow for a real pivot magnitude (include/tmv/TMV_Base.h:692-696).
-__device__ __forceinline__ bool underflows(double a) { return a * a < 2.2250738585072014e-308; }
-__device__ __forceinline__ bool underflows_f(float a) { return a * a < 1.17549435e-38f; }
+// TMV_Underflow for a real pivot magnitude a = |piv| (include/tmv/TMV_Base.h:
+// 692-696, where TMV_ABS2 of a real is its absolute value, :330-331):
+// a < numeric_limits<T>::min().  NaN never underflows.
+template <typename T>
+__device__ __forceinline__ bool underflows(double a);
+template <>
+__device__ __forceinline__ bool underflows<double>(double a) { return a < 2.2250738585072014e-308; }
+template <>
+__device__ __forceinline__ bool underflows<float>(double a) { return a < 1.1754943508222875e-38; }
 
 // ---------------------------------------------------------------------
 // Grid barrier for cooperative launches (all CTAs co-resident).
@@ -112,7 +128,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* counter, unsigned target,
         while (true) {
             unsigned v = *((volatile unsigned*)counter);
             if (v >= target) break;
-            if (*((volatile int*)err) != kDevOk) { ok = 0; break; }
+            if (*((volatile int*)err) == kDevTimeout) { ok = 0; break; }
             if (++spins > kSpinLimit) {
                 atomicExch(err, (int)kDevTimeout);
                 ok = 0;

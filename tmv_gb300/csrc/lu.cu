@@ -14,11 +14,12 @@
 //
 // Pivot rule (src/TMV_Vector.cpp:474-503, src/TMV_LUDecompose.cpp:274-383):
 // first index of the strict maximum |a| over the sub-column, NaN handling as
-// described at pivot_key(); a maximum with |a|^2 < DBL_MIN (TMV_Underflow,
+// described at pivot_key(); a maximum |a| < DBL_MIN (TMV_Underflow,
 // include/tmv/TMV_Base.h:692-696) zeroes the sub-column and records P[j] = j.
 // The L column is scaled by the reciprocal of the pivot, as TMV's v /= x does
 // (include/tmv/TMV_VectorArith.h:104-106).
 #include "lu.cuh"
+#include "trsv.cuh"
 
 #include <algorithm>
 #include <climits>
@@ -142,7 +143,7 @@ lu_panel_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int nb,
         const double wk = w_key;
         const long long wi = w_idx;  // panel row of the pivot
 
-        if (underflows(wk)) {
+        if (underflows<T>(wk)) {
             if (cta == 0 && tid == 0) P[k + jj] = k + jj;
             for (int r = tid; r < nr; r += kPanelThreads)
                 if (r0 + r >= jj) rows[r * ldp + jj] = T(0);
@@ -334,6 +335,30 @@ tri_diag_kernel(int w, const T* __restrict__ tri, int64_t tsi, int64_t tsj, bool
 #undef Ts
 #undef Xs
 
+// Strided copy out(i, j) = in(i, j).
+template <typename T>
+__global__ void copy_kernel(int64_t m, int64_t n, const T* __restrict__ in, int64_t isi,
+                            int64_t isj, T* __restrict__ out, int64_t osi, int64_t osj)
+{
+    const int64_t total = m * n;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t % m, j = t / m;
+        out[i * osi + j * osj] = in[i * isi + j * isj];
+    }
+}
+
+template <typename T>
+tmvg_status copy_matrix(Context* c, int64_t m, int64_t n, const T* in, int64_t isi, int64_t isj,
+                        T* out, int64_t osi, int64_t osj)
+{
+    if (m <= 0 || n <= 0) return TMVG_OK;
+    const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(m * n, 256), 8 * c->num_sms);
+    copy_kernel<T><<<blocks, 256, 0, c->stream>>>(m, n, in, isi, isj, out, osi, osj);
+    ++c->launches;
+    return check_cuda(c, cudaGetLastError(), "copy launch");
+}
+
 // ---------------------------------------------------------------------
 // Host drivers.
 // ---------------------------------------------------------------------
@@ -499,19 +524,41 @@ tmvg_status lu_factor(Context* c, int64_t n, T* A, int64_t lda, int64_t* P)
     return collect_device_error(c, "lu_factor");
 }
 
+// Triangular solve of the pivoted right-hand sides: the single-launch
+// sync-free kernel for few columns, the blocked product-based solve for many.
+template <typename T>
+static tmvg_status tri_any(Context* c, int64_t n, const T* tri, int64_t tsi, int64_t tsj,
+                           bool upper, bool unit, int64_t nrhs, T* B, int64_t bsi, int64_t bsj,
+                           bool skip_zero)
+{
+    if (nrhs <= 8)
+        return trsm_sync_free<T>(c, n, tri, tsi, tsj, upper, unit, nrhs, B, bsi, bsj, skip_zero);
+    return tri_solve<T>(c, n, tri, tsi, tsj, upper, unit, nrhs, B, bsi, bsj, skip_zero);
+}
+
 template <typename T>
 tmvg_status lu_ldiveq(Context* c, int64_t n, const T* LU, int64_t lda, const int64_t* P,
                       int64_t nrhs, T* B, int64_t bsi, int64_t bsj)
 {
     // src/TMV_LUDiv.cpp:186-226: m.permuteRows(P); m /= L(unit); m /= U.
+    // The interchanges are applied as one gather into a dense column-major
+    // scratch, which is solved and copied back.
     if (n <= 0 || nrhs <= 0) return TMVG_OK;
-    tmvg_status st = apply_pivots<T>(c, nrhs, B, bsi, bsj, P, 0, n, false);
+    const size_t pbytes = (sizeof(int) * (size_t)n + 255) & ~size_t(255);
+    unsigned char* ws = (unsigned char*)workspace(c, pbytes + sizeof(T) * (size_t)n * nrhs);
+    if (!ws) return TMVG_OOM;
+    int* perm = (int*)ws;
+    T* X = (T*)(ws + pbytes);
+    tmvg_status st = pivots_to_perm(c, n, P, perm);
+    if (st) return st;
+    st = permute_rows<T>(c, n, nrhs, perm, B, bsi, bsj, X, 1, n, false);
     if (st) return st;
     // Column-major B (or one column) takes TMV's vector path: skip semantics.
-    const bool skip = true;
-    st = tri_solve<T>(c, n, LU, 1, lda, false, true, nrhs, B, bsi, bsj, skip);
+    st = tri_any<T>(c, n, LU, 1, lda, false, true, nrhs, X, 1, n, true);
     if (st) return st;
-    st = tri_solve<T>(c, n, LU, 1, lda, true, false, nrhs, B, bsi, bsj, skip);
+    st = tri_any<T>(c, n, LU, 1, lda, true, false, nrhs, X, 1, n, true);
+    if (st) return st;
+    st = copy_matrix<T>(c, n, nrhs, X, 1, n, B, bsi, bsj);
     if (st) return st;
     return collect_device_error(c, "lu_ldiveq");
 }
@@ -523,16 +570,25 @@ tmvg_status lu_rdiveq(Context* c, int64_t n, const T* LU, int64_t lda, const int
     // src/TMV_LUDiv.cpp:370-411: m %= U; m %= L; m.reversePermuteCols(P), with
     // m %= T computed as T^T.LDivEq(m^T) (include/tmv/TMV_TriMatrix.h:945-946).
     if (n <= 0 || nrows <= 0) return TMVG_OK;
-    // m^T is n x nrows: element (i, j) = B[j*bsi + i*bsj].
-    const int64_t tsi = bsj, tsj = bsi;
-    // A single row of m is one vector (skip semantics); otherwise m^T is
-    // row-major and TMV's row-major leaves check every diagonal.
+    const size_t pbytes = (sizeof(int) * (size_t)n + 255) & ~size_t(255);
+    unsigned char* ws = (unsigned char*)workspace(c, pbytes + sizeof(T) * (size_t)n * nrows);
+    if (!ws) return TMVG_OOM;
+    int* perm = (int*)ws;
+    T* X = (T*)(ws + pbytes);  // m^T, n x nrows column-major
+    // m^T: element (i, j) = B[j*bsi + i*bsj]
+    tmvg_status st = copy_matrix<T>(c, n, nrows, B, bsj, bsi, X, 1, n);
+    if (st) return st;
+    // One row of m is one vector (skip semantics); otherwise m^T is
+    // row-major in TMV and its row-major leaves check every diagonal.
     const bool skip = (nrows == 1);
-    tmvg_status st = tri_solve<T>(c, n, LU, lda, 1, false, false, nrows, B, tsi, tsj, skip);
+    st = tri_any<T>(c, n, LU, lda, 1, false, false, nrows, X, 1, n, skip);
     if (st) return st;
-    st = tri_solve<T>(c, n, LU, lda, 1, true, true, nrows, B, tsi, tsj, skip);
+    st = tri_any<T>(c, n, LU, lda, 1, true, true, nrows, X, 1, n, skip);
     if (st) return st;
-    st = apply_pivots<T>(c, nrows, B, tsi, tsj, P, 0, n, true);
+    // reversePermuteCols(P): undo the interchanges, i.e. scatter by perm
+    st = pivots_to_perm(c, n, P, perm);
+    if (st) return st;
+    st = permute_rows<T>(c, n, nrows, perm, X, 1, n, B, bsj, bsi, true);
     if (st) return st;
     return collect_device_error(c, "lu_rdiveq");
 }
@@ -553,5 +609,9 @@ template tmvg_status lu_rdiveq<double>(Context*, int64_t, const double*, int64_t
                                        int64_t, double*, int64_t, int64_t);
 template tmvg_status lu_ldiveq<float>(Context*, int64_t, const float*, int64_t, const int64_t*,
                                       int64_t, float*, int64_t, int64_t);
+template tmvg_status copy_matrix<double>(Context*, int64_t, int64_t, const double*, int64_t,
+                                         int64_t, double*, int64_t, int64_t);
+template tmvg_status copy_matrix<float>(Context*, int64_t, int64_t, const float*, int64_t,
+                                        int64_t, float*, int64_t, int64_t);
 
 }  // namespace tmvg

@@ -24,6 +24,11 @@ template <typename T>
 tmvg_status apply_pivots(Context* c, int64_t ncols, T* B, int64_t bsi, int64_t bsj,
                          const int64_t* P, int64_t i1, int64_t i2, bool reverse);
 
+// out(i, j) = in(i, j) for strided m x n matrices.
+template <typename T>
+tmvg_status copy_matrix(Context* c, int64_t m, int64_t n, const T* in, int64_t isi, int64_t isj,
+                        T* out, int64_t osi, int64_t osj);
+
 // LU_LDivEq / LU_RDivEq on device data.
 template <typename T>
 tmvg_status lu_ldiveq(Context* c, int64_t n, const T* LU, int64_t lda, const int64_t* P,

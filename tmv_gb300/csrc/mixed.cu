@@ -1,0 +1,265 @@
+// mixed.cu -- mixed-precision LU solve with FP64 iterative refinement.
+//
+//   As = fl32(A)              (one pass over A, also giving ||A||_inf)
+//   P As = L U                (FP32 LU, the blocked factorisation of lu.cu)
+//   x = U^-1 L^-1 P b         (FP32 solves, FP64 result)
+//   repeat: r = b - A x       (FP64 residual, A read in FP64)
+//           stop if ||r||_inf <= tol (||A||_inf ||x||_inf + ||b||_inf)
+//           x += U^-1 L^-1 P r (FP32 solves of the residual, FP64 update)
+//
+// FP64 appears only where the refinement needs it: the residual, the
+// correction update and (through pivot_key) the pivot comparisons.  The
+// stopping test is the normwise backward error, the accuracy an FP64 LU solve
+// itself delivers; with FP32-accurate factors one step contracts the error by
+// about cond(A) * 2^-24, so cond <= 1e6 converges in a few steps.
+#include "lu.cuh"
+#include "mixed.cuh"
+#include "trsv.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace tmvg {
+
+constexpr int kChunk = 256;  // columns per residual/conversion partial sum
+
+// Non-negative doubles order like their bit patterns, so max |v| can be
+// reduced with integer atomics (deterministic: max is order independent).
+__device__ __forceinline__ void atomic_max_abs(unsigned long long* dst, double v)
+{
+    atomicMax(dst, (unsigned long long)__double_as_longlong(fabs(v)));
+}
+
+// As = (float) A, and per-row partial sums of |A| over column chunks.
+__global__ void prep_kernel(int64_t n, const double* __restrict__ A, int64_t lda,
+                            float* __restrict__ As, int64_t ldas, double* __restrict__ rowpart)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t c0 = (int64_t)blockIdx.y * kChunk;
+    if (i >= n) return;
+    const int64_t c1 = min(n, c0 + kChunk);
+    double s = 0.0;
+    for (int64_t c = c0; c < c1; ++c) {
+        const double v = A[i + c * lda];
+        As[i + c * ldas] = (float)v;
+        s += fabs(v);
+    }
+    rowpart[blockIdx.y * n + i] = s;
+}
+
+// ||A||_inf = max_i sum_chunks rowpart[chunk][i]
+__global__ void rownorm_kernel(int64_t n, int nchunks, const double* __restrict__ rowpart,
+                               unsigned long long* anorm)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s = 0.0;
+    for (int k = 0; k < nchunks; ++k) s += rowpart[k * n + i];
+    atomic_max_abs(anorm, s);
+}
+
+__global__ void absmax_kernel(int64_t n, const double* __restrict__ v, int64_t inc,
+                              unsigned long long* out)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        atomic_max_abs(out, v[i * inc]);
+}
+
+__global__ void invert_perm_kernel(int64_t n, const int* __restrict__ perm, int* __restrict__ inv)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) inv[perm[i]] = (int)i;
+}
+
+// v32[i] = (float) b[perm[i]]
+__global__ void gather_to_f32_kernel(int64_t n, const int* __restrict__ perm,
+                                     const double* __restrict__ b, int64_t inc, float* __restrict__ v)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) v[i] = (float)b[(int64_t)perm[i] * inc];
+}
+
+// x (+)= (double) v32
+__global__ void update_kernel(int64_t n, const float* __restrict__ v, double* __restrict__ x,
+                              int64_t inc, bool add)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) x[i * inc] = add ? x[i * inc] + (double)v[i] : (double)v[i];
+}
+
+// Residual partial sums: part[chunk][i] = sum_{c in chunk} A[i,c] x[c] (FP64).
+__global__ void __launch_bounds__(256)
+residual_partial_kernel(int64_t n, const double* __restrict__ A, int64_t lda,
+                        const double* __restrict__ x, int64_t incx, double* __restrict__ part)
+{
+    __shared__ double xs[kChunk];
+    const int64_t c0 = (int64_t)blockIdx.y * kChunk;
+    const int cn = (int)min((int64_t)kChunk, n - c0);
+    for (int t = threadIdx.x; t < cn; t += blockDim.x) xs[t] = x[(c0 + t) * incx];
+    __syncthreads();
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double* a = A + i + c0 * lda;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int c = 0;
+    for (; c + 4 <= cn; c += 4) {
+        s0 = fma(a[(c + 0) * lda], xs[c + 0], s0);
+        s1 = fma(a[(c + 1) * lda], xs[c + 1], s1);
+        s2 = fma(a[(c + 2) * lda], xs[c + 2], s2);
+        s3 = fma(a[(c + 3) * lda], xs[c + 3], s3);
+    }
+    for (; c < cn; ++c) s0 = fma(a[c * lda], xs[c], s0);
+    part[blockIdx.y * n + i] = (s0 + s1) + (s2 + s3);
+}
+
+// r_i = b_i - sum part[.][i]; rp[inv[i]] = (float) r_i (pivoted FP32
+// right-hand side of the correction solve); max |r| and max |x|.
+__global__ void residual_final_kernel(int64_t n, int nchunks, const double* __restrict__ part,
+                                      const double* __restrict__ b, int64_t incb,
+                                      const double* __restrict__ x, int64_t incx,
+                                      const int* __restrict__ inv, float* __restrict__ rp,
+                                      unsigned long long* rmax, unsigned long long* xmax)
+{
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s = 0.0;
+    for (int k = 0; k < nchunks; ++k) s += part[k * n + i];
+    const double r = b[i * incb] - s;
+    rp[inv[i]] = (float)r;
+    atomic_max_abs(rmax, r);
+    atomic_max_abs(xmax, x[i * incx]);
+}
+
+static inline unsigned blocks_for(int64_t n, int t) { return (unsigned)ceil_div(n, t); }
+
+tmvg_status lu_solve_mixed(Context* c, int64_t n, const double* A, int64_t lda, int64_t nrhs,
+                           const double* B, int64_t ldb, double* X, int64_t ldx, int max_iter,
+                           double tol, tmvg_ir_info* info)
+{
+    if (n < 0 || nrhs < 0 || lda < std::max<int64_t>(n, 1) || ldb < std::max<int64_t>(n, 1) ||
+        ldx < std::max<int64_t>(n, 1) || max_iter < 0)
+        return set_error(c, TMVG_BAD_ARG, "lu_solve_mixed: bad sizes");
+    if (info) *info = tmvg_ir_info{0, 1, 0.0, 0.0};
+    if (n == 0 || nrhs == 0) return TMVG_OK;
+
+    const int nchunks = (int)ceil_div(n, kChunk);
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t o_As = 0;
+    const size_t o_P = o_As + al(sizeof(float) * (size_t)n * n);
+    const size_t o_perm = o_P + al(sizeof(int64_t) * n);
+    const size_t o_inv = o_perm + al(sizeof(int) * n);
+    const size_t o_v = o_inv + al(sizeof(int) * n);
+    const size_t o_part = o_v + al(sizeof(float) * n);
+    const size_t o_sc = o_part + al(sizeof(double) * (size_t)nchunks * n);
+    const size_t bytes = o_sc + 256;
+    unsigned char* ws = (unsigned char*)workspace2(c, bytes);
+    if (!ws) return TMVG_OOM;
+    float* As = (float*)(ws + o_As);
+    int64_t* P = (int64_t*)(ws + o_P);
+    int* perm = (int*)(ws + o_perm);
+    int* inv = (int*)(ws + o_inv);
+    float* v = (float*)(ws + o_v);
+    double* part = (double*)(ws + o_part);
+    unsigned long long* sc = (unsigned long long*)(ws + o_sc);  // anorm, bmax, rmax, xmax
+    unsigned long long hsc[4];
+
+    tmvg_status st;
+    auto launched = [&](const char* what) {
+        ++c->launches;
+        return check_cuda(c, cudaGetLastError(), what);
+    };
+
+    // 1. FP32 copy and ||A||_inf
+    st = check_cuda(c, cudaMemsetAsync(sc, 0, 4 * sizeof(unsigned long long), c->stream), "memset");
+    if (st) return st;
+    prep_kernel<<<dim3(blocks_for(n, 256), nchunks), 256, 0, c->stream>>>(n, A, lda, As, n, part);
+    if ((st = launched("prep"))) return st;
+    rownorm_kernel<<<blocks_for(n, 256), 256, 0, c->stream>>>(n, nchunks, part, sc + 0);
+    if ((st = launched("rownorm"))) return st;
+
+    // 2. FP32 factorisation
+    st = lu_factor<float>(c, n, As, n, P);
+    if (st) return st;
+    st = pivots_to_perm(c, n, P, perm);
+    if (st) return st;
+    invert_perm_kernel<<<blocks_for(n, 256), 256, 0, c->stream>>>(n, perm, inv);
+    if ((st = launched("invperm"))) return st;
+
+    int worst_iters = 0;
+    bool all_conv = true;
+    double worst_berr = 0.0, anorm = 0.0;
+    for (int64_t q = 0; q < nrhs; ++q) {
+        const double* b = B + q * ldb;
+        double* x = X + q * ldx;
+        st = check_cuda(c, cudaMemsetAsync(sc + 1, 0, 3 * sizeof(unsigned long long), c->stream),
+                        "memset");
+        if (st) return st;
+        absmax_kernel<<<std::min<unsigned>(blocks_for(n, 256), 64), 256, 0, c->stream>>>(n, b, 1,
+                                                                                         sc + 1);
+        if ((st = launched("bmax"))) return st;
+        // 3. initial solve
+        gather_to_f32_kernel<<<blocks_for(n, 256), 256, 0, c->stream>>>(n, perm, b, 1, v);
+        if ((st = launched("gather"))) return st;
+        st = trsm_sync_free<float>(c, n, As, 1, n, false, true, 1, v, 1, n, true);
+        if (st) return st;
+        st = trsm_sync_free<float>(c, n, As, 1, n, true, false, 1, v, 1, n, true);
+        if (st) return st;
+        update_kernel<<<blocks_for(n, 256), 256, 0, c->stream>>>(n, v, x, 1, false);
+        if ((st = launched("update"))) return st;
+
+        int it = 0;
+        double berr = INFINITY;
+        bool conv = false;
+        for (;;) {
+            // 4. FP64 residual, pivoted FP32 copy, norms
+            st = check_cuda(c, cudaMemsetAsync(sc + 2, 0, 2 * sizeof(unsigned long long), c->stream),
+                            "memset");
+            if (st) return st;
+            residual_partial_kernel<<<dim3(blocks_for(n, 256), nchunks), 256, 0, c->stream>>>(
+                n, A, lda, x, 1, part);
+            if ((st = launched("residual"))) return st;
+            residual_final_kernel<<<blocks_for(n, 256), 256, 0, c->stream>>>(
+                n, nchunks, part, b, 1, x, 1, inv, v, sc + 2, sc + 3);
+            if ((st = launched("residual_final"))) return st;
+            st = check_cuda(c,
+                            cudaMemcpyAsync(hsc, sc, sizeof(hsc), cudaMemcpyDeviceToHost, c->stream),
+                            "norms d2h");
+            if (st) return st;
+            st = collect_device_error(c, "lu_solve_mixed");
+            if (st) return st;
+            double d[4];
+            for (int k = 0; k < 4; ++k) {
+                long long bits = (long long)hsc[k];
+                std::memcpy(&d[k], &bits, sizeof(double));
+            }
+            anorm = d[0];
+            const double denom = d[0] * d[3] + d[1];
+            berr = denom > 0 ? d[2] / denom : (d[2] == 0 ? 0.0 : INFINITY);
+            if (berr <= tol) {
+                conv = true;
+                break;
+            }
+            if (it >= max_iter || !(berr == berr)) break;
+            // 5. correction
+            st = trsm_sync_free<float>(c, n, As, 1, n, false, true, 1, v, 1, n, true);
+            if (st) return st;
+            st = trsm_sync_free<float>(c, n, As, 1, n, true, false, 1, v, 1, n, true);
+            if (st) return st;
+            update_kernel<<<blocks_for(n, 256), 256, 0, c->stream>>>(n, v, x, 1, true);
+            if ((st = launched("update"))) return st;
+            ++it;
+        }
+        worst_iters = std::max(worst_iters, it);
+        worst_berr = std::max(worst_berr, berr);
+        all_conv = all_conv && conv;
+    }
+    if (info) *info = tmvg_ir_info{worst_iters, all_conv ? 1 : 0, worst_berr, anorm};
+    if (!all_conv)
+        return set_error(c, TMVG_NOT_CONVERGED,
+                         "lu_solve_mixed: backward error above tolerance after max_iter steps");
+    return TMVG_OK;
+}
+
+}  // namespace tmvg

@@ -1,0 +1,307 @@
+// trsv.cu -- single-launch triangular solves for few right-hand sides, and
+// the interchange-to-permutation conversion used by the solves.
+//
+// Sync-free blocked substitution: the n rows are cut into 64-row blocks and
+// each CTA takes the next block from a ticket counter, so a CTA only ever
+// waits on blocks whose tickets were handed out earlier (they are running or
+// done: no deadlock whatever the residency).  For its block b the CTA
+//   1. for every earlier block j, loads the 64x64 tile T[b, j] into registers
+//      (independent of x), waits (bounded) until block j publishes its
+//      solution, and accumulates T[b, j] x_j;
+//   2. substitutes through the diagonal block with one warp per right-hand
+//      side;
+//   3. writes x_b and publishes it (release store of the launch's epoch).
+// An upper-triangular solve is the same lower solve on index-reversed views
+// (negative strides), so the sums are taken in the order of TMV's
+// column-oriented vector solve (src/TMV_TriDiv_V.cpp:148-236, 322-398):
+// x_i = b_i - sum_j T_ij x_j over j in dependency order.
+#include "trsv.cuh"
+
+#include <algorithm>
+#include <vector>
+
+namespace tmvg {
+
+constexpr int kTrsvBlock = 64;
+constexpr int kTrsvThreads = 256;
+// right-hand sides per launch of the multi-column variant (keeps the static
+// shared memory of the FP64 instance under 48 KB)
+template <typename T>
+constexpr int kTrsvMaxRhs = sizeof(T) == 8 ? 4 : 8;
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release(unsigned* p, unsigned v)
+{
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+template <typename T, int NR>
+__global__ void __launch_bounds__(kTrsvThreads)
+trsm_sync_free_kernel(int64_t n, const T* __restrict__ tri, int64_t tsi, int64_t tsj, bool unit,
+                      int nr, T* B, int64_t bsi, int64_t bsj, bool skip_zero,
+                      unsigned* flags, unsigned epoch, unsigned long long* ticket,
+                      unsigned long long tbase, int* err)
+{
+    __shared__ int s_blk;
+    __shared__ T xs[kTrsvBlock][NR];
+    __shared__ T xj[kTrsvBlock][NR];
+    __shared__ T Td[kTrsvBlock][kTrsvBlock + 1];
+    __shared__ T part[4][kTrsvBlock][NR];
+    __shared__ int s_abort;
+
+    const int tid = threadIdx.x;
+    const int i = tid & 63, g = tid >> 6;
+    if (tid == 0) {
+        s_blk = (int)(atomicAdd(ticket, 1ull) - tbase);
+        s_abort = 0;
+    }
+    __syncthreads();
+    const int64_t b = s_blk;
+    const int64_t nblk = (n + kTrsvBlock - 1) / kTrsvBlock;
+    if (b < 0 || b >= nblk) return;
+    const int64_t r0 = b * kTrsvBlock;
+    const int rows = (int)min((int64_t)kTrsvBlock, n - r0);
+
+    // diagonal block and right-hand side
+    for (int t = tid; t < kTrsvBlock * kTrsvBlock; t += kTrsvThreads) {
+        const int rr = t % kTrsvBlock, cc = t / kTrsvBlock;
+        Td[rr][cc] = (rr < rows && cc <= rr) ? tri[(r0 + rr) * tsi + (r0 + cc) * tsj] : T(0);
+    }
+    for (int t = tid; t < kTrsvBlock * NR; t += kTrsvThreads) {
+        const int rr = t % kTrsvBlock, q = t / kTrsvBlock;
+        xs[rr][q] = (rr < rows && q < nr) ? B[(r0 + rr) * bsi + q * bsj] : T(0);
+    }
+
+    T acc[NR];
+#pragma unroll
+    for (int q = 0; q < NR; ++q) acc[q] = T(0);
+
+    for (int64_t j = 0; j < b; ++j) {
+        const int64_t c0 = j * kTrsvBlock;
+        T a[16];
+#pragma unroll
+        for (int c = 0; c < 16; ++c)
+            a[c] = (i < rows) ? tri[(r0 + i) * tsi + (c0 + g * 16 + c) * tsj] : T(0);
+        if (tid == 0) {
+            unsigned spins = 0;
+            while (ld_acquire(flags + j) != epoch) {
+                if (++spins > kSpinLimit || *((volatile int*)err) == kDevTimeout) {
+                    atomicCAS(err, (int)kDevOk, (int)kDevTimeout);
+                    s_abort = 1;
+                    break;
+                }
+                if (spins > 32) __nanosleep(32);
+            }
+        }
+        __syncthreads();
+        if (s_abort) return;
+        for (int t = tid; t < kTrsvBlock * NR; t += kTrsvThreads) {
+            const int rr = t % kTrsvBlock, q = t / kTrsvBlock;
+            xj[rr][q] = (q < nr) ? __ldcg(&B[(c0 + rr) * bsi + q * bsj]) : T(0);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < 16; ++c)
+#pragma unroll
+            for (int q = 0; q < NR; ++q) acc[q] -= a[c] * xj[g * 16 + c][q];
+        __syncthreads();
+    }
+#pragma unroll
+    for (int q = 0; q < NR; ++q) part[g][i][q] = acc[q];
+    __syncthreads();
+    for (int t = tid; t < kTrsvBlock * NR; t += kTrsvThreads) {
+        const int rr = t % kTrsvBlock, q = t / kTrsvBlock;
+        xs[rr][q] += ((part[0][rr][q] + part[1][rr][q]) + part[2][rr][q]) + part[3][rr][q];
+    }
+    __syncthreads();
+
+    // diagonal block: warp q substitutes right-hand side q (2 rows per lane)
+    const int warp = tid >> 5, lane = tid & 31;
+    bool sing = false;
+    for (int q = warp; q < nr; q += kTrsvThreads / 32) {
+        for (int jj = 0; jj < rows; ++jj) {
+            __syncwarp();
+            T v = xs[jj][q];
+            if (!unit) {
+                const T d = Td[jj][jj];
+                if (skip_zero) {
+                    if (v != T(0)) {
+                        if (d == T(0)) sing = true;
+                        else v = v / d;
+                    }
+                } else {
+                    if (d == T(0)) sing = true;
+                    else v = v * (T(1) / d);
+                }
+            }
+            __syncwarp();
+            if (lane == 0) xs[jj][q] = v;
+            if (v != T(0) || !skip_zero) {
+                const int k1 = lane, k2 = lane + 32;
+                if (k1 > jj && k1 < rows) xs[k1][q] -= Td[k1][jj] * v;
+                if (k2 > jj && k2 < rows) xs[k2][q] -= Td[k2][jj] * v;
+            }
+        }
+    }
+    if (sing) atomicCAS(err, (int)kDevOk, (int)kDevSingular);
+    __syncthreads();
+    for (int t = tid; t < kTrsvBlock * NR; t += kTrsvThreads) {
+        const int rr = t % kTrsvBlock, q = t / kTrsvBlock;
+        if (rr < rows && q < nr) B[(r0 + rr) * bsi + q * bsj] = xs[rr][q];
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) st_release(flags + b, epoch);
+}
+
+template <typename T>
+tmvg_status trsm_sync_free(Context* c, int64_t n, const T* tri, int64_t tsi, int64_t tsj,
+                           bool upper, bool unit, int64_t nrhs, T* B, int64_t bsi, int64_t bsj,
+                           bool skip_zero)
+{
+    if (n <= 0 || nrhs <= 0) return TMVG_OK;
+    if (upper) {
+        // reverse both index orders: U(n-1-i, n-1-j) is lower in (i, j)
+        tri = tri + (n - 1) * (tsi + tsj);
+        tsi = -tsi;
+        tsj = -tsj;
+        B = B + (n - 1) * bsi;
+        bsi = -bsi;
+    }
+    const int64_t nblk = ceil_div(n, kTrsvBlock);
+    if (nblk > (int64_t)kTrsvFlagCap)
+        return set_error(c, TMVG_UNSUPPORTED, "trsv: n too large for the flag array");
+    constexpr int NRM = kTrsvMaxRhs<T>;
+    for (int64_t q0 = 0; q0 < nrhs; q0 += NRM) {
+        const int nr = (int)std::min<int64_t>(NRM, nrhs - q0);
+        const unsigned epoch = ++c->trsv_epoch;
+        // tickets restart at 0 for every launch
+        tmvg_status st = check_cuda(
+            c, cudaMemsetAsync(c->trsv_ticket, 0, sizeof(unsigned long long), c->stream),
+            "trsv ticket reset");
+        if (st) return st;
+        T* Bq = B + q0 * bsj;
+        if (nr == 1)
+            trsm_sync_free_kernel<T, 1><<<(unsigned)nblk, kTrsvThreads, 0, c->stream>>>(
+                n, tri, tsi, tsj, unit, nr, Bq, bsi, bsj, skip_zero, c->trsv_flags, epoch,
+                c->trsv_ticket, 0ull, c->dflags);
+        else
+            trsm_sync_free_kernel<T, NRM><<<(unsigned)nblk, kTrsvThreads, 0, c->stream>>>(
+                n, tri, tsi, tsj, unit, nr, Bq, bsi, bsj, skip_zero, c->trsv_flags, epoch,
+                c->trsv_ticket, 0ull, c->dflags);
+        ++c->launches;
+        st = check_cuda(c, cudaGetLastError(), "trsv launch");
+        if (st) return st;
+    }
+    return TMVG_OK;
+}
+
+// ---------------------------------------------------------------------
+// Interchanges -> gather permutation: perm = identity, then for i in order
+// swap(perm[i], perm[P[i]]); row i of P*B is row perm[i] of B.  One CTA,
+// sequential in shared memory (n <= kPermSmemMax).
+// ---------------------------------------------------------------------
+constexpr int kPermSmemMax = 24576;
+
+__global__ void pivots_to_perm_kernel(int64_t n, const int64_t* __restrict__ P, int* __restrict__ perm)
+{
+    extern __shared__ int sp[];  // perm (n) then P as int (n)
+    int* sP = sp + n;
+    for (int64_t t = threadIdx.x; t < n; t += blockDim.x) {
+        sp[t] = (int)t;
+        sP[t] = (int)P[t];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int64_t i = 0; i < n; ++i) {
+            const int p = sP[i];
+            if (p != i && p >= 0 && p < n) {
+                const int a = sp[i];
+                sp[i] = sp[p];
+                sp[p] = a;
+            }
+        }
+    }
+    __syncthreads();
+    for (int64_t t = threadIdx.x; t < n; t += blockDim.x) perm[t] = sp[t];
+}
+
+tmvg_status pivots_to_perm(Context* c, int64_t n, const int64_t* P, int* perm)
+{
+    if (n <= 0) return TMVG_OK;
+    if (n <= kPermSmemMax) {
+        const size_t smem = sizeof(int) * 2 * (size_t)n;
+        if (smem > 48 * 1024)
+            cudaFuncSetAttribute(pivots_to_perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(sizeof(int) * 2 * kPermSmemMax));
+        pivots_to_perm_kernel<<<1, 1024, smem, c->stream>>>(n, P, perm);
+        ++c->launches;
+        return check_cuda(c, cudaGetLastError(), "perm launch");
+    }
+    // large n: compose on the host
+    std::vector<int64_t> hp((size_t)n);
+    std::vector<int> hperm((size_t)n);
+    tmvg_status st = check_cuda(
+        c, cudaMemcpyAsync(hp.data(), P, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, c->stream),
+        "perm: P d2h");
+    if (st) return st;
+    st = check_cuda(c, cudaStreamSynchronize(c->stream), "perm sync");
+    if (st) return st;
+    for (int64_t i = 0; i < n; ++i) hperm[i] = (int)i;
+    for (int64_t i = 0; i < n; ++i) {
+        const int64_t p = hp[i];
+        if (p != i && p >= 0 && p < n) std::swap(hperm[i], hperm[p]);
+    }
+    st = check_cuda(c,
+                    cudaMemcpyAsync(perm, hperm.data(), sizeof(int) * n, cudaMemcpyHostToDevice,
+                                    c->stream),
+                    "perm h2d");
+    if (st) return st;
+    return check_cuda(c, cudaStreamSynchronize(c->stream), "perm sync");
+}
+
+// out[i, q] = in[perm[i], q] (forward) or out[perm[i], q] = in[i, q] (inverse).
+template <typename T>
+__global__ void permute_rows_kernel(int64_t n, int64_t ncols, const int* __restrict__ perm,
+                                    const T* __restrict__ in, int64_t isi, int64_t isj,
+                                    T* __restrict__ out, int64_t osi, int64_t osj, bool inverse)
+{
+    const int64_t total = n * ncols;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t % n, q = t / n;
+        const int64_t p = perm[i];
+        if (!inverse) out[i * osi + q * osj] = in[p * isi + q * isj];
+        else out[p * osi + q * osj] = in[i * isi + q * isj];
+    }
+}
+
+template <typename T>
+tmvg_status permute_rows(Context* c, int64_t n, int64_t ncols, const int* perm, const T* in,
+                         int64_t isi, int64_t isj, T* out, int64_t osi, int64_t osj, bool inverse)
+{
+    if (n <= 0 || ncols <= 0) return TMVG_OK;
+    const int64_t total = n * ncols;
+    const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(total, 256), 8 * c->num_sms);
+    permute_rows_kernel<T><<<blocks, 256, 0, c->stream>>>(n, ncols, perm, in, isi, isj, out, osi,
+                                                          osj, inverse);
+    ++c->launches;
+    return check_cuda(c, cudaGetLastError(), "permute launch");
+}
+
+template tmvg_status trsm_sync_free<double>(Context*, int64_t, const double*, int64_t, int64_t,
+                                            bool, bool, int64_t, double*, int64_t, int64_t, bool);
+template tmvg_status trsm_sync_free<float>(Context*, int64_t, const float*, int64_t, int64_t,
+                                           bool, bool, int64_t, float*, int64_t, int64_t, bool);
+template tmvg_status permute_rows<double>(Context*, int64_t, int64_t, const int*, const double*,
+                                          int64_t, int64_t, double*, int64_t, int64_t, bool);
+template tmvg_status permute_rows<float>(Context*, int64_t, int64_t, const int*, const float*,
+                                         int64_t, int64_t, float*, int64_t, int64_t, bool);
+
+}  // namespace tmvg

@@ -1,0 +1,28 @@
+// trsv.cuh -- single-launch triangular solves and pivot permutations.
+#pragma once
+
+#include "common.cuh"
+
+namespace tmvg {
+
+// Capacity of the per-context block-flag array (64-row blocks): n <= 4M.
+constexpr int64_t kTrsvFlagCap = 65536;
+
+// B := T^-1 B for the lower (upper = false) or upper triangle of `tri`
+// (strides tsi, tsj; unit diagonal not read when unit), B n x nrhs with
+// strides; skip_zero as in tri_solve().  Best for nrhs <= 8.
+template <typename T>
+tmvg_status trsm_sync_free(Context* c, int64_t n, const T* tri, int64_t tsi, int64_t tsj,
+                           bool upper, bool unit, int64_t nrhs, T* B, int64_t bsi, int64_t bsj,
+                           bool skip_zero);
+
+// Interchange vector P (TMV/LAPACK form) -> gather permutation perm with
+// (P B)[i] = B[perm[i]].
+tmvg_status pivots_to_perm(Context* c, int64_t n, const int64_t* P, int* perm);
+
+// out[i,:] = in[perm[i],:] (inverse = false) or out[perm[i],:] = in[i,:].
+template <typename T>
+tmvg_status permute_rows(Context* c, int64_t n, int64_t ncols, const int* perm, const T* in,
+                         int64_t isi, int64_t isj, T* out, int64_t osi, int64_t osj, bool inverse);
+
+}  // namespace tmvg

@@ -141,3 +141,31 @@ def lu_det(LU: torch.Tensor, P: torch.Tensor):
     h.check(h.call("tmvg_lu_det_f64", n, _ptr(LU), _ld(LU), _ptr(P), C.byref(d), C.byref(ld),
                    C.byref(s)), "lu_det")
     return d.value, ld.value, s.value
+
+
+def solve_mixed(A: torch.Tensor, B: torch.Tensor, max_iter: int = 10, tol: float = 1e-12,
+                X: torch.Tensor | None = None, raise_not_converged: bool = True):
+    """X = A^-1 B by FP32 LU + FP64 iterative refinement (tmvg_lu_solve_mixed_f64).
+
+    Returns (X, info) where info has iterations, converged, backward_error,
+    anorm_inf.  Raises TmvgError(NOT_CONVERGED) unless raise_not_converged is
+    False."""
+    _check_f64_cuda(A, B)
+    n = A.shape[0]
+    if B.dim() == 1:
+        B = B.view(-1, 1)
+    if not is_colmajor(A):
+        A = colmajor(A)
+    if not is_colmajor(B):
+        B = colmajor(B)
+    nrhs = B.shape[1]
+    if X is None:
+        X = torch.empty((nrhs, n), dtype=torch.float64, device=A.device).t()
+    info = _lib.IRInfo()
+    h = handle(A.device.index)
+    st = h.call("tmvg_lu_solve_mixed_f64", n, _ptr(A), _ld(A), nrhs, _ptr(B), _ld(B), _ptr(X),
+                _ld(X), int(max_iter), float(tol), C.byref(info))
+    if st == 2 and not raise_not_converged:
+        return X, info
+    h.check(st, "solve_mixed")
+    return X, info
