@@ -267,9 +267,89 @@ def run_gpu(args) -> dict:
     }
     if cpu is not None:
         out["cpu_baseline"] = cpu
+    if not args.no_extras and not args.no_batched:
+        out["batched"] = batched_bench(dev, args, with_cpu=(rank == 0 and not args.no_cpu_baseline))
     if world > 1:
         torch.distributed.destroy_process_group()
     return out if rank == 0 else None
+
+
+def batched_workload(count: int, seed: int = 4):
+    """Systems n_i ~ U{8..256}, nrhs_i ~ U{1..16}; A_i ~ N(0,1) + 2 sqrt(n_i) I,
+    B_i ~ N(0,1), packed column-major in order."""
+    rng = np.random.default_rng(seed)
+    n = rng.integers(8, 257, size=count).astype(np.int64)
+    r = rng.integers(1, 17, size=count).astype(np.int64)
+    return n, r
+
+
+def batched_bench(dev, args, with_cpu: bool) -> dict:
+    import torch
+
+    from tmv_gb300.batched import BatchPlan
+
+    count = args.batch_count
+    n, r = batched_workload(count)
+    plan = BatchPlan(n, r, tune=True)
+    g = torch.Generator(device=dev)
+    g.manual_seed(4)
+    A0 = torch.randn(plan.a_elems, dtype=torch.float64, device=dev, generator=g)
+    B0 = torch.randn(plan.b_elems, dtype=torch.float64, device=dev, generator=g)
+    # diagonal shift 2 sqrt(n_i)
+    idx = np.concatenate([plan.a_off[s] + np.arange(n[s]) * (n[s] + 1) for s in range(count)])
+    shift = np.repeat(2.0 * np.sqrt(n.astype(np.float64)), n)
+    A0[torch.from_numpy(idx).to(dev)] += torch.from_numpy(shift).to(dev)
+    A, B = A0.clone(), B0.clone()
+    P = torch.empty(plan.p_elems, dtype=torch.int64, device=dev)
+    st = torch.empty(count, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(max(args.warmup, 1)):
+        A.copy_(A0)
+        B.copy_(B0)
+        plan.solve(A, B, P, st)
+    total = 0.0
+    steps = max(args.steps, 1)
+    for _ in range(steps):
+        A.copy_(A0)
+        B.copy_(B0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        plan.solve(A, B, P, st)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        total += e0.elapsed_time(e1)
+    ms = total / steps
+    bad = int((st != 0).sum().item())
+    tflops = plan.flops / (ms * 1e-3) / 1e12
+    out = {"value": round(count / (ms * 1e-3), 1), "unit": "solves/s", "systems": count,
+           "ms_per_batch": round(ms, 3), "tflops_fp64": round(tflops, 4),
+           "roofline": {"kernel": "batched_lu_kernel (FP64 LU + solve, one persistent launch)",
+                        "bound": "fp64", "achieved": round(tflops, 4),
+                        "peak": FP64_DFMA_PEAK_TFLOPS, "unit": "TFLOP/s",
+                        "frac": round(tflops / FP64_DFMA_PEAK_TFLOPS, 4),
+                        "peak_source": "measured FP64 DFMA throughput",
+                        "algorithmic_flop_per_launch": plan.flops},
+           "panel_widths_by_class": plan.panel_widths, "singular_systems": bad,
+           "config": "n_i ~ U{8..256}, nrhs_i ~ U{1..16}, A_i ~ N(0,1) + 2 sqrt(n_i) I, FP64, "
+                     "CUDA graph replay, tiles from the autotuner"}
+    if with_cpu:
+        import oracle
+
+        orc = oracle.port()
+        cores = os.cpu_count() or 1
+        orc.set_threads(cores)
+        m = min(count, args.batch_cpu_sample)
+        hA = A0[: int(plan.a_off[m - 1] + n[m - 1] ** 2)].cpu().numpy()
+        hB = B0[: int(plan.b_off[m - 1] + n[m - 1] * r[m - 1])].cpu().numpy().copy()
+        t0 = time.perf_counter()
+        orc.batched_divide(n[:m], r[:m], plan.a_off[:m], plan.b_off[:m], hA, hB)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": round(m / dt, 1), "unit": "solves/s", "cores": cores,
+                               "kind": "port",
+                               "sample": f"first {m} systems of the batch, OpenMP over systems "
+                                         f"({dt:.2f} s)"}
+    plan.close()
+    return out
 
 
 def mixed_roofline(dev, n: int) -> dict:
@@ -411,6 +491,9 @@ def main():
     ap.add_argument("--matrix-cache", default=None,
                     help="load the workload matrix from this file if present, else save it "
                          "there (lets a profiler run skip the QR-based generation)")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batch-count", type=int, default=20000)
+    ap.add_argument("--batch-cpu-sample", type=int, default=2000)
     ap.add_argument("--no-extras", action="store_true",
                     help="time the step only (no FP64 comparison, e2e, roofline or CPU leg)")
     args = ap.parse_args()

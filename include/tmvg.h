@@ -153,6 +153,55 @@ tmvg_status tmvg_lu_solve_mixed_f64_host(tmvg_handle h, int64_t n, const double*
                                          int64_t nrhs, const double* B, double* X,
                                          int max_iter, double tol, tmvg_ir_info* info);
 
+/* ---- solve adjoint (forward / backward pair) ------------------------------
+ * Forward: X = A^-1 B (A column-major n x n, B n x nrhs), keeping the LU
+ * factors and interchanges for the backward (same work as tmvg_divide_f64).
+ * Backward, given G = dL/dX (n x nrhs) and the saved LU, P and X:
+ *   gB = dL/dB = A^-T G   -- the transpose solve with the saved factors,
+ *                            U^T then L^T then the reversed interchanges,
+ *                            i.e. TMV's (G^T % A)^T (LU_RDivEq,
+ *                            src/TMV_LUDiv.cpp:370-411);
+ *   gA = dL/dA = -gB X^T  -- an FP64 outer-product GEMM (K = nrhs).
+ * gB and gA are outputs (column-major, ldgb / ldga); either may be NULL to
+ * skip it (gA needs gB, which is then computed into scratch).  TMV has no
+ * adjoint; this pair has the contract of an autograd backward. */
+tmvg_status tmvg_lu_solve_fwd_f64(tmvg_handle h, int64_t n, const double* A, int64_t lda,
+                                  int64_t nrhs, const double* B, int64_t ldb, double* X,
+                                  int64_t ldx, double* LU, int64_t* P);
+tmvg_status tmvg_lu_solve_bwd_f64(tmvg_handle h, int64_t n, const double* LU, int64_t lda,
+                                  const int64_t* P, int64_t nrhs, const double* X,
+                                  int64_t ldx, const double* G, int64_t ldg, double* gB,
+                                  int64_t ldgb, double* gA, int64_t ldga);
+
+/* ---- batched uneven LU solves ---------------------------------------------
+ * Thousands of independent systems X_s = A_s^-1 B_s (1 <= n_s <= 256,
+ * 0 <= nrhs_s <= 16) factored and solved in FP64 by one persistent kernel
+ * launch, replayed from a CUDA graph captured when the plan is created.
+ * Layout: A_s column-major n_s x n_s at A + a_off[s], B_s column-major
+ * n_s x nrhs_s at B + b_off[s]; a_off/b_off NULL means packed in order.
+ * A_s is overwritten by its LU factors, B_s by X_s, the interchanges go to
+ * P + (n_0 + ... + n_{s-1}); status[s] = 1 where a zero U(j,j) met a
+ * nonzero (TMV's SingularUpperTriMatrix), else 0.  With tune_tiles the
+ * plan times the panel widths 8/16/32 on a sample of every size class
+ * (n <= 32, 64, 128, 256) and keeps the fastest.
+ * Replaces a loop of LUDiv<double> B_s / A_s (src/TMV_LUD.cpp:74-120). */
+typedef struct tmvg_batch_plan_s* tmvg_batch_plan;
+
+tmvg_status tmvg_batch_plan_create(tmvg_handle h, int64_t count, const int64_t* n,
+                                   const int64_t* nrhs, const int64_t* a_off,
+                                   const int64_t* b_off, int tune_tiles,
+                                   tmvg_batch_plan* plan);
+/* Buffer extents (elements), total algorithmic FLOPs
+ * (sum 2n^3/3 + 2n^2 nrhs) and the panel width per size class (4 ints). */
+tmvg_status tmvg_batch_plan_info(tmvg_batch_plan plan, int64_t* a_elems,
+                                 int64_t* b_elems, int64_t* p_elems, double* flops,
+                                 int* panel_widths);
+tmvg_status tmvg_batch_plan_set_tiles(tmvg_batch_plan plan, const int* panel_widths);
+/* Device pointers; synchronous. */
+tmvg_status tmvg_batched_lu_solve_f64(tmvg_batch_plan plan, double* A, double* B,
+                                      int64_t* P, int32_t* status);
+tmvg_status tmvg_batch_plan_destroy(tmvg_batch_plan plan);
+
 #if defined(__GNUC__)
 #pragma GCC visibility pop
 #endif

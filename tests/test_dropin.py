@@ -1,0 +1,71 @@
+"""The link-time drop-in under unmodified TMV (tmv_gb300/shim).
+
+Builds libtmv_gb300_dropin.so from the TMV sources where they are present
+(the build needs them) and checks that TMV's own entry points for real double
+data now come from the shim, that TMV's CPU code stays reachable under the
+renamed names for the other types, and that a program using only TMV's API
+links and reports a missing GPU through TMV's exception type.  No GPU needed.
+"""
+import os
+import subprocess
+from pathlib import Path
+
+import pytest
+
+import oracle
+
+ROOT = Path(__file__).resolve().parent.parent
+SHIM = ROOT / "tmv_gb300" / "shim"
+REF = Path(os.environ.get("TMV_REFERENCE", "/root/reference"))
+
+pytestmark = pytest.mark.skipif(not (REF / "src" / "TMV_MultMM.cpp").exists(),
+                                reason="TMV sources not present")
+
+
+@pytest.fixture(scope="module")
+def dropin():
+    from tmv_gb300.build import LIB, build_library
+
+    if not LIB.exists():
+        build_library()
+    if not oracle.ref_available():
+        oracle.build_ref(str(REF))
+    subprocess.run(["make", "-s", "-j8", "-C", str(SHIM), f"REF={REF}"], check=True)
+    return SHIM / "_build"
+
+
+def symbols(path, defined_only=True):
+    args = ["nm", "-C"] + (["--defined-only"] if defined_only else []) + [str(path)]
+    return subprocess.run(args, capture_output=True, text=True, check=True).stdout
+
+
+def test_double_entry_points_come_from_the_shim(dropin):
+    mm = symbols(dropin / "shim_multmm.o")
+    assert ("tmv::MultMM<false, double, double, double>(double, tmv::GenMatrix<double> const&, "
+            "tmv::GenMatrix<double> const&, tmv::MatrixView<double, 0>)") in mm
+    assert "tmv::MultMM<true, double, double, double>" in mm
+    lu = symbols(dropin / "shim_lu.o")
+    assert "tmv::LU_Decompose<double>(tmv::MatrixView<double, 0>, long*)" in lu
+    assert "tmv::LU_LDivEq<double, double>" in lu and "tmv::LU_RDivEq<double, double>" in lu
+    # the shim reaches the GPU only through the C ABI
+    undef = subprocess.run(["nm", "-u", str(dropin / "shim_multmm.o")], capture_output=True,
+                           text=True).stdout
+    assert "tmvg_multmm_f64_host" in undef
+
+
+def test_tmv_cpu_code_kept_under_renamed_entry_points(dropin):
+    cpu = symbols(dropin / "cpu_TMV_MultMM.o")
+    assert "tmv::TMVG_CPU_MultMM<false, std::complex<double>" in cpu
+    assert "tmv::MultMM<" not in cpu.replace("TMVG_CPU_MultMM<", "")
+    lib = symbols(dropin / "libtmv_gb300_dropin.so")
+    assert "tmv::TMVG_CPU_LU_Decompose<float>" in lib
+    assert "tmv::TMVG_CPU_LU_LDivEq<std::complex<double>, double>" in lib
+
+
+def test_unmodified_tmv_program_links_and_reports(dropin):
+    r = subprocess.run([str(dropin / "dropin_demo")], capture_output=True, text=True, timeout=120)
+    # without a GPU: TMV's Error carrying the C ABI's status; with one: 0
+    if r.returncode == 2:
+        assert "tmv::Error" in r.stdout and "tmvg_create" in r.stdout
+    else:
+        assert r.returncode == 0, r.stdout

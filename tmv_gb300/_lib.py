@@ -68,6 +68,15 @@ _SIGS = {
                                           C.POINTER(IRInfo)]),
     "tmvg_lu_solve_mixed_f64_host": (C.c_int, [vp, i64, vp, i64, vp, vp, C.c_int, dbl,
                                                C.POINTER(IRInfo)]),
+    "tmvg_lu_solve_fwd_f64": (C.c_int, [vp, i64, vp, i64, i64, vp, i64, vp, i64, vp, vp]),
+    "tmvg_lu_solve_bwd_f64": (C.c_int, [vp, i64, vp, i64, vp, i64, vp, i64, vp, i64, vp, i64,
+                                        vp, i64]),
+    "tmvg_batch_plan_create": (C.c_int, [vp, i64, vp, vp, vp, vp, C.c_int, C.POINTER(vp)]),
+    "tmvg_batch_plan_info": (C.c_int, [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64),
+                                       C.POINTER(dbl), C.POINTER(C.c_int)]),
+    "tmvg_batch_plan_set_tiles": (C.c_int, [vp, C.POINTER(C.c_int)]),
+    "tmvg_batched_lu_solve_f64": (C.c_int, [vp, vp, vp, vp, vp]),
+    "tmvg_batch_plan_destroy": (C.c_int, [vp]),
 }
 
 _lib = None

@@ -1,0 +1,600 @@
+// batched.cu -- thousands of uneven LU factor + solve problems in one
+// persistent launch (FP64), replayed from a captured CUDA graph.
+//
+// Layout: system s has order n[s] and nrhs[s] right-hand sides; A_s is the
+// column-major n x n block at A + a_off[s], B_s the column-major n x nrhs
+// block at B + b_off[s] (overwritten by X_s = A_s^-1 B_s), the pivots go to
+// P + p_off[s] and A_s is overwritten by its LU factors, as LU_Decompose and
+// LU_LDivEq do for one matrix (src/TMV_LUDecompose.cpp:514,
+// src/TMV_LUDiv.cpp:186).  status[s] = 1 when a zero U(j,j) met a nonzero
+// (TMV's SingularUpperTriMatrix), else 0.
+//
+// Kernel: grid = SMs x resident CTAs; each CTA repeatedly takes the next
+// system from an atomic queue over `order` (largest n first, so the tail of
+// the launch holds the small systems) and runs, for n <= 256:
+//   for each panel of PW columns:
+//     factor the panel in shared memory with TMV's pivot rule (pivot_key),
+//     apply its interchanges to the other columns of A_s and to B_s,
+//     U12 = L11^-1 A12 (one column per thread),
+//     A22 -= L21 U12 (4x4 register tiles, FP64 FMA),
+//   then forward/back substitution of B_s staged in shared memory.
+// FP64 FMA throughput (about 2 per SM per clock on GB300) bounds the kernel.
+// PW is chosen per size class by tune_batched().
+#include "batched.cuh"
+#include "lu.cuh"
+
+#include <algorithm>
+#include <chrono>
+#include <climits>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+namespace tmvg {
+
+constexpr int kBatchThreads = 256;
+constexpr int kBatchMaxN = 256;
+constexpr int kBatchMaxRhs = 16;
+constexpr int kNumClasses = 4;  // n <= 32, <= 64, <= 128, <= 256
+
+__host__ __device__ inline int size_class(int64_t n)
+{
+    return n <= 32 ? 0 : n <= 64 ? 1 : n <= 128 ? 2 : 3;
+}
+
+// Shared-memory doubles a panel width needs: panel [256][PW+1] + U12 [PW][256].
+__host__ __device__ constexpr int batch_smem_doubles(int pw)
+{
+    return kBatchMaxN * (pw + 1) + pw * kBatchMaxN;
+}
+
+// Is column c of an n-column LU the second column of one of TMV's two-column
+// recursion leaves (src/TMV_LUDecompose.cpp:241-245, 274-358)?
+__device__ inline bool r2_column(int64_t n, int64_t c)
+{
+    int64_t off = 0, R = n;
+    while (R > 2) {
+        int64_t N1 = R / 2;
+        if (N1 > 64) N1 = (N1 / 64) * 64;
+        if (c < off + N1) R = N1;
+        else { off += N1; R -= N1; }
+    }
+    return R == 2 && c == off + 1;
+}
+
+struct BatchDev {
+    const int64_t* n;
+    const int64_t* nrhs;
+    const int64_t* a_off;
+    const int64_t* b_off;
+    const int64_t* p_off;
+    const int* order;
+    double* A;
+    double* B;
+    int64_t* P;
+    int* status;
+    int64_t count;
+    int pw[kNumClasses];
+};
+
+template <int PW>
+__device__ void factor_solve_one(int64_t n, int64_t r, double* __restrict__ A, double* __restrict__ B,
+                                 int64_t* __restrict__ P, int* __restrict__ status, double* smem)
+{
+    constexpr int LDP = PW + 1;
+    double* pan = smem;                     // [256][LDP]
+    double* u12 = smem + kBatchMaxN * LDP;  // [PW][256]
+    __shared__ double s_key[kBatchThreads / 32];
+    __shared__ long long s_idx[kBatchThreads / 32];
+    __shared__ double w_key;
+    __shared__ long long w_idx;
+    __shared__ long long s_piv[PW];
+    __shared__ int s_sing;
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) s_sing = 0;
+    bool prev_uf = false;
+
+    for (int64_t k0 = 0; k0 < n; k0 += PW) {
+        const int w = (int)min((int64_t)PW, n - k0);
+        const int m = (int)(n - k0);
+        for (int t = tid; t < m * w; t += kBatchThreads) {
+            const int rr = t % m, cc = t / m;
+            pan[rr * LDP + cc] = A[(k0 + rr) + (k0 + cc) * n];
+        }
+        __syncthreads();
+        for (int j = 0; j < w; ++j) {
+            const bool r2 = r2_column(n, k0 + j) && !prev_uf;
+            double bk = -INFINITY;
+            long long bi = LLONG_MAX;
+            for (int rr = j + tid; rr < m; rr += kBatchThreads)
+                pivot_combine(bk, bi, pivot_key(pan[rr * LDP + j], rr == j, r2), (long long)rr);
+            warp_pivot_reduce(bk, bi);
+            if (lane == 0) { s_key[warp] = bk; s_idx[warp] = bi; }
+            __syncthreads();
+            if (warp == 0) {
+                bk = lane < kBatchThreads / 32 ? s_key[lane] : -INFINITY;
+                bi = lane < kBatchThreads / 32 ? s_idx[lane] : LLONG_MAX;
+                warp_pivot_reduce(bk, bi);
+                if (lane == 0) { w_key = bk; w_idx = bi; }
+            }
+            __syncthreads();
+            const double wk = w_key;
+            const int wi = (int)w_idx;
+            if (underflows<double>(wk)) {
+                if (tid == 0) s_piv[j] = k0 + j;
+                for (int rr = j + tid; rr < m; rr += kBatchThreads) pan[rr * LDP + j] = 0.0;
+                prev_uf = true;
+            } else {
+                prev_uf = false;
+                if (tid == 0) s_piv[j] = k0 + wi;
+                if (wi != j && tid < w) {
+                    const double t = pan[j * LDP + tid];
+                    pan[j * LDP + tid] = pan[wi * LDP + tid];
+                    pan[wi * LDP + tid] = t;
+                }
+                __syncthreads();
+                const double inv = 1.0 / pan[j * LDP + j];
+                for (int rr = j + 1 + tid; rr < m; rr += kBatchThreads) {
+                    double* row = pan + rr * LDP;
+                    const double l = row[j] * inv;
+                    row[j] = l;
+                    for (int cc = j + 1; cc < w; ++cc) row[cc] -= l * pan[j * LDP + cc];
+                }
+            }
+            __syncthreads();
+        }
+        for (int t = tid; t < m * w; t += kBatchThreads) {
+            const int rr = t % m, cc = t / m;
+            A[(k0 + rr) + (k0 + cc) * n] = pan[rr * LDP + cc];
+        }
+        for (int j = tid; j < w; j += kBatchThreads) P[k0 + j] = s_piv[j];
+        // interchanges on the other columns of A and on B
+        for (int64_t col = tid; col < n + r; col += kBatchThreads) {
+            if (col >= k0 && col < k0 + w) continue;
+            double* p = col < n ? A + col * n : B + (col - n) * n;
+            for (int j = 0; j < w; ++j) {
+                const int64_t i = k0 + j, q = s_piv[j];
+                if (q != i) {
+                    const double t = p[i];
+                    p[i] = p[q];
+                    p[q] = t;
+                }
+            }
+        }
+        __syncthreads();
+        const int ncol = (int)(n - k0 - w);
+        if (ncol > 0) {
+            // U12 = L11^-1 A12, one column per thread, substituted in shared memory
+            for (int c = tid; c < ncol; c += kBatchThreads) {
+                double* colp = A + k0 + (k0 + w + c) * n;
+                for (int kk = 0; kk < w; ++kk) {
+                    double x = colp[kk];
+                    for (int jj = 0; jj < kk; ++jj)
+                        x -= pan[kk * LDP + jj] * u12[jj * kBatchMaxN + c];
+                    u12[kk * kBatchMaxN + c] = x;
+                    colp[kk] = x;
+                }
+            }
+            __syncthreads();
+            // A22 -= L21 U12
+            const int m2 = m - w;
+            const int ti = (m2 + 3) / 4, tj = (ncol + 3) / 4;
+            for (int t = tid; t < ti * tj; t += kBatchThreads) {
+                const int i0 = (t % ti) * 4, j0 = (t / ti) * 4;
+                double acc[4][4];
+#pragma unroll
+                for (int a = 0; a < 4; ++a)
+#pragma unroll
+                    for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+                for (int kk = 0; kk < w; ++kk) {
+                    double av[4], bv[4];
+#pragma unroll
+                    for (int a = 0; a < 4; ++a)
+                        av[a] = (i0 + a < m2) ? pan[(w + i0 + a) * LDP + kk] : 0.0;
+#pragma unroll
+                    for (int b = 0; b < 4; ++b)
+                        bv[b] = (j0 + b < ncol) ? u12[kk * kBatchMaxN + j0 + b] : 0.0;
+#pragma unroll
+                    for (int a = 0; a < 4; ++a)
+#pragma unroll
+                        for (int b = 0; b < 4; ++b) acc[a][b] = fma(av[a], bv[b], acc[a][b]);
+                }
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                    if (j0 + b >= ncol) continue;
+                    double* cp = A + (k0 + w + i0) + (k0 + w + j0 + b) * n;
+#pragma unroll
+                    for (int a = 0; a < 4; ++a)
+                        if (i0 + a < m2) cp[a] -= acc[a][b];
+                }
+            }
+        }
+        __syncthreads();
+    }
+
+    // Solve: B holds P B; L (unit) then U, column-oriented as TMV's vector
+    // solve (src/TMV_TriDiv_V.cpp:148-236, 322-398) with its zero skipping.
+    if (r > 0) {
+        double* bs = smem;  // [256][kBatchMaxRhs]
+        for (int t = tid; t < n * r; t += kBatchThreads) {
+            const int i = t % n, q = t / n;
+            bs[i * kBatchMaxRhs + q] = B[i + q * n];
+        }
+        __syncthreads();
+        for (int64_t j = 0; j < n - 1; ++j) {
+            const int len = (int)(n - 1 - j);
+            for (int t = tid; t < len * r; t += kBatchThreads) {
+                const int i = (int)(j + 1) + t % len, q = t / len;
+                const double xj = bs[j * kBatchMaxRhs + q];
+                if (xj != 0.0) bs[i * kBatchMaxRhs + q] -= A[i + j * n] * xj;
+            }
+            __syncthreads();
+        }
+        for (int64_t j = n - 1; j >= 0; --j) {
+            if (tid < r) {
+                double v = bs[j * kBatchMaxRhs + tid];
+                if (v != 0.0) {
+                    const double d = A[j + j * n];
+                    if (d == 0.0) s_sing = 1;
+                    else bs[j * kBatchMaxRhs + tid] = v / d;
+                }
+            }
+            __syncthreads();
+            const int len = (int)j;
+            for (int t = tid; t < len * r; t += kBatchThreads) {
+                const int i = t % len, q = t / len;
+                const double xj = bs[j * kBatchMaxRhs + q];
+                if (xj != 0.0) bs[i * kBatchMaxRhs + q] -= A[i + j * n] * xj;
+            }
+            __syncthreads();
+        }
+        for (int t = tid; t < n * r; t += kBatchThreads) {
+            const int i = t % n, q = t / n;
+            B[i + q * n] = bs[i * kBatchMaxRhs + q];
+        }
+    }
+    __syncthreads();
+    if (tid == 0) *status = s_sing;
+}
+
+__global__ void __launch_bounds__(kBatchThreads, 2)
+batched_lu_kernel(const BatchDev* __restrict__ args, unsigned* queue)
+{
+    extern __shared__ __align__(16) double bsmem[];
+    __shared__ int s_item;
+    const BatchDev& a = *args;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = (int)atomicAdd(queue, 1u);
+        __syncthreads();
+        const int item = s_item;
+        __syncthreads();
+        if (item >= a.count) return;
+        const int s = a.order[item];
+        const int64_t n = a.n[s], r = a.nrhs[s];
+        double* A = a.A + a.a_off[s];
+        double* B = a.B + a.b_off[s];
+        int64_t* P = a.P + a.p_off[s];
+        int* st = a.status + s;
+        switch (a.pw[size_class(n)]) {
+            case 8: factor_solve_one<8>(n, r, A, B, P, st, bsmem); break;
+            case 32: factor_solve_one<32>(n, r, A, B, P, st, bsmem); break;
+            default: factor_solve_one<16>(n, r, A, B, P, st, bsmem); break;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------
+// Plan: descriptors on the device, processing order, tile choice, graph.
+// ---------------------------------------------------------------------
+struct BatchPlan {
+    Context* c = nullptr;
+    int64_t count = 0;
+    int64_t a_elems = 0, b_elems = 0, p_elems = 0;
+    int64_t* d_desc = nullptr;  // n, nrhs, a_off, b_off, p_off (5 * count)
+    int* d_order = nullptr;
+    BatchDev* d_args = nullptr;
+    BatchDev* h_args = nullptr;  // pinned
+    unsigned* d_queue = nullptr;
+    int grid = 0;
+    size_t smem = 0;
+    int pw[kNumClasses] = {16, 16, 16, 16};
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    double flops = 0;
+    std::vector<int64_t> hn, hr;
+};
+
+static size_t smem_for(const int pw[kNumClasses])
+{
+    int mx = 8;
+    for (int k = 0; k < kNumClasses; ++k) mx = std::max(mx, pw[k]);
+    return sizeof(double) * (size_t)batch_smem_doubles(mx);
+}
+
+static tmvg_status build_graph(BatchPlan* p)
+{
+    Context* c = p->c;
+    if (p->exec) { cudaGraphExecDestroy(p->exec); p->exec = nullptr; }
+    if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
+    p->smem = smem_for(p->pw);
+    tmvg_status st = check_cuda(
+        c, cudaFuncSetAttribute(batched_lu_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)p->smem),
+        "batched: smem attribute");
+    if (st) return st;
+    int per_sm = 0;
+    st = check_cuda(c,
+                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_lu_kernel,
+                                                                  kBatchThreads, p->smem),
+                    "batched: occupancy");
+    if (st) return st;
+    per_sm = std::max(per_sm, 1);
+    p->grid = (int)std::min<int64_t>((int64_t)per_sm * c->num_sms, std::max<int64_t>(p->count, 1));
+    // capture: reset the queue, run the persistent kernel
+    cudaStream_t cap;
+    st = check_cuda(c, cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "batched: stream");
+    if (st) return st;
+    cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    cudaMemsetAsync(p->d_queue, 0, sizeof(unsigned), cap);
+    batched_lu_kernel<<<p->grid, kBatchThreads, p->smem, cap>>>(p->d_args, p->d_queue);
+    cudaError_t e = cudaStreamEndCapture(cap, &p->graph);
+    cudaStreamDestroy(cap);
+    st = check_cuda(c, e, "batched: capture");
+    if (st) return st;
+    return check_cuda(c, cudaGraphInstantiate(&p->exec, p->graph, 0), "batched: instantiate");
+}
+
+static tmvg_status run_plan(BatchPlan* p, double* A, double* B, int64_t* P, int* status)
+{
+    Context* c = p->c;
+    BatchDev& h = *p->h_args;
+    h.n = p->d_desc;
+    h.nrhs = p->d_desc + p->count;
+    h.a_off = p->d_desc + 2 * p->count;
+    h.b_off = p->d_desc + 3 * p->count;
+    h.p_off = p->d_desc + 4 * p->count;
+    h.order = p->d_order;
+    h.A = A;
+    h.B = B;
+    h.P = P;
+    h.status = status;
+    h.count = p->count;
+    for (int k = 0; k < kNumClasses; ++k) h.pw[k] = p->pw[k];
+    tmvg_status st = check_cuda(
+        c, cudaMemcpyAsync(p->d_args, p->h_args, sizeof(BatchDev), cudaMemcpyHostToDevice, c->stream),
+        "batched: args");
+    if (st) return st;
+    st = check_cuda(c, cudaGraphLaunch(p->exec, c->stream), "batched: graph launch");
+    if (st) return st;
+    c->launches += 1;
+    // the pinned argument block must not change before the copy has run
+    return check_cuda(c, cudaStreamSynchronize(c->stream), "batched: sync");
+}
+
+// Time each panel width on the systems of each size class (a sample of at
+// most 256 of them, on scratch copies) and keep the fastest.
+static tmvg_status tune(BatchPlan* p)
+{
+    Context* c = p->c;
+    const int cand[3] = {8, 16, 32};
+    std::vector<std::vector<int64_t>> members(kNumClasses);
+    for (int64_t s = 0; s < p->count; ++s) members[size_class(p->hn[s])].push_back(s);
+    for (int k = 0; k < kNumClasses; ++k) {
+        if (members[k].empty()) continue;
+        const size_t take = std::min<size_t>(members[k].size(), 256);
+        // scratch sub-batch: packed copies of the sampled systems
+        std::vector<int64_t> n(take), r(take), ao(take), bo(take), po(take);
+        int64_t A_el = 0, B_el = 0, P_el = 0;
+        for (size_t i = 0; i < take; ++i) {
+            const int64_t s = members[k][i];
+            n[i] = p->hn[s]; r[i] = p->hr[s];
+            ao[i] = A_el; bo[i] = B_el; po[i] = P_el;
+            A_el += n[i] * n[i]; B_el += n[i] * r[i]; P_el += n[i];
+        }
+        BatchPlan sub;
+        sub.c = c;
+        sub.count = (int64_t)take;
+        tmvg_status st = TMVG_OK;
+        double *dA = nullptr, *dB = nullptr;
+        int64_t* dP = nullptr;
+        int* dS = nullptr;
+        if (cudaMalloc(&sub.d_desc, sizeof(int64_t) * 5 * take) != cudaSuccess ||
+            cudaMalloc(&sub.d_order, sizeof(int) * take) != cudaSuccess ||
+            cudaMalloc(&sub.d_args, sizeof(BatchDev)) != cudaSuccess ||
+            cudaMallocHost(&sub.h_args, sizeof(BatchDev)) != cudaSuccess ||
+            cudaMalloc(&sub.d_queue, sizeof(unsigned)) != cudaSuccess ||
+            cudaMalloc(&dA, sizeof(double) * std::max<int64_t>(A_el, 1)) != cudaSuccess ||
+            cudaMalloc(&dB, sizeof(double) * std::max<int64_t>(B_el, 1)) != cudaSuccess ||
+            cudaMalloc(&dP, sizeof(int64_t) * std::max<int64_t>(P_el, 1)) != cudaSuccess ||
+            cudaMalloc(&dS, sizeof(int) * take) != cudaSuccess) {
+            cudaGetLastError();
+            st = set_error(c, TMVG_OOM, "batched tuning: scratch");
+        }
+        if (!st) {
+            std::vector<int64_t> desc;
+            desc.insert(desc.end(), n.begin(), n.end());
+            desc.insert(desc.end(), r.begin(), r.end());
+            desc.insert(desc.end(), ao.begin(), ao.end());
+            desc.insert(desc.end(), bo.begin(), bo.end());
+            desc.insert(desc.end(), po.begin(), po.end());
+            std::vector<int> ord(take);
+            std::iota(ord.begin(), ord.end(), 0);
+            cudaMemcpy(sub.d_desc, desc.data(), sizeof(int64_t) * desc.size(), cudaMemcpyHostToDevice);
+            cudaMemcpy(sub.d_order, ord.data(), sizeof(int) * take, cudaMemcpyHostToDevice);
+            // diagonally dominant test systems (values only affect pivoting)
+            std::vector<double> hA(A_el), hB(B_el, 1.0);
+            uint64_t x = 88172645463325252ull;
+            for (int64_t i = 0; i < A_el; ++i) {
+                x ^= x << 13; x ^= x >> 7; x ^= x << 17;
+                hA[i] = (double)(x >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+            }
+            for (size_t i = 0; i < take; ++i)
+                for (int64_t d = 0; d < n[i]; ++d) hA[ao[i] + d * (n[i] + 1)] += 2.0 * n[i];
+            float best_ms = 1e30f;
+            int best = 16;
+            cudaEvent_t e0, e1;
+            cudaEventCreate(&e0);
+            cudaEventCreate(&e1);
+            for (int ci = 0; ci < 3 && !st; ++ci) {
+                for (int q = 0; q < kNumClasses; ++q) sub.pw[q] = cand[ci];
+                st = build_graph(&sub);
+                if (st) break;
+                float ms_sum = 0;
+                for (int rep = 0; rep < 2 && !st; ++rep) {
+                    cudaMemcpy(dA, hA.data(), sizeof(double) * A_el, cudaMemcpyHostToDevice);
+                    cudaMemcpy(dB, hB.data(), sizeof(double) * B_el, cudaMemcpyHostToDevice);
+                    cudaEventRecord(e0, c->stream);
+                    st = run_plan(&sub, dA, dB, dP, dS);
+                    cudaEventRecord(e1, c->stream);
+                    cudaEventSynchronize(e1);
+                    float ms = 0;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    if (rep == 1) ms_sum += ms;
+                }
+                if (!st && ms_sum < best_ms) { best_ms = ms_sum; best = cand[ci]; }
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            p->pw[k] = best;
+        }
+        if (sub.exec) cudaGraphExecDestroy(sub.exec);
+        if (sub.graph) cudaGraphDestroy(sub.graph);
+        cudaFree(sub.d_desc); cudaFree(sub.d_order); cudaFree(sub.d_args);
+        if (sub.h_args) cudaFreeHost(sub.h_args);
+        cudaFree(sub.d_queue); cudaFree(dA); cudaFree(dB); cudaFree(dP); cudaFree(dS);
+        if (st) return st;
+    }
+    return TMVG_OK;
+}
+
+}  // namespace tmvg
+
+using namespace tmvg;
+
+extern "C" {
+
+tmvg_status tmvg_batch_plan_create(tmvg_handle h, int64_t count, const int64_t* n,
+                                   const int64_t* nrhs, const int64_t* a_off, const int64_t* b_off,
+                                   int tune_tiles, tmvg_batch_plan* plan)
+{
+    Context* c = reinterpret_cast<Context*>(h);
+    if (!c || !plan || count < 0 || (count > 0 && (!n || !nrhs))) return TMVG_BAD_ARG;
+    *plan = nullptr;
+    c->last_error.clear();
+    cudaSetDevice(c->device);
+    if (count > INT_MAX) return set_error(c, TMVG_UNSUPPORTED, "batch: too many systems");
+    BatchPlan* p = new BatchPlan();
+    p->c = c;
+    p->count = count;
+    p->hn.assign(n, n + count);
+    p->hr.assign(nrhs, nrhs + count);
+    std::vector<int64_t> desc(5 * count);
+    int64_t A_el = 0, B_el = 0, P_el = 0;
+    for (int64_t s = 0; s < count; ++s) {
+        if (n[s] < 1 || n[s] > kBatchMaxN || nrhs[s] < 0 || nrhs[s] > kBatchMaxRhs) {
+            delete p;
+            return set_error(c, TMVG_UNSUPPORTED,
+                             "batch: each system needs 1 <= n <= 256 and 0 <= nrhs <= 16");
+        }
+        desc[s] = n[s];
+        desc[count + s] = nrhs[s];
+        desc[2 * count + s] = a_off ? a_off[s] : A_el;
+        desc[3 * count + s] = b_off ? b_off[s] : B_el;
+        desc[4 * count + s] = P_el;
+        A_el = std::max(A_el, desc[2 * count + s] + n[s] * n[s]);
+        B_el = std::max(B_el, desc[3 * count + s] + n[s] * nrhs[s]);
+        P_el += n[s];
+        p->flops += 2.0 * n[s] * n[s] * n[s] / 3.0 + 2.0 * n[s] * n[s] * nrhs[s];
+    }
+    p->a_elems = A_el;
+    p->b_elems = B_el;
+    p->p_elems = P_el;
+    // largest systems first
+    std::vector<int> order(count);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return n[x] > n[y]; });
+    tmvg_status st = TMVG_OK;
+    if (cudaMalloc(&p->d_desc, sizeof(int64_t) * std::max<int64_t>(5 * count, 1)) != cudaSuccess ||
+        cudaMalloc(&p->d_order, sizeof(int) * std::max<int64_t>(count, 1)) != cudaSuccess ||
+        cudaMalloc(&p->d_args, sizeof(BatchDev)) != cudaSuccess ||
+        cudaMallocHost(&p->h_args, sizeof(BatchDev)) != cudaSuccess ||
+        cudaMalloc(&p->d_queue, sizeof(unsigned)) != cudaSuccess) {
+        cudaGetLastError();
+        st = set_error(c, TMVG_OOM, "batch plan allocation");
+    }
+    if (!st && count > 0) {
+        st = check_cuda(c, cudaMemcpy(p->d_desc, desc.data(), sizeof(int64_t) * 5 * count,
+                                      cudaMemcpyHostToDevice), "batch desc upload");
+        if (!st)
+            st = check_cuda(c, cudaMemcpy(p->d_order, order.data(), sizeof(int) * count,
+                                          cudaMemcpyHostToDevice), "batch order upload");
+    }
+    if (!st && tune_tiles && count > 0) st = tune(p);
+    if (!st) st = build_graph(p);
+    if (st) {
+        tmvg_batch_plan_destroy(reinterpret_cast<tmvg_batch_plan>(p));
+        return st;
+    }
+    *plan = reinterpret_cast<tmvg_batch_plan>(p);
+    return TMVG_OK;
+}
+
+tmvg_status tmvg_batch_plan_info(tmvg_batch_plan plan, int64_t* a_elems, int64_t* b_elems,
+                                 int64_t* p_elems, double* flops, int* panel_widths)
+{
+    BatchPlan* p = reinterpret_cast<BatchPlan*>(plan);
+    if (!p) return TMVG_BAD_ARG;
+    if (a_elems) *a_elems = p->a_elems;
+    if (b_elems) *b_elems = p->b_elems;
+    if (p_elems) *p_elems = p->p_elems;
+    if (flops) *flops = p->flops;
+    if (panel_widths)
+        for (int k = 0; k < kNumClasses; ++k) panel_widths[k] = p->pw[k];
+    return TMVG_OK;
+}
+
+tmvg_status tmvg_batch_plan_set_tiles(tmvg_batch_plan plan, const int* panel_widths)
+{
+    BatchPlan* p = reinterpret_cast<BatchPlan*>(plan);
+    if (!p || !panel_widths) return TMVG_BAD_ARG;
+    for (int k = 0; k < kNumClasses; ++k) {
+        const int w = panel_widths[k];
+        if (w != 8 && w != 16 && w != 32) return set_error(p->c, TMVG_BAD_ARG, "panel width must be 8, 16 or 32");
+    }
+    for (int k = 0; k < kNumClasses; ++k) p->pw[k] = panel_widths[k];
+    cudaSetDevice(p->c->device);
+    return build_graph(p);
+}
+
+tmvg_status tmvg_batched_lu_solve_f64(tmvg_batch_plan plan, double* A, double* B, int64_t* P,
+                                      int32_t* status)
+{
+    BatchPlan* p = reinterpret_cast<BatchPlan*>(plan);
+    if (!p) return TMVG_BAD_ARG;
+    Context* c = p->c;
+    c->last_error.clear();
+    cudaSetDevice(c->device);
+    if (p->count == 0) return TMVG_OK;
+    if (!A || !B || !P || !status) return set_error(c, TMVG_BAD_ARG, "batched: null buffer");
+    return run_plan(p, A, B, P, status);
+}
+
+tmvg_status tmvg_batch_plan_destroy(tmvg_batch_plan plan)
+{
+    BatchPlan* p = reinterpret_cast<BatchPlan*>(plan);
+    if (!p) return TMVG_OK;
+    cudaSetDevice(p->c->device);
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    cudaFree(p->d_desc);
+    cudaFree(p->d_order);
+    cudaFree(p->d_args);
+    if (p->h_args) cudaFreeHost(p->h_args);
+    cudaFree(p->d_queue);
+    delete p;
+    return TMVG_OK;
+}
+
+}  // extern "C"

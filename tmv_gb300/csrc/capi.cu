@@ -571,4 +571,50 @@ tmvg_status tmvg_lu_solve_mixed_f64_host(tmvg_handle h, int64_t n, const double*
     return st;
 }
 
+tmvg_status tmvg_lu_solve_fwd_f64(tmvg_handle h, int64_t n, const double* A, int64_t lda,
+                                  int64_t nrhs, const double* B, int64_t ldb, double* X,
+                                  int64_t ldx, double* LU, int64_t* P)
+{
+    return tmvg_divide_f64(h, n, A, lda, nrhs, B, ldb, X, ldx, LU, P);
+}
+
+tmvg_status tmvg_lu_solve_bwd_f64(tmvg_handle h, int64_t n, const double* LU, int64_t lda,
+                                  const int64_t* P, int64_t nrhs, const double* X, int64_t ldx,
+                                  const double* G, int64_t ldg, double* gB, int64_t ldgb,
+                                  double* gA, int64_t ldga)
+{
+    CTX_OR_BAIL(h);
+    if (n < 0 || nrhs < 0 || lda < std::max<int64_t>(n, 1) || ldx < std::max<int64_t>(n, 1) ||
+        ldg < std::max<int64_t>(n, 1) || (gB && ldgb < std::max<int64_t>(n, 1)) ||
+        (gA && ldga < std::max<int64_t>(n, 1)))
+        return set_error(c, TMVG_BAD_ARG, "lu_solve_bwd: bad sizes");
+    if (n == 0 || (!gB && !gA)) return TMVG_OK;
+    double* gb = gB;
+    int64_t ldb2 = ldgb;
+    if (!gb) {
+        gb = (double*)workspace2(c, sizeof(double) * (size_t)n * std::max<int64_t>(nrhs, 1));
+        if (!gb) return TMVG_OOM;
+        ldb2 = n;
+    }
+    if (nrhs > 0) {
+        // gB = A^-T G: copy G, then gB^T := gB^T (P L U)^-1 (LU_RDivEq on the
+        // nrhs x n view gB^T, element (i, j) at gb[i*ldb2 + j])
+        tmvg_status st = check_cuda(
+            c,
+            cudaMemcpy2DAsync(gb, ldb2 * sizeof(double), G, ldg * sizeof(double),
+                              n * sizeof(double), nrhs, cudaMemcpyDeviceToDevice, c->stream),
+            "bwd: copy G");
+        if (st) return st;
+        st = lu_rdiveq<double>(c, n, LU, lda, P, nrhs, gb, ldb2, 1);
+        if (st) return st;
+    }
+    if (gA) {
+        // gA = -gB X^T: (n x nrhs) * (nrhs x n), X^T(i, j) = X[j + i*ldx]
+        tmvg_status st = gemm<double>(c, n, n, nrhs, -1.0, Mat<const double>{gb, 1, ldb2},
+                                      Mat<const double>{X, ldx, 1}, 0.0, Mat<double>{gA, 1, ldga});
+        if (st) return st;
+    }
+    return check_cuda(c, cudaStreamSynchronize(c->stream), "bwd sync");
+}
+
 }  // extern "C"

@@ -1,0 +1,96 @@
+// shim_lu.cpp -- tmv::LU_Decompose (src/TMV_LUDecompose.cpp:514-559) and
+// tmv::LU_LDivEq / LU_RDivEq (src/TMV_LUDiv.cpp:186-226, 370-411) for every
+// instantiation of TMV_LUDecompose.inst and TMV_LUDiv.inst.  Square real
+// double problems go to the GPU; the other types (and rectangular
+// LU_Decompose, which LUDiv never asks for) run TMV's own CPU code.
+#include "TMV_LUDiv.h"
+#include "shim_common.h"
+#include "tmv/TMV_LUD.h"
+#include "tmv/TMV_TriDiv.h"
+#include "tmv/TMV_TriMatrix.h"
+
+#ifdef INST_INT
+#undef INST_INT
+#endif
+
+namespace tmv {
+
+static void gpu_lu_decompose(MatrixView<double> A, ptrdiff_t* P)
+{
+    using namespace tmvg_shim;
+    if (A.colsize() != A.rowsize()) {
+        TMVG_CPU_LU_Decompose(A, P);
+        return;
+    }
+    if (!dense_view(A)) {
+        Matrix<double, ColMajor> At(A);
+        gpu_lu_decompose(At.view(), P);
+        A = At;
+        return;
+    }
+    static_assert(sizeof(ptrdiff_t) == sizeof(int64_t), "LP64 pivots");
+    check(tmvg_lu_decompose_f64_host(gpu(), A.colsize(), A.ptr(), A.stepi(), A.stepj(),
+                                     reinterpret_cast<int64_t*>(P)),
+          "tmv::LU_Decompose");
+}
+
+template <class T>
+void LU_Decompose(MatrixView<T> A, ptrdiff_t* P)
+{
+    if constexpr (std::is_same<T, double>::value) gpu_lu_decompose(A, P);
+    else TMVG_CPU_LU_Decompose(A, P);
+}
+
+static void gpu_lu_div(bool right, const GenMatrix<double>& LUx, const ptrdiff_t* P,
+                       MatrixView<double> m)
+{
+    using namespace tmvg_shim;
+    if (!(LUx.iscm() && !LUx.isconj())) {
+        Matrix<double, ColMajor> LUc(LUx);
+        gpu_lu_div(right, LUc, P, m);
+        return;
+    }
+    if (!dense_view(m)) {
+        Matrix<double, ColMajor> mt(m);
+        gpu_lu_div(right, LUx, P, mt.view());
+        m = mt;
+        return;
+    }
+    const ptrdiff_t n = LUx.colsize();
+    const int64_t* p = reinterpret_cast<const int64_t*>(P);
+    tmvg_status s = right
+        ? tmvg_lu_rdiveq_f64_host(gpu(), n, LUx.cptr(), LUx.stepj(), p, m.colsize(), m.ptr(),
+                                  m.stepi(), m.stepj())
+        : tmvg_lu_ldiveq_f64_host(gpu(), n, LUx.cptr(), LUx.stepj(), p, m.rowsize(), m.ptr(),
+                                  m.stepi(), m.stepj());
+    if (s == TMVG_SINGULAR) throw SingularUpperTriMatrix<double>(LUx.upperTri());
+    check(s, right ? "tmv::LU_RDivEq" : "tmv::LU_LDivEq");
+}
+
+template <class T, class T1>
+void LU_LDivEq(const GenMatrix<T1>& LUx, const ptrdiff_t* P, MatrixView<T> m)
+{
+    if constexpr (std::is_same<T, double>::value && std::is_same<T1, double>::value)
+        gpu_lu_div(false, LUx, P, m);
+    else
+        TMVG_CPU_LU_LDivEq(LUx, P, m);
+}
+
+template <class T, class T1>
+void LU_RDivEq(const GenMatrix<T1>& LUx, const ptrdiff_t* P, MatrixView<T> m)
+{
+    if constexpr (std::is_same<T, double>::value && std::is_same<T1, double>::value)
+        gpu_lu_div(true, LUx, P, m);
+    else
+        TMVG_CPU_LU_RDivEq(LUx, P, m);
+}
+
+#define InstFile "TMV_LUDecompose.inst"
+#include "TMV_Inst.h"
+#undef InstFile
+
+#define InstFile "TMV_LUDiv.inst"
+#include "TMV_Inst.h"
+#undef InstFile
+
+}  // namespace tmv
