@@ -92,6 +92,23 @@ tmvg_status tmvg_lu_decompose_f64(tmvg_handle h, int64_t n, double* A,
 tmvg_status tmvg_lu_decompose_f64_host(tmvg_handle h, int64_t n, double* A,
                                        int64_t sAi, int64_t sAj, int64_t* P);
 
+/* ---- LU_Decompose without device allocation --------------------------
+ * No counterpart in TMV: an extra entry point for callers that cannot
+ * allocate device memory (their device memory belongs to another allocator,
+ * such as a framework's caching allocator or a fixed arena, or an allocation
+ * is not acceptable on their code path).  Same result as
+ * tmvg_lu_decompose_f64 for a column-major n x n device matrix A and device
+ * pivots P, but it calls no cudaMalloc/cudaFree and needs no tmvg_handle:
+ * all scratch lives in one static device array of about 343 KiB that every
+ * GPU loading this library holds until the process exits.  Runs on the
+ * current device and the given cudaStream_t (NULL: legacy default stream);
+ * synchronous.  Limit: n <= 16384, larger n returns TMVG_UNSUPPORTED.  The
+ * first call on a device looks up the array's device address; make that
+ * first call before any stream capture.  Calls share the array, so calls
+ * that overlap on the GPU (other threads or streams) race: serialise them. */
+tmvg_status tmvg_lu_decompose_f64_noalloc(int64_t n, double* A, int64_t lda,
+                                          int64_t* P, void* cuda_stream);
+
 /* ---- LU_LDivEq / LU_RDivEq -------------------------------------------
  * LDivEq: B := (P L U)^-1 B, B n x nrhs column-major (ldb).
  * RDivEq: B := B (P L U)^-1, B nrows x n column-major (ldb).

@@ -56,6 +56,7 @@ _SIGS = {
                                        i64, vp, i64, i64]),
     "tmvg_lu_decompose_f64": (C.c_int, [vp, i64, vp, i64, vp]),
     "tmvg_lu_decompose_f64_host": (C.c_int, [vp, i64, vp, i64, i64, vp]),
+    "tmvg_lu_decompose_f64_noalloc": (C.c_int, [i64, vp, i64, vp, vp]),
     "tmvg_lu_ldiveq_f64": (C.c_int, [vp, i64, vp, i64, vp, i64, vp, i64]),
     "tmvg_lu_rdiveq_f64": (C.c_int, [vp, i64, vp, i64, vp, i64, vp, i64]),
     "tmvg_lu_ldiveq_f64_host": (C.c_int, [vp, i64, vp, i64, vp, i64, vp, i64, i64]),

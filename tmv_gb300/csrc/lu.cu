@@ -23,6 +23,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <mutex>
 #include <vector>
 
 namespace tmvg {
@@ -615,3 +616,159 @@ template tmvg_status copy_matrix<float>(Context*, int64_t, int64_t, const float*
                                         int64_t, float*, int64_t, int64_t);
 
 }  // namespace tmvg
+
+// =====================================================================
+// LU factorisation without device allocation.
+//
+// Some callers of this library cannot allocate device memory: programs whose
+// device memory is owned entirely by another allocator (a framework's caching
+// allocator or a fixed arena that must not see cudaMalloc behind its back),
+// and code paths where an allocation's latency or failure is not acceptable.
+// tmvg_lu_decompose_f64_noalloc serves them: it runs the same kernels as
+// tmvg_lu_decompose_f64 but takes every scratch word from the file-scope
+// array below, which each GPU that loads this library holds until the process
+// exits (kNoAllocBytes, about 343 KiB).  It needs no tmvg_handle (creating one
+// allocates).  Limits: n <= kNoAllocMaxN = 16384 (larger n returns
+// TMVG_UNSUPPORTED before any device work); at most kNoAllocMaxCtas = 160
+// panel CTAs are used.
+// =====================================================================
+namespace tmvg {
+namespace {
+constexpr int64_t kNoAllocMaxN = 16384;
+constexpr int kNoAllocMaxCtas = 160;
+constexpr size_t kNaOffErr = 0;    // int[2]: device error word + aux
+constexpr size_t kNaOffBar = 64;   // unsigned: grid-barrier counter
+constexpr size_t kNaOffKey = 256;  // double[2 * kNoAllocMaxCtas]
+constexpr size_t kNaOffIdx = kNaOffKey + sizeof(double) * 2 * kNoAllocMaxCtas;
+constexpr size_t kNaOffRows = kNaOffIdx + sizeof(long long) * 2 * kNoAllocMaxCtas;
+constexpr size_t kNaOffDiag = kNaOffRows + sizeof(double) * 2 * kNoAllocMaxCtas * kPanelMax;
+constexpr size_t kNaOffModes = kNaOffDiag + sizeof(double) * 2 * kPanelMax;
+constexpr size_t kNoAllocBytes = kNaOffModes + kNoAllocMaxN;
+constexpr int kNoAllocMaxDevices = 64;
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_lu_noalloc_scratch[kNoAllocBytes];
+
+// Device address of the scratch array on `device` (which must be current).
+// The host-side name of a __device__ array is only a stand-in, so the
+// address is asked of the runtime once per device and cached.
+static unsigned char* noalloc_scratch(int device, tmvg_status* st)
+{
+    static std::mutex mu;
+    static unsigned char* addr[kNoAllocMaxDevices] = {};
+    std::lock_guard<std::mutex> lock(mu);
+    if (device < 0 || device >= kNoAllocMaxDevices) {
+        *st = TMVG_UNSUPPORTED;
+        return nullptr;
+    }
+    if (!addr[device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_lu_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            cudaGetLastError();
+            *st = TMVG_CUDA_ERROR;
+            return nullptr;
+        }
+        addr[device] = static_cast<unsigned char*>(p);
+    }
+    *st = TMVG_OK;
+    return addr[device];
+}
+
+}  // namespace tmvg
+
+extern "C" tmvg_status tmvg_lu_decompose_f64_noalloc(int64_t n, double* A, int64_t lda, int64_t* P,
+                                                     void* stream)
+{
+    using namespace tmvg;
+    if (n < 0 || lda < std::max<int64_t>(n, 1)) return TMVG_BAD_ARG;
+    if (n > kNoAllocMaxN) return TMVG_UNSUPPORTED;
+    if (n == 0) return TMVG_OK;
+    if (!A || !P) return TMVG_BAD_ARG;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return TMVG_NO_DEVICE;
+    }
+    tmvg_status st = TMVG_OK;
+    unsigned char* s = noalloc_scratch(dev, &st);
+    if (!s) return st;
+
+    // A context on the stack: no workspace, flags and barrier in the scratch.
+    Context c;
+    c.device = dev;
+    c.num_sms = std::min(sms, kNoAllocMaxCtas);
+    c.stream = static_cast<cudaStream_t>(stream);
+    c.dflags = reinterpret_cast<int*>(s + kNaOffErr);
+    c.dbar = reinterpret_cast<unsigned*>(s + kNaOffBar);
+    double* cand_key = reinterpret_cast<double*>(s + kNaOffKey);
+    long long* cand_idx = reinterpret_cast<long long*>(s + kNaOffIdx);
+    double* cand_rows = reinterpret_cast<double*>(s + kNaOffRows);
+    double* diag_row = reinterpret_cast<double*>(s + kNaOffDiag);
+    unsigned char* modes = s + kNaOffModes;
+
+    // The array keeps the last call's contents: clear the error words.
+    st = check_cuda(&c, cudaMemsetAsync(s, 0, 256, c.stream), "noalloc: clear");
+    if (st) return st;
+    {
+        std::vector<unsigned char> hm((size_t)n, 0);
+        leaf_modes(0, n, hm);
+        st = check_cuda(&c, cudaMemcpyAsync(modes, hm.data(), (size_t)n, cudaMemcpyHostToDevice, c.stream),
+                        "noalloc: modes");
+        if (st) return st;
+        st = check_cuda(&c, cudaStreamSynchronize(c.stream), "noalloc: modes sync");
+        if (st) return st;
+    }
+    const int nbmax = panel_width<double>();
+    cudaFuncSetAttribute(lu_panel_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         200 * 1024);
+    for (int64_t k = 0; k < n; k += nbmax) {
+        const int nb = (int)std::min<int64_t>(nbmax, n - k);
+        const int64_t m = n - k;
+        const int G = (int)std::min<int64_t>(c.num_sms, ceil_div(m, kPanelThreads));
+        const int rows_per_cta = (int)ceil_div(m, G);
+        const size_t smem = (size_t)rows_per_cta * (nb + 1) * sizeof(double);
+        st = check_cuda(&c, cudaMemsetAsync(c.dbar, 0, sizeof(unsigned), c.stream), "noalloc: barrier");
+        if (st) return st;
+        double* Ap = A;
+        int64_t* Pp = P;
+        const unsigned char* mp = modes + k;
+        int64_t ldav = lda, nv = n, kv = k;
+        int nbv = nb, rpc = rows_per_cta;
+        unsigned* bar = c.dbar;
+        int* err = c.dflags;
+        void* args[] = {&Ap, &ldav, &nv, &kv, &nbv, &Pp, &mp, &rpc, &cand_key, &cand_idx,
+                        &cand_rows, &diag_row, &bar, &err};
+        st = check_cuda(&c,
+                        cudaLaunchCooperativeKernel((const void*)lu_panel_kernel<double>, dim3(G),
+                                                    dim3(kPanelThreads), args, smem, c.stream),
+                        "noalloc: panel launch");
+        if (st) return st;
+        if (n > nb) {
+            laswp_kernel<double><<<(unsigned)ceil_div(n, 128), 128, 0, c.stream>>>(A, lda, n, k, nb, P,
+                                                                                  k, k + nb);
+            st = check_cuda(&c, cudaGetLastError(), "noalloc: laswp launch");
+            if (st) return st;
+        }
+        if (k + nb < n) {
+            const int64_t rest = n - k - nb;
+            st = tri_solve<double>(&c, nb, A + k + k * lda, 1, lda, false, true, rest,
+                                   A + k + (k + nb) * lda, 1, lda, false);
+            if (st) return st;
+            st = gemm<double>(&c, rest, rest, nb, -1.0, Mat<const double>{A + (k + nb) + k * lda, 1, lda},
+                              Mat<const double>{A + k + (k + nb) * lda, 1, lda}, 1.0,
+                              Mat<double>{A + (k + nb) + (k + nb) * lda, 1, lda});
+            if (st) return st;
+        }
+    }
+    int code[2] = {0, 0};
+    st = check_cuda(&c, cudaMemcpyAsync(code, c.dflags, sizeof(code), cudaMemcpyDeviceToHost, c.stream),
+                    "noalloc: status");
+    if (st) return st;
+    st = check_cuda(&c, cudaStreamSynchronize(c.stream), "noalloc: sync");
+    if (st) return st;
+    if (code[0] == kDevTimeout) return TMVG_TIMEOUT;
+    if (code[0] != kDevOk) return TMVG_CUDA_ERROR;
+    return TMVG_OK;
+}
