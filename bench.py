@@ -209,6 +209,8 @@ def run_gpu(args) -> dict:
         torch.distributed.barrier()
     clocks = ClockSampler(local)
     clocks.start()
+    # per-kernel-class CUDA events on the library's stream, over the timed steps
+    h.timing_enable(True)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -226,6 +228,8 @@ def run_gpu(args) -> dict:
     clk = clocks.stop()
     launches = (h.launches() - launches0) // max(args.steps, 1)
     ms_step = ms / args.steps
+    kernels = kernel_breakdown(h, args.steps, ms_step)
+    h.timing_enable(False)
     flops = lu_solve_flops(n, nrhs)
     value = flops * world / (ms_step * 1e-3) / 1e12
 
@@ -236,11 +240,8 @@ def run_gpu(args) -> dict:
     berr = float(r.abs().max() / (Acm.abs().sum(dim=1).max() * x.abs().max() + B.abs().max()))
     fwd = float((X - X64).norm() / X64.norm()) if X64 is not None else None
 
-    if args.no_extras:
-        roof, e2e = None, None
-    else:
-        roof = mixed_roofline(dev, n) if mixed else gemm_roofline(dev, n)
-        e2e = e2e_host(args, Acm, B, n, nrhs, mixed)
+    roof = dominant_roofline(kernels, mixed)
+    e2e = None if args.no_extras else e2e_host(args, Acm, B, n, nrhs, mixed)
 
     if rank == 0 and not args.no_cpu_baseline and not args.no_extras:
         cpu = cpu_baseline(np.asfortranarray(Acm.cpu().numpy()), B.cpu().numpy(), n, cond)
@@ -263,7 +264,8 @@ def run_gpu(args) -> dict:
         "fp64_gpu_lu": {"value": round(flops / (fp64_ms * 1e-3) / 1e12, 4), "unit": "TFLOP/s",
                         "ms_per_solve": round(fp64_ms, 3)},
         "speedup_vs_fp64_gpu_lu": (round(fp64_ms / ms_step, 3) if X64 is not None else None),
-        "roofline": roof, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
+        "roofline": roof, "kernels": kernels, "e2e": e2e, "gpu_launches": int(launches),
+        "clocks": clk,
     }
     if cpu is not None:
         out["cpu_baseline"] = cpu
@@ -352,45 +354,70 @@ def batched_bench(dev, args, with_cpu: bool) -> dict:
     return out
 
 
-def mixed_roofline(dev, n: int) -> dict:
-    """FP32 trailing update (A22 -= L21 U12, K = 128) timed alone at the size
-    of the first trailing update of the n x n factorisation; FFMA SIMT path."""
-    import torch
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic
+# byte of each kernel class, from one ncu capture of the class's kernels on
+# the n = 8192 workload (the capture commands and figures are in profiles/).
+NCU_TRAFFIC_PER_ALG_BYTE: dict = {}
 
-    from tmv_gb300 import _lib  # noqa: F401
-    from tmv_gb300 import linalg
+KERNEL_NAMES = {
+    "panel": "lu_panel_cluster_kernel (16-CTA cluster panel factorisation)",
+    "trailing_update": "A22 -= L21 U12 (FP32: split + tf32x3_update_kernel on tcgen05; "
+                       "FP64: gemm_simt_kernel<double>)",
+    "tri_solve": "trsv_invdiag_kernel (sync-free triangular solve, inverted 128-blocks)",
+    "residual": "residual_partial_kernel + residual_final_kernel (FP64 b - A x)",
+}
 
-    return {"kernel": "see profiles/ (mixed path launch list)", "bound": "tensor",
-            "achieved": None, "peak": None, "unit": "TFLOP/s", "frac": None, "traffic": None}
+
+def kernel_breakdown(h, steps: int, ms_step: float) -> dict:
+    """Per kernel class: spans, event time, share of the step and achieved
+    bandwidth / flop rate over the timed steps (CUDA events recorded by the
+    library on its stream around every span)."""
+    out = {}
+    for cls in ("panel", "trailing_update", "tri_solve", "residual"):
+        t = h.timing(cls)
+        if t["spans"] == 0 or t["total_ms"] <= 0:
+            continue
+        sec = t["total_ms"] * 1e-3
+        out[cls] = {"spans_per_step": t["spans"] / steps,
+                    "ms_per_step": round(t["total_ms"] / steps, 3),
+                    "share_of_step": round(t["total_ms"] / steps / ms_step, 4),
+                    "ms_per_span": round(t["total_ms"] / t["spans"], 4),
+                    "alg_bytes_per_span": t["bytes"] / t["spans"],
+                    "alg_flops_per_span": t["flops"] / t["spans"],
+                    "achieved_gbs": round(t["bytes"] / sec / 1e9, 2),
+                    "achieved_tflops": round(t["flops"] / sec / 1e12, 4)}
+    return out
 
 
-def gemm_roofline(dev, n: int) -> dict:
-    import torch
+def dominant_roofline(kernels: dict, mixed: bool) -> dict | None:
+    """Roofline of the kernel class with the largest share of the step.
 
-    from tmv_gb300 import linalg
-
-    m = n - 64
-    a = linalg.colmajor(torch.randn(m, 64, dtype=torch.float64, device=dev))
-    bb = linalg.colmajor(torch.randn(64, m, dtype=torch.float64, device=dev))
-    c = linalg.colmajor(torch.randn(m, m, dtype=torch.float64, device=dev))
-    for _ in range(2):
-        linalg.multmm(True, -1.0, a, bb, c)
-    s = torch.cuda.current_stream(dev)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    reps = 5
-    e0.record(s)
-    for _ in range(reps):
-        linalg.multmm(True, -1.0, a, bb, c)
-    e1.record(s)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / reps
-    flop = 2.0 * m * m * 64
-    ach = flop / (ms * 1e-3) / 1e12
-    return {"kernel": "gemm_simt_kernel<double> (trailing update A22 -= L21 U12, K=64)",
-            "bound": "tensor", "achieved": round(ach, 4), "peak": FP64_DFMA_PEAK_TFLOPS,
-            "unit": "TFLOP/s", "frac": round(ach / FP64_DFMA_PEAK_TFLOPS, 4), "traffic": None,
-            "peak_source": "measured FP64 DFMA throughput (no FP64 entry in MEASURED_PEAKS.json)",
-            "algorithmic_flop_per_launch": flop, "ms_per_launch": round(ms, 4)}
+    The FP32 factorisation's classes and the FP64 residual are bounded by
+    HBM bandwidth (arithmetic intensity below the ridge; the panel is in
+    practice latency-bound and its fraction shows it).  The FP64 trailing
+    update is bounded by the FP64 DFMA rate."""
+    if not kernels:
+        return None
+    cls = max(kernels, key=lambda k: kernels[k]["ms_per_step"])
+    k = kernels[cls]
+    pk = peaks()
+    if cls == "trailing_update" and not mixed:
+        ach, peak = k["achieved_tflops"], FP64_DFMA_PEAK_TFLOPS
+        out = {"bound": "fp64", "unit": "TFLOP/s",
+               "peak_source": "measured FP64 DFMA throughput (MEASURED_PEAKS.json has no FP64 entry)"}
+        per = k["alg_flops_per_span"]
+    else:
+        ach, peak = k["achieved_gbs"], float(pk["hbm_gbs"])
+        out = {"bound": "hbm", "unit": "GB/s",
+               "peak_source": f"{pk['_source']} HBM copy bandwidth (hbm_gbs)"}
+        per = k["alg_bytes_per_span"]
+    ratio = NCU_TRAFFIC_PER_ALG_BYTE.get(cls)
+    out.update({"kernel": KERNEL_NAMES[cls], "class": cls, "achieved": ach, "peak": peak,
+                "frac": round(ach / peak, 4),
+                "traffic": (k["alg_bytes_per_span"] * ratio) if ratio else None,
+                "alg_per_launch": per, "ms_per_launch": k["ms_per_span"],
+                "share_of_step": k["share_of_step"]})
+    return out
 
 
 def e2e_host(args, Acm, B, n, nrhs, mixed=False) -> dict:

@@ -51,6 +51,35 @@ const char* tmvg_status_string(tmvg_status s);
 /* Create a context on `device` (its current CUDA context, default stream). */
 tmvg_status tmvg_create(tmvg_handle* h, int device);
 tmvg_status tmvg_destroy(tmvg_handle h);
+
+/* Kernel-class timing, a measurement hook with no counterpart in TMV.  While
+ * enabled, the library records CUDA events on the handle's stream around
+ * the launches of each class below and adds up, per class, the spans, their
+ * elapsed time and the algorithmic work they do:
+ *   TRAILING_UPDATE  A22 -= L21 U12 of each LU panel step (with the operand
+ *                    split of the tensor-core path); bytes = sizeof(T) x
+ *                    (2 m n + m k + k n), flops = 2 m n k
+ *   PANEL            one panel factorisation; bytes = 2 sizeof(T) m nb,
+ *                    flops = the panel's multiply-adds x 2
+ *   TRI_SOLVE        one triangular solve of the mixed solve; bytes = the
+ *                    triangle read once plus right-hand side in and out
+ *   RESIDUAL         one FP64 residual b - A x; bytes = 8 n^2 + vectors
+ * Enabling (or disabling) clears the sums; reading synchronises the stream.
+ * Do not enable it while the stream is being captured into a CUDA graph. */
+#define TMVG_KCLASS_TRAILING_UPDATE 0
+#define TMVG_KCLASS_PANEL 1
+#define TMVG_KCLASS_TRI_SOLVE 2
+#define TMVG_KCLASS_RESIDUAL 3
+
+typedef struct tmvg_kernel_timing {
+    int64_t spans;   /* timed spans (one per panel step, solve, residual) */
+    double total_ms; /* summed event time */
+    double bytes;    /* summed algorithmic bytes */
+    double flops;    /* summed algorithmic flops */
+} tmvg_kernel_timing;
+
+tmvg_status tmvg_timing_enable(tmvg_handle h, int on);
+tmvg_status tmvg_timing_read(tmvg_handle h, int kclass, tmvg_kernel_timing* out);
 /* Use this cudaStream_t for all later calls (NULL = legacy default stream). */
 tmvg_status tmvg_set_stream(tmvg_handle h, void* cuda_stream);
 tmvg_status tmvg_synchronize(tmvg_handle h);
@@ -78,6 +107,17 @@ tmvg_status tmvg_multmm_f64_host(tmvg_handle h, int add, double alpha,
                                  const double* B, int64_t sBi, int64_t sBj,
                                  double* C, int64_t sCi, int64_t sCj);
 
+/* ---- FP32-accurate product on the tensor cores -----------------------
+ * C -= A * B for FP32 column-major device data, A m x k, B k x n, with k a
+ * multiple of 32 up to 128: the trailing-update shape of the mixed-precision
+ * LU.  Runs on tcgen05 tensor cores with TF32 operands split as hi + lo
+ * (three products per step, FP32 accumulation), so the result has FP32
+ * accuracy.  Synchronous.  No TMV counterpart (TMV's float MultMM is
+ * src/TMV_MultMM.cpp:405 on the CPU). */
+tmvg_status tmvg_gemm_f32_tf32x3(tmvg_handle h, int64_t m, int64_t n, int64_t k,
+                                 const float* A, int64_t lda, const float* B,
+                                 int64_t ldb, float* C, int64_t ldc);
+
 /* ---- LU_Decompose ----------------------------------------------------
  * In-place P A = L U of an n x n column-major matrix (leading dim lda):
  * L unit lower below the diagonal, U on and above it, P[0..n) interchanges.
@@ -99,7 +139,7 @@ tmvg_status tmvg_lu_decompose_f64_host(tmvg_handle h, int64_t n, double* A,
  * is not acceptable on their code path).  Same result as
  * tmvg_lu_decompose_f64 for a column-major n x n device matrix A and device
  * pivots P, but it calls no cudaMalloc/cudaFree and needs no tmvg_handle:
- * all scratch lives in one static device array of about 343 KiB that every
+ * all scratch lives in one static device array of 353,540 bytes (345 KiB) that every
  * GPU loading this library holds until the process exits.  Runs on the
  * current device and the given cudaStream_t (NULL: legacy default stream);
  * synchronous.  Limit: n <= 16384, larger n returns TMVG_UNSUPPORTED.  The
@@ -199,7 +239,7 @@ tmvg_status tmvg_lu_solve_bwd_f64(tmvg_handle h, int64_t n, const double* LU, in
  * A_s is overwritten by its LU factors, B_s by X_s, the interchanges go to
  * P + (n_0 + ... + n_{s-1}); status[s] = 1 where a zero U(j,j) met a
  * nonzero (TMV's SingularUpperTriMatrix), else 0.  With tune_tiles the
- * plan times the panel widths 8/16/32 on a sample of every size class
+ * plan times the panel widths 8 and 16 on a sample of every size class
  * (n <= 32, 64, 128, 256) and keeps the fastest.
  * Replaces a loop of LUDiv<double> B_s / A_s (src/TMV_LUD.cpp:74-120). */
 typedef struct tmvg_batch_plan_s* tmvg_batch_plan;

@@ -47,7 +47,7 @@ def test_golden_batch_matches_tmv(dev):
     assert np.abs(X - g["X"]).max() <= 1e-12 * np.abs(g["X"]).max()
 
 
-@pytest.mark.parametrize("tiles", [(8, 8, 8, 8), (16, 16, 16, 16), (32, 32, 32, 32), (8, 16, 32, 16)])
+@pytest.mark.parametrize("tiles", [(8, 8, 8, 8), (16, 16, 16, 16), (8, 16, 8, 16)])
 def test_random_batch_vs_oracle(dev, orc, tiles):
     rng = np.random.default_rng(10)
     n, r, a_off, b_off, A, B = make_batch(rng, 120, 1, 256, 0, 16, shift=0.0)
@@ -87,7 +87,7 @@ def test_autotuned_plan_and_workload_properties(dev, orc):
     rng = np.random.default_rng(12)
     n, r, a_off, b_off, A, B = make_batch(rng, 600, 8, 256, 1, 16)
     LU, X, P, st, plan = run(dev, n, r, A, B, tune=True)
-    assert set(plan.panel_widths) <= {8, 16, 32}
+    assert set(plan.panel_widths) <= {8, 16}
     assert not st.any()
     # backward error of every system
     worst = 0.0

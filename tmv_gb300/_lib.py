@@ -41,6 +41,15 @@ class IRInfo(C.Structure):
                 ("backward_error", C.c_double), ("anorm_inf", C.c_double)]
 
 
+class KernelTiming(C.Structure):
+    """tmvg_kernel_timing: spans, summed event ms, algorithmic bytes and flops."""
+
+    _fields_ = [("spans", C.c_int64), ("total_ms", C.c_double), ("bytes", C.c_double),
+                ("flops", C.c_double)]
+
+
+KCLASS = {"trailing_update": 0, "panel": 1, "tri_solve": 2, "residual": 3}
+
 _SIGS = {
     "tmvg_version": (C.c_int, []),
     "tmvg_status_string": (C.c_char_p, [C.c_int]),
@@ -50,10 +59,13 @@ _SIGS = {
     "tmvg_synchronize": (C.c_int, [vp]),
     "tmvg_last_error": (C.c_char_p, [vp]),
     "tmvg_launch_count": (i64, [vp]),
+    "tmvg_timing_enable": (C.c_int, [vp, C.c_int]),
+    "tmvg_timing_read": (C.c_int, [vp, C.c_int, C.POINTER(KernelTiming)]),
     "tmvg_multmm_f64": (C.c_int, [vp, C.c_int, dbl, i64, i64, i64, vp, i64, i64, vp, i64, i64,
                                   vp, i64, i64]),
     "tmvg_multmm_f64_host": (C.c_int, [vp, C.c_int, dbl, i64, i64, i64, vp, i64, i64, vp, i64,
                                        i64, vp, i64, i64]),
+    "tmvg_gemm_f32_tf32x3": (C.c_int, [vp, i64, i64, i64, vp, i64, vp, i64, vp, i64]),
     "tmvg_lu_decompose_f64": (C.c_int, [vp, i64, vp, i64, vp]),
     "tmvg_lu_decompose_f64_host": (C.c_int, [vp, i64, vp, i64, i64, vp]),
     "tmvg_lu_decompose_f64_noalloc": (C.c_int, [i64, vp, i64, vp, vp]),
@@ -144,3 +156,13 @@ class Handle:
 
     def call(self, name: str, *args) -> int:
         return getattr(self.lib, name)(self.h, *args)
+
+    def timing_enable(self, on: bool) -> None:
+        """Turn kernel-class timing on or off (either clears the sums)."""
+        self.check(self.lib.tmvg_timing_enable(self.h, 1 if on else 0), "timing_enable")
+
+    def timing(self, kclass: str) -> dict:
+        """Summed spans, event ms, algorithmic bytes and flops of one kernel class."""
+        t = KernelTiming()
+        self.check(self.lib.tmvg_timing_read(self.h, KCLASS[kclass], C.byref(t)), "timing_read")
+        return {"spans": int(t.spans), "total_ms": t.total_ms, "bytes": t.bytes, "flops": t.flops}

@@ -19,9 +19,10 @@
 //     A22 -= L21 U12 (4x4 register tiles, FP64 FMA),
 //   then forward/back substitution of B_s staged in shared memory.
 // FP64 FMA throughput (about 2 per SM per clock on GB300) bounds the kernel.
-// PW is chosen per size class by tune_batched().
+// PW (8 or 16) is chosen per size class by the plan's tuner.
 #include "batched.cuh"
 #include "lu.cuh"
+#include "pivots.cuh"
 
 #include <algorithm>
 #include <chrono>
@@ -88,7 +89,8 @@ __device__ void factor_solve_one(int64_t n, int64_t r, double* __restrict__ A, d
     __shared__ long long s_idx[kBatchThreads / 32];
     __shared__ double w_key;
     __shared__ long long w_idx;
-    __shared__ long long s_piv[PW];
+    __shared__ int s_piv[PW];
+    __shared__ int s_pairs[1 + 2 * kMaxPairs];
     __shared__ int s_sing;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -122,12 +124,12 @@ __device__ void factor_solve_one(int64_t n, int64_t r, double* __restrict__ A, d
             const double wk = w_key;
             const int wi = (int)w_idx;
             if (underflows<double>(wk)) {
-                if (tid == 0) s_piv[j] = k0 + j;
+                if (tid == 0) s_piv[j] = (int)(k0 + j);
                 for (int rr = j + tid; rr < m; rr += kBatchThreads) pan[rr * LDP + j] = 0.0;
                 prev_uf = true;
             } else {
                 prev_uf = false;
-                if (tid == 0) s_piv[j] = k0 + wi;
+                if (tid == 0) s_piv[j] = (int)(k0 + wi);
                 if (wi != j && tid < w) {
                     const double t = pan[j * LDP + tid];
                     pan[j * LDP + tid] = pan[wi * LDP + tid];
@@ -149,17 +151,23 @@ __device__ void factor_solve_one(int64_t n, int64_t r, double* __restrict__ A, d
             A[(k0 + rr) + (k0 + cc) * n] = pan[rr * LDP + cc];
         }
         for (int j = tid; j < w; j += kBatchThreads) P[k0 + j] = s_piv[j];
-        // interchanges on the other columns of A and on B
-        for (int64_t col = tid; col < n + r; col += kBatchThreads) {
-            if (col >= k0 && col < k0 + w) continue;
-            double* p = col < n ? A + col * n : B + (col - n) * n;
-            for (int j = 0; j < w; ++j) {
-                const int64_t i = k0 + j, q = s_piv[j];
-                if (q != i) {
-                    const double t = p[i];
-                    p[i] = p[q];
-                    p[q] = t;
-                }
+        // interchanges on the other columns of A and on B: the panel's swaps
+        // as (dst, src) row pairs, applied per column as one gather
+        if (warp == 0) panel_row_pairs(k0, w, s_piv, s_pairs);
+        __syncthreads();
+        {
+            const int np = s_pairs[0];
+            const int* dst = s_pairs + 1;
+            const int* src = s_pairs + 1 + kMaxPairs;
+            // a warp per column, a lane per pair: at most 2 PW <= 32 rows move
+            static_assert(2 * PW <= 32, "one lane per row pair");
+            for (int64_t col = warp; col < n + r; col += kBatchThreads / 32) {
+                if (col >= k0 && col < k0 + w) continue;
+                double* p = col < n ? A + col * n : B + (col - n) * n;
+                double v = 0.0;
+                if (lane < np) v = p[src[lane]];
+                __syncwarp();
+                if (lane < np) p[dst[lane]] = v;
             }
         }
         __syncthreads();
@@ -276,11 +284,8 @@ batched_lu_kernel(const BatchDev* __restrict__ args, unsigned* queue)
         double* B = a.B + a.b_off[s];
         int64_t* P = a.P + a.p_off[s];
         int* st = a.status + s;
-        switch (a.pw[size_class(n)]) {
-            case 8: factor_solve_one<8>(n, r, A, B, P, st, bsmem); break;
-            case 32: factor_solve_one<32>(n, r, A, B, P, st, bsmem); break;
-            default: factor_solve_one<16>(n, r, A, B, P, st, bsmem); break;
-        }
+        if (a.pw[size_class(n)] == 8) factor_solve_one<8>(n, r, A, B, P, st, bsmem);
+        else factor_solve_one<16>(n, r, A, B, P, st, bsmem);
         __syncthreads();
     }
 }
@@ -378,7 +383,7 @@ static tmvg_status run_plan(BatchPlan* p, double* A, double* B, int64_t* P, int*
 static tmvg_status tune(BatchPlan* p)
 {
     Context* c = p->c;
-    const int cand[3] = {8, 16, 32};
+    const int cand[2] = {8, 16};
     std::vector<std::vector<int64_t>> members(kNumClasses);
     for (int64_t s = 0; s < p->count; ++s) members[size_class(p->hn[s])].push_back(s);
     for (int k = 0; k < kNumClasses; ++k) {
@@ -437,7 +442,7 @@ static tmvg_status tune(BatchPlan* p)
             cudaEvent_t e0, e1;
             cudaEventCreate(&e0);
             cudaEventCreate(&e1);
-            for (int ci = 0; ci < 3 && !st; ++ci) {
+            for (int ci = 0; ci < 2 && !st; ++ci) {
                 for (int q = 0; q < kNumClasses; ++q) sub.pw[q] = cand[ci];
                 st = build_graph(&sub);
                 if (st) break;
@@ -561,7 +566,7 @@ tmvg_status tmvg_batch_plan_set_tiles(tmvg_batch_plan plan, const int* panel_wid
     if (!p || !panel_widths) return TMVG_BAD_ARG;
     for (int k = 0; k < kNumClasses; ++k) {
         const int w = panel_widths[k];
-        if (w != 8 && w != 16 && w != 32) return set_error(p->c, TMVG_BAD_ARG, "panel width must be 8, 16 or 32");
+        if (w != 8 && w != 16) return set_error(p->c, TMVG_BAD_ARG, "panel width must be 8 or 16");
     }
     for (int k = 0; k < kNumClasses; ++k) p->pw[k] = panel_widths[k];
     cudaSetDevice(p->c->device);

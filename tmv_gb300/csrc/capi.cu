@@ -4,6 +4,7 @@
 #include <new>
 #include <string>
 
+#include "gemm_tc.cuh"
 #include "lu.cuh"
 #include "mixed.cuh"
 #include "trsv.cuh"
@@ -46,6 +47,69 @@ static void* grow(Context* c, void*& buf, size_t& have, size_t bytes)
 
 void* workspace(Context* c, size_t bytes) { return grow(c, c->work, c->work_bytes, bytes); }
 void* workspace2(Context* c, size_t bytes) { return grow(c, c->work2, c->work2_bytes, bytes); }
+void* workspace3(Context* c, size_t bytes) { return grow(c, c->work3, c->work3_bytes, bytes); }
+
+static cudaEvent_t pooled_event(Context* c)
+{
+    if (!c->event_pool.empty()) {
+        cudaEvent_t e = c->event_pool.back();
+        c->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return e;
+}
+
+ScopedTimer::ScopedTimer(Context* c, int cls, double bytes, double flops)
+    : c_(c), cls_(cls), bytes_(bytes), flops_(flops)
+{
+    if (!c_->timing) return;
+    a_ = pooled_event(c_);
+    if (a_ && cudaEventRecord(a_, c_->stream) != cudaSuccess) {
+        cudaGetLastError();
+        c_->event_pool.push_back(a_);
+        a_ = nullptr;
+    }
+}
+
+ScopedTimer::~ScopedTimer()
+{
+    if (!a_) return;
+    cudaEvent_t b = pooled_event(c_);
+    if (!b || cudaEventRecord(b, c_->stream) != cudaSuccess) {
+        cudaGetLastError();
+        c_->event_pool.push_back(a_);
+        if (b) c_->event_pool.push_back(b);
+        return;
+    }
+    c_->spans.push_back({a_, b, cls_, bytes_, flops_});
+}
+
+// Folds every recorded span into the per-class sums (synchronises).
+static tmvg_status drain_spans(Context* c)
+{
+    tmvg_status st = check_cuda(c, cudaStreamSynchronize(c->stream), "timing: sync");
+    if (st) return st;
+    for (const TimedSpan& s : c->spans) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, s.a, s.b) != cudaSuccess) {
+            cudaGetLastError();
+        } else {
+            c->t_launches[s.cls] += 1;
+            c->t_ms[s.cls] += ms;
+            c->t_bytes[s.cls] += s.bytes;
+            c->t_flops[s.cls] += s.flops;
+        }
+        c->event_pool.push_back(s.a);
+        c->event_pool.push_back(s.b);
+    }
+    c->spans.clear();
+    return TMVG_OK;
+}
 
 tmvg_status collect_device_error(Context* c, const char* what)
 {
@@ -247,10 +311,46 @@ tmvg_status tmvg_destroy(tmvg_handle h)
     cudaStreamSynchronize(c->stream);
     if (c->work) cudaFree(c->work);
     if (c->work2) cudaFree(c->work2);
+    if (c->work3) cudaFree(c->work3);
     if (c->trsv_flags) cudaFree(c->trsv_flags);
     if (c->dflags) cudaFree(c->dflags);
     if (c->hflags) cudaFreeHost(c->hflags);
+    for (const TimedSpan& sp : c->spans) {
+        cudaEventDestroy(sp.a);
+        cudaEventDestroy(sp.b);
+    }
+    for (cudaEvent_t e : c->event_pool) cudaEventDestroy(e);
     delete c;
+    return TMVG_OK;
+}
+
+tmvg_status tmvg_timing_enable(tmvg_handle h, int on)
+{
+    Context* c = reinterpret_cast<Context*>(h);
+    if (!c) return TMVG_BAD_ARG;
+    cudaSetDevice(c->device);
+    tmvg_status st = drain_spans(c);
+    if (st) return st;
+    c->timing = on != 0;
+    for (int k = 0; k < kClsCount; ++k) {
+        c->t_launches[k] = 0;
+        c->t_ms[k] = c->t_bytes[k] = c->t_flops[k] = 0.0;
+    }
+    return TMVG_OK;
+}
+
+tmvg_status tmvg_timing_read(tmvg_handle h, int kclass, tmvg_kernel_timing* out)
+{
+    Context* c = reinterpret_cast<Context*>(h);
+    if (!c || !out) return TMVG_BAD_ARG;
+    if (kclass < 0 || kclass >= kClsCount) return set_error(c, TMVG_BAD_ARG, "timing: unknown kernel class");
+    cudaSetDevice(c->device);
+    tmvg_status st = drain_spans(c);
+    if (st) return st;
+    out->spans = c->t_launches[kclass];
+    out->total_ms = c->t_ms[kclass];
+    out->bytes = c->t_bytes[kclass];
+    out->flops = c->t_flops[kclass];
     return TMVG_OK;
 }
 
@@ -615,6 +715,18 @@ tmvg_status tmvg_lu_solve_bwd_f64(tmvg_handle h, int64_t n, const double* LU, in
         if (st) return st;
     }
     return check_cuda(c, cudaStreamSynchronize(c->stream), "bwd sync");
+}
+
+tmvg_status tmvg_gemm_f32_tf32x3(tmvg_handle h, int64_t m, int64_t n, int64_t k, const float* A,
+                                 int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc)
+{
+    CTX_OR_BAIL(h);
+    if (m < 0 || n < 0 || k < 0 || lda < std::max<int64_t>(m, 1) || ldb < std::max<int64_t>(k, 1) ||
+        ldc < std::max<int64_t>(m, 1))
+        return set_error(c, TMVG_BAD_ARG, "gemm_f32_tf32x3: bad sizes");
+    tmvg_status st = gemm_f32_tf32x3_update(c, m, n, k, A, lda, B, ldb, C, ldc);
+    if (st) return st;
+    return collect_device_error(c, "gemm_f32_tf32x3");
 }
 
 }  // extern "C"

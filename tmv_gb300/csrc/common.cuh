@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>
+#include <vector>
 
 #include "tmvg.h"
 
@@ -23,6 +24,23 @@ enum DevError : int {
     kDevOk = 0,
     kDevTimeout = 1,
     kDevSingular = 2,
+};
+
+// Kernel classes timed by tmvg_timing_enable (the TMVG_KCLASS_* values).
+enum KernelClass : int {
+    kClsTrailingUpdate = 0,
+    kClsPanel = 1,
+    kClsTriSolve = 2,
+    kClsResidual = 3,
+    kClsCount = 4,
+};
+
+// One timed span: events recorded on the context's stream around the
+// launches of one kernel class, with the algorithmic work they do.
+struct TimedSpan {
+    cudaEvent_t a, b;
+    int cls;
+    double bytes, flops;
 };
 
 // Per-context state shared by the C entry points.
@@ -49,6 +67,39 @@ struct Context {
     unsigned* trsv_flags = nullptr;
     unsigned trsv_epoch = 0;
     unsigned long long* trsv_ticket = nullptr;
+    // Whether a 16-CTA cluster of the panel kernel can be launched, per
+    // element type (-1 unknown, 0 no, 1 yes): [0] double, [1] float.
+    int cluster_ok[2] = {-1, -1};
+    // The same for the register-resident panel kernel.
+    int reg_cluster_ok[2] = {-1, -1};
+    // Third grow-only workspace: operand copies of the tensor-core update.
+    void* work3 = nullptr;
+    size_t work3_bytes = 0;
+    // Kernel-class timing (off unless tmvg_timing_enable turned it on):
+    // spans recorded but not yet read, recycled events, and per-class sums.
+    bool timing = false;
+    std::vector<TimedSpan> spans;
+    std::vector<cudaEvent_t> event_pool;
+    int64_t t_launches[kClsCount] = {};
+    double t_ms[kClsCount] = {};
+    double t_bytes[kClsCount] = {};
+    double t_flops[kClsCount] = {};
+};
+
+// Records CUDA events on c->stream around its scope when timing is on;
+// the launches inside the scope count as one span of class `cls`.
+class ScopedTimer {
+  public:
+    ScopedTimer(Context* c, int cls, double bytes, double flops);
+    ~ScopedTimer();
+    ScopedTimer(const ScopedTimer&) = delete;
+    ScopedTimer& operator=(const ScopedTimer&) = delete;
+
+  private:
+    Context* c_;
+    int cls_;
+    double bytes_, flops_;
+    cudaEvent_t a_ = nullptr;
 };
 
 tmvg_status set_error(Context* c, tmvg_status s, const std::string& msg);
@@ -56,6 +107,7 @@ tmvg_status check_cuda(Context* c, cudaError_t e, const char* what);
 // Ensure at least `bytes` of workspace; returns nullptr on failure.
 void* workspace(Context* c, size_t bytes);
 void* workspace2(Context* c, size_t bytes);
+void* workspace3(Context* c, size_t bytes);
 // Reads and clears the device error word (synchronises the stream).
 tmvg_status collect_device_error(Context* c, const char* what);
 
@@ -81,7 +133,8 @@ __device__ __forceinline__ double pivot_key(T v, bool first, bool r2mode)
 }
 
 // (key, index) max-reduction with lowest index on ties.
-__device__ __forceinline__ void pivot_combine(double& k, long long& i, double k2, long long i2)
+template <typename I>
+__device__ __forceinline__ void pivot_combine(double& k, I& i, double k2, I i2)
 {
     if (k2 > k || (k2 == k && i2 < i)) {
         k = k2;
@@ -89,12 +142,13 @@ __device__ __forceinline__ void pivot_combine(double& k, long long& i, double k2
     }
 }
 
-__device__ __forceinline__ void warp_pivot_reduce(double& k, long long& i)
+template <typename I>
+__device__ __forceinline__ void warp_pivot_reduce(double& k, I& i)
 {
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
         double k2 = __shfl_xor_sync(0xffffffffu, k, off);
-        long long i2 = __shfl_xor_sync(0xffffffffu, i, off);
+        I i2 = __shfl_xor_sync(0xffffffffu, i, off);
         pivot_combine(k, i, k2, i2);
     }
 }

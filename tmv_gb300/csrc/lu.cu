@@ -18,12 +18,17 @@
 // include/tmv/TMV_Base.h:692-696) zeroes the sub-column and records P[j] = j.
 // The L column is scaled by the reciprocal of the pivot, as TMV's v /= x does
 // (include/tmv/TMV_VectorArith.h:104-106).
+#include "gemm_tc.cuh"
 #include "lu.cuh"
+#include "pivots.cuh"
 #include "trsv.cuh"
+
+#include <cooperative_groups.h>
 
 #include <algorithm>
 #include <climits>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 namespace tmvg {
@@ -64,7 +69,7 @@ __global__ void __launch_bounds__(kPanelThreads)
 lu_panel_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int nb,
                 int64_t* __restrict__ P, const unsigned char* __restrict__ modes,
                 int rows_per_cta, double* cand_key, long long* cand_idx,
-                T* cand_rows, T* diag_row, unsigned* bar, int* err)
+                T* cand_rows, T* diag_row, unsigned* bar, int* err, int* pairs)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* rows = reinterpret_cast<T*>(smem_raw);
@@ -74,6 +79,7 @@ lu_panel_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int nb,
     __shared__ double w_key;
     __shared__ long long w_idx;
     __shared__ T urow[kPanelMax];
+    __shared__ int s_piv[kPanelMax];
 
     const int G = gridDim.x;
     const int cta = blockIdx.x;
@@ -145,12 +151,14 @@ lu_panel_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int nb,
         const long long wi = w_idx;  // panel row of the pivot
 
         if (underflows<T>(wk)) {
+            if (tid == 0) s_piv[jj] = (int)(k + jj);
             if (cta == 0 && tid == 0) P[k + jj] = k + jj;
             for (int r = tid; r < nr; r += kPanelThreads)
                 if (r0 + r >= jj) rows[r * ldp + jj] = T(0);
             prev_uf = true;
         } else {
             prev_uf = false;
+            if (tid == 0) s_piv[jj] = (int)(k + wi);
             if (cta == 0 && tid == 0) P[k + jj] = k + wi;
             const int wc = (int)(wi / rows_per_cta);
             for (int cc = tid; cc < nb; cc += kPanelThreads)
@@ -184,6 +192,349 @@ lu_panel_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int nb,
         const int r = t % nr, cc = t / nr;
         A[(k + r0 + r) + (k + cc) * lda] = rows[r * ldp + cc];
     }
+    if (cta == 0 && warp == 0) panel_row_pairs(k, nb, s_piv, pairs);
+}
+
+
+// ---------------------------------------------------------------------
+// Panel factorisation on one 16-CTA thread-block cluster.
+//
+// When the panel's rows fit in the shared memory of 16 SMs, one cluster
+// holds the whole panel in distributed shared memory and the CTAs exchange
+// pivot candidates and the pivot row through DSMEM, synchronising with the
+// hardware cluster barrier once per column: each CTA publishes its candidate
+// (key, index and a copy of the row) and the owner of row j publishes a copy
+// of row j; after the barrier every CTA reduces the candidates itself and
+// the two owners complete the interchange from the copies.  There is no
+// global-memory traffic or spinning per column.
+// The pivot rule and the arithmetic are those of lu_panel_kernel.
+// ---------------------------------------------------------------------
+constexpr int kClusterCtas = 16;
+
+template <typename T>
+__global__ void __launch_bounds__(kPanelThreads)
+lu_panel_cluster_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int nb,
+                        int64_t* __restrict__ P, const unsigned char* __restrict__ modes,
+                        int rows_per_cta, int* pairs)
+{
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* rows = reinterpret_cast<T*>(smem_raw);
+    const int ldp = nb + 1;
+    __shared__ double s_key[kPanelThreads / 32];
+    __shared__ long long s_idx[kPanelThreads / 32];
+    // per-column candidates published to the cluster, double-buffered by
+    // column parity so one cluster barrier per column separates each write
+    // from the remote reads of the same buffer
+    __shared__ double cand_key[2];
+    __shared__ long long cand_idx[2];
+    __shared__ T cand_row[2][kPanelMax];
+    __shared__ T diag_row[2][kPanelMax];
+    __shared__ T urow[kPanelMax];
+    __shared__ int s_piv[kPanelMax];
+
+    const int G = (int)cluster.num_blocks();
+    const int cta = (int)cluster.block_rank();
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t m = n - k;
+    const int64_t r0 = (int64_t)cta * rows_per_cta;
+    const int nr = (int)max((int64_t)0, min((int64_t)rows_per_cta, m - r0));
+
+    for (int t = tid; t < nr * nb; t += kPanelThreads) {
+        const int r = t % nr, cc = t / nr;
+        rows[r * ldp + cc] = A[(k + r0 + r) + (k + cc) * lda];
+    }
+    __syncthreads();
+
+    bool prev_uf = false;
+    for (int jj = 0; jj < nb; ++jj) {
+        const int par = jj & 1;
+        const bool r2 = modes[jj] && !prev_uf;
+        const int owner_j = jj / rows_per_cta;
+        // each thread scans (and later updates) the rows tid, tid + 256, ...
+        double bk = -INFINITY;
+        long long bi = LLONG_MAX;
+        for (int r = tid; r < nr; r += kPanelThreads) {
+            const int64_t pr = r0 + r;
+            if (pr < jj) continue;
+            pivot_combine(bk, bi, pivot_key(rows[r * ldp + jj], pr == jj, r2), (long long)pr);
+        }
+        warp_pivot_reduce(bk, bi);
+        if (lane == 0) { s_key[warp] = bk; s_idx[warp] = bi; }
+        __syncthreads();
+        if (warp == 0) {
+            bk = lane < kPanelThreads / 32 ? s_key[lane] : -INFINITY;
+            bi = lane < kPanelThreads / 32 ? s_idx[lane] : LLONG_MAX;
+            warp_pivot_reduce(bk, bi);
+            if (lane == 0) { cand_key[par] = bk; cand_idx[par] = bi; }
+            if (bi != LLONG_MAX) {
+                const T* src = rows + (bi - r0) * ldp;
+                for (int cc = lane; cc < nb; cc += 32) cand_row[par][cc] = src[cc];
+            }
+        } else if (warp == 1 && cta == owner_j) {
+            const T* src = rows + (jj - r0) * ldp;
+            for (int cc = lane; cc < nb; cc += 32) diag_row[par][cc] = src[cc];
+        }
+        cluster.sync();  // the only cluster barrier of this column
+        double wk = -INFINITY;
+        long long wi = LLONG_MAX;
+        if (lane < G) {
+            wk = *cluster.map_shared_rank(&cand_key[par], lane);
+            wi = *cluster.map_shared_rank(&cand_idx[par], lane);
+        }
+        warp_pivot_reduce(wk, wi);  // every warp reaches the same winner
+        if (underflows<T>(wk)) {
+            if (tid == 0) s_piv[jj] = (int)(k + jj);
+            if (cta == 0 && tid == 0) P[k + jj] = k + jj;
+            for (int r = tid; r < nr; r += kPanelThreads)
+                if (r0 + r >= jj) rows[r * ldp + jj] = T(0);
+            prev_uf = true;
+            continue;
+        }
+        prev_uf = false;
+        if (tid == 0) s_piv[jj] = (int)(k + wi);
+        if (cta == 0 && tid == 0) P[k + jj] = k + wi;
+        const int owner_w = (int)(wi / rows_per_cta);
+        {
+            const T* wrow = cluster.map_shared_rank(&cand_row[par][0], owner_w);
+            for (int cc = tid; cc < nb; cc += kPanelThreads) {
+                const T v = wrow[cc];
+                urow[cc] = v;
+                if (cta == owner_j) rows[(jj - r0) * ldp + cc] = v;
+            }
+            if (wi != jj && cta == owner_w) {
+                const T* jrow = cluster.map_shared_rank(&diag_row[par][0], owner_j);
+                for (int cc = tid; cc < nb; cc += kPanelThreads) rows[(wi - r0) * ldp + cc] = jrow[cc];
+            }
+        }
+        __syncthreads();
+        const T inv = T(1) / urow[jj];
+        for (int r = tid; r < nr; r += kPanelThreads) {
+            if (r0 + r <= jj) continue;
+            T* rw = rows + r * ldp;
+            const T l = rw[jj] * inv;
+            rw[jj] = l;
+            for (int cc = jj + 1; cc < nb; ++cc) rw[cc] -= l * urow[cc];
+        }
+    }
+    __syncthreads();
+
+    for (int t = tid; t < nr * nb; t += kPanelThreads) {
+        const int r = t % nr, cc = t / nr;
+        A[(k + r0 + r) + (k + cc) * lda] = rows[r * ldp + cc];
+    }
+    if (cta == 0 && warp == 0) panel_row_pairs(k, nb, s_piv, pairs);
+    cluster.sync();  // keep every CTA's shared memory alive until all reads are done
+}
+
+// ---------------------------------------------------------------------
+// Register-resident cluster panel.
+//
+// Every thread holds one row of the panel in registers, so the rank-1 update
+// of column j costs a thread NB-j-1 FMAs against the pivot row read from
+// shared memory.  Register indices must be static, so the row is kept
+// rotated: columns are processed in blocks of 4 (unrolled), the active
+// columns of block q sit at positions 0.. of the register array, and after
+// each block the array rotates left by 4 (finished columns wrap to the end,
+// where the update skips them).  Rows exchanged between threads travel in the
+// same rotated order, which every thread shares.
+//
+// The cluster exchange is push-based, one hardware cluster barrier per
+// column: each CTA reduces its candidate (key, index) and stores it, with a
+// copy of the candidate row, into a receive slot of every CTA of the cluster;
+// the CTA holding row j stores a copy of it the same way.  After the barrier
+// every warp reduces the 16 candidates from its own shared memory and reads
+// the pivot row and the old row j locally, so no load crosses the cluster on
+// the critical path.  Receive slots are double-buffered by column parity: a
+// CTA writes slot parity p for column j+2 only after the barrier of column
+// j+1, which every reader of column j's slots has reached.
+// Used while a 16-CTA cluster covers the panel's rows with one row per
+// thread (m <= 16 * 512).
+// ---------------------------------------------------------------------
+constexpr int kRegPanelThreads = 512;
+constexpr int kRegPanelWarps = kRegPanelThreads / 32;
+constexpr int kRegBlock = 4;
+
+template <typename T>
+struct RegPanel {
+    static constexpr int NB = sizeof(T) == 8 ? 32 : 64;  // columns a thread holds
+};
+
+// Pivot key as an unsigned integer with the same order: -1 (a NaN that is
+// not the first element) -> 0, key k >= 0 -> bits(k) + 1.  Empty slots are 0
+// with index INT_MAX, so they lose to every row.
+__device__ __forceinline__ unsigned long long pivot_key_bits(double k)
+{
+    return k < 0 ? 0ull : (unsigned long long)__double_as_longlong(k) + 1ull;
+}
+
+__device__ __forceinline__ double pivot_key_value(unsigned long long b)
+{
+    return b == 0 ? -1.0 : __longlong_as_double((long long)(b - 1));
+}
+
+// Warp-wide (key desc, index asc) reduction with three redux.sync steps;
+// every lane receives the result.
+__device__ __forceinline__ void warp_key_reduce(unsigned long long& key, int& idx)
+{
+    const unsigned hi = (unsigned)(key >> 32), lo = (unsigned)key;
+    const unsigned mhi = __reduce_max_sync(0xffffffffu, hi);
+    const unsigned mlo = __reduce_max_sync(0xffffffffu, hi == mhi ? lo : 0u);
+    const unsigned mi = __reduce_min_sync(0xffffffffu, (hi == mhi && lo == mlo) ? (unsigned)idx : 0x7fffffffu);
+    key = ((unsigned long long)mhi << 32) | mlo;
+    idx = (int)mi;
+}
+
+template <typename T, int NB>
+__global__ void __launch_bounds__(kRegPanelThreads, 1)
+lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int nb,
+                            int64_t* __restrict__ P, const unsigned char* __restrict__ modes,
+                            int rows_per_cta, int* pairs)
+{
+    static_assert(NB % kRegBlock == 0, "whole blocks");
+    static_assert(NB * sizeof(T) == 256, "a row is 16 vectors of 16 bytes");
+    constexpr int VEC = 16;  // 16-byte vectors per row
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    __shared__ unsigned long long s_key[kRegPanelWarps];
+    __shared__ int s_idx[kRegPanelWarps];
+    __shared__ __align__(16) T warp_row[kRegPanelWarps][NB];  // each warp's candidate row
+    __shared__ __align__(16) T diag_local[NB];                // row j of this CTA
+    // receive slots, written by every CTA of the cluster
+    __shared__ unsigned long long recv_key[2][kClusterCtas];
+    __shared__ int recv_idx[2][kClusterCtas];
+    __shared__ __align__(16) T recv_row[2][kClusterCtas][NB];
+    __shared__ __align__(16) T recv_diag[2][NB];
+    __shared__ unsigned char s_mode[kPanelMax];
+    __shared__ int s_piv[kPanelMax];
+
+    const int G = (int)cluster.num_blocks();
+    const int cta = (int)cluster.block_rank();
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // row indices within the panel fit an int (m <= 16 * 512)
+    const int m = (int)(n - k);
+    const int r0 = cta * rows_per_cta;
+    const int nr = max(0, min(rows_per_cta, m - r0));
+    const bool have = tid < nr;
+    const int pr = r0 + tid;  // this thread's row, counted from the panel's top
+    T* Ap = A + k + k * lda;
+
+    for (int j = tid; j < nb; j += kRegPanelThreads) s_mode[j] = modes[j];
+    T x[NB];
+#pragma unroll
+    for (int c = 0; c < NB; ++c) x[c] = (have && c < nb) ? Ap[pr + c * lda] : T(0);
+    __syncthreads();
+
+    bool prev_uf = false;
+    int rot = 0;  // x[p] holds column (p + rot) mod NB
+    for (int jb = 0; jb < nb; jb += kRegBlock) {
+        const int lim = NB - jb;  // positions >= lim hold finished columns 0..jb-1
+#pragma unroll
+        for (int u = 0; u < kRegBlock; ++u) {
+            const int jj = jb + u;
+            if (jj >= nb) break;
+            const int par = jj & 1;
+            const bool r2 = s_mode[jj] && !prev_uf;
+            const int owner_j = jj / rows_per_cta;
+            // 1. this warp's candidate; its row and row jj into shared memory
+            unsigned long long bk = 0;
+            int bi = INT_MAX;
+            if (have && pr >= jj) {
+                bk = pivot_key_bits(pivot_key(x[u], pr == jj, r2));
+                bi = pr;
+            }
+            warp_key_reduce(bk, bi);
+            if (have && bi == pr) {
+#pragma unroll
+                for (int c = 0; c < NB; ++c) warp_row[warp][c] = x[c];
+            }
+            if (lane == 0) { s_key[warp] = bk; s_idx[warp] = bi; }
+            if (have && pr == jj) {
+#pragma unroll
+                for (int c = 0; c < NB; ++c) diag_local[c] = x[c];
+            }
+            __syncthreads();
+            // 2. push: warp 0 the CTA's candidate, warp 1 row jj (its owner only)
+            if (warp == 0) {
+                bk = lane < kRegPanelWarps ? s_key[lane] : 0ull;
+                bi = lane < kRegPanelWarps ? s_idx[lane] : INT_MAX;
+                warp_key_reduce(bk, bi);
+                if (lane < G) {
+                    *cluster.map_shared_rank(&recv_key[par][cta], lane) = bk;
+                    *cluster.map_shared_rank(&recv_idx[par][cta], lane) = bi;
+                }
+                if (bi != INT_MAX) {
+                    const uint4* src = reinterpret_cast<const uint4*>(warp_row[(bi - r0) >> 5]);
+                    for (int t = lane; t < G * VEC; t += 32) {
+                        uint4* dst = reinterpret_cast<uint4*>(
+                            cluster.map_shared_rank(&recv_row[par][cta][0], t / VEC));
+                        dst[t % VEC] = src[t % VEC];
+                    }
+                }
+            } else if (warp == 1 && cta == owner_j) {
+                const uint4* src = reinterpret_cast<const uint4*>(diag_local);
+                for (int t = lane; t < G * VEC; t += 32) {
+                    uint4* dst = reinterpret_cast<uint4*>(
+                        cluster.map_shared_rank(&recv_diag[par][0], t / VEC));
+                    dst[t % VEC] = src[t % VEC];
+                }
+            }
+            cluster.sync();  // the only cluster barrier of this column
+            // 3. every warp reduces the candidates from its own shared memory
+            unsigned long long wk = lane < G ? recv_key[par][lane] : 0ull;
+            int wi = lane < G ? recv_idx[par][lane] : INT_MAX;
+            warp_key_reduce(wk, wi);
+            if (underflows<T>(pivot_key_value(wk))) {
+                if (tid == 0) s_piv[jj] = (int)(k + jj);
+                if (have && pr >= jj) x[u] = T(0);
+                prev_uf = true;
+                continue;
+            }
+            prev_uf = false;
+            if (tid == 0) s_piv[jj] = (int)(k + wi);
+            const T* urow = recv_row[par][wi / rows_per_cta];
+            // the interchange: row jj takes the pivot row, row wi the old row jj
+            const T* src = nullptr;
+            if (have && pr == jj) src = urow;
+            else if (have && pr == wi) src = recv_diag[par];
+            if (src) {
+#pragma unroll
+                for (int c = 0; c < NB; ++c) x[c] = src[c];
+            }
+            if (have && pr > jj) {
+                const T l = x[u] * (T(1) / urow[u]);
+                x[u] = l;
+#pragma unroll
+                for (int c = u + 1; c < NB; ++c)
+                    if (c < lim) x[c] -= l * urow[c];
+            }
+        }
+        if (jb + kRegBlock < nb) {
+            T t[kRegBlock];
+#pragma unroll
+            for (int c = 0; c < kRegBlock; ++c) t[c] = x[c];
+#pragma unroll
+            for (int c = 0; c < NB - kRegBlock; ++c) x[c] = x[c + kRegBlock];
+#pragma unroll
+            for (int c = 0; c < kRegBlock; ++c) x[NB - kRegBlock + c] = t[c];
+            rot += kRegBlock;
+        }
+    }
+
+    if (have) {
+#pragma unroll
+        for (int p = 0; p < NB; ++p) {
+            const int col = (p + rot) % NB;
+            if (col < nb) Ap[pr + col * lda] = x[p];
+        }
+    }
+    __syncthreads();
+    if (cta == 0) {
+        for (int j = tid; j < nb; j += kRegPanelThreads) P[k + j] = s_piv[j];
+        if (warp == 0) panel_row_pairs(k, nb, s_piv, pairs);
+    }
+    cluster.sync();  // no CTA leaves while another may still store into it
 }
 
 // ---------------------------------------------------------------------
@@ -207,6 +558,70 @@ __global__ void laswp_kernel(T* __restrict__ A, int64_t lda, int64_t ncols, int6
             col[i] = col[p];
             col[p] = a;
         }
+    }
+}
+
+// The panel's row pairs applied to columns [0, ncols) outside [skip0, skip1):
+// one warp per column loads every source value, then stores them.
+template <typename T>
+__global__ void laswp_pairs_kernel(T* __restrict__ A, int64_t lda, int64_t ncols, int64_t skip0,
+                                   int64_t skip1, const int* __restrict__ pairs)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t col = blockIdx.x * (int64_t)(blockDim.x / 32) + (threadIdx.x >> 5);
+    if (col >= ncols || (col >= skip0 && col < skip1)) return;
+    const int np = pairs[0];
+    const int* dst = pairs + 1;
+    const int* src = pairs + 1 + kMaxPairs;
+    T* a = A + col * lda;
+    T v[kMaxPairs / 32];
+#pragma unroll
+    for (int t = 0; t < kMaxPairs / 32; ++t) {
+        const int q = lane + 32 * t;
+        if (q < np) v[t] = a[src[q]];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int t = 0; t < kMaxPairs / 32; ++t) {
+        const int q = lane + 32 * t;
+        if (q < np) a[dst[q]] = v[t];
+    }
+}
+
+// U12 = L11^-1 A12 for a panel: each CTA solves 64 columns of A12 in shared
+// memory, all threads sweeping the rows together (one barrier per row of
+// L11), instead of one thread per column.
+constexpr int kU12Cols = 64;
+template <typename T>
+__global__ void __launch_bounds__(256)
+panel_u12_kernel(int nb, const T* __restrict__ L, int64_t lda, T* __restrict__ A12, int64_t ncols)
+{
+    extern __shared__ __align__(16) unsigned char u12_smem[];
+    T* Ls = reinterpret_cast<T*>(u12_smem);  // [nb][nb+1]
+    T* X = Ls + nb * (nb + 1);               // [nb][kU12Cols+1]
+    const int tid = threadIdx.x;
+    const int64_t c0 = (int64_t)blockIdx.x * kU12Cols;
+    const int nc = (int)min((int64_t)kU12Cols, ncols - c0);
+    for (int t = tid; t < nb * nb; t += 256) {
+        const int i = t % nb, j = t / nb;
+        Ls[i * (nb + 1) + j] = j < i ? L[i + j * lda] : T(0);
+    }
+    for (int t = tid; t < nb * nc; t += 256) {
+        const int i = t % nb, c = t / nb;
+        X[i * (kU12Cols + 1) + c] = A12[i + (c0 + c) * lda];
+    }
+    __syncthreads();
+    for (int j = 0; j < nb - 1; ++j) {
+        const int rowsleft = nb - 1 - j;
+        for (int t = tid; t < rowsleft * nc; t += 256) {
+            const int i = j + 1 + t % rowsleft, c = t / rowsleft;
+            X[i * (kU12Cols + 1) + c] -= Ls[i * (nb + 1) + j] * X[j * (kU12Cols + 1) + c];
+        }
+        __syncthreads();
+    }
+    for (int t = tid; t < nb * nc; t += 256) {
+        const int i = t % nb, c = t / nb;
+        A12[i + (c0 + c) * lda] = X[i * (kU12Cols + 1) + c];
     }
 }
 
@@ -430,12 +845,204 @@ tmvg_status apply_pivots(Context* c, int64_t ncols, T* B, int64_t bsi, int64_t b
     return check_cuda(c, cudaGetLastError(), "pivot_rows launch");
 }
 
+// After the panel at k: its interchanges on the other columns (row pairs),
+// U12 = L11^-1 A12, and the trailing update A22 -= L21 U12.
+// Multiply-adds x 2 of factoring an m x nb panel: column j scales m-j-1
+// entries and updates (m-j-1) x (nb-j-1) of them.
+static double panel_flops(int64_t m, int nb)
+{
+    double f = 0.0;
+    for (int j = 0; j < nb; ++j) f += (double)(m - j - 1) * (1.0 + 2.0 * (nb - j - 1));
+    return f;
+}
+
+// Trailing updates of at least this many rows and columns use the tensor
+// cores in the FP32 factorisation; smaller ones stay on the SIMT kernel.
+constexpr int64_t kTcMinRest = 256;
+
+template <typename T>
+static tmvg_status panel_update(Context* c, int64_t n, T* A, int64_t lda, int64_t k, int nb,
+                                const int* pairs)
+{
+    tmvg_status st;
+    if (n > nb) {
+        const int cols_per_cta = 8;  // one warp per column
+        laswp_pairs_kernel<T><<<(unsigned)ceil_div(n, cols_per_cta), 32 * cols_per_cta, 0, c->stream>>>(
+            A, lda, n, k, k + nb, pairs);
+        ++c->launches;
+        st = check_cuda(c, cudaGetLastError(), "lu: laswp launch");
+        if (st) return st;
+    }
+    if (k + nb < n) {
+        const int64_t rest = n - k - nb;
+        const size_t smem = sizeof(T) * ((size_t)nb * (nb + 1) + (size_t)nb * (kU12Cols + 1));
+        if (smem > 48 * 1024)
+            cudaFuncSetAttribute(panel_u12_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
+        panel_u12_kernel<T><<<(unsigned)ceil_div(rest, kU12Cols), 256, smem, c->stream>>>(
+            nb, A + k + k * lda, lda, A + k + (k + nb) * lda, rest);
+        ++c->launches;
+        st = check_cuda(c, cudaGetLastError(), "lu: u12 launch");
+        if (st) return st;
+        const double fr = (double)rest;
+        ScopedTimer timer(c, kClsTrailingUpdate, sizeof(T) * (2.0 * fr * fr + 2.0 * fr * nb),
+                          2.0 * fr * fr * nb);
+        if constexpr (std::is_same<T, float>::value) {
+            // FP32 factor: 3xTF32 on the tensor cores keeps FP32 accuracy
+            if (rest >= kTcMinRest && tf32x3_supported(nb))
+                return gemm_f32_tf32x3_update(c, rest, rest, nb, A + (k + nb) + k * lda, lda,
+                                              A + k + (k + nb) * lda, lda,
+                                              A + (k + nb) + (k + nb) * lda, lda);
+        }
+        st = gemm<T>(c, rest, rest, nb, T(-1), Mat<const T>{A + (k + nb) + k * lda, 1, lda},
+                     Mat<const T>{A + k + (k + nb) * lda, 1, lda}, T(1),
+                     Mat<T>{A + (k + nb) + (k + nb) * lda, 1, lda});
+        if (st) return st;
+    }
+    return TMVG_OK;
+}
+
+constexpr size_t kClusterSmemMax = 200 * 1024;
+
+// Can this device run the 16-CTA panel cluster with the largest shared
+// memory the kernel may ask for?  Checked once per context and type.
+template <typename T>
+static bool cluster_panel_ok(Context* c)
+{
+    int& ok = c->cluster_ok[sizeof(T) == 8 ? 0 : 1];
+    if (ok >= 0) return ok == 1;
+    ok = 0;
+    if (cudaFuncSetAttribute(lu_panel_cluster_kernel<T>,
+                             cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
+        cudaFuncSetAttribute(lu_panel_cluster_kernel<T>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kClusterSmemMax) !=
+            cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kClusterCtas;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(kClusterCtas);
+    cfg.blockDim = dim3(kPanelThreads);
+    cfg.dynamicSmemBytes = kClusterSmemMax;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, lu_panel_cluster_kernel<T>, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    ok = clusters >= 1 ? 1 : 0;
+    return ok == 1;
+}
+
+// Panel width for the cluster path: the widest of 128/64/32 (FP32) or
+// 64/32 (FP64) whose ceil(n/16) rows fit a CTA's shared memory; 0 if none.
+template <typename T>
+static int cluster_panel_width(int64_t n)
+{
+    const int64_t rows = ceil_div(n, kClusterCtas);
+    const int cands[3] = {sizeof(T) == 8 ? 64 : 128, sizeof(T) == 8 ? 32 : 64, 32};
+    for (int w : cands)
+        if ((size_t)rows * (w + 1) * sizeof(T) <= kClusterSmemMax) return w;
+    return 0;
+}
+
+template <typename T>
+static tmvg_status launch_panel_cluster(Context* c, T* A, int64_t lda, int64_t n, int64_t k, int nb,
+                                        int64_t* P, const unsigned char* modes, int* pairs)
+{
+    const int64_t m = n - k;
+    const int rpc = (int)ceil_div(m, kClusterCtas);
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kClusterCtas;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(kClusterCtas);
+    cfg.blockDim = dim3(kPanelThreads);
+    cfg.dynamicSmemBytes = (size_t)rpc * (nb + 1) * sizeof(T);
+    cfg.stream = c->stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    ++c->launches;
+    return check_cuda(c,
+                      cudaLaunchKernelEx(&cfg, lu_panel_cluster_kernel<T>, A, lda, n, k, nb, P,
+                                         modes, rpc, pairs),
+                      "lu: cluster panel launch");
+}
+
+// Can this device run the 16-CTA cluster of the register-resident panel?
+template <typename T>
+static bool reg_panel_ok(Context* c)
+{
+    int& ok = c->reg_cluster_ok[sizeof(T) == 8 ? 0 : 1];
+    if (ok >= 0) return ok == 1;
+    ok = 0;
+    auto kern = lu_panel_cluster_reg_kernel<T, RegPanel<T>::NB>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kClusterCtas;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(kClusterCtas);
+    cfg.blockDim = dim3(kRegPanelThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, kern, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    ok = clusters >= 1 ? 1 : 0;
+    return ok == 1;
+}
+
+template <typename T>
+static tmvg_status launch_panel_cluster_reg(Context* c, T* A, int64_t lda, int64_t n, int64_t k,
+                                            int nb, int64_t* P, const unsigned char* modes, int* pairs)
+{
+    const int64_t m = n - k;
+    const int rpc = (int)ceil_div(m, kClusterCtas);
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kClusterCtas;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(kClusterCtas);
+    cfg.blockDim = dim3(kRegPanelThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = c->stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    ++c->launches;
+    return check_cuda(c,
+                      cudaLaunchKernelEx(&cfg, lu_panel_cluster_reg_kernel<T, RegPanel<T>::NB>, A,
+                                         lda, n, k, nb, P, modes, rpc, pairs),
+                      "lu: register panel launch");
+}
+
 template <typename T>
 tmvg_status lu_factor(Context* c, int64_t n, T* A, int64_t lda, int64_t* P)
 {
     if (n < 0 || lda < std::max<int64_t>(n, 1)) return set_error(c, TMVG_BAD_ARG, "lu: bad n/lda");
     if (n == 0) return TMVG_OK;
-    const int nbmax = panel_width<T>();
+    // one panel row per thread of a 16-CTA cluster while the rows fit
+    const bool reg = n <= (int64_t)kClusterCtas * kRegPanelThreads && reg_panel_ok<T>(c);
+    const int cl_nb = reg ? RegPanel<T>::NB : cluster_panel_ok<T>(c) ? cluster_panel_width<T>(n) : 0;
+    const int nbmax = cl_nb > 0 ? cl_nb : panel_width<T>();
 
     // Panel geometry: one CTA per 256 rows up to one per SM.
     const int64_t G_full = std::min<int64_t>(c->num_sms, ceil_div(n, kPanelThreads));
@@ -450,7 +1057,8 @@ tmvg_status lu_factor(Context* c, int64_t n, T* A, int64_t lda, int64_t* P)
     const size_t off_rows = (off_idx + sizeof(long long) * 2 * G_full + 255) & ~size_t(255);
     const size_t off_diag = off_rows + sizeof(T) * 2 * G_full * kPanelMax;
     const size_t off_modes = (off_diag + sizeof(T) * 2 * kPanelMax + 255) & ~size_t(255);
-    const size_t bytes = off_modes + (size_t)n;
+    const size_t off_pairs = (off_modes + (size_t)n + 255) & ~size_t(255);
+    const size_t bytes = off_pairs + sizeof(int) * (1 + 2 * kMaxPairs);
     unsigned char* ws = (unsigned char*)workspace(c, bytes);
     if (!ws) return TMVG_OOM;
     double* cand_key = (double*)(ws + off_key);
@@ -458,6 +1066,7 @@ tmvg_status lu_factor(Context* c, int64_t n, T* A, int64_t lda, int64_t* P)
     T* cand_rows = (T*)(ws + off_rows);
     T* diag_row = (T*)(ws + off_diag);
     unsigned char* modes = ws + off_modes;
+    int* pairs = (int*)(ws + off_pairs);
     {
         std::vector<unsigned char> hm((size_t)n, 0);
         leaf_modes(0, n, hm);
@@ -481,6 +1090,18 @@ tmvg_status lu_factor(Context* c, int64_t n, T* A, int64_t lda, int64_t* P)
     for (int64_t k = 0; k < n; k += nbmax) {
         const int nb = (int)std::min<int64_t>(nbmax, n - k);
         const int64_t m = n - k;
+        if (cl_nb > 0) {
+            tmvg_status st;
+            {
+                ScopedTimer timer(c, kClsPanel, 2.0 * sizeof(T) * m * nb, panel_flops(m, nb));
+                st = reg ? launch_panel_cluster_reg<T>(c, A, lda, n, k, nb, P, modes + k, pairs)
+                         : launch_panel_cluster<T>(c, A, lda, n, k, nb, P, modes + k, pairs);
+            }
+            if (st) return st;
+            st = panel_update<T>(c, n, A, lda, k, nb, pairs);
+            if (st) return st;
+            continue;
+        }
         const int G = (int)std::min<int64_t>(c->num_sms, ceil_div(m, kPanelThreads));
         const int rows_per_cta = (int)ceil_div(m, G);
         const size_t smem = (size_t)rows_per_cta * (nb + 1) * sizeof(T);
@@ -495,32 +1116,18 @@ tmvg_status lu_factor(Context* c, int64_t n, T* A, int64_t lda, int64_t* P)
         unsigned* bar = c->dbar;
         int* err = c->dflags;
         void* args[] = {&Ap, &ldav, &nv, &kv, &nbv, &Pp, &mp, &rpc, &cand_key, &cand_idx,
-                        &cand_rows, &diag_row, &bar, &err};
-        st = check_cuda(c,
-                        cudaLaunchCooperativeKernel((const void*)lu_panel_kernel<T>, dim3(G),
-                                                    dim3(kPanelThreads), args, smem, c->stream),
-                        "lu: panel launch");
+                        &cand_rows, &diag_row, &bar, &err, &pairs};
+        {
+            ScopedTimer timer(c, kClsPanel, 2.0 * sizeof(T) * m * nb, panel_flops(m, nb));
+            st = check_cuda(c,
+                            cudaLaunchCooperativeKernel((const void*)lu_panel_kernel<T>, dim3(G),
+                                                        dim3(kPanelThreads), args, smem, c->stream),
+                            "lu: panel launch");
+        }
         if (st) return st;
         ++c->launches;
-
-        // interchanges on the other columns
-        if (n > nb) {
-            laswp_kernel<T><<<(unsigned)ceil_div(n, 128), 128, 0, c->stream>>>(A, lda, n, k, nb, P,
-                                                                              k, k + nb);
-            ++c->launches;
-            st = check_cuda(c, cudaGetLastError(), "lu: laswp launch");
-            if (st) return st;
-        }
-        if (k + nb < n) {
-            const int64_t rest = n - k - nb;
-            st = tri_solve<T>(c, nb, A + k + k * lda, 1, lda, false, true, rest,
-                              A + k + (k + nb) * lda, 1, lda, false);
-            if (st) return st;
-            st = gemm<T>(c, rest, rest, nb, T(-1), Mat<const T>{A + (k + nb) + k * lda, 1, lda},
-                         Mat<const T>{A + k + (k + nb) * lda, 1, lda}, T(1),
-                         Mat<T>{A + (k + nb) + (k + nb) * lda, 1, lda});
-            if (st) return st;
-        }
+        st = panel_update<T>(c, n, A, lda, k, nb, pairs);
+        if (st) return st;
     }
     return collect_device_error(c, "lu_factor");
 }
@@ -627,7 +1234,7 @@ template tmvg_status copy_matrix<float>(Context*, int64_t, int64_t, const float*
 // tmvg_lu_decompose_f64_noalloc serves them: it runs the same kernels as
 // tmvg_lu_decompose_f64 but takes every scratch word from the file-scope
 // array below, which each GPU that loads this library holds until the process
-// exits (kNoAllocBytes, about 343 KiB).  It needs no tmvg_handle (creating one
+// exits (kNoAllocBytes = 353,540 bytes, about 345 KiB).  It needs no tmvg_handle (creating one
 // allocates).  Limits: n <= kNoAllocMaxN = 16384 (larger n returns
 // TMVG_UNSUPPORTED before any device work); at most kNoAllocMaxCtas = 160
 // panel CTAs are used.
@@ -643,7 +1250,8 @@ constexpr size_t kNaOffIdx = kNaOffKey + sizeof(double) * 2 * kNoAllocMaxCtas;
 constexpr size_t kNaOffRows = kNaOffIdx + sizeof(long long) * 2 * kNoAllocMaxCtas;
 constexpr size_t kNaOffDiag = kNaOffRows + sizeof(double) * 2 * kNoAllocMaxCtas * kPanelMax;
 constexpr size_t kNaOffModes = kNaOffDiag + sizeof(double) * 2 * kPanelMax;
-constexpr size_t kNoAllocBytes = kNaOffModes + kNoAllocMaxN;
+constexpr size_t kNaOffPairs = kNaOffModes + kNoAllocMaxN;  // int[1 + 2*kMaxPairs]
+constexpr size_t kNoAllocBytes = kNaOffPairs + sizeof(int) * (1 + 2 * kMaxPairs);
 constexpr int kNoAllocMaxDevices = 64;
 }  // namespace
 
@@ -707,6 +1315,7 @@ extern "C" tmvg_status tmvg_lu_decompose_f64_noalloc(int64_t n, double* A, int64
     double* cand_rows = reinterpret_cast<double*>(s + kNaOffRows);
     double* diag_row = reinterpret_cast<double*>(s + kNaOffDiag);
     unsigned char* modes = s + kNaOffModes;
+    int* pairs = reinterpret_cast<int*>(s + kNaOffPairs);
 
     // The array keeps the last call's contents: clear the error words.
     st = check_cuda(&c, cudaMemsetAsync(s, 0, 256, c.stream), "noalloc: clear");
@@ -739,28 +1348,14 @@ extern "C" tmvg_status tmvg_lu_decompose_f64_noalloc(int64_t n, double* A, int64
         unsigned* bar = c.dbar;
         int* err = c.dflags;
         void* args[] = {&Ap, &ldav, &nv, &kv, &nbv, &Pp, &mp, &rpc, &cand_key, &cand_idx,
-                        &cand_rows, &diag_row, &bar, &err};
+                        &cand_rows, &diag_row, &bar, &err, &pairs};
         st = check_cuda(&c,
                         cudaLaunchCooperativeKernel((const void*)lu_panel_kernel<double>, dim3(G),
                                                     dim3(kPanelThreads), args, smem, c.stream),
                         "noalloc: panel launch");
         if (st) return st;
-        if (n > nb) {
-            laswp_kernel<double><<<(unsigned)ceil_div(n, 128), 128, 0, c.stream>>>(A, lda, n, k, nb, P,
-                                                                                  k, k + nb);
-            st = check_cuda(&c, cudaGetLastError(), "noalloc: laswp launch");
-            if (st) return st;
-        }
-        if (k + nb < n) {
-            const int64_t rest = n - k - nb;
-            st = tri_solve<double>(&c, nb, A + k + k * lda, 1, lda, false, true, rest,
-                                   A + k + (k + nb) * lda, 1, lda, false);
-            if (st) return st;
-            st = gemm<double>(&c, rest, rest, nb, -1.0, Mat<const double>{A + (k + nb) + k * lda, 1, lda},
-                              Mat<const double>{A + k + (k + nb) * lda, 1, lda}, 1.0,
-                              Mat<double>{A + (k + nb) + (k + nb) * lda, 1, lda});
-            if (st) return st;
-        }
+        st = panel_update<double>(&c, n, A, lda, k, nb, pairs);
+        if (st) return st;
     }
     int code[2] = {0, 0};
     st = check_cuda(&c, cudaMemcpyAsync(code, c.dflags, sizeof(code), cudaMemcpyDeviceToHost, c.stream),

@@ -153,7 +153,11 @@ tmvg_status lu_solve_mixed(Context* c, int64_t n, const double* A, int64_t lda, 
     const size_t o_v = o_inv + al(sizeof(int) * n);
     const size_t o_part = o_v + al(sizeof(float) * n);
     const size_t o_sc = o_part + al(sizeof(double) * (size_t)nchunks * n);
-    const size_t bytes = o_sc + 256;
+    const int64_t nib = ceil_div(n, kInvBlock);
+    const size_t o_dl = o_sc + 256;
+    const size_t o_du = o_dl + al(sizeof(float) * (size_t)nib * kInvBlock * kInvBlock);
+    const size_t o_sg = o_du + al(sizeof(float) * (size_t)nib * kInvBlock * kInvBlock);
+    const size_t bytes = o_sg + al(sizeof(int) * 2 * nib);
     unsigned char* ws = (unsigned char*)workspace2(c, bytes);
     if (!ws) return TMVG_OOM;
     float* As = (float*)(ws + o_As);
@@ -164,6 +168,10 @@ tmvg_status lu_solve_mixed(Context* c, int64_t n, const double* A, int64_t lda, 
     double* part = (double*)(ws + o_part);
     unsigned long long* sc = (unsigned long long*)(ws + o_sc);  // anorm, bmax, rmax, xmax
     unsigned long long hsc[4];
+    float* dinvL = (float*)(ws + o_dl);
+    float* dinvU = (float*)(ws + o_du);
+    int* singL = (int*)(ws + o_sg);
+    int* singU = singL + nib;
 
     tmvg_status st;
     auto launched = [&](const char* what) {
@@ -186,6 +194,28 @@ tmvg_status lu_solve_mixed(Context* c, int64_t n, const double* A, int64_t lda, 
     if (st) return st;
     invert_perm_kernel<<<blocks_for(n, 256), 256, 0, c->stream>>>(n, perm, inv);
     if ((st = launched("invperm"))) return st;
+    // inverses of the 128 x 128 diagonal blocks of L and U, reused by every
+    // solve of the refinement loop
+    st = trsv_factor_inverse_blocks<float>(c, n, As, 1, n, false, true, dinvL, singL);
+    if (st) return st;
+    st = trsv_factor_inverse_blocks<float>(c, n, As, 1, n, true, false, dinvU, singU);
+    if (st) return st;
+    // one triangular solve reads its triangle, the inverted diagonal blocks
+    // and the vector (in and out)
+    const double fn = (double)n;
+    const double tri_bytes = 4.0 * (fn * (fn + 1) / 2 + fn * kInvBlock + 2 * fn);
+    auto solve32 = [&](float* vec) -> tmvg_status {
+        tmvg_status s2;
+        {
+            ScopedTimer timer(c, kClsTriSolve, tri_bytes, fn * fn);
+            s2 = trsv_with_inverse_blocks<float>(c, n, As, 1, n, false, true, dinvL, singL, vec, 1,
+                                                 true);
+        }
+        if (s2) return s2;
+        ScopedTimer timer(c, kClsTriSolve, tri_bytes, fn * fn);
+        return trsv_with_inverse_blocks<float>(c, n, As, 1, n, true, false, dinvU, singU, vec, 1,
+                                               true);
+    };
 
     int worst_iters = 0;
     bool all_conv = true;
@@ -202,9 +232,7 @@ tmvg_status lu_solve_mixed(Context* c, int64_t n, const double* A, int64_t lda, 
         // 3. initial solve
         gather_to_f32_kernel<<<blocks_for(n, 256), 256, 0, c->stream>>>(n, perm, b, 1, v);
         if ((st = launched("gather"))) return st;
-        st = trsm_sync_free<float>(c, n, As, 1, n, false, true, 1, v, 1, n, true);
-        if (st) return st;
-        st = trsm_sync_free<float>(c, n, As, 1, n, true, false, 1, v, 1, n, true);
+        st = solve32(v);
         if (st) return st;
         update_kernel<<<blocks_for(n, 256), 256, 0, c->stream>>>(n, v, x, 1, false);
         if ((st = launched("update"))) return st;
@@ -217,12 +245,17 @@ tmvg_status lu_solve_mixed(Context* c, int64_t n, const double* A, int64_t lda, 
             st = check_cuda(c, cudaMemsetAsync(sc + 2, 0, 2 * sizeof(unsigned long long), c->stream),
                             "memset");
             if (st) return st;
-            residual_partial_kernel<<<dim3(blocks_for(n, 256), nchunks), 256, 0, c->stream>>>(
-                n, A, lda, x, 1, part);
-            if ((st = launched("residual"))) return st;
-            residual_final_kernel<<<blocks_for(n, 256), 256, 0, c->stream>>>(
-                n, nchunks, part, b, 1, x, 1, inv, v, sc + 2, sc + 3);
-            if ((st = launched("residual_final"))) return st;
+            {
+                // reads A (FP64) once, x per column chunk, b; writes the FP32 residual
+                ScopedTimer timer(c, kClsResidual, 8.0 * fn * fn + 8.0 * fn * (nchunks + 1) + 4.0 * fn,
+                                  2.0 * fn * fn);
+                residual_partial_kernel<<<dim3(blocks_for(n, 256), nchunks), 256, 0, c->stream>>>(
+                    n, A, lda, x, 1, part);
+                if ((st = launched("residual"))) return st;
+                residual_final_kernel<<<blocks_for(n, 256), 256, 0, c->stream>>>(
+                    n, nchunks, part, b, 1, x, 1, inv, v, sc + 2, sc + 3);
+                if ((st = launched("residual_final"))) return st;
+            }
             st = check_cuda(c,
                             cudaMemcpyAsync(hsc, sc, sizeof(hsc), cudaMemcpyDeviceToHost, c->stream),
                             "norms d2h");
@@ -243,9 +276,7 @@ tmvg_status lu_solve_mixed(Context* c, int64_t n, const double* A, int64_t lda, 
             }
             if (it >= max_iter || !(berr == berr)) break;
             // 5. correction
-            st = trsm_sync_free<float>(c, n, As, 1, n, false, true, 1, v, 1, n, true);
-            if (st) return st;
-            st = trsm_sync_free<float>(c, n, As, 1, n, true, false, 1, v, 1, n, true);
+            st = solve32(v);
             if (st) return st;
             update_kernel<<<blocks_for(n, 256), 256, 0, c->stream>>>(n, v, x, 1, true);
             if ((st = launched("update"))) return st;

@@ -203,6 +203,217 @@ tmvg_status trsm_sync_free(Context* c, int64_t n, const T* tri, int64_t tsi, int
 }
 
 // ---------------------------------------------------------------------
+// Repeated single right-hand-side solves with one factor (the refinement
+// loop of the mixed solve): the same sync-free block chain, with 128-row
+// blocks whose diagonal blocks are inverted once per factor, so the step on
+// the chain's critical path is two short mat-vecs instead of a 128-step
+// substitution.  Blocks with a zero diagonal keep the substitution (and
+// TMV's zero-skipping semantics); the others use D^-1.
+// ---------------------------------------------------------------------
+constexpr int kIB = 128;  // block rows of the inverse-diagonal solve
+
+// One CTA per diagonal block: Dinv_b = D_b^-1 (lower, column-major kIB x kIB
+// at dinv + b*kIB*kIB).  singular[b] = 1 if D_b has a zero diagonal.
+template <typename T>
+__global__ void __launch_bounds__(kIB)
+invert_diag_blocks_kernel(int64_t n, const T* __restrict__ tri, int64_t tsi, int64_t tsj,
+                          bool unit, T* __restrict__ dinv, int* __restrict__ singular)
+{
+    extern __shared__ __align__(16) unsigned char inv_smem[];
+    T* D = reinterpret_cast<T*>(inv_smem);  // [kIB][kIB+1]
+    T* X = D + kIB * (kIB + 1);              // [kIB][kIB+1], X[i][j] = (D^-1)_ij
+    __shared__ int s_sing;
+    const int64_t b = blockIdx.x;
+    const int64_t r0 = b * kIB;
+    const int rows = (int)min((int64_t)kIB, n - r0);
+    const int tid = threadIdx.x;
+    if (tid == 0) s_sing = 0;
+    for (int t = tid; t < kIB * kIB; t += kIB) {
+        const int i = t % kIB, j = t / kIB;
+        D[i * (kIB + 1) + j] = (i < rows && j <= i) ? tri[(r0 + i) * tsi + (r0 + j) * tsj] : T(0);
+    }
+    __syncthreads();
+    if (!unit && tid < rows && D[tid * (kIB + 1) + tid] == T(0)) s_sing = 1;
+    __syncthreads();
+    if (s_sing) {
+        if (tid == 0) singular[b] = 1;
+        return;
+    }
+    // column j of the inverse by forward substitution
+    const int j = tid;
+    if (j < rows) {
+        for (int i = 0; i < j; ++i) X[i * (kIB + 1) + j] = T(0);
+        const T djj = unit ? T(1) : D[j * (kIB + 1) + j];
+        X[j * (kIB + 1) + j] = T(1) / djj;
+        for (int i = j + 1; i < rows; ++i) {
+            T s = T(0);
+            for (int l = j; l < i; ++l) s -= D[i * (kIB + 1) + l] * X[l * (kIB + 1) + j];
+            X[i * (kIB + 1) + j] = unit ? s : s / D[i * (kIB + 1) + i];
+        }
+    }
+    __syncthreads();
+    T* out = dinv + b * (int64_t)kIB * kIB;
+    for (int t = tid; t < kIB * kIB; t += kIB) {
+        const int i = t % kIB, jj = t / kIB;
+        out[t] = (i < rows && jj < rows) ? X[i * (kIB + 1) + jj] : T(0);
+    }
+    if (tid == 0) singular[b] = 0;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+trsv_invdiag_kernel(int64_t n, const T* __restrict__ tri, int64_t tsi, int64_t tsj,
+                    const T* __restrict__ dinv, const int* __restrict__ singular, bool unit,
+                    T* x, int64_t incx, bool skip_zero, unsigned* flags, unsigned epoch,
+                    unsigned long long* ticket, int* err)
+{
+    __shared__ int s_blk, s_abort;
+    __shared__ T xj[kIB];
+    __shared__ T rhs[kIB];
+    __shared__ T part[2][kIB];
+    const int tid = threadIdx.x;
+    const int i = tid & (kIB - 1), h = tid >> 7;  // row of the block, half of the columns
+    if (tid == 0) {
+        s_blk = (int)atomicAdd(ticket, 1ull);
+        s_abort = 0;
+    }
+    __syncthreads();
+    const int64_t b = s_blk;
+    const int64_t nblk = (n + kIB - 1) / kIB;
+    if (b >= nblk) return;
+    const int64_t r0 = b * kIB;
+    const int rows = (int)min((int64_t)kIB, n - r0);
+
+    T acc = T(0);
+    for (int64_t j = 0; j < b; ++j) {
+        const int64_t c0 = j * kIB + h * 64;
+        T a[64];
+#pragma unroll
+        for (int c = 0; c < 64; ++c) a[c] = (i < rows) ? tri[(r0 + i) * tsi + (c0 + c) * tsj] : T(0);
+        if (tid == 0) {
+            unsigned spins = 0;
+            while (ld_acquire(flags + j) != epoch) {
+                if (++spins > kSpinLimit || *((volatile int*)err) == kDevTimeout) {
+                    atomicCAS(err, (int)kDevOk, (int)kDevTimeout);
+                    s_abort = 1;
+                    break;
+                }
+                if (spins > 32) __nanosleep(32);
+            }
+        }
+        __syncthreads();
+        if (s_abort) return;
+        if (tid < kIB) xj[tid] = __ldcg(&x[(j * kIB + tid) * incx]);
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < 64; ++c) acc -= a[c] * xj[h * 64 + c];
+        __syncthreads();
+    }
+    part[h][i] = acc;
+    if (tid < kIB) rhs[tid] = tid < rows ? x[(r0 + tid) * incx] : T(0);
+    __syncthreads();
+    if (tid < kIB) rhs[tid] += part[0][tid] + part[1][tid];
+    __syncthreads();
+    if (!singular[b]) {
+        // x_b = Dinv_b rhs (lower): row i sums columns l <= i, split in halves
+        const T* Di = dinv + b * (int64_t)kIB * kIB;
+        T s = T(0);
+        const int l0 = h * 64;
+        for (int l = l0; l < l0 + 64; ++l) s += Di[i + l * kIB] * rhs[l];
+        part[h][i] = s;
+        __syncthreads();
+        if (tid < rows) x[(r0 + tid) * incx] = part[0][tid] + part[1][tid];
+    } else if (tid < 32) {
+        // zero diagonal somewhere: substitution with TMV's zero skipping
+        bool sing = false;
+        for (int jj = 0; jj < rows; ++jj) {
+            __syncwarp();
+            T v = rhs[jj];
+            if (!unit) {
+                const T d = tri[(r0 + jj) * tsi + (r0 + jj) * tsj];
+                if (skip_zero) {
+                    if (v != T(0)) {
+                        if (d == T(0)) sing = true;
+                        else v = v / d;
+                    }
+                } else {
+                    if (d == T(0)) sing = true;
+                    else v = v * (T(1) / d);
+                }
+            }
+            __syncwarp();
+            if (tid == 0) rhs[jj] = v;
+            if (v != T(0) || !skip_zero)
+                for (int k2 = jj + 1 + tid; k2 < rows; k2 += 32)
+                    rhs[k2] -= tri[(r0 + k2) * tsi + (r0 + jj) * tsj] * v;
+        }
+        if (sing) atomicCAS(err, (int)kDevOk, (int)kDevSingular);
+        __syncwarp();
+        for (int k2 = tid; k2 < rows; k2 += 32) x[(r0 + k2) * incx] = rhs[k2];
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) st_release(flags + b, epoch);
+}
+
+template <typename T>
+tmvg_status trsv_factor_inverse_blocks(Context* c, int64_t n, const T* tri, int64_t tsi,
+                                       int64_t tsj, bool upper, bool unit, T* dinv, int* singular)
+{
+    if (n <= 0) return TMVG_OK;
+    if (upper) {
+        tri = tri + (n - 1) * (tsi + tsj);
+        tsi = -tsi;
+        tsj = -tsj;
+    }
+    const int64_t nblk = ceil_div(n, kIB);
+    const size_t smem = sizeof(T) * 2 * kIB * (kIB + 1);
+    cudaFuncSetAttribute(invert_diag_blocks_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    invert_diag_blocks_kernel<T><<<(unsigned)nblk, kIB, smem, c->stream>>>(n, tri, tsi, tsj, unit,
+                                                                            dinv, singular);
+    ++c->launches;
+    return check_cuda(c, cudaGetLastError(), "invert diag launch");
+}
+
+template <typename T>
+tmvg_status trsv_with_inverse_blocks(Context* c, int64_t n, const T* tri, int64_t tsi, int64_t tsj,
+                                     bool upper, bool unit, const T* dinv, const int* singular,
+                                     T* x, int64_t incx, bool skip_zero)
+{
+    if (n <= 0) return TMVG_OK;
+    if (upper) {
+        tri = tri + (n - 1) * (tsi + tsj);
+        tsi = -tsi;
+        tsj = -tsj;
+        x = x + (n - 1) * incx;
+        incx = -incx;
+    }
+    const int64_t nblk = ceil_div(n, kIB);
+    if (nblk > kTrsvFlagCap) return set_error(c, TMVG_UNSUPPORTED, "trsv: n too large");
+    const unsigned epoch = ++c->trsv_epoch;
+    tmvg_status st = check_cuda(
+        c, cudaMemsetAsync(c->trsv_ticket, 0, sizeof(unsigned long long), c->stream), "ticket");
+    if (st) return st;
+    trsv_invdiag_kernel<T><<<(unsigned)nblk, 256, 0, c->stream>>>(
+        n, tri, tsi, tsj, dinv, singular, unit, x, incx, skip_zero, c->trsv_flags, epoch,
+        c->trsv_ticket, c->dflags);
+    ++c->launches;
+    return check_cuda(c, cudaGetLastError(), "trsv invdiag launch");
+}
+
+template tmvg_status trsv_factor_inverse_blocks<float>(Context*, int64_t, const float*, int64_t,
+                                                       int64_t, bool, bool, float*, int*);
+template tmvg_status trsv_factor_inverse_blocks<double>(Context*, int64_t, const double*, int64_t,
+                                                        int64_t, bool, bool, double*, int*);
+template tmvg_status trsv_with_inverse_blocks<float>(Context*, int64_t, const float*, int64_t,
+                                                     int64_t, bool, bool, const float*, const int*,
+                                                     float*, int64_t, bool);
+template tmvg_status trsv_with_inverse_blocks<double>(Context*, int64_t, const double*, int64_t,
+                                                      int64_t, bool, bool, const double*,
+                                                      const int*, double*, int64_t, bool);
+
+// ---------------------------------------------------------------------
 // Interchanges -> gather permutation: perm = identity, then for i in order
 // swap(perm[i], perm[P[i]]); row i of P*B is row perm[i] of B.  One CTA,
 // sequential in shared memory (n <= kPermSmemMax).

@@ -16,6 +16,18 @@ tmvg_status trsm_sync_free(Context* c, int64_t n, const T* tri, int64_t tsi, int
                            bool upper, bool unit, int64_t nrhs, T* B, int64_t bsi, int64_t bsj,
                            bool skip_zero);
 
+// Repeated one-column solves with one triangle: invert its 128 x 128
+// diagonal blocks once (dinv: ceil(n/128)*128*128 elements, singular:
+// ceil(n/128) ints), then solve x := T^-1 x with one launch per solve.
+constexpr int64_t kInvBlock = 128;
+template <typename T>
+tmvg_status trsv_factor_inverse_blocks(Context* c, int64_t n, const T* tri, int64_t tsi,
+                                       int64_t tsj, bool upper, bool unit, T* dinv, int* singular);
+template <typename T>
+tmvg_status trsv_with_inverse_blocks(Context* c, int64_t n, const T* tri, int64_t tsi, int64_t tsj,
+                                     bool upper, bool unit, const T* dinv, const int* singular,
+                                     T* x, int64_t incx, bool skip_zero);
+
 // Interchange vector P (TMV/LAPACK form) -> gather permutation perm with
 // (P B)[i] = B[perm[i]].
 tmvg_status pivots_to_perm(Context* c, int64_t n, const int64_t* P, int* perm);
