@@ -1,5 +1,6 @@
 // capi.cu -- extern "C" entry points (include/tmvg.h) and context plumbing.
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -64,12 +65,12 @@ static cudaEvent_t pooled_event(Context* c)
     return e;
 }
 
-ScopedTimer::ScopedTimer(Context* c, int cls, double bytes, double flops)
-    : c_(c), cls_(cls), bytes_(bytes), flops_(flops)
+ScopedTimer::ScopedTimer(Context* c, int cls, double bytes, double flops, cudaStream_t stream)
+    : c_(c), cls_(cls), bytes_(bytes), flops_(flops), stream_(stream)
 {
     if (!c_->timing) return;
     a_ = pooled_event(c_);
-    if (a_ && cudaEventRecord(a_, c_->stream) != cudaSuccess) {
+    if (a_ && cudaEventRecord(a_, stream_) != cudaSuccess) {
         cudaGetLastError();
         c_->event_pool.push_back(a_);
         a_ = nullptr;
@@ -80,7 +81,7 @@ ScopedTimer::~ScopedTimer()
 {
     if (!a_) return;
     cudaEvent_t b = pooled_event(c_);
-    if (!b || cudaEventRecord(b, c_->stream) != cudaSuccess) {
+    if (!b || cudaEventRecord(b, stream_) != cudaSuccess) {
         cudaGetLastError();
         c_->event_pool.push_back(a_);
         if (b) c_->event_pool.push_back(b);
@@ -89,11 +90,30 @@ ScopedTimer::~ScopedTimer()
     c_->spans.push_back({a_, b, cls_, bytes_, flops_});
 }
 
+tmvg_status ensure_side_stream(Context* c)
+{
+    if (c->side) return TMVG_OK;
+    int least = 0, greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    if (cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, greatest) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_narrow, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_panel, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(c, TMVG_CUDA_ERROR, "side stream creation failed");
+    }
+    return TMVG_OK;
+}
+
 // Folds every recorded span into the per-class sums (synchronises).
 static tmvg_status drain_spans(Context* c)
 {
     tmvg_status st = check_cuda(c, cudaStreamSynchronize(c->stream), "timing: sync");
     if (st) return st;
+    if (c->side) {
+        st = check_cuda(c, cudaStreamSynchronize(c->side), "timing: sync");
+        if (st) return st;
+    }
     for (const TimedSpan& s : c->spans) {
         float ms = 0.0f;
         if (cudaEventElapsedTime(&ms, s.a, s.b) != cudaSuccess) {
@@ -299,6 +319,8 @@ tmvg_status tmvg_create(tmvg_handle* h, int device)
         delete c;
         return TMVG_CUDA_ERROR;
     }
+    const char* ser = std::getenv("TMVG_SERIALIZE_LOOKAHEAD");
+    c->serialize_lookahead = ser && ser[0] == '1';
     *h = reinterpret_cast<tmvg_handle>(c);
     return TMVG_OK;
 }
@@ -320,6 +342,10 @@ tmvg_status tmvg_destroy(tmvg_handle h)
         cudaEventDestroy(sp.b);
     }
     for (cudaEvent_t e : c->event_pool) cudaEventDestroy(e);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_narrow) cudaEventDestroy(c->ev_narrow);
+    if (c->ev_panel) cudaEventDestroy(c->ev_panel);
+    if (c->side) cudaStreamDestroy(c->side);
     delete c;
     return TMVG_OK;
 }

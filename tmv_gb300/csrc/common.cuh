@@ -84,13 +84,27 @@ struct Context {
     double t_ms[kClsCount] = {};
     double t_bytes[kClsCount] = {};
     double t_flops[kClsCount] = {};
+    // Look-ahead of the LU: a high-priority side stream for the panels and
+    // the events that order it against `stream` (created on first use).
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_narrow = nullptr, ev_panel = nullptr;
+    // TMVG_SERIALIZE_LOOKAHEAD=1 at creation: every side-stream panel is
+    // waited for on the host before the main stream's next launch, which
+    // fixes one extreme interleaving of the two streams (used by tests to
+    // show that no cross-stream dependency is missing).
+    bool serialize_lookahead = false;
 };
+
+// The side stream and its events (nullptr-safe to call repeatedly).
+tmvg_status ensure_side_stream(Context* c);
 
 // Records CUDA events on c->stream around its scope when timing is on;
 // the launches inside the scope count as one span of class `cls`.
 class ScopedTimer {
   public:
-    ScopedTimer(Context* c, int cls, double bytes, double flops);
+    ScopedTimer(Context* c, int cls, double bytes, double flops, cudaStream_t stream);
+    ScopedTimer(Context* c, int cls, double bytes, double flops)
+        : ScopedTimer(c, cls, bytes, flops, c->stream) {}
     ~ScopedTimer();
     ScopedTimer(const ScopedTimer&) = delete;
     ScopedTimer& operator=(const ScopedTimer&) = delete;
@@ -99,6 +113,7 @@ class ScopedTimer {
     Context* c_;
     int cls_;
     double bytes_, flops_;
+    cudaStream_t stream_;
     cudaEvent_t a_ = nullptr;
 };
 

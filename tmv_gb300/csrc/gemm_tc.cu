@@ -19,6 +19,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include "async.cuh"
 #include "gemm.cuh"
 #include "gemm_tc.cuh"
 
@@ -30,46 +31,6 @@ namespace tmvg {
 constexpr int kTcM = 128;        // tile rows (UMMA M)
 constexpr int kTcThreads = 128;  // four warps: one per 32 TMEM lanes
 constexpr int kKChunk = 32;      // floats in one 128-byte swizzle row
-constexpr unsigned kTryWaitLimit = 1u << 22;
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p)
-{
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_fence_init()
-{
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-                 "r"(bytes)
-                 : "memory");
-}
-
-// Wait for the phase with the given parity to complete; false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
-{
-    for (unsigned spins = 0; spins < kTryWaitLimit; ++spins) {
-        uint32_t done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(smem_u32(bar)), "r"(parity)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
-}
 
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0,
                                             int c1)
@@ -288,12 +249,6 @@ tf32x3_update_kernel(const __grid_constant__ CUtensorMap mAhi, const __grid_cons
     }
 }
 
-__device__ __forceinline__ float tf32_round(float x)
-{
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return __uint_as_float(r);
-}
 
 // A (m x K, column-major, lda) -> hi/lo row-major m x K (K contiguous), via
 // 32 x 32 shared-memory tiles so both sides stay coalesced.
@@ -409,29 +364,61 @@ static bool make_c_map(CUtensorMap* map, float* C, int64_t m, int64_t n, int64_t
               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+tmvg_status tf32x3_buffers(Context* c, int64_t m, int64_t n, int64_t K, Tf32x3Buffers* b)
+{
+    // B hi/lo first so that their place depends on n and K only
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t sa = al(sizeof(float) * (size_t)m * K), sb = al(sizeof(float) * (size_t)n * K);
+    unsigned char* ws = (unsigned char*)workspace3(c, 2 * sa + 2 * sb);
+    if (!ws) return TMVG_OOM;
+    b->Bhi = (float*)ws;
+    b->Blo = (float*)(ws + sb);
+    b->Ahi = (float*)(ws + 2 * sb);
+    b->Alo = (float*)(ws + 2 * sb + sa);
+    return TMVG_OK;
+}
+
+tmvg_status tf32x3_split_a(Context* c, int64_t m, int64_t K, const float* A, int64_t lda,
+                           const Tf32x3Buffers& b)
+{
+    if (m <= 0) return TMVG_OK;
+    split_transpose_kernel<<<dim3((unsigned)ceil_div(m, 32), (unsigned)ceil_div(K, 32)), dim3(32, 8), 0,
+                             c->stream>>>(m, (int)K, A, lda, b.Ahi, b.Alo);
+    ++c->launches;
+    return check_cuda(c, cudaGetLastError(), "tf32x3 split A");
+}
+
+tmvg_status tf32x3_split_b(Context* c, int64_t n, int64_t K, const float* B, int64_t ldb,
+                           const Tf32x3Buffers& b)
+{
+    if (n <= 0) return TMVG_OK;
+    split_cols_kernel<<<(unsigned)std::min<int64_t>(ceil_div(n * K, 256), 16 * c->num_sms), 256, 0,
+                        c->stream>>>(n, (int)K, B, ldb, b.Bhi, b.Blo);
+    ++c->launches;
+    return check_cuda(c, cudaGetLastError(), "tf32x3 split B");
+}
+
 tmvg_status gemm_f32_tf32x3_update(Context* c, int64_t m, int64_t n, int64_t K, const float* A,
                                    int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc)
 {
     if (m <= 0 || n <= 0 || K <= 0) return TMVG_OK;
     if (!tf32x3_supported(K)) return set_error(c, TMVG_UNSUPPORTED, "tf32x3: K must be 32, 64, 96 or 128");
     if (m > INT_MAX || n > INT_MAX) return set_error(c, TMVG_UNSUPPORTED, "tf32x3: size");
-    // scratch: A hi/lo (m x K) and B hi/lo (K x n), 256-byte aligned
-    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
-    const size_t sa = al(sizeof(float) * (size_t)m * K), sb = al(sizeof(float) * (size_t)n * K);
-    unsigned char* ws = (unsigned char*)workspace3(c, 2 * sa + 2 * sb);
-    if (!ws) return TMVG_OOM;
-    float* Ahi = (float*)ws;
-    float* Alo = (float*)(ws + sa);
-    float* Bhi = (float*)(ws + 2 * sa);
-    float* Blo = (float*)(ws + 2 * sa + sb);
-    split_transpose_kernel<<<dim3((unsigned)ceil_div(m, 32), (unsigned)ceil_div(K, 32)), dim3(32, 8), 0,
-                             c->stream>>>(m, (int)K, A, lda, Ahi, Alo);
-    ++c->launches;
-    split_cols_kernel<<<(unsigned)std::min<int64_t>(ceil_div(n * K, 256), 16 * c->num_sms), 256, 0,
-                        c->stream>>>(n, (int)K, B, ldb, Bhi, Blo);
-    ++c->launches;
-    tmvg_status st = check_cuda(c, cudaGetLastError(), "tf32x3 split");
-    if (st) return st;
+    Tf32x3Buffers b;
+    tmvg_status st = tf32x3_buffers(c, m, n, K, &b);
+    if (!st) st = tf32x3_split_a(c, m, K, A, lda, b);
+    if (!st) st = tf32x3_split_b(c, n, K, B, ldb, b);
+    if (!st) st = tf32x3_apply(c, m, n, K, b, C, ldc);
+    return st;
+}
+
+tmvg_status tf32x3_apply(Context* c, int64_t m, int64_t n, int64_t K, const Tf32x3Buffers& b, float* C,
+                         int64_t ldc)
+{
+    if (m <= 0 || n <= 0 || K <= 0) return TMVG_OK;
+    if (!tf32x3_supported(K)) return set_error(c, TMVG_UNSUPPORTED, "tf32x3: K must be 32, 64, 96 or 128");
+    if (m > INT_MAX || n > INT_MAX) return set_error(c, TMVG_UNSUPPORTED, "tf32x3: size");
+    const float *Ahi = b.Ahi, *Alo = b.Alo, *Bhi = b.Bhi, *Blo = b.Blo;
     const bool wide = n >= 128 && K <= 64;
     const int BN = wide ? 128 : 64;
     CUtensorMap maps[5];

@@ -18,6 +18,7 @@
 // include/tmv/TMV_Base.h:692-696) zeroes the sub-column and records P[j] = j.
 // The L column is scaled by the reciprocal of the pivot, as TMV's v /= x does
 // (include/tmv/TMV_VectorArith.h:104-106).
+#include "async.cuh"
 #include "gemm_tc.cuh"
 #include "lu.cuh"
 #include "pivots.cuh"
@@ -340,17 +341,19 @@ lu_panel_cluster_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, in
 // where the update skips them).  Rows exchanged between threads travel in the
 // same rotated order, which every thread shares.
 //
-// The cluster exchange is push-based, one hardware cluster barrier per
-// column: each CTA reduces its candidate (key, index) and stores it, with a
-// copy of the candidate row, into a receive slot of every CTA of the cluster;
-// the CTA holding row j stores a copy of it the same way.  After the barrier
-// every warp reduces the 16 candidates from its own shared memory and reads
-// the pivot row and the old row j locally, so no load crosses the cluster on
-// the critical path.  Receive slots are double-buffered by column parity: a
-// CTA writes slot parity p for column j+2 only after the barrier of column
-// j+1, which every reader of column j's slots has reached.
-// Used while a 16-CTA cluster covers the panel's rows with one row per
-// thread (m <= 16 * 512).
+// The cluster exchange has no cluster barrier: each CTA reduces its
+// candidate (key, index) and pushes it, with a copy of the candidate row,
+// into a receive slot of every CTA of the cluster with st.async stores that
+// complete transactions on the receiver's mbarrier; the CTA holding row j
+// pushes a copy of row j the same way.  A CTA waits only for the bytes of its
+// own slots (one mbarrier per column parity, re-armed each use), then every
+// warp reduces the 16 candidates from its own shared memory and reads the
+// pivot row and the old row j locally.  A CTA pushes column j+2 into slot
+// parity p only after it has received every CTA's column j+1 data, which each
+// CTA sends after it has finished reading its column j slots.  The waits are
+// bounded: on a timeout the CTA records kDevTimeout and stops, and the others
+// time out in turn.  Used while a 16-CTA cluster covers the panel's rows with
+// one row per thread (m <= 16 * 512).
 // ---------------------------------------------------------------------
 constexpr int kRegPanelThreads = 512;
 constexpr int kRegPanelWarps = kRegPanelThreads / 32;
@@ -386,11 +389,64 @@ __device__ __forceinline__ void warp_key_reduce(unsigned long long& key, int& id
     idx = (int)mi;
 }
 
+// 16-byte vectors of a row held in registers (4 floats or 2 doubles).
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+    using type = float4;
+    static constexpr int E = 4;
+    __device__ static float get(const float4& v, int e)
+    {
+        return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w;
+    }
+    __device__ static float4 make(const float* x) { return make_float4(x[0], x[1], x[2], x[3]); }
+};
+template <>
+struct Vec16<double> {
+    using type = double2;
+    static constexpr int E = 2;
+    __device__ static double get(const double2& v, int e) { return e == 0 ? v.x : v.y; }
+    __device__ static double2 make(const double* x) { return make_double2(x[0], x[1]); }
+};
+
+template <typename T, int NB>
+__device__ __forceinline__ void store_row(T* dst, const T (&x)[NB])
+{
+    using V = Vec16<T>;
+#pragma unroll
+    for (int v = 0; v < NB / V::E; ++v)
+        reinterpret_cast<typename V::type*>(dst)[v] = V::make(&x[v * V::E]);
+}
+
+template <typename T, int NB>
+__device__ __forceinline__ void load_row(T (&x)[NB], const T* src)
+{
+    using V = Vec16<T>;
+#pragma unroll
+    for (int v = 0; v < NB / V::E; ++v) {
+        const typename V::type t = reinterpret_cast<const typename V::type*>(src)[v];
+#pragma unroll
+        for (int e = 0; e < V::E; ++e) x[v * V::E + e] = V::get(t, e);
+    }
+}
+
+__device__ __forceinline__ float recip_rn(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double recip_rn(double x) { return __drcp_rn(x); }
+
+template <typename T, int NB>
+struct RegSlot {
+    uint4 meta[kClusterCtas];             // per source CTA: key (x, y), index (z)
+    T rows[kClusterCtas][NB];             // per source CTA: its candidate row
+    T diag[NB];                           // row j, from the CTA that holds it
+};
+
 template <typename T, int NB>
 __global__ void __launch_bounds__(kRegPanelThreads, 1)
 lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int nb,
                             int64_t* __restrict__ P, const unsigned char* __restrict__ modes,
-                            int rows_per_cta, int* pairs)
+                            int rows_per_cta, int* pairs, int* err, float* __restrict__ ahi,
+                            float* __restrict__ alo)
 {
     static_assert(NB % kRegBlock == 0, "whole blocks");
     static_assert(NB * sizeof(T) == 256, "a row is 16 vectors of 16 bytes");
@@ -401,13 +457,11 @@ lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k
     __shared__ int s_idx[kRegPanelWarps];
     __shared__ __align__(16) T warp_row[kRegPanelWarps][NB];  // each warp's candidate row
     __shared__ __align__(16) T diag_local[NB];                // row j of this CTA
-    // receive slots, written by every CTA of the cluster
-    __shared__ unsigned long long recv_key[2][kClusterCtas];
-    __shared__ int recv_idx[2][kClusterCtas];
-    __shared__ __align__(16) T recv_row[2][kClusterCtas][NB];
-    __shared__ __align__(16) T recv_diag[2][NB];
+    __shared__ __align__(16) RegSlot<T, NB> slot[2];          // receive slots by column parity
+    __shared__ __align__(8) uint64_t mbar[2];
     __shared__ unsigned char s_mode[kPanelMax];
     __shared__ int s_piv[kPanelMax];
+    __shared__ int s_abort;
 
     const int G = (int)cluster.num_blocks();
     const int cta = (int)cluster.block_rank();
@@ -419,12 +473,19 @@ lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k
     const bool have = tid < nr;
     const int pr = r0 + tid;  // this thread's row, counted from the panel's top
     T* Ap = A + k + k * lda;
+    const uint32_t slot_bytes = (uint32_t)(G * (16 + NB * sizeof(T)) + NB * sizeof(T));
 
+    if (tid == 0) {
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
+        s_abort = 0;
+        mbar_fence_init();
+    }
     for (int j = tid; j < nb; j += kRegPanelThreads) s_mode[j] = modes[j];
     T x[NB];
 #pragma unroll
     for (int c = 0; c < NB; ++c) x[c] = (have && c < nb) ? Ap[pr + c * lda] : T(0);
-    __syncthreads();
+    cluster.sync();  // every CTA's mbarriers are initialised before any push
 
     bool prev_uf = false;
     int rot = 0;  // x[p] holds column (p + rot) mod NB
@@ -437,6 +498,7 @@ lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k
             const int par = jj & 1;
             const bool r2 = s_mode[jj] && !prev_uf;
             const int owner_j = jj / rows_per_cta;
+            if (tid == 0) mbar_expect_tx(&mbar[par], slot_bytes);
             // 1. this warp's candidate; its row and row jj into shared memory
             unsigned long long bk = 0;
             int bi = INT_MAX;
@@ -445,45 +507,49 @@ lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k
                 bi = pr;
             }
             warp_key_reduce(bk, bi);
-            if (have && bi == pr) {
-#pragma unroll
-                for (int c = 0; c < NB; ++c) warp_row[warp][c] = x[c];
-            }
+            if (have && bi == pr) store_row<T, NB>(warp_row[warp], x);
             if (lane == 0) { s_key[warp] = bk; s_idx[warp] = bi; }
-            if (have && pr == jj) {
-#pragma unroll
-                for (int c = 0; c < NB; ++c) diag_local[c] = x[c];
-            }
+            if (have && pr == jj) store_row<T, NB>(diag_local, x);
             __syncthreads();
             // 2. push: warp 0 the CTA's candidate, warp 1 row jj (its owner only)
             if (warp == 0) {
                 bk = lane < kRegPanelWarps ? s_key[lane] : 0ull;
                 bi = lane < kRegPanelWarps ? s_idx[lane] : INT_MAX;
                 warp_key_reduce(bk, bi);
-                if (lane < G) {
-                    *cluster.map_shared_rank(&recv_key[par][cta], lane) = bk;
-                    *cluster.map_shared_rank(&recv_idx[par][cta], lane) = bi;
-                }
-                if (bi != INT_MAX) {
-                    const uint4* src = reinterpret_cast<const uint4*>(warp_row[(bi - r0) >> 5]);
-                    for (int t = lane; t < G * VEC; t += 32) {
-                        uint4* dst = reinterpret_cast<uint4*>(
-                            cluster.map_shared_rank(&recv_row[par][cta][0], t / VEC));
-                        dst[t % VEC] = src[t % VEC];
-                    }
+                const uint4* src = reinterpret_cast<const uint4*>(
+                    warp_row[bi != INT_MAX ? (bi - r0) >> 5 : 0]);
+                const uint4 meta = make_uint4((unsigned)bk, (unsigned)(bk >> 32), (unsigned)bi, 0u);
+                for (int t = lane; t < G * (VEC + 1); t += 32) {
+                    const int d = t / (VEC + 1), v = t % (VEC + 1);
+                    const uint32_t mb = cluster_addr(&mbar[par], d);
+                    if (v == VEC)
+                        st_async16(cluster_addr(&slot[par].meta[cta], d), meta, mb);
+                    else
+                        st_async16(cluster_addr(&slot[par].rows[cta][v * (16 / sizeof(T))], d), src[v], mb);
                 }
             } else if (warp == 1 && cta == owner_j) {
                 const uint4* src = reinterpret_cast<const uint4*>(diag_local);
                 for (int t = lane; t < G * VEC; t += 32) {
-                    uint4* dst = reinterpret_cast<uint4*>(
-                        cluster.map_shared_rank(&recv_diag[par][0], t / VEC));
-                    dst[t % VEC] = src[t % VEC];
+                    const int d = t / VEC, v = t % VEC;
+                    st_async16(cluster_addr(&slot[par].diag[v * (16 / sizeof(T))], d), src[v],
+                               cluster_addr(&mbar[par], d));
                 }
             }
-            cluster.sync();  // the only cluster barrier of this column
-            // 3. every warp reduces the candidates from its own shared memory
-            unsigned long long wk = lane < G ? recv_key[par][lane] : 0ull;
-            int wi = lane < G ? recv_idx[par][lane] : INT_MAX;
+            // 3. every thread waits for this CTA's slots (bounded; the data is
+            // visible to the threads that observe the phase), then reduces
+            // them locally; a timeout anywhere stops the whole CTA
+            const bool got = mbar_wait(&mbar[par], (uint32_t)((jj >> 1) & 1));
+            if (__syncthreads_or(!got)) {
+                if (tid == 0) {
+                    s_abort = 1;
+                    atomicCAS(err, (int)kDevOk, (int)kDevTimeout);
+                }
+                __syncthreads();
+                break;
+            }
+            const uint4 mt = lane < G ? slot[par].meta[lane] : make_uint4(0u, 0u, (unsigned)INT_MAX, 0u);
+            unsigned long long wk = ((unsigned long long)mt.y << 32) | mt.x;
+            int wi = (int)mt.z;
             warp_key_reduce(wk, wi);
             if (underflows<T>(pivot_key_value(wk))) {
                 if (tid == 0) s_piv[jj] = (int)(k + jj);
@@ -493,23 +559,30 @@ lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k
             }
             prev_uf = false;
             if (tid == 0) s_piv[jj] = (int)(k + wi);
-            const T* urow = recv_row[par][wi / rows_per_cta];
+            const T* urow = slot[par].rows[wi / rows_per_cta];
             // the interchange: row jj takes the pivot row, row wi the old row jj
             const T* src = nullptr;
             if (have && pr == jj) src = urow;
-            else if (have && pr == wi) src = recv_diag[par];
-            if (src) {
-#pragma unroll
-                for (int c = 0; c < NB; ++c) x[c] = src[c];
-            }
+            else if (have && pr == wi) src = slot[par].diag;
+            if (src) load_row<T, NB>(x, src);
             if (have && pr > jj) {
-                const T l = x[u] * (T(1) / urow[u]);
+                // TMV scales the column by the reciprocal of the pivot
+                using V = Vec16<T>;
+                const T l = x[u] * recip_rn(urow[u]);
                 x[u] = l;
 #pragma unroll
-                for (int c = u + 1; c < NB; ++c)
-                    if (c < lim) x[c] -= l * urow[c];
+                for (int v = 0; v < NB / V::E; ++v) {
+                    if ((v + 1) * V::E <= u + 1) continue;  // columns <= u only
+                    const typename V::type uv = reinterpret_cast<const typename V::type*>(urow)[v];
+#pragma unroll
+                    for (int e = 0; e < V::E; ++e) {
+                        const int c = v * V::E + e;
+                        if (c > u && c < lim) x[c] -= l * V::get(uv, e);
+                    }
+                }
             }
         }
+        if (s_abort) break;
         if (jb + kRegBlock < nb) {
             T t[kRegBlock];
 #pragma unroll
@@ -522,17 +595,31 @@ lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k
         }
     }
 
-    if (have) {
+    if (!s_abort) {
+        if (have) {
+            // with ahi (FP32 factorisation) the rows below the panel block are
+            // also written as the TF32 hi/lo split of L21 (row-major, nb wide)
+            // that the step's tensor-core update reads
+            const bool split = std::is_same<T, float>::value && ahi != nullptr && pr >= nb;
 #pragma unroll
-        for (int p = 0; p < NB; ++p) {
-            const int col = (p + rot) % NB;
-            if (col < nb) Ap[pr + col * lda] = x[p];
+            for (int p = 0; p < NB; ++p) {
+                const int col = (p + rot) % NB;
+                if (col < nb) {
+                    Ap[pr + col * lda] = x[p];
+                    if (split) {
+                        const float v = (float)x[p];
+                        const float h = tf32_round(v);
+                        ahi[(int64_t)(pr - nb) * nb + col] = h;
+                        alo[(int64_t)(pr - nb) * nb + col] = tf32_round(v - h);
+                    }
+                }
+            }
         }
-    }
-    __syncthreads();
-    if (cta == 0) {
-        for (int j = tid; j < nb; j += kRegPanelThreads) P[k + j] = s_piv[j];
-        if (warp == 0) panel_row_pairs(k, nb, s_piv, pairs);
+        __syncthreads();
+        if (cta == 0) {
+            for (int j = tid; j < nb; j += kRegPanelThreads) P[k + j] = s_piv[j];
+            if (warp == 0) panel_row_pairs(k, nb, s_piv, pairs);
+        }
     }
     cluster.sync();  // no CTA leaves while another may still store into it
 }
@@ -622,6 +709,97 @@ panel_u12_kernel(int nb, const T* __restrict__ L, int64_t lda, T* __restrict__ A
     for (int t = tid; t < nb * nc; t += 256) {
         const int i = t % nb, c = t / nb;
         A12[i + (c0 + c) * lda] = X[i * (kU12Cols + 1) + c];
+    }
+}
+
+// ---------------------------------------------------------------------
+// U12 = L11^-1 A12 with one column per thread held in registers.
+//
+// L11 (unit lower, nb <= NB) is staged transposed in shared memory so that the
+// multipliers of column j are read as 16-byte broadcast vectors; a CTA's
+// columns of A12 are staged through shared memory so that global reads and
+// writes stay coalesced.  Each column's substitution runs in the same order
+// as the scalar kernel (j ascending), so results are bitwise the same.  With
+// SPLIT the kernel also writes the TF32 hi/lo split of U12 (column-major,
+// leading dimension nb) for the tensor-core trailing update.
+// ---------------------------------------------------------------------
+constexpr int kU12RegThreads = 64;   // columns per CTA, one per computing thread
+constexpr int kU12RegBlock = 256;    // threads per CTA: all of them stage, 64 compute
+
+template <typename T, int NB, bool SPLIT>
+__global__ void __launch_bounds__(kU12RegBlock)
+u12_reg_kernel(int nb, const T* __restrict__ L, int64_t lda, T* __restrict__ A12, int64_t ncols,
+               float* __restrict__ Bhi, float* __restrict__ Blo)
+{
+    using V = Vec16<T>;
+    constexpr int XP = NB + V::E;  // padded staging row: conflict-free vector access
+    __shared__ __align__(16) T LsT[NB][NB];  // LsT[j][i] = L(i, j) for i > j, else 0
+    __shared__ __align__(16) T Xs[kU12RegThreads][XP];
+    const int tid = threadIdx.x;
+    const int64_t c0 = (int64_t)blockIdx.x * kU12RegThreads;
+
+    // stage L11 and this CTA's columns, eight independent loads in flight
+    constexpr int LU = 8;
+    for (int t0 = tid; t0 < NB * NB; t0 += kU12RegBlock * LU) {
+        T v[LU];
+#pragma unroll
+        for (int q = 0; q < LU; ++q) {
+            const int t = t0 + q * kU12RegBlock;
+            const int i = t % NB, j = t / NB;
+            v[q] = (t < NB * NB && i < nb && j < nb && i > j) ? L[i + (int64_t)j * lda] : T(0);
+        }
+#pragma unroll
+        for (int q = 0; q < LU; ++q) {
+            const int t = t0 + q * kU12RegBlock;
+            if (t < NB * NB) LsT[t / NB][t % NB] = v[q];
+        }
+    }
+    for (int t0 = tid; t0 < kU12RegThreads * NB; t0 += kU12RegBlock * LU) {
+        T v[LU];
+#pragma unroll
+        for (int q = 0; q < LU; ++q) {
+            const int t = t0 + q * kU12RegBlock;
+            const int i = t % NB, c = t / NB;
+            v[q] = (t < kU12RegThreads * NB && i < nb && c0 + c < ncols) ? A12[i + (c0 + c) * lda] : T(0);
+        }
+#pragma unroll
+        for (int q = 0; q < LU; ++q) {
+            const int t = t0 + q * kU12RegBlock;
+            if (t < kU12RegThreads * NB) Xs[t / NB][t % NB] = v[q];
+        }
+    }
+    __syncthreads();
+
+    if (tid < kU12RegThreads) {
+    T x[NB];
+    load_row<T, NB>(x, Xs[tid]);
+#pragma unroll
+    for (int j = 0; j < NB - 1; ++j) {
+#pragma unroll
+        for (int v = (j + 1) / V::E; v < NB / V::E; ++v) {
+            const typename V::type lv = reinterpret_cast<const typename V::type*>(LsT[j])[v];
+#pragma unroll
+            for (int e = 0; e < V::E; ++e) {
+                const int i = v * V::E + e;
+                if (i > j) x[i] -= V::get(lv, e) * x[j];
+            }
+        }
+    }
+    store_row<T, NB>(Xs[tid], x);
+    }
+    __syncthreads();
+
+    for (int t0 = tid; t0 < kU12RegThreads * NB; t0 += kU12RegBlock) {
+        const int i = t0 % NB, c = t0 / NB;
+        if (i < nb && c0 + c < ncols) {
+            const T val = Xs[c][i];
+            A12[i + (c0 + c) * lda] = val;
+            if constexpr (SPLIT) {
+                const float h = tf32_round((float)val);
+                Bhi[(c0 + c) * nb + i] = h;
+                Blo[(c0 + c) * nb + i] = tf32_round((float)val - h);
+            }
+        }
     }
 }
 
@@ -860,46 +1038,118 @@ static double panel_flops(int64_t m, int nb)
 // cores in the FP32 factorisation; smaller ones stay on the SIMT kernel.
 constexpr int64_t kTcMinRest = 256;
 
+// The panel's interchanges on every other column of A (stream order: after
+// the panel, before any update that reads those rows).
+template <typename T>
+static tmvg_status laswp_step(Context* c, int64_t n, T* A, int64_t lda, int64_t k, int nb, const int* pairs)
+{
+    if (n <= nb) return TMVG_OK;
+    const int cols_per_cta = 8;  // one warp per column
+    laswp_pairs_kernel<T><<<(unsigned)ceil_div(n, cols_per_cta), 32 * cols_per_cta, 0, c->stream>>>(
+        A, lda, n, k, k + nb, pairs);
+    ++c->launches;
+    return check_cuda(c, cudaGetLastError(), "lu: laswp launch");
+}
+
+// The panel's interchanges on columns [c0, c1) except [skip0, skip1).
+template <typename T>
+static tmvg_status laswp_cols(Context* c, T* A, int64_t lda, int64_t c0, int64_t c1, int64_t skip0,
+                              int64_t skip1, const int* pairs)
+{
+    if (c1 <= c0) return TMVG_OK;
+    const int cols_per_cta = 8;  // one warp per column
+    laswp_pairs_kernel<T><<<(unsigned)ceil_div(c1 - c0, cols_per_cta), 32 * cols_per_cta, 0, c->stream>>>(
+        A + c0 * lda, lda, c1 - c0, skip0 - c0, skip1 - c0, pairs);
+    ++c->launches;
+    return check_cuda(c, cudaGetLastError(), "lu: laswp launch");
+}
+
+// Whether the FP32 trailing updates of step (k, nb) run on the tensor cores;
+// if so, the step's split copies are set up and L21 is split into them.
+template <typename T>
+static tmvg_status tc_step_setup(Context* c, int64_t n, T* A, int64_t lda, int64_t k, int nb, bool* tc,
+                                 Tf32x3Buffers* b)
+{
+    *tc = false;
+    if constexpr (std::is_same<T, float>::value) {
+        const int64_t rest = n - k - nb;
+        if (rest >= kTcMinRest && tf32x3_supported(nb)) {
+            tmvg_status st = tf32x3_buffers(c, rest, rest, nb, b);
+            if (st) return st;
+            st = tf32x3_split_a(c, rest, nb, A + (k + nb) + k * lda, lda, *b);
+            if (st) return st;
+            *tc = true;
+        }
+    }
+    return TMVG_OK;
+}
+
+// For the columns [c0, c0 + nc) right of panel (k, nb): U12 = L11^-1 A12, then
+// A22 -= L21 U12 on those columns (tensor cores when tc, with U12's split
+// copy written by the U12 kernel at its offset in b).
+template <typename T>
+static tmvg_status update_columns(Context* c, int64_t n, T* A, int64_t lda, int64_t k, int nb, int64_t c0,
+                                  int64_t nc, bool tc, const Tf32x3Buffers& b)
+{
+    if (nc <= 0) return TMVG_OK;
+    const int64_t rest = n - k - nb;  // rows below the panel
+    const T* L11 = A + k + k * lda;
+    T* A12 = A + k + c0 * lda;
+    const double fr = (double)rest, fc = (double)nc;
+    ScopedTimer timer(c, kClsTrailingUpdate, sizeof(T) * (2.0 * fr * fc + fr * nb + nb * fc), 2.0 * fr * fc * nb);
+    Tf32x3Buffers bc = b;  // B copies of these columns
+    if (tc) {
+        bc.Bhi = b.Bhi + (c0 - k - nb) * nb;
+        bc.Blo = b.Blo + (c0 - k - nb) * nb;
+    }
+    tmvg_status st;
+    if (nb <= RegPanel<T>::NB) {
+        constexpr int NB = RegPanel<T>::NB;
+        const unsigned grid = (unsigned)ceil_div(nc, kU12RegThreads);
+        if (tc)
+            u12_reg_kernel<T, NB, true><<<grid, kU12RegBlock, 0, c->stream>>>(nb, L11, lda, A12, nc,
+                                                                             bc.Bhi, bc.Blo);
+        else
+            u12_reg_kernel<T, NB, false><<<grid, kU12RegBlock, 0, c->stream>>>(nb, L11, lda, A12, nc,
+                                                                              nullptr, nullptr);
+        ++c->launches;
+        st = check_cuda(c, cudaGetLastError(), "lu: u12 launch");
+        if (st) return st;
+    } else {
+        const size_t smem = sizeof(T) * ((size_t)nb * (nb + 1) + (size_t)nb * (kU12Cols + 1));
+        if (smem > 48 * 1024)
+            cudaFuncSetAttribute(panel_u12_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        panel_u12_kernel<T><<<(unsigned)ceil_div(nc, kU12Cols), 256, smem, c->stream>>>(nb, L11, lda, A12, nc);
+        ++c->launches;
+        st = check_cuda(c, cudaGetLastError(), "lu: u12 launch");
+        if (st) return st;
+        if constexpr (std::is_same<T, float>::value) {
+            if (tc) {
+                st = tf32x3_split_b(c, nc, nb, A12, lda, bc);
+                if (st) return st;
+            }
+        }
+    }
+    if constexpr (std::is_same<T, float>::value) {
+        // FP32 factor: 3xTF32 on the tensor cores keeps FP32 accuracy
+        if (tc) return tf32x3_apply(c, rest, nc, nb, bc, A + (k + nb) + c0 * lda, lda);
+    }
+    return gemm<T>(c, rest, nc, nb, T(-1), Mat<const T>{A + (k + nb) + k * lda, 1, lda},
+                   Mat<const T>{A12, 1, lda}, T(1), Mat<T>{A + (k + nb) + c0 * lda, 1, lda});
+}
+
+// Everything of step (k, nb) after its panel: interchanges, U12, update.
 template <typename T>
 static tmvg_status panel_update(Context* c, int64_t n, T* A, int64_t lda, int64_t k, int nb,
                                 const int* pairs)
 {
-    tmvg_status st;
-    if (n > nb) {
-        const int cols_per_cta = 8;  // one warp per column
-        laswp_pairs_kernel<T><<<(unsigned)ceil_div(n, cols_per_cta), 32 * cols_per_cta, 0, c->stream>>>(
-            A, lda, n, k, k + nb, pairs);
-        ++c->launches;
-        st = check_cuda(c, cudaGetLastError(), "lu: laswp launch");
-        if (st) return st;
-    }
-    if (k + nb < n) {
-        const int64_t rest = n - k - nb;
-        const size_t smem = sizeof(T) * ((size_t)nb * (nb + 1) + (size_t)nb * (kU12Cols + 1));
-        if (smem > 48 * 1024)
-            cudaFuncSetAttribute(panel_u12_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem);
-        panel_u12_kernel<T><<<(unsigned)ceil_div(rest, kU12Cols), 256, smem, c->stream>>>(
-            nb, A + k + k * lda, lda, A + k + (k + nb) * lda, rest);
-        ++c->launches;
-        st = check_cuda(c, cudaGetLastError(), "lu: u12 launch");
-        if (st) return st;
-        const double fr = (double)rest;
-        ScopedTimer timer(c, kClsTrailingUpdate, sizeof(T) * (2.0 * fr * fr + 2.0 * fr * nb),
-                          2.0 * fr * fr * nb);
-        if constexpr (std::is_same<T, float>::value) {
-            // FP32 factor: 3xTF32 on the tensor cores keeps FP32 accuracy
-            if (rest >= kTcMinRest && tf32x3_supported(nb))
-                return gemm_f32_tf32x3_update(c, rest, rest, nb, A + (k + nb) + k * lda, lda,
-                                              A + k + (k + nb) * lda, lda,
-                                              A + (k + nb) + (k + nb) * lda, lda);
-        }
-        st = gemm<T>(c, rest, rest, nb, T(-1), Mat<const T>{A + (k + nb) + k * lda, 1, lda},
-                     Mat<const T>{A + k + (k + nb) * lda, 1, lda}, T(1),
-                     Mat<T>{A + (k + nb) + (k + nb) * lda, 1, lda});
-        if (st) return st;
-    }
-    return TMVG_OK;
+    tmvg_status st = laswp_step<T>(c, n, A, lda, k, nb, pairs);
+    if (st || k + nb >= n) return st;
+    bool tc;
+    Tf32x3Buffers b{};
+    st = tc_step_setup<T>(c, n, A, lda, k, nb, &tc, &b);
+    if (st) return st;
+    return update_columns<T>(c, n, A, lda, k, nb, k + nb, n - k - nb, tc, b);
 }
 
 constexpr size_t kClusterSmemMax = 200 * 1024;
@@ -953,8 +1203,8 @@ static int cluster_panel_width(int64_t n)
 }
 
 template <typename T>
-static tmvg_status launch_panel_cluster(Context* c, T* A, int64_t lda, int64_t n, int64_t k, int nb,
-                                        int64_t* P, const unsigned char* modes, int* pairs)
+static tmvg_status launch_panel_cluster(Context* c, cudaStream_t s, T* A, int64_t lda, int64_t n, int64_t k,
+                                        int nb, int64_t* P, const unsigned char* modes, int* pairs)
 {
     const int64_t m = n - k;
     const int rpc = (int)ceil_div(m, kClusterCtas);
@@ -967,7 +1217,7 @@ static tmvg_status launch_panel_cluster(Context* c, T* A, int64_t lda, int64_t n
     cfg.gridDim = dim3(kClusterCtas);
     cfg.blockDim = dim3(kPanelThreads);
     cfg.dynamicSmemBytes = (size_t)rpc * (nb + 1) * sizeof(T);
-    cfg.stream = c->stream;
+    cfg.stream = s;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     ++c->launches;
@@ -1010,8 +1260,9 @@ static bool reg_panel_ok(Context* c)
 }
 
 template <typename T>
-static tmvg_status launch_panel_cluster_reg(Context* c, T* A, int64_t lda, int64_t n, int64_t k,
-                                            int nb, int64_t* P, const unsigned char* modes, int* pairs)
+static tmvg_status launch_panel_cluster_reg(Context* c, cudaStream_t s, T* A, int64_t lda, int64_t n,
+                                            int64_t k, int nb, int64_t* P, const unsigned char* modes,
+                                            int* pairs, float* ahi, float* alo)
 {
     const int64_t m = n - k;
     const int rpc = (int)ceil_div(m, kClusterCtas);
@@ -1024,13 +1275,13 @@ static tmvg_status launch_panel_cluster_reg(Context* c, T* A, int64_t lda, int64
     cfg.gridDim = dim3(kClusterCtas);
     cfg.blockDim = dim3(kRegPanelThreads);
     cfg.dynamicSmemBytes = 0;
-    cfg.stream = c->stream;
+    cfg.stream = s;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     ++c->launches;
     return check_cuda(c,
                       cudaLaunchKernelEx(&cfg, lu_panel_cluster_reg_kernel<T, RegPanel<T>::NB>, A,
-                                         lda, n, k, nb, P, modes, rpc, pairs),
+                                         lda, n, k, nb, P, modes, rpc, pairs, c->dflags, ahi, alo),
                       "lu: register panel launch");
 }
 
@@ -1058,7 +1309,10 @@ tmvg_status lu_factor(Context* c, int64_t n, T* A, int64_t lda, int64_t* P)
     const size_t off_diag = off_rows + sizeof(T) * 2 * G_full * kPanelMax;
     const size_t off_modes = (off_diag + sizeof(T) * 2 * kPanelMax + 255) & ~size_t(255);
     const size_t off_pairs = (off_modes + (size_t)n + 255) & ~size_t(255);
-    const size_t bytes = off_pairs + sizeof(int) * (1 + 2 * kMaxPairs);
+    // two pair lists: with look-ahead, step s+1's panel writes its list while
+    // step s's interchanges still read theirs
+    const size_t pairs_len = 1 + 2 * (size_t)kMaxPairs;
+    const size_t bytes = off_pairs + sizeof(int) * 2 * pairs_len;
     unsigned char* ws = (unsigned char*)workspace(c, bytes);
     if (!ws) return TMVG_OOM;
     double* cand_key = (double*)(ws + off_key);
@@ -1087,21 +1341,93 @@ tmvg_status lu_factor(Context* c, int64_t n, T* A, int64_t lda, int64_t* P)
         attr_set[ai] = true;
     }
 
+    if (cl_nb > 0) {
+        // Look-ahead: panel k+1 runs on the high-priority side stream as soon
+        // as its own columns are updated, while the rest of step k's update
+        // runs on the main stream.
+        tmvg_status st = ensure_side_stream(c);
+        if (st) return st;
+        cudaStream_t side = c->side;
+        // FP32: split copies for the tensor-core updates, U12 (B) once and
+        // L21 (A) double-buffered by step parity, since the panel kernel of
+        // step s+1 writes its L21 split while step s's update still reads.
+        bool tc_any = false;
+        Tf32x3Buffers arena[2] = {};
+        if constexpr (std::is_same<T, float>::value) {
+            if (n - nbmax >= kTcMinRest && tf32x3_supported(nbmax)) {
+                const size_t part = ((size_t)n * nbmax * sizeof(float) + 255) & ~size_t(255);
+                unsigned char* w3 = (unsigned char*)workspace3(c, 6 * part);
+                if (!w3) return TMVG_OOM;
+                for (int q = 0; q < 2; ++q) {
+                    arena[q].Bhi = (float*)w3;
+                    arena[q].Blo = (float*)(w3 + part);
+                    arena[q].Ahi = (float*)(w3 + (2 + 2 * q) * part);
+                    arena[q].Alo = (float*)(w3 + (3 + 2 * q) * part);
+                }
+                tc_any = true;
+            }
+        }
+        auto tc_for = [&](int64_t kk, int w) {
+            return tc_any && n - kk - w >= kTcMinRest && tf32x3_supported(w);
+        };
+        auto pairs_of = [&](int64_t step) { return pairs + (step & 1) * pairs_len; };
+        auto panel = [&](int64_t kk, int w, int64_t step) -> tmvg_status {
+            ScopedTimer timer(c, kClsPanel, 2.0 * sizeof(T) * (n - kk) * w, panel_flops(n - kk, w), side);
+            float* ahi = nullptr;
+            float* alo = nullptr;
+            if (reg && tc_for(kk, w)) {
+                ahi = arena[step & 1].Ahi;
+                alo = arena[step & 1].Alo;
+            }
+            int* pp = pairs_of(step);
+            tmvg_status s2 = reg ? launch_panel_cluster_reg<T>(c, side, A, lda, n, kk, w, P, modes + kk, pp, ahi, alo)
+                                 : launch_panel_cluster<T>(c, side, A, lda, n, kk, w, P, modes + kk, pp);
+            if (!s2 && c->serialize_lookahead) s2 = check_cuda(c, cudaStreamSynchronize(side), "lu: serialize");
+            return s2;
+        };
+        st = check_cuda(c, cudaEventRecord(c->ev_fork, c->stream), "lu: fork");
+        if (!st) st = check_cuda(c, cudaStreamWaitEvent(side, c->ev_fork, 0), "lu: fork");
+        if (!st) st = panel(0, (int)std::min<int64_t>(nbmax, n), 0);
+        if (!st) st = check_cuda(c, cudaEventRecord(c->ev_panel, side), "lu: panel event");
+        for (int64_t k = 0, step = 0; k < n && !st; k += nbmax, ++step) {
+            const int nb = (int)std::min<int64_t>(nbmax, n - k);
+            st = check_cuda(c, cudaStreamWaitEvent(c->stream, c->ev_panel, 0), "lu: join");
+            if (st) break;
+            const int* pk = pairs_of(step);
+            if (k + nb >= n) {
+                st = laswp_step<T>(c, n, A, lda, k, nb, pk);
+                break;
+            }
+            const int64_t rest = n - k - nb;
+            const int nb2 = (int)std::min<int64_t>(nbmax, rest);
+            // the next panel's columns first: interchanges, U12, update
+            st = laswp_cols<T>(c, A, lda, k + nb, k + nb + nb2, 0, 0, pk);
+            const bool tc = tc_for(k, nb);
+            const Tf32x3Buffers& b = arena[step & 1];
+            if constexpr (std::is_same<T, float>::value) {
+                // the register panel kernel writes the L21 split itself
+                if (!st && tc && !reg) st = tf32x3_split_a(c, rest, nb, A + (k + nb) + k * lda, lda, b);
+            }
+            if (!st) st = update_columns<T>(c, n, A, lda, k, nb, k + nb, nb2, tc, b);
+            if (!st) st = check_cuda(c, cudaEventRecord(c->ev_narrow, c->stream), "lu: narrow event");
+            if (!st) st = check_cuda(c, cudaStreamWaitEvent(side, c->ev_narrow, 0), "lu: narrow wait");
+            if (!st) st = panel(k + nb, nb2, step + 1);
+            if (!st) st = check_cuda(c, cudaEventRecord(c->ev_panel, side), "lu: panel event");
+            // then everything else of this step, overlapping the next panel
+            if (!st) st = laswp_cols<T>(c, A, lda, 0, n, k, k + nb + nb2, pk);
+            if (!st) st = update_columns<T>(c, n, A, lda, k, nb, k + nb + nb2, rest - nb2, tc, b);
+        }
+        if (st) {
+            // leave no side work unordered after an error
+            cudaStreamSynchronize(side);
+            return st;
+        }
+        return collect_device_error(c, "lu_factor");
+    }
+
     for (int64_t k = 0; k < n; k += nbmax) {
         const int nb = (int)std::min<int64_t>(nbmax, n - k);
         const int64_t m = n - k;
-        if (cl_nb > 0) {
-            tmvg_status st;
-            {
-                ScopedTimer timer(c, kClsPanel, 2.0 * sizeof(T) * m * nb, panel_flops(m, nb));
-                st = reg ? launch_panel_cluster_reg<T>(c, A, lda, n, k, nb, P, modes + k, pairs)
-                         : launch_panel_cluster<T>(c, A, lda, n, k, nb, P, modes + k, pairs);
-            }
-            if (st) return st;
-            st = panel_update<T>(c, n, A, lda, k, nb, pairs);
-            if (st) return st;
-            continue;
-        }
         const int G = (int)std::min<int64_t>(c->num_sms, ceil_div(m, kPanelThreads));
         const int rows_per_cta = (int)ceil_div(m, G);
         const size_t smem = (size_t)rows_per_cta * (nb + 1) * sizeof(T);
