@@ -155,6 +155,20 @@ def run_gpu(args) -> dict:
 
         dist.init_process_group("nccl", device_id=dev)
 
+    if args.path == "batched":
+        b = batched_bench(dev, args, with_cpu=(rank == 0 and not args.no_cpu_baseline))
+        out = {"metric": "batched uneven FP64 LU solves/s", "value": b["value"], "unit": "solves/s",
+               "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+               "ms_per_step": b["ms_per_batch"], "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+               "config": {"workload": b["config"], "systems": b["systems"]},
+               "roofline": b["roofline"], "gpu_launches": 1}
+        if "cpu_baseline" in b:
+            out["cpu_baseline"] = b["cpu_baseline"]
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return out if rank == 0 else None
+
     n, nrhs, cond = args.n, 1, args.cond
     cache = Path(args.matrix_cache) if args.matrix_cache else None
     if cache is not None and cache.exists():
@@ -514,7 +528,9 @@ def main():
     ap.add_argument("--n", type=int, default=8192)
     ap.add_argument("--cond", type=float, default=1e6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--path", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--path", default="mixed", choices=["mixed", "fp64", "batched"],
+                    help="mixed: the headline solve; fp64: the FP64 LU solve alone; batched: "
+                         "only the batched uneven solver (for profiling it)")
     ap.add_argument("--matrix-cache", default=None,
                     help="load the workload matrix from this file if present, else save it "
                          "there (lets a profiler run skip the QR-based generation)")

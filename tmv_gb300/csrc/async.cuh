@@ -67,4 +67,48 @@ __device__ __forceinline__ void st_async16(uint32_t dst, const uint4& v, uint32_
         : "memory");
 }
 
+// Wait with cluster-scope acquire (pairs with release arrivals from other
+// CTAs of the cluster); false on timeout.
+__device__ __forceinline__ bool mbar_wait_cluster(uint64_t* bar, uint32_t parity)
+{
+    for (unsigned spins = 0; spins < kTryWaitLimit; ++spins) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// Arrival on an mbarrier of another CTA (address from cluster_addr) with
+// cluster-scope release: this thread's earlier writes, and those it has
+// observed, are visible to a thread that acquires the completed phase.
+__device__ __forceinline__ void mbar_arrive_remote_release(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// 16-byte store into / load from another CTA's shared memory.
+__device__ __forceinline__ void st_cluster16(uint32_t dst, const uint4& v)
+{
+    asm volatile("st.shared::cluster.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(dst), "r"(v.x), "r"(v.y),
+                 "r"(v.z), "r"(v.w)
+                 : "memory");
+}
+
+__device__ __forceinline__ uint4 ld_cluster16(uint32_t src)
+{
+    uint4 v;
+    asm volatile("ld.shared::cluster.v4.u32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "r"(src)
+                 : "memory");
+    return v;
+}
+
 }  // namespace tmvg

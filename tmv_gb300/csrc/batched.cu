@@ -9,14 +9,15 @@
 // src/TMV_LUDiv.cpp:186).  status[s] = 1 when a zero U(j,j) met a nonzero
 // (TMV's SingularUpperTriMatrix), else 0.
 //
-// Kernel: grid = SMs x resident CTAs; each CTA repeatedly takes the next
+// Kernel: grid = SMs x resident CTAs (128 threads, four per SM, so that one
+// CTA's barrier-bound phases overlap another's FMA work); each CTA repeatedly takes the next
 // system from an atomic queue over `order` (largest n first, so the tail of
 // the launch holds the small systems) and runs, for n <= 256:
 //   for each panel of PW columns:
 //     factor the panel in shared memory with TMV's pivot rule (pivot_key),
 //     apply its interchanges to the other columns of A_s and to B_s,
-//     U12 = L11^-1 A12 (one column per thread),
-//     A22 -= L21 U12 (4x4 register tiles, FP64 FMA),
+//     U12 = L11^-1 A12 (one column per thread, in registers),
+//     A22 -= L21 U12 (4x4 register tiles, FP64 FMA, U12 read back from A),
 //   then forward/back substitution of B_s staged in shared memory.
 // FP64 FMA throughput (about 2 per SM per clock on GB300) bounds the kernel.
 // PW (8 or 16) is chosen per size class by the plan's tuner.
@@ -33,20 +34,21 @@
 
 namespace tmvg {
 
-constexpr int kBatchThreads = 256;
+constexpr int kBatchThreads = 128;
 constexpr int kBatchMaxN = 256;
 constexpr int kBatchMaxRhs = 16;
 constexpr int kNumClasses = 4;  // n <= 32, <= 64, <= 128, <= 256
+constexpr int kSolveBlock = 32;  // columns per block of the substitutions
 
 __host__ __device__ inline int size_class(int64_t n)
 {
     return n <= 32 ? 0 : n <= 64 ? 1 : n <= 128 ? 2 : 3;
 }
 
-// Shared-memory doubles a panel width needs: panel [256][PW+1] + U12 [PW][256].
+// Shared-memory doubles a panel width needs: the panel [256][PW+1].
 __host__ __device__ constexpr int batch_smem_doubles(int pw)
 {
-    return kBatchMaxN * (pw + 1) + pw * kBatchMaxN;
+    return kBatchMaxN * (pw + 1);
 }
 
 // Is column c of an n-column LU the second column of one of TMV's two-column
@@ -83,8 +85,7 @@ __device__ void factor_solve_one(int64_t n, int64_t r, double* __restrict__ A, d
                                  int64_t* __restrict__ P, int* __restrict__ status, double* smem)
 {
     constexpr int LDP = PW + 1;
-    double* pan = smem;                     // [256][LDP]
-    double* u12 = smem + kBatchMaxN * LDP;  // [PW][256]
+    double* pan = smem;  // [256][LDP]
     __shared__ double s_key[kBatchThreads / 32];
     __shared__ long long s_idx[kBatchThreads / 32];
     __shared__ double w_key;
@@ -173,36 +174,45 @@ __device__ void factor_solve_one(int64_t n, int64_t r, double* __restrict__ A, d
         __syncthreads();
         const int ncol = (int)(n - k0 - w);
         if (ncol > 0) {
-            // U12 = L11^-1 A12, one column per thread, substituted in shared memory
+            // U12 = L11^-1 A12, one column per thread in registers, written
+            // back in place (the update below reads it from A12)
             for (int c = tid; c < ncol; c += kBatchThreads) {
                 double* colp = A + k0 + (k0 + w + c) * n;
-                for (int kk = 0; kk < w; ++kk) {
-                    double x = colp[kk];
-                    for (int jj = 0; jj < kk; ++jj)
-                        x -= pan[kk * LDP + jj] * u12[jj * kBatchMaxN + c];
-                    u12[kk * kBatchMaxN + c] = x;
-                    colp[kk] = x;
+                double x[PW];
+#pragma unroll
+                for (int kk = 0; kk < PW; ++kk) x[kk] = kk < w ? colp[kk] : 0.0;
+#pragma unroll
+                for (int kk = 1; kk < PW; ++kk) {
+#pragma unroll
+                    for (int jj = 0; jj < kk; ++jj) x[kk] -= pan[kk * LDP + jj] * x[jj];
+                    asm volatile("" ::: "memory");  // keeps the loads of later rows from being hoisted
                 }
+#pragma unroll
+                for (int kk = 0; kk < PW; ++kk)
+                    if (kk < w) colp[kk] = x[kk];
             }
             __syncthreads();
-            // A22 -= L21 U12
+            // A22 -= L21 U12: 4x4 tiles, a tile's rows strided by ti so that
+            // consecutive threads read consecutive panel rows
             const int m2 = m - w;
             const int ti = (m2 + 3) / 4, tj = (ncol + 3) / 4;
             for (int t = tid; t < ti * tj; t += kBatchThreads) {
-                const int i0 = (t % ti) * 4, j0 = (t / ti) * 4;
+                const int iq = t % ti, j0 = (t / ti) * 4;
                 double acc[4][4];
 #pragma unroll
                 for (int a = 0; a < 4; ++a)
 #pragma unroll
                     for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+                const double* u = A + k0 + (k0 + w + j0) * n;
                 for (int kk = 0; kk < w; ++kk) {
                     double av[4], bv[4];
 #pragma unroll
-                    for (int a = 0; a < 4; ++a)
-                        av[a] = (i0 + a < m2) ? pan[(w + i0 + a) * LDP + kk] : 0.0;
+                    for (int a = 0; a < 4; ++a) {
+                        const int ra = iq + a * ti;
+                        av[a] = ra < m2 ? pan[(w + ra) * LDP + kk] : 0.0;
+                    }
 #pragma unroll
-                    for (int b = 0; b < 4; ++b)
-                        bv[b] = (j0 + b < ncol) ? u12[kk * kBatchMaxN + j0 + b] : 0.0;
+                    for (int b = 0; b < 4; ++b) bv[b] = (j0 + b < ncol) ? u[kk + b * n] : 0.0;
 #pragma unroll
                     for (int a = 0; a < 4; ++a)
 #pragma unroll
@@ -211,62 +221,112 @@ __device__ void factor_solve_one(int64_t n, int64_t r, double* __restrict__ A, d
 #pragma unroll
                 for (int b = 0; b < 4; ++b) {
                     if (j0 + b >= ncol) continue;
-                    double* cp = A + (k0 + w + i0) + (k0 + w + j0 + b) * n;
+                    double* cp = A + (k0 + w) + (k0 + w + j0 + b) * n;
 #pragma unroll
-                    for (int a = 0; a < 4; ++a)
-                        if (i0 + a < m2) cp[a] -= acc[a][b];
+                    for (int a = 0; a < 4; ++a) {
+                        const int ra = iq + a * ti;
+                        if (ra < m2) cp[ra] -= acc[a][b];
+                    }
                 }
             }
         }
         __syncthreads();
     }
 
-    // Solve: B holds P B; L (unit) then U, column-oriented as TMV's vector
-    // solve (src/TMV_TriDiv_V.cpp:148-236, 322-398) with its zero skipping.
+    // Solve: B holds P B; L (unit) then U, with the arithmetic and zero
+    // skipping of TMV's column-oriented vector solve (src/TMV_TriDiv_V.cpp:
+    // 148-236, 322-398), blocked by kSolveBlock columns: one warp solves the
+    // diagonal block (staged in shared memory, a lane per right-hand side),
+    // then every thread updates its (row, rhs) entries below (or above) the
+    // block over the block's columns in TMV's order, streaming the factor
+    // from global memory.  Each entry receives the same subtractions in the
+    // same order as the column-by-column loop.
     if (r > 0) {
-        double* bs = smem;  // [256][kBatchMaxRhs]
+        constexpr int XS = kBatchMaxN + 1;                  // padded rhs stride
+        double* xs = smem;                                   // [kBatchMaxRhs][XS]
+        double* dg = smem + kBatchMaxRhs * XS;               // [kSolveBlock][kSolveBlock + 1]
+        constexpr int DS = kSolveBlock + 1;
         for (int t = tid; t < n * r; t += kBatchThreads) {
             const int i = t % n, q = t / n;
-            bs[i * kBatchMaxRhs + q] = B[i + q * n];
+            xs[q * XS + i] = B[i + q * n];
         }
         __syncthreads();
-        for (int64_t j = 0; j < n - 1; ++j) {
-            const int len = (int)(n - 1 - j);
-            for (int t = tid; t < len * r; t += kBatchThreads) {
-                const int i = (int)(j + 1) + t % len, q = t / len;
-                const double xj = bs[j * kBatchMaxRhs + q];
-                if (xj != 0.0) bs[i * kBatchMaxRhs + q] -= A[i + j * n] * xj;
+        // forward: unit lower L
+        for (int j0 = 0; j0 < n; j0 += kSolveBlock) {
+            const int jb = (int)min((int64_t)kSolveBlock, n - j0);
+            for (int t = tid; t < jb * jb; t += kBatchThreads) {
+                const int i = t % jb, k = t / jb;
+                dg[i * DS + k] = A[(j0 + i) + (int64_t)(j0 + k) * n];
             }
             __syncthreads();
-        }
-        for (int64_t j = n - 1; j >= 0; --j) {
-            if (tid < r) {
-                double v = bs[j * kBatchMaxRhs + tid];
-                if (v != 0.0) {
-                    const double d = A[j + j * n];
-                    if (d == 0.0) s_sing = 1;
-                    else bs[j * kBatchMaxRhs + tid] = v / d;
+            if (warp == 0 && lane < r) {
+                double* xq = xs + lane * XS + j0;
+                for (int k = 0; k < jb; ++k) {
+                    const double xk = xq[k];
+                    if (xk != 0.0)
+                        for (int i = k + 1; i < jb; ++i) xq[i] -= dg[i * DS + k] * xk;
                 }
             }
             __syncthreads();
-            const int len = (int)j;
-            for (int t = tid; t < len * r; t += kBatchThreads) {
-                const int i = t % len, q = t / len;
-                const double xj = bs[j * kBatchMaxRhs + q];
-                if (xj != 0.0) bs[i * kBatchMaxRhs + q] -= A[i + j * n] * xj;
+            const int below = (int)(n - j0 - jb);
+            for (int t = tid; t < below * r; t += kBatchThreads) {
+                const int i = j0 + jb + t % below, q = t / below;
+                const double* xq = xs + q * XS + j0;
+                const double* lc = A + i + (int64_t)j0 * n;
+                double v = xs[q * XS + i];
+                for (int k = 0; k < jb; ++k) {
+                    const double xk = xq[k];
+                    if (xk != 0.0) v -= lc[(int64_t)k * n] * xk;
+                }
+                xs[q * XS + i] = v;
+            }
+            __syncthreads();
+        }
+        // backward: upper U, columns from the last
+        for (int j1 = (int)n; j1 > 0; j1 -= kSolveBlock) {
+            const int j0 = max(0, j1 - kSolveBlock), jb = j1 - j0;
+            for (int t = tid; t < jb * jb; t += kBatchThreads) {
+                const int i = t % jb, k = t / jb;
+                dg[i * DS + k] = A[(j0 + i) + (int64_t)(j0 + k) * n];
+            }
+            __syncthreads();
+            if (warp == 0 && lane < r) {
+                double* xq = xs + lane * XS + j0;
+                for (int k = jb - 1; k >= 0; --k) {
+                    double v = xq[k];
+                    if (v != 0.0) {
+                        const double d = dg[k * DS + k];
+                        if (d == 0.0) s_sing = 1;
+                        else xq[k] = v = v / d;
+                    }
+                    if (v != 0.0)
+                        for (int i = 0; i < k; ++i) xq[i] -= dg[i * DS + k] * v;
+                }
+            }
+            __syncthreads();
+            for (int t = tid; t < j0 * r; t += kBatchThreads) {
+                const int i = t % j0, q = t / j0;
+                const double* xq = xs + q * XS + j0;
+                const double* uc = A + i + (int64_t)j0 * n;
+                double v = xs[q * XS + i];
+                for (int k = jb - 1; k >= 0; --k) {
+                    const double xk = xq[k];
+                    if (xk != 0.0) v -= uc[(int64_t)k * n] * xk;
+                }
+                xs[q * XS + i] = v;
             }
             __syncthreads();
         }
         for (int t = tid; t < n * r; t += kBatchThreads) {
             const int i = t % n, q = t / n;
-            B[i + q * n] = bs[i * kBatchMaxRhs + q];
+            B[i + q * n] = xs[q * XS + i];
         }
     }
     __syncthreads();
     if (tid == 0) *status = s_sing;
 }
 
-__global__ void __launch_bounds__(kBatchThreads, 2)
+__global__ void __launch_bounds__(kBatchThreads, 4)
 batched_lu_kernel(const BatchDev* __restrict__ args, unsigned* queue)
 {
     extern __shared__ __align__(16) double bsmem[];
@@ -315,7 +375,10 @@ static size_t smem_for(const int pw[kNumClasses])
 {
     int mx = 8;
     for (int k = 0; k < kNumClasses; ++k) mx = std::max(mx, pw[k]);
-    return sizeof(double) * (size_t)batch_smem_doubles(mx);
+    // the factorisation's panel and U12, or the solve's right-hand sides and
+    // diagonal block, whichever is larger
+    const int solve = kBatchMaxRhs * (kBatchMaxN + 1) + kSolveBlock * (kSolveBlock + 1);
+    return sizeof(double) * (size_t)std::max(batch_smem_doubles(mx), solve);
 }
 
 static tmvg_status build_graph(BatchPlan* p)

@@ -2,6 +2,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <initializer_list>
 #include <new>
 #include <string>
 
@@ -151,23 +152,32 @@ tmvg_status collect_device_error(Context* c, const char* what)
 }
 
 // RAII stream-ordered device buffer for the host-pointer entry points.
+// Device buffers of the host (_host) entry points: views into one grow-only
+// context arena, so repeated calls of the same size allocate nothing.  The
+// arena is only used inside one synchronous host call at a time.
 struct DevBuf {
-    Context* c;
     void* p = nullptr;
-    DevBuf(Context* ctx, size_t bytes) : c(ctx)
-    {
-        if (bytes == 0) bytes = 16;
-        if (cudaMallocAsync(&p, bytes, c->stream) != cudaSuccess) {
-            cudaGetLastError();
-            p = nullptr;
-        }
-    }
-    ~DevBuf()
-    {
-        if (p) cudaFreeAsync(p, c->stream);
-    }
     template <typename T>
     T* as() { return static_cast<T*>(p); }
+};
+
+struct IoBufs {
+    DevBuf b[4];
+    bool ok = false;
+    IoBufs(Context* c, std::initializer_list<size_t> sizes)
+    {
+        size_t off[4] = {0, 0, 0, 0}, total = 0;
+        int q = 0;
+        for (size_t sz : sizes) {
+            off[q++] = total;
+            total += ((sz ? sz : 16) + 255) & ~size_t(255);
+        }
+        unsigned char* base = static_cast<unsigned char*>(grow(c, c->io, c->io_bytes, total));
+        if (!base) return;
+        for (int i = 0; i < q; ++i) b[i].p = base + off[i];
+        ok = true;
+    }
+    DevBuf& operator[](int i) { return b[i]; }
 };
 
 // 32x32 tiled transpose: out (cols x rows, column-major) = in^T where in is
@@ -334,7 +344,9 @@ tmvg_status tmvg_destroy(tmvg_handle h)
     if (c->work) cudaFree(c->work);
     if (c->work2) cudaFree(c->work2);
     if (c->work3) cudaFree(c->work3);
+    if (c->io) cudaFree(c->io);
     if (c->trsv_flags) cudaFree(c->trsv_flags);
+    if (c->trsv_pub) cudaFree(c->trsv_pub);
     if (c->dflags) cudaFree(c->dflags);
     if (c->hflags) cudaFreeHost(c->hflags);
     for (const TimedSpan& sp : c->spans) {
@@ -422,10 +434,10 @@ tmvg_status tmvg_multmm_f64_host(tmvg_handle h, int add, double alpha, int64_t m
     CTX_OR_BAIL(h);
     if (m < 0 || n < 0 || k < 0) return set_error(c, TMVG_BAD_ARG, "multmm: negative size");
     if (m == 0 || n == 0) return TMVG_OK;
-    DevBuf dA(c, sizeof(double) * m * k), dB(c, sizeof(double) * k * n),
-        dC(c, sizeof(double) * m * n),
-        tmp(c, sizeof(double) * std::max(std::max(m * k, k * n), m * n));
-    if (!dA.p || !dB.p || !dC.p || !tmp.p) return set_error(c, TMVG_OOM, "multmm: device buffers");
+    IoBufs io(c, {sizeof(double) * m * k, sizeof(double) * k * n, sizeof(double) * m * n,
+                  sizeof(double) * std::max(std::max(m * k, k * n), m * n)});
+    if (!io.ok) return set_error(c, TMVG_OOM, "multmm: device buffers");
+    DevBuf &dA = io[0], &dB = io[1], &dC = io[2], &tmp = io[3];
     tmvg_status st = h2d_matrix(c, dA.as<double>(), A, m, k, sAi, sAj, tmp.as<double>());
     if (!st) st = h2d_matrix(c, dB.as<double>(), B, k, n, sBi, sBj, tmp.as<double>());
     if (!st && add) st = h2d_matrix(c, dC.as<double>(), C, m, n, sCi, sCj, tmp.as<double>());
@@ -450,9 +462,9 @@ tmvg_status tmvg_lu_decompose_f64_host(tmvg_handle h, int64_t n, double* A, int6
     CTX_OR_BAIL(h);
     if (n < 0) return set_error(c, TMVG_BAD_ARG, "lu: negative n");
     if (n == 0) return TMVG_OK;
-    DevBuf dA(c, sizeof(double) * n * n), tmp(c, sizeof(double) * n * n),
-        dP(c, sizeof(int64_t) * n);
-    if (!dA.p || !tmp.p || !dP.p) return set_error(c, TMVG_OOM, "lu: device buffers");
+    IoBufs io(c, {sizeof(double) * n * n, sizeof(double) * n * n, sizeof(int64_t) * n});
+    if (!io.ok) return set_error(c, TMVG_OOM, "lu: device buffers");
+    DevBuf &dA = io[0], &tmp = io[1], &dP = io[2];
     tmvg_status st = h2d_matrix(c, dA.as<double>(), A, n, n, sAi, sAj, tmp.as<double>());
     if (!st) st = lu_factor<double>(c, n, dA.as<double>(), n, dP.as<int64_t>());
     if (!st) st = d2h_matrix(c, A, dA.as<double>(), n, n, sAi, sAj, tmp.as<double>());
@@ -490,9 +502,10 @@ static tmvg_status div_host(Context* c, bool right, int64_t n, const double* LU,
         return set_error(c, TMVG_BAD_ARG, "div: bad sizes");
     if (n == 0 || other == 0) return TMVG_OK;
     const int64_t rows = right ? other : n, cols = right ? n : other;
-    DevBuf dLU(c, sizeof(double) * n * n), dP(c, sizeof(int64_t) * n),
-        dB(c, sizeof(double) * rows * cols), tmp(c, sizeof(double) * rows * cols);
-    if (!dLU.p || !dP.p || !dB.p || !tmp.p) return set_error(c, TMVG_OOM, "div: device buffers");
+    IoBufs io(c, {sizeof(double) * n * n, sizeof(int64_t) * n, sizeof(double) * rows * cols,
+                  sizeof(double) * rows * cols});
+    if (!io.ok) return set_error(c, TMVG_OOM, "div: device buffers");
+    DevBuf &dLU = io[0], &dP = io[1], &dB = io[2], &tmp = io[3];
     tmvg_status st = check_cuda(
         c,
         cudaMemcpy2DAsync(dLU.p, n * sizeof(double), LU, lda * sizeof(double), n * sizeof(double),
@@ -565,9 +578,10 @@ tmvg_status tmvg_divide_f64_host(tmvg_handle h, int64_t n, const double* A, int6
     CTX_OR_BAIL(h);
     if (n < 0 || nrhs < 0) return set_error(c, TMVG_BAD_ARG, "divide: bad sizes");
     if (n == 0) return TMVG_OK;
-    DevBuf dA(c, sizeof(double) * n * n), dP(c, sizeof(int64_t) * n),
-        dX(c, sizeof(double) * n * std::max<int64_t>(nrhs, 1));
-    if (!dA.p || !dP.p || !dX.p) return set_error(c, TMVG_OOM, "divide: device buffers");
+    IoBufs io(c, {sizeof(double) * n * n, sizeof(int64_t) * n,
+                  sizeof(double) * n * std::max<int64_t>(nrhs, 1)});
+    if (!io.ok) return set_error(c, TMVG_OOM, "divide: device buffers");
+    DevBuf &dA = io[0], &dP = io[1], &dX = io[2];
     tmvg_status st = check_cuda(
         c, cudaMemcpyAsync(dA.p, A, sizeof(double) * n * n, cudaMemcpyHostToDevice, c->stream),
         "divide: A h2d");
@@ -672,9 +686,9 @@ tmvg_status tmvg_lu_solve_mixed_f64_host(tmvg_handle h, int64_t n, const double*
     CTX_OR_BAIL(h);
     if (n < 0 || nrhs < 0) return set_error(c, TMVG_BAD_ARG, "lu_solve_mixed: bad sizes");
     if (n == 0 || nrhs == 0) return TMVG_OK;
-    DevBuf dA(c, sizeof(double) * n * n), dB(c, sizeof(double) * n * nrhs),
-        dX(c, sizeof(double) * n * nrhs);
-    if (!dA.p || !dB.p || !dX.p) return set_error(c, TMVG_OOM, "lu_solve_mixed: device buffers");
+    IoBufs io(c, {sizeof(double) * n * n, sizeof(double) * n * nrhs, sizeof(double) * n * nrhs});
+    if (!io.ok) return set_error(c, TMVG_OOM, "lu_solve_mixed: device buffers");
+    DevBuf &dA = io[0], &dB = io[1], &dX = io[2];
     tmvg_status st = check_cuda(
         c, cudaMemcpyAsync(dA.p, A, sizeof(double) * n * n, cudaMemcpyHostToDevice, c->stream),
         "mixed: A h2d");

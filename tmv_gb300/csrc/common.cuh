@@ -67,6 +67,10 @@ struct Context {
     unsigned* trsv_flags = nullptr;
     unsigned trsv_epoch = 0;
     unsigned long long* trsv_ticket = nullptr;
+    // FP32 inverse-block solves publish each solution entry as one 64-bit
+    // word (epoch << 32 | value bits); grow-only, never needs clearing.
+    unsigned long long* trsv_pub = nullptr;
+    size_t trsv_pub_len = 0;
     // Whether a 16-CTA cluster of the panel kernel can be launched, per
     // element type (-1 unknown, 0 no, 1 yes): [0] double, [1] float.
     int cluster_ok[2] = {-1, -1};
@@ -75,6 +79,9 @@ struct Context {
     // Third grow-only workspace: operand copies of the tensor-core update.
     void* work3 = nullptr;
     size_t work3_bytes = 0;
+    // Device copies of the host entry points' operands (grow-only).
+    void* io = nullptr;
+    size_t io_bytes = 0;
     // Kernel-class timing (off unless tmvg_timing_enable turned it on):
     // spans recorded but not yet read, recycled events, and per-class sums.
     bool timing = false;

@@ -28,6 +28,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <cstring>
 #include <mutex>
 #include <type_traits>
 #include <vector>
@@ -341,19 +342,21 @@ lu_panel_cluster_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, in
 // where the update skips them).  Rows exchanged between threads travel in the
 // same rotated order, which every thread shares.
 //
-// The cluster exchange has no cluster barrier: each CTA reduces its
-// candidate (key, index) and pushes it, with a copy of the candidate row,
-// into a receive slot of every CTA of the cluster with st.async stores that
-// complete transactions on the receiver's mbarrier; the CTA holding row j
-// pushes a copy of row j the same way.  A CTA waits only for the bytes of its
-// own slots (one mbarrier per column parity, re-armed each use), then every
-// warp reduces the 16 candidates from its own shared memory and reads the
-// pivot row and the old row j locally.  A CTA pushes column j+2 into slot
-// parity p only after it has received every CTA's column j+1 data, which each
-// CTA sends after it has finished reading its column j slots.  The waits are
-// bounded: on a timeout the CTA records kDevTimeout and stops, and the others
-// time out in turn.  Used while a 16-CTA cluster covers the panel's rows with
-// one row per thread (m <= 16 * 512).
+// The cluster exchange has no cluster barrier.  Each CTA reduces its
+// candidate and publishes it in its own shared memory (the row, double-
+// buffered by column parity; the CTA holding row j publishes row j the same
+// way), then stores the 16-byte candidate record (key, index) into a slot of
+// every CTA and arrives, with cluster-scope release, on that CTA's mbarrier
+// for the column's parity.  A CTA's warp 0 waits (acquire) until all 16
+// records are in, reduces them, pulls the pivot row from the CTA that holds
+// it (and, in the CTA that holds the pivot row, the old row j), and hands
+// both to the block through shared memory: one DSMEM round trip per column.
+// A CTA rewrites a parity's published rows and remote slots only two columns
+// later, after every CTA has arrived for the column in between, which each
+// does after its pulls of the column before.  The waits are bounded: on a
+// timeout the CTA records kDevTimeout and stops, and the others time out in
+// turn.  Used while a 16-CTA cluster covers the panel's rows with one row per
+// thread (m <= 16 * 512).
 // ---------------------------------------------------------------------
 constexpr int kRegPanelThreads = 512;
 constexpr int kRegPanelWarps = kRegPanelThreads / 32;
@@ -434,12 +437,6 @@ __device__ __forceinline__ void load_row(T (&x)[NB], const T* src)
 __device__ __forceinline__ float recip_rn(float x) { return __frcp_rn(x); }
 __device__ __forceinline__ double recip_rn(double x) { return __drcp_rn(x); }
 
-template <typename T, int NB>
-struct RegSlot {
-    uint4 meta[kClusterCtas];             // per source CTA: key (x, y), index (z)
-    T rows[kClusterCtas][NB];             // per source CTA: its candidate row
-    T diag[NB];                           // row j, from the CTA that holds it
-};
 
 template <typename T, int NB>
 __global__ void __launch_bounds__(kRegPanelThreads, 1)
@@ -450,15 +447,22 @@ lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k
 {
     static_assert(NB % kRegBlock == 0, "whole blocks");
     static_assert(NB * sizeof(T) == 256, "a row is 16 vectors of 16 bytes");
-    constexpr int VEC = 16;  // 16-byte vectors per row
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     __shared__ unsigned long long s_key[kRegPanelWarps];
     __shared__ int s_idx[kRegPanelWarps];
     __shared__ __align__(16) T warp_row[kRegPanelWarps][NB];  // each warp's candidate row
-    __shared__ __align__(16) T diag_local[NB];                // row j of this CTA
-    __shared__ __align__(16) RegSlot<T, NB> slot[2];          // receive slots by column parity
+    // published for remote pulls, double-buffered by column parity
+    __shared__ __align__(16) T pub_row[2][NB];   // this CTA's candidate row
+    __shared__ __align__(16) T pub_diag[2][NB];  // row j, in the CTA that holds it
+    __shared__ __align__(16) uint4 slot[2][kClusterCtas];  // records stored by every CTA
     __shared__ __align__(8) uint64_t mbar[2];
+    // the column's outcome, handed from warp 0 to the block
+    __shared__ __align__(16) T urow[NB];
+    __shared__ __align__(16) T umask[NB];  // urow with zeros outside the columns to update
+    __shared__ __align__(16) T drow[NB];
+    __shared__ unsigned long long s_wk;
+    __shared__ int s_wi;
     __shared__ unsigned char s_mode[kPanelMax];
     __shared__ int s_piv[kPanelMax];
     __shared__ int s_abort;
@@ -473,11 +477,10 @@ lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k
     const bool have = tid < nr;
     const int pr = r0 + tid;  // this thread's row, counted from the panel's top
     T* Ap = A + k + k * lda;
-    const uint32_t slot_bytes = (uint32_t)(G * (16 + NB * sizeof(T)) + NB * sizeof(T));
 
     if (tid == 0) {
-        mbar_init(&mbar[0], 1);
-        mbar_init(&mbar[1], 1);
+        mbar_init(&mbar[0], (uint32_t)G);
+        mbar_init(&mbar[1], (uint32_t)G);
         s_abort = 0;
         mbar_fence_init();
     }
@@ -485,7 +488,7 @@ lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k
     T x[NB];
 #pragma unroll
     for (int c = 0; c < NB; ++c) x[c] = (have && c < nb) ? Ap[pr + c * lda] : T(0);
-    cluster.sync();  // every CTA's mbarriers are initialised before any push
+    cluster.sync();  // every CTA's mbarriers are initialised before any arrival
 
     bool prev_uf = false;
     int rot = 0;  // x[p] holds column (p + rot) mod NB
@@ -497,9 +500,8 @@ lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k
             if (jj >= nb) break;
             const int par = jj & 1;
             const bool r2 = s_mode[jj] && !prev_uf;
-            const int owner_j = jj / rows_per_cta;
-            if (tid == 0) mbar_expect_tx(&mbar[par], slot_bytes);
-            // 1. this warp's candidate; its row and row jj into shared memory
+            const int owner_j = jj < rows_per_cta ? 0 : jj / rows_per_cta;
+            // 1. this warp's candidate; its row, and row jj, into shared memory
             unsigned long long bk = 0;
             int bi = INT_MAX;
             if (have && pr >= jj) {
@@ -509,48 +511,64 @@ lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k
             warp_key_reduce(bk, bi);
             if (have && bi == pr) store_row<T, NB>(warp_row[warp], x);
             if (lane == 0) { s_key[warp] = bk; s_idx[warp] = bi; }
-            if (have && pr == jj) store_row<T, NB>(diag_local, x);
+            if (have && pr == jj) store_row<T, NB>(pub_diag[par], x);
             __syncthreads();
-            // 2. push: warp 0 the CTA's candidate, warp 1 row jj (its owner only)
             if (warp == 0) {
+                // 2. publish this CTA's candidate, store its record into every
+                //    CTA and arrive there (release)
                 bk = lane < kRegPanelWarps ? s_key[lane] : 0ull;
                 bi = lane < kRegPanelWarps ? s_idx[lane] : INT_MAX;
                 warp_key_reduce(bk, bi);
-                const uint4* src = reinterpret_cast<const uint4*>(
-                    warp_row[bi != INT_MAX ? (bi - r0) >> 5 : 0]);
-                const uint4 meta = make_uint4((unsigned)bk, (unsigned)(bk >> 32), (unsigned)bi, 0u);
-                for (int t = lane; t < G * (VEC + 1); t += 32) {
-                    const int d = t / (VEC + 1), v = t % (VEC + 1);
-                    const uint32_t mb = cluster_addr(&mbar[par], d);
-                    if (v == VEC)
-                        st_async16(cluster_addr(&slot[par].meta[cta], d), meta, mb);
-                    else
-                        st_async16(cluster_addr(&slot[par].rows[cta][v * (16 / sizeof(T))], d), src[v], mb);
+                if (bi != INT_MAX && lane < 16)
+                    reinterpret_cast<uint4*>(pub_row[par])[lane] =
+                        reinterpret_cast<const uint4*>(warp_row[(bi - r0) >> 5])[lane];
+                __syncwarp();
+                if (lane < G) {
+                    st_cluster16(cluster_addr(&slot[par][cta], lane),
+                                 make_uint4((unsigned)bk, (unsigned)(bk >> 32), (unsigned)bi, 0u));
+                    mbar_arrive_remote_release(cluster_addr(&mbar[par], lane));
                 }
-            } else if (warp == 1 && cta == owner_j) {
-                const uint4* src = reinterpret_cast<const uint4*>(diag_local);
-                for (int t = lane; t < G * VEC; t += 32) {
-                    const int d = t / VEC, v = t % VEC;
-                    st_async16(cluster_addr(&slot[par].diag[v * (16 / sizeof(T))], d), src[v],
-                               cluster_addr(&mbar[par], d));
+                // 3. wait for every CTA's record (bounded), reduce, pull rows
+                // every lane acquires the phase itself: its loads below must
+                // see the records and the published rows
+                const bool got = __all_sync(0xffffffffu, mbar_wait_cluster(&mbar[par], (uint32_t)((jj >> 1) & 1)));
+                if (!got) {
+                    if (lane == 0) {
+                        s_abort = 1;
+                        atomicCAS(err, (int)kDevOk, (int)kDevTimeout);
+                    }
+                } else {
+                    const uint4 mt = lane < G ? slot[par][lane] : make_uint4(0u, 0u, (unsigned)INT_MAX, 0u);
+                    unsigned long long wk = ((unsigned long long)mt.y << 32) | mt.x;
+                    int wi = (int)mt.z;
+                    warp_key_reduce(wk, wi);
+                    if (lane == 0) { s_wk = wk; s_wi = wi; }
+                    if (!underflows<T>(pivot_key_value(wk))) {
+                        const int owner_w = wi / rows_per_cta;
+                        if (lane < 16) {
+                            const uint4 v = ld_cluster16(cluster_addr(&pub_row[par][0], owner_w) + 16 * lane);
+                            reinterpret_cast<uint4*>(urow)[lane] = v;
+                            // the columns this step updates are positions u+1 .. lim-1
+                            T e[16 / sizeof(T)];
+                            memcpy(e, &v, 16);
+#pragma unroll
+                            for (int q = 0; q < (int)(16 / sizeof(T)); ++q) {
+                                const int pos = lane * (int)(16 / sizeof(T)) + q;
+                                if (pos <= u || pos >= lim) e[q] = T(0);
+                            }
+                            uint4 w;
+                            memcpy(&w, e, 16);
+                            reinterpret_cast<uint4*>(umask)[lane] = w;
+                        } else if (cta == owner_w && wi != jj)
+                            reinterpret_cast<uint4*>(drow)[lane - 16] =
+                                ld_cluster16(cluster_addr(&pub_diag[par][0], owner_j) + 16 * (lane - 16));
+                    }
                 }
             }
-            // 3. every thread waits for this CTA's slots (bounded; the data is
-            // visible to the threads that observe the phase), then reduces
-            // them locally; a timeout anywhere stops the whole CTA
-            const bool got = mbar_wait(&mbar[par], (uint32_t)((jj >> 1) & 1));
-            if (__syncthreads_or(!got)) {
-                if (tid == 0) {
-                    s_abort = 1;
-                    atomicCAS(err, (int)kDevOk, (int)kDevTimeout);
-                }
-                __syncthreads();
-                break;
-            }
-            const uint4 mt = lane < G ? slot[par].meta[lane] : make_uint4(0u, 0u, (unsigned)INT_MAX, 0u);
-            unsigned long long wk = ((unsigned long long)mt.y << 32) | mt.x;
-            int wi = (int)mt.z;
-            warp_key_reduce(wk, wi);
+            __syncthreads();
+            if (s_abort) break;
+            const unsigned long long wk = s_wk;
+            const int wi = s_wi;
             if (underflows<T>(pivot_key_value(wk))) {
                 if (tid == 0) s_piv[jj] = (int)(k + jj);
                 if (have && pr >= jj) x[u] = T(0);
@@ -559,25 +577,50 @@ lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k
             }
             prev_uf = false;
             if (tid == 0) s_piv[jj] = (int)(k + wi);
-            const T* urow = slot[par].rows[wi / rows_per_cta];
             // the interchange: row jj takes the pivot row, row wi the old row jj
             const T* src = nullptr;
             if (have && pr == jj) src = urow;
-            else if (have && pr == wi) src = slot[par].diag;
+            else if (have && pr == wi) src = drow;
             if (src) load_row<T, NB>(x, src);
             if (have && pr > jj) {
                 // TMV scales the column by the reciprocal of the pivot
                 using V = Vec16<T>;
                 const T l = x[u] * recip_rn(urow[u]);
                 x[u] = l;
+                if (isfinite(l)) {
+                    // full width against the masked pivot row: a zero there
+                    // leaves x unchanged (up to the sign of a zero x)
+                    if constexpr (std::is_same<T, float>::value) {
+                        const float2 nl = make_float2(-l, -l);
 #pragma unroll
-                for (int v = 0; v < NB / V::E; ++v) {
-                    if ((v + 1) * V::E <= u + 1) continue;  // columns <= u only
-                    const typename V::type uv = reinterpret_cast<const typename V::type*>(urow)[v];
+                        for (int v = 0; v < NB / 4; ++v) {
+                            const float4 uv = reinterpret_cast<const float4*>(umask)[v];
+                            const float2 a = __ffma2_rn(nl, make_float2(uv.x, uv.y), make_float2(x[4 * v], x[4 * v + 1]));
+                            const float2 b = __ffma2_rn(nl, make_float2(uv.z, uv.w), make_float2(x[4 * v + 2], x[4 * v + 3]));
+                            x[4 * v] = a.x;
+                            x[4 * v + 1] = a.y;
+                            x[4 * v + 2] = b.x;
+                            x[4 * v + 3] = b.y;
+                        }
+                    } else {
 #pragma unroll
-                    for (int e = 0; e < V::E; ++e) {
-                        const int c = v * V::E + e;
-                        if (c > u && c < lim) x[c] -= l * V::get(uv, e);
+                        for (int v = 0; v < NB / V::E; ++v) {
+                            const typename V::type uv = reinterpret_cast<const typename V::type*>(umask)[v];
+#pragma unroll
+                            for (int e = 0; e < V::E; ++e) x[v * V::E + e] -= l * V::get(uv, e);
+                        }
+                    }
+                } else {
+                    // a NaN or infinite multiplier touches only the columns to update
+#pragma unroll
+                    for (int v = 0; v < NB / V::E; ++v) {
+                        if ((v + 1) * V::E <= u + 1) continue;  // columns <= u only
+                        const typename V::type uv = reinterpret_cast<const typename V::type*>(urow)[v];
+#pragma unroll
+                        for (int e = 0; e < V::E; ++e) {
+                            const int c = v * V::E + e;
+                            if (c > u && c < lim) x[c] -= l * V::get(uv, e);
+                        }
                     }
                 }
             }

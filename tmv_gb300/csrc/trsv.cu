@@ -17,6 +17,8 @@
 // x_i = b_i - sum_j T_ij x_j over j in dependency order.
 #include "trsv.cuh"
 
+#include <type_traits>
+
 #include <algorithm>
 #include <vector>
 
@@ -356,6 +358,139 @@ trsv_invdiag_kernel(int64_t n, const T* __restrict__ tri, int64_t tsi, int64_t t
     if (tid == 0) st_release(flags + b, epoch);
 }
 
+// ---------------------------------------------------------------------
+// FP32 inverse-block solve with published values.
+//
+// Same blocking and arithmetic as trsv_invdiag_kernel, but a finished block
+// publishes each entry as one 64-bit word (epoch << 32 | float bits) with a
+// relaxed gpu-scope store, so the word is both the value and its ready flag:
+// a consumer thread polls exactly the word it needs (bounded), and the
+// separate flag, fence and reload of x drop out of the dependency chain.
+// Each CTA also loads its inverse diagonal block and right-hand side before
+// it waits for anything.
+// ---------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p)
+{
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v)
+{
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__global__ void __launch_bounds__(256)
+trsv_pub_kernel(int64_t n, const float* __restrict__ tri, int64_t tsi, int64_t tsj,
+                const float* __restrict__ dinv, const int* __restrict__ singular, bool unit,
+                float* x, int64_t incx, bool skip_zero, unsigned long long* pub, unsigned epoch,
+                unsigned long long* ticket, int* err)
+{
+    __shared__ int s_blk, s_abort;
+    __shared__ float xj[2][kIB];
+    __shared__ float rhs[kIB];
+    __shared__ float part[2][kIB];
+    const int tid = threadIdx.x;
+    const int i = tid & (kIB - 1), h = tid >> 7;  // row of the block, half of the columns
+    if (tid == 0) {
+        s_blk = (int)atomicAdd(ticket, 1ull);
+        s_abort = 0;
+    }
+    __syncthreads();
+    const int64_t b = s_blk;
+    const int64_t nblk = (n + kIB - 1) / kIB;
+    if (b >= nblk) return;
+    const int64_t r0 = b * kIB;
+    const int rows = (int)min((int64_t)kIB, n - r0);
+    const unsigned long long tag = (unsigned long long)epoch << 32;
+
+    // independent of the other blocks: right-hand side and inverse block
+    const float b_i = (tid < kIB && tid < rows) ? x[(r0 + tid) * incx] : 0.0f;
+    const bool sing = singular[b] != 0;
+    float di[64];
+    {
+        const float* Di = dinv + b * (int64_t)kIB * kIB;
+#pragma unroll
+        for (int l = 0; l < 64; ++l) di[l] = sing ? 0.0f : Di[i + (h * 64 + l) * kIB];
+    }
+
+    float acc = 0.0f;
+    for (int64_t j = 0; j < b; ++j) {
+        const int64_t c0 = j * kIB + h * 64;
+        float a[64];
+#pragma unroll
+        for (int c = 0; c < 64; ++c) a[c] = (i < rows) ? tri[(r0 + i) * tsi + (c0 + c) * tsj] : 0.0f;
+        float* xb = xj[j & 1];
+        if (tid < kIB) {
+            const unsigned long long* w = pub + j * kIB + tid;
+            unsigned long long v = ld_relaxed_u64(w);
+            unsigned spins = 0;
+            while ((v & 0xffffffff00000000ull) != tag) {
+                if (++spins > kSpinLimit || *((volatile int*)err) == kDevTimeout) {
+                    atomicCAS(err, (int)kDevOk, (int)kDevTimeout);
+                    s_abort = 1;
+                    break;
+                }
+                if (spins > 32) __nanosleep(32);
+                v = ld_relaxed_u64(w);
+            }
+            xb[tid] = __uint_as_float((unsigned)v);
+        }
+        __syncthreads();  // xb complete; the other buffer is free again
+        if (s_abort) return;
+#pragma unroll
+        for (int c = 0; c < 64; ++c) acc -= a[c] * xb[h * 64 + c];
+    }
+    part[h][i] = acc;
+    __syncthreads();
+    if (tid < kIB) rhs[tid] = b_i + part[0][tid] + part[1][tid];
+    __syncthreads();
+    if (!sing) {
+        // x_b = Dinv_b rhs: row i sums its half of the columns
+        float sum = 0.0f;
+#pragma unroll
+        for (int l = 0; l < 64; ++l) sum += di[l] * rhs[h * 64 + l];
+        part[h][i] = sum;
+        __syncthreads();
+        if (tid < rows) {
+            const float v = part[0][tid] + part[1][tid];
+            x[(r0 + tid) * incx] = v;
+            st_relaxed_u64(pub + r0 + tid, tag | __float_as_uint(v));
+        }
+    } else if (tid < 32) {
+        // zero diagonal somewhere: substitution with TMV's zero skipping
+        bool sg = false;
+        for (int jj = 0; jj < rows; ++jj) {
+            __syncwarp();
+            float v = rhs[jj];
+            if (!unit) {
+                const float d = tri[(r0 + jj) * tsi + (r0 + jj) * tsj];
+                if (skip_zero) {
+                    if (v != 0.0f) {
+                        if (d == 0.0f) sg = true;
+                        else v = v / d;
+                    }
+                } else {
+                    if (d == 0.0f) sg = true;
+                    else v = v * (1.0f / d);
+                }
+            }
+            __syncwarp();
+            if (tid == 0) rhs[jj] = v;
+            if (v != 0.0f || !skip_zero)
+                for (int k2 = jj + 1 + tid; k2 < rows; k2 += 32)
+                    rhs[k2] -= tri[(r0 + k2) * tsi + (r0 + jj) * tsj] * v;
+        }
+        if (sg) atomicCAS(err, (int)kDevOk, (int)kDevSingular);
+        __syncwarp();
+        for (int k2 = tid; k2 < rows; k2 += 32) {
+            x[(r0 + k2) * incx] = rhs[k2];
+            st_relaxed_u64(pub + r0 + k2, tag | __float_as_uint(rhs[k2]));
+        }
+    }
+}
+
 template <typename T>
 tmvg_status trsv_factor_inverse_blocks(Context* c, int64_t n, const T* tri, int64_t tsi,
                                        int64_t tsj, bool upper, bool unit, T* dinv, int* singular)
@@ -395,6 +530,31 @@ tmvg_status trsv_with_inverse_blocks(Context* c, int64_t n, const T* tri, int64_
     tmvg_status st = check_cuda(
         c, cudaMemsetAsync(c->trsv_ticket, 0, sizeof(unsigned long long), c->stream), "ticket");
     if (st) return st;
+    if constexpr (std::is_same<T, float>::value) {
+        if ((size_t)n > c->trsv_pub_len) {
+            // grow-only; the old words are discarded with the buffer
+            st = check_cuda(c, cudaStreamSynchronize(c->stream), "trsv pub sync");
+            if (st) return st;
+            if (c->trsv_pub) cudaFree(c->trsv_pub);
+            c->trsv_pub = nullptr;
+            c->trsv_pub_len = 0;
+            if (cudaMalloc(&c->trsv_pub, sizeof(unsigned long long) * (size_t)n) != cudaSuccess) {
+                cudaGetLastError();
+                return set_error(c, TMVG_OOM, "trsv: publication buffer");
+            }
+            // epoch 0 is never used by a solve
+            st = check_cuda(c, cudaMemset(c->trsv_pub, 0, sizeof(unsigned long long) * (size_t)n),
+                            "trsv pub clear");
+            if (st) return st;
+            c->trsv_pub_len = (size_t)n;
+        }
+        if (epoch == 0) ++c->trsv_epoch;  // skip the clear value on wrap-around
+        trsv_pub_kernel<<<(unsigned)nblk, 256, 0, c->stream>>>(
+            n, tri, tsi, tsj, dinv, singular, unit, x, incx, skip_zero, c->trsv_pub,
+            c->trsv_epoch, c->trsv_ticket, c->dflags);
+        ++c->launches;
+        return check_cuda(c, cudaGetLastError(), "trsv pub launch");
+    }
     trsv_invdiag_kernel<T><<<(unsigned)nblk, 256, 0, c->stream>>>(
         n, tri, tsi, tsj, dinv, singular, unit, x, incx, skip_zero, c->trsv_flags, epoch,
         c->trsv_ticket, c->dflags);
