@@ -369,15 +369,19 @@ def batched_bench(dev, args, with_cpu: bool) -> dict:
 
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic
-# byte of each kernel class, from one ncu capture of the class's kernels on
-# the n = 8192 workload (the capture commands and figures are in profiles/).
-NCU_TRAFFIC_PER_ALG_BYTE: dict = {}
+# byte of each kernel class, from one ncu capture of the class's main kernel
+# on the n = 8192 workload (commands and figures in profiles/):
+#   panel: lu_panel_cluster_reg_kernel, k = 256: 2.14 MB / 4.06 MB
+#   trailing_update: tf32x3_update_kernel, k = 256: 432.1 MB / 495.7 MB
+#   tri_solve: trsv_pub_kernel: 139.6 MB / 138.5 MB
+# The traffic of a span is its algorithmic bytes times the ratio.
+NCU_TRAFFIC_PER_ALG_BYTE: dict = {"panel": 0.527, "trailing_update": 0.872, "tri_solve": 1.008}
 
 KERNEL_NAMES = {
-    "panel": "lu_panel_cluster_kernel (16-CTA cluster panel factorisation)",
-    "trailing_update": "A22 -= L21 U12 (FP32: split + tf32x3_update_kernel on tcgen05; "
-                       "FP64: gemm_simt_kernel<double>)",
-    "tri_solve": "trsv_invdiag_kernel (sync-free triangular solve, inverted 128-blocks)",
+    "panel": "lu_panel_cluster_reg_kernel (16-CTA cluster, register-resident FP32 panel)",
+    "trailing_update": "U12 solve + A22 -= L21 U12 (FP32: u12_reg_kernel + tf32x3_update_kernel "
+                       "on tcgen05; FP64: u12_reg_kernel + gemm_simt_kernel<double>)",
+    "tri_solve": "trsv_pub_kernel (FP32 inverse-block triangular solve)",
     "residual": "residual_partial_kernel + residual_final_kernel (FP64 b - A x)",
 }
 
