@@ -766,10 +766,11 @@ panel_u12_kernel(int nb, const T* __restrict__ L, int64_t lda, T* __restrict__ A
 // SPLIT the kernel also writes the TF32 hi/lo split of U12 (column-major,
 // leading dimension nb) for the tensor-core trailing update.
 // ---------------------------------------------------------------------
-constexpr int kU12RegThreads = 64;   // columns per CTA, one per computing thread
-constexpr int kU12RegBlock = 256;    // threads per CTA: all of them stage, 64 compute
+constexpr int kU12RegThreads = 64;   // columns per CTA (wide launches), one per computing thread
+constexpr int kU12NarrowCols = 8;    // columns per CTA when only a panel's width is solved
+constexpr int kU12RegBlock = 256;    // threads per CTA: all of them stage, COLS compute
 
-template <typename T, int NB, bool SPLIT>
+template <typename T, int NB, bool SPLIT, int COLS>
 __global__ void __launch_bounds__(kU12RegBlock)
 u12_reg_kernel(int nb, const T* __restrict__ L, int64_t lda, T* __restrict__ A12, int64_t ncols,
                float* __restrict__ Bhi, float* __restrict__ Blo)
@@ -777,9 +778,9 @@ u12_reg_kernel(int nb, const T* __restrict__ L, int64_t lda, T* __restrict__ A12
     using V = Vec16<T>;
     constexpr int XP = NB + V::E;  // padded staging row: conflict-free vector access
     __shared__ __align__(16) T LsT[NB][NB];  // LsT[j][i] = L(i, j) for i > j, else 0
-    __shared__ __align__(16) T Xs[kU12RegThreads][XP];
+    __shared__ __align__(16) T Xs[COLS][XP];
     const int tid = threadIdx.x;
-    const int64_t c0 = (int64_t)blockIdx.x * kU12RegThreads;
+    const int64_t c0 = (int64_t)blockIdx.x * COLS;
 
     // stage L11 and this CTA's columns, eight independent loads in flight
     constexpr int LU = 8;
@@ -797,23 +798,23 @@ u12_reg_kernel(int nb, const T* __restrict__ L, int64_t lda, T* __restrict__ A12
             if (t < NB * NB) LsT[t / NB][t % NB] = v[q];
         }
     }
-    for (int t0 = tid; t0 < kU12RegThreads * NB; t0 += kU12RegBlock * LU) {
+    for (int t0 = tid; t0 < COLS * NB; t0 += kU12RegBlock * LU) {
         T v[LU];
 #pragma unroll
         for (int q = 0; q < LU; ++q) {
             const int t = t0 + q * kU12RegBlock;
             const int i = t % NB, c = t / NB;
-            v[q] = (t < kU12RegThreads * NB && i < nb && c0 + c < ncols) ? A12[i + (c0 + c) * lda] : T(0);
+            v[q] = (t < COLS * NB && i < nb && c0 + c < ncols) ? A12[i + (c0 + c) * lda] : T(0);
         }
 #pragma unroll
         for (int q = 0; q < LU; ++q) {
             const int t = t0 + q * kU12RegBlock;
-            if (t < kU12RegThreads * NB) Xs[t / NB][t % NB] = v[q];
+            if (t < COLS * NB) Xs[t / NB][t % NB] = v[q];
         }
     }
     __syncthreads();
 
-    if (tid < kU12RegThreads) {
+    if (tid < COLS) {
     T x[NB];
     load_row<T, NB>(x, Xs[tid]);
 #pragma unroll
@@ -832,7 +833,7 @@ u12_reg_kernel(int nb, const T* __restrict__ L, int64_t lda, T* __restrict__ A12
     }
     __syncthreads();
 
-    for (int t0 = tid; t0 < kU12RegThreads * NB; t0 += kU12RegBlock) {
+    for (int t0 = tid; t0 < COLS * NB; t0 += kU12RegBlock) {
         const int i = t0 % NB, c = t0 / NB;
         if (i < nb && c0 + c < ncols) {
             const T val = Xs[c][i];
@@ -1148,13 +1149,25 @@ static tmvg_status update_columns(Context* c, int64_t n, T* A, int64_t lda, int6
     tmvg_status st;
     if (nb <= RegPanel<T>::NB) {
         constexpr int NB = RegPanel<T>::NB;
-        const unsigned grid = (unsigned)ceil_div(nc, kU12RegThreads);
-        if (tc)
-            u12_reg_kernel<T, NB, true><<<grid, kU12RegBlock, 0, c->stream>>>(nb, L11, lda, A12, nc,
-                                                                             bc.Bhi, bc.Blo);
-        else
-            u12_reg_kernel<T, NB, false><<<grid, kU12RegBlock, 0, c->stream>>>(nb, L11, lda, A12, nc,
-                                                                              nullptr, nullptr);
+        // a few columns (the next panel's): spread over more CTAs, since
+        // each one's latency is staging L11 and the substitution chain
+        if (nc <= NB) {
+            const unsigned grid = (unsigned)ceil_div(nc, kU12NarrowCols);
+            if (tc)
+                u12_reg_kernel<T, NB, true, kU12NarrowCols><<<grid, kU12RegBlock, 0, c->stream>>>(
+                    nb, L11, lda, A12, nc, bc.Bhi, bc.Blo);
+            else
+                u12_reg_kernel<T, NB, false, kU12NarrowCols><<<grid, kU12RegBlock, 0, c->stream>>>(
+                    nb, L11, lda, A12, nc, nullptr, nullptr);
+        } else {
+            const unsigned grid = (unsigned)ceil_div(nc, kU12RegThreads);
+            if (tc)
+                u12_reg_kernel<T, NB, true, kU12RegThreads><<<grid, kU12RegBlock, 0, c->stream>>>(
+                    nb, L11, lda, A12, nc, bc.Bhi, bc.Blo);
+            else
+                u12_reg_kernel<T, NB, false, kU12RegThreads><<<grid, kU12RegBlock, 0, c->stream>>>(
+                    nb, L11, lda, A12, nc, nullptr, nullptr);
+        }
         ++c->launches;
         st = check_cuda(c, cudaGetLastError(), "lu: u12 launch");
         if (st) return st;
