@@ -392,6 +392,48 @@ __device__ __forceinline__ void warp_key_reduce(unsigned long long& key, int& id
     idx = (int)mi;
 }
 
+// Pivot key of a panel element with integer operations only: the IEEE bits
+// of |v| plus 1 (non-negative floats order like their bit patterns, and the
+// conversion of a float to double is exact, so this is the order of the FP64
+// comparison of pivot_key()); 0 for a NaN that is not the first element; the
+// first element's NaN counts as +inf, or as 0 in the second column of a
+// two-column leaf.  FP64 instructions run at 1/64 of the FP32 rate on this
+// part, and every thread of the panel computes a key per column.
+__device__ __forceinline__ unsigned long long reg_pivot_key(float v, bool first, bool r2mode)
+{
+    const unsigned a = __float_as_uint(v) & 0x7fffffffu;
+    if (a > 0x7f800000u) return first ? (r2mode ? 1ull : 0x7f800001ull) : 0ull;
+    return (unsigned long long)a + 1ull;
+}
+__device__ __forceinline__ unsigned long long reg_pivot_key(double v, bool first, bool r2mode)
+{
+    const unsigned long long a = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+    if (a > 0x7ff0000000000000ull) return first ? (r2mode ? 1ull : 0x7ff0000000000001ull) : 0ull;
+    return a + 1ull;
+}
+
+// |pivot| < numeric_limits<T>::min() on a reg_pivot_key (key 0 included).
+template <typename T>
+__device__ __forceinline__ bool reg_key_underflows(unsigned long long key)
+{
+    return sizeof(T) == 4 ? key <= 0x00800000ull : key <= 0x0010000000000000ull;
+}
+
+// warp_key_reduce for reg_pivot_key: FP32 keys fit 32 bits (two redux steps).
+template <typename T>
+__device__ __forceinline__ void reg_key_reduce(unsigned long long& key, int& idx)
+{
+    if constexpr (sizeof(T) == 4) {
+        const unsigned k32 = (unsigned)key;
+        const unsigned mk = __reduce_max_sync(0xffffffffu, k32);
+        const unsigned mi = __reduce_min_sync(0xffffffffu, k32 == mk ? (unsigned)idx : 0x7fffffffu);
+        key = mk;
+        idx = (int)mi;
+    } else {
+        warp_key_reduce(key, idx);
+    }
+}
+
 // 16-byte vectors of a row held in registers (4 floats or 2 doubles).
 template <typename T>
 struct Vec16;
@@ -505,10 +547,10 @@ lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k
             unsigned long long bk = 0;
             int bi = INT_MAX;
             if (have && pr >= jj) {
-                bk = pivot_key_bits(pivot_key(x[u], pr == jj, r2));
+                bk = reg_pivot_key(x[u], pr == jj, r2);
                 bi = pr;
             }
-            warp_key_reduce(bk, bi);
+            reg_key_reduce<T>(bk, bi);
             if (have && bi == pr) store_row<T, NB>(warp_row[warp], x);
             if (lane == 0) { s_key[warp] = bk; s_idx[warp] = bi; }
             if (have && pr == jj) store_row<T, NB>(pub_diag[par], x);
@@ -518,7 +560,7 @@ lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k
                 //    CTA and arrive there (release)
                 bk = lane < kRegPanelWarps ? s_key[lane] : 0ull;
                 bi = lane < kRegPanelWarps ? s_idx[lane] : INT_MAX;
-                warp_key_reduce(bk, bi);
+                reg_key_reduce<T>(bk, bi);
                 if (bi != INT_MAX && lane < 16)
                     reinterpret_cast<uint4*>(pub_row[par])[lane] =
                         reinterpret_cast<const uint4*>(warp_row[(bi - r0) >> 5])[lane];
@@ -541,9 +583,9 @@ lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k
                     const uint4 mt = lane < G ? slot[par][lane] : make_uint4(0u, 0u, (unsigned)INT_MAX, 0u);
                     unsigned long long wk = ((unsigned long long)mt.y << 32) | mt.x;
                     int wi = (int)mt.z;
-                    warp_key_reduce(wk, wi);
+                    reg_key_reduce<T>(wk, wi);
                     if (lane == 0) { s_wk = wk; s_wi = wi; }
-                    if (!underflows<T>(pivot_key_value(wk))) {
+                    if (!reg_key_underflows<T>(wk)) {
                         const int owner_w = wi / rows_per_cta;
                         if (lane < 16) {
                             const uint4 v = ld_cluster16(cluster_addr(&pub_row[par][0], owner_w) + 16 * lane);
@@ -569,7 +611,7 @@ lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k
             if (s_abort) break;
             const unsigned long long wk = s_wk;
             const int wi = s_wi;
-            if (underflows<T>(pivot_key_value(wk))) {
+            if (reg_key_underflows<T>(wk)) {
                 if (tid == 0) s_piv[jj] = (int)(k + jj);
                 if (have && pr >= jj) x[u] = T(0);
                 prev_uf = true;
