@@ -186,6 +186,30 @@ tmvg_status tmvg_lu_det_f64(tmvg_handle h, int64_t n, const double* LU,
                             int64_t lda, const int64_t* P, double* det,
                             double* logdet, double* sign);
 
+/* m.inverse(): A^-1 from stored factors, U^-1 L^-1 with its columns
+ * reverse-permuted by P.  Replaces LU_Inverse<double,double>
+ * (src/TMV_LUInverse.cpp:236-299), reached through LUDiv::doMakeInverse
+ * (src/TMV_LUD.cpp:158-170).  Minv: n x n column-major (ldm), or a host view
+ * with strides (msi, msj) for the _host form.  TMVG_SINGULAR for a zero
+ * U(j,j), where TMV throws SingularUpperTriMatrix (src/TMV_TriInverse.cpp:58-68). */
+tmvg_status tmvg_lu_inverse_f64(tmvg_handle h, int64_t n, const double* LU,
+                                int64_t lda, const int64_t* P, double* Minv,
+                                int64_t ldm);
+tmvg_status tmvg_lu_inverse_f64_host(tmvg_handle h, int64_t n,
+                                     const double* LU, int64_t lda,
+                                     const int64_t* P, double* Minv,
+                                     int64_t msi, int64_t msj);
+
+/* m.makeInverseATA(ata): (A^T A)^-1 from stored factors (the permutation
+ * cancels).  Replaces LUDiv::doMakeInverseATA (src/TMV_LUD.cpp:172-200). */
+tmvg_status tmvg_lu_inverse_ata_f64(tmvg_handle h, int64_t n, const double* LU,
+                                    int64_t lda, double* ATA, int64_t ldata);
+
+/* m.isSingular(): *singular = 1 when min |U(j,j)| <= epsilon * max |U(j,j)|.
+ * Replaces LUDiv::isSingular (src/TMV_LUD.cpp:204-209). */
+tmvg_status tmvg_lu_is_singular_f64(tmvg_handle h, int64_t n, const double* LU,
+                                    int64_t lda, int* singular);
+
 /* ---- mixed-precision solve with FP64 iterative refinement ---------------
  * X = A^-1 B for a column-major FP64 A: the factorisation runs in FP32
  * (pivots chosen by comparing in FP64), then each column is refined with

@@ -167,6 +167,34 @@ class Port(_Backend):
         return d.value, ld.value, s.value
 
 
+    def lu_inverse(self, LU: np.ndarray, P: np.ndarray) -> np.ndarray:
+        """LU_Inverse: A^-1 from the factors (column-major)."""
+        n = LU.shape[0]
+        LU = np.asfortranarray(LU)
+        M = np.zeros((n, n), order="F")
+        f = self._f("lu_inverse", C.c_int, [i64, vp, i64, vp, vp, i64])
+        rc = f(n, _p(LU), max(n, 1), _p(np.ascontiguousarray(P, dtype=np.int64)), _p(M), max(n, 1))
+        if rc:
+            raise RuntimeError(f"lu_inverse rc={rc}")
+        return M
+
+    def lu_inverse_ata(self, LU: np.ndarray) -> np.ndarray:
+        """LUDiv::makeInverseATA: (A^T A)^-1 from the factors."""
+        n = LU.shape[0]
+        LU = np.asfortranarray(LU)
+        M = np.zeros((n, n), order="F")
+        f = self._f("lu_inverse_ata", C.c_int, [i64, vp, i64, vp, i64])
+        rc = f(n, _p(LU), max(n, 1), _p(M), max(n, 1))
+        if rc:
+            raise RuntimeError(f"lu_inverse_ata rc={rc}")
+        return M
+
+    def lu_is_singular(self, LU: np.ndarray) -> bool:
+        LU = np.asfortranarray(LU)
+        f = self._f("lu_is_singular", C.c_int, [i64, vp, i64])
+        return bool(f(LU.shape[0], _p(LU), max(LU.shape[0], 1)))
+
+
 class Ref(_Backend):
     prefix = "tmvref_"
 
@@ -191,6 +219,17 @@ class Ref(_Backend):
         if rc:
             raise RuntimeError(f"rdivide rc={rc}")
         return X
+
+    def inverse_of(self, A: np.ndarray):
+        """TMV's own m.inverse(), m.makeInverseATA() and m.isSingular()."""
+        n = A.shape[0]
+        A = np.asfortranarray(A)
+        M = np.zeros((n, n), order="F")
+        T = np.zeros((n, n), order="F")
+        s = C.c_int(0)
+        f = self._f("inverse", C.c_int, [i64, vp, vp, vp, C.POINTER(C.c_int)])
+        rc = f(n, _p(A), _p(M), _p(T), C.byref(s))
+        return rc, M, T, bool(s.value)
 
     def det_of(self, A: np.ndarray):
         d, ld, s = dbl(), dbl(), dbl()

@@ -165,6 +165,26 @@ int tmvref_det(ptrdiff_t n, const double* A, double* det, double* logdet,
     });
 }
 
+int tmvref_inverse(ptrdiff_t n, const double* A, double* minv, double* ata, int* singular)
+{
+    // m.inverse() (LUDiv::doMakeInverse -> LU_Inverse), m.makeInverseATA()
+    // and m.isSingular() on an LU-divided copy of A
+    return guarded([&] {
+        tmv::Matrix<double, tmv::ColMajor> m(
+            tmv::MatrixViewOf(A, n, n, tmv::ColMajor));
+        m.divideUsing(tmv::LU);
+        m.saveDiv();
+        m.setDiv();
+        if (singular) *singular = m.isSingular() ? 1 : 0;
+        if (minv) tmv::MatrixViewOf(minv, n, n, tmv::ColMajor) = m.inverse();
+        if (ata) {
+            tmv::Matrix<double, tmv::ColMajor> t(n, n);
+            m.makeInverseATA(t);
+            tmv::MatrixViewOf(ata, n, n, tmv::ColMajor) = t;
+        }
+    });
+}
+
 // Ragged batch: system i has order n[i], nrhs[i] right-hand sides, A_i at
 // A + a_off[i] (column-major n_i x n_i), B_i at B + b_off[i] (column-major
 // n_i x nrhs_i).  X_i = B_i / A_i is written over B_i.  status[i] per system.

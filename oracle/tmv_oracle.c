@@ -24,6 +24,11 @@
  *   TriLDivEq (vector) ........... src/TMV_TriDiv_V.cpp:148-462
  *   LU_LDivEq / LU_RDivEq ........ src/TMV_LUDiv.cpp:46-55,186-226,232-242,370-411
  *   LUDiv::det / logDet .......... src/TMV_LUD.cpp:132-190
+ *   LU_Inverse ................... src/TMV_LUInverse.cpp:38-52,236-299
+ *   RecursiveInverse (upper tri) . src/TMV_TriInverse.cpp:49-88
+ *   LUDiv::makeInverseATA ........ src/TMV_LUD.cpp:172-200
+ *   LUDiv::isSingular ............ src/TMV_LUD.cpp:204-209,
+ *                                  src/TMV_Vector.cpp:539-600
  *
  * Built with -ffp-contract=off so that a*b+c is never fused, as in the
  * reference's x86 build.
@@ -852,6 +857,130 @@ void oracle_lu_det(ptrdiff_t n, const double* LU, ptrdiff_t lda,
     *logdet = ld;
     *sign = s;
     *det = s == 0.0 ? 0.0 : s * exp(ld);
+}
+
+/* ------------------------------------------------------------------ */
+/* Inverses                                                            */
+/* ------------------------------------------------------------------ */
+
+/* In-place inverse of the upper triangle of U (with unit, the diagonal is
+ * taken as 1 and neither read nor written).  src/TMV_TriInverse.cpp:49-88:
+ * split k = N/2, rounded down to a multiple of 64 above 64; invert U00 and
+ * U11; U01 = -U00 U01; U01 *= U11.  A zero U_jj is singular (TMV throws
+ * SingularUpperTriMatrix). */
+static int upper_invert(view U, int unit)
+{
+    const idx N = U.m;
+    if (N <= 0) return ORACLE_OK;
+    if (N == 1) {
+        if (!unit) {
+            if (AT(U, 0, 0) == 0.0) return ORACLE_SINGULAR;
+            AT(U, 0, 0) = 1.0 / AT(U, 0, 0);
+        }
+        return ORACLE_OK;
+    }
+    idx k = N / 2;
+    if (k > 64) k = k / 64 * 64;
+    view U00 = sub(U, 0, k, 0, k), U01 = sub(U, 0, k, k, N), U11 = sub(U, k, N, k, N);
+    int rc = upper_invert(U00, unit);
+    if (rc) return rc;
+    rc = upper_invert(U11, unit);
+    if (rc) return rc;
+    /* U01 = -U00 U01: row i of the result reads rows i.. of U01, so rows
+     * are produced top down in place */
+    for (idx j = 0; j < U01.n; ++j)
+        for (idx i = 0; i < k; ++i) {
+            double t = unit ? AT(U01, i, j) : AT(U00, i, i) * AT(U01, i, j);
+            for (idx l = i + 1; l < k; ++l) t += AT(U00, i, l) * AT(U01, l, j);
+            AT(U01, i, j) = -t;
+        }
+    /* U01 *= U11: column j of the result reads columns ..j, produced right
+     * to left in place */
+    for (idx i = 0; i < k; ++i)
+        for (idx j = U01.n - 1; j >= 0; --j) {
+            double t = unit ? AT(U01, i, j) : AT(U01, i, j) * AT(U11, j, j);
+            for (idx l = 0; l < j; ++l) t += AT(U01, i, l) * AT(U11, l, j);
+            AT(U01, i, j) = t;
+        }
+    return ORACLE_OK;
+}
+
+int oracle_lu_inverse(ptrdiff_t n, const double* LU, ptrdiff_t lda,
+                      const ptrdiff_t* P, double* M, ptrdiff_t ldm)
+{
+    /* src/TMV_LUInverse.cpp:38-52 (NonLapLUInverse) and 236-299
+     * (LU_Inverse): minv = LUx; U.invertSelf(); L.invertSelf();
+     * minv = U*L; minv.reversePermuteCols(P).  L.invertSelf() is the upper
+     * routine on the transposed view (include/tmv/TMV_TriMatrix.h:2674-2675). */
+    if (n <= 0) return ORACLE_OK;
+    view Mv = mkview(M, n, n, 1, ldm);
+    for (idx j = 0; j < n; ++j)
+        for (idx i = 0; i < n; ++i) AT(Mv, i, j) = LU[i + j * lda];
+    int rc = upper_invert(Mv, 0);
+    if (rc) return rc;
+    rc = upper_invert(transp(Mv), 1);
+    if (rc) return rc;
+    /* minv = U^-1 L^-1 (U upper with its diagonal, L unit lower) */
+    double* T = (double*)malloc(sizeof(double) * (size_t)(n * n));
+    if (!T) return ORACLE_NOMEM;
+    for (idx j = 0; j < n; ++j)
+        for (idx i = 0; i < n; ++i) {
+            const idx l0 = i > j ? i : j;
+            double t = l0 == j ? AT(Mv, i, j) : 0.0; /* U(i,j) * L(j,j) = U(i,j) */
+            for (idx l = l0 == j ? j + 1 : l0; l < n; ++l) t += AT(Mv, i, l) * AT(Mv, l, j);
+            T[i + j * n] = t;
+        }
+    for (idx j = 0; j < n; ++j)
+        for (idx i = 0; i < n; ++i) AT(Mv, i, j) = T[i + j * n];
+    free(T);
+    reverse_permute_rows(transp(Mv), P, 0, n);
+    return ORACLE_OK;
+}
+
+int oracle_lu_inverse_ata(ptrdiff_t n, const double* LU, ptrdiff_t lda,
+                          double* M, ptrdiff_t ldm)
+{
+    /* LUDiv::doMakeInverseATA, non-transposed case (src/TMV_LUD.cpp:172-200):
+     * linv = L.inverse(); ata = linv * linv^T; ata /= U; ata %= U^T.
+     * (A^T A)^-1 = U^-1 L^-1 L^-T U^-T: the permutation cancels. */
+    if (n <= 0) return ORACLE_OK;
+    view Mv = mkview(M, n, n, 1, ldm);
+    double* Li = (double*)malloc(sizeof(double) * (size_t)(n * n));
+    if (!Li) return ORACLE_NOMEM;
+    view Lv = mkview(Li, n, n, 1, n);
+    for (idx j = 0; j < n; ++j)
+        for (idx i = 0; i < n; ++i) AT(Lv, i, j) = i > j ? LU[i + j * lda] : (i == j ? 1.0 : 0.0);
+    int rc = upper_invert(transp(Lv), 1);
+    if (rc) { free(Li); return rc; }
+    /* ata = linv linv^T, linv unit lower */
+    for (idx j = 0; j < n; ++j)
+        for (idx i = 0; i < n; ++i) {
+            const idx lmax = i < j ? i : j;
+            double t = 0.0;
+            for (idx l = 0; l <= lmax; ++l) t += AT(Lv, i, l) * AT(Lv, j, l);
+            AT(Mv, i, j) = t;
+        }
+    free(Li);
+    tri U = {mkview((double*)LU, n, n, 1, lda), 1, 0};
+    rc = tri_ldiveq(U, Mv); /* ata /= U */
+    if (rc) return rc;
+    return tri_ldiveq(U, transp(Mv)); /* ata %= U^T: (ata^T) /= U */
+}
+
+int oracle_lu_is_singular(ptrdiff_t n, const double* LU, ptrdiff_t lda)
+{
+    /* src/TMV_LUD.cpp:204-209: diag.minAbs2Element() <=
+     * epsilon * diag.maxAbs2Element(), with Abs2 = |x| for a real and the
+     * first-extreme scans of src/TMV_Vector.cpp:539-600 (NaN never replaces
+     * the running value). */
+    if (n <= 0) return 0;
+    double mn = fabs(LU[0]), mx = mn;
+    for (idx j = 1; j < n; ++j) {
+        const double a = fabs(LU[j + j * lda]);
+        if (a > mx) mx = a;
+        if (a < mn) mn = a;
+    }
+    return mn <= DBL_EPSILON * mx;
 }
 
 int oracle_batched_divide(ptrdiff_t count, const ptrdiff_t* n,

@@ -65,6 +65,18 @@ void oracle_lu_det(ptrdiff_t n, const double* LU, ptrdiff_t lda,
                    const ptrdiff_t* P, double* det, double* logdet,
                    double* sign);
 
+/* LU_Inverse: M = A^-1 from the factors (U^-1 L^-1, columns reverse-
+ * permuted).  ORACLE_SINGULAR for a zero U_jj. */
+int oracle_lu_inverse(ptrdiff_t n, const double* LU, ptrdiff_t lda,
+                      const ptrdiff_t* P, double* M, ptrdiff_t ldm);
+
+/* LUDiv::makeInverseATA: M = (A^T A)^-1 from the factors. */
+int oracle_lu_inverse_ata(ptrdiff_t n, const double* LU, ptrdiff_t lda,
+                          double* M, ptrdiff_t ldm);
+
+/* LUDiv::isSingular: 1 when min |U_jj| <= epsilon * max |U_jj|. */
+int oracle_lu_is_singular(ptrdiff_t n, const double* LU, ptrdiff_t lda);
+
 /* Ragged batch of X_i = B_i / A_i (B_i overwritten), OpenMP over systems. */
 int oracle_batched_divide(ptrdiff_t count, const ptrdiff_t* n,
                           const ptrdiff_t* nrhs, const ptrdiff_t* a_off,

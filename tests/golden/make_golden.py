@@ -190,6 +190,31 @@ def batched_small(ref):
                         A=Abuf, B=Bbuf, X=X)
 
 
+def inverse(ref):
+    # m.inverse(), m.makeInverseATA(), m.isSingular() as TMV computes them
+    # (src/TMV_LUInverse.cpp:236-299, src/TMV_LUD.cpp:158-209): the 4x4
+    # known-answer matrix of tests/TMV_TestMatrixDiv.cpp:11-18, a seeded
+    # 96 x 96 system with 2*sqrt(n) on the diagonal, and a matrix whose U has
+    # an exact zero pivot (TMV throws SingularUpperTriMatrix: rc 1).
+    m4, _ = tmv_square4()
+    rng = np.random.default_rng(20240607)
+    n = 96
+    A = rng.standard_normal((n, n)) + 2.0 * np.sqrt(n) * np.eye(n)
+    S = np.asfortranarray(np.arange(36, dtype=np.float64).reshape(6, 6) % 7.0)
+    S[:, 3] = S[:, 1]  # rank deficient: an exact zero pivot in U
+    out = {}
+    for name, M in (("sq4", m4), ("r96", A), ("sing6", S)):
+        M = fortran(M)
+        rc, Minv, Mata, sing = ref.inverse_of(M)
+        out[name] = M
+        out[name + "_rc"] = np.array(rc)
+        out[name + "_singular"] = np.array(sing)
+        if rc == 0:
+            out[name + "_inv"] = Minv
+            out[name + "_ata"] = Mata
+    np.savez_compressed(HERE / "inverse.npz", **out)
+
+
 def main():
     if not oracle.ref_available():
         oracle.build_ref(str(REFERENCE))
@@ -201,6 +226,7 @@ def main():
     random_lu(ref)
     special(ref)
     batched_small(ref)
+    inverse(ref)
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

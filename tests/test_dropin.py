@@ -47,6 +47,7 @@ def test_double_entry_points_come_from_the_shim(dropin):
     lu = symbols(dropin / "shim_lu.o")
     assert "tmv::LU_Decompose<double>(tmv::MatrixView<double, 0>, long*)" in lu
     assert "tmv::LU_LDivEq<double, double>" in lu and "tmv::LU_RDivEq<double, double>" in lu
+    assert "tmv::LU_Inverse<double, double>" in lu
     # the shim reaches the GPU only through the C ABI
     undef = subprocess.run(["nm", "-u", str(dropin / "shim_multmm.o")], capture_output=True,
                            text=True).stdout
@@ -60,6 +61,7 @@ def test_tmv_cpu_code_kept_under_renamed_entry_points(dropin):
     lib = symbols(dropin / "libtmv_gb300_dropin.so")
     assert "tmv::TMVG_CPU_LU_Decompose<float>" in lib
     assert "tmv::TMVG_CPU_LU_LDivEq<std::complex<double>, double>" in lib
+    assert "tmv::TMVG_CPU_LU_Inverse<std::complex<double>, std::complex<double> >" in lib
 
 
 def test_unmodified_tmv_program_links_and_reports(dropin):

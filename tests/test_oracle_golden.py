@@ -139,3 +139,23 @@ def test_batched_small(orc):
     st = orc.batched_divide(g["n"], g["nrhs"], g["a_off"], g["b_off"], g["A"].copy(), X)
     assert not st.any()
     assert np.abs(X - g["X"]).max() <= 1e-13 * np.abs(g["X"]).max()
+
+
+def test_inverse_fixtures(orc):
+    # TMV's m.inverse(), makeInverseATA() and isSingular() (inverse.npz)
+    g = load("inverse.npz")
+    for name in ["sq4", "r96", "sing6"]:
+        M = np.asfortranarray(g[name])
+        LU = M.copy(order="F")
+        P = orc.lu_decompose(LU)
+        assert orc.lu_is_singular(LU) == bool(g[name + "_singular"]), name
+        if int(g[name + "_rc"]) == 0:
+            assert rel_frob(orc.lu_inverse(LU, P), g[name + "_inv"]) <= 1e-13, name
+            assert rel_frob(orc.lu_inverse_ata(LU), g[name + "_ata"]) <= 1e-13, name
+        else:
+            with pytest.raises(RuntimeError):
+                orc.lu_inverse(LU, P)
+    # the 4x4 known answer: det 28800 (tests/TMV_TestMatrixDiv.cpp:76), so
+    # A * A^-1 = I to rounding
+    m = g["sq4"]
+    assert np.abs(m @ g["sq4_inv"] - np.eye(4)).max() < 1e-14

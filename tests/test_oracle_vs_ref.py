@@ -84,3 +84,27 @@ def test_singular_solve_agrees(orc, ref):
         orc.divide(a, b)
     with pytest.raises(oracle.OracleSingular):
         ref.divide(a, b)
+
+
+def test_inverse_ata_singular_match_tmv(orc, ref):
+    # LU_Inverse, makeInverseATA and isSingular (src/TMV_LUInverse.cpp:236-299,
+    # src/TMV_LUD.cpp:172-209) restated against TMV's own results
+    rng = np.random.default_rng(17)
+    for n in [1, 3, 8, 64, 65, 129, 200]:
+        a = np.asfortranarray(rng.standard_normal((n, n)) + 2.0 * np.sqrt(n) * np.eye(n))
+        rc, inv_t, ata_t, sing_t = ref.inverse_of(a)
+        assert rc == 0
+        LU = a.copy(order="F")
+        P = orc.lu_decompose(LU)
+        assert np.linalg.norm(orc.lu_inverse(LU, P) - inv_t) <= 1e-13 * np.linalg.norm(inv_t), n
+        assert np.linalg.norm(orc.lu_inverse_ata(LU) - ata_t) <= 1e-13 * np.linalg.norm(ata_t), n
+        assert orc.lu_is_singular(LU) == sing_t
+    # a zero pivot: TMV throws SingularUpperTriMatrix, the oracle reports it
+    s = np.asfortranarray(np.arange(36, dtype=np.float64).reshape(6, 6) % 7.0)
+    s[:, 3] = s[:, 1]
+    rc, _, _, sing_t = ref.inverse_of(s)
+    LU = s.copy(order="F")
+    P = orc.lu_decompose(LU)
+    assert rc == 1 and sing_t and orc.lu_is_singular(LU)
+    with pytest.raises(RuntimeError):
+        orc.lu_inverse(LU, P)

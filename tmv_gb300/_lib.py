@@ -77,6 +77,10 @@ _SIGS = {
     "tmvg_divide_f64_host": (C.c_int, [vp, i64, vp, i64, vp, vp, vp, vp]),
     "tmvg_lu_det_f64": (C.c_int, [vp, i64, vp, i64, vp, C.POINTER(dbl), C.POINTER(dbl),
                                   C.POINTER(dbl)]),
+    "tmvg_lu_inverse_f64": (C.c_int, [vp, i64, vp, i64, vp, vp, i64]),
+    "tmvg_lu_inverse_f64_host": (C.c_int, [vp, i64, vp, i64, vp, vp, i64, i64]),
+    "tmvg_lu_inverse_ata_f64": (C.c_int, [vp, i64, vp, i64, vp, i64]),
+    "tmvg_lu_is_singular_f64": (C.c_int, [vp, i64, vp, i64, C.POINTER(C.c_int)]),
     "tmvg_lu_solve_mixed_f64": (C.c_int, [vp, i64, vp, i64, i64, vp, i64, vp, i64, C.c_int, dbl,
                                           C.POINTER(IRInfo)]),
     "tmvg_lu_solve_mixed_f64_host": (C.c_int, [vp, i64, vp, i64, vp, vp, C.c_int, dbl,

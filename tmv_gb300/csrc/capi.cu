@@ -3,6 +3,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <initializer_list>
+#include <limits>
 #include <new>
 #include <string>
 
@@ -668,6 +669,85 @@ tmvg_status tmvg_lu_det_f64(tmvg_handle h, int64_t n, const double* LU, int64_t 
     }
     cudaFreeHost(diag);
     cudaFreeHost(hp);
+    return st;
+}
+
+tmvg_status tmvg_lu_inverse_f64(tmvg_handle h, int64_t n, const double* LU, int64_t lda,
+                                const int64_t* P, double* Minv, int64_t ldm)
+{
+    CTX_OR_BAIL(h);
+    if (n < 0 || lda < std::max<int64_t>(n, 1) || ldm < std::max<int64_t>(n, 1))
+        return set_error(c, TMVG_BAD_ARG, "inverse: bad sizes");
+    return lu_inverse<double>(c, n, LU, lda, P, Minv, ldm);
+}
+
+tmvg_status tmvg_lu_inverse_f64_host(tmvg_handle h, int64_t n, const double* LU, int64_t lda,
+                                     const int64_t* P, double* Minv, int64_t msi, int64_t msj)
+{
+    // LUDiv::doMakeInverse -> LU_Inverse on host views (src/TMV_LUD.cpp:158-170)
+    CTX_OR_BAIL(h);
+    if (n < 0 || lda < std::max<int64_t>(n, 1)) return set_error(c, TMVG_BAD_ARG, "inverse: bad sizes");
+    if (n == 0) return TMVG_OK;
+    IoBufs io(c, {sizeof(double) * n * n, sizeof(int64_t) * n, sizeof(double) * n * n,
+                  sizeof(double) * n * n});
+    if (!io.ok) return set_error(c, TMVG_OOM, "inverse: device buffers");
+    DevBuf &dLU = io[0], &dP = io[1], &dM = io[2], &tmp = io[3];
+    tmvg_status st = check_cuda(
+        c,
+        cudaMemcpy2DAsync(dLU.p, n * sizeof(double), LU, lda * sizeof(double), n * sizeof(double), n,
+                          cudaMemcpyHostToDevice, c->stream),
+        "inverse: LU h2d");
+    if (!st)
+        st = check_cuda(c, cudaMemcpyAsync(dP.p, P, sizeof(int64_t) * n, cudaMemcpyHostToDevice, c->stream),
+                        "inverse: P h2d");
+    if (!st) st = lu_inverse<double>(c, n, dLU.as<double>(), n, dP.as<int64_t>(), dM.as<double>(), n);
+    if (!st) st = d2h_matrix(c, Minv, dM.as<double>(), n, n, msi, msj, tmp.as<double>());
+    if (!st) st = check_cuda(c, cudaStreamSynchronize(c->stream), "inverse sync");
+    return st;
+}
+
+tmvg_status tmvg_lu_inverse_ata_f64(tmvg_handle h, int64_t n, const double* LU, int64_t lda,
+                                    double* ATA, int64_t ldata)
+{
+    CTX_OR_BAIL(h);
+    if (n < 0 || lda < std::max<int64_t>(n, 1) || ldata < std::max<int64_t>(n, 1))
+        return set_error(c, TMVG_BAD_ARG, "inverse_ata: bad sizes");
+    return lu_inverse_ata<double>(c, n, LU, lda, ATA, ldata);
+}
+
+tmvg_status tmvg_lu_is_singular_f64(tmvg_handle h, int64_t n, const double* LU, int64_t lda,
+                                    int* singular)
+{
+    // LUDiv::isSingular (src/TMV_LUD.cpp:204-209): min |U_jj| <= epsilon *
+    // max |U_jj| (Abs2 of a real is |x|), scanned in order with strict
+    // comparisons as FindMin/MaxAbs2Element do (src/TMV_Vector.cpp:539-600),
+    // so a NaN never replaces the running extreme.  O(n): the diagonal is
+    // read back and reduced on the host.
+    CTX_OR_BAIL(h);
+    if (n < 0 || lda < std::max<int64_t>(n, 1) || !singular)
+        return set_error(c, TMVG_BAD_ARG, "is_singular: bad arguments");
+    *singular = 0;
+    if (n == 0) return TMVG_OK;
+    double* diag = nullptr;
+    if (cudaMallocHost(&diag, sizeof(double) * n) != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(c, TMVG_OOM, "is_singular: host buffer");
+    }
+    tmvg_status st = check_cuda(c,
+                                cudaMemcpy2DAsync(diag, sizeof(double), LU, (lda + 1) * sizeof(double),
+                                                  sizeof(double), n, cudaMemcpyDeviceToHost, c->stream),
+                                "is_singular: diag d2h");
+    if (!st) st = check_cuda(c, cudaStreamSynchronize(c->stream), "is_singular sync");
+    if (!st) {
+        double mn = std::fabs(diag[0]), mx = mn;
+        for (int64_t j = 1; j < n; ++j) {
+            const double a = std::fabs(diag[j]);
+            if (a > mx) mx = a;
+            if (a < mn) mn = a;
+        }
+        *singular = mn <= std::numeric_limits<double>::epsilon() * mx ? 1 : 0;
+    }
+    cudaFreeHost(diag);
     return st;
 }
 

@@ -1625,7 +1625,98 @@ tmvg_status lu_rdiveq(Context* c, int64_t n, const T* LU, int64_t lda, const int
     return collect_device_error(c, "lu_rdiveq");
 }
 
+// ---------------------------------------------------------------------
+// Inverse from the factors.
+// ---------------------------------------------------------------------
+template <typename T>
+__global__ void identity_kernel(int64_t n, T* __restrict__ M, int64_t ldm)
+{
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * n;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t % n, j = t / n;
+        M[i + j * ldm] = i == j ? T(1) : T(0);
+    }
+}
+
+// out[:, perm[j]] = in[:, j] (reversePermuteCols with perm from pivots_to_perm).
+template <typename T>
+__global__ void scatter_cols_kernel(int64_t n, const int* __restrict__ perm, const T* __restrict__ in,
+                                    int64_t ldi, T* __restrict__ out, int64_t ldo)
+{
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * n;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t % n, j = t / n;
+        out[i + (int64_t)perm[j] * ldo] = in[i + j * ldi];
+    }
+}
+
+// Y = U^-1 L^-1 into the dense n x n buffer Y (leading dimension n).
+// L^-1 is the unit-lower solve of the identity: column block c of L^-1 is
+// zero above row block c, so block step kb solves and updates only the
+// columns [0, kb + w) (n^3/3 flops); U^-1 (L^-1) is the dense upper solve
+// (n^3 flops).  A zero U(j,j) is reported as singular.
+template <typename T>
+static tmvg_status inverse_unpermuted(Context* c, int64_t n, const T* LU, int64_t lda, T* Y)
+{
+    const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(n * n, 256), 8 * c->num_sms);
+    identity_kernel<T><<<blocks, 256, 0, c->stream>>>(n, Y, n);
+    ++c->launches;
+    tmvg_status st = check_cuda(c, cudaGetLastError(), "inverse: identity launch");
+    for (int64_t kb = 0; kb < n && !st; kb += kTriBlock) {
+        const int w = (int)std::min<int64_t>(kTriBlock, n - kb);
+        const int64_t cols = kb + w;
+        st = launch_tri_diag<T>(c, w, LU + kb + kb * lda, 1, lda, false, true, cols, Y + kb, 1, n, false);
+        if (!st && kb + w < n)
+            st = gemm<T>(c, n - kb - w, cols, w, T(-1), Mat<const T>{LU + (kb + w) + kb * lda, 1, lda},
+                         Mat<const T>{Y + kb, 1, n}, T(1), Mat<T>{Y + kb + w, 1, n});
+    }
+    if (!st) st = tri_solve<T>(c, n, LU, 1, lda, true, false, n, Y, 1, n, false);
+    return st;
+}
+
+template <typename T>
+tmvg_status lu_inverse(Context* c, int64_t n, const T* LU, int64_t lda, const int64_t* P, T* M, int64_t ldm)
+{
+    // LU_Inverse (src/TMV_LUInverse.cpp:38-52, 236-299): A^-1 = U^-1 L^-1,
+    // then minv.reversePermuteCols(P), here one column scatter.
+    if (n <= 0) return TMVG_OK;
+    const size_t pbytes = (sizeof(int) * (size_t)n + 255) & ~size_t(255);
+    unsigned char* ws = (unsigned char*)workspace(c, pbytes + sizeof(T) * (size_t)n * n);
+    if (!ws) return TMVG_OOM;
+    int* perm = (int*)ws;
+    T* Y = (T*)(ws + pbytes);
+    tmvg_status st = inverse_unpermuted<T>(c, n, LU, lda, Y);
+    if (!st) st = pivots_to_perm(c, n, P, perm);
+    if (!st) {
+        const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(n * n, 256), 8 * c->num_sms);
+        scatter_cols_kernel<T><<<blocks, 256, 0, c->stream>>>(n, perm, Y, n, M, ldm);
+        ++c->launches;
+        st = check_cuda(c, cudaGetLastError(), "inverse: scatter launch");
+    }
+    if (st) return st;
+    return collect_device_error(c, "lu_inverse");
+}
+
+template <typename T>
+tmvg_status lu_inverse_ata(Context* c, int64_t n, const T* LU, int64_t lda, T* M, int64_t ldm)
+{
+    // LUDiv::doMakeInverseATA (src/TMV_LUD.cpp:172-200): (A^T A)^-1 =
+    // U^-1 L^-1 L^-T U^-T = Y Y^T with Y = U^-1 L^-1 (the permutation
+    // cancels); TMV forms the same product as linv*linv^T, /= U, %= U^T.
+    if (n <= 0) return TMVG_OK;
+    T* Y = (T*)workspace(c, sizeof(T) * (size_t)n * n);
+    if (!Y) return TMVG_OOM;
+    tmvg_status st = inverse_unpermuted<T>(c, n, LU, lda, Y);
+    if (!st)
+        st = gemm<T>(c, n, n, n, T(1), Mat<const T>{Y, 1, n}, Mat<const T>{Y, n, 1}, T(0), Mat<T>{M, 1, ldm});
+    if (st) return st;
+    return collect_device_error(c, "lu_inverse_ata");
+}
+
 template tmvg_status lu_factor<double>(Context*, int64_t, double*, int64_t, int64_t*);
+template tmvg_status lu_inverse<double>(Context*, int64_t, const double*, int64_t, const int64_t*, double*,
+                                        int64_t);
+template tmvg_status lu_inverse_ata<double>(Context*, int64_t, const double*, int64_t, double*, int64_t);
 template tmvg_status lu_factor<float>(Context*, int64_t, float*, int64_t, int64_t*);
 template tmvg_status tri_solve<double>(Context*, int64_t, const double*, int64_t, int64_t, bool,
                                        bool, int64_t, double*, int64_t, int64_t, bool);

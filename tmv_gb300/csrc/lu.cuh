@@ -37,4 +37,11 @@ template <typename T>
 tmvg_status lu_rdiveq(Context* c, int64_t n, const T* LU, int64_t lda, const int64_t* P,
                       int64_t nrows, T* B, int64_t bsi, int64_t bsj);
 
+// LU_Inverse: M = A^-1 from the factors (n x n, leading dimension ldm);
+// LUDiv::makeInverseATA: M = (A^T A)^-1.
+template <typename T>
+tmvg_status lu_inverse(Context* c, int64_t n, const T* LU, int64_t lda, const int64_t* P, T* M, int64_t ldm);
+template <typename T>
+tmvg_status lu_inverse_ata(Context* c, int64_t n, const T* LU, int64_t lda, T* M, int64_t ldm);
+
 }  // namespace tmvg

@@ -143,6 +143,42 @@ def lu_det(LU: torch.Tensor, P: torch.Tensor):
     return d.value, ld.value, s.value
 
 
+def lu_inverse(LU: torch.Tensor, P: torch.Tensor) -> torch.Tensor:
+    """A^-1 from stored factors, column-major (LU_Inverse, src/TMV_LUInverse.cpp:236-299)."""
+    _check_f64_cuda(LU)
+    n = LU.shape[0]
+    M = torch.empty((n, n), dtype=torch.float64, device=LU.device).t()
+    if n == 0:
+        return M
+    h = handle(LU.device.index)
+    h.check(h.call("tmvg_lu_inverse_f64", n, _ptr(LU), _ld(LU), _ptr(P), _ptr(M), _ld(M)),
+            "lu_inverse")
+    return M
+
+
+def lu_inverse_ata(LU: torch.Tensor) -> torch.Tensor:
+    """(A^T A)^-1 from stored factors (LUDiv::makeInverseATA, src/TMV_LUD.cpp:172-200)."""
+    _check_f64_cuda(LU)
+    n = LU.shape[0]
+    M = torch.empty((n, n), dtype=torch.float64, device=LU.device).t()
+    if n == 0:
+        return M
+    h = handle(LU.device.index)
+    h.check(h.call("tmvg_lu_inverse_ata_f64", n, _ptr(LU), _ld(LU), _ptr(M), _ld(M)),
+            "lu_inverse_ata")
+    return M
+
+
+def lu_is_singular(LU: torch.Tensor) -> bool:
+    """LUDiv::isSingular (src/TMV_LUD.cpp:204-209): min |U_jj| <= eps * max |U_jj|."""
+    _check_f64_cuda(LU)
+    s = C.c_int(0)
+    h = handle(LU.device.index)
+    h.check(h.call("tmvg_lu_is_singular_f64", LU.shape[0], _ptr(LU), _ld(LU), C.byref(s)),
+            "lu_is_singular")
+    return bool(s.value)
+
+
 def solve_mixed(A: torch.Tensor, B: torch.Tensor, max_iter: int = 10, tol: float = 1e-12,
                 X: torch.Tensor | None = None, raise_not_converged: bool = True):
     """X = A^-1 B by FP32 LU + FP64 iterative refinement (tmvg_lu_solve_mixed_f64).

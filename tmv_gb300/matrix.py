@@ -65,11 +65,15 @@ class LUDiv:
         return self._det[1], self._det[2]
 
     def isSingular(self) -> bool:
-        # src/TMV_LUD.cpp:204-209: min |U_jj|^2 <= eps * max |U_jj|^2
-        d2 = torch.diagonal(self.LU) ** 2
-        if d2.numel() == 0:
-            return False
-        return bool(d2.min() <= np.finfo(np.float64).eps * d2.max())
+        return linalg.lu_is_singular(self.LU)
+
+    def makeInverse(self) -> torch.Tensor:
+        """A^-1 (LUDiv::doMakeInverse, src/TMV_LUD.cpp:158-170)."""
+        return linalg.lu_inverse(self.LU, self.P)
+
+    def makeInverseATA(self) -> torch.Tensor:
+        """(A^T A)^-1 (LUDiv::doMakeInverseATA, src/TMV_LUD.cpp:172-200)."""
+        return linalg.lu_inverse_ata(self.LU)
 
     def ldiv(self, b: torch.Tensor) -> torch.Tensor:
         x = linalg.colmajor(b)
@@ -226,9 +230,16 @@ class Matrix:
         return r
 
     def inverse(self) -> "Matrix":
-        n = self.colsize()
-        eye = torch.eye(n, dtype=torch.float64, device=self.t.device)
-        return Matrix._wrap(eye) / self
+        self.setDiv()
+        r = Matrix._wrap(self._div.makeInverse())
+        self._done()
+        return r
+
+    def makeInverseATA(self) -> "Matrix":
+        self.setDiv()
+        r = Matrix._wrap(self._div.makeInverseATA())
+        self._done()
+        return r
 
     def norm(self) -> float:
         return float(torch.linalg.norm(self.t))

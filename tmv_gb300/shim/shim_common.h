@@ -5,7 +5,7 @@
 //
 // The drop-in is built by tmv_gb300/shim/Makefile from the TMV sources: every
 // TMV translation unit is compiled unchanged except TMV_MultMM.cpp,
-// TMV_LUDecompose.cpp and TMV_LUDiv.cpp, which are compiled with their entry
+// TMV_LUDecompose.cpp, TMV_LUDiv.cpp and TMV_LUInverse.cpp, which are compiled with their entry
 // points renamed to the TMVG_CPU_ names below; the shim translation units
 // then define the original entry points for exactly the instantiation lists
 // of TMV's .inst files.
@@ -30,6 +30,8 @@ template <typename T, typename T1>
 void TMVG_CPU_LU_LDivEq(const GenMatrix<T1>& LUx, const ptrdiff_t* P, MatrixView<T> m);
 template <typename T, typename T1>
 void TMVG_CPU_LU_RDivEq(const GenMatrix<T1>& LUx, const ptrdiff_t* P, MatrixView<T> m);
+template <typename T, typename T1>
+void TMVG_CPU_LU_Inverse(const GenMatrix<T1>& LUx, const ptrdiff_t* P, MatrixView<T> minv);
 
 namespace tmvg_shim {
 

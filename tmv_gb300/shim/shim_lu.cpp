@@ -1,6 +1,7 @@
 // shim_lu.cpp -- tmv::LU_Decompose (src/TMV_LUDecompose.cpp:514-559) and
-// tmv::LU_LDivEq / LU_RDivEq (src/TMV_LUDiv.cpp:186-226, 370-411) for every
-// instantiation of TMV_LUDecompose.inst and TMV_LUDiv.inst.  Square real
+// tmv::LU_LDivEq / LU_RDivEq (src/TMV_LUDiv.cpp:186-226, 370-411) and
+// tmv::LU_Inverse (src/TMV_LUInverse.cpp:236-299) for every instantiation of
+// TMV_LUDecompose.inst, TMV_LUDiv.inst and TMV_LUInverse.inst.  Square real
 // double problems go to the GPU; the other types (and rectangular
 // LU_Decompose, which LUDiv never asks for) run TMV's own CPU code.
 #include "TMV_LUDiv.h"
@@ -85,11 +86,45 @@ void LU_RDivEq(const GenMatrix<T1>& LUx, const ptrdiff_t* P, MatrixView<T> m)
         TMVG_CPU_LU_RDivEq(LUx, P, m);
 }
 
+static void gpu_lu_inverse(const GenMatrix<double>& LUx, const ptrdiff_t* P, MatrixView<double> minv)
+{
+    using namespace tmvg_shim;
+    if (!(LUx.iscm() && !LUx.isconj())) {
+        Matrix<double, ColMajor> LUc(LUx);
+        gpu_lu_inverse(LUc, P, minv);
+        return;
+    }
+    if (!dense_view(minv)) {
+        Matrix<double, ColMajor> mt(minv.colsize(), minv.rowsize());
+        gpu_lu_inverse(LUx, P, mt.view());
+        minv = mt;
+        return;
+    }
+    tmvg_status s = tmvg_lu_inverse_f64_host(gpu(), LUx.colsize(), LUx.cptr(), LUx.stepj(),
+                                             reinterpret_cast<const int64_t*>(P), minv.ptr(),
+                                             minv.stepi(), minv.stepj());
+    if (s == TMVG_SINGULAR) throw SingularUpperTriMatrix<double>(LUx.upperTri());
+    check(s, "tmv::LU_Inverse");
+}
+
+template <class T, class T1>
+void LU_Inverse(const GenMatrix<T1>& LUx, const ptrdiff_t* P, MatrixView<T> minv)
+{
+    if constexpr (std::is_same<T, double>::value && std::is_same<T1, double>::value)
+        gpu_lu_inverse(LUx, P, minv);
+    else
+        TMVG_CPU_LU_Inverse(LUx, P, minv);
+}
+
 #define InstFile "TMV_LUDecompose.inst"
 #include "TMV_Inst.h"
 #undef InstFile
 
 #define InstFile "TMV_LUDiv.inst"
+#include "TMV_Inst.h"
+#undef InstFile
+
+#define InstFile "TMV_LUInverse.inst"
 #include "TMV_Inst.h"
 #undef InstFile
 
