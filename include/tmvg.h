@@ -210,6 +210,32 @@ tmvg_status tmvg_lu_inverse_ata_f64(tmvg_handle h, int64_t n, const double* LU,
 tmvg_status tmvg_lu_is_singular_f64(tmvg_handle h, int64_t n, const double* LU,
                                     int64_t lda, int* singular);
 
+/* m /= T for a standalone triangle: B := T^-1 B, T the upper (upper = 1) or
+ * lower triangle at (T, tsi, tsj), unit diagonal not read when unitdiag; B
+ * n x nrhs with strides.  Replaces TriLDivEq<double,double> for
+ * UpperTriMatrix / LowerTriMatrix (src/TMV_TriDiv_M.cpp:583-710), reached
+ * through m /= U, x = b/U.  TMVG_SINGULAR as TMV throws SingularUpper/
+ * LowerTriMatrix (one column or a column-major B: a zero T(j,j) that divides
+ * a nonzero entry; otherwise any zero T(j,j)). */
+tmvg_status tmvg_tri_ldiveq_f64(tmvg_handle h, int upper, int unitdiag, int64_t n,
+                                const double* T, int64_t tsi, int64_t tsj,
+                                int64_t nrhs, double* B, int64_t bsi, int64_t bsj);
+
+/* m %= T: B := B T^-1 (B nrows x n), through T^T.LDivEq(m^T) as TMV does
+ * (include/tmv/TMV_TriMatrix.h:945-946). */
+tmvg_status tmvg_tri_rdiveq_f64(tmvg_handle h, int upper, int unitdiag, int64_t n,
+                                const double* T, int64_t tsi, int64_t tsj,
+                                int64_t nrows, double* B, int64_t bsi, int64_t bsj);
+
+/* y (+)= alpha A x: A m x n with strides, x (n) and y (m) with increments; x
+ * may share storage with y.  alpha = 0 or n = 0 leaves A unread.  Replaces
+ * MultMV<add,double,double,double> (src/TMV_MultMV.cpp:1134-1175), reached
+ * through y = A*x, y += alpha*A*x. */
+tmvg_status tmvg_multmv_f64(tmvg_handle h, int add, double alpha, int64_t m,
+                            int64_t n, const double* A, int64_t sAi, int64_t sAj,
+                            const double* x, int64_t incx, double* y,
+                            int64_t incy);
+
 /* ---- mixed-precision solve with FP64 iterative refinement ---------------
  * X = A^-1 B for a column-major FP64 A: the factorisation runs in FP32
  * (pivots chosen by comparing in FP64), then each column is refined with

@@ -195,6 +195,24 @@ class Port(_Backend):
         return bool(f(LU.shape[0], _p(LU), max(LU.shape[0], 1)))
 
 
+    def multmv(self, add: bool, alpha: float, A: np.ndarray, x: np.ndarray, y: np.ndarray) -> None:
+        """y (+)= alpha A x in place (MultMV<add>); A any strides, x and y 1-D."""
+        f = self._f("multmv", C.c_int, [C.c_int, dbl, i64, i64, vp, i64, i64, vp, i64, vp, i64])
+        rc = f(int(add), alpha, A.shape[0], A.shape[1], _p(A), *_strides(A), _p(x),
+               x.strides[0] // 8, _p(y), y.strides[0] // 8)
+        if rc:
+            raise RuntimeError(f"multmv rc={rc}")
+
+    def tri_ldiveq(self, upper: bool, unit: bool, T: np.ndarray, B: np.ndarray) -> int:
+        """B := T^-1 B in place for the upper or lower triangle of T (TriLDivEq);
+        returns the status (1: singular, as TMV throws)."""
+        f = self._f("tri_ldiveq", C.c_int, [C.c_int, C.c_int, i64, vp, i64, i64, vp, i64, i64])
+        if T.strides[0] != 8:
+            raise ValueError("the port's tri_ldiveq takes a column-major triangle")
+        return f(int(upper), int(unit), T.shape[0], _p(T), max(T.strides[1] // 8, 1), B.shape[1],
+                 _p(B), *_strides(B))
+
+
 class Ref(_Backend):
     prefix = "tmvref_"
 
@@ -219,6 +237,18 @@ class Ref(_Backend):
         if rc:
             raise RuntimeError(f"rdivide rc={rc}")
         return X
+
+    def multmv(self, add: bool, alpha: float, A: np.ndarray, x: np.ndarray, y: np.ndarray) -> None:
+        f = self._f("multmv", C.c_int, [C.c_int, dbl, i64, i64, vp, i64, i64, vp, i64, vp, i64])
+        rc = f(int(add), alpha, A.shape[0], A.shape[1], _p(A), *_strides(A), _p(x),
+               x.strides[0] // 8, _p(y), y.strides[0] // 8)
+        if rc:
+            raise RuntimeError(f"multmv rc={rc}")
+
+    def tri_ldiveq(self, upper: bool, unit: bool, T: np.ndarray, B: np.ndarray) -> int:
+        f = self._f("tri_ldiveq", C.c_int, [C.c_int, C.c_int, i64, vp, i64, i64, i64, vp, i64, i64])
+        return f(int(upper), int(unit), T.shape[0], _p(T), *_strides(T), B.shape[1], _p(B),
+                 *_strides(B))
 
     def inverse_of(self, A: np.ndarray):
         """TMV's own m.inverse(), m.makeInverseATA() and m.isSingular()."""

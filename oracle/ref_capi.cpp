@@ -165,6 +165,33 @@ int tmvref_det(ptrdiff_t n, const double* A, double* det, double* logdet,
     });
 }
 
+int tmvref_multmv(int add, double alpha, ptrdiff_t m, ptrdiff_t n, const double* A,
+                  ptrdiff_t sAi, ptrdiff_t sAj, const double* x, ptrdiff_t incx, double* y,
+                  ptrdiff_t incy)
+{
+    // y = alpha*A*x / y += alpha*A*x on views (MultMV<add>)
+    return guarded([&] {
+        tmv::ConstMatrixView<double> Av = tmv::MatrixViewOf(A, m, n, sAi, sAj);
+        tmv::ConstVectorView<double> xv = tmv::VectorViewOf(x, n, incx);
+        tmv::VectorView<double> yv = tmv::VectorViewOf(y, m, incy);
+        if (add) yv += alpha * Av * xv;
+        else yv = alpha * Av * xv;
+    });
+}
+
+int tmvref_tri_ldiveq(int upper, int unitdiag, ptrdiff_t n, const double* T, ptrdiff_t tsi,
+                      ptrdiff_t tsj, ptrdiff_t nrhs, double* B, ptrdiff_t bsi, ptrdiff_t bsj)
+{
+    // m /= U or m /= L (TriLDivEq) on views
+    return guarded([&] {
+        tmv::ConstMatrixView<double> Tv = tmv::MatrixViewOf(T, n, n, tsi, tsj);
+        tmv::MatrixView<double> Bv = tmv::MatrixViewOf(B, n, nrhs, bsi, bsj);
+        const tmv::DiagType dt = unitdiag ? tmv::UnitDiag : tmv::NonUnitDiag;
+        if (upper) Bv /= Tv.upperTri(dt);
+        else Bv /= Tv.lowerTri(dt);
+    });
+}
+
 int tmvref_inverse(ptrdiff_t n, const double* A, double* minv, double* ata, int* singular)
 {
     // m.inverse() (LUDiv::doMakeInverse -> LU_Inverse), m.makeInverseATA()

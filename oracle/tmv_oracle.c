@@ -27,6 +27,7 @@
  *   LU_Inverse ................... src/TMV_LUInverse.cpp:38-52,236-299
  *   RecursiveInverse (upper tri) . src/TMV_TriInverse.cpp:49-88
  *   LUDiv::makeInverseATA ........ src/TMV_LUD.cpp:172-200
+ *   MultMV ....................... src/TMV_MultMV.cpp:80-215,298-380,1134-1175
  *   LUDiv::isSingular ............ src/TMV_LUD.cpp:204-209,
  *                                  src/TMV_Vector.cpp:539-600
  *
@@ -981,6 +982,77 @@ int oracle_lu_is_singular(ptrdiff_t n, const double* LU, ptrdiff_t lda)
         if (a < mn) mn = a;
     }
     return mn <= DBL_EPSILON * mx;
+}
+
+/* ------------------------------------------------------------------ */
+/* Matrix-vector product                                               */
+/* ------------------------------------------------------------------ */
+
+/* UnitAMultMV1 (src/TMV_MultMV.cpp:186-215) with unit-step x and y: the row
+ * form (RowMultMV, :80-122) for a row-major A, the column form (ColMultMV,
+ * :124-184, which skips columns with x_j == 0) for a column-major one,
+ * otherwise the row form when N >= M. */
+static void unit_multmv(int add, view A, const double* x, double* y)
+{
+    const idx M = A.m, N = A.n;
+    const int row = isrm(A) ? 1 : iscm(A) ? 0 : (N >= M);
+    if (row) {
+        for (idx i = 0; i < M; ++i) {
+            double t = 0.0;
+            for (idx j = 0; j < N; ++j) t += x[j] * AT(A, i, j);
+            y[i] = add ? y[i] + t : t;
+        }
+        return;
+    }
+    idx j0 = 0;
+    if (!add) {
+        if (x[0] == 0.0)
+            for (idx i = 0; i < M; ++i) y[i] = 0.0;
+        else
+            for (idx i = 0; i < M; ++i) y[i] = x[0] * AT(A, i, 0);
+        j0 = 1;
+    }
+    for (idx j = j0; j < N; ++j)
+        if (x[j] != 0.0)
+            for (idx i = 0; i < M; ++i) y[i] += x[j] * AT(A, i, j);
+}
+
+int oracle_multmv(int add, double alpha, ptrdiff_t m, ptrdiff_t n, const double* A,
+                  ptrdiff_t sAi, ptrdiff_t sAj, const double* x, ptrdiff_t incx,
+                  double* y, ptrdiff_t incy)
+{
+    /* MultMV (src/TMV_MultMV.cpp:1134-1175): alpha == 0 or an empty x sets y
+     * to zero unless add.  NonBlasMultMV (:298-380): with a strided x, or
+     * alpha != 1 with M/4 >= N and unit-step y, x is scaled by alpha into a
+     * copy first; otherwise with alpha != 1 or a strided y the product goes
+     * to a temporary that is scaled into y; else straight into y. */
+    if (m <= 0) return ORACLE_OK;
+    if (n <= 0 || alpha == 0.0) {
+        if (!add)
+            for (idx i = 0; i < m; ++i) y[i * incy] = 0.0;
+        return ORACLE_OK;
+    }
+    view Av = mkview((double*)A, m, n, sAi, sAj);
+    double* xx = (double*)malloc(sizeof(double) * (size_t)n);
+    double* yy = (double*)malloc(sizeof(double) * (size_t)m);
+    if (!xx || !yy) { free(xx); free(yy); return ORACLE_NOMEM; }
+    if (incx != 1 || (alpha != 1.0 && incy == 1 && m / 4 >= n)) {
+        for (idx j = 0; j < n; ++j) xx[j] = alpha * x[j * incx];
+        if (incy != 1) {
+            unit_multmv(0, Av, xx, yy);
+            for (idx i = 0; i < m; ++i) y[i * incy] = add ? y[i * incy] + yy[i] : yy[i];
+        } else {
+            unit_multmv(add, Av, xx, y);
+        }
+    } else if (incy != 1 || alpha != 1.0) {
+        unit_multmv(0, Av, x, yy);
+        for (idx i = 0; i < m; ++i) y[i * incy] = add ? y[i * incy] + alpha * yy[i] : alpha * yy[i];
+    } else {
+        unit_multmv(add, Av, x, y);
+    }
+    free(xx);
+    free(yy);
+    return ORACLE_OK;
 }
 
 int oracle_batched_divide(ptrdiff_t count, const ptrdiff_t* n,

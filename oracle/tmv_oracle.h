@@ -77,6 +77,11 @@ int oracle_lu_inverse_ata(ptrdiff_t n, const double* LU, ptrdiff_t lda,
 /* LUDiv::isSingular: 1 when min |U_jj| <= epsilon * max |U_jj|. */
 int oracle_lu_is_singular(ptrdiff_t n, const double* LU, ptrdiff_t lda);
 
+/* MultMV<add>: y (+)= alpha A x (A m x n, strides; x, y increments). */
+int oracle_multmv(int add, double alpha, ptrdiff_t m, ptrdiff_t n, const double* A,
+                  ptrdiff_t sAi, ptrdiff_t sAj, const double* x, ptrdiff_t incx,
+                  double* y, ptrdiff_t incy);
+
 /* Ragged batch of X_i = B_i / A_i (B_i overwritten), OpenMP over systems. */
 int oracle_batched_divide(ptrdiff_t count, const ptrdiff_t* n,
                           const ptrdiff_t* nrhs, const ptrdiff_t* a_off,

@@ -215,6 +215,44 @@ def inverse(ref):
     np.savez_compressed(HERE / "inverse.npz", **out)
 
 
+def multmv_tri(ref):
+    # MultMV<add> (src/TMV_MultMV.cpp:1134) and TriLDivEq (src/TMV_TriDiv_M.cpp:583)
+    # as TMV computes them, on the cases whose semantics a GPU must keep:
+    # a NaN in a column whose x_j is zero (the column form skips it, the row
+    # form does not), and a zero U(j,j) met by a zero entry (one column or a
+    # column-major block: skipped) or by a row-major block (TMV throws: rc 1).
+    rng = np.random.default_rng(20240612)
+    out = {}
+    a = rng.standard_normal((37, 23))
+    a[6, 5] = np.nan
+    x = rng.standard_normal(23)
+    x[5] = 0.0
+    y0 = rng.standard_normal(37)
+    out["mv_A"], out["mv_x"], out["mv_y0"] = a, x, y0
+    for lay in ("F", "C"):
+        A = np.asfortranarray(a) if lay == "F" else np.ascontiguousarray(a)
+        for add in (0, 1):
+            y = y0.copy()
+            ref.multmv(add, 0.5, A, x, y)
+            out[f"mv_{lay}_{add}"] = y
+    n = 9
+    U = np.triu(rng.standard_normal((n, n)) + 3.0 * np.eye(n))
+    U[4, 4] = 0.0
+    U[4, 5:] = 0.0
+    out["tri_U"] = U
+    b = rng.standard_normal((n, 3))
+    b[4, :] = 0.0
+    out["tri_b"] = b
+    for name, B in (("v", np.asfortranarray(b[:, :1])), ("F", np.asfortranarray(b)),
+                    ("C", np.ascontiguousarray(b))):
+        Bc = B.copy(order="K")
+        rc = ref.tri_ldiveq(True, False, np.asfortranarray(U), Bc)
+        out[f"tri_{name}_rc"] = np.array(rc)
+        if rc == 0:
+            out[f"tri_{name}"] = np.asfortranarray(Bc)
+    np.savez_compressed(HERE / "multmv_tri.npz", **out)
+
+
 def main():
     if not oracle.ref_available():
         oracle.build_ref(str(REFERENCE))
@@ -227,6 +265,7 @@ def main():
     special(ref)
     batched_small(ref)
     inverse(ref)
+    multmv_tri(ref)
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

@@ -159,3 +159,24 @@ def test_inverse_fixtures(orc):
     # A * A^-1 = I to rounding
     m = g["sq4"]
     assert np.abs(m @ g["sq4_inv"] - np.eye(4)).max() < 1e-14
+
+
+def test_multmv_tri_fixtures(orc):
+    # TMV's MultMV and TriLDivEq on their special cases (multmv_tri.npz)
+    g = load("multmv_tri.npz")
+    a, x, y0 = g["mv_A"], g["mv_x"], g["mv_y0"]
+    for lay, A in (("F", np.asfortranarray(a)), ("C", np.ascontiguousarray(a))):
+        for add in (0, 1):
+            y = y0.copy()
+            orc.multmv(bool(add), 0.5, A, x, y)
+            ref = g[f"mv_{lay}_{add}"]
+            assert np.array_equal(np.isnan(y), np.isnan(ref))
+            ok = ~np.isnan(ref)
+            assert np.abs(y[ok] - ref[ok]).max() <= 1e-14 * np.abs(ref[ok]).max()
+    U, b = np.asfortranarray(g["tri_U"]), g["tri_b"]
+    for name, B in (("v", np.asfortranarray(b[:, :1])), ("F", np.asfortranarray(b)),
+                    ("C", np.ascontiguousarray(b))):
+        rc = orc.tri_ldiveq(True, False, U, B)
+        assert rc == int(g[f"tri_{name}_rc"]), name
+        if rc == 0:
+            assert rel_frob(B, g[f"tri_{name}"]) <= 1e-14

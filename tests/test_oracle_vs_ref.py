@@ -108,3 +108,31 @@ def test_inverse_ata_singular_match_tmv(orc, ref):
     assert rc == 1 and sing_t and orc.lu_is_singular(LU)
     with pytest.raises(RuntimeError):
         orc.lu_inverse(LU, P)
+
+
+def test_multmv_and_tri_ldiveq_match_tmv(orc, ref):
+    # MultMV<add> (src/TMV_MultMV.cpp:1134) over TMV's layouts and alpha/add
+    # branches; TriLDivEq (src/TMV_TriDiv_M.cpp:583) for both triangles
+    rng = np.random.default_rng(23)
+    for m, n in [(1, 1), (5, 3), (3, 5), (77, 40), (40, 77), (300, 301)]:
+        a = rng.standard_normal((m, n))
+        big = np.zeros((2 * m + 1, 3 * n + 2))
+        big[: 2 * m : 2, : 3 * n : 3] = a
+        for A in (np.asfortranarray(a), np.ascontiguousarray(a), big[: 2 * m : 2, : 3 * n : 3]):
+            x = rng.standard_normal(n)
+            y0 = rng.standard_normal(m)
+            for add in (False, True):
+                for alpha in (1.0, -0.75):
+                    y1, y2 = y0.copy(), y0.copy()
+                    orc.multmv(add, alpha, A, x, y1)
+                    ref.multmv(add, alpha, A, x, y2)
+                    assert np.abs(y1 - y2).max() <= 1e-14 * max(np.abs(y2).max(), 1.0)
+    for n in [1, 7, 64, 65, 200]:
+        T = np.asfortranarray(rng.standard_normal((n, n)) + 2.0 * np.sqrt(n) * np.eye(n))
+        for upper in (True, False):
+            for unit in (True, False):
+                for b in (rng.standard_normal((n, 1)), rng.standard_normal((n, 5))):
+                    for B1 in (np.array(b, order="F", copy=True), np.array(b, order="C", copy=True)):
+                        B2 = B1.copy(order="K")
+                        assert orc.tri_ldiveq(upper, unit, T, B1) == ref.tri_ldiveq(upper, unit, T, B2) == 0
+                        assert np.abs(B1 - B2).max() <= 1e-13 * max(np.abs(B2).max(), 1.0)

@@ -81,6 +81,9 @@ _SIGS = {
     "tmvg_lu_inverse_f64_host": (C.c_int, [vp, i64, vp, i64, vp, vp, i64, i64]),
     "tmvg_lu_inverse_ata_f64": (C.c_int, [vp, i64, vp, i64, vp, i64]),
     "tmvg_lu_is_singular_f64": (C.c_int, [vp, i64, vp, i64, C.POINTER(C.c_int)]),
+    "tmvg_tri_ldiveq_f64": (C.c_int, [vp, C.c_int, C.c_int, i64, vp, i64, i64, i64, vp, i64, i64]),
+    "tmvg_tri_rdiveq_f64": (C.c_int, [vp, C.c_int, C.c_int, i64, vp, i64, i64, i64, vp, i64, i64]),
+    "tmvg_multmv_f64": (C.c_int, [vp, C.c_int, dbl, i64, i64, vp, i64, i64, vp, i64, vp, i64]),
     "tmvg_lu_solve_mixed_f64": (C.c_int, [vp, i64, vp, i64, i64, vp, i64, vp, i64, C.c_int, dbl,
                                           C.POINTER(IRInfo)]),
     "tmvg_lu_solve_mixed_f64_host": (C.c_int, [vp, i64, vp, i64, vp, vp, C.c_int, dbl,

@@ -10,6 +10,7 @@
 #include "gemm_tc.cuh"
 #include "lu.cuh"
 #include "mixed.cuh"
+#include "multmv.cuh"
 #include "trsv.cuh"
 
 namespace tmvg {
@@ -749,6 +750,35 @@ tmvg_status tmvg_lu_is_singular_f64(tmvg_handle h, int64_t n, const double* LU, 
     }
     cudaFreeHost(diag);
     return st;
+}
+
+tmvg_status tmvg_tri_ldiveq_f64(tmvg_handle h, int upper, int unitdiag, int64_t n, const double* T,
+                                int64_t tsi, int64_t tsj, int64_t nrhs, double* B, int64_t bsi,
+                                int64_t bsj)
+{
+    CTX_OR_BAIL(h);
+    if (n < 0 || nrhs < 0) return set_error(c, TMVG_BAD_ARG, "tri_ldiveq: bad sizes");
+    return tri_ldiveq<double>(c, n, T, tsi, tsj, upper != 0, unitdiag != 0, nrhs, B, bsi, bsj);
+}
+
+tmvg_status tmvg_tri_rdiveq_f64(tmvg_handle h, int upper, int unitdiag, int64_t n, const double* T,
+                                int64_t tsi, int64_t tsj, int64_t nrows, double* B, int64_t bsi,
+                                int64_t bsj)
+{
+    // m %= T is T^T.LDivEq(m^T) (include/tmv/TMV_TriMatrix.h:945-946): the
+    // transposed triangle (upper <-> lower, strides swapped) divides m^T.
+    CTX_OR_BAIL(h);
+    if (n < 0 || nrows < 0) return set_error(c, TMVG_BAD_ARG, "tri_rdiveq: bad sizes");
+    return tri_ldiveq<double>(c, n, T, tsj, tsi, upper == 0, unitdiag != 0, nrows, B, bsj, bsi);
+}
+
+tmvg_status tmvg_multmv_f64(tmvg_handle h, int add, double alpha, int64_t m, int64_t n, const double* A,
+                            int64_t sAi, int64_t sAj, const double* x, int64_t incx, double* y,
+                            int64_t incy)
+{
+    CTX_OR_BAIL(h);
+    if (m < 0 || n < 0) return set_error(c, TMVG_BAD_ARG, "multmv: bad sizes");
+    return multmv(c, add != 0, alpha, m, n, A, sAi, sAj, x, incx, y, incy);
 }
 
 tmvg_status tmvg_lu_solve_mixed_f64(tmvg_handle h, int64_t n, const double* A, int64_t lda,

@@ -1568,6 +1568,22 @@ static tmvg_status tri_any(Context* c, int64_t n, const T* tri, int64_t tsi, int
     return tri_solve<T>(c, n, tri, tsi, tsj, upper, unit, nrhs, B, bsi, bsj, skip_zero);
 }
 
+// m /= T for a standalone triangle (TriLDivEq(GenUpper/LowerTriMatrix, MatrixView),
+// src/TMV_TriDiv_M.cpp:583-710): one right-hand side takes TMV's vector path
+// (a zero T(j,j) matters only where the entry it divides is nonzero), a
+// column-major B the same column-by-column rule of NonBlasTriLDivEq's
+// leaves; any other B treats every zero T(j,j) as singular.
+template <typename T>
+tmvg_status tri_ldiveq(Context* c, int64_t n, const T* tri, int64_t tsi, int64_t tsj, bool upper, bool unit,
+                       int64_t nrhs, T* B, int64_t bsi, int64_t bsj)
+{
+    if (n <= 0 || nrhs <= 0) return TMVG_OK;
+    const bool skip = nrhs == 1 || bsi == 1;
+    tmvg_status st = tri_any<T>(c, n, tri, tsi, tsj, upper, unit, nrhs, B, bsi, bsj, skip);
+    if (st) return st;
+    return collect_device_error(c, "tri_ldiveq");
+}
+
 template <typename T>
 tmvg_status lu_ldiveq(Context* c, int64_t n, const T* LU, int64_t lda, const int64_t* P,
                       int64_t nrhs, T* B, int64_t bsi, int64_t bsj)
@@ -1716,6 +1732,8 @@ tmvg_status lu_inverse_ata(Context* c, int64_t n, const T* LU, int64_t lda, T* M
 template tmvg_status lu_factor<double>(Context*, int64_t, double*, int64_t, int64_t*);
 template tmvg_status lu_inverse<double>(Context*, int64_t, const double*, int64_t, const int64_t*, double*,
                                         int64_t);
+template tmvg_status tri_ldiveq<double>(Context*, int64_t, const double*, int64_t, int64_t, bool, bool,
+                                        int64_t, double*, int64_t, int64_t);
 template tmvg_status lu_inverse_ata<double>(Context*, int64_t, const double*, int64_t, double*, int64_t);
 template tmvg_status lu_factor<float>(Context*, int64_t, float*, int64_t, int64_t*);
 template tmvg_status tri_solve<double>(Context*, int64_t, const double*, int64_t, int64_t, bool,

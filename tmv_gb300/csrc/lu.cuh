@@ -37,6 +37,11 @@ template <typename T>
 tmvg_status lu_rdiveq(Context* c, int64_t n, const T* LU, int64_t lda, const int64_t* P,
                       int64_t nrows, T* B, int64_t bsi, int64_t bsj);
 
+// m /= T for a standalone unit-lower / lower / upper triangle (TriLDivEq).
+template <typename T>
+tmvg_status tri_ldiveq(Context* c, int64_t n, const T* tri, int64_t tsi, int64_t tsj, bool upper, bool unit,
+                       int64_t nrhs, T* B, int64_t bsi, int64_t bsj);
+
 // LU_Inverse: M = A^-1 from the factors (n x n, leading dimension ldm);
 // LUDiv::makeInverseATA: M = (A^T A)^-1.
 template <typename T>

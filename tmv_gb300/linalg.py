@@ -143,6 +143,48 @@ def lu_det(LU: torch.Tensor, P: torch.Tensor):
     return d.value, ld.value, s.value
 
 
+def multmv(add: bool, alpha: float, A: torch.Tensor, x: torch.Tensor, y: torch.Tensor) -> None:
+    """y (+)= alpha A x in place (tmv::MultMV<add>, src/TMV_MultMV.cpp:1134-1175).
+
+    A is a 2-D float64 CUDA tensor with any strides, x and y 1-D (any
+    stride); x may be y itself."""
+    _check_f64_cuda(A, x, y)
+    m, n = A.shape
+    if x.dim() != 1 or y.dim() != 1 or x.shape[0] != n or y.shape[0] != m:
+        raise ValueError("multmv: size mismatch")
+    h = handle(A.device.index)
+    h.check(h.call("tmvg_multmv_f64", int(add), float(alpha), m, n, _ptr(A), A.stride(0), A.stride(1),
+                   _ptr(x), x.stride(0), _ptr(y), y.stride(0)), "multmv")
+
+
+def tri_ldiveq(T: torch.Tensor, upper: bool, unit: bool, B: torch.Tensor) -> None:
+    """B := T^-1 B in place for the upper or lower triangle of T (m /= U,
+    m /= L: TriLDivEq, src/TMV_TriDiv_M.cpp:583-710).  Raises SingularError
+    where TMV throws SingularUpper/LowerTriMatrix."""
+    _check_f64_cuda(T, B)
+    n = T.shape[0]
+    if B.dim() == 1:
+        B = B.view(-1, 1)
+    if T.shape[1] != n or B.shape[0] != n:
+        raise ValueError("tri_ldiveq: size mismatch")
+    h = handle(T.device.index)
+    h.check(h.call("tmvg_tri_ldiveq_f64", int(upper), int(unit), n, _ptr(T), T.stride(0), T.stride(1),
+                   B.shape[1], _ptr(B), B.stride(0), B.stride(1)), "tri_ldiveq")
+
+
+def tri_rdiveq(T: torch.Tensor, upper: bool, unit: bool, B: torch.Tensor) -> None:
+    """B := B T^-1 in place (m %= U, m %= L); B is nrows x n."""
+    _check_f64_cuda(T, B)
+    n = T.shape[0]
+    if B.dim() == 1:
+        B = B.view(1, -1)
+    if T.shape[1] != n or B.shape[1] != n:
+        raise ValueError("tri_rdiveq: size mismatch")
+    h = handle(T.device.index)
+    h.check(h.call("tmvg_tri_rdiveq_f64", int(upper), int(unit), n, _ptr(T), T.stride(0), T.stride(1),
+                   B.shape[0], _ptr(B), B.stride(0), B.stride(1)), "tri_rdiveq")
+
+
 def lu_inverse(LU: torch.Tensor, P: torch.Tensor) -> torch.Tensor:
     """A^-1 from stored factors, column-major (LU_Inverse, src/TMV_LUInverse.cpp:236-299)."""
     _check_f64_cuda(LU)

@@ -86,6 +86,26 @@ class LUDiv:
         return x
 
 
+UnitDiag = "UnitDiag"
+NonUnitDiag = "NonUnitDiag"
+
+
+class TriMatrixView:
+    """The upper or lower triangle of a Matrix (m.upperTri(dt), m.lowerTri(dt):
+    tmv::UpperTriMatrixView / LowerTriMatrixView).  `B / T` is T^-1 B and
+    `B % T` is B T^-1 (TriLDivEq, src/TMV_TriDiv_M.cpp:583-710)."""
+
+    def __init__(self, t: torch.Tensor, upper: bool, dt: str):
+        if dt not in (UnitDiag, NonUnitDiag):
+            raise ValueError("dt must be UnitDiag or NonUnitDiag")
+        self.t = t
+        self.upper = upper
+        self.unit = dt == UnitDiag
+
+    def size(self) -> int:
+        return self.t.shape[0]
+
+
 class Matrix:
     """Column-major float64 matrix on a CUDA device (tmv::Matrix<double,ColMajor>)."""
 
@@ -119,10 +139,22 @@ class Matrix:
     def numpy(self) -> np.ndarray:
         return self.t.cpu().numpy()
 
+    def upperTri(self, dt: str = NonUnitDiag) -> TriMatrixView:
+        return TriMatrixView(self.t, True, dt)
+
+    def lowerTri(self, dt: str = NonUnitDiag) -> TriMatrixView:
+        return TriMatrixView(self.t, False, dt)
+
     # -- product -----------------------------------------------------------
     def __mul__(self, other):
         if isinstance(other, (int, float)):
             return Matrix(self.t * float(other))
+        if (isinstance(other, torch.Tensor) or isinstance(other, np.ndarray)) and other.ndim == 1:
+            # y = A x (MultMV<false>, src/TMV_MultMV.cpp:1134)
+            x = torch.as_tensor(other, dtype=torch.float64, device=self.t.device)
+            y = torch.empty(self.colsize(), dtype=torch.float64, device=self.t.device)
+            linalg.multmv(False, 1.0, self.t, x, y)
+            return y
         if not isinstance(other, Matrix):
             other = Matrix(other)
         m, k = self.shape
@@ -197,15 +229,24 @@ class Matrix:
         return Matrix._wrap(x)
 
     def __truediv__(self, other):
-        """self / other: for a Matrix `other`, X = other^-1 self (TMV's b/m)."""
+        """self / other: for a Matrix `other`, X = other^-1 self (TMV's b/m);
+        for a triangle, X = T^-1 self (TriLDivEq)."""
         if isinstance(other, (int, float)):
             return Matrix(self.t / float(other))
+        if isinstance(other, TriMatrixView):
+            x = linalg.colmajor(self.t)
+            linalg.tri_ldiveq(other.t, other.upper, other.unit, x)
+            return Matrix._wrap(x)
         if not isinstance(other, Matrix):
             other = Matrix(other)
         return other._ldiv(self)
 
     def __mod__(self, other):
-        """self % other: X = self other^-1 (TMV's b%m)."""
+        """self % other: X = self other^-1 (TMV's b%m); X = self T^-1 for a triangle."""
+        if isinstance(other, TriMatrixView):
+            x = linalg.colmajor(self.t)
+            linalg.tri_rdiveq(other.t, other.upper, other.unit, x)
+            return Matrix._wrap(x)
         if not isinstance(other, Matrix):
             other = Matrix(other)
         return other._rdiv(self)
