@@ -307,6 +307,23 @@ tmvg_status tmvg_batch_plan_set_tiles(tmvg_batch_plan plan, const int* panel_wid
 /* Device pointers; synchronous. */
 tmvg_status tmvg_batched_lu_solve_f64(tmvg_batch_plan plan, double* A, double* B,
                                       int64_t* P, int32_t* status);
+/* The same batch with FP32 factors and FP64 refinement (the systems the
+ * batched workload calls FP32-refined): per system, an FP32 copy of A is
+ * factored with pivots chosen by comparing in FP64 (P receives them), then
+ * x = 0 and, until every column's normwise backward error
+ * ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf) <= tol, r = b - A x in
+ * FP64, d = A^-1 r with the FP32 factors, x += d in FP64, at most max_iter
+ * corrections, all in the same persistent launch (a captured CUDA graph).  A
+ * and the right-hand sides are read, not modified; B receives X.
+ * status[s]: 0 converged, 1 a zero U(j,j) of the FP32 factors met a nonzero
+ * (TMV's SingularUpperTriMatrix), 2 not converged (B holds the last iterate).
+ * iters[s] (corrections applied) and berr[s] (worst column's backward error
+ * at exit) are optional.  TMV has no mixed-precision path; this is another
+ * engine for the same X_i = B_i / A_i (LUDiv::doLDiv, src/TMV_LUD.cpp:112-120). */
+tmvg_status tmvg_batched_lu_solve_mixed_f64(tmvg_batch_plan plan, const double* A,
+                                            double* B, int64_t* P, int32_t* status,
+                                            int max_iter, double tol,
+                                            int32_t* iters, double* berr);
 tmvg_status tmvg_batch_plan_destroy(tmvg_batch_plan plan);
 
 #if defined(__GNUC__)

@@ -96,6 +96,7 @@ _SIGS = {
                                        C.POINTER(dbl), C.POINTER(C.c_int)]),
     "tmvg_batch_plan_set_tiles": (C.c_int, [vp, C.POINTER(C.c_int)]),
     "tmvg_batched_lu_solve_f64": (C.c_int, [vp, vp, vp, vp, vp]),
+    "tmvg_batched_lu_solve_mixed_f64": (C.c_int, [vp, vp, vp, vp, vp, C.c_int, dbl, vp, vp]),
     "tmvg_batch_plan_destroy": (C.c_int, [vp]),
 }
 

@@ -4,6 +4,7 @@
     A, B = plan.alloc()                     # device buffers of the right size
     ... fill A (A_s column-major at plan.a_off[s]) and B ...
     P, status = plan.solve(A, B)            # one graph launch: X_s over B_s
+    P, status, iters, berr = plan.solve_mixed(A, B)   # FP32 factors + FP64 refinement
 
 Mirrors a loop of TMV's B_s / A_s (LUDiv<double>, src/TMV_LUD.cpp:74-120)
 over independent systems.
@@ -70,6 +71,26 @@ class BatchPlan:
             self.plan, C.c_void_p(A.data_ptr()), C.c_void_p(B.data_ptr()),
             C.c_void_p(P.data_ptr()), C.c_void_p(status.data_ptr())), "batched solve")
         return P, status
+
+    def solve_mixed(self, A: torch.Tensor, B: torch.Tensor, max_iter: int = 10, tol: float = 1e-12,
+                    P: torch.Tensor | None = None, status: torch.Tensor | None = None):
+        """X_s = A_s^-1 B_s with FP32 factors and FP64 refinement, one graph
+        launch (tmvg_batched_lu_solve_mixed_f64).  A is left unchanged; B
+        receives X.  Returns (P, status, iters, berr): status 0 converged, 1
+        singular FP32 factors, 2 not converged."""
+        dev = A.device
+        if P is None:
+            P = torch.empty(max(self.p_elems, 1), dtype=torch.int64, device=dev)
+        if status is None:
+            status = torch.empty(max(self.count, 1), dtype=torch.int32, device=dev)
+        iters = torch.empty(max(self.count, 1), dtype=torch.int32, device=dev)
+        berr = torch.empty(max(self.count, 1), dtype=torch.float64, device=dev)
+        self.h.set_stream(torch.cuda.current_stream(dev).cuda_stream)
+        self.h.check(self.h.lib.tmvg_batched_lu_solve_mixed_f64(
+            self.plan, C.c_void_p(A.data_ptr()), C.c_void_p(B.data_ptr()), C.c_void_p(P.data_ptr()),
+            C.c_void_p(status.data_ptr()), int(max_iter), float(tol), C.c_void_p(iters.data_ptr()),
+            C.c_void_p(berr.data_ptr())), "batched mixed solve")
+        return P, status, iters, berr
 
     def close(self) -> None:
         if getattr(self, "plan", None):

@@ -78,24 +78,40 @@ struct BatchDev {
     int* status;
     int64_t count;
     int pw[kNumClasses];
+    // mixed precision only: FP32 factors (at a_off), refinement limits and
+    // optional per-system outputs
+    float* As;
+    int max_iter;
+    double tol;
+    int* iters;
+    double* berr;
 };
 
-template <int PW>
-__device__ void factor_solve_one(int64_t n, int64_t r, double* __restrict__ A, double* __restrict__ B,
-                                 int64_t* __restrict__ P, int* __restrict__ status, double* smem)
+// FP32 factors stage U12 in shared memory for the trailing update (FP32 FMA
+// is fast enough that streaming U12 from L1/L2 bounds it); FP64 reads it back
+// from A (the FP64 FMA pipe is the bound there, and the smaller footprint
+// keeps four CTAs per SM).
+template <typename T>
+constexpr bool kStageU12 = sizeof(T) == 4;
+
+// The blocked LU of one system in place (A n x n column-major, element type
+// T), pivots to P; the interchanges are also applied to the r columns of B
+// (B may be null with r = 0).  Pivot keys compare in FP64 for either T.
+template <typename T, int PW>
+__device__ void factor_one(int64_t n, int64_t r, T* __restrict__ A, T* __restrict__ B,
+                           int64_t* __restrict__ P, T* smem)
 {
     constexpr int LDP = PW + 1;
-    double* pan = smem;  // [256][LDP]
+    T* pan = smem;  // [256][LDP]
+    T* u12s = smem + kBatchMaxN * LDP;  // FP32 only: U12 rows [PW][256]
     __shared__ double s_key[kBatchThreads / 32];
     __shared__ long long s_idx[kBatchThreads / 32];
     __shared__ double w_key;
     __shared__ long long w_idx;
     __shared__ int s_piv[PW];
     __shared__ int s_pairs[1 + 2 * kMaxPairs];
-    __shared__ int s_sing;
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) s_sing = 0;
     bool prev_uf = false;
 
     for (int64_t k0 = 0; k0 < n; k0 += PW) {
@@ -124,23 +140,23 @@ __device__ void factor_solve_one(int64_t n, int64_t r, double* __restrict__ A, d
             __syncthreads();
             const double wk = w_key;
             const int wi = (int)w_idx;
-            if (underflows<double>(wk)) {
+            if (underflows<T>(wk)) {
                 if (tid == 0) s_piv[j] = (int)(k0 + j);
-                for (int rr = j + tid; rr < m; rr += kBatchThreads) pan[rr * LDP + j] = 0.0;
+                for (int rr = j + tid; rr < m; rr += kBatchThreads) pan[rr * LDP + j] = T(0);
                 prev_uf = true;
             } else {
                 prev_uf = false;
                 if (tid == 0) s_piv[j] = (int)(k0 + wi);
                 if (wi != j && tid < w) {
-                    const double t = pan[j * LDP + tid];
+                    const T t = pan[j * LDP + tid];
                     pan[j * LDP + tid] = pan[wi * LDP + tid];
                     pan[wi * LDP + tid] = t;
                 }
                 __syncthreads();
-                const double inv = 1.0 / pan[j * LDP + j];
+                const T inv = T(1) / pan[j * LDP + j];
                 for (int rr = j + 1 + tid; rr < m; rr += kBatchThreads) {
-                    double* row = pan + rr * LDP;
-                    const double l = row[j] * inv;
+                    T* row = pan + rr * LDP;
+                    const T l = row[j] * inv;
                     row[j] = l;
                     for (int cc = j + 1; cc < w; ++cc) row[cc] -= l * pan[j * LDP + cc];
                 }
@@ -164,8 +180,8 @@ __device__ void factor_solve_one(int64_t n, int64_t r, double* __restrict__ A, d
             static_assert(2 * PW <= 32, "one lane per row pair");
             for (int64_t col = warp; col < n + r; col += kBatchThreads / 32) {
                 if (col >= k0 && col < k0 + w) continue;
-                double* p = col < n ? A + col * n : B + (col - n) * n;
-                double v = 0.0;
+                T* p = col < n ? A + col * n : B + (col - n) * n;
+                T v = T(0);
                 if (lane < np) v = p[src[lane]];
                 __syncwarp();
                 if (lane < np) p[dst[lane]] = v;
@@ -177,10 +193,10 @@ __device__ void factor_solve_one(int64_t n, int64_t r, double* __restrict__ A, d
             // U12 = L11^-1 A12, one column per thread in registers, written
             // back in place (the update below reads it from A12)
             for (int c = tid; c < ncol; c += kBatchThreads) {
-                double* colp = A + k0 + (k0 + w + c) * n;
-                double x[PW];
+                T* colp = A + k0 + (k0 + w + c) * n;
+                T x[PW];
 #pragma unroll
-                for (int kk = 0; kk < PW; ++kk) x[kk] = kk < w ? colp[kk] : 0.0;
+                for (int kk = 0; kk < PW; ++kk) x[kk] = kk < w ? colp[kk] : T(0);
 #pragma unroll
                 for (int kk = 1; kk < PW; ++kk) {
 #pragma unroll
@@ -190,6 +206,13 @@ __device__ void factor_solve_one(int64_t n, int64_t r, double* __restrict__ A, d
 #pragma unroll
                 for (int kk = 0; kk < PW; ++kk)
                     if (kk < w) colp[kk] = x[kk];
+                if constexpr (kStageU12<T>) {
+                    // FP32: U12 also staged in shared memory (row kk at
+                    // u12s[kk * kBatchMaxN]), the update below reads it there
+#pragma unroll
+                    for (int kk = 0; kk < PW; ++kk)
+                        if (kk < w) u12s[kk * kBatchMaxN + c] = x[kk];
+                }
             }
             __syncthreads();
             // A22 -= L21 U12: 4x4 tiles, a tile's rows strided by ti so that
@@ -198,21 +221,26 @@ __device__ void factor_solve_one(int64_t n, int64_t r, double* __restrict__ A, d
             const int ti = (m2 + 3) / 4, tj = (ncol + 3) / 4;
             for (int t = tid; t < ti * tj; t += kBatchThreads) {
                 const int iq = t % ti, j0 = (t / ti) * 4;
-                double acc[4][4];
+                T acc[4][4];
 #pragma unroll
                 for (int a = 0; a < 4; ++a)
 #pragma unroll
-                    for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
-                const double* u = A + k0 + (k0 + w + j0) * n;
+                    for (int b = 0; b < 4; ++b) acc[a][b] = T(0);
+                const T* u = A + k0 + (k0 + w + j0) * n;
                 for (int kk = 0; kk < w; ++kk) {
-                    double av[4], bv[4];
+                    T av[4], bv[4];
 #pragma unroll
                     for (int a = 0; a < 4; ++a) {
                         const int ra = iq + a * ti;
-                        av[a] = ra < m2 ? pan[(w + ra) * LDP + kk] : 0.0;
+                        av[a] = ra < m2 ? pan[(w + ra) * LDP + kk] : T(0);
                     }
+                    if constexpr (kStageU12<T>) {
 #pragma unroll
-                    for (int b = 0; b < 4; ++b) bv[b] = (j0 + b < ncol) ? u[kk + b * n] : 0.0;
+                        for (int b = 0; b < 4; ++b) bv[b] = (j0 + b < ncol) ? u12s[kk * kBatchMaxN + j0 + b] : T(0);
+                    } else {
+#pragma unroll
+                        for (int b = 0; b < 4; ++b) bv[b] = (j0 + b < ncol) ? u[kk + b * n] : T(0);
+                    }
 #pragma unroll
                     for (int a = 0; a < 4; ++a)
 #pragma unroll
@@ -221,7 +249,7 @@ __device__ void factor_solve_one(int64_t n, int64_t r, double* __restrict__ A, d
 #pragma unroll
                 for (int b = 0; b < 4; ++b) {
                     if (j0 + b >= ncol) continue;
-                    double* cp = A + (k0 + w) + (k0 + w + j0 + b) * n;
+                    T* cp = A + (k0 + w) + (k0 + w + j0 + b) * n;
 #pragma unroll
                     for (int a = 0; a < 4; ++a) {
                         const int ra = iq + a * ti;
@@ -232,38 +260,35 @@ __device__ void factor_solve_one(int64_t n, int64_t r, double* __restrict__ A, d
         }
         __syncthreads();
     }
+}
 
-    // Solve: B holds P B; L (unit) then U, with the arithmetic and zero
-    // skipping of TMV's column-oriented vector solve (src/TMV_TriDiv_V.cpp:
-    // 148-236, 322-398), blocked by kSolveBlock columns: one warp solves the
-    // diagonal block (staged in shared memory, a lane per right-hand side),
-    // then every thread updates its (row, rhs) entries below (or above) the
-    // block over the block's columns in TMV's order, streaming the factor
-    // from global memory.  Each entry receives the same subtractions in the
-    // same order as the column-by-column loop.
-    if (r > 0) {
-        constexpr int XS = kBatchMaxN + 1;                  // padded rhs stride
-        double* xs = smem;                                   // [kBatchMaxRhs][XS]
-        double* dg = smem + kBatchMaxRhs * XS;               // [kSolveBlock][kSolveBlock + 1]
-        constexpr int DS = kSolveBlock + 1;
-        for (int t = tid; t < n * r; t += kBatchThreads) {
-            const int i = t % n, q = t / n;
-            xs[q * XS + i] = B[i + q * n];
-        }
-        __syncthreads();
+// x := U^-1 L^-1 x for the r right-hand sides staged in shared memory (xs,
+// stride XS) with the LU factors of one system (LU, n x n column-major), in
+// the arithmetic and zero skipping of TMV's column-oriented vector solve
+// (src/TMV_TriDiv_V.cpp:148-236, 322-398), blocked by kSolveBlock columns:
+// one warp solves the diagonal block (staged in dg, a lane per right-hand
+// side), then every thread updates its (row, rhs) entries below (or above)
+// the block over the block's columns in TMV's order, streaming the factor
+// from global memory.  A zero U(j,j) that divides a nonzero sets *sing.
+template <typename T>
+__device__ void lu_solve_staged(int64_t n, int64_t r, const T* __restrict__ LU, T* xs, int XS, T* dg,
+                                int* sing)
+{
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int DS = kSolveBlock + 1;
         // forward: unit lower L
         for (int j0 = 0; j0 < n; j0 += kSolveBlock) {
             const int jb = (int)min((int64_t)kSolveBlock, n - j0);
             for (int t = tid; t < jb * jb; t += kBatchThreads) {
                 const int i = t % jb, k = t / jb;
-                dg[i * DS + k] = A[(j0 + i) + (int64_t)(j0 + k) * n];
+                dg[i * DS + k] = LU[(j0 + i) + (int64_t)(j0 + k) * n];
             }
             __syncthreads();
             if (warp == 0 && lane < r) {
-                double* xq = xs + lane * XS + j0;
+                T* xq = xs + lane * XS + j0;
                 for (int k = 0; k < jb; ++k) {
-                    const double xk = xq[k];
-                    if (xk != 0.0)
+                    const T xk = xq[k];
+                    if (xk != T(0))
                         for (int i = k + 1; i < jb; ++i) xq[i] -= dg[i * DS + k] * xk;
                 }
             }
@@ -271,12 +296,12 @@ __device__ void factor_solve_one(int64_t n, int64_t r, double* __restrict__ A, d
             const int below = (int)(n - j0 - jb);
             for (int t = tid; t < below * r; t += kBatchThreads) {
                 const int i = j0 + jb + t % below, q = t / below;
-                const double* xq = xs + q * XS + j0;
-                const double* lc = A + i + (int64_t)j0 * n;
-                double v = xs[q * XS + i];
+                const T* xq = xs + q * XS + j0;
+                const T* lc = LU + i + (int64_t)j0 * n;
+                T v = xs[q * XS + i];
                 for (int k = 0; k < jb; ++k) {
-                    const double xk = xq[k];
-                    if (xk != 0.0) v -= lc[(int64_t)k * n] * xk;
+                    const T xk = xq[k];
+                    if (xk != T(0)) v -= lc[(int64_t)k * n] * xk;
                 }
                 xs[q * XS + i] = v;
             }
@@ -287,36 +312,58 @@ __device__ void factor_solve_one(int64_t n, int64_t r, double* __restrict__ A, d
             const int j0 = max(0, j1 - kSolveBlock), jb = j1 - j0;
             for (int t = tid; t < jb * jb; t += kBatchThreads) {
                 const int i = t % jb, k = t / jb;
-                dg[i * DS + k] = A[(j0 + i) + (int64_t)(j0 + k) * n];
+                dg[i * DS + k] = LU[(j0 + i) + (int64_t)(j0 + k) * n];
             }
             __syncthreads();
             if (warp == 0 && lane < r) {
-                double* xq = xs + lane * XS + j0;
+                T* xq = xs + lane * XS + j0;
                 for (int k = jb - 1; k >= 0; --k) {
-                    double v = xq[k];
-                    if (v != 0.0) {
-                        const double d = dg[k * DS + k];
-                        if (d == 0.0) s_sing = 1;
+                    T v = xq[k];
+                    if (v != T(0)) {
+                        const T d = dg[k * DS + k];
+                        if (d == T(0)) *sing = 1;
                         else xq[k] = v = v / d;
                     }
-                    if (v != 0.0)
+                    if (v != T(0))
                         for (int i = 0; i < k; ++i) xq[i] -= dg[i * DS + k] * v;
                 }
             }
             __syncthreads();
             for (int t = tid; t < j0 * r; t += kBatchThreads) {
                 const int i = t % j0, q = t / j0;
-                const double* xq = xs + q * XS + j0;
-                const double* uc = A + i + (int64_t)j0 * n;
-                double v = xs[q * XS + i];
+                const T* xq = xs + q * XS + j0;
+                const T* uc = LU + i + (int64_t)j0 * n;
+                T v = xs[q * XS + i];
                 for (int k = jb - 1; k >= 0; --k) {
-                    const double xk = xq[k];
-                    if (xk != 0.0) v -= uc[(int64_t)k * n] * xk;
+                    const T xk = xq[k];
+                    if (xk != T(0)) v -= uc[(int64_t)k * n] * xk;
                 }
                 xs[q * XS + i] = v;
             }
             __syncthreads();
         }
+}
+
+template <int PW>
+__device__ void factor_solve_one(int64_t n, int64_t r, double* __restrict__ A, double* __restrict__ B,
+                                 int64_t* __restrict__ P, int* __restrict__ status, double* smem)
+{
+    __shared__ int s_sing;
+    const int tid = threadIdx.x;
+    if (tid == 0) s_sing = 0;
+    factor_one<double, PW>(n, r, A, B, P, smem);
+
+    // Solve: B holds P B; L (unit) then U (lu_solve_staged)
+    if (r > 0) {
+        constexpr int XS = kBatchMaxN + 1;                  // padded rhs stride
+        double* xs = smem;                                   // [kBatchMaxRhs][XS]
+        double* dg = smem + kBatchMaxRhs * XS;               // [kSolveBlock][kSolveBlock + 1]
+        for (int t = tid; t < n * r; t += kBatchThreads) {
+            const int i = t % n, q = t / n;
+            xs[q * XS + i] = B[i + q * n];
+        }
+        __syncthreads();
+        lu_solve_staged<double>(n, r, A, xs, XS, dg, &s_sing);
         for (int t = tid; t < n * r; t += kBatchThreads) {
             const int i = t % n, q = t / n;
             B[i + q * n] = xs[q * XS + i];
@@ -351,6 +398,212 @@ batched_lu_kernel(const BatchDev* __restrict__ args, unsigned* queue)
 }
 
 // ---------------------------------------------------------------------
+// Mixed precision: FP32 factors, FP64 refinement, one persistent launch.
+//
+// Per system: As = (float) A together with ||A||_inf (TMV's norm: the
+// largest row sum of |a_ij|); the blocked LU of As (factor_one<float>, pivot
+// keys compared in FP64); then x = 0 and, until every column's normwise
+// backward error ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf) <= tol:
+// r = b - A x accumulated in FP64 (A, b and x in FP64), stored as FP32 in the
+// pivoted order, d = U^-1 L^-1 r in FP32 (lu_solve_staged<float>), x += d in
+// FP64.  A and b are not modified; x goes to B at the end.  status: 0
+// converged, 1 a zero U(j,j) of the FP32 factors met a nonzero, 2 not
+// converged within max_iter corrections (B holds the last iterate).
+// ---------------------------------------------------------------------
+__device__ __forceinline__ void smem_max_abs(unsigned long long* slot, double v)
+{
+    // non-negative doubles order like their bit patterns; a NaN is kept as NaN
+    const double a = fabs(v);
+    atomicMax(slot, (unsigned long long)__double_as_longlong(a != a ? __longlong_as_double(0x7ff8000000000000LL) : a));
+}
+
+// max(|a|, |b|) with a NaN kept
+__device__ __forceinline__ double nan_max_abs(double a, double b)
+{
+    const double x = fabs(a), y = fabs(b);
+    return (x != x || y != y) ? __longlong_as_double(0x7ff8000000000000LL) : fmax(x, y);
+}
+
+template <int PW>
+__device__ void mixed_one(const BatchDev& d, int s, unsigned char* smem_raw)
+{
+    constexpr int XS = kBatchMaxN + 1;
+    constexpr int RPT = kBatchMaxN / kBatchThreads;  // rows per thread in the residual
+    static_assert(RPT == 2, "the residual loop handles two row blocks");
+    __shared__ unsigned long long s_anorm;
+    __shared__ unsigned long long s_bn[kBatchMaxRhs], s_rn[kBatchMaxRhs], s_xn[kBatchMaxRhs];
+    __shared__ int s_inv[kBatchMaxN];  // row i of r goes to position s_inv[i] of P r
+    __shared__ int s_sing, s_done;
+
+    const int tid = threadIdx.x;
+    const int64_t n = d.n[s], r = d.nrhs[s];
+    const double* __restrict__ A = d.A + d.a_off[s];
+    double* __restrict__ B = d.B + d.b_off[s];
+    float* __restrict__ As = d.As + d.a_off[s];
+    int64_t* __restrict__ P = d.P + d.p_off[s];
+
+    // 1. FP32 copy and ||A||_inf
+    if (tid == 0) { s_anorm = 0ull; s_sing = 0; s_done = 0; }
+    __syncthreads();
+    for (int i = tid; i < n; i += kBatchThreads) {
+        double rs = 0.0;
+        for (int64_t j = 0; j < n; ++j) {
+            const double v = A[i + j * n];
+            As[i + j * n] = (float)v;
+            rs += fabs(v);
+        }
+        smem_max_abs(&s_anorm, rs);
+    }
+    __syncthreads();
+    // 2. FP32 factorisation (interchanges on As only: b stays in place)
+    factor_one<float, PW>(n, 0, As, nullptr, P, reinterpret_cast<float*>(smem_raw));
+    __syncthreads();
+    // the gather of P r: apply the interchanges to the identity, invert
+    if (tid == 0) {
+        for (int i = 0; i < n; ++i) s_inv[i] = i;  // s_inv used as perm first
+        for (int k = 0; k < n; ++k) {
+            const int p = (int)P[k];
+            const int t = s_inv[k];
+            s_inv[k] = s_inv[p];
+            s_inv[p] = t;
+        }
+    }
+    __syncthreads();
+    int perm_of[RPT];
+#pragma unroll
+    for (int u = 0; u < RPT; ++u) perm_of[u] = tid + u * kBatchThreads < n ? s_inv[tid + u * kBatchThreads] : 0;
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < RPT; ++u)
+        if (tid + u * kBatchThreads < n) s_inv[perm_of[u]] = tid + u * kBatchThreads;
+    __syncthreads();
+
+    double* xs = reinterpret_cast<double*>(smem_raw);          // x: [kBatchMaxRhs][XS] FP64
+    float* ds = reinterpret_cast<float*>(xs + kBatchMaxRhs * XS);  // r, then d: [kBatchMaxRhs][XS] FP32
+    float* dg = ds + kBatchMaxRhs * XS;                          // [kSolveBlock][kSolveBlock + 1]
+    for (int t = tid; t < kBatchMaxRhs * XS; t += kBatchThreads) xs[t] = 0.0;
+    if (tid < kBatchMaxRhs) s_bn[tid] = 0ull;
+    __syncthreads();
+    for (int t = tid; t < n * r; t += kBatchThreads) smem_max_abs(&s_bn[t / n], B[t % n + (t / n) * n]);
+    const double anorm = __longlong_as_double((long long)s_anorm);
+    int it = 0;
+    for (;; ++it) {
+        if (tid < kBatchMaxRhs) { s_rn[tid] = 0ull; s_xn[tid] = 0ull; }
+        __syncthreads();
+        // r = b - A x (FP64), into ds in the pivoted order, and its norms
+        double acc[RPT][kBatchMaxRhs];
+#pragma unroll
+        for (int u = 0; u < RPT; ++u)
+#pragma unroll
+            for (int q = 0; q < kBatchMaxRhs; ++q) {
+                const int i = tid + u * kBatchThreads;
+                acc[u][q] = (q < r && i < n) ? B[i + q * n] : 0.0;
+            }
+        // warps whose rows all lie beyond n skip their FMAs (FP64 issue is
+        // the bound here): the second row block only when n > 128
+        if (it > 0 && (tid & ~31) < n) {
+            const bool two = kBatchThreads + (tid & ~31) < n;
+            for (int64_t j = 0; j < n; ++j) {
+                const int i0 = tid, i1 = tid + kBatchThreads;
+                const double a0 = i0 < n ? __ldg(A + i0 + j * n) : 0.0;
+                if (two) {
+                    const double a1 = i1 < n ? __ldg(A + i1 + j * n) : 0.0;
+#pragma unroll
+                    for (int q = 0; q < kBatchMaxRhs; ++q) {
+                        if (q >= r) break;
+                        const double xq = xs[q * XS + j];
+                        acc[0][q] = fma(-a0, xq, acc[0][q]);
+                        acc[1][q] = fma(-a1, xq, acc[1][q]);
+                    }
+                } else {
+#pragma unroll
+                    for (int q = 0; q < kBatchMaxRhs; ++q) {
+                        if (q >= r) break;
+                        acc[0][q] = fma(-a0, xs[q * XS + j], acc[0][q]);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kBatchMaxRhs; ++q) {
+            if (q >= r) break;
+            double rm = 0.0, xm = 0.0;
+#pragma unroll
+            for (int u = 0; u < RPT; ++u) {
+                const int i = tid + u * kBatchThreads;
+                if (i >= n) continue;
+                ds[q * XS + s_inv[i]] = (float)acc[u][q];
+                rm = nan_max_abs(rm, acc[u][q]);
+                xm = nan_max_abs(xm, xs[q * XS + i]);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                rm = nan_max_abs(rm, __shfl_xor_sync(0xffffffffu, rm, o));
+                xm = nan_max_abs(xm, __shfl_xor_sync(0xffffffffu, xm, o));
+            }
+            if ((tid & 31) == 0) {
+                smem_max_abs(&s_rn[q], rm);
+                smem_max_abs(&s_xn[q], xm);
+            }
+        }
+        __syncthreads();
+        // every column's backward error
+        if (tid == 0) {
+            double worst = 0.0;
+            bool ok = true;
+            for (int q = 0; q < r; ++q) {
+                const double rn = __longlong_as_double((long long)s_rn[q]);
+                const double den = anorm * __longlong_as_double((long long)s_xn[q]) +
+                                   __longlong_as_double((long long)s_bn[q]);
+                const double be = den > 0.0 ? rn / den : (rn > 0.0 ? INFINITY : 0.0);
+                if (!(be <= d.tol)) ok = false;
+                if (!(be <= worst)) worst = be;  // NaN propagates
+            }
+            if (d.berr) d.berr[s] = worst;
+            s_done = (ok || s_sing || it >= d.max_iter) ? 1 : 0;
+            if (!ok && !s_sing && it >= d.max_iter) s_done = 2;
+        }
+        __syncthreads();
+        if (s_done) break;
+        // d = U^-1 L^-1 (P r) in FP32; x += d in FP64
+        lu_solve_staged<float>(n, r, As, ds, XS, dg, &s_sing);
+        __syncthreads();
+        for (int t = tid; t < n * r; t += kBatchThreads) {
+            const int i = t % n, q = t / n;
+            xs[q * XS + i] += (double)ds[q * XS + i];
+        }
+        __syncthreads();
+    }
+    for (int t = tid; t < n * r; t += kBatchThreads) {
+        const int i = t % n, q = t / n;
+        B[i + q * n] = xs[q * XS + i];
+    }
+    if (tid == 0) {
+        d.status[s] = s_sing ? 1 : (s_done == 2 ? 2 : 0);
+        if (d.iters) d.iters[s] = it;
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kBatchThreads, 4)
+batched_mixed_kernel(const BatchDev* __restrict__ args, unsigned* queue)
+{
+    extern __shared__ __align__(16) unsigned char bsmem_mixed[];
+    __shared__ int s_item;
+    const BatchDev& a = *args;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = (int)atomicAdd(queue, 1u);
+        __syncthreads();
+        const int item = s_item;
+        __syncthreads();
+        if (item >= a.count) return;
+        const int s = a.order[item];
+        if (a.pw[size_class(a.n[s])] == 8) mixed_one<8>(a, s, bsmem_mixed);
+        else mixed_one<16>(a, s, bsmem_mixed);
+    }
+}
+
+// ---------------------------------------------------------------------
 // Plan: descriptors on the device, processing order, tile choice, graph.
 // ---------------------------------------------------------------------
 struct BatchPlan {
@@ -367,6 +620,12 @@ struct BatchPlan {
     int pw[kNumClasses] = {16, 16, 16, 16};
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    // mixed precision: FP32 factors (a_elems floats), its own graph
+    float* d_As = nullptr;
+    cudaGraph_t graph_mixed = nullptr;
+    cudaGraphExec_t exec_mixed = nullptr;
+    int grid_mixed = 0;
+    size_t smem_mixed = 0;
     double flops = 0;
     std::vector<int64_t> hn, hr;
 };
@@ -414,9 +673,50 @@ static tmvg_status build_graph(BatchPlan* p)
     return check_cuda(c, cudaGraphInstantiate(&p->exec, p->graph, 0), "batched: instantiate");
 }
 
-static tmvg_status run_plan(BatchPlan* p, double* A, double* B, int64_t* P, int* status)
+// Shared memory of the mixed kernel: the FP32 panel, or the refinement's
+// FP64 iterate, FP32 correction and FP32 diagonal block.
+static size_t smem_mixed_bytes()
+{
+    const size_t panel = sizeof(float) * ((size_t)batch_smem_doubles(16) + 16 * kBatchMaxN);
+    const size_t refine = sizeof(double) * kBatchMaxRhs * (kBatchMaxN + 1) +
+                          sizeof(float) * (kBatchMaxRhs * (kBatchMaxN + 1) + kSolveBlock * (kSolveBlock + 1));
+    return std::max(panel, refine);
+}
+
+static tmvg_status build_graph_mixed(BatchPlan* p)
 {
     Context* c = p->c;
+    if (p->exec_mixed) { cudaGraphExecDestroy(p->exec_mixed); p->exec_mixed = nullptr; }
+    if (p->graph_mixed) { cudaGraphDestroy(p->graph_mixed); p->graph_mixed = nullptr; }
+    p->smem_mixed = smem_mixed_bytes();
+    tmvg_status st = check_cuda(
+        c, cudaFuncSetAttribute(batched_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)p->smem_mixed),
+        "batched mixed: smem attribute");
+    if (st) return st;
+    int per_sm = 0;
+    st = check_cuda(c,
+                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_mixed_kernel, kBatchThreads,
+                                                                  p->smem_mixed),
+                    "batched mixed: occupancy");
+    if (st) return st;
+    per_sm = std::max(per_sm, 1);
+    p->grid_mixed = (int)std::min<int64_t>((int64_t)per_sm * c->num_sms, std::max<int64_t>(p->count, 1));
+    cudaStream_t cap;
+    st = check_cuda(c, cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "batched mixed: stream");
+    if (st) return st;
+    cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    cudaMemsetAsync(p->d_queue, 0, sizeof(unsigned), cap);
+    batched_mixed_kernel<<<p->grid_mixed, kBatchThreads, p->smem_mixed, cap>>>(p->d_args, p->d_queue);
+    cudaError_t e = cudaStreamEndCapture(cap, &p->graph_mixed);
+    cudaStreamDestroy(cap);
+    st = check_cuda(c, e, "batched mixed: capture");
+    if (st) return st;
+    return check_cuda(c, cudaGraphInstantiate(&p->exec_mixed, p->graph_mixed, 0), "batched mixed: instantiate");
+}
+
+static void fill_args(BatchPlan* p, double* A, double* B, int64_t* P, int* status)
+{
     BatchDev& h = *p->h_args;
     h.n = p->d_desc;
     h.nrhs = p->d_desc + p->count;
@@ -430,6 +730,49 @@ static tmvg_status run_plan(BatchPlan* p, double* A, double* B, int64_t* P, int*
     h.status = status;
     h.count = p->count;
     for (int k = 0; k < kNumClasses; ++k) h.pw[k] = p->pw[k];
+    h.As = nullptr;
+    h.max_iter = 0;
+    h.tol = 0.0;
+    h.iters = nullptr;
+    h.berr = nullptr;
+}
+
+static tmvg_status run_plan_mixed(BatchPlan* p, const double* A, double* B, int64_t* P, int* status,
+                                  int max_iter, double tol, int* iters, double* berr)
+{
+    Context* c = p->c;
+    if (!p->d_As) {
+        if (cudaMalloc(&p->d_As, sizeof(float) * (size_t)std::max<int64_t>(p->a_elems, 1)) != cudaSuccess) {
+            cudaGetLastError();
+            p->d_As = nullptr;
+            return set_error(c, TMVG_OOM, "batched mixed: FP32 factors");
+        }
+    }
+    if (!p->exec_mixed) {
+        tmvg_status st = build_graph_mixed(p);
+        if (st) return st;
+    }
+    fill_args(p, const_cast<double*>(A), B, P, status);
+    BatchDev& h = *p->h_args;
+    h.As = p->d_As;
+    h.max_iter = max_iter;
+    h.tol = tol;
+    h.iters = iters;
+    h.berr = berr;
+    tmvg_status st = check_cuda(
+        c, cudaMemcpyAsync(p->d_args, p->h_args, sizeof(BatchDev), cudaMemcpyHostToDevice, c->stream),
+        "batched mixed: args");
+    if (st) return st;
+    st = check_cuda(c, cudaGraphLaunch(p->exec_mixed, c->stream), "batched mixed: graph launch");
+    if (st) return st;
+    c->launches += 1;
+    return check_cuda(c, cudaStreamSynchronize(c->stream), "batched mixed: sync");
+}
+
+static tmvg_status run_plan(BatchPlan* p, double* A, double* B, int64_t* P, int* status)
+{
+    Context* c = p->c;
+    fill_args(p, A, B, P, status);
     tmvg_status st = check_cuda(
         c, cudaMemcpyAsync(p->d_args, p->h_args, sizeof(BatchDev), cudaMemcpyHostToDevice, c->stream),
         "batched: args");
@@ -649,6 +992,21 @@ tmvg_status tmvg_batched_lu_solve_f64(tmvg_batch_plan plan, double* A, double* B
     return run_plan(p, A, B, P, status);
 }
 
+tmvg_status tmvg_batched_lu_solve_mixed_f64(tmvg_batch_plan plan, const double* A, double* B, int64_t* P,
+                                            int32_t* status, int max_iter, double tol, int32_t* iters,
+                                            double* berr)
+{
+    BatchPlan* p = reinterpret_cast<BatchPlan*>(plan);
+    if (!p) return TMVG_BAD_ARG;
+    Context* c = p->c;
+    c->last_error.clear();
+    cudaSetDevice(c->device);
+    if (max_iter < 0 || !(tol >= 0.0)) return set_error(c, TMVG_BAD_ARG, "batched mixed: max_iter/tol");
+    if (p->count == 0) return TMVG_OK;
+    if (!A || !B || !P || !status) return set_error(c, TMVG_BAD_ARG, "batched mixed: null buffer");
+    return run_plan_mixed(p, A, B, P, status, max_iter, tol, iters, berr);
+}
+
 tmvg_status tmvg_batch_plan_destroy(tmvg_batch_plan plan)
 {
     BatchPlan* p = reinterpret_cast<BatchPlan*>(plan);
@@ -656,6 +1014,9 @@ tmvg_status tmvg_batch_plan_destroy(tmvg_batch_plan plan)
     cudaSetDevice(p->c->device);
     if (p->exec) cudaGraphExecDestroy(p->exec);
     if (p->graph) cudaGraphDestroy(p->graph);
+    if (p->exec_mixed) cudaGraphExecDestroy(p->exec_mixed);
+    if (p->graph_mixed) cudaGraphDestroy(p->graph_mixed);
+    cudaFree(p->d_As);
     cudaFree(p->d_desc);
     cudaFree(p->d_order);
     cudaFree(p->d_args);
