@@ -406,7 +406,7 @@ def batched_bench(dev, args, with_cpu: bool) -> dict:
 NCU_TRAFFIC_PER_ALG_BYTE: dict = {"panel": 0.527, "trailing_update": 0.872, "tri_solve": 1.008}
 
 KERNEL_NAMES = {
-    "panel": "lu_panel_cluster_reg_kernel (16-CTA cluster, register-resident FP32 panel)",
+    "panel": "lu_panel_cluster_reg2_kernel (16-CTA cluster, two register-resident FP32 panel rows per thread)",
     "trailing_update": "U12 solve + A22 -= L21 U12 (FP32: u12_reg_kernel + tf32x3_update_kernel "
                        "on tcgen05; FP64: u12_reg_kernel + gemm_simt_kernel<double>)",
     "tri_solve": "trsv_pub_kernel (FP32 inverse-block triangular solve)",

@@ -333,9 +333,9 @@ lu_panel_cluster_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, in
 // ---------------------------------------------------------------------
 // Register-resident cluster panel.
 //
-// Every thread holds one row of the panel in registers, so the rank-1 update
-// of column j costs a thread NB-j-1 FMAs against the pivot row read from
-// shared memory.  Register indices must be static, so the row is kept
+// Every thread holds panel rows in registers (two: lu_panel_cluster_reg2_kernel),
+// so the rank-1 update of column j costs a thread NB-j-1 FMAs per row against
+// the pivot row read from shared memory.  Register indices must be static, so the row is kept
 // rotated: columns are processed in blocks of 4 (unrolled), the active
 // columns of block q sit at positions 0.. of the register array, and after
 // each block the array rotates left by 4 (finished columns wrap to the end,
@@ -355,11 +355,9 @@ lu_panel_cluster_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, in
 // later, after every CTA has arrived for the column in between, which each
 // does after its pulls of the column before.  The waits are bounded: on a
 // timeout the CTA records kDevTimeout and stops, and the others time out in
-// turn.  Used while a 16-CTA cluster covers the panel's rows with one row per
-// thread (m <= 16 * 512).
+// turn.  Used while a 16-CTA cluster covers the panel's rows with two rows
+// per thread (m <= 16 * 512); a panel of at most 256 rows runs in one CTA.
 // ---------------------------------------------------------------------
-constexpr int kRegPanelThreads = 512;
-constexpr int kRegPanelWarps = kRegPanelThreads / 32;
 constexpr int kRegBlock = 4;
 
 template <typename T>
@@ -480,20 +478,73 @@ __device__ __forceinline__ float recip_rn(float x) { return __frcp_rn(x); }
 __device__ __forceinline__ double recip_rn(double x) { return __drcp_rn(x); }
 
 
+// ---------------------------------------------------------------------
+// Register panel, two rows per thread: 256 threads per CTA, each holding
+// panel rows r0 + t and r0 + t + 256 in registers (16 CTAs: m <= 8192).  Per
+// column a thread reads the masked pivot row from shared memory once and
+// updates both rows with it; with one row per thread (512 threads) those
+// broadcast reads and the per-warp key reduction, candidate store and
+// barrier work cost 5-7 % more per column (measured).
+// ---------------------------------------------------------------------
+constexpr int kReg2Threads = 256;
+constexpr int kReg2Warps = kReg2Threads / 32;
+
+// x[c] -= l * um[c] over the row (full width against the masked pivot row)
+// when l is finite; otherwise only positions u < c < lim, from the unmasked
+// pivot row.
 template <typename T, int NB>
-__global__ void __launch_bounds__(kRegPanelThreads, 1)
-lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int nb,
-                            int64_t* __restrict__ P, const unsigned char* __restrict__ modes,
-                            int rows_per_cta, int* pairs, int* err, float* __restrict__ ahi,
-                            float* __restrict__ alo)
+__device__ __forceinline__ void reg2_update(T (&x)[NB], T l, const T* __restrict__ um, const T* __restrict__ ur,
+                                            int u, int lim)
+{
+    using V = Vec16<T>;
+    if (isfinite(l)) {
+        if constexpr (std::is_same<T, float>::value) {
+            const float2 nl = make_float2(-l, -l);
+#pragma unroll
+            for (int v = 0; v < NB / 4; ++v) {
+                const float4 uv = reinterpret_cast<const float4*>(um)[v];
+                const float2 a = __ffma2_rn(nl, make_float2(uv.x, uv.y), make_float2(x[4 * v], x[4 * v + 1]));
+                const float2 b = __ffma2_rn(nl, make_float2(uv.z, uv.w), make_float2(x[4 * v + 2], x[4 * v + 3]));
+                x[4 * v] = a.x;
+                x[4 * v + 1] = a.y;
+                x[4 * v + 2] = b.x;
+                x[4 * v + 3] = b.y;
+            }
+        } else {
+#pragma unroll
+            for (int v = 0; v < NB / V::E; ++v) {
+                const typename V::type uv = reinterpret_cast<const typename V::type*>(um)[v];
+#pragma unroll
+                for (int e = 0; e < V::E; ++e) x[v * V::E + e] -= l * V::get(uv, e);
+            }
+        }
+    } else {
+#pragma unroll
+        for (int v = 0; v < NB / V::E; ++v) {
+            const typename V::type uv = reinterpret_cast<const typename V::type*>(ur)[v];
+#pragma unroll
+            for (int e = 0; e < V::E; ++e) {
+                const int c = v * V::E + e;
+                if (c > u && c < lim) x[c] -= l * V::get(uv, e);
+            }
+        }
+    }
+}
+
+template <typename T, int NB>
+__global__ void __launch_bounds__(kReg2Threads, 1)
+lu_panel_cluster_reg2_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int nb,
+                             int64_t* __restrict__ P, const unsigned char* __restrict__ modes,
+                             int rows_per_cta, int* pairs, int* err, float* __restrict__ ahi,
+                             float* __restrict__ alo)
 {
     static_assert(NB % kRegBlock == 0, "whole blocks");
     static_assert(NB * sizeof(T) == 256, "a row is 16 vectors of 16 bytes");
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
-    __shared__ unsigned long long s_key[kRegPanelWarps];
-    __shared__ int s_idx[kRegPanelWarps];
-    __shared__ __align__(16) T warp_row[kRegPanelWarps][NB];  // each warp's candidate row
+    __shared__ unsigned long long s_key[kReg2Warps];
+    __shared__ int s_idx[kReg2Warps];
+    __shared__ __align__(16) T warp_row[kReg2Warps][NB];  // each warp's candidate row
     // published for remote pulls, double-buffered by column parity
     __shared__ __align__(16) T pub_row[2][NB];   // this CTA's candidate row
     __shared__ __align__(16) T pub_diag[2][NB];  // row j, in the CTA that holds it
@@ -516,8 +567,8 @@ lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k
     const int m = (int)(n - k);
     const int r0 = cta * rows_per_cta;
     const int nr = max(0, min(rows_per_cta, m - r0));
-    const bool have = tid < nr;
-    const int pr = r0 + tid;  // this thread's row, counted from the panel's top
+    const bool ha = tid < nr, hb = tid + kReg2Threads < nr;
+    const int pa = r0 + tid, pb = r0 + tid + kReg2Threads;  // this thread's rows
     T* Ap = A + k + k * lda;
 
     if (tid == 0) {
@@ -526,14 +577,17 @@ lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k
         s_abort = 0;
         mbar_fence_init();
     }
-    for (int j = tid; j < nb; j += kRegPanelThreads) s_mode[j] = modes[j];
-    T x[NB];
+    for (int j = tid; j < nb; j += kReg2Threads) s_mode[j] = modes[j];
+    T x[NB], y[NB];
 #pragma unroll
-    for (int c = 0; c < NB; ++c) x[c] = (have && c < nb) ? Ap[pr + c * lda] : T(0);
+    for (int c = 0; c < NB; ++c) {
+        x[c] = (ha && c < nb) ? Ap[pa + c * lda] : T(0);
+        y[c] = (hb && c < nb) ? Ap[pb + c * lda] : T(0);
+    }
     cluster.sync();  // every CTA's mbarriers are initialised before any arrival
 
     bool prev_uf = false;
-    int rot = 0;  // x[p] holds column (p + rot) mod NB
+    int rot = 0;  // x[p], y[p] hold column (p + rot) mod NB
     for (int jb = 0; jb < nb; jb += kRegBlock) {
         const int lim = NB - jb;  // positions >= lim hold finished columns 0..jb-1
 #pragma unroll
@@ -543,27 +597,37 @@ lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k
             const int par = jj & 1;
             const bool r2 = s_mode[jj] && !prev_uf;
             const int owner_j = jj < rows_per_cta ? 0 : jj / rows_per_cta;
-            // 1. this warp's candidate; its row, and row jj, into shared memory
+            // 1. this warp's candidate (the better of each thread's two rows,
+            //    the lower row on a tie); its row, and row jj, into shared memory
             unsigned long long bk = 0;
             int bi = INT_MAX;
-            if (have && pr >= jj) {
-                bk = reg_pivot_key(x[u], pr == jj, r2);
-                bi = pr;
+            if (ha && pa >= jj) {
+                bk = reg_pivot_key(x[u], pa == jj, r2);
+                bi = pa;
+            }
+            if (hb && pb >= jj) {
+                const unsigned long long kb = reg_pivot_key(y[u], pb == jj, r2);
+                if (bi == INT_MAX || kb > bk) {
+                    bk = kb;
+                    bi = pb;
+                }
             }
             reg_key_reduce<T>(bk, bi);
-            if (have && bi == pr) store_row<T, NB>(warp_row[warp], x);
+            if (bi == pa) store_row<T, NB>(warp_row[warp], x);
+            else if (bi == pb) store_row<T, NB>(warp_row[warp], y);
             if (lane == 0) { s_key[warp] = bk; s_idx[warp] = bi; }
-            if (have && pr == jj) store_row<T, NB>(pub_diag[par], x);
+            if (ha && pa == jj) store_row<T, NB>(pub_diag[par], x);
+            else if (hb && pb == jj) store_row<T, NB>(pub_diag[par], y);
             __syncthreads();
             if (warp == 0) {
                 // 2. publish this CTA's candidate, store its record into every
                 //    CTA and arrive there (release)
-                bk = lane < kRegPanelWarps ? s_key[lane] : 0ull;
-                bi = lane < kRegPanelWarps ? s_idx[lane] : INT_MAX;
+                bk = lane < kReg2Warps ? s_key[lane] : 0ull;
+                bi = lane < kReg2Warps ? s_idx[lane] : INT_MAX;
                 reg_key_reduce<T>(bk, bi);
                 if (bi != INT_MAX && lane < 16)
                     reinterpret_cast<uint4*>(pub_row[par])[lane] =
-                        reinterpret_cast<const uint4*>(warp_row[(bi - r0) >> 5])[lane];
+                        reinterpret_cast<const uint4*>(warp_row[((bi - r0) & (kReg2Threads - 1)) >> 5])[lane];
                 __syncwarp();
                 if (lane < G) {
                     st_cluster16(cluster_addr(&slot[par][cta], lane),
@@ -571,8 +635,6 @@ lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k
                     mbar_arrive_remote_release(cluster_addr(&mbar[par], lane));
                 }
                 // 3. wait for every CTA's record (bounded), reduce, pull rows
-                // every lane acquires the phase itself: its loads below must
-                // see the records and the published rows
                 const bool got = __all_sync(0xffffffffu, mbar_wait_cluster(&mbar[par], (uint32_t)((jj >> 1) & 1)));
                 if (!got) {
                     if (lane == 0) {
@@ -586,7 +648,8 @@ lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k
                     reg_key_reduce<T>(wk, wi);
                     if (lane == 0) { s_wk = wk; s_wi = wi; }
                     if (!reg_key_underflows<T>(wk)) {
-                        const int owner_w = wi / rows_per_cta;
+                        // the winning record's lane is the CTA that holds row wi
+                        const int owner_w = __ffs(__ballot_sync(0xffffffffu, lane < G && (int)mt.z == wi)) - 1;
                         if (lane < 16) {
                             const uint4 v = ld_cluster16(cluster_addr(&pub_row[par][0], owner_w) + 16 * lane);
                             reinterpret_cast<uint4*>(urow)[lane] = v;
@@ -613,96 +676,81 @@ lu_panel_cluster_reg_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k
             const int wi = s_wi;
             if (reg_key_underflows<T>(wk)) {
                 if (tid == 0) s_piv[jj] = (int)(k + jj);
-                if (have && pr >= jj) x[u] = T(0);
+                if (ha && pa >= jj) x[u] = T(0);
+                if (hb && pb >= jj) y[u] = T(0);
                 prev_uf = true;
                 continue;
             }
             prev_uf = false;
             if (tid == 0) s_piv[jj] = (int)(k + wi);
             // the interchange: row jj takes the pivot row, row wi the old row jj
-            const T* src = nullptr;
-            if (have && pr == jj) src = urow;
-            else if (have && pr == wi) src = drow;
-            if (src) load_row<T, NB>(x, src);
-            if (have && pr > jj) {
-                // TMV scales the column by the reciprocal of the pivot
-                using V = Vec16<T>;
-                const T l = x[u] * recip_rn(urow[u]);
+            if (ha && pa == jj) load_row<T, NB>(x, urow);
+            else if (ha && pa == wi) load_row<T, NB>(x, drow);
+            if (hb && pb == jj) load_row<T, NB>(y, urow);
+            else if (hb && pb == wi) load_row<T, NB>(y, drow);
+            // TMV scales the column by the reciprocal of the pivot
+            const T rp = recip_rn(urow[u]);
+            if (ha && pa > jj) {
+                const T l = x[u] * rp;
                 x[u] = l;
-                if (isfinite(l)) {
-                    // full width against the masked pivot row: a zero there
-                    // leaves x unchanged (up to the sign of a zero x)
-                    if constexpr (std::is_same<T, float>::value) {
-                        const float2 nl = make_float2(-l, -l);
-#pragma unroll
-                        for (int v = 0; v < NB / 4; ++v) {
-                            const float4 uv = reinterpret_cast<const float4*>(umask)[v];
-                            const float2 a = __ffma2_rn(nl, make_float2(uv.x, uv.y), make_float2(x[4 * v], x[4 * v + 1]));
-                            const float2 b = __ffma2_rn(nl, make_float2(uv.z, uv.w), make_float2(x[4 * v + 2], x[4 * v + 3]));
-                            x[4 * v] = a.x;
-                            x[4 * v + 1] = a.y;
-                            x[4 * v + 2] = b.x;
-                            x[4 * v + 3] = b.y;
-                        }
-                    } else {
-#pragma unroll
-                        for (int v = 0; v < NB / V::E; ++v) {
-                            const typename V::type uv = reinterpret_cast<const typename V::type*>(umask)[v];
-#pragma unroll
-                            for (int e = 0; e < V::E; ++e) x[v * V::E + e] -= l * V::get(uv, e);
-                        }
-                    }
-                } else {
-                    // a NaN or infinite multiplier touches only the columns to update
-#pragma unroll
-                    for (int v = 0; v < NB / V::E; ++v) {
-                        if ((v + 1) * V::E <= u + 1) continue;  // columns <= u only
-                        const typename V::type uv = reinterpret_cast<const typename V::type*>(urow)[v];
-#pragma unroll
-                        for (int e = 0; e < V::E; ++e) {
-                            const int c = v * V::E + e;
-                            if (c > u && c < lim) x[c] -= l * V::get(uv, e);
-                        }
-                    }
-                }
+                reg2_update<T, NB>(x, l, umask, urow, u, lim);
+            }
+            if (hb && pb > jj) {
+                const T l = y[u] * rp;
+                y[u] = l;
+                reg2_update<T, NB>(y, l, umask, urow, u, lim);
             }
         }
         if (s_abort) break;
         if (jb + kRegBlock < nb) {
-            T t[kRegBlock];
+            T t[kRegBlock], t2[kRegBlock];
 #pragma unroll
-            for (int c = 0; c < kRegBlock; ++c) t[c] = x[c];
+            for (int c = 0; c < kRegBlock; ++c) {
+                t[c] = x[c];
+                t2[c] = y[c];
+            }
 #pragma unroll
-            for (int c = 0; c < NB - kRegBlock; ++c) x[c] = x[c + kRegBlock];
+            for (int c = 0; c < NB - kRegBlock; ++c) {
+                x[c] = x[c + kRegBlock];
+                y[c] = y[c + kRegBlock];
+            }
 #pragma unroll
-            for (int c = 0; c < kRegBlock; ++c) x[NB - kRegBlock + c] = t[c];
+            for (int c = 0; c < kRegBlock; ++c) {
+                x[NB - kRegBlock + c] = t[c];
+                y[NB - kRegBlock + c] = t2[c];
+            }
             rot += kRegBlock;
         }
     }
 
     if (!s_abort) {
-        if (have) {
-            // with ahi (FP32 factorisation) the rows below the panel block are
-            // also written as the TF32 hi/lo split of L21 (row-major, nb wide)
-            // that the step's tensor-core update reads
+        // with ahi (FP32 factorisation) the rows below the panel block are
+        // also written as the TF32 hi/lo split of L21 (row-major, nb wide)
+        // that the step's tensor-core update reads
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const bool have = h == 0 ? ha : hb;
+            const int pr = h == 0 ? pa : pb;
+            if (!have) continue;
             const bool split = std::is_same<T, float>::value && ahi != nullptr && pr >= nb;
 #pragma unroll
             for (int p = 0; p < NB; ++p) {
                 const int col = (p + rot) % NB;
                 if (col < nb) {
-                    Ap[pr + col * lda] = x[p];
+                    const T v = h == 0 ? x[p] : y[p];
+                    Ap[pr + col * lda] = v;
                     if (split) {
-                        const float v = (float)x[p];
-                        const float h = tf32_round(v);
-                        ahi[(int64_t)(pr - nb) * nb + col] = h;
-                        alo[(int64_t)(pr - nb) * nb + col] = tf32_round(v - h);
+                        const float f = (float)v;
+                        const float hi = tf32_round(f);
+                        ahi[(int64_t)(pr - nb) * nb + col] = hi;
+                        alo[(int64_t)(pr - nb) * nb + col] = tf32_round(f - hi);
                     }
                 }
             }
         }
         __syncthreads();
         if (cta == 0) {
-            for (int j = tid; j < nb; j += kRegPanelThreads) P[k + j] = s_piv[j];
+            for (int j = tid; j < nb; j += kReg2Threads) P[k + j] = s_piv[j];
             if (warp == 0) panel_row_pairs(k, nb, s_piv, pairs);
         }
     }
@@ -1332,7 +1380,7 @@ static bool reg_panel_ok(Context* c)
     int& ok = c->reg_cluster_ok[sizeof(T) == 8 ? 0 : 1];
     if (ok >= 0) return ok == 1;
     ok = 0;
-    auto kern = lu_panel_cluster_reg_kernel<T, RegPanel<T>::NB>;
+    auto kern = lu_panel_cluster_reg2_kernel<T, RegPanel<T>::NB>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
         cudaGetLastError();
         return false;
@@ -1344,7 +1392,7 @@ static bool reg_panel_ok(Context* c)
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.gridDim = dim3(kClusterCtas);
-    cfg.blockDim = dim3(kRegPanelThreads);
+    cfg.blockDim = dim3(kReg2Threads);
     cfg.dynamicSmemBytes = 0;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
@@ -1362,23 +1410,26 @@ static tmvg_status launch_panel_cluster_reg(Context* c, cudaStream_t s, T* A, in
                                             int64_t k, int nb, int64_t* P, const unsigned char* modes,
                                             int* pairs, float* ahi, float* alo)
 {
+    // two rows per thread in 16 CTAs; a panel of at most 256 rows in one CTA
+    // (no cluster exchange; faster there, measured)
     const int64_t m = n - k;
-    const int rpc = (int)ceil_div(m, kClusterCtas);
+    const int G = m <= kReg2Threads ? 1 : kClusterCtas;
+    const int rpc = (int)ceil_div(m, G);
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = kClusterCtas;
+    attr[0].val.clusterDim.x = G;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
-    cfg.gridDim = dim3(kClusterCtas);
-    cfg.blockDim = dim3(kRegPanelThreads);
+    cfg.gridDim = dim3(G);
+    cfg.blockDim = dim3(kReg2Threads);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = s;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     ++c->launches;
     return check_cuda(c,
-                      cudaLaunchKernelEx(&cfg, lu_panel_cluster_reg_kernel<T, RegPanel<T>::NB>, A,
+                      cudaLaunchKernelEx(&cfg, lu_panel_cluster_reg2_kernel<T, RegPanel<T>::NB>, A,
                                          lda, n, k, nb, P, modes, rpc, pairs, c->dflags, ahi, alo),
                       "lu: register panel launch");
 }
@@ -1389,7 +1440,7 @@ tmvg_status lu_factor(Context* c, int64_t n, T* A, int64_t lda, int64_t* P)
     if (n < 0 || lda < std::max<int64_t>(n, 1)) return set_error(c, TMVG_BAD_ARG, "lu: bad n/lda");
     if (n == 0) return TMVG_OK;
     // one panel row per thread of a 16-CTA cluster while the rows fit
-    const bool reg = n <= (int64_t)kClusterCtas * kRegPanelThreads && reg_panel_ok<T>(c);
+    const bool reg = n <= (int64_t)kClusterCtas * 2 * kReg2Threads && reg_panel_ok<T>(c);
     const int cl_nb = reg ? RegPanel<T>::NB : cluster_panel_ok<T>(c) ? cluster_panel_width<T>(n) : 0;
     const int nbmax = cl_nb > 0 ? cl_nb : panel_width<T>();
 
