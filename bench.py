@@ -399,11 +399,11 @@ def batched_bench(dev, args, with_cpu: bool) -> dict:
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic
 # byte of each kernel class, from one ncu capture of the class's main kernel
 # on the n = 8192 workload (commands and figures in profiles/):
-#   panel: lu_panel_cluster_reg_kernel, k = 256: 2.14 MB / 4.06 MB
+#   panel: lu_panel_cluster_reg2_kernel, k = 256: 2.19 MB / 4.06 MB
 #   trailing_update: tf32x3_update_kernel, k = 256: 432.1 MB / 495.7 MB
 #   tri_solve: trsv_pub_kernel: 139.6 MB / 138.5 MB
 # The traffic of a span is its algorithmic bytes times the ratio.
-NCU_TRAFFIC_PER_ALG_BYTE: dict = {"panel": 0.527, "trailing_update": 0.872, "tri_solve": 1.008}
+NCU_TRAFFIC_PER_ALG_BYTE: dict = {"panel": 0.540, "trailing_update": 0.872, "tri_solve": 1.008}
 
 KERNEL_NAMES = {
     "panel": "lu_panel_cluster_reg2_kernel (16-CTA cluster, two register-resident FP32 panel rows per thread)",

@@ -4,8 +4,8 @@
 // of TMV's UnitAMultMV1 (src/TMV_MultMV.cpp:186-215), chosen the same way
 // (row form for a row-major A, column form for a column-major one, else the
 // row form when N >= M):
-//   * column form (ColMultMV, :124-184): a column sweep, one thread per row,
-//     the columns split into chunks of kMvChunk over blockIdx.y; a column
+//   * column form (ColMultMV, :124-184): a column sweep, one thread per two
+//     adjacent rows, the columns split into chunks of kMvChunk over blockIdx.y; a column
 //     whose x_j is zero is skipped, as TMV skips it (a NaN there does not
 //     reach y); each chunk writes its partial sums and one pass adds the
 //     chunks in order and applies alpha and add;
@@ -21,7 +21,7 @@
 
 namespace tmvg {
 
-constexpr int kMvChunk = 1024;  // columns per partial sum of the column sweep
+constexpr int kMvChunk = 256;  // columns per partial sum of the column sweep (1024 CTAs at 8192^2)
 constexpr int kMvThreads = 256;
 
 __global__ void mv_copy_kernel(int64_t n, const double* __restrict__ x, int64_t incx, double* __restrict__ out)
@@ -30,7 +30,8 @@ __global__ void mv_copy_kernel(int64_t n, const double* __restrict__ x, int64_t 
         out[i] = x[i * incx];
 }
 
-// part[chunk * m + i] = sum_{j in chunk} A[i, j] x[j]
+// part[chunk * m + i] = sum_{j in chunk} A[i, j] x[j]; with a unit row step
+// each thread takes two adjacent rows (one 16-byte load per column)
 __global__ void __launch_bounds__(kMvThreads)
 mv_cols_partial_kernel(int64_t m, int64_t n, const double* __restrict__ A, int64_t sAi, int64_t sAj,
                        const double* __restrict__ x, double* __restrict__ part)
@@ -40,21 +41,40 @@ mv_cols_partial_kernel(int64_t m, int64_t n, const double* __restrict__ A, int64
     const int cn = (int)min((int64_t)kMvChunk, n - j0);
     for (int t = threadIdx.x; t < cn; t += blockDim.x) xs[t] = x[j0 + t];
     __syncthreads();
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t i = 2 * (blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
     if (i >= m) return;
     const double* a = A + i * sAi + j0 * sAj;
-    // four independent partial sums keep four loads in flight per thread
-    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-    int j = 0;
-    for (; j + 4 <= cn; j += 4) {
-        if (xs[j] != 0.0) s0 = fma(a[(int64_t)j * sAj], xs[j], s0);
-        if (xs[j + 1] != 0.0) s1 = fma(a[(int64_t)(j + 1) * sAj], xs[j + 1], s1);
-        if (xs[j + 2] != 0.0) s2 = fma(a[(int64_t)(j + 2) * sAj], xs[j + 2], s2);
-        if (xs[j + 3] != 0.0) s3 = fma(a[(int64_t)(j + 3) * sAj], xs[j + 3], s3);
+    // a column with x_j == 0 keeps the sums as they are (TMV skips it)
+    const bool pair = sAi == 1 && i + 1 < m && ((reinterpret_cast<uintptr_t>(a) | (uintptr_t)(sAj * 8)) & 15) == 0;
+    double s0 = 0.0, s1 = 0.0, t0 = 0.0, t1 = 0.0;
+    if (pair) {
+        int j = 0;
+        for (; j + 2 <= cn; j += 2) {
+            const double2 v0 = *reinterpret_cast<const double2*>(a + (int64_t)j * sAj);
+            const double2 v1 = *reinterpret_cast<const double2*>(a + (int64_t)(j + 1) * sAj);
+            const double x0 = xs[j], x1 = xs[j + 1];
+            if (x0 != 0.0) { s0 = fma(v0.x, x0, s0); t0 = fma(v0.y, x0, t0); }
+            if (x1 != 0.0) { s1 = fma(v1.x, x1, s1); t1 = fma(v1.y, x1, t1); }
+        }
+        if (j < cn) {
+            const double2 v0 = *reinterpret_cast<const double2*>(a + (int64_t)j * sAj);
+            if (xs[j] != 0.0) { s0 = fma(v0.x, xs[j], s0); t0 = fma(v0.y, xs[j], t0); }
+        }
+        part[(int64_t)blockIdx.y * m + i] = s0 + s1;
+        part[(int64_t)blockIdx.y * m + i + 1] = t0 + t1;
+        return;
     }
-    for (; j < cn; ++j)
-        if (xs[j] != 0.0) s0 = fma(a[(int64_t)j * sAj], xs[j], s0);
-    part[(int64_t)blockIdx.y * m + i] = (s0 + s1) + (s2 + s3);
+    for (int r = 0; r < 2 && i + r < m; ++r) {
+        const double* ar = a + r * sAi;
+        double u0 = 0.0, u1 = 0.0;
+        int j = 0;
+        for (; j + 2 <= cn; j += 2) {
+            if (xs[j] != 0.0) u0 = fma(ar[(int64_t)j * sAj], xs[j], u0);
+            if (xs[j + 1] != 0.0) u1 = fma(ar[(int64_t)(j + 1) * sAj], xs[j + 1], u1);
+        }
+        if (j < cn && xs[j] != 0.0) u0 = fma(ar[(int64_t)j * sAj], xs[j], u0);
+        part[(int64_t)blockIdx.y * m + i + r] = u0 + u1;
+    }
 }
 
 __global__ void mv_cols_final_kernel(int64_t m, int nchunks, const double* __restrict__ part, double alpha,
@@ -132,7 +152,7 @@ tmvg_status multmv(Context* c, bool add, double alpha, int64_t m, int64_t n, con
         ++c->launches;
         return check_cuda(c, cudaGetLastError(), "multmv: rows launch");
     }
-    dim3 g((unsigned)ceil_div(m, kMvThreads), (unsigned)nchunks);
+    dim3 g((unsigned)ceil_div(m, 2 * kMvThreads), (unsigned)nchunks);
     if (g.x > 65535u * 1024u || g.y > 65535u) return set_error(c, TMVG_UNSUPPORTED, "multmv: matrix too large");
     mv_cols_partial_kernel<<<g, kMvThreads, 0, c->stream>>>(m, n, A, sAi, sAj, xc, part);
     ++c->launches;
