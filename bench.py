@@ -286,6 +286,8 @@ def run_gpu(args) -> dict:
         out["cpu_baseline"] = cpu
     if not args.no_extras and not args.no_batched:
         out["batched"] = batched_bench(dev, args, with_cpu=(rank == 0 and not args.no_cpu_baseline))
+    if not args.no_extras:
+        out["other_workloads"] = other_workloads(dev, with_cpu=(rank == 0 and not args.no_cpu_baseline))
     if world > 1:
         torch.distributed.destroy_process_group()
     return out if rank == 0 else None
@@ -500,6 +502,94 @@ def e2e_host(args, Acm, B, n, nrhs, mixed=False) -> dict:
     return {"value": round(lu_solve_flops(n, nrhs) / dt / 1e12, 4), "unit": "TFLOP/s",
             "h2d_bytes_per_step": 8 * n * n + 8 * n * nrhs, "d2h_bytes_per_step": 8 * n * nrhs,
             "ms_per_step": round(dt * 1e3, 3), "steps": steps}
+
+
+def other_workloads(dev, with_cpu: bool) -> dict:
+    """The other measured workloads, each timed with CUDA events over device-
+    resident inputs (seeded synthetic data with the shapes and distributions
+    of the workloads): FP64 product C = A*B at M=N=K=1024 (A, B ~ U[-1,1]);
+    FP64 LU factor + solve at n = 4096 (A ~ N(0,1) + 4 sqrt(n) I, 8 right-hand
+    sides); the solve adjoint at n = 2048 (64 right-hand sides): forward
+    X = A^-1 B, backward gB = A^-T G and gA = -gB X^T."""
+    import torch
+
+    from tmv_gb300 import adjoint, linalg
+
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MiB > L2
+
+    def ev_time(fn, reps=5, warm=3):
+        for _ in range(warm):
+            fn()
+        best = float("inf")
+        for i in range(reps):
+            flush.fill_(float(i))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        return best
+
+    out = {}
+    g = torch.Generator(device=dev)
+    g.manual_seed(1)
+    m = 1024
+    A = (torch.rand((m, m), dtype=torch.float64, device=dev, generator=g) * 2 - 1).t()
+    Bm = (torch.rand((m, m), dtype=torch.float64, device=dev, generator=g) * 2 - 1).t()
+    C = torch.empty((m, m), dtype=torch.float64, device=dev).t()
+    ms = ev_time(lambda: linalg.multmm(False, 1.0, A, Bm, C))
+    tf = 2.0 * m ** 3 / (ms * 1e-3) / 1e12
+    out["fp64_gemm_1024"] = {"value": round(tf, 4), "unit": "TFLOP/s", "ms": round(ms, 4),
+                             "roofline": {"bound": "fp64", "achieved": round(tf, 4),
+                                          "peak": FP64_DFMA_PEAK_TFLOPS, "unit": "TFLOP/s",
+                                          "frac": round(tf / FP64_DFMA_PEAK_TFLOPS, 4)},
+                             "kernel": "gemm_simt_kernel<double> (MultMM, column-major operands)",
+                             "flush": "256 MiB written between runs"}
+    if with_cpu:
+        import oracle
+
+        orc = oracle.port()
+        orc.set_threads(os.cpu_count() or 1)
+        Ah, Bh = np.asfortranarray(A.cpu().numpy()), np.asfortranarray(Bm.cpu().numpy())
+        Ch = np.zeros((m, m), order="F")
+        t0 = time.perf_counter()
+        orc.multmm(False, 1.0, Ah, Bh, Ch)
+        dt = time.perf_counter() - t0
+        out["fp64_gemm_1024"]["cpu_baseline"] = {
+            "value": round(2.0 * m ** 3 / dt / 1e12, 5), "unit": "TFLOP/s", "cores": os.cpu_count() or 1,
+            "kind": "port", "sample": f"one 1024^3 MultMM (OpenMP block product, {dt:.2f} s)"}
+    n = 4096
+    A4 = torch.randn((n, n), dtype=torch.float64, device=dev, generator=g)
+    A4 += 4.0 * np.sqrt(n) * torch.eye(n, dtype=torch.float64, device=dev)
+    A4 = linalg.colmajor(A4)
+    B4 = linalg.colmajor(torch.randn((n, 8), dtype=torch.float64, device=dev, generator=g))
+    ms = ev_time(lambda: linalg.divide(A4, B4), reps=3, warm=1)
+    fl = lu_solve_flops(n, 8)
+    tf = fl / (ms * 1e-3) / 1e12
+    out["fp64_lu_solve_4096"] = {"value": round(tf, 4), "unit": "TFLOP/s", "ms": round(ms, 3),
+                                 "roofline": {"bound": "fp64", "achieved": round(tf, 4),
+                                              "peak": FP64_DFMA_PEAK_TFLOPS, "unit": "TFLOP/s",
+                                              "frac": round(tf / FP64_DFMA_PEAK_TFLOPS, 4)},
+                                 "workload": "X = B/A, n = 4096, 8 right-hand sides, A ~ N(0,1) + 4 sqrt(n) I"}
+    n = 2048
+    A5 = torch.randn((n, n), dtype=torch.float64, device=dev, generator=g)
+    A5 += 3.0 * np.sqrt(n) * torch.eye(n, dtype=torch.float64, device=dev)
+    A5 = linalg.colmajor(A5)
+    B5 = linalg.colmajor(torch.randn((n, 64), dtype=torch.float64, device=dev, generator=g))
+    G5 = linalg.colmajor(torch.randn((n, 64), dtype=torch.float64, device=dev, generator=g))
+    X5, LU5, P5 = adjoint.solve_fwd(A5, B5)
+    fwd_ms = ev_time(lambda: adjoint.solve_fwd(A5, B5), reps=3, warm=1)
+    bwd_ms = ev_time(lambda: adjoint.solve_bwd(LU5, P5, X5, G5), reps=3, warm=1)
+    out["adjoint_2048x64"] = {
+        "forward_ms": round(fwd_ms, 3), "backward_ms": round(bwd_ms, 3),
+        "forward_tflops": round(lu_solve_flops(n, 64) / (fwd_ms * 1e-3) / 1e12, 4),
+        "backward_tflops": round(4.0 * n * n * 64 / (bwd_ms * 1e-3) / 1e12, 4),
+        "workload": "X = A^-1 B (n = 2048, 64 right-hand sides), backward gB = A^-T G and gA = -gB X^T "
+                    "from the stored factors"}
+    del flush
+    return out
 
 
 def cpu_baseline(A: np.ndarray, B: np.ndarray, n: int, cond: float) -> dict:

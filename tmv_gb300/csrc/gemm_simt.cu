@@ -127,6 +127,17 @@ struct SimtTile<double> { static constexpr int TM = 4, TN = 4, BK = 16; };
 template <>
 struct SimtTile<float> { static constexpr int TM = 8, TN = 8, BK = 8; };
 
+// Half-size tiles for products whose full-size grid would not cover the SMs
+// (the narrow updates of blocked triangular solves: m x 64 x 64).  Each C
+// element is still one thread's k-ordered FMA chain, so the result does not
+// depend on the tile size.
+template <typename T>
+struct SimtSmallTile;
+template <>
+struct SimtSmallTile<double> { static constexpr int TM = 2, TN = 2, BK = 16; };
+template <>
+struct SimtSmallTile<float> { static constexpr int TM = 4, TN = 4, BK = 8; };
+
 template <typename T, bool ARM, bool BRM>
 static tmvg_status launch_gemm(Context* c, int64_t m, int64_t n, int64_t k, T alpha,
                                const T* A, int64_t lda, const T* B, int64_t ldb,
@@ -134,6 +145,15 @@ static tmvg_status launch_gemm(Context* c, int64_t m, int64_t n, int64_t k, T al
 {
     constexpr int TM = SimtTile<T>::TM, TN = SimtTile<T>::TN, BK = SimtTile<T>::BK;
     dim3 grid((unsigned)ceil_div(m, 16 * TM), (unsigned)ceil_div(n, 16 * TN));
+    if ((int64_t)grid.x * grid.y < c->num_sms) {
+        constexpr int STM = SimtSmallTile<T>::TM, STN = SimtSmallTile<T>::TN, SBK = SimtSmallTile<T>::BK;
+        dim3 g2((unsigned)ceil_div(m, 16 * STM), (unsigned)ceil_div(n, 16 * STN));
+        if (g2.y > 65535) return set_error(c, TMVG_UNSUPPORTED, "gemm: n too large");
+        gemm_simt_kernel<T, STM, STN, SBK, ARM, BRM><<<g2, 256, 0, c->stream>>>(
+            m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);
+        ++c->launches;
+        return check_cuda(c, cudaGetLastError(), "gemm launch");
+    }
     if (grid.y > 65535) return set_error(c, TMVG_UNSUPPORTED, "gemm: n too large");
     gemm_simt_kernel<T, TM, TN, BK, ARM, BRM><<<grid, 256, 0, c->stream>>>(
         m, n, k, alpha, A, lda, B, ldb, beta, C, ldc);

@@ -971,9 +971,10 @@ __global__ void pivot_rows_kernel(int64_t ncols, T* __restrict__ B, int64_t bsi,
 // src/TMV_TriDiv_M.cpp:58-188) every zero diagonal is singular and the row
 // is multiplied by the reciprocal.
 // ---------------------------------------------------------------------
-constexpr int kTriCols = 64;
+constexpr int kTriCols = 64;     // right-hand sides per CTA of the diagonal-block solve
+constexpr int kTriThreads = 256; // threads per CTA of the diagonal-block solve
 template <typename T>
-__global__ void __launch_bounds__(kTriCols)
+__global__ void __launch_bounds__(kTriThreads)
 tri_diag_kernel(int w, const T* __restrict__ tri, int64_t tsi, int64_t tsj, bool upper,
                 bool unit, int64_t nrhs, T* __restrict__ B, int64_t bsi, int64_t bsj,
                 bool skip_zero, int* err)
@@ -988,73 +989,65 @@ tri_diag_kernel(int w, const T* __restrict__ tri, int64_t tsi, int64_t tsj, bool
     const int64_t c0 = (int64_t)blockIdx.x * kTriCols;
     const int ncb = (int)min((int64_t)kTriCols, nrhs - c0);
 
-    for (int t = tid; t < w * w; t += kTriCols) {
+    for (int t = tid; t < w * w; t += kTriThreads) {
         const int i = t % w, j = t / w;
         const bool need = upper ? (j >= i) : (i >= j);
         Ts(i, j) = need ? tri[i * tsi + j * tsj] : T(0);
     }
     if (bsi == 1) {
-        for (int t = tid; t < w * ncb; t += kTriCols) {
+        for (int t = tid; t < w * ncb; t += kTriThreads) {
             const int i = t % w, cl = t / w;
             Xs(i, cl) = B[i + (c0 + cl) * bsj];
         }
     } else {
-        for (int t = tid; t < w * ncb; t += kTriCols) {
+        for (int t = tid; t < w * ncb; t += kTriThreads) {
             const int cl = t % ncb, i = t / ncb;
             Xs(i, cl) = B[i * bsi + (c0 + cl) * bsj];
         }
     }
     __syncthreads();
 
-    if (tid < ncb) {
-        bool sing = false;
-        if (!upper) {
-            for (int i = 0; i < w; ++i) {
-                T s = Xs(i, tid);
-                for (int j = 0; j < i; ++j) s -= Ts(i, j) * Xs(j, tid);
-                if (!unit) {
-                    const T d = Ts(i, i);
-                    if (skip_zero) {
-                        if (s != T(0)) {
-                            if (d == T(0)) sing = true;
-                            else s = s / d;
-                        }
-                    } else {
+    // Column-oriented substitution, one step per diagonal entry: the thread
+    // owning (j, col) divides x_j, then every (i, col) below (above) takes
+    // x_i -= T(i, j) x_j.  Each x_i receives its subtractions in the order
+    // j = 0, 1, ... (upper: w-1, w-2, ...), as the row-by-row dot product
+    // does, so the results are the same.
+    bool sing = false;
+    for (int s = 0; s < w; ++s) {
+        const int j = upper ? w - 1 - s : s;
+        if (!unit) {
+            for (int cl = tid; cl < ncb; cl += kTriThreads) {
+                T v = Xs(j, cl);
+                const T d = Ts(j, j);
+                if (skip_zero) {
+                    if (v != T(0)) {
                         if (d == T(0)) sing = true;
-                        else s = s * (T(1) / d);
+                        else v = v / d;
                     }
+                } else {
+                    if (d == T(0)) sing = true;
+                    else v = v * (T(1) / d);
                 }
-                Xs(i, tid) = s;
+                Xs(j, cl) = v;
             }
-        } else {
-            for (int i = w - 1; i >= 0; --i) {
-                T s = Xs(i, tid);
-                for (int j = w - 1; j > i; --j) s -= Ts(i, j) * Xs(j, tid);
-                if (!unit) {
-                    const T d = Ts(i, i);
-                    if (skip_zero) {
-                        if (s != T(0)) {
-                            if (d == T(0)) sing = true;
-                            else s = s / d;
-                        }
-                    } else {
-                        if (d == T(0)) sing = true;
-                        else s = s * (T(1) / d);
-                    }
-                }
-                Xs(i, tid) = s;
-            }
+            __syncthreads();
         }
-        if (sing) atomicCAS(err, (int)kDevOk, (int)kDevSingular);
+        const int r0 = upper ? 0 : j + 1, r1 = upper ? j : w;
+        const int rows = r1 - r0;
+        for (int t = tid; t < rows * ncb; t += kTriThreads) {
+            const int i = r0 + t % rows, cl = t / rows;
+            Xs(i, cl) -= Ts(i, j) * Xs(j, cl);
+        }
+        __syncthreads();
     }
-    __syncthreads();
+    if (sing) atomicCAS(err, (int)kDevOk, (int)kDevSingular);
     if (bsi == 1) {
-        for (int t = tid; t < w * ncb; t += kTriCols) {
+        for (int t = tid; t < w * ncb; t += kTriThreads) {
             const int i = t % w, cl = t / w;
             B[i + (c0 + cl) * bsj] = Xs(i, cl);
         }
     } else {
-        for (int t = tid; t < w * ncb; t += kTriCols) {
+        for (int t = tid; t < w * ncb; t += kTriThreads) {
             const int cl = t % ncb, i = t / ncb;
             B[i * bsi + (c0 + cl) * bsj] = Xs(i, cl);
         }
@@ -1102,7 +1095,7 @@ static tmvg_status launch_tri_diag(Context* c, int w, const T* tri, int64_t tsi,
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(tri_diag_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)(sizeof(T) * (kTriBlock * (kTriBlock + 1) + kTriBlock * (kTriCols + 1))));
-    tri_diag_kernel<T><<<(unsigned)blocks, kTriCols, smem, c->stream>>>(
+    tri_diag_kernel<T><<<(unsigned)blocks, kTriThreads, smem, c->stream>>>(
         w, tri, tsi, tsj, upper, unit, nrhs, B, bsi, bsj, skip_zero, c->dflags);
     ++c->launches;
     return check_cuda(c, cudaGetLastError(), "tri_diag launch");
