@@ -35,6 +35,26 @@ sys.path.insert(0, str(ROOT))
 METRIC = "n=8192 LU-solve TFLOP/s mixed+IR vs FP64 GPU at 1e-12 rel err; batched solves/s"
 
 
+def max_over_ranks(ms: float, device) -> float:
+    """The slowest rank's time (replicas: every rank runs its own workload),
+    then a barrier so that no rank starts other work inside another's
+    measurement.  Works with any process-group backend (nccl on the GPUs,
+    gloo in the CPU tests)."""
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
+def aggregate_value(units_per_rank: float, world: int, ms: float) -> float:
+    """Whole-job throughput: the units all ranks processed over the slowest
+    rank's time (weak scaling, fixed work per rank)."""
+    return units_per_rank * world / (ms * 1e-3)
+
+
 def lu_solve_flops(n: int, nrhs: int) -> float:
     return 2.0 * n ** 3 / 3.0 + 2.0 * n * n * nrhs
 
@@ -236,17 +256,14 @@ def run_gpu(args) -> dict:
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-        torch.distributed.barrier()
+        ms = max_over_ranks(ms, dev)
     clk = clocks.stop()
     launches = (h.launches() - launches0) // max(args.steps, 1)
     ms_step = ms / args.steps
     kernels = kernel_breakdown(h, args.steps, ms_step)
     h.timing_enable(False)
     flops = lu_solve_flops(n, nrhs)
-    value = flops * world / (ms_step * 1e-3) / 1e12
+    value = aggregate_value(flops, world, ms_step) / 1e12
 
     # accuracy of the last solve: normwise backward error, and forward
     # difference from the FP64 GPU LU solution
