@@ -863,7 +863,7 @@ constexpr int kU12RegBlock = 256;    // threads per CTA: all of them stage, COLS
 template <typename T, int NB, bool SPLIT, int COLS>
 __global__ void __launch_bounds__(kU12RegBlock)
 u12_reg_kernel(int nb, const T* __restrict__ L, int64_t lda, T* __restrict__ A12, int64_t ncols,
-               float* __restrict__ Bhi, float* __restrict__ Blo)
+               float* __restrict__ Bhi, float* __restrict__ Blo, const int* __restrict__ pairs, int64_t k)
 {
     using V = Vec16<T>;
     constexpr int XP = NB + V::E;  // padded staging row: conflict-free vector access
@@ -871,6 +871,32 @@ u12_reg_kernel(int nb, const T* __restrict__ L, int64_t lda, T* __restrict__ A12
     __shared__ __align__(16) T Xs[COLS][XP];
     const int tid = threadIdx.x;
     const int64_t c0 = (int64_t)blockIdx.x * COLS;
+
+    if (pairs) {
+        // the step's row interchanges on this CTA's columns first (over all
+        // rows: a warp per column, a lane per row pair; A12 - k is row 0)
+        const int lane = tid & 31, w = tid >> 5;
+        const int np = pairs[0];
+        const int* dst = pairs + 1;
+        const int* src = pairs + 1 + kMaxPairs;
+        for (int cc = w; cc < COLS; cc += kU12RegBlock / 32) {
+            if (c0 + cc >= ncols) break;
+            T* a = A12 - k + (c0 + cc) * lda;
+            T v[kMaxPairs / 32];
+#pragma unroll
+            for (int t = 0; t < kMaxPairs / 32; ++t) {
+                const int q = lane + 32 * t;
+                if (q < np) v[t] = a[src[q]];
+            }
+            __syncwarp();
+#pragma unroll
+            for (int t = 0; t < kMaxPairs / 32; ++t) {
+                const int q = lane + 32 * t;
+                if (q < np) a[dst[q]] = v[t];
+            }
+        }
+        __syncthreads();
+    }
 
     // stage L11 and this CTA's columns, eight independent loads in flight
     constexpr int LU = 8;
@@ -1216,9 +1242,16 @@ static tmvg_status tc_step_setup(Context* c, int64_t n, T* A, int64_t lda, int64
 // copy written by the U12 kernel at its offset in b).
 template <typename T>
 static tmvg_status update_columns(Context* c, int64_t n, T* A, int64_t lda, int64_t k, int nb, int64_t c0,
-                                  int64_t nc, bool tc, const Tf32x3Buffers& b)
+                                  int64_t nc, bool tc, const Tf32x3Buffers& b, const int* pairs = nullptr)
 {
+    // pairs: the step's row interchanges, still to be applied to these
+    // columns (fused into the U12 kernel for the next panel's columns)
     if (nc <= 0) return TMVG_OK;
+    const bool fuse_swaps = pairs && nb <= RegPanel<T>::NB && nc <= RegPanel<T>::NB;
+    if (pairs && !fuse_swaps) {
+        tmvg_status st0 = laswp_cols<T>(c, A, lda, c0, c0 + nc, 0, 0, pairs);
+        if (st0) return st0;
+    }
     const int64_t rest = n - k - nb;  // rows below the panel
     const T* L11 = A + k + k * lda;
     T* A12 = A + k + c0 * lda;
@@ -1234,22 +1267,23 @@ static tmvg_status update_columns(Context* c, int64_t n, T* A, int64_t lda, int6
         constexpr int NB = RegPanel<T>::NB;
         // a few columns (the next panel's): spread over more CTAs, since
         // each one's latency is staging L11 and the substitution chain
+        const int* sp = fuse_swaps ? pairs : nullptr;
         if (nc <= NB) {
             const unsigned grid = (unsigned)ceil_div(nc, kU12NarrowCols);
             if (tc)
                 u12_reg_kernel<T, NB, true, kU12NarrowCols><<<grid, kU12RegBlock, 0, c->stream>>>(
-                    nb, L11, lda, A12, nc, bc.Bhi, bc.Blo);
+                    nb, L11, lda, A12, nc, bc.Bhi, bc.Blo, sp, k);
             else
                 u12_reg_kernel<T, NB, false, kU12NarrowCols><<<grid, kU12RegBlock, 0, c->stream>>>(
-                    nb, L11, lda, A12, nc, nullptr, nullptr);
+                    nb, L11, lda, A12, nc, nullptr, nullptr, sp, k);
         } else {
             const unsigned grid = (unsigned)ceil_div(nc, kU12RegThreads);
             if (tc)
                 u12_reg_kernel<T, NB, true, kU12RegThreads><<<grid, kU12RegBlock, 0, c->stream>>>(
-                    nb, L11, lda, A12, nc, bc.Bhi, bc.Blo);
+                    nb, L11, lda, A12, nc, bc.Bhi, bc.Blo, nullptr, k);
             else
                 u12_reg_kernel<T, NB, false, kU12RegThreads><<<grid, kU12RegBlock, 0, c->stream>>>(
-                    nb, L11, lda, A12, nc, nullptr, nullptr);
+                    nb, L11, lda, A12, nc, nullptr, nullptr, nullptr, k);
         }
         ++c->launches;
         st = check_cuda(c, cudaGetLastError(), "lu: u12 launch");
@@ -1542,15 +1576,15 @@ tmvg_status lu_factor(Context* c, int64_t n, T* A, int64_t lda, int64_t* P)
             }
             const int64_t rest = n - k - nb;
             const int nb2 = (int)std::min<int64_t>(nbmax, rest);
-            // the next panel's columns first: interchanges, U12, update
-            st = laswp_cols<T>(c, A, lda, k + nb, k + nb + nb2, 0, 0, pk);
+            // the next panel's columns first: interchanges (inside the U12
+            // kernel), U12, update
             const bool tc = tc_for(k, nb);
             const Tf32x3Buffers& b = arena[step & 1];
             if constexpr (std::is_same<T, float>::value) {
                 // the register panel kernel writes the L21 split itself
                 if (!st && tc && !reg) st = tf32x3_split_a(c, rest, nb, A + (k + nb) + k * lda, lda, b);
             }
-            if (!st) st = update_columns<T>(c, n, A, lda, k, nb, k + nb, nb2, tc, b);
+            if (!st) st = update_columns<T>(c, n, A, lda, k, nb, k + nb, nb2, tc, b, pk);
             if (!st) st = check_cuda(c, cudaEventRecord(c->ev_narrow, c->stream), "lu: narrow event");
             if (!st) st = check_cuda(c, cudaStreamWaitEvent(side, c->ev_narrow, 0), "lu: narrow wait");
             if (!st) st = panel(k + nb, nb2, step + 1);
