@@ -92,7 +92,11 @@ def haar_matrix_numpy(n: int, cond: float, seed: int):
 
 
 class ClockSampler:
-    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+    """Samples SM clocks and throttle reasons with nvidia-smi every 20 ms from
+    start() to stop(), each line stamped with the host time it was read;
+    window() marks the timed region, and stop() summarises the samples read
+    inside it (or, if the region was shorter than the sampling period, all
+    samples under load, saying so)."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -101,13 +105,14 @@ class ClockSampler:
     def __init__(self, gpu_index: int = 0):
         self.gpu = gpu_index
         self.proc = None
-        self.lines: list[str] = []
+        self.lines: list[tuple[float, str]] = []
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -116,32 +121,46 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.time(), line.strip()))
+
+    def window(self, t0: float, t1: float):
+        self.t0, self.t1 = t0, t1
 
     def stop(self) -> dict:
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.05)  # the last in-window sample
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
-            f = [x.strip() for x in ln.split(",")]
-            if len(f) < 9:
-                continue
-            try:
-                sm.append(float(f[1]))
-                mx = float(f[2])
-            except ValueError:
-                continue
-            for nm, v in zip(names, f[5:9]):
-                if v.lower() == "active":
-                    reasons.add(nm)
+
+        def summarise(lines):
+            sm, mx, reasons = [], None, set()
+            for _, ln in lines:
+                f = [x.strip() for x in ln.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx = float(f[2])
+                except ValueError:
+                    continue
+                for nm, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+            return sm, mx, reasons
+
+        inside = [x for x in self.lines if self.t0 is not None and self.t0 <= x[0] <= self.t1]
+        sm, mx, reasons = summarise(inside)
+        scope = "timed region"
+        if not sm:
+            sm, mx, reasons = summarise(self.lines)
+            scope = "all samples under load (timed region shorter than the sampling period)"
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "scope": scope}
 
 
 def peaks() -> dict:
@@ -229,6 +248,8 @@ def run_gpu(args) -> dict:
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / steps, out
 
+    clocks = ClockSampler(local)
+    clocks.start()
     # the plain FP64 GPU LU on the same system (the comparison point)
     if args.no_extras:
         fp64_ms, X64 = float("nan"), None
@@ -242,25 +263,36 @@ def run_gpu(args) -> dict:
     launches0 = h.launches()
     if world > 1:
         torch.distributed.barrier()
-    clocks = ClockSampler(local)
-    clocks.start()
-    # per-kernel-class CUDA events on the library's stream, over the timed steps
-    h.timing_enable(True)
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    tw0 = time.time()
     e0.record(stream)
     for _ in range(args.steps):
         X = step()
     e1.record(stream)
     torch.cuda.synchronize()
+    clocks.window(tw0, time.time())
     ms = e0.elapsed_time(e1)
     if world > 1:
         ms = max_over_ranks(ms, dev)
     clk = clocks.stop()
     launches = (h.launches() - launches0) // max(args.steps, 1)
     ms_step = ms / args.steps
-    kernels = kernel_breakdown(h, args.steps, ms_step)
+    # per-kernel-class breakdown in a second pass of the same steps: the
+    # library records CUDA events on its streams around every span, which
+    # costs about 3 % of a step, so the timed pass above runs without them
+    bsteps = max(1, min(args.steps, 3))
+    h.timing_enable(True)
+    torch.cuda.synchronize()
+    b0 = torch.cuda.Event(enable_timing=True)
+    b1 = torch.cuda.Event(enable_timing=True)
+    b0.record(stream)
+    for _ in range(bsteps):
+        step()
+    b1.record(stream)
+    torch.cuda.synchronize()
+    kernels = kernel_breakdown(h, bsteps, b0.elapsed_time(b1) / bsteps)
     h.timing_enable(False)
     flops = lu_solve_flops(n, nrhs)
     value = aggregate_value(flops, world, ms_step) / 1e12
@@ -435,8 +467,9 @@ KERNEL_NAMES = {
 
 def kernel_breakdown(h, steps: int, ms_step: float) -> dict:
     """Per kernel class: spans, event time, share of the step and achieved
-    bandwidth / flop rate over the timed steps (CUDA events recorded by the
-    library on its stream around every span)."""
+    bandwidth / flop rate over the breakdown pass (CUDA events recorded by
+    the library on its streams around every span; ms_step is that pass's
+    own time per step)."""
     out = {}
     for cls in ("panel", "trailing_update", "tri_solve", "residual"):
         t = h.timing(cls)
