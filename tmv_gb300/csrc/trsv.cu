@@ -381,7 +381,10 @@ __device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned l
     asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-__global__ void __launch_bounds__(256)
+constexpr int kPubThreads = 512;          // four threads per row of a block
+constexpr int kPubCols = kIB / 4;          // columns of a tile per thread
+
+__global__ void __launch_bounds__(kPubThreads)
 trsv_pub_kernel(int64_t n, const float* __restrict__ tri, int64_t tsi, int64_t tsj,
                 const float* __restrict__ dinv, const int* __restrict__ singular, bool unit,
                 float* x, int64_t incx, bool skip_zero, unsigned long long* pub, unsigned epoch,
@@ -390,9 +393,9 @@ trsv_pub_kernel(int64_t n, const float* __restrict__ tri, int64_t tsi, int64_t t
     __shared__ int s_blk, s_abort;
     __shared__ float xj[2][kIB];
     __shared__ float rhs[kIB];
-    __shared__ float part[2][kIB];
+    __shared__ float part[4][kIB];
     const int tid = threadIdx.x;
-    const int i = tid & (kIB - 1), h = tid >> 7;  // row of the block, half of the columns
+    const int i = tid & (kIB - 1), q = tid >> 7;  // row of the block, quarter of the columns
     if (tid == 0) {
         s_blk = (int)atomicAdd(ticket, 1ull);
         s_abort = 0;
@@ -408,19 +411,22 @@ trsv_pub_kernel(int64_t n, const float* __restrict__ tri, int64_t tsi, int64_t t
     // independent of the other blocks: right-hand side and inverse block
     const float b_i = (tid < kIB && tid < rows) ? x[(r0 + tid) * incx] : 0.0f;
     const bool sing = singular[b] != 0;
-    float di[64];
+    float di[kPubCols];
     {
         const float* Di = dinv + b * (int64_t)kIB * kIB;
 #pragma unroll
-        for (int l = 0; l < 64; ++l) di[l] = sing ? 0.0f : Di[i + (h * 64 + l) * kIB];
+        for (int l = 0; l < kPubCols; ++l) di[l] = sing ? 0.0f : Di[i + (q * kPubCols + l) * kIB];
     }
 
-    float acc = 0.0f;
-    for (int64_t j = 0; j < b; ++j) {
-        const int64_t c0 = j * kIB + h * 64;
-        float a[64];
+    // tile j of this block's rows: the next tile's entries are loaded while
+    // the current one waits for x_j and is applied (two register buffers)
+    auto load_tile = [&](float (&a)[kPubCols], int64_t j) {
+        const int64_t c0 = j * kIB + q * kPubCols;
 #pragma unroll
-        for (int c = 0; c < 64; ++c) a[c] = (i < rows) ? tri[(r0 + i) * tsi + (c0 + c) * tsj] : 0.0f;
+        for (int c = 0; c < kPubCols; ++c) a[c] = (i < rows) ? tri[(r0 + i) * tsi + (c0 + c) * tsj] : 0.0f;
+    };
+    float acc0 = 0.0f, acc1 = 0.0f;
+    auto apply_tile = [&](const float (&a)[kPubCols], int64_t j) -> bool {
         float* xb = xj[j & 1];
         if (tid < kIB) {
             const unsigned long long* w = pub + j * kIB + tid;
@@ -438,23 +444,38 @@ trsv_pub_kernel(int64_t n, const float* __restrict__ tri, int64_t tsi, int64_t t
             xb[tid] = __uint_as_float((unsigned)v);
         }
         __syncthreads();  // xb complete; the other buffer is free again
-        if (s_abort) return;
+        if (s_abort) return false;
 #pragma unroll
-        for (int c = 0; c < 64; ++c) acc -= a[c] * xb[h * 64 + c];
+        for (int c = 0; c < kPubCols; c += 2) {
+            acc0 -= a[c] * xb[q * kPubCols + c];
+            acc1 -= a[c + 1] * xb[q * kPubCols + c + 1];
+        }
+        return true;
+    };
+    {
+        float ta[kPubCols], tb[kPubCols];
+        if (b > 0) load_tile(ta, 0);
+        for (int64_t j = 0; j < b; j += 2) {
+            if (j + 1 < b) load_tile(tb, j + 1);
+            if (!apply_tile(ta, j)) return;
+            if (j + 1 >= b) break;
+            if (j + 2 < b) load_tile(ta, j + 2);
+            if (!apply_tile(tb, j + 1)) return;
+        }
     }
-    part[h][i] = acc;
+    part[q][i] = acc0 + acc1;
     __syncthreads();
-    if (tid < kIB) rhs[tid] = b_i + part[0][tid] + part[1][tid];
+    if (tid < kIB) rhs[tid] = b_i + ((part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]));
     __syncthreads();
     if (!sing) {
-        // x_b = Dinv_b rhs: row i sums its half of the columns
+        // x_b = Dinv_b rhs: row i sums its quarter of the columns
         float sum = 0.0f;
 #pragma unroll
-        for (int l = 0; l < 64; ++l) sum += di[l] * rhs[h * 64 + l];
-        part[h][i] = sum;
+        for (int l = 0; l < kPubCols; ++l) sum += di[l] * rhs[q * kPubCols + l];
+        part[q][i] = sum;
         __syncthreads();
         if (tid < rows) {
-            const float v = part[0][tid] + part[1][tid];
+            const float v = (part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]);
             x[(r0 + tid) * incx] = v;
             st_relaxed_u64(pub + r0 + tid, tag | __float_as_uint(v));
         }
@@ -549,7 +570,7 @@ tmvg_status trsv_with_inverse_blocks(Context* c, int64_t n, const T* tri, int64_
             c->trsv_pub_len = (size_t)n;
         }
         if (epoch == 0) ++c->trsv_epoch;  // skip the clear value on wrap-around
-        trsv_pub_kernel<<<(unsigned)nblk, 256, 0, c->stream>>>(
+        trsv_pub_kernel<<<(unsigned)nblk, kPubThreads, 0, c->stream>>>(
             n, tri, tsi, tsj, dinv, singular, unit, x, incx, skip_zero, c->trsv_pub,
             c->trsv_epoch, c->trsv_ticket, c->dflags);
         ++c->launches;
