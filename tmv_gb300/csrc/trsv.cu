@@ -426,11 +426,15 @@ trsv_pub_kernel(int64_t n, const float* __restrict__ tri, int64_t tsi, int64_t t
         for (int c = 0; c < kPubCols; ++c) a[c] = (i < rows) ? tri[(r0 + i) * tsi + (c0 + c) * tsj] : 0.0f;
     };
     float acc0 = 0.0f, acc1 = 0.0f;
+    // the word of x_j a thread polls was loaded one tile ahead (vpre), so its
+    // latency hides behind the previous tile's barrier and FMAs
+    unsigned long long vpre = 0;
+    if (b > 0 && tid < kIB) vpre = ld_relaxed_u64(pub + tid);
     auto apply_tile = [&](const float (&a)[kPubCols], int64_t j) -> bool {
         float* xb = xj[j & 1];
         if (tid < kIB) {
             const unsigned long long* w = pub + j * kIB + tid;
-            unsigned long long v = ld_relaxed_u64(w);
+            unsigned long long v = vpre;
             unsigned spins = 0;
             while ((v & 0xffffffff00000000ull) != tag) {
                 if (++spins > kSpinLimit || *((volatile int*)err) == kDevTimeout) {
@@ -442,6 +446,7 @@ trsv_pub_kernel(int64_t n, const float* __restrict__ tri, int64_t tsi, int64_t t
                 v = ld_relaxed_u64(w);
             }
             xb[tid] = __uint_as_float((unsigned)v);
+            if (j + 1 < b) vpre = ld_relaxed_u64(w + kIB);
         }
         __syncthreads();  // xb complete; the other buffer is free again
         if (s_abort) return false;
