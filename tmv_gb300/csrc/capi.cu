@@ -100,7 +100,7 @@ tmvg_status ensure_side_stream(Context* c)
     cudaDeviceGetStreamPriorityRange(&least, &greatest);
     if (cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, greatest) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->ev_narrow, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_wide, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_panel, cudaEventDisableTiming) != cudaSuccess) {
         cudaGetLastError();
         return set_error(c, TMVG_CUDA_ERROR, "side stream creation failed");
@@ -357,7 +357,7 @@ tmvg_status tmvg_destroy(tmvg_handle h)
     }
     for (cudaEvent_t e : c->event_pool) cudaEventDestroy(e);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
-    if (c->ev_narrow) cudaEventDestroy(c->ev_narrow);
+    if (c->ev_wide) cudaEventDestroy(c->ev_wide);
     if (c->ev_panel) cudaEventDestroy(c->ev_panel);
     if (c->side) cudaStreamDestroy(c->side);
     delete c;

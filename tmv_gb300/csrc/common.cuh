@@ -94,7 +94,7 @@ struct Context {
     // Look-ahead of the LU: a high-priority side stream for the panels and
     // the events that order it against `stream` (created on first use).
     cudaStream_t side = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_narrow = nullptr, ev_panel = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_wide = nullptr, ev_panel = nullptr;
     // TMVG_SERIALIZE_LOOKAHEAD=1 at creation: every side-stream panel is
     // waited for on the host before the main stream's next launch, which
     // fixes one extreme interleaving of the two streams (used by tests to

@@ -1561,38 +1561,55 @@ tmvg_status lu_factor(Context* c, int64_t n, T* A, int64_t lda, int64_t* P)
             if (!s2 && c->serialize_lookahead) s2 = check_cuda(c, cudaStreamSynchronize(side), "lu: serialize");
             return s2;
         };
+        // The chain of the factorisation runs on the side stream with no
+        // hand-off between streams: panel k, the update of the next panel's
+        // columns with step k (interchanges inside the U12 kernel, U12, the
+        // narrow update), panel k+1, ...  The main stream applies step k to
+        // every other column (the wide update) once the narrow update of step
+        // k is done (event ev_fork), overlapping panel k+1, and the side
+        // stream's narrow update of step k+1 waits for that wide update (it
+        // covers the same columns with step k first; event ev_wide), which
+        // is normally finished by then.  The event waits are enqueued before
+        // the events are recorded again, so each refers to its own step.
         st = check_cuda(c, cudaEventRecord(c->ev_fork, c->stream), "lu: fork");
         if (!st) st = check_cuda(c, cudaStreamWaitEvent(side, c->ev_fork, 0), "lu: fork");
         if (!st) st = panel(0, (int)std::min<int64_t>(nbmax, n), 0);
         if (!st) st = check_cuda(c, cudaEventRecord(c->ev_panel, side), "lu: panel event");
+        cudaStream_t main_stream = c->stream;
         for (int64_t k = 0, step = 0; k < n && !st; k += nbmax, ++step) {
             const int nb = (int)std::min<int64_t>(nbmax, n - k);
-            st = check_cuda(c, cudaStreamWaitEvent(c->stream, c->ev_panel, 0), "lu: join");
-            if (st) break;
             const int* pk = pairs_of(step);
             if (k + nb >= n) {
-                st = laswp_step<T>(c, n, A, lda, k, nb, pk);
+                st = check_cuda(c, cudaStreamWaitEvent(c->stream, c->ev_panel, 0), "lu: join");
+                if (!st) st = laswp_step<T>(c, n, A, lda, k, nb, pk);
                 break;
             }
             const int64_t rest = n - k - nb;
             const int nb2 = (int)std::min<int64_t>(nbmax, rest);
-            // the next panel's columns first: interchanges (inside the U12
-            // kernel), U12, update
             const bool tc = tc_for(k, nb);
             const Tf32x3Buffers& b = arena[step & 1];
+            // side: the next panel's columns (after the previous step's wide
+            // update, event ev_wide), then the next panel
+            if (step > 0) st = check_cuda(c, cudaStreamWaitEvent(side, c->ev_wide, 0), "lu: wide wait");
+            c->stream = side;
             if constexpr (std::is_same<T, float>::value) {
                 // the register panel kernel writes the L21 split itself
                 if (!st && tc && !reg) st = tf32x3_split_a(c, rest, nb, A + (k + nb) + k * lda, lda, b);
             }
             if (!st) st = update_columns<T>(c, n, A, lda, k, nb, k + nb, nb2, tc, b, pk);
-            if (!st) st = check_cuda(c, cudaEventRecord(c->ev_narrow, c->stream), "lu: narrow event");
-            if (!st) st = check_cuda(c, cudaStreamWaitEvent(side, c->ev_narrow, 0), "lu: narrow wait");
+            c->stream = main_stream;
+            // the wide update starts after the narrow one, not beside it: the
+            // narrow update, on the chain, gets the whole GPU
+            if (!st) st = check_cuda(c, cudaEventRecord(c->ev_fork, side), "lu: narrow done");
+            if (!st) st = check_cuda(c, cudaStreamWaitEvent(c->stream, c->ev_fork, 0), "lu: join");
             if (!st) st = panel(k + nb, nb2, step + 1);
             if (!st) st = check_cuda(c, cudaEventRecord(c->ev_panel, side), "lu: panel event");
-            // then everything else of this step, overlapping the next panel
+            // main: everything else of step k, overlapping the next panel
             if (!st) st = laswp_cols<T>(c, A, lda, 0, n, k, k + nb + nb2, pk);
             if (!st) st = update_columns<T>(c, n, A, lda, k, nb, k + nb + nb2, rest - nb2, tc, b);
+            if (!st) st = check_cuda(c, cudaEventRecord(c->ev_wide, c->stream), "lu: wide event");
         }
+        c->stream = main_stream;
         if (st) {
             // leave no side work unordered after an error
             cudaStreamSynchronize(side);
