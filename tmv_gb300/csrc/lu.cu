@@ -481,7 +481,7 @@ __device__ __forceinline__ double recip_rn(double x) { return __drcp_rn(x); }
 // ---------------------------------------------------------------------
 // Register panel, two rows per thread: 256 threads per CTA, each holding
 // panel rows r0 + t and r0 + t + 256 in registers (16 CTAs: m <= 8192).  Per
-// column a thread reads the masked pivot row from shared memory once and
+// column a thread reads the pivot row's active part from shared memory once and
 // updates both rows with it; with one row per thread (512 threads) those
 // broadcast reads and the per-warp key reduction, candidate store and
 // barrier work cost 5-7 % more per column (measured).
@@ -489,43 +489,54 @@ __device__ __forceinline__ double recip_rn(double x) { return __drcp_rn(x); }
 constexpr int kReg2Threads = 256;
 constexpr int kReg2Warps = kReg2Threads / 32;
 
-// x[c] -= l * um[c] over the row (full width against the masked pivot row)
-// when l is finite; otherwise only positions u < c < lim, from the unmasked
-// pivot row.
+// The rank-1 update of one column on both of a thread's rows: x[c] -= lx *
+// ur[c] (when ux) and y[c] -= ly * ur[c] (when uy) for the positions this
+// step updates, u < c < lim.  lim is a multiple of kRegBlock, so the vectors
+// below it are whole and the finished columns above it are skipped with one
+// uniform branch per vector; u < kRegBlock folds to a constant in the
+// unrolled column loop, so the positions up to u in the first vector drop
+// out at compile time.  Only those positions are touched, as in TMV, so a
+// non-finite multiplier needs no separate path.  One shared-memory read of
+// each pivot-row vector serves both rows.
 template <typename T, int NB>
-__device__ __forceinline__ void reg2_update(T (&x)[NB], T l, const T* __restrict__ um, const T* __restrict__ ur,
-                                            int u, int lim)
+__device__ __forceinline__ void reg2_update(T (&x)[NB], T lx, bool ux, T (&y)[NB], T ly, bool uy,
+                                            const T* __restrict__ ur, int u, int lim)
 {
     using V = Vec16<T>;
-    if (isfinite(l)) {
-        if constexpr (std::is_same<T, float>::value) {
-            const float2 nl = make_float2(-l, -l);
+    static_assert(V::E <= kRegBlock && kRegBlock % V::E == 0, "vectors within a block");
 #pragma unroll
-            for (int v = 0; v < NB / 4; ++v) {
-                const float4 uv = reinterpret_cast<const float4*>(um)[v];
-                const float2 a = __ffma2_rn(nl, make_float2(uv.x, uv.y), make_float2(x[4 * v], x[4 * v + 1]));
-                const float2 b = __ffma2_rn(nl, make_float2(uv.z, uv.w), make_float2(x[4 * v + 2], x[4 * v + 3]));
-                x[4 * v] = a.x;
-                x[4 * v + 1] = a.y;
-                x[4 * v + 2] = b.x;
-                x[4 * v + 3] = b.y;
+    for (int v = 0; v < NB / V::E; ++v) {
+        if (v * V::E >= lim) break;
+        const typename V::type uv = reinterpret_cast<const typename V::type*>(ur)[v];
+        if constexpr (std::is_same<T, float>::value) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int c = 4 * v + 2 * h;
+                const float2 up = h == 0 ? make_float2(uv.x, uv.y) : make_float2(uv.z, uv.w);
+                if (c > u) {
+                    if (ux) {
+                        const float2 r = __ffma2_rn(make_float2(-lx, -lx), up, make_float2(x[c], x[c + 1]));
+                        x[c] = r.x;
+                        x[c + 1] = r.y;
+                    }
+                    if (uy) {
+                        const float2 r = __ffma2_rn(make_float2(-ly, -ly), up, make_float2(y[c], y[c + 1]));
+                        y[c] = r.x;
+                        y[c + 1] = r.y;
+                    }
+                } else if (c + 1 > u) {
+                    if (ux) x[c + 1] = fmaf(-lx, up.y, x[c + 1]);
+                    if (uy) y[c + 1] = fmaf(-ly, up.y, y[c + 1]);
+                }
             }
         } else {
 #pragma unroll
-            for (int v = 0; v < NB / V::E; ++v) {
-                const typename V::type uv = reinterpret_cast<const typename V::type*>(um)[v];
-#pragma unroll
-                for (int e = 0; e < V::E; ++e) x[v * V::E + e] -= l * V::get(uv, e);
-            }
-        }
-    } else {
-#pragma unroll
-        for (int v = 0; v < NB / V::E; ++v) {
-            const typename V::type uv = reinterpret_cast<const typename V::type*>(ur)[v];
-#pragma unroll
             for (int e = 0; e < V::E; ++e) {
                 const int c = v * V::E + e;
-                if (c > u && c < lim) x[c] -= l * V::get(uv, e);
+                if (c > u) {
+                    if (ux) x[c] = fma(-lx, V::get(uv, e), x[c]);
+                    if (uy) y[c] = fma(-ly, V::get(uv, e), y[c]);
+                }
             }
         }
     }
@@ -552,7 +563,6 @@ lu_panel_cluster_reg2_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t 
     __shared__ __align__(8) uint64_t mbar[2];
     // the column's outcome, handed from warp 0 to the block
     __shared__ __align__(16) T urow[NB];
-    __shared__ __align__(16) T umask[NB];  // urow with zeros outside the columns to update
     __shared__ __align__(16) T drow[NB];
     __shared__ unsigned long long s_wk;
     __shared__ int s_wi;
@@ -650,21 +660,10 @@ lu_panel_cluster_reg2_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t 
                     if (!reg_key_underflows<T>(wk)) {
                         // the winning record's lane is the CTA that holds row wi
                         const int owner_w = __ffs(__ballot_sync(0xffffffffu, lane < G && (int)mt.z == wi)) - 1;
-                        if (lane < 16) {
-                            const uint4 v = ld_cluster16(cluster_addr(&pub_row[par][0], owner_w) + 16 * lane);
-                            reinterpret_cast<uint4*>(urow)[lane] = v;
-                            // the columns this step updates are positions u+1 .. lim-1
-                            T e[16 / sizeof(T)];
-                            memcpy(e, &v, 16);
-#pragma unroll
-                            for (int q = 0; q < (int)(16 / sizeof(T)); ++q) {
-                                const int pos = lane * (int)(16 / sizeof(T)) + q;
-                                if (pos <= u || pos >= lim) e[q] = T(0);
-                            }
-                            uint4 w;
-                            memcpy(&w, e, 16);
-                            reinterpret_cast<uint4*>(umask)[lane] = w;
-                        } else if (cta == owner_w && wi != jj)
+                        if (lane < 16)
+                            reinterpret_cast<uint4*>(urow)[lane] =
+                                ld_cluster16(cluster_addr(&pub_row[par][0], owner_w) + 16 * lane);
+                        else if (cta == owner_w && wi != jj)
                             reinterpret_cast<uint4*>(drow)[lane - 16] =
                                 ld_cluster16(cluster_addr(&pub_diag[par][0], owner_j) + 16 * (lane - 16));
                     }
@@ -690,16 +689,11 @@ lu_panel_cluster_reg2_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t 
             else if (hb && pb == wi) load_row<T, NB>(y, drow);
             // TMV scales the column by the reciprocal of the pivot
             const T rp = recip_rn(urow[u]);
-            if (ha && pa > jj) {
-                const T l = x[u] * rp;
-                x[u] = l;
-                reg2_update<T, NB>(x, l, umask, urow, u, lim);
-            }
-            if (hb && pb > jj) {
-                const T l = y[u] * rp;
-                y[u] = l;
-                reg2_update<T, NB>(y, l, umask, urow, u, lim);
-            }
+            const bool ux = ha && pa > jj, uy = hb && pb > jj;
+            const T lx = x[u] * rp, ly = y[u] * rp;
+            if (ux) x[u] = lx;
+            if (uy) y[u] = ly;
+            reg2_update<T, NB>(x, lx, ux, y, ly, uy, urow, u, lim);
         }
         if (s_abort) break;
         if (jb + kRegBlock < nb) {
