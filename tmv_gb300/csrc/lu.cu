@@ -356,7 +356,8 @@ lu_panel_cluster_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, in
 // does after its pulls of the column before.  The waits are bounded: on a
 // timeout the CTA records kDevTimeout and stops, and the others time out in
 // turn.  Used while a 16-CTA cluster covers the panel's rows with two rows
-// per thread (m <= 16 * 512); a panel of at most 256 rows runs in one CTA.
+// per thread (m <= 16 * 512); a panel of at most 512 rows runs in one CTA,
+// which takes its own candidate with no exchange.
 // ---------------------------------------------------------------------
 constexpr int kRegBlock = 4;
 
@@ -630,42 +631,57 @@ lu_panel_cluster_reg2_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t 
             else if (hb && pb == jj) store_row<T, NB>(pub_diag[par], y);
             __syncthreads();
             if (warp == 0) {
-                // 2. publish this CTA's candidate, store its record into every
-                //    CTA and arrive there (release)
+                // 2. this CTA's candidate
                 bk = lane < kReg2Warps ? s_key[lane] : 0ull;
                 bi = lane < kReg2Warps ? s_idx[lane] : INT_MAX;
                 reg_key_reduce<T>(bk, bi);
-                if (bi != INT_MAX && lane < 16)
-                    reinterpret_cast<uint4*>(pub_row[par])[lane] =
-                        reinterpret_cast<const uint4*>(warp_row[((bi - r0) & (kReg2Threads - 1)) >> 5])[lane];
-                __syncwarp();
-                if (lane < G) {
-                    st_cluster16(cluster_addr(&slot[par][cta], lane),
-                                 make_uint4((unsigned)bk, (unsigned)(bk >> 32), (unsigned)bi, 0u));
-                    mbar_arrive_remote_release(cluster_addr(&mbar[par], lane));
-                }
-                // 3. wait for every CTA's record (bounded), reduce, pull rows
-                const bool got = __all_sync(0xffffffffu, mbar_wait_cluster(&mbar[par], (uint32_t)((jj >> 1) & 1)));
-                if (!got) {
-                    if (lane == 0) {
-                        s_abort = 1;
-                        atomicCAS(err, (int)kDevOk, (int)kDevTimeout);
+                if (G == 1) {
+                    // one CTA: its candidate is the pivot, taken without the
+                    // cluster exchange
+                    if (lane == 0) { s_wk = bk; s_wi = bi; }
+                    if (!reg_key_underflows<T>(bk)) {
+                        if (lane < 16)
+                            reinterpret_cast<uint4*>(urow)[lane] = reinterpret_cast<const uint4*>(
+                                warp_row[((bi - r0) & (kReg2Threads - 1)) >> 5])[lane];
+                        else if (bi != jj)
+                            reinterpret_cast<uint4*>(drow)[lane - 16] =
+                                reinterpret_cast<const uint4*>(pub_diag[par])[lane - 16];
                     }
                 } else {
-                    const uint4 mt = lane < G ? slot[par][lane] : make_uint4(0u, 0u, (unsigned)INT_MAX, 0u);
-                    unsigned long long wk = ((unsigned long long)mt.y << 32) | mt.x;
-                    int wi = (int)mt.z;
-                    reg_key_reduce<T>(wk, wi);
-                    if (lane == 0) { s_wk = wk; s_wi = wi; }
-                    if (!reg_key_underflows<T>(wk)) {
-                        // the winning record's lane is the CTA that holds row wi
-                        const int owner_w = __ffs(__ballot_sync(0xffffffffu, lane < G && (int)mt.z == wi)) - 1;
-                        if (lane < 16)
-                            reinterpret_cast<uint4*>(urow)[lane] =
-                                ld_cluster16(cluster_addr(&pub_row[par][0], owner_w) + 16 * lane);
-                        else if (cta == owner_w && wi != jj)
-                            reinterpret_cast<uint4*>(drow)[lane - 16] =
-                                ld_cluster16(cluster_addr(&pub_diag[par][0], owner_j) + 16 * (lane - 16));
+                    // publish it, store its record into every CTA and arrive
+                    // there (release)
+                    if (bi != INT_MAX && lane < 16)
+                        reinterpret_cast<uint4*>(pub_row[par])[lane] =
+                            reinterpret_cast<const uint4*>(warp_row[((bi - r0) & (kReg2Threads - 1)) >> 5])[lane];
+                    __syncwarp();
+                    if (lane < G) {
+                        st_cluster16(cluster_addr(&slot[par][cta], lane),
+                                     make_uint4((unsigned)bk, (unsigned)(bk >> 32), (unsigned)bi, 0u));
+                        mbar_arrive_remote_release(cluster_addr(&mbar[par], lane));
+                    }
+                    // 3. wait for every CTA's record (bounded), reduce, pull rows
+                    const bool got = __all_sync(0xffffffffu, mbar_wait_cluster(&mbar[par], (uint32_t)((jj >> 1) & 1)));
+                    if (!got) {
+                        if (lane == 0) {
+                            s_abort = 1;
+                            atomicCAS(err, (int)kDevOk, (int)kDevTimeout);
+                        }
+                    } else {
+                        const uint4 mt = lane < G ? slot[par][lane] : make_uint4(0u, 0u, (unsigned)INT_MAX, 0u);
+                        unsigned long long wk = ((unsigned long long)mt.y << 32) | mt.x;
+                        int wi = (int)mt.z;
+                        reg_key_reduce<T>(wk, wi);
+                        if (lane == 0) { s_wk = wk; s_wi = wi; }
+                        if (!reg_key_underflows<T>(wk)) {
+                            // the winning record's lane is the CTA that holds row wi
+                            const int owner_w = __ffs(__ballot_sync(0xffffffffu, lane < G && (int)mt.z == wi)) - 1;
+                            if (lane < 16)
+                                reinterpret_cast<uint4*>(urow)[lane] =
+                                    ld_cluster16(cluster_addr(&pub_row[par][0], owner_w) + 16 * lane);
+                            else if (cta == owner_w && wi != jj)
+                                reinterpret_cast<uint4*>(drow)[lane - 16] =
+                                    ld_cluster16(cluster_addr(&pub_diag[par][0], owner_j) + 16 * (lane - 16));
+                        }
                     }
                 }
             }
@@ -1431,10 +1447,10 @@ static tmvg_status launch_panel_cluster_reg(Context* c, cudaStream_t s, T* A, in
                                             int64_t k, int nb, int64_t* P, const unsigned char* modes,
                                             int* pairs, float* ahi, float* alo)
 {
-    // two rows per thread in 16 CTAs; a panel of at most 256 rows in one CTA
-    // (no cluster exchange; faster there, measured)
+    // two rows per thread in 16 CTAs; a panel of at most 512 rows in one CTA
+    // (no cluster exchange)
     const int64_t m = n - k;
-    const int G = m <= kReg2Threads ? 1 : kClusterCtas;
+    const int G = m <= 2 * kReg2Threads ? 1 : kClusterCtas;
     const int rpc = (int)ceil_div(m, G);
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
