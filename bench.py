@@ -545,13 +545,17 @@ def e2e_host(args, Acm, B, n, nrhs, mixed=False) -> dict:
                            C.c_void_p(hB.data_ptr()), C.c_void_p(hX.data_ptr()), None, None))
     call()
     steps = max(1, min(args.steps, 5))
+    per_call = []
     t0 = time.perf_counter()
     for _ in range(steps):
-        call()
+        t1 = time.perf_counter()
+        call()  # synchronous: returns after X is back in host memory
+        per_call.append((time.perf_counter() - t1) * 1e3)
     dt = (time.perf_counter() - t0) / steps
     return {"value": round(lu_solve_flops(n, nrhs) / dt / 1e12, 4), "unit": "TFLOP/s",
             "h2d_bytes_per_step": 8 * n * n + 8 * n * nrhs, "d2h_bytes_per_step": 8 * n * nrhs,
-            "ms_per_step": round(dt * 1e3, 3), "steps": steps}
+            "ms_per_step": round(dt * 1e3, 3), "steps": steps,
+            "ms_per_call": [round(t, 3) for t in per_call]}
 
 
 def other_workloads(dev, with_cpu: bool) -> dict:
