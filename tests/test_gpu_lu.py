@@ -180,6 +180,47 @@ def test_ldiveq_rdiveq_vs_oracle(dev, orc, n, nrhs):
     assert rel_frob(to_host(Y), y_o) <= 1e-12
 
 
+@pytest.mark.parametrize("n", [65, 130, 300, 1000])
+def test_arbitrary_pivot_vectors(dev, orc, n):
+    """LU_LDivEq / LU_RDivEq with pivot vectors no factorisation produces:
+    pivots above their row (P[i] < i), repeated targets, jumps across the
+    64-row chunks the interchange -> permutation conversion cuts the swaps
+    into. The swaps are TMV's (src/TMV_Permutation.cpp swap(i, P[i]) in
+    order); checked against the oracle and against numpy applying them."""
+    import torch
+
+    from tmv_gb300 import linalg
+
+    rng = np.random.default_rng(900 + n)
+    lu = np.tril(rng.standard_normal((n, n)), -1) * (0.5 / np.sqrt(n))
+    lu += np.triu(rng.standard_normal((n, n)) * (0.5 / np.sqrt(n)), 1) + np.diag(2.0 + rng.random(n))
+    p = np.array([rng.integers(0, n) if i % 3 else min(n - 1, i + 64 * (i % 5)) for i in range(n)],
+                 dtype=np.int64)
+    p[n // 2:n // 2 + 10] = n - 1  # one row chosen again and again
+    b = rng.standard_normal((n, 3))
+    x_o = np.asfortranarray(b.copy())
+    orc.ldiveq(np.asfortranarray(lu), p, x_o)
+    # numpy: x = U^-1 L^-1 (rows of b swapped in order)
+    pb = b.copy()
+    for i in range(n):
+        pb[[i, p[i]]] = pb[[p[i], i]]
+    L = np.tril(lu, -1) + np.eye(n)
+    x_np = np.linalg.solve(np.triu(lu), np.linalg.solve(L, pb))
+    assert rel_frob(x_o, x_np) <= 1e-12
+    LU = to_dev(lu, dev, "F")
+    P = torch.from_numpy(p).to(dev)
+    X = to_dev(b, dev, "F")
+    linalg.lu_ldiveq(LU, P, X)
+    w = rng.standard_normal((2, n))
+    y_o = np.asfortranarray(w.copy())
+    orc.rdiveq(np.asfortranarray(lu), p, y_o)
+    Y = to_dev(w, dev, "F")
+    linalg.lu_rdiveq(LU, P, Y)
+    torch.cuda.synchronize()
+    assert rel_frob(to_host(X), x_o) <= 1e-12
+    assert rel_frob(to_host(Y), y_o) <= 1e-12
+
+
 def test_config2_lu_solve_4096(dev, orc):
     # FP64 LU factor + solve, n = 4096, N(0,1) + 4 sqrt(n) I, 8 RHS:
     # pivots identical to the oracle, solution within 1e-12 relative error.

@@ -52,6 +52,7 @@ static void* grow(Context* c, void*& buf, size_t& have, size_t bytes)
 void* workspace(Context* c, size_t bytes) { return grow(c, c->work, c->work_bytes, bytes); }
 void* workspace2(Context* c, size_t bytes) { return grow(c, c->work2, c->work2_bytes, bytes); }
 void* workspace3(Context* c, size_t bytes) { return grow(c, c->work3, c->work3_bytes, bytes); }
+void* perm_lists_buffer(Context* c, size_t bytes) { return grow(c, c->perm_lists, c->perm_lists_bytes, bytes); }
 
 static cudaEvent_t pooled_event(Context* c)
 {
@@ -347,6 +348,7 @@ tmvg_status tmvg_destroy(tmvg_handle h)
     if (c->work2) cudaFree(c->work2);
     if (c->work3) cudaFree(c->work3);
     if (c->io) cudaFree(c->io);
+    if (c->perm_lists) cudaFree(c->perm_lists);
     if (c->trsv_flags) cudaFree(c->trsv_flags);
     if (c->trsv_pub) cudaFree(c->trsv_pub);
     if (c->dflags) cudaFree(c->dflags);

@@ -82,6 +82,10 @@ struct Context {
     // Device copies of the host entry points' operands (grow-only).
     void* io = nullptr;
     size_t io_bytes = 0;
+    // Row-gather lists of the interchange -> permutation conversion
+    // (grow-only; its callers keep the permutation in `work`).
+    void* perm_lists = nullptr;
+    size_t perm_lists_bytes = 0;
     // Kernel-class timing (off unless tmvg_timing_enable turned it on):
     // spans recorded but not yet read, recycled events, and per-class sums.
     bool timing = false;
@@ -130,6 +134,7 @@ tmvg_status check_cuda(Context* c, cudaError_t e, const char* what);
 void* workspace(Context* c, size_t bytes);
 void* workspace2(Context* c, size_t bytes);
 void* workspace3(Context* c, size_t bytes);
+void* perm_lists_buffer(Context* c, size_t bytes);
 // Reads and clears the device error word (synchronises the stream).
 tmvg_status collect_device_error(Context* c, const char* what);
 

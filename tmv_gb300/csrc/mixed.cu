@@ -31,7 +31,15 @@ __device__ __forceinline__ void atomic_max_abs(unsigned long long* dst, double v
     atomicMax(dst, (unsigned long long)__double_as_longlong(fabs(v)));
 }
 
-// As = (float) A, and per-row partial sums of |A| over column chunks.
+// As = (float) A, and per-row partial sums of |A| over column chunks.  The
+// sums are taken in FP32 over the converted values (two accumulators of 128
+// terms): FP64 additions run at 1/64 of the FP32 rate on this part, and an
+// FP64 sum per element made this pass FP64-bound (261 us at n = 8192 against
+// 131 us, 91 % of the HBM copy rate, with FP32 sums).  Their relative error
+// is below 2e-5; each partial is scaled down by (1 - 2^-12) so that ||A||_inf
+// never comes out larger than it is and the backward error the refinement
+// tests against (|r| / (||A|| ||x|| + ||b||)) never smaller.  A chunk whose
+// FP32 sum overflows is summed again in FP64.
 __global__ void prep_kernel(int64_t n, const double* __restrict__ A, int64_t lda,
                             float* __restrict__ As, int64_t ldas, double* __restrict__ rowpart)
 {
@@ -39,13 +47,28 @@ __global__ void prep_kernel(int64_t n, const double* __restrict__ A, int64_t lda
     const int64_t c0 = (int64_t)blockIdx.y * kChunk;
     if (i >= n) return;
     const int64_t c1 = min(n, c0 + kChunk);
-    double s = 0.0;
-    for (int64_t c = c0; c < c1; ++c) {
-        const double v = A[i + c * lda];
-        As[i + c * ldas] = (float)v;
-        s += fabs(v);
+    float s0 = 0.f, s1 = 0.f;
+    int64_t c = c0;
+    for (; c + 2 <= c1; c += 2) {
+        const float v0 = (float)A[i + c * lda], v1 = (float)A[i + (c + 1) * lda];
+        As[i + c * ldas] = v0;
+        As[i + (c + 1) * ldas] = v1;
+        s0 += fabsf(v0);
+        s1 += fabsf(v1);
     }
-    rowpart[blockIdx.y * n + i] = s;
+    if (c < c1) {
+        const float v = (float)A[i + c * lda];
+        As[i + c * ldas] = v;
+        s0 += fabsf(v);
+    }
+    double sum = ((double)s0 + (double)s1) * (1.0 - 0x1p-12);
+    if (!isfinite(s0 + s1)) {
+        // an FP32 sum that overflowed (entries near the FP32 limit), or a
+        // NaN: the chunk again in FP64
+        sum = 0.0;
+        for (c = c0; c < c1; ++c) sum += fabs(A[i + c * lda]);
+    }
+    rowpart[blockIdx.y * n + i] = sum;
 }
 
 // ||A||_inf = max_i sum_chunks rowpart[chunk][i]

@@ -13,9 +13,10 @@ constexpr int kPairsPanelMax = 128;
 // swap(row k+t, row piv[t]) for t = 0..nb-1 in order moves row src[q] to
 // row dst[q] for at most 2*nb pairs; only rows k..k+nb-1 and the pivot rows
 // change.  One warp replays the swaps on row labels in shared memory: the
-// panel block [k, k+nb) is an array, rows outside it (only ever pivot rows)
-// live in a short list searched with a ballot.  pairs[0] = count, then the
-// dst and src arrays of kMaxPairs each.
+// panel block [k, k+nb) is an array, rows outside it (only ever pivot rows;
+// a pivot row above the block, which no factorisation produces, is handled
+// the same way) live in a short list searched with a ballot.  pairs[0] =
+// count, then the dst and src arrays of kMaxPairs each.
 // ---------------------------------------------------------------------
 constexpr int kMaxPairs = 2 * kPairsPanelMax;
 
@@ -32,7 +33,7 @@ __device__ inline void panel_row_pairs(int64_t k, int nb, const int* piv, int* p
         const int p = piv[t];
         const int i = (int)(k + t);
         if (p != i) {
-            if (p < k + nb) {
+            if (p >= k && p < k + nb) {
                 if (lane == 0) {
                     const int a = blk[t];
                     blk[t] = blk[p - k];

@@ -16,6 +16,7 @@
 // column-oriented vector solve (src/TMV_TriDiv_V.cpp:148-236, 322-398):
 // x_i = b_i - sum_j T_ij x_j over j in dependency order.
 #include "trsv.cuh"
+#include "pivots.cuh"
 
 #include <type_traits>
 
@@ -601,66 +602,94 @@ template tmvg_status trsv_with_inverse_blocks<double>(Context*, int64_t, const d
 
 // ---------------------------------------------------------------------
 // Interchanges -> gather permutation: perm = identity, then for i in order
-// swap(perm[i], perm[P[i]]); row i of P*B is row perm[i] of B.  One CTA,
-// sequential in shared memory (n <= kPermSmemMax).
+// swap(perm[i], perm[P[i]]) (a P[i] outside [0, n) is skipped); row i of
+// P*B is row perm[i] of B.  The swaps are cut into chunks of kPermChunk: a
+// chunk [k, k+64) moves only rows k..k+63 and its pivot rows, so one 32-thread
+// CTA per chunk turns its swaps into a row gather of at most 128 pairs
+// (panel_row_pairs), all chunks at once; then one CTA applies the gathers in
+// chunk order to the permutation, in shared memory (n <= kPermSmemMax) or in
+// global memory.  The sequential form costs a dependent shared-memory round
+// trip per swap (about 330 us at n = 8192); this one about a chunk's.
 // ---------------------------------------------------------------------
-constexpr int kPermSmemMax = 24576;
+constexpr int kPermChunk = 64;
+constexpr int kPermListInts = 1 + 2 * kMaxPairs;  // one chunk's list: count, dst[], src[]
+constexpr int kPermChunkPairs = 2 * kPermChunk;    // most pairs a chunk can have
+constexpr int kPermStage = 16;                     // chunk lists staged in shared memory at once
+constexpr int kPermThreads = 128;
+constexpr int kPermSmemMax = 49152;
+static_assert(kPermChunkPairs <= kPermThreads, "a thread per pair");
 
-__global__ void pivots_to_perm_kernel(int64_t n, const int64_t* __restrict__ P, int* __restrict__ perm)
+__global__ void __launch_bounds__(32) perm_chunk_pairs_kernel(int64_t n, const int64_t* __restrict__ P,
+                                                              int* __restrict__ lists)
 {
-    extern __shared__ int sp[];  // perm (n) then P as int (n)
-    int* sP = sp + n;
-    for (int64_t t = threadIdx.x; t < n; t += blockDim.x) {
-        sp[t] = (int)t;
-        sP[t] = (int)P[t];
+    __shared__ int piv[kPermChunk];
+    const int64_t k = (int64_t)blockIdx.x * kPermChunk;
+    const int nb = (int)min((int64_t)kPermChunk, n - k);
+    for (int t = threadIdx.x; t < nb; t += 32) {
+        const int64_t p = P[k + t];
+        piv[t] = (p >= 0 && p < n) ? (int)p : (int)(k + t);
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int64_t i = 0; i < n; ++i) {
-            const int p = sP[i];
-            if (p != i && p >= 0 && p < n) {
-                const int a = sp[i];
-                sp[i] = sp[p];
-                sp[p] = a;
-            }
+    __syncwarp();
+    panel_row_pairs(k, nb, piv, lists + (int64_t)blockIdx.x * kPermListInts);
+}
+
+__global__ void __launch_bounds__(kPermThreads) perm_apply_kernel(int64_t n, int nchunks,
+                                                                  const int* __restrict__ lists,
+                                                                  int* __restrict__ perm, bool in_smem)
+{
+    extern __shared__ int sy[];  // the permutation, when it fits
+    __shared__ int st_cnt[kPermStage];
+    __shared__ int st_dst[kPermStage][kPermChunkPairs];
+    __shared__ int st_src[kPermStage][kPermChunkPairs];
+    int* y = in_smem ? sy : perm;
+    const int tid = threadIdx.x;
+    for (int64_t t = tid; t < n; t += kPermThreads) y[t] = (int)t;
+    for (int b0 = 0; b0 < nchunks; b0 += kPermStage) {
+        const int nst = min(kPermStage, nchunks - b0);
+        __syncthreads();  // the previous stage is applied (and y initialised)
+        for (int e = tid; e < nst * kPermChunkPairs; e += kPermThreads) {
+            const int b = e / kPermChunkPairs, q = e % kPermChunkPairs;
+            const int* L = lists + (int64_t)(b0 + b) * kPermListInts;
+            st_dst[b][q] = L[1 + q];
+            st_src[b][q] = L[1 + kMaxPairs + q];
+        }
+        if (tid < nst) st_cnt[tid] = lists[(int64_t)(b0 + tid) * kPermListInts];
+        __syncthreads();
+        for (int b = 0; b < nst; ++b) {
+            const int np = st_cnt[b];
+            const int v = tid < np ? y[st_src[b][tid]] : 0;
+            __syncthreads();
+            if (tid < np) y[st_dst[b][tid]] = v;
+            __syncthreads();
         }
     }
-    __syncthreads();
-    for (int64_t t = threadIdx.x; t < n; t += blockDim.x) perm[t] = sp[t];
+    if (in_smem) {
+        __syncthreads();
+        for (int64_t t = tid; t < n; t += kPermThreads) perm[t] = sy[t];
+    }
 }
 
 tmvg_status pivots_to_perm(Context* c, int64_t n, const int64_t* P, int* perm)
 {
     if (n <= 0) return TMVG_OK;
-    if (n <= kPermSmemMax) {
-        const size_t smem = sizeof(int) * 2 * (size_t)n;
-        if (smem > 48 * 1024)
-            cudaFuncSetAttribute(pivots_to_perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(sizeof(int) * 2 * kPermSmemMax));
-        pivots_to_perm_kernel<<<1, 1024, smem, c->stream>>>(n, P, perm);
-        ++c->launches;
-        return check_cuda(c, cudaGetLastError(), "perm launch");
-    }
-    // large n: compose on the host
-    std::vector<int64_t> hp((size_t)n);
-    std::vector<int> hperm((size_t)n);
-    tmvg_status st = check_cuda(
-        c, cudaMemcpyAsync(hp.data(), P, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, c->stream),
-        "perm: P d2h");
+    if (n > (int64_t)INT32_MAX) return set_error(c, TMVG_UNSUPPORTED, "perm: n too large");
+    const int64_t nchunks = ceil_div(n, kPermChunk);
+    int* lists = (int*)perm_lists_buffer(c, sizeof(int) * (size_t)nchunks * kPermListInts);
+    if (!lists) return TMVG_OOM;
+    perm_chunk_pairs_kernel<<<(unsigned)nchunks, 32, 0, c->stream>>>(n, P, lists);
+    ++c->launches;
+    tmvg_status st = check_cuda(c, cudaGetLastError(), "perm: chunk launch");
     if (st) return st;
-    st = check_cuda(c, cudaStreamSynchronize(c->stream), "perm sync");
-    if (st) return st;
-    for (int64_t i = 0; i < n; ++i) hperm[i] = (int)i;
-    for (int64_t i = 0; i < n; ++i) {
-        const int64_t p = hp[i];
-        if (p != i && p >= 0 && p < n) std::swap(hperm[i], hperm[p]);
-    }
-    st = check_cuda(c,
-                    cudaMemcpyAsync(perm, hperm.data(), sizeof(int) * n, cudaMemcpyHostToDevice,
-                                    c->stream),
-                    "perm h2d");
-    if (st) return st;
-    return check_cuda(c, cudaStreamSynchronize(c->stream), "perm sync");
+    const bool in_smem = n <= kPermSmemMax;
+    const size_t smem = in_smem ? sizeof(int) * (size_t)n : 0;
+    // the staged lists take 16 KB of static shared memory beside the
+    // permutation: above 48 KB in all, the kernel must opt in
+    if (smem + sizeof(int) * (kPermStage * (2 * kPermChunkPairs + 1)) > 48 * 1024)
+        cudaFuncSetAttribute(perm_apply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(sizeof(int) * kPermSmemMax));
+    perm_apply_kernel<<<1, kPermThreads, smem, c->stream>>>(n, (int)nchunks, lists, perm, in_smem);
+    ++c->launches;
+    return check_cuda(c, cudaGetLastError(), "perm: apply launch");
 }
 
 // out[i, q] = in[perm[i], q] (forward) or out[perm[i], q] = in[i, q] (inverse).
