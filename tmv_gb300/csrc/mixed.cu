@@ -219,9 +219,7 @@ tmvg_status lu_solve_mixed(Context* c, int64_t n, const double* A, int64_t lda, 
     if ((st = launched("invperm"))) return st;
     // inverses of the 128 x 128 diagonal blocks of L and U, reused by every
     // solve of the refinement loop
-    st = trsv_factor_inverse_blocks<float>(c, n, As, 1, n, false, true, dinvL, singL);
-    if (st) return st;
-    st = trsv_factor_inverse_blocks<float>(c, n, As, 1, n, true, false, dinvU, singU);
+    st = trsv_lu_inverse_blocks<float>(c, n, As, n, dinvL, singL, dinvU, singU);
     if (st) return st;
     // one triangular solve reads its triangle, the inverted diagonal blocks
     // and the vector (in and out)

@@ -215,52 +215,74 @@ tmvg_status trsm_sync_free(Context* c, int64_t n, const T* tri, int64_t tsi, int
 // ---------------------------------------------------------------------
 constexpr int kIB = 128;  // block rows of the inverse-diagonal solve
 
+// One triangle's diagonal blocks to invert: D = the lower triangle at tri
+// with strides (tsi, tsj) (an upper triangle is passed reversed), the
+// inverses to dinv, the zero-diagonal flags to singular.
+template <typename T>
+struct InvBlocksJob {
+    const T* tri;
+    int64_t tsi, tsj;
+    bool unit;
+    T* dinv;
+    int* singular;
+};
+
 // One CTA per diagonal block: Dinv_b = D_b^-1 (lower, column-major kIB x kIB
-// at dinv + b*kIB*kIB).  singular[b] = 1 if D_b has a zero diagonal.
+// at dinv + b*kIB*kIB).  singular[b] = 1 if D_b has a zero diagonal.  Blocks
+// [0, nblk) are job 0's, [nblk, 2 nblk) job 1's (the two triangles of one
+// factor in one launch).  Column j of the inverse by forward substitution in
+// thread j; the diagonal's reciprocals are taken once per block.
 template <typename T>
 __global__ void __launch_bounds__(kIB)
-invert_diag_blocks_kernel(int64_t n, const T* __restrict__ tri, int64_t tsi, int64_t tsj,
-                          bool unit, T* __restrict__ dinv, int* __restrict__ singular)
+invert_diag_blocks_kernel(int64_t n, int64_t nblk, InvBlocksJob<T> job0, InvBlocksJob<T> job1)
 {
     extern __shared__ __align__(16) unsigned char inv_smem[];
     T* D = reinterpret_cast<T*>(inv_smem);  // [kIB][kIB+1]
     T* X = D + kIB * (kIB + 1);              // [kIB][kIB+1], X[i][j] = (D^-1)_ij
+    __shared__ T rdiag[kIB];
     __shared__ int s_sing;
-    const int64_t b = blockIdx.x;
+    const bool second = blockIdx.x >= nblk;
+    const InvBlocksJob<T> job = second ? job1 : job0;
+    const int64_t b = second ? blockIdx.x - nblk : blockIdx.x;
     const int64_t r0 = b * kIB;
     const int rows = (int)min((int64_t)kIB, n - r0);
     const int tid = threadIdx.x;
     if (tid == 0) s_sing = 0;
     for (int t = tid; t < kIB * kIB; t += kIB) {
         const int i = t % kIB, j = t / kIB;
-        D[i * (kIB + 1) + j] = (i < rows && j <= i) ? tri[(r0 + i) * tsi + (r0 + j) * tsj] : T(0);
+        D[i * (kIB + 1) + j] = (i < rows && j <= i) ? job.tri[(r0 + i) * job.tsi + (r0 + j) * job.tsj] : T(0);
     }
     __syncthreads();
-    if (!unit && tid < rows && D[tid * (kIB + 1) + tid] == T(0)) s_sing = 1;
+    if (!job.unit && tid < rows && D[tid * (kIB + 1) + tid] == T(0)) s_sing = 1;
+    rdiag[tid] = (job.unit || tid >= rows) ? T(1) : T(1) / D[tid * (kIB + 1) + tid];
     __syncthreads();
     if (s_sing) {
-        if (tid == 0) singular[b] = 1;
+        if (tid == 0) job.singular[b] = 1;
         return;
     }
-    // column j of the inverse by forward substitution
     const int j = tid;
     if (j < rows) {
         for (int i = 0; i < j; ++i) X[i * (kIB + 1) + j] = T(0);
-        const T djj = unit ? T(1) : D[j * (kIB + 1) + j];
-        X[j * (kIB + 1) + j] = T(1) / djj;
+        X[j * (kIB + 1) + j] = rdiag[j];
         for (int i = j + 1; i < rows; ++i) {
-            T s = T(0);
-            for (int l = j; l < i; ++l) s -= D[i * (kIB + 1) + l] * X[l * (kIB + 1) + j];
-            X[i * (kIB + 1) + j] = unit ? s : s / D[i * (kIB + 1) + i];
+            const T* Di = D + i * (kIB + 1);
+            T s0 = T(0), s1 = T(0);
+            int l = j;
+            for (; l + 2 <= i; l += 2) {
+                s0 -= Di[l] * X[l * (kIB + 1) + j];
+                s1 -= Di[l + 1] * X[(l + 1) * (kIB + 1) + j];
+            }
+            if (l < i) s0 -= Di[l] * X[l * (kIB + 1) + j];
+            X[i * (kIB + 1) + j] = (s0 + s1) * rdiag[i];
         }
     }
     __syncthreads();
-    T* out = dinv + b * (int64_t)kIB * kIB;
+    T* out = job.dinv + b * (int64_t)kIB * kIB;
     for (int t = tid; t < kIB * kIB; t += kIB) {
         const int i = t % kIB, jj = t / kIB;
         out[t] = (i < rows && jj < rows) ? X[i * (kIB + 1) + jj] : T(0);
     }
-    if (tid == 0) singular[b] = 0;
+    if (tid == 0) job.singular[b] = 0;
 }
 
 template <typename T>
@@ -519,23 +541,47 @@ trsv_pub_kernel(int64_t n, const float* __restrict__ tri, int64_t tsi, int64_t t
 }
 
 template <typename T>
-tmvg_status trsv_factor_inverse_blocks(Context* c, int64_t n, const T* tri, int64_t tsi,
-                                       int64_t tsj, bool upper, bool unit, T* dinv, int* singular)
+static InvBlocksJob<T> inv_blocks_job(int64_t n, const T* tri, int64_t tsi, int64_t tsj, bool upper,
+                                      bool unit, T* dinv, int* singular)
 {
-    if (n <= 0) return TMVG_OK;
     if (upper) {
         tri = tri + (n - 1) * (tsi + tsj);
         tsi = -tsi;
         tsj = -tsj;
     }
+    return InvBlocksJob<T>{tri, tsi, tsj, unit, dinv, singular};
+}
+
+template <typename T>
+static tmvg_status launch_inv_blocks(Context* c, int64_t n, const InvBlocksJob<T>& j0,
+                                     const InvBlocksJob<T>& j1, int jobs)
+{
     const int64_t nblk = ceil_div(n, kIB);
     const size_t smem = sizeof(T) * 2 * kIB * (kIB + 1);
     cudaFuncSetAttribute(invert_diag_blocks_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
-    invert_diag_blocks_kernel<T><<<(unsigned)nblk, kIB, smem, c->stream>>>(n, tri, tsi, tsj, unit,
-                                                                            dinv, singular);
+    invert_diag_blocks_kernel<T><<<(unsigned)(jobs * nblk), kIB, smem, c->stream>>>(n, nblk, j0, j1);
     ++c->launches;
     return check_cuda(c, cudaGetLastError(), "invert diag launch");
+}
+
+template <typename T>
+tmvg_status trsv_factor_inverse_blocks(Context* c, int64_t n, const T* tri, int64_t tsi,
+                                       int64_t tsj, bool upper, bool unit, T* dinv, int* singular)
+{
+    if (n <= 0) return TMVG_OK;
+    const InvBlocksJob<T> j = inv_blocks_job<T>(n, tri, tsi, tsj, upper, unit, dinv, singular);
+    return launch_inv_blocks<T>(c, n, j, j, 1);
+}
+
+template <typename T>
+tmvg_status trsv_lu_inverse_blocks(Context* c, int64_t n, const T* LU, int64_t ld, T* dinvL,
+                                   int* singL, T* dinvU, int* singU)
+{
+    if (n <= 0) return TMVG_OK;
+    const InvBlocksJob<T> jl = inv_blocks_job<T>(n, LU, 1, ld, false, true, dinvL, singL);
+    const InvBlocksJob<T> ju = inv_blocks_job<T>(n, LU, 1, ld, true, false, dinvU, singU);
+    return launch_inv_blocks<T>(c, n, jl, ju, 2);
 }
 
 template <typename T>
@@ -589,6 +635,8 @@ tmvg_status trsv_with_inverse_blocks(Context* c, int64_t n, const T* tri, int64_
     return check_cuda(c, cudaGetLastError(), "trsv invdiag launch");
 }
 
+template tmvg_status trsv_lu_inverse_blocks<float>(Context*, int64_t, const float*, int64_t, float*,
+                                                   int*, float*, int*);
 template tmvg_status trsv_factor_inverse_blocks<float>(Context*, int64_t, const float*, int64_t,
                                                        int64_t, bool, bool, float*, int*);
 template tmvg_status trsv_factor_inverse_blocks<double>(Context*, int64_t, const double*, int64_t,

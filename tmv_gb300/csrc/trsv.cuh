@@ -23,6 +23,11 @@ constexpr int64_t kInvBlock = 128;
 template <typename T>
 tmvg_status trsv_factor_inverse_blocks(Context* c, int64_t n, const T* tri, int64_t tsi,
                                        int64_t tsj, bool upper, bool unit, T* dinv, int* singular);
+// Both triangles of a packed LU factor (column-major, leading dimension ld)
+// in one launch: unit lower L into (dinvL, singL), upper U into (dinvU, singU).
+template <typename T>
+tmvg_status trsv_lu_inverse_blocks(Context* c, int64_t n, const T* LU, int64_t ld, T* dinvL,
+                                   int* singL, T* dinvU, int* singU);
 template <typename T>
 tmvg_status trsv_with_inverse_blocks(Context* c, int64_t n, const T* tri, int64_t tsi, int64_t tsj,
                                      bool upper, bool unit, const T* dinv, const int* singular,
