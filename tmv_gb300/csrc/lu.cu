@@ -548,8 +548,10 @@ __global__ void __launch_bounds__(kReg2Threads, 1)
 lu_panel_cluster_reg2_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int nb,
                              int64_t* __restrict__ P, const unsigned char* __restrict__ modes,
                              int rows_per_cta, int* pairs, int* err, float* __restrict__ ahi,
-                             float* __restrict__ alo)
+                             float* __restrict__ alo, const T* __restrict__ Sp, int64_t lds)
 {
+    // Sp: the panel's columns come from this scratch panel (row i, column c
+    // at Sp[i + c lds]) instead of A
     static_assert(NB % kRegBlock == 0, "whole blocks");
     static_assert(NB * sizeof(T) == 256, "a row is 16 vectors of 16 bytes");
     namespace cg = cooperative_groups;
@@ -589,11 +591,13 @@ lu_panel_cluster_reg2_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t 
         mbar_fence_init();
     }
     for (int j = tid; j < nb; j += kReg2Threads) s_mode[j] = modes[j];
+    const T* Xp = Sp ? Sp : Ap;
+    const int64_t ldx = Sp ? lds : lda;
     T x[NB], y[NB];
 #pragma unroll
     for (int c = 0; c < NB; ++c) {
-        x[c] = (ha && c < nb) ? Ap[pa + c * lda] : T(0);
-        y[c] = (hb && c < nb) ? Ap[pb + c * lda] : T(0);
+        x[c] = (ha && c < nb) ? Xp[pa + c * ldx] : T(0);
+        y[c] = (hb && c < nb) ? Xp[pb + c * ldx] : T(0);
     }
     cluster.sync();  // every CTA's mbarriers are initialised before any arrival
 
@@ -971,6 +975,185 @@ u12_reg_kernel(int nb, const T* __restrict__ L, int64_t lda, T* __restrict__ A12
             }
         }
     }
+}
+
+// ---------------------------------------------------------------------
+// FP32 register path: the update of the next panel's columns [c0, c0+nc)
+// with step k (the "narrow" update on the chain between two panels) in one
+// kernel, out of place.  Each CTA takes kNarrowRows trailing rows:
+//   1. the step's row pairs give every row its source row (row r of the new
+//      columns is old row src(r));
+//   2. U12 = L11^-1 A12' for the gathered block rows k..k+63, solved in the
+//      CTA (64 threads, one column each, L11 transposed in shared memory;
+//      every CTA solves the same small block, which costs no more time than
+//      one);
+//   3. its rows: S = A(src(r), c0..) - L21(r, :) U12, FP32 FMAs (kNarrowRows/32
+//      rows x 8 columns per thread).
+// CTA 0 also writes U12.  The results go to the scratch panel S (row r at
+// S[(r - k) + c lds]) and not into A, because a row's source may be a row
+// another CTA overwrites; the next panel kernel reads its columns from S,
+// and U12 is copied into A on the main stream, off the chain.
+// ---------------------------------------------------------------------
+constexpr int kNarrowRows = 64;
+constexpr int kNarrowThreads = 256;
+constexpr int kNarrowNB = 64;  // the step's width: the FP32 register panel's
+constexpr int kNarrowXP = kNarrowNB + 4;
+constexpr size_t kNarrowSmem =
+    sizeof(float) * ((size_t)kNarrowNB * kNarrowNB + (size_t)kNarrowNB * kNarrowXP + (size_t)kNarrowRows * (kNarrowNB + 1));
+
+__global__ void __launch_bounds__(kNarrowThreads)
+narrow_update_f32_kernel(const float* __restrict__ A, int64_t lda, int64_t n, int64_t k, int64_t c0, int nc,
+                         const int* __restrict__ pairs, float* __restrict__ S, int64_t lds)
+{
+    constexpr int NB = kNarrowNB, XP = kNarrowXP;
+    using V = Vec16<float>;
+    extern __shared__ __align__(16) float nsm[];
+    float (*LsT)[NB] = reinterpret_cast<float (*)[NB]>(nsm);          // LsT[j][i] = L(i, j), i > j
+    float (*Us)[XP] = reinterpret_cast<float (*)[XP]>(nsm + NB * NB);  // Us[c][i]: column c of A12'
+    float (*UT)[XP] = Us;                                              // then UT[t][c] = U12(t, c)
+    float (*Ls)[NB + 1] = reinterpret_cast<float (*)[NB + 1]>(nsm + NB * NB + NB * XP);  // this CTA's L21 rows
+    __shared__ int s_dst[2 * NB], s_src[2 * NB];
+    __shared__ int map_blk[NB], map_row[kNarrowRows];
+    const int tid = threadIdx.x;
+    const int64_t r0 = k + NB + (int64_t)blockIdx.x * kNarrowRows;  // this CTA's first row
+    const int R = (int)min((int64_t)kNarrowRows, n - r0);
+    constexpr int RQ = kNarrowRows / 32;
+    const int rg = tid & 31, cg = tid >> 5;  // outputs: rows rg + 32 q (q < RQ), columns 8 cg + e
+    // loads that need no row map first (L11, this CTA's L21 rows), in flight
+    // together with the pair list; every load of a batch is issued before
+    // its values are stored
+    {
+        constexpr int QB = NB * NB / kNarrowThreads;           // 16
+        constexpr int QL = kNarrowRows * NB / kNarrowThreads;  // 32
+        float lv[QB], v[QL];
+#pragma unroll
+        for (int q = 0; q < QB; ++q) {
+            const int t = tid + q * kNarrowThreads;
+            const int i = t % NB, j = t / NB;
+            lv[q] = i > j ? A[(k + i) + (k + j) * lda] : 0.f;
+        }
+#pragma unroll
+        for (int q = 0; q < QL; ++q) {
+            const int t = tid + q * kNarrowThreads;
+            const int r = t % kNarrowRows, j = t / kNarrowRows;
+            v[q] = r < R ? A[(r0 + r) + (k + j) * lda] : 0.f;
+        }
+        const int np = min(pairs[0], 2 * NB);
+        if (tid < np) {
+            s_dst[tid] = pairs[1 + tid];
+            s_src[tid] = pairs[1 + kMaxPairs + tid];
+        }
+        if (tid < NB) map_blk[tid] = (int)(k + tid);
+        if (tid < kNarrowRows) map_row[tid] = (int)(r0 + tid);
+#pragma unroll
+        for (int q = 0; q < QB; ++q) {
+            const int t = tid + q * kNarrowThreads;
+            LsT[t / NB][t % NB] = lv[q];
+        }
+#pragma unroll
+        for (int q = 0; q < QL; ++q) {
+            const int t = tid + q * kNarrowThreads;
+            Ls[t % kNarrowRows][t / kNarrowRows] = v[q];
+        }
+        __syncthreads();
+        if (tid < np) {
+            const int64_t d = s_dst[tid];
+            if (d >= k && d < k + NB) map_blk[d - k] = s_src[tid];
+            else if (d >= r0 && d < r0 + R) map_row[d - r0] = s_src[tid];
+        }
+        __syncthreads();
+    }
+    // the gathered A12' and this thread's outputs (their source rows)
+    float acc[RQ][8];
+    {
+        constexpr int QB = NB * NB / kNarrowThreads;
+        float uv[QB];
+#pragma unroll
+        for (int q = 0; q < QB; ++q) {
+            const int t = tid + q * kNarrowThreads;
+            const int i = t % NB, j = t / NB;
+            uv[q] = j < nc ? A[map_blk[i] + (c0 + j) * lda] : 0.f;
+        }
+#pragma unroll
+        for (int q = 0; q < RQ; ++q)
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const int r = rg + 32 * q, cc = 8 * cg + e;
+                acc[q][e] = (r < R && cc < nc) ? A[map_row[r] + (c0 + cc) * lda] : 0.f;
+            }
+#pragma unroll
+        for (int q = 0; q < QB; ++q) {
+            const int t = tid + q * kNarrowThreads;
+            Us[t / NB][t % NB] = uv[q];
+        }
+    }
+    __syncthreads();
+    // U12 = L11^-1 A12', a column per thread; written transposed over the
+    // staged columns once every solving thread has read its own
+    float x[NB];
+    if (tid < nc) load_row<float, NB>(x, Us[tid]);
+    __syncthreads();
+    if (tid < nc) {
+#pragma unroll
+        for (int j = 0; j < NB - 1; ++j) {
+#pragma unroll
+            for (int v = (j + 1) / V::E; v < NB / V::E; ++v) {
+                const float4 lv = reinterpret_cast<const float4*>(LsT[j])[v];
+#pragma unroll
+                for (int e = 0; e < V::E; ++e) {
+                    const int i = v * V::E + e;
+                    if (i > j) x[i] -= V::get(lv, e) * x[j];
+                }
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < NB; ++i) UT[i][tid] = x[i];
+    } else if (tid < NB) {
+#pragma unroll
+        for (int i = 0; i < NB; ++i) UT[i][tid] = 0.f;
+    }
+    __syncthreads();
+    if (blockIdx.x == 0) {
+        // U12 into the scratch panel's first rows (copied into A later)
+        for (int t = tid; t < NB * nc; t += kNarrowThreads) {
+            const int i = t % NB, j = t / NB;
+            S[i + j * lds] = UT[i][j];
+        }
+    }
+#pragma unroll 4
+    for (int t = 0; t < NB; ++t) {
+        float l[RQ];
+#pragma unroll
+        for (int q = 0; q < RQ; ++q) l[q] = Ls[rg + 32 * q][t];
+        const float4 u0 = reinterpret_cast<const float4*>(&UT[t][8 * cg])[0];
+        const float4 u1 = reinterpret_cast<const float4*>(&UT[t][8 * cg])[1];
+        const float u[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
+#pragma unroll
+        for (int q = 0; q < RQ; ++q)
+#pragma unroll
+            for (int e = 0; e < 8; ++e) acc[q][e] = fmaf(-l[q], u[e], acc[q][e]);
+    }
+#pragma unroll
+    for (int q = 0; q < RQ; ++q)
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const int r = rg + 32 * q, cc = 8 * cg + e;
+            if (r < R && cc < nc) S[(r0 + r - k) + cc * lds] = acc[q][e];
+        }
+}
+
+static tmvg_status narrow_update_f32(Context* c, const float* A, int64_t lda, int64_t n, int64_t k, int64_t c0,
+                                     int nc, const int* pairs, float* S, int64_t lds)
+{
+    const int64_t rest = n - k - kNarrowNB;
+    const double fr = (double)rest, fc = (double)nc;
+    ScopedTimer timer(c, kClsTrailingUpdate, sizeof(float) * (2.0 * fr * fc + fr * kNarrowNB + kNarrowNB * fc),
+                      2.0 * fr * fc * kNarrowNB);
+    cudaFuncSetAttribute(narrow_update_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kNarrowSmem);
+    const unsigned grid = (unsigned)std::max<int64_t>(1, ceil_div(rest, kNarrowRows));
+    narrow_update_f32_kernel<<<grid, kNarrowThreads, kNarrowSmem, c->stream>>>(A, lda, n, k, c0, nc, pairs, S, lds);
+    ++c->launches;
+    return check_cuda(c, cudaGetLastError(), "lu: narrow update launch");
 }
 
 // General interchanges on a strided matrix (one thread per column).
@@ -1445,7 +1628,8 @@ static bool reg_panel_ok(Context* c)
 template <typename T>
 static tmvg_status launch_panel_cluster_reg(Context* c, cudaStream_t s, T* A, int64_t lda, int64_t n,
                                             int64_t k, int nb, int64_t* P, const unsigned char* modes,
-                                            int* pairs, float* ahi, float* alo)
+                                            int* pairs, float* ahi, float* alo, const T* Sp = nullptr,
+                                            int64_t lds = 0)
 {
     // two rows per thread in 16 CTAs; a panel of at most 512 rows in one CTA
     // (no cluster exchange)
@@ -1467,7 +1651,8 @@ static tmvg_status launch_panel_cluster_reg(Context* c, cudaStream_t s, T* A, in
     ++c->launches;
     return check_cuda(c,
                       cudaLaunchKernelEx(&cfg, lu_panel_cluster_reg2_kernel<T, RegPanel<T>::NB>, A,
-                                         lda, n, k, nb, P, modes, rpc, pairs, c->dflags, ahi, alo),
+                                         lda, n, k, nb, P, modes, rpc, pairs, c->dflags, ahi, alo, Sp,
+                                         lds),
                       "lu: register panel launch");
 }
 
@@ -1539,25 +1724,41 @@ tmvg_status lu_factor(Context* c, int64_t n, T* A, int64_t lda, int64_t* P)
         // step s+1 writes its L21 split while step s's update still reads.
         bool tc_any = false;
         Tf32x3Buffers arena[2] = {};
+        // FP32 register path: the narrow update writes the next panel's
+        // columns into a scratch panel (n x 64, double-buffered by step
+        // parity) that the panel kernel reads
+        T* Sbuf[2] = {nullptr, nullptr};
         if constexpr (std::is_same<T, float>::value) {
-            if (n - nbmax >= kTcMinRest && tf32x3_supported(nbmax)) {
-                const size_t part = ((size_t)n * nbmax * sizeof(float) + 255) & ~size_t(255);
-                unsigned char* w3 = (unsigned char*)workspace3(c, 6 * part);
+            const bool tc = n - nbmax >= kTcMinRest && tf32x3_supported(nbmax);
+            const bool fused = reg && nbmax == kNarrowNB;
+            const size_t part = ((size_t)n * nbmax * sizeof(float) + 255) & ~size_t(255);
+            const int nparts = (tc ? 6 : 0) + (fused ? 2 : 0);
+            if (nparts > 0) {
+                unsigned char* w3 = (unsigned char*)workspace3(c, nparts * part);
                 if (!w3) return TMVG_OOM;
-                for (int q = 0; q < 2; ++q) {
-                    arena[q].Bhi = (float*)w3;
-                    arena[q].Blo = (float*)(w3 + part);
-                    arena[q].Ahi = (float*)(w3 + (2 + 2 * q) * part);
-                    arena[q].Alo = (float*)(w3 + (3 + 2 * q) * part);
+                if (tc) {
+                    for (int q = 0; q < 2; ++q) {
+                        arena[q].Bhi = (float*)w3;
+                        arena[q].Blo = (float*)(w3 + part);
+                        arena[q].Ahi = (float*)(w3 + (2 + 2 * q) * part);
+                        arena[q].Alo = (float*)(w3 + (3 + 2 * q) * part);
+                    }
+                    tc_any = true;
                 }
-                tc_any = true;
+                if (fused) {
+                    Sbuf[0] = (T*)(w3 + (nparts - 2) * part);
+                    Sbuf[1] = (T*)(w3 + (nparts - 1) * part);
+                }
             }
         }
         auto tc_for = [&](int64_t kk, int w) {
             return tc_any && n - kk - w >= kTcMinRest && tf32x3_supported(w);
         };
         auto pairs_of = [&](int64_t step) { return pairs + (step & 1) * pairs_len; };
-        auto panel = [&](int64_t kk, int w, int64_t step) -> tmvg_status {
+        // from_scratch: the panel's columns are in the scratch panel of the
+        // step before (row r at Sbuf[(step - 1) & 1][r - (kk - nbmax)]),
+        // written by its fused narrow update
+        auto panel = [&](int64_t kk, int w, int64_t step, bool from_scratch = false) -> tmvg_status {
             ScopedTimer timer(c, kClsPanel, 2.0 * sizeof(T) * (n - kk) * w, panel_flops(n - kk, w), side);
             float* ahi = nullptr;
             float* alo = nullptr;
@@ -1566,8 +1767,12 @@ tmvg_status lu_factor(Context* c, int64_t n, T* A, int64_t lda, int64_t* P)
                 alo = arena[step & 1].Alo;
             }
             int* pp = pairs_of(step);
-            tmvg_status s2 = reg ? launch_panel_cluster_reg<T>(c, side, A, lda, n, kk, w, P, modes + kk, pp, ahi, alo)
-                                 : launch_panel_cluster<T>(c, side, A, lda, n, kk, w, P, modes + kk, pp);
+            tmvg_status s2 =
+                reg ? (from_scratch
+                           ? launch_panel_cluster_reg<T>(c, side, A, lda, n, kk, w, P, modes + kk, pp, ahi, alo,
+                                                         Sbuf[(step - 1) & 1] + nbmax, n)
+                           : launch_panel_cluster_reg<T>(c, side, A, lda, n, kk, w, P, modes + kk, pp, ahi, alo))
+                    : launch_panel_cluster<T>(c, side, A, lda, n, kk, w, P, modes + kk, pp);
             if (!s2 && c->serialize_lookahead) s2 = check_cuda(c, cudaStreamSynchronize(side), "lu: serialize");
             return s2;
         };
@@ -1602,19 +1807,33 @@ tmvg_status lu_factor(Context* c, int64_t n, T* A, int64_t lda, int64_t* P)
             // update, event ev_wide), then the next panel
             if (step > 0) st = check_cuda(c, cudaStreamWaitEvent(side, c->ev_wide, 0), "lu: wide wait");
             c->stream = side;
+            // the fused narrow update (FP32 register path, 64-wide step) writes
+            // the next panel's columns into Sp; otherwise they are updated in A
+            T* Sk = Sbuf[step & 1];
+            const bool fused = Sk != nullptr && nb == kNarrowNB;
             if constexpr (std::is_same<T, float>::value) {
                 // the register panel kernel writes the L21 split itself
                 if (!st && tc && !reg) st = tf32x3_split_a(c, rest, nb, A + (k + nb) + k * lda, lda, b);
+                if (!st && fused) st = narrow_update_f32(c, A, lda, n, k, k + nb, nb2, pk, Sk, n);
             }
-            if (!st) st = update_columns<T>(c, n, A, lda, k, nb, k + nb, nb2, tc, b, pk);
+            if (!st && !fused) st = update_columns<T>(c, n, A, lda, k, nb, k + nb, nb2, tc, b, pk);
             c->stream = main_stream;
             // the wide update starts after the narrow one, not beside it: the
             // narrow update, on the chain, gets the whole GPU
             if (!st) st = check_cuda(c, cudaEventRecord(c->ev_fork, side), "lu: narrow done");
             if (!st) st = check_cuda(c, cudaStreamWaitEvent(c->stream, c->ev_fork, 0), "lu: join");
-            if (!st) st = panel(k + nb, nb2, step + 1);
+            if (!st) st = panel(k + nb, nb2, step + 1, fused);
             if (!st) st = check_cuda(c, cudaEventRecord(c->ev_panel, side), "lu: panel event");
-            // main: everything else of step k, overlapping the next panel
+            // main: everything else of step k, overlapping the next panel;
+            // with the fused narrow update first its U12 (the scratch panel's
+            // first nb rows) into A: the next panel reads the scratch panel
+            // and writes only rows below these, and the scratch panel is
+            // reused two steps later, after this step's wide update
+            if (!st && fused)
+                st = check_cuda(c,
+                                cudaMemcpy2DAsync(A + k + (k + nb) * lda, sizeof(T) * lda, Sk, sizeof(T) * n,
+                                                  sizeof(T) * nb, nb2, cudaMemcpyDeviceToDevice, c->stream),
+                                "lu: U12 copy");
             if (!st) st = laswp_cols<T>(c, A, lda, 0, n, k, k + nb + nb2, pk);
             if (!st) st = update_columns<T>(c, n, A, lda, k, nb, k + nb + nb2, rest - nb2, tc, b);
             if (!st) st = check_cuda(c, cudaEventRecord(c->ev_wide, c->stream), "lu: wide event");
