@@ -117,9 +117,19 @@ __device__ void factor_one(int64_t n, int64_t r, T* __restrict__ A, T* __restric
     for (int64_t k0 = 0; k0 < n; k0 += PW) {
         const int w = (int)min((int64_t)PW, n - k0);
         const int m = (int)(n - k0);
-        for (int t = tid; t < m * w; t += kBatchThreads) {
-            const int rr = t % m, cc = t / m;
-            pan[rr * LDP + cc] = A[(k0 + rr) + (k0 + cc) * n];
+        // eight loads in flight per thread before their stores
+        for (int t0 = tid; t0 < m * w; t0 += kBatchThreads * 8) {
+            T v[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int t = t0 + q * kBatchThreads;
+                v[q] = t < m * w ? A[(k0 + t % m) + (k0 + t / m) * n] : T(0);
+            }
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int t = t0 + q * kBatchThreads;
+                if (t < m * w) pan[(t % m) * LDP + t / m] = v[q];
+            }
         }
         __syncthreads();
         for (int j = 0; j < w; ++j) {
@@ -226,6 +236,21 @@ __device__ void factor_one(int64_t n, int64_t r, T* __restrict__ A, T* __restric
                 for (int a = 0; a < 4; ++a)
 #pragma unroll
                     for (int b = 0; b < 4; ++b) acc[a][b] = T(0);
+                // FP32: the tile's C entries are loaded before the products,
+                // so their latency overlaps them (each C entry is this
+                // thread's alone, and the products read shared memory only)
+                float cv[4][4];
+                if constexpr (kStageU12<T>) {
+#pragma unroll
+                    for (int b = 0; b < 4; ++b) {
+                        const T* cp = A + (k0 + w) + (k0 + w + j0 + b) * n;
+#pragma unroll
+                        for (int a = 0; a < 4; ++a) {
+                            const int ra = iq + a * ti;
+                            cv[a][b] = (j0 + b < ncol && ra < m2) ? (float)cp[ra] : 0.f;
+                        }
+                    }
+                }
                 const T* u = A + k0 + (k0 + w + j0) * n;
                 for (int kk = 0; kk < w; ++kk) {
                     T av[4], bv[4];
@@ -253,7 +278,10 @@ __device__ void factor_one(int64_t n, int64_t r, T* __restrict__ A, T* __restric
 #pragma unroll
                     for (int a = 0; a < 4; ++a) {
                         const int ra = iq + a * ti;
-                        if (ra < m2) cp[ra] -= acc[a][b];
+                        if (ra < m2) {
+                            if constexpr (kStageU12<T>) cp[ra] = (T)cv[a][b] - acc[a][b];
+                            else cp[ra] -= acc[a][b];
+                        }
                     }
                 }
             }
