@@ -304,13 +304,29 @@ __device__ void lu_solve_staged(int64_t n, int64_t r, const T* __restrict__ LU, 
 {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     constexpr int DS = kSolveBlock + 1;
+    // factor entries a thread loads ahead of their (zero-skipping) use
+    constexpr int PF = sizeof(T) == 8 ? 8 : 16;
+    static_assert(kSolveBlock % PF == 0, "whole prefetch groups");
+    // the diagonal block into dg, eight loads in flight per thread
+    auto stage = [&](int j0, int jb) {
+        for (int t0 = tid; t0 < jb * jb; t0 += kBatchThreads * 8) {
+            T v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int t = t0 + u * kBatchThreads;
+                v[u] = t < jb * jb ? LU[(j0 + t % jb) + (int64_t)(j0 + t / jb) * n] : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int t = t0 + u * kBatchThreads;
+                if (t < jb * jb) dg[(t % jb) * DS + t / jb] = v[u];
+            }
+        }
+    };
         // forward: unit lower L
         for (int j0 = 0; j0 < n; j0 += kSolveBlock) {
             const int jb = (int)min((int64_t)kSolveBlock, n - j0);
-            for (int t = tid; t < jb * jb; t += kBatchThreads) {
-                const int i = t % jb, k = t / jb;
-                dg[i * DS + k] = LU[(j0 + i) + (int64_t)(j0 + k) * n];
-            }
+            stage(j0, jb);
             __syncthreads();
             if (warp == 0 && lane < r) {
                 T* xq = xs + lane * XS + j0;
@@ -327,9 +343,15 @@ __device__ void lu_solve_staged(int64_t n, int64_t r, const T* __restrict__ LU, 
                 const T* xq = xs + q * XS + j0;
                 const T* lc = LU + i + (int64_t)j0 * n;
                 T v = xs[q * XS + i];
-                for (int k = 0; k < jb; ++k) {
-                    const T xk = xq[k];
-                    if (xk != T(0)) v -= lc[(int64_t)k * n] * xk;
+                for (int k0 = 0; k0 < jb; k0 += PF) {
+                    T lv[PF];
+#pragma unroll
+                    for (int u = 0; u < PF; ++u) lv[u] = k0 + u < jb ? lc[(int64_t)(k0 + u) * n] : T(0);
+#pragma unroll
+                    for (int u = 0; u < PF; ++u) {
+                        const T xk = k0 + u < jb ? xq[k0 + u] : T(0);
+                        if (xk != T(0)) v -= lv[u] * xk;
+                    }
                 }
                 xs[q * XS + i] = v;
             }
@@ -338,10 +360,7 @@ __device__ void lu_solve_staged(int64_t n, int64_t r, const T* __restrict__ LU, 
         // backward: upper U, columns from the last
         for (int j1 = (int)n; j1 > 0; j1 -= kSolveBlock) {
             const int j0 = max(0, j1 - kSolveBlock), jb = j1 - j0;
-            for (int t = tid; t < jb * jb; t += kBatchThreads) {
-                const int i = t % jb, k = t / jb;
-                dg[i * DS + k] = LU[(j0 + i) + (int64_t)(j0 + k) * n];
-            }
+            stage(j0, jb);
             __syncthreads();
             if (warp == 0 && lane < r) {
                 T* xq = xs + lane * XS + j0;
@@ -362,9 +381,21 @@ __device__ void lu_solve_staged(int64_t n, int64_t r, const T* __restrict__ LU, 
                 const T* xq = xs + q * XS + j0;
                 const T* uc = LU + i + (int64_t)j0 * n;
                 T v = xs[q * XS + i];
-                for (int k = jb - 1; k >= 0; --k) {
-                    const T xk = xq[k];
-                    if (xk != T(0)) v -= uc[(int64_t)k * n] * xk;
+                // columns from the last, as before: groups of PF taken from
+                // the top of the block down
+                for (int kt = jb; kt > 0; kt -= PF) {
+                    T uv[PF];
+#pragma unroll
+                    for (int u = 0; u < PF; ++u) {
+                        const int k = kt - 1 - u;
+                        uv[u] = k >= 0 ? uc[(int64_t)k * n] : T(0);
+                    }
+#pragma unroll
+                    for (int u = 0; u < PF; ++u) {
+                        const int k = kt - 1 - u;
+                        const T xk = k >= 0 ? xq[k] : T(0);
+                        if (xk != T(0)) v -= uv[u] * xk;
+                    }
                 }
                 xs[q * XS + i] = v;
             }
