@@ -1208,20 +1208,43 @@ tri_diag_kernel(int w, const T* __restrict__ tri, int64_t tsi, int64_t tsj, bool
     const int64_t c0 = (int64_t)blockIdx.x * kTriCols;
     const int ncb = (int)min((int64_t)kTriCols, nrhs - c0);
 
-    for (int t = tid; t < w * w; t += kTriThreads) {
-        const int i = t % w, j = t / w;
-        const bool need = upper ? (j >= i) : (i >= j);
-        Ts(i, j) = need ? tri[i * tsi + j * tsj] : T(0);
-    }
-    if (bsi == 1) {
-        for (int t = tid; t < w * ncb; t += kTriThreads) {
-            const int i = t % w, cl = t / w;
-            Xs(i, cl) = B[i + (c0 + cl) * bsj];
+    // staging: eight loads in flight per thread before their stores
+    constexpr int QS = 8;
+    for (int t0 = tid; t0 < w * w; t0 += kTriThreads * QS) {
+        T v[QS];
+#pragma unroll
+        for (int u = 0; u < QS; ++u) {
+            const int t = t0 + u * kTriThreads;
+            const int i = t % w, j = t / w;
+            const bool need = t < w * w && (upper ? (j >= i) : (i >= j));
+            v[u] = need ? tri[i * tsi + j * tsj] : T(0);
         }
-    } else {
-        for (int t = tid; t < w * ncb; t += kTriThreads) {
-            const int cl = t % ncb, i = t / ncb;
-            Xs(i, cl) = B[i * bsi + (c0 + cl) * bsj];
+#pragma unroll
+        for (int u = 0; u < QS; ++u) {
+            const int t = t0 + u * kTriThreads;
+            if (t < w * w) Ts(t % w, t / w) = v[u];
+        }
+    }
+    for (int t0 = tid; t0 < w * ncb; t0 += kTriThreads * QS) {
+        T v[QS];
+#pragma unroll
+        for (int u = 0; u < QS; ++u) {
+            const int t = t0 + u * kTriThreads;
+            if (t < w * ncb) {
+                // a unit row step reads down the columns, otherwise along the rows
+                const int i = bsi == 1 ? t % w : t / ncb, cl = bsi == 1 ? t / w : t % ncb;
+                v[u] = B[i * bsi + (c0 + cl) * bsj];
+            } else {
+                v[u] = T(0);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < QS; ++u) {
+            const int t = t0 + u * kTriThreads;
+            if (t < w * ncb) {
+                const int i = bsi == 1 ? t % w : t / ncb, cl = bsi == 1 ? t / w : t % ncb;
+                Xs(i, cl) = v[u];
+            }
         }
     }
     __syncthreads();

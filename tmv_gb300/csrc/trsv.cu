@@ -248,9 +248,22 @@ invert_diag_blocks_kernel(int64_t n, int64_t nblk, InvBlocksJob<T> job0, InvBloc
     const int rows = (int)min((int64_t)kIB, n - r0);
     const int tid = threadIdx.x;
     if (tid == 0) s_sing = 0;
-    for (int t = tid; t < kIB * kIB; t += kIB) {
-        const int i = t % kIB, j = t / kIB;
-        D[i * (kIB + 1) + j] = (i < rows && j <= i) ? job.tri[(r0 + i) * job.tsi + (r0 + j) * job.tsj] : T(0);
+    // staged sixteen loads at a time per thread (column j = t / kIB of the
+    // block, row i = t % kIB = this thread)
+    constexpr int QS = 16;
+    for (int t0 = tid; t0 < kIB * kIB; t0 += kIB * QS) {
+        T v[QS];
+#pragma unroll
+        for (int u = 0; u < QS; ++u) {
+            const int t = t0 + u * kIB;
+            const int i = t % kIB, j = t / kIB;
+            v[u] = (i < rows && j <= i) ? job.tri[(r0 + i) * job.tsi + (r0 + j) * job.tsj] : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < QS; ++u) {
+            const int t = t0 + u * kIB;
+            D[(t % kIB) * (kIB + 1) + t / kIB] = v[u];
+        }
     }
     __syncthreads();
     if (!job.unit && tid < rows && D[tid * (kIB + 1) + tid] == T(0)) s_sing = 1;
@@ -695,11 +708,21 @@ __global__ void __launch_bounds__(kPermThreads) perm_apply_kernel(int64_t n, int
     for (int b0 = 0; b0 < nchunks; b0 += kPermStage) {
         const int nst = min(kPermStage, nchunks - b0);
         __syncthreads();  // the previous stage is applied (and y initialised)
-        for (int e = tid; e < nst * kPermChunkPairs; e += kPermThreads) {
-            const int b = e / kPermChunkPairs, q = e % kPermChunkPairs;
-            const int* L = lists + (int64_t)(b0 + b) * kPermListInts;
-            st_dst[b][q] = L[1 + q];
-            st_src[b][q] = L[1 + kMaxPairs + q];
+        // a stage's lists, every load of a thread issued before its stores
+        // (kPermChunkPairs == kPermThreads: a thread takes one pair slot of
+        // every chunk)
+        static_assert(kPermChunkPairs == kPermThreads, "one slot per thread and chunk");
+        int vd[kPermStage], vs[kPermStage];
+#pragma unroll
+        for (int b = 0; b < kPermStage; ++b) {
+            const int* L = lists + (int64_t)(b0 + (b < nst ? b : 0)) * kPermListInts;
+            vd[b] = L[1 + tid];
+            vs[b] = L[1 + kMaxPairs + tid];
+        }
+#pragma unroll
+        for (int b = 0; b < kPermStage; ++b) {
+            st_dst[b][tid] = vd[b];
+            st_src[b][tid] = vs[b];
         }
         if (tid < nst) st_cnt[tid] = lists[(int64_t)(b0 + tid) * kPermListInts];
         __syncthreads();
