@@ -515,6 +515,13 @@ def dominant_roofline(kernels: dict, mixed: bool) -> dict | None:
                 "traffic": (k["alg_bytes_per_span"] * ratio) if ratio else None,
                 "alg_per_launch": per, "ms_per_launch": k["ms_per_span"],
                 "share_of_step": k["share_of_step"]})
+    if cls == "panel":
+        # a panel launch is a chain of nb pivot decisions (FP32 register
+        # panel 64 columns wide, FP64 32), each a cluster-wide argmax and a
+        # pivot-row exchange: latency, not bandwidth or tensor throughput
+        cols = 64 if mixed else 32
+        out["limiter"] = (f"latency: {cols} sequential pivot decisions per launch, "
+                          f"{k['ms_per_span'] * 1e3 / cols:.2f} us each")
     return out
 
 
