@@ -95,6 +95,31 @@ class _Backend:
             raise RuntimeError(f"lu rc={rc}")
         return P
 
+    # complex<double>: column-major (Fortran-order) complex128 arrays
+    def lu_decompose_z(self, A: np.ndarray) -> np.ndarray:
+        """In place; returns P (int64)."""
+        assert A.dtype == np.complex128 and A.flags.f_contiguous and A.shape[0] == A.shape[1]
+        n = A.shape[0]
+        P = np.zeros(n, dtype=np.int64)
+        f = self._f("lu_decompose_z", C.c_int, [i64, vp, i64, vp])
+        rc = f(n, _p(A), n, _p(P))
+        if rc:
+            raise RuntimeError(f"lu_z rc={rc}")
+        return P
+
+    def ldiveq_z(self, LU: np.ndarray, P: np.ndarray, B: np.ndarray) -> None:
+        """B (n x nrhs, Fortran-order complex128) := (P L U)^-1 B in place."""
+        assert LU.dtype == np.complex128 and LU.flags.f_contiguous
+        assert B.dtype == np.complex128 and B.flags.f_contiguous
+        n = LU.shape[0]
+        nrhs = 1 if B.ndim == 1 else B.shape[1]
+        f = self._f("lu_ldiveq_z", C.c_int, [i64, vp, i64, vp, i64, vp, i64])
+        rc = f(n, _p(LU), n, _p(P), nrhs, _p(B), n)
+        if rc == SINGULAR:
+            raise OracleSingular("singular")
+        if rc:
+            raise RuntimeError(f"ldiveq_z rc={rc}")
+
     def ldiveq(self, LU: np.ndarray, P: np.ndarray, B: np.ndarray) -> None:
         n = LU.shape[0]
         Bv = B.reshape(n, -1) if B.ndim == 1 else B

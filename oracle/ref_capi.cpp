@@ -18,6 +18,9 @@
 //   tmvref_rdivide       X = B % m (LUDiv::doRDiv, src/TMV_LUD.cpp:122-130)
 //   tmvref_det           m.det(), m.logDet(&s) (src/TMV_LUD.cpp:132-190)
 //   tmvref_batched_divide  one B_i/A_i per system, OpenMP over systems.
+//   tmvref_lu_decompose_z, tmvref_lu_ldiveq_z  the same LU_Decompose and
+//                        LU_LDivEq for std::complex<double> (column-major,
+//                        interleaved entries).
 //
 // Status: 0 ok, 1 tmv::Singular thrown, 2 other tmv::Error, 3 other exception.
 
@@ -76,6 +79,26 @@ int tmvref_lu_decompose(ptrdiff_t n, double* A, ptrdiff_t sAi, ptrdiff_t sAj,
     return guarded([&] {
         tmv::MatrixView<double> Av = tmv::MatrixViewOf(A, n, n, sAi, sAj);
         tmv::LU_Decompose(Av, P);
+    });
+}
+
+int tmvref_lu_decompose_z(ptrdiff_t n, double* A, ptrdiff_t lda, ptrdiff_t* P)
+{
+    return guarded([&] {
+        typedef std::complex<double> Z;
+        tmv::MatrixView<Z> Av = tmv::MatrixViewOf(reinterpret_cast<Z*>(A), n, n, 1, lda);
+        tmv::LU_Decompose(Av, P);
+    });
+}
+
+int tmvref_lu_ldiveq_z(ptrdiff_t n, const double* LU, ptrdiff_t lda, const ptrdiff_t* P,
+                       ptrdiff_t nrhs, double* B, ptrdiff_t ldb)
+{
+    return guarded([&] {
+        typedef std::complex<double> Z;
+        tmv::ConstMatrixView<Z> LUv = tmv::MatrixViewOf(reinterpret_cast<const Z*>(LU), n, n, 1, lda);
+        tmv::MatrixView<Z> Bv = tmv::MatrixViewOf(reinterpret_cast<Z*>(B), n, nrhs, 1, ldb);
+        tmv::LU_LDivEq(LUv, P, Bv);
     });
 }
 

@@ -88,6 +88,12 @@ int oracle_batched_divide(ptrdiff_t count, const ptrdiff_t* n,
                           const ptrdiff_t* b_off, const double* A, double* B,
                           int* status);
 
+/* complex<double> (tmv_oracle_z.c): column-major, entries interleaved
+ * (re, im), leading dimensions in complex elements. */
+int oracle_lu_decompose_z(ptrdiff_t n, double* A, ptrdiff_t lda, ptrdiff_t* P);
+int oracle_lu_ldiveq_z(ptrdiff_t n, const double* LU, ptrdiff_t lda, const ptrdiff_t* P,
+                       ptrdiff_t nrhs, double* B, ptrdiff_t ldb);
+
 #ifdef __cplusplus
 }
 #endif

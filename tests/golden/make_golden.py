@@ -253,22 +253,49 @@ def multmv_tri(ref):
     np.savez_compressed(HERE / "multmv_tri.npz", **out)
 
 
-def main():
+def complex_lu(ref):
+    # LU_Decompose and LU_LDivEq for std::complex<double> as TMV computes
+    # them: seeded complex systems, and 3 x 3 cases for the pivot rule (TMV's
+    # modulus: a tie keeps the first index, a larger |re| + |im| with a
+    # smaller modulus loses; a zero column underflows)
+    rng = np.random.default_rng(20241203)
+    out = {}
+    for n in [1, 4, 17, 65]:
+        a = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+        b = rng.standard_normal((n, 2)) + 1j * rng.standard_normal((n, 2))
+        A = np.asfortranarray(a.copy())
+        P = ref.lu_decompose_z(A)
+        X = np.asfortranarray(b.copy())
+        ref.ldiveq_z(A, P, X)
+        out.update({f"a{n}": a, f"b{n}": b, f"LU{n}": A, f"P{n}": P, f"X{n}": X})
+    cases = [
+        [[3 + 4j, 1, 1 - 1j], [5 + 0j, 2, 2 - 2j], [0 + 5j, 3, 3 - 3j]],
+        [[1 + 1j, 1, 1 - 1j], [1.5 + 0j, 2, 2 - 2j], [0.1 + 0.1j, 3, 3 - 3j]],
+        [[0j, 1, 1 - 1j], [0j, 2, 2 - 2j], [0j, 3, 3 - 3j]],
+    ]
+    for q, c in enumerate(cases):
+        a = np.array(c, dtype=np.complex128)
+        A = np.asfortranarray(a.copy())
+        P = ref.lu_decompose_z(A)
+        out.update({f"s{q}": a, f"sLU{q}": A, f"sP{q}": P})
+    np.savez_compressed(HERE / "complex_lu.npz", **out)
+
+
+FIXTURES = [arith8, square4, decomp200, bign, random_lu, special, batched_small, inverse,
+            multmv_tri, complex_lu]
+
+
+def main(names: list[str]):
+    """Regenerates every fixture, or only those named on the command line."""
     if not oracle.ref_available():
         oracle.build_ref(str(REFERENCE))
     ref = oracle.ref()
-    arith8(ref)
-    square4(ref)
-    decomp200(ref)
-    bign(ref)
-    random_lu(ref)
-    special(ref)
-    batched_small(ref)
-    inverse(ref)
-    multmv_tri(ref)
+    for fx in FIXTURES:
+        if not names or fx.__name__ in names:
+            fx(ref)
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -180,3 +180,23 @@ def test_multmv_tri_fixtures(orc):
         assert rc == int(g[f"tri_{name}_rc"]), name
         if rc == 0:
             assert rel_frob(B, g[f"tri_{name}"]) <= 1e-14
+
+
+def test_complex_lu_fixtures(orc):
+    # TMV's own complex<double> LU_Decompose / LU_LDivEq (complex_lu.npz)
+    g = load("complex_lu.npz")
+    for n in [1, 4, 17, 65]:
+        a, b = g[f"a{n}"], g[f"b{n}"]
+        A = np.asfortranarray(a.copy())
+        P = orc.lu_decompose_z(A)
+        assert np.array_equal(P, g[f"P{n}"]), n
+        LU = g[f"LU{n}"]
+        assert np.abs(A - LU).max() <= 1e-12 * np.abs(LU).max(), n
+        X = np.asfortranarray(b.copy())
+        orc.ldiveq_z(A, P, X)
+        assert np.abs(X - g[f"X{n}"]).max() <= 1e-11 * np.abs(g[f"X{n}"]).max(), n
+    for q in range(3):
+        A = np.asfortranarray(g[f"s{q}"].copy())
+        P = orc.lu_decompose_z(A)
+        assert np.array_equal(P, g[f"sP{q}"])
+        np.testing.assert_array_equal(A, g[f"sLU{q}"])

@@ -136,3 +136,47 @@ def test_multmv_and_tri_ldiveq_match_tmv(orc, ref):
                         B2 = B1.copy(order="K")
                         assert orc.tri_ldiveq(upper, unit, T, B1) == ref.tri_ldiveq(upper, unit, T, B2) == 0
                         assert np.abs(B1 - B2).max() <= 1e-13 * max(np.abs(B2).max(), 1.0)
+
+
+@pytest.mark.parametrize("generic", [False, True])
+def test_complex_lu_and_solve_match_tmv(orc, generic):
+    # complex<double>: TMV's modulus for the pivot search, its guarded
+    # reciprocal for the scaling and the divisions; the block steps round
+    # differently from TMV's blocked complex product, so values to 1e-12
+    r = oracle.ref(generic=generic)
+    rng = np.random.default_rng(41)
+    for n in [1, 2, 3, 4, 5, 17, 64, 65, 130, 300]:
+        a = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+        A1, A2 = np.asfortranarray(a.copy()), np.asfortranarray(a.copy())
+        p1, p2 = orc.lu_decompose_z(A1), r.lu_decompose_z(A2)
+        assert np.array_equal(p1, p2), n
+        assert np.abs(A1 - A2).max() <= 1e-12 * np.abs(A2).max(), n
+        if n <= 3:  # the leaves alone: the same operations in the same order
+            assert np.array_equal(A1, A2), n
+        b = rng.standard_normal((n, 3)) + 1j * rng.standard_normal((n, 3))
+        x1, x2 = np.asfortranarray(b.copy()), np.asfortranarray(b.copy())
+        orc.ldiveq_z(A1, p1, x1)
+        r.ldiveq_z(A2, p2, x2)
+        scale = np.abs(a).sum(axis=1).max() * np.abs(x2).max()
+        assert np.abs(a @ x1 - b).max() <= 1e-13 * scale, n
+        assert np.abs(x1 - x2).max() <= 1e-11 * np.abs(x2).max(), n
+
+
+def test_complex_pivot_rule_and_special_entries(orc, ref):
+    # ties under TMV's modulus keep the first index; an entry whose |re| + |im|
+    # is larger but whose modulus is smaller loses; a zero column underflows
+    cases = [
+        np.array([[3 + 4j, 1], [5 + 0j, 2], [0 + 5j, 3]]),
+        np.array([[1 + 1j, 1], [1.5 + 0j, 2], [0.1 + 0.1j, 3]]),
+        np.array([[0j, 1], [0j, 2], [0j, 3]]),
+    ]
+    for c in cases:
+        m = c.shape[0]
+        a = np.zeros((m, m), dtype=np.complex128)
+        a[:, :2] = c
+        if m > 2:
+            a[:, 2] = np.arange(1, m + 1) * (1 - 1j)
+        A1, A2 = np.asfortranarray(a.copy()), np.asfortranarray(a.copy())
+        p1, p2 = orc.lu_decompose_z(A1), ref.lu_decompose_z(A2)
+        assert np.array_equal(p1, p2)
+        np.testing.assert_array_equal(A1, A2)
