@@ -236,6 +236,27 @@ tmvg_status tmvg_multmv_f64(tmvg_handle h, int add, double alpha, int64_t m,
                             const double* x, int64_t incx, double* y,
                             int64_t incy);
 
+/* ---- complex<double> LU ------------------------------------------------
+ * Device pointers; A, LU, B column-major with entries interleaved (real,
+ * imaginary), leading dimensions in complex elements.
+ * tmvg_lu_decompose_z64: A := P L U in place, P[0..n) interchanges.  Pivot
+ * rule as TMV's complex instantiation: first index of the strict maximum of
+ * TMV's modulus (TMV_ABS, include/tmv/TMV_Base.h:312-325); a column whose
+ * largest modulus is below DBL_MIN is zeroed with P[j] = j; the column is
+ * scaled by TMV_InverseOf of the pivot.  Never fails on singular input.
+ * Replaces: template void tmv::LU_Decompose(MatrixView<std::complex<double> >,
+ *           ptrdiff_t*) (src/TMV_LUDecompose.cpp:514-559).
+ * tmvg_lu_ldiveq_z64: B := (P L U)^-1 B, each column with TMV's vector
+ * solves (zero entries skipped; a division by U(j,j) as TMV_Divide);
+ * TMVG_SINGULAR when a zero U(j,j) meets a nonzero entry.  Synchronises.
+ * Replaces: template void tmv::LU_LDivEq(const GenMatrix<std::complex<double> >&,
+ *           const ptrdiff_t*, MatrixView<std::complex<double> >)
+ *           (src/TMV_LUDiv.cpp:186). */
+tmvg_status tmvg_lu_decompose_z64(tmvg_handle h, int64_t n, double* A, int64_t lda,
+                                  int64_t* P);
+tmvg_status tmvg_lu_ldiveq_z64(tmvg_handle h, int64_t n, const double* LU, int64_t lda,
+                               const int64_t* P, int64_t nrhs, double* B, int64_t ldb);
+
 /* ---- mixed-precision solve with FP64 iterative refinement ---------------
  * X = A^-1 B for a column-major FP64 A: the factorisation runs in FP32
  * (pivots chosen by comparing in FP64), then each column is refined with

@@ -1,0 +1,89 @@
+"""LU_Decompose / LU_LDivEq for complex<double> on the GPU against the
+oracle's complex restatement (itself pinned to TMV's complex instantiations
+and to tests/golden/complex_lu.npz)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev(a, dev):
+    import torch
+
+    return torch.from_numpy(np.asfortranarray(a)).to(dev).t().contiguous().t()
+
+
+def _host(t):
+    return np.asfortranarray(t.cpu().numpy())
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 17, 64, 65, 130, 300])
+def test_complex_lu_and_solve_match_oracle(dev, orc, n):
+    import torch
+
+    from tmv_gb300 import linalg
+
+    rng = np.random.default_rng(700 + n)
+    a = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    lu_o = np.asfortranarray(a.copy())
+    p_o = orc.lu_decompose_z(lu_o)
+    A = _dev(a, dev)
+    P = linalg.lu_decompose_z(A)
+    torch.cuda.synchronize()
+    assert np.array_equal(P.cpu().numpy(), p_o)
+    assert np.abs(_host(A) - lu_o).max() <= 1e-12 * np.abs(lu_o).max()
+    b = rng.standard_normal((n, 4)) + 1j * rng.standard_normal((n, 4))
+    x_o = np.asfortranarray(b.copy())
+    orc.ldiveq_z(lu_o, p_o, x_o)
+    X = _dev(b, dev)
+    linalg.lu_ldiveq_z(A, P, X)
+    x = _host(X)
+    assert np.abs(x - x_o).max() <= 1e-11 * np.abs(x_o).max()
+    scale = np.abs(a).sum(axis=1).max() * np.abs(x).max()
+    assert np.abs(a @ x - b).max() <= 1e-13 * scale
+
+
+def test_complex_golden_and_pivot_rule(dev):
+    # TMV's own complex factors and solutions, and the pivot-rule cases
+    # (exact arithmetic: bitwise)
+    from pathlib import Path
+
+    import torch
+
+    from tmv_gb300 import linalg
+
+    g = np.load(Path(__file__).resolve().parent / "golden" / "complex_lu.npz")
+    for n in [1, 4, 17, 65]:
+        A = _dev(g[f"a{n}"], dev)
+        P = linalg.lu_decompose_z(A)
+        torch.cuda.synchronize()
+        assert np.array_equal(P.cpu().numpy(), g[f"P{n}"]), n
+        LU = g[f"LU{n}"]
+        assert np.abs(_host(A) - LU).max() <= 1e-12 * np.abs(LU).max(), n
+        X = _dev(g[f"b{n}"], dev)
+        linalg.lu_ldiveq_z(A, P, X)
+        assert np.abs(_host(X) - g[f"X{n}"]).max() <= 1e-11 * np.abs(g[f"X{n}"]).max(), n
+    for q in range(3):
+        A = _dev(g[f"s{q}"], dev)
+        P = linalg.lu_decompose_z(A)
+        torch.cuda.synchronize()
+        assert np.array_equal(P.cpu().numpy(), g[f"sP{q}"])
+        np.testing.assert_array_equal(_host(A), g[f"sLU{q}"])
+
+
+def test_complex_singular_solve_raises(dev, orc):
+    from tmv_gb300 import _lib, linalg
+
+    a = np.array([[1 + 1j, 2, 0], [0, 0, 0], [3j, 1, 0]], dtype=np.complex128)  # zero column 2
+    A = _dev(a, dev)
+    P = linalg.lu_decompose_z(A)
+    lu_o = np.asfortranarray(a.copy())
+    p_o = orc.lu_decompose_z(lu_o)
+    assert np.array_equal(P.cpu().numpy(), p_o)
+    np.testing.assert_array_equal(_host(A), lu_o)
+    X = _dev(np.ones((3, 1), dtype=np.complex128), dev)
+    with pytest.raises(_lib.SingularError):
+        linalg.lu_ldiveq_z(A, P, X)
+    # the context stays usable
+    Y = _dev(np.eye(3, dtype=np.complex128)[:, :1] * 0, dev)
+    linalg.lu_ldiveq_z(A, P, Y)

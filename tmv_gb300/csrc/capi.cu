@@ -11,6 +11,7 @@
 #include "lu.cuh"
 #include "mixed.cuh"
 #include "multmv.cuh"
+#include "zlu.cuh"
 #include "trsv.cuh"
 
 namespace tmvg {
@@ -781,6 +782,20 @@ tmvg_status tmvg_multmv_f64(tmvg_handle h, int add, double alpha, int64_t m, int
     CTX_OR_BAIL(h);
     if (m < 0 || n < 0) return set_error(c, TMVG_BAD_ARG, "multmv: bad sizes");
     return multmv(c, add != 0, alpha, m, n, A, sAi, sAj, x, incx, y, incy);
+}
+
+tmvg_status tmvg_lu_decompose_z64(tmvg_handle h, int64_t n, double* A, int64_t lda, int64_t* P)
+{
+    CTX_OR_BAIL(h);
+    return zlu_factor(c, n, reinterpret_cast<double2*>(A), lda, P);
+}
+
+tmvg_status tmvg_lu_ldiveq_z64(tmvg_handle h, int64_t n, const double* LU, int64_t lda, const int64_t* P,
+                               int64_t nrhs, double* B, int64_t ldb)
+{
+    CTX_OR_BAIL(h);
+    return zlu_ldiveq(c, n, reinterpret_cast<const double2*>(LU), lda, P, nrhs,
+                      reinterpret_cast<double2*>(B), ldb);
 }
 
 tmvg_status tmvg_lu_solve_mixed_f64(tmvg_handle h, int64_t n, const double* A, int64_t lda,

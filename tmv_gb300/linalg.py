@@ -97,6 +97,38 @@ def lu_ldiveq(LU: torch.Tensor, P: torch.Tensor, B: torch.Tensor) -> None:
                    _ld(B)), "lu_ldiveq")
 
 
+def _check_z_cuda(*ts: torch.Tensor) -> None:
+    for t in ts:
+        if not (t.is_cuda and t.dtype == torch.complex128):
+            raise TypeError("complex128 CUDA tensors required")
+
+
+def lu_decompose_z(A: torch.Tensor) -> torch.Tensor:
+    """LU_Decompose of a column-major complex128 n x n CUDA tensor in place
+    (tmvg_lu_decompose_z64, TMV's complex<double> instantiation); returns
+    the int64 interchanges."""
+    _check_z_cuda(A)
+    n = A.shape[0]
+    if A.shape[1] != n or not is_colmajor(A):
+        raise ValueError("lu_decompose_z: A must be a column-major square matrix")
+    P = torch.empty(n, dtype=torch.int64, device=A.device)
+    h = handle(A.device.index)
+    h.check(h.call("tmvg_lu_decompose_z64", n, _ptr(A), _ld(A), _ptr(P)), "lu_decompose_z")
+    return P
+
+
+def lu_ldiveq_z(LU: torch.Tensor, P: torch.Tensor, B: torch.Tensor) -> None:
+    """B := (P L U)^-1 B for complex128 column-major CUDA tensors
+    (tmvg_lu_ldiveq_z64); raises SingularError like TMV."""
+    _check_z_cuda(LU, B)
+    n = LU.shape[0]
+    if B.dim() != 2 or B.shape[0] != n or not is_colmajor(B) or not is_colmajor(LU):
+        raise ValueError("lu_ldiveq_z: B must be column-major n x nrhs")
+    h = handle(LU.device.index)
+    h.check(h.call("tmvg_lu_ldiveq_z64", n, _ptr(LU), _ld(LU), _ptr(P), B.shape[1], _ptr(B), _ld(B)),
+            "lu_ldiveq_z")
+
+
 def lu_rdiveq(LU: torch.Tensor, P: torch.Tensor, B: torch.Tensor) -> None:
     """B := B (P L U)^-1 in place (tmv::LU_RDivEq, src/TMV_LUDiv.cpp:370)."""
     _check_f64_cuda(LU, B)
