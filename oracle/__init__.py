@@ -120,6 +120,18 @@ class _Backend:
         if rc:
             raise RuntimeError(f"ldiveq_z rc={rc}")
 
+    def rdiveq_z(self, LU: np.ndarray, P: np.ndarray, B: np.ndarray) -> None:
+        """B (nrows x n, Fortran-order complex128) := B (P L U)^-1 in place."""
+        assert LU.dtype == np.complex128 and LU.flags.f_contiguous
+        assert B.dtype == np.complex128 and B.flags.f_contiguous and B.ndim == 2
+        n = LU.shape[0]
+        f = self._f("lu_rdiveq_z", C.c_int, [i64, vp, i64, vp, i64, vp, i64])
+        rc = f(n, _p(LU), n, _p(P), B.shape[0], _p(B), max(B.shape[0], 1))
+        if rc == SINGULAR:
+            raise OracleSingular("singular")
+        if rc:
+            raise RuntimeError(f"rdiveq_z rc={rc}")
+
     def ldiveq(self, LU: np.ndarray, P: np.ndarray, B: np.ndarray) -> None:
         n = LU.shape[0]
         Bv = B.reshape(n, -1) if B.ndim == 1 else B
@@ -175,6 +187,14 @@ class _Backend:
 
 class Port(_Backend):
     prefix = "oracle_"
+
+    def lu_det_z(self, LU: np.ndarray, P: np.ndarray):
+        """(det, logdet, sign) from complex LU factors."""
+        d, s = np.zeros(2), np.zeros(2)
+        ld = C.c_double()
+        f = self._f("lu_det_z", None, [i64, vp, i64, vp, vp, C.POINTER(C.c_double), vp])
+        f(LU.shape[0], _p(LU), LU.shape[0], _p(P), _p(d), C.byref(ld), _p(s))
+        return complex(d[0], d[1]), ld.value, complex(s[0], s[1])
 
     def _lu(self, A, P):
         f = self._f("lu_decompose", C.c_int, [i64, i64, vp, i64, i64, vp])
@@ -240,6 +260,17 @@ class Port(_Backend):
 
 class Ref(_Backend):
     prefix = "tmvref_"
+
+    def det_z(self, a: np.ndarray):
+        """(det, logdet, sign) of a complex matrix through LUDiv."""
+        A = np.asfortranarray(a, dtype=np.complex128)
+        d, s = np.zeros(2), np.zeros(2)
+        ld = C.c_double()
+        f = self._f("det_z", C.c_int, [i64, vp, vp, C.POINTER(C.c_double), vp])
+        rc = f(A.shape[0], _p(A), _p(d), C.byref(ld), _p(s))
+        if rc:
+            raise RuntimeError(f"det_z rc={rc}")
+        return complex(d[0], d[1]), ld.value, complex(s[0], s[1])
 
     def _lu(self, A, P):
         if A.shape[0] != A.shape[1]:

@@ -18,8 +18,8 @@
 //   tmvref_rdivide       X = B % m (LUDiv::doRDiv, src/TMV_LUD.cpp:122-130)
 //   tmvref_det           m.det(), m.logDet(&s) (src/TMV_LUD.cpp:132-190)
 //   tmvref_batched_divide  one B_i/A_i per system, OpenMP over systems.
-//   tmvref_lu_decompose_z, tmvref_lu_ldiveq_z  the same LU_Decompose and
-//                        LU_LDivEq for std::complex<double> (column-major,
+//   tmvref_lu_decompose_z, tmvref_lu_ldiveq_z, tmvref_lu_rdiveq_z, tmvref_det_z
+//                        the same for std::complex<double> (column-major,
 //                        interleaved entries).
 //
 // Status: 0 ok, 1 tmv::Singular thrown, 2 other tmv::Error, 3 other exception.
@@ -99,6 +99,35 @@ int tmvref_lu_ldiveq_z(ptrdiff_t n, const double* LU, ptrdiff_t lda, const ptrdi
         tmv::ConstMatrixView<Z> LUv = tmv::MatrixViewOf(reinterpret_cast<const Z*>(LU), n, n, 1, lda);
         tmv::MatrixView<Z> Bv = tmv::MatrixViewOf(reinterpret_cast<Z*>(B), n, nrhs, 1, ldb);
         tmv::LU_LDivEq(LUv, P, Bv);
+    });
+}
+
+int tmvref_lu_rdiveq_z(ptrdiff_t n, const double* LU, ptrdiff_t lda, const ptrdiff_t* P,
+                       ptrdiff_t nrows, double* B, ptrdiff_t ldb)
+{
+    return guarded([&] {
+        typedef std::complex<double> Z;
+        tmv::ConstMatrixView<Z> LUv = tmv::MatrixViewOf(reinterpret_cast<const Z*>(LU), n, n, 1, lda);
+        tmv::MatrixView<Z> Bv = tmv::MatrixViewOf(reinterpret_cast<Z*>(B), nrows, n, 1, ldb);
+        tmv::LU_RDivEq(LUv, P, Bv);
+    });
+}
+
+// det and logDet of a complex matrix through LUDiv (src/TMV_LUD.cpp:132-156)
+int tmvref_det_z(ptrdiff_t n, const double* A, double* det, double* logdet, double* sign)
+{
+    return guarded([&] {
+        typedef std::complex<double> Z;
+        tmv::Matrix<Z, tmv::ColMajor> m(n, n);
+        std::memcpy(m.ptr(), A, sizeof(Z) * n * n);
+        m.divideUsing(tmv::LU);
+        const Z d = m.det();
+        Z s;
+        *logdet = m.logDet(&s);
+        det[0] = d.real();
+        det[1] = d.imag();
+        sign[0] = s.real();
+        sign[1] = s.imag();
     });
 }
 

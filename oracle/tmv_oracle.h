@@ -93,6 +93,12 @@ int oracle_batched_divide(ptrdiff_t count, const ptrdiff_t* n,
 int oracle_lu_decompose_z(ptrdiff_t n, double* A, ptrdiff_t lda, ptrdiff_t* P);
 int oracle_lu_ldiveq_z(ptrdiff_t n, const double* LU, ptrdiff_t lda, const ptrdiff_t* P,
                        ptrdiff_t nrhs, double* B, ptrdiff_t ldb);
+/* B (nrows x n, column-major) := B (P L U)^-1, row by row */
+int oracle_lu_rdiveq_z(ptrdiff_t n, const double* LU, ptrdiff_t lda, const ptrdiff_t* P,
+                       ptrdiff_t nrows, double* B, ptrdiff_t ldb);
+/* det and sign as (re, im) pairs */
+void oracle_lu_det_z(ptrdiff_t n, const double* LU, ptrdiff_t lda, const ptrdiff_t* P,
+                     double* det, double* logdet, double* sign);
 
 #ifdef __cplusplus
 }

@@ -1,5 +1,6 @@
-/* tmv_oracle_z.c -- C restatement of TMV 0.76's LU_Decompose and LU_LDivEq
- * for std::complex<double> (TEST INFRASTRUCTURE ONLY).
+/* tmv_oracle_z.c -- C restatement of TMV 0.76's LU_Decompose, LU_LDivEq,
+ * LU_RDivEq and LUDiv::det/logDet for std::complex<double> (TEST
+ * INFRASTRUCTURE ONLY).
  *
  * The complex instantiations follow the real ones (tmv_oracle.c) step for
  * step; what changes is TMV's complex arithmetic:
@@ -256,4 +257,93 @@ int oracle_lu_ldiveq_z(ptrdiff_t n, const double* LU, ptrdiff_t lda, const ptrdi
         if (rc) return rc;
     }
     return ORACLE_OK;
+}
+
+/* LU_RDivEq (src/TMV_LUDiv.cpp:370-411) for one row x of m: m %= U, m %= L,
+ * m.reversePermuteCols(P), where m %= T is T^T.LDivEq(m^T)
+ * (include/tmv/TMV_TriMatrix.h:945-946).  U^T and L^T of a column-major LU
+ * are row-major, so TMV takes the row-oriented vector solves
+ * (src/TMV_TriDiv_V.cpp:59-146, 237-320) after trimming the leading (lower)
+ * or trailing (upper) zeros of x (:401-462); a zero U(i,i) met there is
+ * singular. */
+static int lu_rsolve_row(zview LU, const ptrdiff_t* P, zc* x, idx incx)
+{
+    const idx N = LU.m;
+#define X(i) x[(i) * incx]
+    /* x := x U^-1: U^T lower, non-unit */
+    idx i1 = 0;
+    while (i1 < N && X(i1) == 0.0) ++i1;
+    for (idx i = i1; i < N; ++i) {
+        for (idx j = i1; j < i; ++j) X(i) -= X(j) * ZA(LU, j, i);
+        if (ZA(LU, i, i) == 0.0) return ORACLE_SINGULAR;
+        X(i) = X(i) * tmv_inverse_of(ZA(LU, i, i));
+    }
+    /* x := x L^-1: L^T upper, unit */
+    idx i2 = N;
+    while (i2 > 0 && X(i2 - 1) == 0.0) --i2;
+    for (idx i = i2 - 1; i >= 0; --i)
+        for (idx j = i + 1; j < i2; ++j) X(i) -= X(j) * ZA(LU, j, i);
+    /* reversePermuteCols(P) */
+    for (idx i = N - 1; i >= 0; --i) {
+        const idx p = P[i];
+        if (p != i) {
+            const zc t = X(i);
+            X(i) = X(p);
+            X(p) = t;
+        }
+    }
+#undef X
+    return ORACLE_OK;
+}
+
+int oracle_lu_rdiveq_z(ptrdiff_t n, const double* LU, ptrdiff_t lda, const ptrdiff_t* P,
+                       ptrdiff_t nrows, double* B, ptrdiff_t ldb)
+{
+    /* B: nrows x n, column-major (leading dimension ldb); each row in turn */
+    zview f = {(zc*)LU, n, n, lda};
+    for (idx r = 0; r < nrows; ++r) {
+        const int rc = lu_rsolve_row(f, P, (zc*)B + r, ldb);
+        if (rc) return rc;
+    }
+    return ORACLE_OK;
+}
+
+/* LUDiv::det / logDet (src/TMV_LUD.cpp:132-156) with GenDiagMatrix::logDet
+ * (src/TMV_DiagMatrix.cpp:59-85): logdet sums log TMV_ABS(U_jj) and the
+ * sign multiplies by TMV_SIGN(U_jj, |U_jj|) = U_jj / |U_jj| componentwise
+ * (include/tmv/TMV_Base.h:708-716); a zero U_jj gives log(0) = -inf and sign
+ * 0; the permutation's determinant multiplies the sign; det = sign
+ * exp(logdet), 0 with a zero sign. */
+void oracle_lu_det_z(ptrdiff_t n, const double* LU, ptrdiff_t lda, const ptrdiff_t* P,
+                     double* det, double* logdet, double* sign)
+{
+    zview f = {(zc*)LU, n, n, lda};
+    zc s = 1.0;
+    double ld = 0.0;
+    int pd = 1;
+    for (idx j = 0; j < n; ++j) {
+        const zc u = ZA(f, j, j);
+        if (u == 0.0) {
+            ld = log(creal(u));
+            s = 0.0;
+        } else {
+            const double a = tmv_abs(u);
+            ld += log(a);
+            const zc sg = a > 0 ? CMPLX(creal(u) / a, cimag(u) / a) : CMPLX(1.0, 0.0);
+            s *= sg;
+        }
+        if (P[j] != j) pd = -pd;
+    }
+    s = (double)pd * s;
+    *logdet = ld;
+    sign[0] = creal(s);
+    sign[1] = cimag(s);
+    if (s == 0.0) {
+        det[0] = 0.0;
+        det[1] = 0.0;
+    } else {
+        const zc d = s * exp(ld);
+        det[0] = creal(d);
+        det[1] = cimag(d);
+    }
 }

@@ -254,20 +254,28 @@ def multmv_tri(ref):
 
 
 def complex_lu(ref):
-    # LU_Decompose and LU_LDivEq for std::complex<double> as TMV computes
-    # them: seeded complex systems, and 3 x 3 cases for the pivot rule (TMV's
+    # LU_Decompose, LU_LDivEq, LU_RDivEq and det/logDet for
+    # std::complex<double> as TMV computes them: seeded complex systems, and
+    # 3 x 3 cases for the pivot rule (TMV's
     # modulus: a tie keeps the first index, a larger |re| + |im| with a
     # smaller modulus loses; a zero column underflows)
     rng = np.random.default_rng(20241203)
+    rng_w = np.random.default_rng(20241204)  # the right-division operands
     out = {}
     for n in [1, 4, 17, 65]:
         a = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
         b = rng.standard_normal((n, 2)) + 1j * rng.standard_normal((n, 2))
+        w = rng_w.standard_normal((2, n)) + 1j * rng_w.standard_normal((2, n))
         A = np.asfortranarray(a.copy())
         P = ref.lu_decompose_z(A)
         X = np.asfortranarray(b.copy())
         ref.ldiveq_z(A, P, X)
-        out.update({f"a{n}": a, f"b{n}": b, f"LU{n}": A, f"P{n}": P, f"X{n}": X})
+        Y = np.asfortranarray(w.copy())
+        ref.rdiveq_z(A, P, Y)
+        det, logdet, sign = ref.det_z(a)
+        out.update({f"a{n}": a, f"b{n}": b, f"w{n}": w, f"LU{n}": A, f"P{n}": P, f"X{n}": X,
+                    f"Y{n}": Y, f"det{n}": np.array([det]), f"logdet{n}": np.array([logdet]),
+                    f"sign{n}": np.array([sign])})
     cases = [
         [[3 + 4j, 1, 1 - 1j], [5 + 0j, 2, 2 - 2j], [0 + 5j, 3, 3 - 3j]],
         [[1 + 1j, 1, 1 - 1j], [1.5 + 0j, 2, 2 - 2j], [0.1 + 0.1j, 3, 3 - 3j]],

@@ -183,7 +183,8 @@ def test_multmv_tri_fixtures(orc):
 
 
 def test_complex_lu_fixtures(orc):
-    # TMV's own complex<double> LU_Decompose / LU_LDivEq (complex_lu.npz)
+    # TMV's own complex<double> LU_Decompose / LU_LDivEq / LU_RDivEq /
+    # det (complex_lu.npz)
     g = load("complex_lu.npz")
     for n in [1, 4, 17, 65]:
         a, b = g[f"a{n}"], g[f"b{n}"]
@@ -195,6 +196,13 @@ def test_complex_lu_fixtures(orc):
         X = np.asfortranarray(b.copy())
         orc.ldiveq_z(A, P, X)
         assert np.abs(X - g[f"X{n}"]).max() <= 1e-11 * np.abs(g[f"X{n}"]).max(), n
+        Y = np.asfortranarray(g[f"w{n}"].copy())
+        orc.rdiveq_z(A, P, Y)
+        assert np.abs(Y - g[f"Y{n}"]).max() <= 1e-11 * np.abs(g[f"Y{n}"]).max(), n
+        det, logdet, sign = orc.lu_det_z(A, P)
+        assert abs(det - g[f"det{n}"][0]) <= 1e-12 * abs(g[f"det{n}"][0]), n
+        assert abs(logdet - g[f"logdet{n}"][0]) <= 1e-12 * max(1.0, abs(logdet)), n
+        assert abs(sign - g[f"sign{n}"][0]) <= 1e-12, n
     for q in range(3):
         A = np.asfortranarray(g[f"s{q}"].copy())
         P = orc.lu_decompose_z(A)

@@ -180,3 +180,34 @@ def test_complex_pivot_rule_and_special_entries(orc, ref):
         p1, p2 = orc.lu_decompose_z(A1), ref.lu_decompose_z(A2)
         assert np.array_equal(p1, p2)
         np.testing.assert_array_equal(A1, A2)
+
+
+def test_complex_rdiveq_and_det_match_tmv(orc, ref):
+    # b % m (row-oriented transposed solves) and det/logDet for complex
+    rng = np.random.default_rng(43)
+    for n in [1, 2, 3, 5, 17, 65, 130]:
+        a = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+        A1, A2 = np.asfortranarray(a.copy()), np.asfortranarray(a.copy())
+        p1, p2 = orc.lu_decompose_z(A1), ref.lu_decompose_z(A2)
+        for rows in [1, 3]:
+            w = rng.standard_normal((rows, n)) + 1j * rng.standard_normal((rows, n))
+            y1, y2 = np.asfortranarray(w.copy()), np.asfortranarray(w.copy())
+            orc.rdiveq_z(A1, p1, y1)
+            ref.rdiveq_z(A2, p2, y2)
+            assert np.abs(y1 - y2).max() <= 1e-11 * np.abs(y2).max(), (n, rows)
+            if n <= 3 and rows == 1:
+                assert np.array_equal(y1, y2), n
+            scale = np.abs(a).sum(axis=0).max() * np.abs(y1).max()
+            assert np.abs(y1 @ a - w).max() <= 1e-13 * scale
+        d1, l1, s1 = orc.lu_det_z(A1, p1)
+        d2, l2, s2 = ref.det_z(a)
+        assert abs(d1 - d2) <= 1e-12 * abs(d2) and abs(l1 - l2) <= 1e-12 * max(1.0, abs(l2))
+        assert abs(s1 - s2) <= 1e-12
+    # a zero column: det 0, logdet -inf, sign 0, and b % m singular in both
+    a = np.array([[1 + 1j, 2, 0], [0, 0, 0], [3j, 1, 0]], dtype=np.complex128)
+    A1, A2 = np.asfortranarray(a.copy()), np.asfortranarray(a.copy())
+    p1, p2 = orc.lu_decompose_z(A1), ref.lu_decompose_z(A2)
+    assert orc.lu_det_z(A1, p1) == ref.det_z(a) == (0j, -np.inf, 0j)
+    for backend, (f, p) in ((orc, (A1, p1)), (ref, (A2, p2))):
+        with pytest.raises(oracle.OracleSingular):
+            backend.rdiveq_z(f, p, np.asfortranarray(np.ones((1, 3), dtype=np.complex128)))
