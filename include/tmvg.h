@@ -256,6 +256,19 @@ tmvg_status tmvg_lu_decompose_z64(tmvg_handle h, int64_t n, double* A, int64_t l
                                   int64_t* P);
 tmvg_status tmvg_lu_ldiveq_z64(tmvg_handle h, int64_t n, const double* LU, int64_t lda,
                                const int64_t* P, int64_t nrhs, double* B, int64_t ldb);
+/* B (nrows x n, column-major, leading dimension ldb) := B (P L U)^-1 with
+ * TMV's row-oriented solves of the transposed factors (leading / trailing
+ * zeros trimmed, a zero U(i,i) then TMVG_SINGULAR).  Synchronises.
+ * Replaces: template void tmv::LU_RDivEq(const GenMatrix<std::complex<double> >&,
+ *           const ptrdiff_t*, MatrixView<std::complex<double> >)
+ *           (src/TMV_LUDiv.cpp:370). */
+tmvg_status tmvg_lu_rdiveq_z64(tmvg_handle h, int64_t n, const double* LU, int64_t lda,
+                               const int64_t* P, int64_t nrows, double* B, int64_t ldb);
+/* det (re, im), logdet = sum log|U_jj| and sign (re, im) from the factors,
+ * host outputs.  Replaces: LUDiv<std::complex<double> >::det / logDet
+ * (src/TMV_LUD.cpp:132-156). */
+tmvg_status tmvg_lu_det_z64(tmvg_handle h, int64_t n, const double* LU, int64_t lda,
+                            const int64_t* P, double* det, double* logdet, double* sign);
 
 /* ---- mixed-precision solve with FP64 iterative refinement ---------------
  * X = A^-1 B for a column-major FP64 A: the factorisation runs in FP32

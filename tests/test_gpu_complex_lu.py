@@ -87,3 +87,62 @@ def test_complex_singular_solve_raises(dev, orc):
     # the context stays usable
     Y = _dev(np.eye(3, dtype=np.complex128)[:, :1] * 0, dev)
     linalg.lu_ldiveq_z(A, P, Y)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 17, 65, 130])
+def test_complex_rdiveq_and_det_match_oracle(dev, orc, n):
+    # b % m and det / logDet from the GPU factors, against the oracle's
+    # restatement applied to the same factors
+    import torch
+
+    from tmv_gb300 import linalg
+
+    rng = np.random.default_rng(800 + n)
+    a = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    A = _dev(a, dev)
+    P = linalg.lu_decompose_z(A)
+    torch.cuda.synchronize()
+    lu, p = _host(A), P.cpu().numpy()
+    for rows in [1, 3]:
+        w = rng.standard_normal((rows, n)) + 1j * rng.standard_normal((rows, n))
+        y_o = np.asfortranarray(w.copy())
+        orc.rdiveq_z(lu, p, y_o)
+        Y = _dev(w, dev)
+        linalg.lu_rdiveq_z(A, P, Y)
+        y = _host(Y)
+        # the same operations in the same order on the same factors
+        np.testing.assert_array_equal(y, y_o)
+        scale = np.abs(a).sum(axis=0).max() * np.abs(y).max()
+        assert np.abs(y @ a - w).max() <= 1e-13 * scale
+    det, logdet, sign = linalg.lu_det_z(A, P)
+    d_o, l_o, s_o = orc.lu_det_z(lu, p)
+    assert abs(det - d_o) <= 1e-13 * abs(d_o) and abs(logdet - l_o) <= 1e-13 * max(1.0, abs(l_o))
+    assert abs(sign - s_o) <= 1e-14
+    assert abs(det - np.linalg.det(a)) <= 1e-10 * abs(np.linalg.det(a))
+
+
+def test_complex_rdiveq_golden_and_singular(dev):
+    from pathlib import Path
+
+    import torch
+
+    from tmv_gb300 import _lib, linalg
+
+    g = np.load(Path(__file__).resolve().parent / "golden" / "complex_lu.npz")
+    for n in [1, 4, 17, 65]:
+        A = _dev(g[f"a{n}"], dev)
+        P = linalg.lu_decompose_z(A)
+        Y = _dev(g[f"w{n}"], dev)
+        linalg.lu_rdiveq_z(A, P, Y)
+        torch.cuda.synchronize()
+        assert np.abs(_host(Y) - g[f"Y{n}"]).max() <= 1e-11 * np.abs(g[f"Y{n}"]).max(), n
+        det, logdet, sign = linalg.lu_det_z(A, P)
+        # a product of n diagonal entries, each within rounding of TMV's
+        assert abs(det - g[f"det{n}"][0]) <= 1e-11 * abs(g[f"det{n}"][0]), n
+        assert abs(sign - g[f"sign{n}"][0]) <= 1e-11, n
+    a = np.array([[1 + 1j, 2, 0], [0, 0, 0], [3j, 1, 0]], dtype=np.complex128)
+    A = _dev(a, dev)
+    P = linalg.lu_decompose_z(A)
+    assert linalg.lu_det_z(A, P) == (0j, -np.inf, 0j)
+    with pytest.raises(_lib.SingularError):
+        linalg.lu_rdiveq_z(A, P, _dev(np.ones((1, 3), dtype=np.complex128), dev))

@@ -3,9 +3,11 @@
 #include <cstdlib>
 #include <cstring>
 #include <initializer_list>
+#include <complex>
 #include <limits>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "gemm_tc.cuh"
 #include "lu.cuh"
@@ -796,6 +798,75 @@ tmvg_status tmvg_lu_ldiveq_z64(tmvg_handle h, int64_t n, const double* LU, int64
     CTX_OR_BAIL(h);
     return zlu_ldiveq(c, n, reinterpret_cast<const double2*>(LU), lda, P, nrhs,
                       reinterpret_cast<double2*>(B), ldb);
+}
+
+tmvg_status tmvg_lu_rdiveq_z64(tmvg_handle h, int64_t n, const double* LU, int64_t lda, const int64_t* P,
+                               int64_t nrows, double* B, int64_t ldb)
+{
+    CTX_OR_BAIL(h);
+    return zlu_rdiveq(c, n, reinterpret_cast<const double2*>(LU), lda, P, nrows,
+                      reinterpret_cast<double2*>(B), ldb);
+}
+
+tmvg_status tmvg_lu_det_z64(tmvg_handle h, int64_t n, const double* LU, int64_t lda, const int64_t* P,
+                            double* det, double* logdet, double* sign)
+{
+    // LUDiv::det / logDet (src/TMV_LUD.cpp:132-156) with GenDiagMatrix::logDet
+    // (src/TMV_DiagMatrix.cpp:59-85) for std::complex<double>: log TMV_ABS(U_jj)
+    // summed, the sign multiplied by TMV_SIGN(U_jj, |U_jj|) = U_jj / |U_jj|
+    // componentwise (include/tmv/TMV_Base.h:708-716), a zero U_jj gives
+    // log(0) and sign 0, the permutation's determinant multiplies the sign.
+    // O(n): the diagonal and P are read back and reduced on the host in
+    // TMV's order, as for the real determinant.
+    CTX_OR_BAIL(h);
+    if (n < 0 || lda < std::max<int64_t>(n, 1) || !det || !logdet || !sign)
+        return set_error(c, TMVG_BAD_ARG, "det_z: bad arguments");
+    std::vector<double> diag(2 * (size_t)std::max<int64_t>(n, 1));
+    std::vector<int64_t> hp((size_t)std::max<int64_t>(n, 1));
+    tmvg_status st = TMVG_OK;
+    if (n > 0) {
+        st = check_cuda(c,
+                        cudaMemcpy2DAsync(diag.data(), 2 * sizeof(double), LU, 2 * (lda + 1) * sizeof(double),
+                                          2 * sizeof(double), n, cudaMemcpyDeviceToHost, c->stream),
+                        "det_z: diag d2h");
+        if (!st)
+            st = check_cuda(c, cudaMemcpyAsync(hp.data(), P, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, c->stream),
+                            "det_z: P d2h");
+        if (!st) st = check_cuda(c, cudaStreamSynchronize(c->stream), "det_z sync");
+    }
+    if (st) return st;
+    std::complex<double> s(1.0, 0.0);
+    double ld = 0.0;
+    int pd = 1;
+    for (int64_t j = 0; j < n; ++j) {
+        const std::complex<double> u(diag[2 * j], diag[2 * j + 1]);
+        if (u == std::complex<double>(0.0, 0.0)) {
+            ld = std::log(u.real());
+            s = 0.0;
+        } else {
+            // TMV_ABS: the modulus scaled by the larger component
+            double xr = u.real(), xi = u.imag();
+            const double ar = std::fabs(xr), ai = std::fabs(xi);
+            const double sc = ar < ai ? ai : ar;
+            xr /= sc;
+            xi /= sc;
+            const double a = sc * std::sqrt(xr * xr + xi * xi);
+            ld += std::log(a);
+            const std::complex<double> sg = a > 0 ? std::complex<double>(u.real() / a, u.imag() / a)
+                                                  : std::complex<double>(1.0, 0.0);
+            s *= sg;
+        }
+        if (hp[j] != j) pd = -pd;
+    }
+    s = (double)pd * s;
+    *logdet = ld;
+    sign[0] = s.real();
+    sign[1] = s.imag();
+    const std::complex<double> d = s == std::complex<double>(0.0, 0.0) ? std::complex<double>(0.0, 0.0)
+                                                                       : s * std::exp(ld);
+    det[0] = d.real();
+    det[1] = d.imag();
+    return TMVG_OK;
 }
 
 tmvg_status tmvg_lu_solve_mixed_f64(tmvg_handle h, int64_t n, const double* A, int64_t lda,

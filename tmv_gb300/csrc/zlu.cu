@@ -15,8 +15,9 @@
 // (no fused multiply-add), as the host computes them.
 //
 // A first GPU form: right-looking, one column per step (pivot search in one
-// CTA, row interchange, scaling, rank-1 update over the grid), the solve one
-// CTA per right-hand side.  Values agree with TMV's recursive factorisation
+// CTA, row interchange, scaling, rank-1 update over the grid), the left
+// solve one CTA per right-hand side, the right solve (LU_RDivEq) one row per
+// CTA substituted in TMV's order.  Values agree with TMV's recursive factorisation
 // to rounding; pivots are TMV's wherever rounding does not decide a tie.
 #include "zlu.cuh"
 
@@ -245,6 +246,63 @@ tmvg_status zlu_ldiveq(Context* c, int64_t n, const double2* LU, int64_t lda, co
     const tmvg_status st = check_cuda(c, cudaGetLastError(), "lu_ldiveq_z: launch");
     if (st) return st;
     return collect_device_error(c, "lu_ldiveq_z");
+}
+
+// One row of B per CTA: b := b (P L U)^-1 (LU_RDivEq, src/TMV_LUDiv.cpp:370-411:
+// m %= U, m %= L, m.reversePermuteCols(P)).  m %= T is T^T.LDivEq(m^T), and
+// U^T and L^T of a column-major LU are row-major, so TMV takes its
+// row-oriented vector solves (src/TMV_TriDiv_V.cpp:59-146, 237-320) after
+// trimming the leading (lower) or trailing (upper) zeros of b (:401-462): each
+// entry's terms subtracted one by one in index order, a zero U(i,i) singular.
+// One thread substitutes the row in that order.
+__global__ void zlu_rsolve_kernel(int64_t n, const double2* __restrict__ LU, int64_t lda,
+                                  const int64_t* __restrict__ P, double2* B, int64_t ldb, int* err)
+{
+    if (threadIdx.x != 0) return;
+    double2* x = B + blockIdx.x;  // row r: entry j at x[j * ldb]
+#define X(i) x[(i) * ldb]
+    int64_t i1 = 0;
+    while (i1 < n && !znonzero(X(i1))) ++i1;
+    for (int64_t i = i1; i < n; ++i) {
+        double2 v = X(i);
+        for (int64_t j = i1; j < i; ++j) v = zsub(v, zmul(X(j), LU[j + i * lda]));
+        const double2 d = LU[i + i * lda];
+        if (!znonzero(d)) {
+            atomicCAS(err, (int)kDevOk, (int)kDevSingular);
+            return;
+        }
+        X(i) = zmul(v, tmv_inverse_of(d));
+    }
+    int64_t i2 = n;
+    while (i2 > 0 && !znonzero(X(i2 - 1))) --i2;
+    for (int64_t i = i2 - 1; i >= 0; --i) {
+        double2 v = X(i);
+        for (int64_t j = i + 1; j < i2; ++j) v = zsub(v, zmul(X(j), LU[j + i * lda]));
+        X(i) = v;
+    }
+    for (int64_t i = n - 1; i >= 0; --i) {
+        const int64_t p = P[i];
+        if (p != i && p >= 0 && p < n) {
+            const double2 t = X(i);
+            X(i) = X(p);
+            X(p) = t;
+        }
+    }
+#undef X
+}
+
+tmvg_status zlu_rdiveq(Context* c, int64_t n, const double2* LU, int64_t lda, const int64_t* P, int64_t nrows,
+                       double2* B, int64_t ldb)
+{
+    if (n < 0 || nrows < 0 || lda < std::max<int64_t>(n, 1) || ldb < std::max<int64_t>(nrows, 1))
+        return set_error(c, TMVG_BAD_ARG, "lu_rdiveq_z: bad sizes");
+    if (n == 0 || nrows == 0) return TMVG_OK;
+    if (nrows > 65535) return set_error(c, TMVG_UNSUPPORTED, "lu_rdiveq_z: too many rows");
+    zlu_rsolve_kernel<<<(unsigned)nrows, 32, 0, c->stream>>>(n, LU, lda, P, B, ldb, c->dflags);
+    ++c->launches;
+    const tmvg_status st = check_cuda(c, cudaGetLastError(), "lu_rdiveq_z: launch");
+    if (st) return st;
+    return collect_device_error(c, "lu_rdiveq_z");
 }
 
 }  // namespace tmvg

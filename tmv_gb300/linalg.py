@@ -129,6 +129,33 @@ def lu_ldiveq_z(LU: torch.Tensor, P: torch.Tensor, B: torch.Tensor) -> None:
             "lu_ldiveq_z")
 
 
+def lu_rdiveq_z(LU: torch.Tensor, P: torch.Tensor, B: torch.Tensor) -> None:
+    """B (nrows x n) := B (P L U)^-1 for complex128 column-major CUDA tensors
+    (tmvg_lu_rdiveq_z64, TMV's b % m); raises SingularError like TMV."""
+    _check_z_cuda(LU, B)
+    n = LU.shape[0]
+    if B.dim() != 2 or B.shape[1] != n or not is_colmajor(B) or not is_colmajor(LU):
+        raise ValueError("lu_rdiveq_z: B must be column-major nrows x n")
+    h = handle(LU.device.index)
+    ldb = max(B.stride(1) if B.shape[1] > 1 else B.shape[0], 1)
+    h.check(h.call("tmvg_lu_rdiveq_z64", n, _ptr(LU), _ld(LU), _ptr(P), B.shape[0], _ptr(B), ldb),
+            "lu_rdiveq_z")
+
+
+def lu_det_z(LU: torch.Tensor, P: torch.Tensor):
+    """(det, logdet, sign) of the matrix factored in LU (complex128), as
+    LUDiv::det / logDet (tmvg_lu_det_z64)."""
+    import numpy as np
+
+    _check_z_cuda(LU)
+    d, s = np.zeros(2), np.zeros(2)
+    ld = C.c_double()
+    h = handle(LU.device.index)
+    h.check(h.call("tmvg_lu_det_z64", LU.shape[0], _ptr(LU), _ld(LU), _ptr(P), C.c_void_p(d.ctypes.data),
+                   C.byref(ld), C.c_void_p(s.ctypes.data)), "lu_det_z")
+    return complex(d[0], d[1]), ld.value, complex(s[0], s[1])
+
+
 def lu_rdiveq(LU: torch.Tensor, P: torch.Tensor, B: torch.Tensor) -> None:
     """B := B (P L U)^-1 in place (tmv::LU_RDivEq, src/TMV_LUDiv.cpp:370)."""
     _check_f64_cuda(LU, B)
