@@ -264,6 +264,13 @@ tmvg_status tmvg_lu_ldiveq_z64(tmvg_handle h, int64_t n, const double* LU, int64
  *           (src/TMV_LUDiv.cpp:370). */
 tmvg_status tmvg_lu_rdiveq_z64(tmvg_handle h, int64_t n, const double* LU, int64_t lda,
                                const int64_t* P, int64_t nrows, double* B, int64_t ldb);
+/* Minv (n x n, column-major) := (P L U)^-1, TMV's m.inverse() up to
+ * rounding; TMVG_SINGULAR for a zero U(j,j).  Synchronises.
+ * Replaces: template void tmv::LU_Inverse(const GenMatrix<std::complex<double> >&,
+ *           const ptrdiff_t*, MatrixView<std::complex<double> >)
+ *           (src/TMV_LUInverse.cpp:236). */
+tmvg_status tmvg_lu_inverse_z64(tmvg_handle h, int64_t n, const double* LU, int64_t lda,
+                                const int64_t* P, double* Minv, int64_t ldm);
 /* det (re, im), logdet = sum log|U_jj| and sign (re, im) from the factors,
  * host outputs.  Replaces: LUDiv<std::complex<double> >::det / logDet
  * (src/TMV_LUD.cpp:132-156). */

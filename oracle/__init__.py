@@ -261,6 +261,18 @@ class Port(_Backend):
 class Ref(_Backend):
     prefix = "tmvref_"
 
+    def inverse_z(self, a: np.ndarray) -> np.ndarray:
+        """m.inverse() of a complex matrix through LUDiv (LU_Inverse)."""
+        A = np.asfortranarray(a, dtype=np.complex128)
+        M = np.zeros_like(A, order="F")
+        f = self._f("inverse_z", C.c_int, [i64, vp, vp])
+        rc = f(A.shape[0], _p(A), _p(M))
+        if rc == SINGULAR:
+            raise OracleSingular("singular")
+        if rc:
+            raise RuntimeError(f"inverse_z rc={rc}")
+        return M
+
     def det_z(self, a: np.ndarray):
         """(det, logdet, sign) of a complex matrix through LUDiv."""
         A = np.asfortranarray(a, dtype=np.complex128)

@@ -18,7 +18,8 @@
 //   tmvref_rdivide       X = B % m (LUDiv::doRDiv, src/TMV_LUD.cpp:122-130)
 //   tmvref_det           m.det(), m.logDet(&s) (src/TMV_LUD.cpp:132-190)
 //   tmvref_batched_divide  one B_i/A_i per system, OpenMP over systems.
-//   tmvref_lu_decompose_z, tmvref_lu_ldiveq_z, tmvref_lu_rdiveq_z, tmvref_det_z
+//   tmvref_lu_decompose_z, tmvref_lu_ldiveq_z, tmvref_lu_rdiveq_z, tmvref_det_z,
+//   tmvref_inverse_z
 //                        the same for std::complex<double> (column-major,
 //                        interleaved entries).
 //
@@ -241,6 +242,18 @@ int tmvref_tri_ldiveq(int upper, int unitdiag, ptrdiff_t n, const double* T, ptr
         const tmv::DiagType dt = unitdiag ? tmv::UnitDiag : tmv::NonUnitDiag;
         if (upper) Bv /= Tv.upperTri(dt);
         else Bv /= Tv.lowerTri(dt);
+    });
+}
+
+// m.inverse() of a complex matrix (LUDiv::doMakeInverse -> LU_Inverse)
+int tmvref_inverse_z(ptrdiff_t n, const double* A, double* minv)
+{
+    return guarded([&] {
+        typedef std::complex<double> Z;
+        tmv::Matrix<Z, tmv::ColMajor> m(n, n);
+        std::memcpy(m.ptr(), A, sizeof(Z) * n * n);
+        m.divideUsing(tmv::LU);
+        tmv::MatrixViewOf(reinterpret_cast<Z*>(minv), n, n, tmv::ColMajor) = m.inverse();
     });
 }
 

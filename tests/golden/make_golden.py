@@ -254,7 +254,7 @@ def multmv_tri(ref):
 
 
 def complex_lu(ref):
-    # LU_Decompose, LU_LDivEq, LU_RDivEq and det/logDet for
+    # LU_Decompose, LU_LDivEq, LU_RDivEq, det/logDet and inverse() for
     # std::complex<double> as TMV computes them: seeded complex systems, and
     # 3 x 3 cases for the pivot rule (TMV's
     # modulus: a tie keeps the first index, a larger |re| + |im| with a
@@ -273,6 +273,7 @@ def complex_lu(ref):
         Y = np.asfortranarray(w.copy())
         ref.rdiveq_z(A, P, Y)
         det, logdet, sign = ref.det_z(a)
+        out[f"inv{n}"] = ref.inverse_z(a)
         out.update({f"a{n}": a, f"b{n}": b, f"w{n}": w, f"LU{n}": A, f"P{n}": P, f"X{n}": X,
                     f"Y{n}": Y, f"det{n}": np.array([det]), f"logdet{n}": np.array([logdet]),
                     f"sign{n}": np.array([sign])})

@@ -146,3 +146,29 @@ def test_complex_rdiveq_golden_and_singular(dev):
     assert linalg.lu_det_z(A, P) == (0j, -np.inf, 0j)
     with pytest.raises(_lib.SingularError):
         linalg.lu_rdiveq_z(A, P, _dev(np.ones((1, 3), dtype=np.complex128), dev))
+
+
+def test_complex_inverse_matches_tmv(dev):
+    # m.inverse() against TMV's own (complex_lu.npz), A A^-1 = I, singular
+    from pathlib import Path
+
+    import torch
+
+    from tmv_gb300 import _lib, linalg
+
+    g = np.load(Path(__file__).resolve().parent / "golden" / "complex_lu.npz")
+    for n in [1, 4, 17, 65]:
+        a = g[f"a{n}"]
+        A = _dev(a, dev)
+        P = linalg.lu_decompose_z(A)
+        M = linalg.lu_inverse_z(A, P)
+        torch.cuda.synchronize()
+        m = _host(M)
+        inv = g[f"inv{n}"]
+        assert np.abs(m - inv).max() <= 1e-11 * np.abs(inv).max(), n
+        assert np.abs(a @ m - np.eye(n)).max() <= 1e-12 * np.abs(a).sum(axis=1).max() * np.abs(m).max() * n
+    a = np.array([[1 + 1j, 2, 0], [0, 0, 0], [3j, 1, 0]], dtype=np.complex128)
+    A = _dev(a, dev)
+    P = linalg.lu_decompose_z(A)
+    with pytest.raises(_lib.SingularError):
+        linalg.lu_inverse_z(A, P)

@@ -808,6 +808,13 @@ tmvg_status tmvg_lu_rdiveq_z64(tmvg_handle h, int64_t n, const double* LU, int64
                       reinterpret_cast<double2*>(B), ldb);
 }
 
+tmvg_status tmvg_lu_inverse_z64(tmvg_handle h, int64_t n, const double* LU, int64_t lda, const int64_t* P,
+                                double* Minv, int64_t ldm)
+{
+    CTX_OR_BAIL(h);
+    return zlu_inverse(c, n, reinterpret_cast<const double2*>(LU), lda, P, reinterpret_cast<double2*>(Minv), ldm);
+}
+
 tmvg_status tmvg_lu_det_z64(tmvg_handle h, int64_t n, const double* LU, int64_t lda, const int64_t* P,
                             double* det, double* logdet, double* sign)
 {

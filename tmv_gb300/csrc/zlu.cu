@@ -305,4 +305,33 @@ tmvg_status zlu_rdiveq(Context* c, int64_t n, const double2* LU, int64_t lda, co
     return collect_device_error(c, "lu_rdiveq_z");
 }
 
+__global__ void zlu_identity_kernel(int64_t n, double2* M, int64_t ldm)
+{
+    const int64_t total = n * n;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = t % n, j = t / n;
+        M[i + j * ldm] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+    }
+}
+
+// m.inverse() from the factors (LUDiv::doMakeInverse -> LU_Inverse,
+// src/TMV_LUInverse.cpp:236): M = (P L U)^-1, which is TMV's U^-1 L^-1 with
+// its columns reverse-permuted, here as the left division of the identity
+// (one column per CTA, TMV's vector solves); values agree to rounding.  A
+// zero U(j,j) met by a column is TMVG_SINGULAR, as TMV's triangular inverse
+// throws.
+tmvg_status zlu_inverse(Context* c, int64_t n, const double2* LU, int64_t lda, const int64_t* P, double2* M,
+                        int64_t ldm)
+{
+    if (n < 0 || lda < std::max<int64_t>(n, 1) || ldm < std::max<int64_t>(n, 1))
+        return set_error(c, TMVG_BAD_ARG, "inverse_z: bad sizes");
+    if (n == 0) return TMVG_OK;
+    const unsigned blocks = (unsigned)std::min<int64_t>(ceil_div(n * n, kZThreads), 8 * c->num_sms);
+    zlu_identity_kernel<<<blocks, kZThreads, 0, c->stream>>>(n, M, ldm);
+    ++c->launches;
+    const tmvg_status st = check_cuda(c, cudaGetLastError(), "inverse_z: launch");
+    if (st) return st;
+    return zlu_ldiveq(c, n, LU, lda, P, n, M, ldm);
+}
+
 }  // namespace tmvg

@@ -15,5 +15,7 @@ tmvg_status zlu_ldiveq(Context* c, int64_t n, const double2* LU, int64_t lda, co
                        double2* B, int64_t ldb);
 tmvg_status zlu_rdiveq(Context* c, int64_t n, const double2* LU, int64_t lda, const int64_t* P, int64_t nrows,
                        double2* B, int64_t ldb);
+tmvg_status zlu_inverse(Context* c, int64_t n, const double2* LU, int64_t lda, const int64_t* P, double2* M,
+                        int64_t ldm);
 
 }  // namespace tmvg

@@ -142,6 +142,17 @@ def lu_rdiveq_z(LU: torch.Tensor, P: torch.Tensor, B: torch.Tensor) -> None:
             "lu_rdiveq_z")
 
 
+def lu_inverse_z(LU: torch.Tensor, P: torch.Tensor) -> torch.Tensor:
+    """m.inverse() from complex128 factors (tmvg_lu_inverse_z64): a new
+    column-major n x n tensor; raises SingularError like TMV."""
+    _check_z_cuda(LU)
+    n = LU.shape[0]
+    M = torch.empty((n, n), dtype=torch.complex128, device=LU.device).t()
+    h = handle(LU.device.index)
+    h.check(h.call("tmvg_lu_inverse_z64", n, _ptr(LU), _ld(LU), _ptr(P), _ptr(M), max(n, 1)), "lu_inverse_z")
+    return M
+
+
 def lu_det_z(LU: torch.Tensor, P: torch.Tensor):
     """(det, logdet, sign) of the matrix factored in LU (complex128), as
     LUDiv::det / logDet (tmvg_lu_det_z64)."""
