@@ -96,6 +96,20 @@ class _Backend:
         return P
 
     # complex<double>: column-major (Fortran-order) complex128 arrays
+    def multmm_z(self, add: bool, alpha: complex, A: np.ndarray, B: np.ndarray, Cm: np.ndarray) -> None:
+        """C (+)= alpha A B for complex128 arrays of any strides."""
+        for x in (A, B, Cm):
+            assert x.dtype == np.complex128
+        m, k = A.shape
+        n = B.shape[1]
+        al = np.array([complex(alpha).real, complex(alpha).imag])
+        f = self._f("multmm_z", C.c_int, [C.c_int, vp, i64, i64, i64, vp, i64, i64, vp, i64, i64,
+                                          vp, i64, i64])
+        rc = f(int(add), _p(al), m, n, k, _p(A), *_strides(A), _p(B), *_strides(B), _p(Cm),
+               *_strides(Cm))
+        if rc:
+            raise RuntimeError(f"multmm_z rc={rc}")
+
     def lu_decompose_z(self, A: np.ndarray) -> np.ndarray:
         """In place; returns P (int64)."""
         assert A.dtype == np.complex128 and A.flags.f_contiguous and A.shape[0] == A.shape[1]

@@ -19,7 +19,7 @@
 //   tmvref_det           m.det(), m.logDet(&s) (src/TMV_LUD.cpp:132-190)
 //   tmvref_batched_divide  one B_i/A_i per system, OpenMP over systems.
 //   tmvref_lu_decompose_z, tmvref_lu_ldiveq_z, tmvref_lu_rdiveq_z, tmvref_det_z,
-//   tmvref_inverse_z
+//   tmvref_inverse_z, tmvref_multmm_z
 //                        the same for std::complex<double> (column-major,
 //                        interleaved entries).
 //
@@ -242,6 +242,23 @@ int tmvref_tri_ldiveq(int upper, int unitdiag, ptrdiff_t n, const double* T, ptr
         const tmv::DiagType dt = unitdiag ? tmv::UnitDiag : tmv::NonUnitDiag;
         if (upper) Bv /= Tv.upperTri(dt);
         else Bv /= Tv.lowerTri(dt);
+    });
+}
+
+// C = alpha A B / C += alpha A B for complex views (the same expression
+// surface as tmvref_multmm)
+int tmvref_multmm_z(int add, const double* alpha, ptrdiff_t m, ptrdiff_t n, ptrdiff_t k,
+                    const double* A, ptrdiff_t sAi, ptrdiff_t sAj, const double* B, ptrdiff_t sBi,
+                    ptrdiff_t sBj, double* C, ptrdiff_t sCi, ptrdiff_t sCj)
+{
+    return guarded([&] {
+        typedef std::complex<double> Z;
+        const Z al(alpha[0], alpha[1]);
+        tmv::ConstMatrixView<Z> Av = tmv::MatrixViewOf(reinterpret_cast<const Z*>(A), m, k, sAi, sAj);
+        tmv::ConstMatrixView<Z> Bv = tmv::MatrixViewOf(reinterpret_cast<const Z*>(B), k, n, sBi, sBj);
+        tmv::MatrixView<Z> Cv = tmv::MatrixViewOf(reinterpret_cast<Z*>(C), m, n, sCi, sCj);
+        if (add) Cv += al * Av * Bv;
+        else Cv = al * Av * Bv;
     });
 }
 

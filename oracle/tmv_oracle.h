@@ -96,6 +96,10 @@ int oracle_lu_ldiveq_z(ptrdiff_t n, const double* LU, ptrdiff_t lda, const ptrdi
 /* B (nrows x n, column-major) := B (P L U)^-1, row by row */
 int oracle_lu_rdiveq_z(ptrdiff_t n, const double* LU, ptrdiff_t lda, const ptrdiff_t* P,
                        ptrdiff_t nrows, double* B, ptrdiff_t ldb);
+/* C (+)= alpha A B, strided complex views; alpha as (re, im) */
+int oracle_multmm_z(int add, const double* alpha, ptrdiff_t m, ptrdiff_t n, ptrdiff_t k,
+                    const double* A, ptrdiff_t sAi, ptrdiff_t sAj, const double* B, ptrdiff_t sBi,
+                    ptrdiff_t sBj, double* C, ptrdiff_t sCi, ptrdiff_t sCj);
 /* det and sign as (re, im) pairs */
 void oracle_lu_det_z(ptrdiff_t n, const double* LU, ptrdiff_t lda, const ptrdiff_t* P,
                      double* det, double* logdet, double* sign);

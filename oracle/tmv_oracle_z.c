@@ -347,3 +347,28 @@ void oracle_lu_det_z(ptrdiff_t n, const double* LU, ptrdiff_t lda, const ptrdiff
         det[1] = cimag(d);
     }
 }
+
+/* MultMM<add> for std::complex<double> (src/TMV_MultMM.cpp:405 through the
+ * tmv::Matrix expression surface): C = alpha A B, or C += alpha A B with
+ * add.  Strided views (element (i, j) of X at X[i*sXi + j*sXj], complex
+ * elements).  Each entry is alpha times its k-ordered sum, then stored or
+ * added; TMV's blocked complex kernels sum in another order, so values agree
+ * to rounding. */
+int oracle_multmm_z(int add, const double* alpha, ptrdiff_t m, ptrdiff_t n, ptrdiff_t k,
+                    const double* A, ptrdiff_t sAi, ptrdiff_t sAj, const double* B, ptrdiff_t sBi,
+                    ptrdiff_t sBj, double* C, ptrdiff_t sCi, ptrdiff_t sCj)
+{
+    const zc* a = (const zc*)A;
+    const zc* b = (const zc*)B;
+    zc* c = (zc*)C;
+    const zc al = CMPLX(alpha[0], alpha[1]);
+    for (idx j = 0; j < n; ++j)
+        for (idx i = 0; i < m; ++i) {
+            zc s = 0.0;
+            for (idx q = 0; q < k; ++q) s += a[i * sAi + q * sAj] * b[q * sBi + j * sBj];
+            const zc v = al * s;
+            if (add) c[i * sCi + j * sCj] += v;
+            else c[i * sCi + j * sCj] = v;
+        }
+    return ORACLE_OK;
+}

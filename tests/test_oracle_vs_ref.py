@@ -211,3 +211,19 @@ def test_complex_rdiveq_and_det_match_tmv(orc, ref):
     for backend, (f, p) in ((orc, (A1, p1)), (ref, (A2, p2))):
         with pytest.raises(oracle.OracleSingular):
             backend.rdiveq_z(f, p, np.asfortranarray(np.ones((1, 3), dtype=np.complex128)))
+
+
+@pytest.mark.parametrize("layouts", ["FFF", "CFF", "FCF", "FFC", "CCC"])
+def test_complex_products_match_tmv(orc, ref, layouts):
+    # MultMM<add> for complex<double> in TMV's layouts (F: column-major,
+    # C: row-major for A, B, C), C = alpha A B and C += alpha A B
+    rng = np.random.default_rng(47)
+    for (m, n, k) in [(1, 1, 1), (7, 5, 3), (64, 64, 64), (100, 37, 80)]:
+        def mk(r, c, o):
+            return np.asarray(rng.standard_normal((r, c)) + 1j * rng.standard_normal((r, c)), order=o)
+        A, B, C0 = mk(m, k, layouts[0]), mk(k, n, layouts[1]), mk(m, n, layouts[2])
+        for add in (0, 1):
+            c1, c2 = C0.copy(order="K"), C0.copy(order="K")
+            orc.multmm_z(add, 0.7 - 1.3j, A, B, c1)
+            ref.multmm_z(add, 0.7 - 1.3j, A, B, c2)
+            assert np.abs(c1 - c2).max() <= 1e-13 * np.abs(c2).max(), (m, n, k, add)
