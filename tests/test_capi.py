@@ -53,6 +53,19 @@ def test_null_handle_is_rejected(lib):
     # entry points check their handle before touching the device
     assert lib.tmvg_synchronize(None) == 3
     assert lib.tmvg_lu_decompose_f64(None, 4, None, 4, None) == 3
+    # the complex<double> entry points too
+    import ctypes as C
+
+    lib.tmvg_lu_decompose_z64.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p]
+    assert lib.tmvg_lu_decompose_z64(None, 4, None, 4, None) == 3
+    for name in ("tmvg_lu_ldiveq_z64", "tmvg_lu_rdiveq_z64"):
+        f = getattr(lib, name)
+        f.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p,
+                      C.c_int64]
+        assert f(None, 4, None, 4, None, 1, None, 4) == 3
+    lib.tmvg_lu_inverse_z64.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p,
+                                        C.c_void_p, C.c_int64]
+    assert lib.tmvg_lu_inverse_z64(None, 4, None, 4, None, None, 4) == 3
 
 
 def test_library_is_sm103a_only():
