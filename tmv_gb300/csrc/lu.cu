@@ -2111,13 +2111,17 @@ template tmvg_status copy_matrix<float>(Context*, int64_t, int64_t, const float*
 // device memory is owned entirely by another allocator (a framework's caching
 // allocator or a fixed arena that must not see cudaMalloc behind its back),
 // and code paths where an allocation's latency or failure is not acceptable.
-// tmvg_lu_decompose_f64_noalloc serves them: it runs the same kernels as
-// tmvg_lu_decompose_f64 but takes every scratch word from the file-scope
-// array below, which each GPU that loads this library holds until the process
-// exits (kNoAllocBytes = 353,540 bytes, about 345 KiB).  It needs no tmvg_handle (creating one
-// allocates).  Limits: n <= kNoAllocMaxN = 16384 (larger n returns
-// TMVG_UNSUPPORTED before any device work); at most kNoAllocMaxCtas = 160
-// panel CTAs are used.
+// tmvg_lu_decompose_f64_noalloc serves them.  It applies the pivot rule of
+// tmvg_lu_decompose_f64 and gives the same factors to rounding, but runs the
+// simplest schedule: the cooperative grid-barrier panel (lu_panel_kernel)
+// with no look-ahead, and every scratch word taken from the file-scope array
+// below, which each GPU that loads this library holds until the process
+// exits (kNoAllocBytes = 353,540 bytes, about 345 KiB).  It needs no
+// tmvg_handle (creating one allocates).  Limits: n <= kNoAllocMaxN = 16384
+// (larger n returns TMVG_UNSUPPORTED before any device work); at most
+// kNoAllocMaxCtas = 160 panel CTAs are used, and a panel CTA's rows must fit
+// in 200 KiB of shared memory (TMVG_UNSUPPORTED otherwise, also before any
+// device work; on a GPU with at least 40 SMs every n <= 16384 fits).
 // =====================================================================
 namespace tmvg {
 namespace {
@@ -2132,35 +2136,27 @@ constexpr size_t kNaOffDiag = kNaOffRows + sizeof(double) * 2 * kNoAllocMaxCtas 
 constexpr size_t kNaOffModes = kNaOffDiag + sizeof(double) * 2 * kPanelMax;
 constexpr size_t kNaOffPairs = kNaOffModes + kNoAllocMaxN;  // int[1 + 2*kMaxPairs]
 constexpr size_t kNoAllocBytes = kNaOffPairs + sizeof(int) * (1 + 2 * kMaxPairs);
-constexpr int kNoAllocMaxDevices = 64;
+constexpr size_t kNoAllocSmemMax = 200 * 1024;
 }  // namespace
 
 static __device__ __align__(256) unsigned char g_lu_noalloc_scratch[kNoAllocBytes];
 
-// Device address of the scratch array on `device` (which must be current).
-// The host-side name of a __device__ array is only a stand-in, so the
-// address is asked of the runtime once per device and cached.
-static unsigned char* noalloc_scratch(int device, tmvg_status* st)
+// Device address of the scratch array in the current context.  The host-side
+// name of a __device__ array is only a stand-in, so the address is asked of
+// the runtime on every call: the lookup allocates nothing, and a cached value
+// would go stale when the module is loaded again (after cudaDeviceReset, or
+// in another context on the same device).
+static unsigned char* noalloc_scratch(tmvg_status* st)
 {
-    static std::mutex mu;
-    static unsigned char* addr[kNoAllocMaxDevices] = {};
-    std::lock_guard<std::mutex> lock(mu);
-    if (device < 0 || device >= kNoAllocMaxDevices) {
-        *st = TMVG_UNSUPPORTED;
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_lu_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        cudaGetLastError();
+        *st = TMVG_CUDA_ERROR;
         return nullptr;
     }
-    if (!addr[device]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_lu_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            cudaGetLastError();
-            *st = TMVG_CUDA_ERROR;
-            return nullptr;
-        }
-        addr[device] = static_cast<unsigned char*>(p);
-    }
     *st = TMVG_OK;
-    return addr[device];
+    return static_cast<unsigned char*>(p);
 }
 
 }  // namespace tmvg
@@ -2179,8 +2175,21 @@ extern "C" tmvg_status tmvg_lu_decompose_f64_noalloc(int64_t n, double* A, int64
         cudaGetLastError();
         return TMVG_NO_DEVICE;
     }
+    // The first panel holds the most rows per CTA: refuse a size whose rows
+    // do not fit in shared memory before any device work.
+    const int nbmax = panel_width<double>();
+    {
+        const int G0 = (int)std::min<int64_t>(std::min(sms, kNoAllocMaxCtas), ceil_div(n, kPanelThreads));
+        const size_t smem0 = (size_t)ceil_div(n, G0) * (std::min<int64_t>(nbmax, n) + 1) * sizeof(double);
+        if (smem0 > kNoAllocSmemMax) return TMVG_UNSUPPORTED;
+    }
+    if (cudaFuncSetAttribute(lu_panel_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kNoAllocSmemMax) != cudaSuccess) {
+        cudaGetLastError();
+        return TMVG_CUDA_ERROR;
+    }
     tmvg_status st = TMVG_OK;
-    unsigned char* s = noalloc_scratch(dev, &st);
+    unsigned char* s = noalloc_scratch(&st);
     if (!s) return st;
 
     // A context on the stack: no workspace, flags and barrier in the scratch.
@@ -2209,9 +2218,6 @@ extern "C" tmvg_status tmvg_lu_decompose_f64_noalloc(int64_t n, double* A, int64
         st = check_cuda(&c, cudaStreamSynchronize(c.stream), "noalloc: modes sync");
         if (st) return st;
     }
-    const int nbmax = panel_width<double>();
-    cudaFuncSetAttribute(lu_panel_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         200 * 1024);
     for (int64_t k = 0; k < n; k += nbmax) {
         const int nb = (int)std::min<int64_t>(nbmax, n - k);
         const int64_t m = n - k;
