@@ -42,10 +42,20 @@ def build_port() -> Path:
     return PORT_LIB
 
 
-def build_ref(reference: str = "/root/reference") -> Path | None:
+def build_ref(reference: str | Path, jobs: int | None = None,
+              tmv_obj: str | Path | None = None) -> Path | None:
+    """Compile TMV from the source tree `reference` into oracle/_ref
+    (tmv_obj: a directory holding TMV's objects already compiled from that
+    tree with the same flags, linked instead of compiled again)."""
+    import os
+
     if not Path(reference, "src", "TMV_LUDecompose.cpp").exists():
         return None
-    subprocess.run(["make", "-s", "-j8", "-C", str(HERE), "ref", f"REF={reference}"], check=True)
+    jobs = jobs or (os.cpu_count() or 4)
+    cmd = ["make", "-s", f"-j{jobs}", "-C", str(HERE), "ref", f"REF={reference}"]
+    if tmv_obj is not None:
+        cmd.append(f"TMV_OBJ={tmv_obj}")
+    subprocess.run(cmd, check=True)
     return REF_LIB
 
 

@@ -1,37 +1,31 @@
-"""The link-time drop-in under unmodified TMV (tmv_gb300/shim).
+"""The link-time drop-in under unmodified TMV (tmv_gb300/shim), on the CPU.
 
-Builds libtmv_gb300_dropin.so from the TMV sources where they are present
-(the build needs them) and checks that TMV's own entry points for real double
-data now come from the shim, that TMV's CPU code stays reachable under the
-renamed names for the other types, and that a program using only TMV's API
-links and reports a missing GPU through TMV's exception type.  No GPU needed.
+Builds libtmv_gb300_dropin.so from a TMV source tree ($TMV_REFERENCE, or the
+copy in third_party/tmv that the build stages) and checks that TMV's own entry
+points for real double data now come from the shim, that TMV's CPU code stays
+reachable under the renamed names for the other types, that the surface
+program of the GPU drop-in tests runs against stock TMV, and that a program
+linked to the drop-in reports a missing GPU through TMV's exception type.  No
+GPU needed (tests/test_gpu_dropin.py runs the same programs on one).
 """
-import os
 import subprocess
-from pathlib import Path
 
+import numpy as np
 import pytest
 
-import oracle
+from tmv_gb300.build import tmv_source_dir
 
-ROOT = Path(__file__).resolve().parent.parent
-SHIM = ROOT / "tmv_gb300" / "shim"
-REF = Path(os.environ.get("TMV_REFERENCE", "/root/reference"))
+TMV = tmv_source_dir()
 
-pytestmark = pytest.mark.skipif(not (REF / "src" / "TMV_MultMM.cpp").exists(),
-                                reason="TMV sources not present")
+pytestmark = pytest.mark.skipif(TMV is None,
+                                reason="no TMV source tree ($TMV_REFERENCE or third_party/tmv)")
 
 
 @pytest.fixture(scope="module")
 def dropin():
-    from tmv_gb300.build import LIB, build_library
+    from tmv_gb300.build import build_dropin
 
-    if not LIB.exists():
-        build_library()
-    if not oracle.ref_available():
-        oracle.build_ref(str(REF))
-    subprocess.run(["make", "-s", "-j8", "-C", str(SHIM), f"REF={REF}"], check=True)
-    return SHIM / "_build"
+    return build_dropin(TMV)
 
 
 def symbols(path, defined_only=True):
@@ -71,3 +65,25 @@ def test_unmodified_tmv_program_links_and_reports(dropin):
         assert "tmv::Error" in r.stdout and "tmvg_create" in r.stdout
     else:
         assert r.returncode == 0, r.stdout
+
+
+def test_surface_program_runs_on_stock_tmv(dropin, tmp_path):
+    """The GPU drop-in test's program, linked to stock TMV: every step runs,
+    the singular solve throws tmv::Singular, and the product agrees with
+    numpy."""
+    import test_gpu_dropin as T
+
+    exe = tmp_path / "tmv_surface_stock"
+    subprocess.run(["g++", "-O2", "-std=gnu++17", "-w", "-DNOBLAS", "-DNOLAP", "-DTMV_NDEBUG",
+                    f"-I{TMV}/include", "-fopenmp", "-o", str(exe), T.SURFACE, f"-L{dropin}",
+                    "-ltmv_stock", f"-Wl,-rpath,{dropin}"], check=True)
+    n, k, p = 40, 17, 3
+    T.write_inputs(tmp_path, np.random.default_rng(5), n, k, p)
+    steps, _ = T.run(exe, tmp_path)
+    assert steps["singular_ldiv"] == "throw Singular"
+    assert all(v == "ok" for s, v in steps.items() if s != "singular_ldiv"), steps
+    raw = np.fromfile(tmp_path / "in.bin", dtype=np.float64)[3:]
+    A = raw[:n * k].reshape((n, k), order="F")
+    B = raw[n * k:n * k + k * p].reshape((k, p), order="F")
+    C = T.load(tmp_path, "prod_ccc", (n, p))
+    assert np.abs(C - A @ B).max() <= 1e-13 * np.abs(A @ B).max()

@@ -1,0 +1,126 @@
+"""Unmodified TMV code on the GPU through the link-time drop-in.
+
+tests/dropin/tmv_surface.cpp uses TMV's public API only: C = A*B in every
+layout, m.divideUsing(tmv::LU), saveDiv, X = R/m, x = b/m, Y = W%m, X /= m,
+det / logDet / isSingular, m.inverse(), the factors and pivots, a row-major m,
+LU_Decompose of a tall and a wide matrix, and a singular m.  The same source
+is linked twice: to stock TMV (compiled from TMV's sources on this machine by
+the drop-in's build) and to libtmv_gb300_dropin.so, where every real double
+product, factorisation, solve and inverse runs on the GPU.  Both programs read
+the same inputs; the test compares what they write:
+* products within 1e-13 relative Frobenius error (the GEMM bar);
+* identical pivot sequences; factors, solves and inverses within 1e-12;
+* determinants within 1e-12 relative, the same sign and singularity verdict;
+* the same outcome of every step: a singular m throws tmv::Singular in both.
+The drop-in run also reports how many calls entered the GPU path.
+"""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from helpers import rel_frob
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SURFACE = os.path.join(ROOT, "tests", "dropin", "tmv_surface.cpp")
+
+
+@pytest.fixture(scope="module")
+def programs(tmp_path_factory):
+    from tmv_gb300.build import OUT as CUDA_OUT
+    from tmv_gb300.build import build_dropin, tmv_source_dir
+
+    tmv = tmv_source_dir()
+    if tmv is None:
+        pytest.skip("no TMV source tree ($TMV_REFERENCE or third_party/tmv)")
+    shim = build_dropin(tmv)
+    d = tmp_path_factory.mktemp("dropin")
+    flags = ["-O2", "-std=gnu++17", "-w", "-DNOBLAS", "-DNOLAP", "-DTMV_NDEBUG",
+             f"-I{tmv}/include", "-fopenmp"]
+    progs = {}
+    for name, libs in (("stock", ["-ltmv_stock"]),
+                       ("gpu", ["-ltmv_gb300_dropin", f"-L{CUDA_OUT}", "-ltmvg",
+                                f"-Wl,-rpath,{CUDA_OUT}"])):
+        exe = d / f"tmv_surface_{name}"
+        subprocess.run(["g++", *flags, "-o", str(exe), SURFACE, f"-L{shim}", *libs,
+                        f"-Wl,-rpath,{shim}"], check=True)
+        progs[name] = exe
+    return progs
+
+
+def haar(rng, n):
+    q, r = np.linalg.qr(rng.standard_normal((n, n)))
+    return q * np.sign(np.diag(r))
+
+
+def write_inputs(d, rng, n, k, p):
+    M = haar(rng, n) @ np.diag(np.logspace(0, -1, n)) @ haar(rng, n).T  # cond 10
+    S = M.copy()
+    S[:, min(3, n - 1)] = 0.0  # exactly singular
+    arrays = [rng.uniform(-1, 1, (n, k)), rng.uniform(-1, 1, (k, p)), M,
+              rng.standard_normal((n, p)), rng.standard_normal((p, n)),
+              rng.standard_normal((n, 1)), S]
+    with open(d / "in.bin", "wb") as f:
+        f.write(np.array([n, k, p], dtype=np.int64).tobytes())
+        for a in arrays:
+            f.write(np.asfortranarray(a).tobytes(order="F"))
+
+
+def run(exe, d, env_extra=None):
+    env = dict(os.environ, **(env_extra or {}))
+    r = subprocess.run([str(exe), str(d)], capture_output=True, text=True, timeout=600, env=env)
+    assert r.returncode == 0, r.stdout + r.stderr
+    steps = {}
+    for line in (d / "results.txt").read_text().splitlines():
+        name, outcome = line.split(" ", 1)
+        steps[name] = "throw Error" if outcome.startswith("throw Error") else outcome
+    return steps, r.stderr
+
+
+def load(d, name, shape):
+    v = np.fromfile(d / f"{name}.bin", dtype=np.float64)
+    return v.reshape(shape, order="F") if shape is not None else v
+
+
+@pytest.mark.parametrize("n,k,p", [(520, 260, 9), (5, 3, 2)])
+def test_tmv_program_on_the_gpu_matches_stock_tmv(programs, tmp_path, n, k, p):
+    dirs = {}
+    for name in ("stock", "gpu"):
+        d = tmp_path / name
+        d.mkdir()
+        write_inputs(d, np.random.default_rng(8100 + n), n, k, p)
+        dirs[name] = d
+    ref_steps, _ = run(programs["stock"], dirs["stock"])
+    gpu_steps, err = run(programs["gpu"], dirs["gpu"], {"TMVG_SHIM_STATS": "1"})
+    assert gpu_steps == ref_steps
+    assert ref_steps["singular_ldiv"] == "throw Singular"
+    assert all(v == "ok" for s, v in ref_steps.items() if s != "singular_ldiv")
+    m = re.search(r"tmvg drop-in: (\d+) GPU calls", err)
+    assert m and int(m.group(1)) >= 20, err
+
+    S, G = dirs["stock"], dirs["gpu"]
+    n2, p2 = (n + 1) // 2, (p + 1) // 2
+    shapes = {"prod_ccc": (n, p), "prod_rcc": (n, p), "prod_crc": (n, p), "prod_rm_c": (n, p),
+              "prod_add": (n, p), "prod_views": (n2, p2), "prod_transpose": (p, n)}
+    for name, shape in shapes.items():
+        e = rel_frob(load(G, name, shape), load(S, name, shape))
+        assert e <= 1e-13, f"{name}: {e:.2e}"
+    assert np.array_equal(load(G, "lu_pivots", None), load(S, "lu_pivots", None))
+    for name, shape in {"lu_factors": (n, n), "lu_ldiv": (n, p), "lu_ldiv_vec": (n, 1),
+                        "lu_rdiv": (p, n), "lu_ldiveq": (n, p), "lu_inverse": (n, n),
+                        "rm_ldiv": (n, p), "rm_rdiv": (p, n)}.items():
+        e = rel_frob(load(G, name, shape), load(S, name, shape))
+        assert e <= 1e-12, f"{name}: {e:.2e}"
+    for name, shape in (("lu_tall", (n, k)), ("lu_wide", (k, n))):
+        assert np.array_equal(load(G, name + "_pivots", None), load(S, name + "_pivots", None))
+        e = rel_frob(load(G, name, shape), load(S, name, shape))
+        assert e <= 1e-12, f"{name}: {e:.2e}"
+    dg, ds = load(G, "lu_det", None), load(S, "lu_det", None)
+    assert abs(dg[0] - ds[0]) <= 1e-12 * abs(ds[0])
+    assert abs(dg[1] - ds[1]) <= 1e-12 * max(abs(ds[1]), 1.0)
+    assert dg[2] == ds[2] and dg[3] == ds[3]
+    assert np.array_equal(load(G, "singular_det", None), load(S, "singular_det", None))

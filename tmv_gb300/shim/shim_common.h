@@ -35,7 +35,9 @@ void TMVG_CPU_LU_Inverse(const GenMatrix<T1>& LUx, const ptrdiff_t* P, MatrixVie
 
 namespace tmvg_shim {
 
-// One context per process, on device $TMVG_DEVICE (default 0).
+// One context per process, on device $TMVG_DEVICE (default 0).  Every call
+// counts one entry into the GPU path; with $TMVG_SHIM_STATS set the count is
+// printed to stderr when the process exits ("tmvg drop-in: N GPU calls").
 tmvg_handle gpu();
 
 // TMV's error conventions (include/tmv/TMV_Base.h:502-648): allocation

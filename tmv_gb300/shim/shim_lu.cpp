@@ -1,9 +1,12 @@
 // shim_lu.cpp -- tmv::LU_Decompose (src/TMV_LUDecompose.cpp:514-559) and
 // tmv::LU_LDivEq / LU_RDivEq (src/TMV_LUDiv.cpp:186-226, 370-411) and
 // tmv::LU_Inverse (src/TMV_LUInverse.cpp:236-299) for every instantiation of
-// TMV_LUDecompose.inst, TMV_LUDiv.inst and TMV_LUInverse.inst.  Square real
-// double problems go to the GPU; the other types (and rectangular
-// LU_Decompose, which LUDiv never asks for) run TMV's own CPU code.
+// TMV_LUDecompose.inst, TMV_LUDiv.inst and TMV_LUInverse.inst.  Real double
+// problems go to the GPU (a rectangular LU_Decompose through a padded square
+// factorisation, below); the other types run TMV's own CPU code.
+#include <string>
+#include <vector>
+
 #include "TMV_LUDiv.h"
 #include "shim_common.h"
 #include "tmv/TMV_LUD.h"
@@ -16,11 +19,44 @@
 
 namespace tmv {
 
+static void gpu_lu_decompose(MatrixView<double> A, ptrdiff_t* P);
+
+// LU_Decompose of an M x N matrix, M != N (TMV factors its R = min(M,N)
+// columns, src/TMV_LUDecompose.cpp:217-235, and writes R interchanges).  The
+// GPU factors the S x S matrix, S = max(M,N), that holds A in its top-left
+// block, the identity in its trailing (S-R) x (S-R) block and zeros
+// elsewhere.  Steps j < R see exactly TMV's columns (the padding adds no
+// candidate larger than a real one: its entries in those columns are zero),
+// so the first R pivots and A's factors are TMV's.  A wide A is then done
+// (steps j >= R touch only padding rows).  For a tall A the steps j >= R may
+// interchange rows >= R of the factored columns, so those interchanges are
+// undone on A's columns, last first.  Shapes far from square would pad to
+// far more memory than A holds: above 16 M N padded elements (and S > 4096)
+// the call throws tmv::Error rather than leave the GPU.
+static void gpu_lu_decompose_rect(MatrixView<double> A, ptrdiff_t* P)
+{
+    const ptrdiff_t M = A.colsize(), N = A.rowsize();
+    const ptrdiff_t R = std::min(M, N), S = std::max(M, N);
+    if ((double)S * (double)S > 16.0 * (double)M * (double)N && S > 4096)
+        throw Error("tmv::LU_Decompose: a " + std::to_string(M) + " x " + std::to_string(N) +
+                    " matrix is too far from square for the GPU path");
+    Matrix<double, ColMajor> Ap(S, S, 0.0);
+    Ap.subMatrix(0, M, 0, N) = A;
+    for (ptrdiff_t t = R; t < S; ++t) Ap(t, t) = 1.0;
+    std::vector<ptrdiff_t> Pp(S);
+    gpu_lu_decompose(Ap.view(), Pp.data());
+    if (M > N)
+        for (ptrdiff_t j = S - 1; j >= R; --j)
+            if (Pp[j] != j) Ap.subMatrix(0, S, 0, N).swapRows(j, Pp[j]);
+    A = Ap.subMatrix(0, M, 0, N);
+    for (ptrdiff_t j = 0; j < R; ++j) P[j] = Pp[j];
+}
+
 static void gpu_lu_decompose(MatrixView<double> A, ptrdiff_t* P)
 {
     using namespace tmvg_shim;
     if (A.colsize() != A.rowsize()) {
-        TMVG_CPU_LU_Decompose(A, P);
+        if (A.colsize() > 0 && A.rowsize() > 0) gpu_lu_decompose_rect(A, P);
         return;
     }
     if (!dense_view(A)) {
