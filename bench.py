@@ -10,9 +10,10 @@ FP64-equivalent TFLOP/s, (2n^3/3 + 2n^2 nrhs) per solve.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
---impl reference times TMV's CPU algorithm (the oracle's C restatement of
-TMV's LU_Decompose + LU_LDivEq with its OpenMP product) on the host cores on
-the same workload and prints the same JSON line with "impl": "reference".
+--impl reference times TMV's own CPU path on the host cores on the same
+workload (TMV 0.76 compiled from its sources on this machine where the build
+step found them, else the oracle's C restatement of the same algorithm) and
+prints the same JSON line with "impl": "reference".
 Inputs are 512 MiB (A in FP64), larger than the 129 MB L2, so no flush is
 needed between steps.
 """
@@ -126,6 +127,19 @@ class ClockSampler:
     def window(self, t0: float, t1: float):
         self.t0, self.t1 = t0, t1
 
+    def median_between(self, t0: float, t1: float) -> float | None:
+        """Median SM clock (MHz) of the samples read between t0 and t1."""
+        time.sleep(0.05)
+        sm = []
+        for t, ln in list(self.lines):
+            if t0 <= t <= t1:
+                f = [x.strip() for x in ln.split(",")]
+                try:
+                    sm.append(float(f[1]))
+                except (IndexError, ValueError):
+                    pass
+        return float(np.median(sm)) if sm else None
+
     def stop(self) -> dict:
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
@@ -173,9 +187,26 @@ def peaks() -> dict:
             "_source": "fallback"}
 
 
-# FP64 DFMA peak of a GB300, measured by a DFMA throughput kernel on this machine
-# (1.19 TFLOP/s at ~1990 MHz; the m8n8k4 DMMA path measured 1.05 TFLOP/s).
-FP64_DFMA_PEAK_TFLOPS = 1.19
+# The FP64 FMA rate every FP64-bound fraction is measured against: taken in
+# this process by the library's DFMA throughput kernel (tmvg_probe_fp64_rate)
+# right after the headline's timed region, under the same sampled clocks.
+FP64_PEAK: dict = {"tflops": None}
+
+
+def measure_fp64_peak(h, clocks) -> dict:
+    t0 = time.time()
+    tf = h.fp64_rate()
+    t1 = time.time()
+    FP64_PEAK.update({"tflops": round(tf, 4), "sm_mhz": clocks.median_between(t0, t1),
+                      "source": "tmvg_probe_fp64_rate (DFMA throughput kernel) in this run"})
+    return dict(FP64_PEAK)
+
+
+def fp64_roofline(achieved_tflops: float) -> dict:
+    pk = FP64_PEAK["tflops"]
+    return {"bound": "fp64", "achieved": round(achieved_tflops, 4), "peak": pk, "unit": "TFLOP/s",
+            "frac": round(achieved_tflops / pk, 4) if pk else None,
+            "peak_source": FP64_PEAK.get("source", "not measured")}
 
 
 def run_gpu(args) -> dict:
@@ -273,6 +304,7 @@ def run_gpu(args) -> dict:
     e1.record(stream)
     torch.cuda.synchronize()
     clocks.window(tw0, time.time())
+    fp64_peak = measure_fp64_peak(h, clocks)
     ms = e0.elapsed_time(e1)
     if world > 1:
         ms = max_over_ranks(ms, dev)
@@ -312,24 +344,29 @@ def run_gpu(args) -> dict:
     else:
         cpu = None
     its = [i[0] for i in infos]
+    sweep = None
+    if mixed and not args.no_extras and not args.no_sweep:
+        sweep = cond_sweep(dev, n, cond, Acm, B, X64, fp64_ms)
     out = {
         "metric": METRIC, "value": round(value, 4), "unit": "TFLOP/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(ms_step, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64" if mixed else "f64", "data": "synthetic",
+        "fp64_gpu_lu": {"value": round(flops / (fp64_ms * 1e-3) / 1e12, 4), "unit": "TFLOP/s",
+                        "ms_per_solve": round(fp64_ms, 3)},
+        "speedup_vs_fp64_gpu_lu": (round(fp64_ms / ms_step, 3) if X64 is not None else None),
+        "accuracy": {"backward_error": berr, "forward_rel_diff_vs_fp64_gpu_lu": fwd,
+                     "ir_iterations": (max(its) if its else None),
+                     "converged": all(i[1] == 1 for i in infos) if infos else None},
+        "equal_accuracy": (sweep["equal_accuracy_at_headline_cond"] if sweep else None),
         "config": {"workload": (f"dense solve n={n}, 1 RHS, cond={cond:g}, Haar U/V; "
                                 + ("FP32 LU + FP64 iterative refinement to backward error 1e-12"
                                    if mixed else "FP64 GPU LU")),
                    "path": args.path, "n": n, "nrhs": nrhs, "cond": cond,
                    "l2": "inputs larger than L2 (A is 512 MiB FP64); no flush"},
-        "accuracy": {"backward_error": berr, "forward_rel_diff_vs_fp64_gpu_lu": fwd,
-                     "ir_iterations": (max(its) if its else None),
-                     "converged": all(i[1] == 1 for i in infos) if infos else None},
-        "fp64_gpu_lu": {"value": round(flops / (fp64_ms * 1e-3) / 1e12, 4), "unit": "TFLOP/s",
-                        "ms_per_solve": round(fp64_ms, 3)},
-        "speedup_vs_fp64_gpu_lu": (round(fp64_ms / ms_step, 3) if X64 is not None else None),
-        "roofline": roof, "kernels": kernels, "e2e": e2e, "gpu_launches": int(launches),
-        "clocks": clk,
+        "roofline": roof, "e2e": e2e, "gpu_launches": int(launches),
+        "clocks": clk, "fp64_peak": fp64_peak,
+        "cond_sweep": (sweep["rows"] if sweep else None), "kernels": kernels,
     }
     if cpu is not None:
         out["cpu_baseline"] = cpu
@@ -340,6 +377,74 @@ def run_gpu(args) -> dict:
     if world > 1:
         torch.distributed.destroy_process_group()
     return out if rank == 0 else None
+
+
+def cond_sweep(dev, n: int, head_cond: float, A_head, B_head, X64_head, fp64_ms_head) -> dict:
+    """The mixed solve against the FP64 GPU LU at every condition number of
+    the workload (1e2, 1e4, 1e6; n = 8192, Haar U/V, 1 right-hand side):
+    * at the headline tolerance (normwise backward error <= 1e-12);
+    * at equal accuracy: the largest tolerance in (1e-14, 3e-15, 1e-15, 4e-16)
+      whose solution differs from the FP64 GPU LU's by at most 50 cond eps
+      (relative 2-norm), the accuracy of the FP64 LU itself;
+    each with its time, refinement steps and speed-up over the FP64 GPU LU on
+    the same system (CUDA events, device-resident inputs)."""
+    import torch
+
+    from tmv_gb300 import linalg
+
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(fn, reps, warm=1):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            r = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps, r
+
+    eps = float(np.finfo(np.float64).eps)
+    rows, head = [], None
+    for cond in (1e2, 1e4, 1e6):
+        if cond == head_cond:
+            A, B, X64, fp64_ms = A_head, B_head, X64_head, fp64_ms_head
+        else:
+            a, b = haar_matrix_torch(n, cond, seed=3, dev=dev)
+            A = linalg.colmajor(a)
+            del a
+            B = b.view(n, 1).clone()
+            fp64_ms, X64 = timed(lambda: linalg.divide(A, B)[0], reps=2)
+        bound = 50.0 * cond * eps
+
+        def mixed_at(tol, max_iter):
+            ms, (X, info) = timed(lambda: linalg.solve_mixed(A, B, max_iter=max_iter, tol=tol,
+                                                             raise_not_converged=False), reps=3)
+            fwd = float((X - X64).norm() / X64.norm())
+            return {"tol": tol, "ms_per_solve": round(ms, 3),
+                    "tflops": round(lu_solve_flops(n, 1) / (ms * 1e-3) / 1e12, 4),
+                    "ir_iterations": int(info.iterations), "converged": int(info.converged) == 1,
+                    "backward_error": float(info.backward_error),
+                    "forward_rel_diff_vs_fp64_gpu_lu": fwd,
+                    "speedup_vs_fp64_gpu_lu": round(fp64_ms / ms, 3)}
+
+        row = {"cond": cond, "fp64_gpu_lu_ms": round(fp64_ms, 3),
+               "mixed_tol_1e-12": mixed_at(1e-12, 10), "equal_accuracy_bound": bound}
+        eq = None
+        for tol in (1e-14, 3e-15, 1e-15, 4e-16):
+            r = mixed_at(tol, 30)
+            if r["converged"] and r["forward_rel_diff_vs_fp64_gpu_lu"] <= bound:
+                eq = r
+                break
+        row["mixed_equal_accuracy"] = eq
+        rows.append(row)
+        if cond == head_cond:
+            head = eq
+        del A, B, X64
+        torch.cuda.empty_cache()
+    return {"rows": rows, "equal_accuracy_at_headline_cond": head}
 
 
 def batched_workload(count: int, seed: int = 4):
@@ -392,10 +497,7 @@ def batched_bench(dev, args, with_cpu: bool) -> dict:
     out = {"value": round(count / (ms * 1e-3), 1), "unit": "solves/s", "systems": count,
            "ms_per_batch": round(ms, 3), "tflops_fp64": round(tflops, 4),
            "roofline": {"kernel": "batched_lu_kernel (FP64 LU + solve, one persistent launch)",
-                        "bound": "fp64", "achieved": round(tflops, 4),
-                        "peak": FP64_DFMA_PEAK_TFLOPS, "unit": "TFLOP/s",
-                        "frac": round(tflops / FP64_DFMA_PEAK_TFLOPS, 4),
-                        "peak_source": "measured FP64 DFMA throughput",
+                        **fp64_roofline(tflops),
                         "algorithmic_flop_per_launch": plan.flops},
            "panel_widths_by_class": plan.panel_widths, "singular_systems": bad,
            "config": "n_i ~ U{8..256}, nrhs_i ~ U{1..16}, A_i ~ N(0,1) + 2 sqrt(n_i) I, FP64, "
@@ -428,9 +530,7 @@ def batched_bench(dev, args, with_cpu: bool) -> dict:
         "config": "the same 20000 systems; per column ||b - A x||_inf <= 1e-12 (||A||_inf ||x||_inf + ||b||_inf), "
                   "at most 10 corrections"}
     if with_cpu:
-        import oracle
-
-        orc = oracle.port()
+        orc, kind, what = cpu_reference()
         cores = os.cpu_count() or 1
         orc.set_threads(cores)
         m = min(count, args.batch_cpu_sample)
@@ -440,9 +540,9 @@ def batched_bench(dev, args, with_cpu: bool) -> dict:
         orc.batched_divide(n[:m], r[:m], plan.a_off[:m], plan.b_off[:m], hA, hB)
         dt = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": round(m / dt, 1), "unit": "solves/s", "cores": cores,
-                               "kind": "port",
+                               "kind": kind,
                                "sample": f"first {m} systems of the batch, OpenMP over systems "
-                                         f"({dt:.2f} s)"}
+                                         f"({dt:.2f} s); {what}"}
     plan.close()
     return out
 
@@ -500,9 +600,8 @@ def dominant_roofline(kernels: dict, mixed: bool) -> dict | None:
     k = kernels[cls]
     pk = peaks()
     if cls == "trailing_update" and not mixed:
-        ach, peak = k["achieved_tflops"], FP64_DFMA_PEAK_TFLOPS
-        out = {"bound": "fp64", "unit": "TFLOP/s",
-               "peak_source": "measured FP64 DFMA throughput (MEASURED_PEAKS.json has no FP64 entry)"}
+        ach, peak = k["achieved_tflops"], FP64_PEAK["tflops"]
+        out = {"bound": "fp64", "unit": "TFLOP/s", "peak_source": FP64_PEAK.get("source")}
         per = k["alg_flops_per_span"]
     else:
         ach, peak = k["achieved_gbs"], float(pk["hbm_gbs"])
@@ -511,7 +610,7 @@ def dominant_roofline(kernels: dict, mixed: bool) -> dict | None:
         per = k["alg_bytes_per_span"]
     ratio = NCU_TRAFFIC_PER_ALG_BYTE.get(cls)
     out.update({"kernel": KERNEL_NAMES[cls], "class": cls, "achieved": ach, "peak": peak,
-                "frac": round(ach / peak, 4),
+                "frac": round(ach / peak, 4) if peak else None,
                 "traffic": (k["alg_bytes_per_span"] * ratio) if ratio else None,
                 "alg_per_launch": per, "ms_per_launch": k["ms_per_span"],
                 "share_of_step": k["share_of_step"]})
@@ -603,15 +702,11 @@ def other_workloads(dev, with_cpu: bool) -> dict:
     ms = ev_time(lambda: linalg.multmm(False, 1.0, A, Bm, C))
     tf = 2.0 * m ** 3 / (ms * 1e-3) / 1e12
     out["fp64_gemm_1024"] = {"value": round(tf, 4), "unit": "TFLOP/s", "ms": round(ms, 4),
-                             "roofline": {"bound": "fp64", "achieved": round(tf, 4),
-                                          "peak": FP64_DFMA_PEAK_TFLOPS, "unit": "TFLOP/s",
-                                          "frac": round(tf / FP64_DFMA_PEAK_TFLOPS, 4)},
+                             "roofline": fp64_roofline(tf),
                              "kernel": "gemm_simt_kernel<double> (MultMM, column-major operands)",
                              "flush": "256 MiB written between runs"}
     if with_cpu:
-        import oracle
-
-        orc = oracle.port()
+        orc, kind, what = cpu_reference()
         orc.set_threads(os.cpu_count() or 1)
         Ah, Bh = np.asfortranarray(A.cpu().numpy()), np.asfortranarray(Bm.cpu().numpy())
         Ch = np.zeros((m, m), order="F")
@@ -620,7 +715,7 @@ def other_workloads(dev, with_cpu: bool) -> dict:
         dt = time.perf_counter() - t0
         out["fp64_gemm_1024"]["cpu_baseline"] = {
             "value": round(2.0 * m ** 3 / dt / 1e12, 5), "unit": "TFLOP/s", "cores": os.cpu_count() or 1,
-            "kind": "port", "sample": f"one 1024^3 MultMM (OpenMP block product, {dt:.2f} s)"}
+            "kind": kind, "sample": f"one 1024^3 MultMM (OpenMP block product, {dt:.2f} s); {what}"}
     n = 4096
     A4 = torch.randn((n, n), dtype=torch.float64, device=dev, generator=g)
     A4 += 4.0 * np.sqrt(n) * torch.eye(n, dtype=torch.float64, device=dev)
@@ -630,9 +725,7 @@ def other_workloads(dev, with_cpu: bool) -> dict:
     fl = lu_solve_flops(n, 8)
     tf = fl / (ms * 1e-3) / 1e12
     out["fp64_lu_solve_4096"] = {"value": round(tf, 4), "unit": "TFLOP/s", "ms": round(ms, 3),
-                                 "roofline": {"bound": "fp64", "achieved": round(tf, 4),
-                                              "peak": FP64_DFMA_PEAK_TFLOPS, "unit": "TFLOP/s",
-                                              "frac": round(tf / FP64_DFMA_PEAK_TFLOPS, 4)},
+                                 "roofline": fp64_roofline(tf),
                                  "workload": "X = B/A, n = 4096, 8 right-hand sides, A ~ N(0,1) + 4 sqrt(n) I"}
     n = 2048
     A5 = torch.randn((n, n), dtype=torch.float64, device=dev, generator=g)
@@ -647,35 +740,47 @@ def other_workloads(dev, with_cpu: bool) -> dict:
         "forward_ms": round(fwd_ms, 3), "backward_ms": round(bwd_ms, 3),
         "forward_tflops": round(lu_solve_flops(n, 64) / (fwd_ms * 1e-3) / 1e12, 4),
         "backward_tflops": round(4.0 * n * n * 64 / (bwd_ms * 1e-3) / 1e12, 4),
+        "forward_roofline": fp64_roofline(lu_solve_flops(n, 64) / (fwd_ms * 1e-3) / 1e12),
+        "backward_roofline": fp64_roofline(4.0 * n * n * 64 / (bwd_ms * 1e-3) / 1e12),
         "workload": "X = A^-1 B (n = 2048, 64 right-hand sides), backward gB = A^-T G and gA = -gB X^T "
                     "from the stored factors"}
     del flush
     return out
 
 
-def cpu_baseline(A: np.ndarray, B: np.ndarray, n: int, cond: float) -> dict:
-    """TMV's FP64 LU + solve algorithm (oracle C restatement, OpenMP product)
-    on the host cores: one solve of the same workload (same A and b)."""
+def cpu_reference():
+    """The CPU implementation timed beside the GPU: TMV 0.76 itself where its
+    library was compiled on this machine (oracle/_ref, built from TMV's
+    sources by the build step: NOBLAS/NOLAP, OpenMP MultMM), else the
+    oracle's C restatement of the same algorithm.  Returns (backend, kind,
+    description)."""
     import oracle
 
-    orc = oracle.port()
+    if oracle.ref_available():
+        return (oracle.ref(), "reference",
+                "TMV 0.76 compiled from its sources on this machine (NOBLAS/NOLAP, OpenMP MultMM)")
+    return oracle.port(), "port", "the oracle's C restatement of TMV's algorithm"
+
+
+def cpu_baseline(A: np.ndarray, B: np.ndarray, n: int, cond: float) -> dict:
+    """TMV's FP64 LU + solve (m.divideUsing(tmv::LU); X = B/m) on the host
+    cores: one solve of the same workload (same A and b)."""
+    orc, kind, what = cpu_reference()
     cores = os.cpu_count() or 1
     orc.set_threads(cores)
     t0 = time.perf_counter()
     X, LU, P = orc.divide(A, B)
     dt = time.perf_counter() - t0
     return {"value": round(lu_solve_flops(n, 1) / dt / 1e12, 5), "unit": "TFLOP/s",
-            "cores": cores, "kind": "port",
-            "sample": f"one FP64 LU_Decompose + LU_LDivEq at n={n}, cond={cond:g} ({dt:.1f} s)"}
+            "cores": cores, "kind": kind,
+            "sample": f"one FP64 LU factor + solve at n={n}, cond={cond:g} ({dt:.1f} s); {what}"}
 
 
 def run_reference(args) -> dict | None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return None
-    import oracle
-
-    orc = oracle.port()
+    orc, kind, what = cpu_reference()
     cores = os.cpu_count() or 1
     orc.set_threads(cores)
     n = args.n
@@ -695,9 +800,9 @@ def run_reference(args) -> dict | None:
             "config": {"workload": f"dense LU solve n={n}, 1 RHS, cond={args.cond:g}",
                        "n": n, "nrhs": 1, "cond": args.cond},
             "cpu_baseline": {"value": round(v, 5), "unit": "TFLOP/s", "cores": cores,
-                             "kind": "port",
-                             "sample": f"{args.steps} FP64 LU solves at n={n} (TMV algorithm, "
-                                       "oracle C restatement; warm-up capped at 1)"},
+                             "kind": kind,
+                             "sample": f"{args.steps} FP64 LU solves at n={n} ({what}; "
+                                       "warm-up capped at 1)"},
             "e2e": {"value": round(v, 5), "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
 
@@ -718,6 +823,8 @@ def main():
                     help="load the workload matrix from this file if present, else save it "
                          "there (lets a profiler run skip the QR-based generation)")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-sweep", action="store_true",
+                    help="skip the condition-number / equal-accuracy sweep")
     ap.add_argument("--batch-count", type=int, default=20000)
     ap.add_argument("--batch-cpu-sample", type=int, default=2000)
     ap.add_argument("--no-extras", action="store_true",

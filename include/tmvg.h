@@ -87,6 +87,24 @@ tmvg_status tmvg_synchronize(tmvg_handle h);
 const char* tmvg_last_error(tmvg_handle h);
 /* Number of kernels this handle has launched since creation. */
 int64_t tmvg_launch_count(tmvg_handle h);
+/* FP64 FMA rate of the handle's device, a measurement hook with no
+ * counterpart in TMV: a throughput kernel of independent DFMA chains on every
+ * SM, timed with CUDA events on the handle's stream (best of three launches
+ * after one warm-up), returned as TFLOP/s (2 flops per FMA).  The FP64-bound
+ * roofline fractions of the benchmark use it, measured in the same process
+ * and under the same clocks as the work.  Synchronises the stream. */
+tmvg_status tmvg_probe_fp64_rate(tmvg_handle h, double* tflops);
+/* Failure-path test hook, no counterpart in TMV.  poll_limit sets how many
+ * polls the block-flag waits of the sync-free triangular solve (the solve of
+ * up to 8 right-hand sides behind tmvg_tri_ldiveq_f64, tmvg_lu_ldiveq_f64 and
+ * the FP64 solves) make before they give up (0 restores the default, 2^24
+ * polls with back-off).  skip_blocks > 0 makes the next such solve hand its
+ * 64-row blocks out from block skip_blocks on, so blocks [0, skip_blocks)
+ * are never solved and their flags never published: the first block that
+ * waits on one gives up after poll_limit polls, the others stop in turn, and
+ * the call returns TMVG_TIMEOUT with the handle still usable (the hook
+ * resets itself after that one launch).  Nothing traps or hangs. */
+tmvg_status tmvg_test_set_wait(tmvg_handle h, uint32_t poll_limit, int32_t skip_blocks);
 
 /* ---- MultMM ----------------------------------------------------------
  * C (+)= alpha * A * B;  A m x k, B k x n, C m x n.  add = 0: C = alpha*A*B,
@@ -136,16 +154,20 @@ tmvg_status tmvg_lu_decompose_f64_host(tmvg_handle h, int64_t n, double* A,
  * No counterpart in TMV: an extra entry point for callers that cannot
  * allocate device memory (their device memory belongs to another allocator,
  * such as a framework's caching allocator or a fixed arena, or an allocation
- * is not acceptable on their code path).  Same result as
- * tmvg_lu_decompose_f64 for a column-major n x n device matrix A and device
- * pivots P, but it calls no cudaMalloc/cudaFree and needs no tmvg_handle:
- * all scratch lives in one static device array of 353,540 bytes (345 KiB) that every
- * GPU loading this library holds until the process exits.  Runs on the
- * current device and the given cudaStream_t (NULL: legacy default stream);
- * synchronous.  Limit: n <= 16384, larger n returns TMVG_UNSUPPORTED.  The
- * first call on a device looks up the array's device address; make that
- * first call before any stream capture.  Calls share the array, so calls
- * that overlap on the GPU (other threads or streams) race: serialise them. */
+ * is not acceptable on their code path).  For a column-major n x n device
+ * matrix A and device pivots P it applies the pivot rule of
+ * tmvg_lu_decompose_f64 and gives the same factors to rounding (it runs the
+ * simplest schedule: the grid-barrier panel kernel, no look-ahead), but it
+ * calls no cudaMalloc/cudaFree and needs no tmvg_handle: all scratch lives in
+ * one static device array of 353,540 bytes (345 KiB) that every GPU loading
+ * this library holds until the process exits; each call looks up the array's
+ * device address in the current context.  Runs on the current device and
+ * the given cudaStream_t (NULL: legacy default stream) and synchronises that
+ * stream before it returns.  Limit: n <= 16384, and a panel CTA's rows must
+ * fit in 200 KiB of shared memory (every n <= 16384 does on a GPU with at
+ * least 40 SMs); other sizes return TMVG_UNSUPPORTED before any device work.
+ * Calls share the array, so calls that overlap on the GPU (other threads or
+ * streams) race: serialise them. */
 tmvg_status tmvg_lu_decompose_f64_noalloc(int64_t n, double* A, int64_t lda,
                                           int64_t* P, void* cuda_stream);
 

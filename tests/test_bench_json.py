@@ -1,7 +1,7 @@
 """bench.py's JSON helpers on the CPU: the LU-solve flop count, the roofline
 entry of the dominant kernel class (HBM-bound classes against the measured
-copy bandwidth, the FP64 trailing update against the DFMA rate, the panel
-with its latency limiter) and the kernel-class breakdown."""
+copy bandwidth, the FP64 trailing update against the DFMA rate measured in
+the run, the panel with its latency limiter) and the kernel-class breakdown."""
 import math
 
 import bench
@@ -33,9 +33,10 @@ def test_panel_roofline_names_its_limiter():
 def test_fp64_update_roofline_is_dfma_bound():
     k = {"trailing_update": _cls(300.0, 100.0, 1.0, 1e9, 1e12, 2.0, 0.85),
          "panel": _cls(20.0, 10.0, 0.1, 1e6, 1e7, 0.09, 0.06)}
+    bench.FP64_PEAK.update({"tflops": 1.25, "source": "test"})
     r = bench.dominant_roofline(k, mixed=False)
     assert r["bound"] == "fp64" and r["unit"] == "TFLOP/s"
-    assert r["peak"] == bench.FP64_DFMA_PEAK_TFLOPS
+    assert r["peak"] == 1.25 and r["frac"] == round(1.0 / 1.25, 4)
     assert "limiter" not in r
     # the FP64 panel is 32 columns wide
     k["panel"]["ms_per_step"] = 400.0
@@ -45,3 +46,12 @@ def test_fp64_update_roofline_is_dfma_bound():
 
 def test_empty_breakdown_has_no_roofline():
     assert bench.dominant_roofline({}, mixed=True) is None
+
+
+def test_fp64_roofline_uses_the_measured_peak():
+    bench.FP64_PEAK.update({"tflops": 1.2, "source": "test"})
+    r = bench.fp64_roofline(0.9)
+    assert r == {"bound": "fp64", "achieved": 0.9, "peak": 1.2, "unit": "TFLOP/s", "frac": 0.75,
+                 "peak_source": "test"}
+    bench.FP64_PEAK.update({"tflops": None})
+    assert bench.fp64_roofline(0.9)["frac"] is None

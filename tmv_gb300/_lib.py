@@ -59,6 +59,8 @@ _SIGS = {
     "tmvg_synchronize": (C.c_int, [vp]),
     "tmvg_last_error": (C.c_char_p, [vp]),
     "tmvg_launch_count": (i64, [vp]),
+    "tmvg_probe_fp64_rate": (C.c_int, [vp, C.POINTER(dbl)]),
+    "tmvg_test_set_wait": (C.c_int, [vp, C.c_uint32, C.c_int32]),
     "tmvg_timing_enable": (C.c_int, [vp, C.c_int]),
     "tmvg_timing_read": (C.c_int, [vp, C.c_int, C.POINTER(KernelTiming)]),
     "tmvg_multmm_f64": (C.c_int, [vp, C.c_int, dbl, i64, i64, i64, vp, i64, i64, vp, i64, i64,
@@ -166,6 +168,12 @@ class Handle:
 
     def launches(self) -> int:
         return int(self.lib.tmvg_launch_count(self.h))
+
+    def fp64_rate(self) -> float:
+        """The device's FP64 FMA rate in TFLOP/s (tmvg_probe_fp64_rate)."""
+        v = dbl()
+        self.check(self.lib.tmvg_probe_fp64_rate(self.h, C.byref(v)), "probe_fp64_rate")
+        return float(v.value)
 
     def call(self, name: str, *args) -> int:
         return getattr(self.lib, name)(self.h, *args)

@@ -424,6 +424,22 @@ int64_t tmvg_launch_count(tmvg_handle h)
     return c ? c->launches : 0;
 }
 
+tmvg_status tmvg_test_set_wait(tmvg_handle h, uint32_t poll_limit, int32_t skip_blocks)
+{
+    CTX_OR_BAIL(h);
+    if (skip_blocks < 0) return set_error(c, TMVG_BAD_ARG, "test_set_wait: negative skip");
+    c->poll_limit = poll_limit;
+    c->test_skip_blocks = skip_blocks;
+    return TMVG_OK;
+}
+
+tmvg_status tmvg_probe_fp64_rate(tmvg_handle h, double* tflops)
+{
+    CTX_OR_BAIL(h);
+    if (!tflops) return set_error(c, TMVG_BAD_ARG, "probe: null output");
+    return probe_fp64_rate(c, tflops);
+}
+
 tmvg_status tmvg_multmm_f64(tmvg_handle h, int add, double alpha, int64_t m, int64_t n, int64_t k,
                             const double* A, int64_t sAi, int64_t sAj, const double* B,
                             int64_t sBi, int64_t sBj, double* C, int64_t sCi, int64_t sCj)

@@ -104,6 +104,12 @@ struct Context {
     // fixes one extreme interleaving of the two streams (used by tests to
     // show that no cross-stream dependency is missing).
     bool serialize_lookahead = false;
+    // Failure-path test hooks (tmvg_test_set_wait): the poll limit of the
+    // sync-free triangular solve's block-flag waits (0: kSpinLimit), and a
+    // number of leading blocks the next such solve never hands out, so their
+    // flags are never published (reset after one launch).
+    unsigned poll_limit = 0;
+    int test_skip_blocks = 0;
 };
 
 // The side stream and its events (nullptr-safe to call repeatedly).
@@ -132,6 +138,8 @@ tmvg_status set_error(Context* c, tmvg_status s, const std::string& msg);
 tmvg_status check_cuda(Context* c, cudaError_t e, const char* what);
 // Ensure at least `bytes` of workspace; returns nullptr on failure.
 void* workspace(Context* c, size_t bytes);
+// FP64 FMA rate of the device in TFLOP/s (probe.cu; synchronises).
+tmvg_status probe_fp64_rate(Context* c, double* tflops);
 void* workspace2(Context* c, size_t bytes);
 void* workspace3(Context* c, size_t bytes);
 void* perm_lists_buffer(Context* c, size_t bytes);

@@ -49,7 +49,7 @@ __global__ void __launch_bounds__(kTrsvThreads)
 trsm_sync_free_kernel(int64_t n, const T* __restrict__ tri, int64_t tsi, int64_t tsj, bool unit,
                       int nr, T* B, int64_t bsi, int64_t bsj, bool skip_zero,
                       unsigned* flags, unsigned epoch, unsigned long long* ticket,
-                      unsigned long long tbase, int* err)
+                      unsigned long long tbase, unsigned spin_limit, int* err)
 {
     __shared__ int s_blk;
     __shared__ T xs[kTrsvBlock][NR];
@@ -94,7 +94,7 @@ trsm_sync_free_kernel(int64_t n, const T* __restrict__ tri, int64_t tsi, int64_t
         if (tid == 0) {
             unsigned spins = 0;
             while (ld_acquire(flags + j) != epoch) {
-                if (++spins > kSpinLimit || *((volatile int*)err) == kDevTimeout) {
+                if (++spins > spin_limit || *((volatile int*)err) == kDevTimeout) {
                     atomicCAS(err, (int)kDevOk, (int)kDevTimeout);
                     s_abort = 1;
                     break;
@@ -190,14 +190,23 @@ tmvg_status trsm_sync_free(Context* c, int64_t n, const T* tri, int64_t tsi, int
             "trsv ticket reset");
         if (st) return st;
         T* Bq = B + q0 * bsj;
+        // tickets map to blocks (ticket - tbase); the failure-path test hook
+        // starts them at block test_skip_blocks, so the blocks before it are
+        // never solved and the first waiting block's bounded wait gives up
+        unsigned long long tbase = 0ull;
+        if (c->test_skip_blocks > 0) {
+            tbase = 0ull - (unsigned long long)c->test_skip_blocks;
+            c->test_skip_blocks = 0;
+        }
+        const unsigned limit = c->poll_limit ? c->poll_limit : kSpinLimit;
         if (nr == 1)
             trsm_sync_free_kernel<T, 1><<<(unsigned)nblk, kTrsvThreads, 0, c->stream>>>(
                 n, tri, tsi, tsj, unit, nr, Bq, bsi, bsj, skip_zero, c->trsv_flags, epoch,
-                c->trsv_ticket, 0ull, c->dflags);
+                c->trsv_ticket, tbase, limit, c->dflags);
         else
             trsm_sync_free_kernel<T, NRM><<<(unsigned)nblk, kTrsvThreads, 0, c->stream>>>(
                 n, tri, tsi, tsj, unit, nr, Bq, bsi, bsj, skip_zero, c->trsv_flags, epoch,
-                c->trsv_ticket, 0ull, c->dflags);
+                c->trsv_ticket, tbase, limit, c->dflags);
         ++c->launches;
         st = check_cuda(c, cudaGetLastError(), "trsv launch");
         if (st) return st;
