@@ -121,10 +121,12 @@ int main(int argc, char** argv)
         save("prod_add", C);
     });
     step("prod_views", [&] {
-        // every other row of A times every other column of B, and a transpose
+        // every other row of A times every other column of B (n2 and p2
+        // of them: TMV's strided subMatrix holds (i2 - i1) / istep rows),
+        // and a transpose
         const ptrdiff_t n2 = (n + 1) / 2, p2 = (p + 1) / 2;
-        tmv::Matrix<double> C = A.subMatrix(0, 2 * n2 - 1, 0, k, 2, 1) *
-                                B.subMatrix(0, k, 0, 2 * p2 - 1, 1, 2);
+        tmv::Matrix<double> C = A.subMatrix(0, 2 * n2, 0, k, 2, 1) *
+                                B.subMatrix(0, k, 0, 2 * p2, 1, 2);
         tmv::Matrix<double> D = B.transpose() * A.transpose();
         save("prod_views", C);
         save("prod_transpose", D);

@@ -87,3 +87,5 @@ def test_surface_program_runs_on_stock_tmv(dropin, tmp_path):
     B = raw[n * k:n * k + k * p].reshape((k, p), order="F")
     C = T.load(tmp_path, "prod_ccc", (n, p))
     assert np.abs(C - A @ B).max() <= 1e-13 * np.abs(A @ B).max()
+    for name, shape in T.result_shapes(n, k, p).items():  # every result has its size
+        assert T.load(tmp_path, name, shape).shape == shape
