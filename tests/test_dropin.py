@@ -89,3 +89,29 @@ def test_surface_program_runs_on_stock_tmv(dropin, tmp_path):
     assert np.abs(C - A @ B).max() <= 1e-13 * np.abs(A @ B).max()
     for name, shape in T.result_shapes(n, k, p).items():  # every result has its size
         assert T.load(tmp_path, name, shape).shape == shape
+
+
+def test_stock_tmv_wide_lu_differs_only_in_its_last_row(dropin, tmp_path):
+    """Stock TMV's LU_Decompose of a wide matrix (M < N) reproduces A except
+    in the last row beyond column M: its two-row recursion leaf updates U(1,
+    2:N) with U(0,1) where L(1,0) belongs (src/TMV_LUDecompose.cpp:349-355).
+    This pins the one place where the drop-in's (correct) result and TMV's
+    differ, which the GPU drop-in test leaves out of its comparison."""
+    import test_gpu_dropin as T
+
+    exe = tmp_path / "tmv_surface_stock"
+    subprocess.run(["g++", "-O2", "-std=gnu++17", "-w", "-DNOBLAS", "-DNOLAP", "-DTMV_NDEBUG",
+                    f"-I{TMV}/include", "-fopenmp", "-o", str(exe), T.SURFACE, f"-L{dropin}",
+                    "-ltmv_stock", f"-Wl,-rpath,{dropin}"], check=True)
+    n, k, p = 40, 17, 3
+    T.write_inputs(tmp_path, np.random.default_rng(12), n, k, p)
+    T.run(exe, tmp_path)
+    raw = np.fromfile(tmp_path / "in.bin", dtype=np.float64)[3:]
+    A = raw[:n * k].reshape((n, k), order="F")
+    M = A.T
+    R = T.plu(T.load(tmp_path, "lu_wide", (k, n)), T.load(tmp_path, "lu_wide_pivots", None).astype(np.int64))
+    bad = np.abs(R - M) > 1e-12 * np.abs(M).max()
+    rows, cols = np.nonzero(bad)
+    assert len(rows) > 0 and set(rows.tolist()) <= {k - 1} and cols.min() >= k
+    Rt = T.plu(T.load(tmp_path, "lu_tall", (n, k)), T.load(tmp_path, "lu_tall_pivots", None).astype(np.int64))
+    assert np.abs(Rt - A).max() <= 1e-13 * np.abs(A).max()
