@@ -101,6 +101,25 @@ __device__ __forceinline__ void st_cluster16(uint32_t dst, const uint4& v)
                  : "memory");
 }
 
+// Orders this thread's earlier generic-proxy shared-memory writes before its
+// (or, after a warp/CTA barrier, its peers') later async-proxy operations.
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// Bulk copy of `bytes` (a multiple of 16, both addresses 16-byte aligned)
+// from this CTA's shared memory to the shared memory of a CTA of the cluster,
+// completing `bytes` transactions on that CTA's mbarrier (dst and mbar from
+// cluster_addr).
+__device__ __forceinline__ void bulk_s2cluster(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+        "r"(smem_u32(src)), "r"(bytes), "r"(mbar)
+        : "memory");
+}
+
 __device__ __forceinline__ uint4 ld_cluster16(uint32_t src)
 {
     uint4 v;

@@ -337,6 +337,8 @@ tmvg_status tmvg_create(tmvg_handle* h, int device)
     }
     const char* ser = std::getenv("TMVG_SERIALIZE_LOOKAHEAD");
     c->serialize_lookahead = ser && ser[0] == '1';
+    const char* reg2 = std::getenv("TMVG_PANEL_REG2");
+    c->panel_reg2 = reg2 && reg2[0] == '1';
     *h = reinterpret_cast<tmvg_handle>(c);
     return TMVG_OK;
 }

@@ -104,6 +104,10 @@ struct Context {
     // fixes one extreme interleaving of the two streams (used by tests to
     // show that no cross-stream dependency is missing).
     bool serialize_lookahead = false;
+    // TMVG_PANEL_REG2=1 at creation: the register panel updates every
+    // column at every step (lu_panel_cluster_reg2_kernel) instead of by
+    // leaves (lu_panel_leaf_kernel); the two give bitwise the same factors.
+    bool panel_reg2 = false;
     // Failure-path test hooks (tmvg_test_set_wait): the poll limit of the
     // sync-free triangular solve's block-flag waits (0: kSpinLimit), and a
     // number of leading blocks the next such solve never hands out, so their

@@ -772,6 +772,438 @@ lu_panel_cluster_reg2_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t 
 }
 
 // ---------------------------------------------------------------------
+// Register panel with leaves: the same cluster, rows and pivot rule as
+// lu_panel_cluster_reg2_kernel (and bitwise the same factors), organised so
+// that a column's chain carries only the work the next pivot decision needs.
+//
+// * The panel's columns are factored in leaves of kLeaf = 8.  At a column
+//   step only the leaf's columns are updated (rank-1 on at most 7 columns);
+//   the leaf's effect on the columns after it is applied once at the end of
+//   the leaf as a rank-8 update A2 -= L1 U12, with U12 = L11^-1 A12 solved
+//   from the leaf's pivot rows.  Each entry still receives TMV's
+//   subtractions in TMV's order (step by step, one fused multiply-add each),
+//   so the factors are bitwise those of the column-by-column update.
+// * Rows never move.  Each thread tracks the current position of its two
+//   rows; an interchange swaps two positions, a pivot row is marked done,
+//   and the rows are written to their final positions at the end.  The tie
+//   rule (lowest position among equal keys) and the NaN rule (the element
+//   at position j) are applied to positions.
+// * The exchange of a column is one message per CTA and destination: the
+//   CTA's candidate key, position and location, and the candidate row's
+//   leaf part, stored into every CTA with st.async, whose arrival completes
+//   the receiver's mbarrier (no cluster-scope release, no second hop).  Every
+//   CTA reduces the 16 messages itself and has the pivot row's leaf part.
+// * The pivot row's other columns (stale by the leaf's earlier steps) are
+//   needed only at the end of the leaf: its owner stages them in shared
+//   memory and bulk-copies them to every CTA, off the column chain.
+// Bounded waits as in lu_panel_cluster_reg2_kernel.
+// ---------------------------------------------------------------------
+constexpr int kLeaf = 8;
+
+template <typename T>
+struct LeafMsg {
+    unsigned long long key;
+    int pos;
+    int loc;  // cta << 16 | 2 * tid + (second row)
+    T leaf[kLeaf];
+};
+
+template <typename T, int NB>
+__device__ __forceinline__ void leaf_stage_row(T* __restrict__ dst, const T (&x)[NB], int pw)
+{
+    using V = Vec16<T>;
+#pragma unroll
+    for (int v = 0; v < NB / V::E; ++v) {
+        if (v * V::E >= pw) break;
+        reinterpret_cast<typename V::type*>(dst)[v] = V::make(&x[v * V::E]);
+    }
+}
+
+// In-leaf rank-1 update of positions u+1..kLeaf-1: x[c] -= l * ur[c].
+template <typename T, int NB>
+__device__ __forceinline__ void leaf_rank1(T (&x)[NB], T l, const T* __restrict__ ur, int u)
+{
+    if constexpr (std::is_same<T, float>::value) {
+#pragma unroll
+        for (int c = 0; c < kLeaf; c += 2) {
+            if (c > u) {
+                const float2 r = __ffma2_rn(make_float2(-l, -l), make_float2(ur[c], ur[c + 1]),
+                                            make_float2(x[c], x[c + 1]));
+                x[c] = r.x;
+                x[c + 1] = r.y;
+            } else if (c + 1 > u) {
+                x[c + 1] = fmaf(-l, ur[c + 1], x[c + 1]);
+            }
+        }
+    } else {
+#pragma unroll
+        for (int c = 0; c < kLeaf; ++c)
+            if (c > u) x[c] = fma(-l, ur[c], x[c]);
+    }
+}
+
+// End-of-leaf update of positions [kLeaf, kLeaf + rcv) of an active row:
+// x[c] -= x[t] * U[t][c] for the leaf's steps t in order (steps whose
+// column underflowed did no update and are skipped).
+template <typename T, int NB>
+__device__ __forceinline__ void leaf_block_update(T (&x)[NB], const T* __restrict__ U, int ldu, int steps,
+                                                  unsigned ufmask, int rcv)
+{
+    using V = Vec16<T>;
+#pragma unroll
+    for (int t = 0; t < kLeaf; ++t) {
+        if (t >= steps) break;
+        if ((ufmask >> t) & 1u) continue;
+        const T l = x[t];
+        const T* ut = U + t * ldu;
+#pragma unroll
+        for (int v = kLeaf / V::E; v < NB / V::E; ++v) {
+            const int c = v * V::E;
+            if (c >= kLeaf + rcv) break;
+            const typename V::type uv = reinterpret_cast<const typename V::type*>(ut)[v];
+            if constexpr (std::is_same<T, float>::value) {
+                const float2 a = __ffma2_rn(make_float2(-l, -l), make_float2(uv.x, uv.y), make_float2(x[c], x[c + 1]));
+                const float2 b = __ffma2_rn(make_float2(-l, -l), make_float2(uv.z, uv.w), make_float2(x[c + 2], x[c + 3]));
+                x[c] = a.x;
+                x[c + 1] = a.y;
+                x[c + 2] = b.x;
+                x[c + 3] = b.y;
+            } else {
+                x[c] = fma(-l, uv.x, x[c]);
+                x[c + 1] = fma(-l, uv.y, x[c + 1]);
+            }
+        }
+    }
+}
+
+// Positions [kLeaf, kLeaf + rcv) of a row that became the leaf's pivot at
+// step t take their final (U) values.
+template <typename T, int NB>
+__device__ __forceinline__ void leaf_take_u(T (&x)[NB], const T* __restrict__ ut, int rcv)
+{
+    using V = Vec16<T>;
+#pragma unroll
+    for (int v = kLeaf / V::E; v < NB / V::E; ++v) {
+        const int c = v * V::E;
+        if (c >= kLeaf + rcv) break;
+        const typename V::type uv = reinterpret_cast<const typename V::type*>(ut)[v];
+#pragma unroll
+        for (int e = 0; e < V::E; ++e) x[c + e] = V::get(uv, e);
+    }
+}
+
+template <typename T, int NB>
+__device__ __forceinline__ void leaf_rotate(T (&x)[NB])
+{
+    T t[kLeaf];
+#pragma unroll
+    for (int c = 0; c < kLeaf; ++c) t[c] = x[c];
+#pragma unroll
+    for (int c = 0; c < NB - kLeaf; ++c) x[c] = x[c + kLeaf];
+#pragma unroll
+    for (int c = 0; c < kLeaf; ++c) x[NB - kLeaf + c] = t[c];
+}
+
+template <typename T, int NB>
+__global__ void __launch_bounds__(kReg2Threads, 1)
+lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int nb,
+                     int64_t* __restrict__ P, const unsigned char* __restrict__ modes,
+                     int rows_per_cta, int* pairs, int* err, float* __restrict__ ahi,
+                     float* __restrict__ alo, const T* __restrict__ Sp, int64_t lds)
+{
+    static_assert(NB % kLeaf == 0, "whole leaves");
+    static_assert(NB * sizeof(T) == 256, "a row is 16 vectors of 16 bytes");
+    using V = Vec16<T>;
+    constexpr int kRem = NB - kLeaf;                          // widest remainder of a leaf
+    constexpr int kMsgVecs = (int)(sizeof(LeafMsg<T>) / 16);  // 16-byte pieces of a message
+    static_assert(sizeof(LeafMsg<T>) % 16 == 0, "message in 16-byte pieces");
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+
+    __shared__ unsigned long long s_key[kReg2Warps];
+    __shared__ int s_idx[kReg2Warps];
+    __shared__ int s_loc[kReg2Warps];
+    __shared__ __align__(16) T warp_leaf[kReg2Warps][kLeaf];      // each warp's candidate's leaf part
+    __shared__ __align__(16) LeafMsg<T> msg[2][kClusterCtas];    // messages, by column parity
+    __shared__ __align__(16) T urow[kLeaf];                       // the pivot row's leaf part
+    __shared__ __align__(16) T s_rem[kLeaf][NB];                  // pivot rows' unfinished parts, then U
+    __shared__ __align__(16) T s_stage[kLeaf][NB];                // this CTA's pivot rows, staged
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ __align__(8) uint64_t mbar_leaf;
+    __shared__ unsigned long long s_wk;
+    __shared__ int s_wi, s_wloc;
+    __shared__ unsigned char s_mode[kPanelMax];
+    __shared__ int s_piv[kPanelMax];
+    __shared__ int s_abort;
+
+    const int G = (int)cluster.num_blocks();
+    const int cta = (int)cluster.block_rank();
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int m = (int)(n - k);
+    const int r0 = cta * rows_per_cta;
+    const int nr = max(0, min(rows_per_cta, m - r0));
+    const bool ha = tid < nr, hb = tid + kReg2Threads < nr;
+    T* Ap = A + k + k * lda;
+
+    if (tid == 0) {
+        mbar_init(&mbar[0], 1u);
+        mbar_init(&mbar[1], 1u);
+        mbar_init(&mbar_leaf, 1u);
+        s_abort = 0;
+        mbar_fence_init();
+    }
+    for (int j = tid; j < nb; j += kReg2Threads) s_mode[j] = modes[j];
+    const T* Xp = Sp ? Sp : Ap;
+    const int64_t ldx = Sp ? lds : lda;
+    T x[NB], y[NB];
+#pragma unroll
+    for (int c = 0; c < NB; ++c) {
+        x[c] = (ha && c < nb) ? Xp[r0 + tid + c * ldx] : T(0);
+        y[c] = (hb && c < nb) ? Xp[r0 + tid + kReg2Threads + c * ldx] : T(0);
+    }
+    // current positions of this thread's rows, whether they still take part,
+    // and the leaf step at which they became a pivot row (-1: not this leaf)
+    int pos_a = r0 + tid, pos_b = r0 + tid + kReg2Threads;
+    bool act_a = ha, act_b = hb;
+    const int loc_a = (cta << 16) | (2 * tid), loc_b = loc_a + 1;
+    cluster.sync();  // every CTA's mbarriers are initialised before any message
+
+    bool prev_uf = false;
+    unsigned leaf_uses = 0;
+    for (int jb = 0; jb < nb; jb += kLeaf) {
+        const int steps = min(kLeaf, nb - jb);
+        const int lim = NB - jb;                          // unfinished positions
+        const int rc = max(0, nb - jb - kLeaf);           // remainder columns still to factor
+        const int rcv = (rc + V::E - 1) / V::E * V::E;    // in whole vectors (<= lim - kLeaf)
+        const int pw = kLeaf + rcv;                       // positions a pivot row sends
+        const bool block = rc > 0;
+        if (block && G > 1 && tid == 0)
+            mbar_expect_tx(&mbar_leaf, (uint32_t)(steps * pw * (int)sizeof(T)));
+        int dstep_a = -1, dstep_b = -1;
+        unsigned ufmask = 0;
+#pragma unroll
+        for (int u = 0; u < kLeaf; ++u) {
+            if (u >= steps) break;
+            const int j = jb + u;
+            const int par = j & 1;
+            const bool r2 = s_mode[j] && !prev_uf;
+            // 1. this warp's candidate: the larger key, the lower position on a tie
+            unsigned long long bk = 0;
+            int bi = INT_MAX;
+            if (act_a) {
+                bk = reg_pivot_key(x[u], pos_a == j, r2);
+                bi = pos_a;
+            }
+            if (act_b) {
+                const unsigned long long kb = reg_pivot_key(y[u], pos_b == j, r2);
+                if (bi == INT_MAX || kb > bk || (kb == bk && pos_b < bi)) {
+                    bk = kb;
+                    bi = pos_b;
+                }
+            }
+            reg_key_reduce<T>(bk, bi);
+            if (bi != INT_MAX) {
+                if (act_a && pos_a == bi) {
+                    leaf_stage_row<T, NB>(warp_leaf[warp], x, kLeaf);
+                    s_loc[warp] = loc_a;
+                } else if (act_b && pos_b == bi) {
+                    leaf_stage_row<T, NB>(warp_leaf[warp], y, kLeaf);
+                    s_loc[warp] = loc_b;
+                }
+            }
+            if (lane == 0) {
+                s_key[warp] = bk;
+                s_idx[warp] = bi;
+            }
+            __syncthreads();
+            if (warp == 0) {
+                // 2. this CTA's candidate
+                bk = lane < kReg2Warps ? s_key[lane] : 0ull;
+                bi = lane < kReg2Warps ? s_idx[lane] : INT_MAX;
+                reg_key_reduce<T>(bk, bi);
+                const unsigned wm = __ballot_sync(0xffffffffu, lane < kReg2Warps && bi != INT_MAX && s_idx[lane] == bi);
+                const int ww = wm ? __ffs(wm) - 1 : -1;
+                if (G == 1) {
+                    if (lane == 0) {
+                        s_wk = bk;
+                        s_wi = bi;
+                        s_wloc = ww >= 0 ? s_loc[ww] : -1;
+                    }
+                    if (ww >= 0 && lane < kLeaf / V::E)
+                        reinterpret_cast<typename V::type*>(urow)[lane] =
+                            reinterpret_cast<const typename V::type*>(warp_leaf[ww])[lane];
+                } else {
+                    // 3. one message into every CTA; its arrival completes
+                    //    that CTA's mbarrier for this column
+                    if (lane == 0) mbar_expect_tx(&mbar[par], (uint32_t)(G * sizeof(LeafMsg<T>)));
+                    if (lane < G) {
+                        const uint32_t dst = cluster_addr(&msg[par][cta], lane);
+                        const uint32_t bar = cluster_addr(&mbar[par], lane);
+                        const int loc = ww >= 0 ? s_loc[ww] : -1;
+                        st_async16(dst, make_uint4((unsigned)bk, (unsigned)(bk >> 32), (unsigned)bi, (unsigned)loc), bar);
+#pragma unroll
+                        for (int q = 1; q < kMsgVecs; ++q) {
+                            const uint4 v = ww >= 0 ? reinterpret_cast<const uint4*>(warp_leaf[ww])[q - 1]
+                                                    : make_uint4(0u, 0u, 0u, 0u);
+                            st_async16(dst + 16 * q, v, bar);
+                        }
+                    }
+                    const bool got = __all_sync(0xffffffffu, mbar_wait(&mbar[par], (uint32_t)((j >> 1) & 1)));
+                    if (!got) {
+                        if (lane == 0) {
+                            s_abort = 1;
+                            atomicCAS(err, (int)kDevOk, (int)kDevTimeout);
+                        }
+                    } else {
+                        unsigned long long wk = lane < G ? msg[par][lane].key : 0ull;
+                        int wi = lane < G ? msg[par][lane].pos : INT_MAX;
+                        reg_key_reduce<T>(wk, wi);
+                        const unsigned om = __ballot_sync(0xffffffffu, lane < G && wi != INT_MAX && msg[par][lane].pos == wi);
+                        const int wo = om ? __ffs(om) - 1 : -1;
+                        if (lane == 0) {
+                            s_wk = wk;
+                            s_wi = wi;
+                            s_wloc = wo >= 0 ? msg[par][wo].loc : -1;
+                        }
+                        if (wo >= 0 && lane < kLeaf / V::E)
+                            reinterpret_cast<typename V::type*>(urow)[lane] =
+                                reinterpret_cast<const typename V::type*>(msg[par][wo].leaf)[lane];
+                    }
+                }
+            }
+            __syncthreads();
+            if (s_abort) break;
+            const unsigned long long wk = s_wk;
+            const int wi = s_wi;
+            const bool uf = reg_key_underflows<T>(wk);
+            // the row that becomes position j's final row: the pivot, or on
+            // underflow the row already at position j (no interchange)
+            bool own_a, own_b;
+            if (uf) {
+                own_a = act_a && pos_a == j;
+                own_b = act_b && pos_b == j;
+                if (act_a) x[u] = T(0);
+                if (act_b) y[u] = T(0);
+                if (tid == 0) s_piv[j] = (int)(k + j);
+                ufmask |= 1u << u;
+                prev_uf = true;
+            } else {
+                const int wloc = s_wloc;
+                own_a = act_a && loc_a == wloc;
+                own_b = act_b && loc_b == wloc;
+                if (tid == 0) s_piv[j] = (int)(k + wi);
+                prev_uf = false;
+                // the interchange: the row at position j moves to position wi
+                if (act_a && !own_a && pos_a == j) pos_a = wi;
+                if (act_b && !own_b && pos_b == j) pos_b = wi;
+            }
+            if (own_a) {
+                act_a = false;
+                pos_a = j;
+                dstep_a = u;
+            }
+            if (own_b) {
+                act_b = false;
+                pos_b = j;
+                dstep_b = u;
+            }
+            // the pivot row's unfinished part goes to every CTA for the leaf's end
+            if (block && (own_a || own_b)) {
+                // one CTA: straight into the receive buffer
+                T* st = G == 1 ? s_rem[u] : s_stage[u];
+                if (own_a) leaf_stage_row<T, NB>(st, x, pw);
+                else leaf_stage_row<T, NB>(st, y, pw);
+                if (G > 1) {
+                    fence_proxy_async_smem();
+                    for (int d = 0; d < G; ++d)
+                        bulk_s2cluster(cluster_addr(&s_rem[u][0], d), st, (uint32_t)(pw * sizeof(T)),
+                                       cluster_addr(&mbar_leaf, d));
+                }
+            }
+            if (!uf) {
+                // TMV scales the column by the reciprocal of the pivot
+                const T rp = recip_rn(urow[u]);
+                if (act_a) {
+                    const T l = x[u] * rp;
+                    x[u] = l;
+                    leaf_rank1<T, NB>(x, l, urow, u);
+                }
+                if (act_b) {
+                    const T l = y[u] * rp;
+                    y[u] = l;
+                    leaf_rank1<T, NB>(y, l, urow, u);
+                }
+            }
+        }
+        if (s_abort) break;
+        if (block) {
+            // 4. the leaf's pivot rows: U12 = L11^-1 A12 (every CTA the same),
+            //    then the rank-8 update of the columns after the leaf
+            if (G > 1) {
+                if (!mbar_wait(&mbar_leaf, leaf_uses & 1u)) {
+                    if (tid == 0) atomicCAS(err, (int)kDevOk, (int)kDevTimeout);
+                    s_abort = 1;  // every thread of the CTA reaches this
+                }
+                ++leaf_uses;
+            }
+            __syncthreads();
+            if (s_abort) break;
+            for (int c = kLeaf + tid; c < kLeaf + rcv; c += kReg2Threads) {
+                for (int t = 1; t < steps; ++t) {
+                    T a = s_rem[t][c];
+                    for (int s = 0; s < t; ++s)
+                        if (!((ufmask >> s) & 1u)) a = fma(-s_rem[t][s], s_rem[s][c], a);
+                    s_rem[t][c] = a;
+                }
+            }
+            __syncthreads();
+            if (act_a) leaf_block_update<T, NB>(x, &s_rem[0][0], NB, steps, ufmask, rcv);
+            else if (dstep_a >= 0) leaf_take_u<T, NB>(x, s_rem[dstep_a], rcv);
+            if (act_b) leaf_block_update<T, NB>(y, &s_rem[0][0], NB, steps, ufmask, rcv);
+            else if (dstep_b >= 0) leaf_take_u<T, NB>(y, s_rem[dstep_b], rcv);
+        }
+        if (jb + kLeaf < nb) {
+            leaf_rotate<T, NB>(x);
+            leaf_rotate<T, NB>(y);
+        }
+    }
+
+    if (!s_abort) {
+        // rows to their final positions; with ahi (FP32 factorisation) the
+        // rows below the panel block also as the TF32 hi/lo split of L21
+        // (row-major, nb wide) that the step's tensor-core update reads
+        const int rot = ((nb - 1) / kLeaf) * kLeaf;  // x[p] holds column (p + rot) mod NB
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const bool have = h == 0 ? ha : hb;
+            const int pr = h == 0 ? pos_a : pos_b;
+            if (!have) continue;
+            const bool split = std::is_same<T, float>::value && ahi != nullptr && pr >= nb;
+#pragma unroll
+            for (int p = 0; p < NB; ++p) {
+                const int col = (p + rot) % NB;
+                if (col < nb) {
+                    const T v = h == 0 ? x[p] : y[p];
+                    Ap[pr + col * lda] = v;
+                    if (split) {
+                        const float f = (float)v;
+                        const float hi = tf32_round(f);
+                        ahi[(int64_t)(pr - nb) * nb + col] = hi;
+                        alo[(int64_t)(pr - nb) * nb + col] = tf32_round(f - hi);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        if (cta == 0) {
+            for (int j = tid; j < nb; j += kReg2Threads) P[k + j] = s_piv[j];
+            if (warp == 0) panel_row_pairs(k, nb, s_piv, pairs);
+        }
+    }
+    cluster.sync();  // no CTA leaves while another may still store into it
+}
+
+// ---------------------------------------------------------------------
 // Row interchanges.
 // ---------------------------------------------------------------------
 // Interchanges P[k..k+nb) applied to columns [0, ncols) except [skip0, skip1).
@@ -1672,11 +2104,16 @@ static tmvg_status launch_panel_cluster_reg(Context* c, cudaStream_t s, T* A, in
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     ++c->launches;
+    if (c->panel_reg2)
+        return check_cuda(c,
+                          cudaLaunchKernelEx(&cfg, lu_panel_cluster_reg2_kernel<T, RegPanel<T>::NB>, A,
+                                             lda, n, k, nb, P, modes, rpc, pairs, c->dflags, ahi, alo, Sp,
+                                             lds),
+                          "lu: register panel launch");
     return check_cuda(c,
-                      cudaLaunchKernelEx(&cfg, lu_panel_cluster_reg2_kernel<T, RegPanel<T>::NB>, A,
-                                         lda, n, k, nb, P, modes, rpc, pairs, c->dflags, ahi, alo, Sp,
-                                         lds),
-                      "lu: register panel launch");
+                      cudaLaunchKernelEx(&cfg, lu_panel_leaf_kernel<T, RegPanel<T>::NB>, A, lda, n, k,
+                                         nb, P, modes, rpc, pairs, c->dflags, ahi, alo, Sp, lds),
+                      "lu: leaf register panel launch");
 }
 
 template <typename T>
