@@ -2055,7 +2055,10 @@ static bool reg_panel_ok(Context* c)
     int& ok = c->reg_cluster_ok[sizeof(T) == 8 ? 0 : 1];
     if (ok >= 0) return ok == 1;
     ok = 0;
-    auto kern = lu_panel_cluster_reg2_kernel<T, RegPanel<T>::NB>;
+    // both register panels (the launcher picks one per handle) need the
+    // 16-CTA cluster
+    auto kern = c->panel_reg2 ? lu_panel_cluster_reg2_kernel<T, RegPanel<T>::NB>
+                              : lu_panel_leaf_kernel<T, RegPanel<T>::NB>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
         cudaGetLastError();
         return false;
