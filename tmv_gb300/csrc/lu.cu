@@ -1016,6 +1016,9 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
                 s_idx[warp] = bi;
             }
             __syncthreads();
+            if (block && G > 1 && u > 0 && warp == kReg2Warps - 1 && lane < G)
+                bulk_s2cluster(cluster_addr(&s_rem[u - 1][0], lane), s_stage[u - 1],
+                               (uint32_t)(pw * sizeof(T)), cluster_addr(&mbar_leaf, lane));
             if (warp == 0) {
                 // 2. this CTA's candidate
                 bk = lane < kReg2Warps ? s_key[lane] : 0ull;
@@ -1108,17 +1111,14 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
                 dstep_b = u;
             }
             // the pivot row's unfinished part goes to every CTA for the leaf's end
+            // (staged here; the last warp bulk-copies it while warp 0 runs
+            // the next column's exchange, or at the leaf's end)
             if (block && (own_a || own_b)) {
                 // one CTA: straight into the receive buffer
                 T* st = G == 1 ? s_rem[u] : s_stage[u];
                 if (own_a) leaf_stage_row<T, NB>(st, x, pw);
                 else leaf_stage_row<T, NB>(st, y, pw);
-                if (G > 1) {
-                    fence_proxy_async_smem();
-                    for (int d = 0; d < G; ++d)
-                        bulk_s2cluster(cluster_addr(&s_rem[u][0], d), st, (uint32_t)(pw * sizeof(T)),
-                                       cluster_addr(&mbar_leaf, d));
-                }
+                if (G > 1) fence_proxy_async_smem();
             }
             if (!uf) {
                 // TMV scales the column by the reciprocal of the pivot
@@ -1140,6 +1140,10 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
             // 4. the leaf's pivot rows: U12 = L11^-1 A12 (every CTA the same),
             //    then the rank-8 update of the columns after the leaf
             if (G > 1) {
+                __syncthreads();  // the last step's pivot row is staged
+                if (warp == kReg2Warps - 1 && lane < G)
+                    bulk_s2cluster(cluster_addr(&s_rem[steps - 1][0], lane), s_stage[steps - 1],
+                                   (uint32_t)(pw * sizeof(T)), cluster_addr(&mbar_leaf, lane));
                 if (!mbar_wait(&mbar_leaf, leaf_uses & 1u)) {
                     if (tid == 0) atomicCAS(err, (int)kDevOk, (int)kDevTimeout);
                     s_abort = 1;  // every thread of the CTA reaches this
@@ -1148,13 +1152,21 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
             }
             __syncthreads();
             if (s_abort) break;
+            // forward substitution per column, in registers, steps in order
             for (int c = kLeaf + tid; c < kLeaf + rcv; c += kReg2Threads) {
-                for (int t = 1; t < steps; ++t) {
-                    T a = s_rem[t][c];
-                    for (int s = 0; s < t; ++s)
-                        if (!((ufmask >> s) & 1u)) a = fma(-s_rem[t][s], s_rem[s][c], a);
-                    s_rem[t][c] = a;
+                T uc[kLeaf];
+#pragma unroll
+                for (int t = 0; t < kLeaf; ++t) uc[t] = t < steps ? s_rem[t][c] : T(0);
+#pragma unroll
+                for (int t = 1; t < kLeaf; ++t) {
+                    if (t >= steps) break;
+#pragma unroll
+                    for (int q = 0; q < t; ++q)
+                        if (!((ufmask >> q) & 1u)) uc[t] = fma(-s_rem[t][q], uc[q], uc[t]);
                 }
+#pragma unroll
+                for (int t = 0; t < kLeaf; ++t)
+                    if (t < steps) s_rem[t][c] = uc[t];
             }
             __syncthreads();
             if (act_a) leaf_block_update<T, NB>(x, &s_rem[0][0], NB, steps, ufmask, rcv);
