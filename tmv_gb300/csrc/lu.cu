@@ -934,6 +934,7 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
     __shared__ int s_wi, s_wloc;
     __shared__ unsigned char s_mode[kPanelMax];
     __shared__ int s_piv[kPanelMax];
+    __shared__ unsigned char s_staged[kLeaf];  // this CTA holds the leaf step's pivot row
     __shared__ int s_abort;
 
     const int G = (int)cluster.num_blocks();
@@ -945,6 +946,7 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
     const bool ha = tid < nr, hb = tid + kReg2Threads < nr;
     T* Ap = A + k + k * lda;
 
+    if (tid < kLeaf) s_staged[tid] = 0;
     if (tid == 0) {
         mbar_init(&mbar[0], 1u);
         mbar_init(&mbar[1], 1u);
@@ -1016,7 +1018,7 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
                 s_idx[warp] = bi;
             }
             __syncthreads();
-            if (block && G > 1 && u > 0 && warp == kReg2Warps - 1 && lane < G)
+            if (block && G > 1 && u > 0 && warp == kReg2Warps - 1 && lane < G && s_staged[u - 1])
                 bulk_s2cluster(cluster_addr(&s_rem[u - 1][0], lane), s_stage[u - 1],
                                (uint32_t)(pw * sizeof(T)), cluster_addr(&mbar_leaf, lane));
             if (warp == 0) {
@@ -1118,7 +1120,10 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
                 T* st = G == 1 ? s_rem[u] : s_stage[u];
                 if (own_a) leaf_stage_row<T, NB>(st, x, pw);
                 else leaf_stage_row<T, NB>(st, y, pw);
-                if (G > 1) fence_proxy_async_smem();
+                if (G > 1) {
+                    fence_proxy_async_smem();
+                    s_staged[u] = 1;
+                }
             }
             if (!uf) {
                 // TMV scales the column by the reciprocal of the pivot
@@ -1141,7 +1146,7 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
             //    then the rank-8 update of the columns after the leaf
             if (G > 1) {
                 __syncthreads();  // the last step's pivot row is staged
-                if (warp == kReg2Warps - 1 && lane < G)
+                if (warp == kReg2Warps - 1 && lane < G && s_staged[steps - 1])
                     bulk_s2cluster(cluster_addr(&s_rem[steps - 1][0], lane), s_stage[steps - 1],
                                    (uint32_t)(pw * sizeof(T)), cluster_addr(&mbar_leaf, lane));
                 if (!mbar_wait(&mbar_leaf, leaf_uses & 1u)) {
@@ -1152,6 +1157,7 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
             }
             __syncthreads();
             if (s_abort) break;
+            if (tid < kLeaf) s_staged[tid] = 0;  // read again only after the next leaf's barriers
             // forward substitution per column, in registers, steps in order
             for (int c = kLeaf + tid; c < kLeaf + rcv; c += kReg2Threads) {
                 T uc[kLeaf];
