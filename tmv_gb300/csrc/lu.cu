@@ -772,39 +772,43 @@ lu_panel_cluster_reg2_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t 
 }
 
 // ---------------------------------------------------------------------
-// Register panel with leaves: the same cluster, rows and pivot rule as
-// lu_panel_cluster_reg2_kernel (and bitwise the same factors), organised so
-// that a column's chain carries only the work the next pivot decision needs.
+// Register panel with leaves: the same cluster, row partition and pivot rule
+// as lu_panel_cluster_reg2_kernel, and bitwise the same factors, organised
+// so that a column's critical chain carries only what the next pivot
+// decision needs; everything else runs in the shadow of the cluster
+// exchange, while warp 0 waits for the other CTAs.
 //
-// * The panel's columns are factored in leaves of kLeaf = 8.  At a column
-//   step only the leaf's columns are updated (rank-1 on at most 7 columns);
-//   the leaf's effect on the columns after it is applied once at the end of
-//   the leaf as a rank-8 update A2 -= L1 U12, with U12 = L11^-1 A12 solved
-//   from the leaf's pivot rows.  Each entry still receives TMV's
-//   subtractions in TMV's order (step by step, one fused multiply-add each),
-//   so the factors are bitwise those of the column-by-column update.
-// * Rows never move.  Each thread tracks the current position of its two
-//   rows; an interchange swaps two positions, a pivot row is marked done,
-//   and the rows are written to their final positions at the end.  The tie
-//   rule (lowest position among equal keys) and the NaN rule (the element
-//   at position j) are applied to positions.
-// * The exchange of a column is one message per CTA and destination: the
-//   CTA's candidate key, position and location, and the candidate row's
-//   leaf part, stored into every CTA with st.async, whose arrival completes
-//   the receiver's mbarrier (no cluster-scope release, no second hop).  Every
-//   CTA reduces the 16 messages itself and has the pivot row's leaf part.
-// * The pivot row's other columns (stale by the leaf's earlier steps) are
-//   needed only at the end of the leaf: its owner stages them in shared
-//   memory and bulk-copies them to every CTA, off the column chain.
+// * One panel row per thread, 512 threads per CTA (16 CTAs: m <= 8192).
+// * Columns are factored in leaves of kLeaf = 8.  After a pivot decision a
+//   thread scales its row's column j and updates column j+1 (the next key);
+//   the rest of the step's rank-1 update on the leaf is owed and paid in the
+//   next column's shadow.  A leaf's effect on the later columns is a rank-8
+//   update A2 -= L1 U12 with U12 = L11^-1 A12 solved from the leaf's pivot
+//   rows: on the next leaf's eight columns at the end of the leaf, on the
+//   rest in the first shadow of the next leaf.  Every entry still receives
+//   TMV's subtractions in TMV's order, one fused multiply-add each.
+// * Rows never move: each thread tracks its row's current position; an
+//   interchange swaps two positions, a pivot row is marked done, and rows
+//   are written to their final positions at the end.  Ties go to the lowest
+//   position, the NaN rule looks at the element at position j.
+// * The exchange of a column is one message per CTA and destination (key,
+//   position, location and the candidate row's leaf part) stored with
+//   st.async, whose arrival completes the receiver's mbarrier; every CTA
+//   reduces the 16 messages itself.
+// * A pivot row's other columns are needed only at the end of its leaf: its
+//   owner stages them in shared memory and bulk-copies them to every CTA in
+//   the next column's shadow.
 // Bounded waits as in lu_panel_cluster_reg2_kernel.
 // ---------------------------------------------------------------------
 constexpr int kLeaf = 8;
+constexpr int kLeafThreads = 512;
+constexpr int kLeafWarps = kLeafThreads / 32;
 
 template <typename T>
 struct LeafMsg {
     unsigned long long key;
     int pos;
-    int loc;  // cta << 16 | 2 * tid + (second row)
+    int loc;  // cta << 16 | thread
     T leaf[kLeaf];
 };
 
@@ -819,76 +823,60 @@ __device__ __forceinline__ void leaf_stage_row(T* __restrict__ dst, const T (&x)
     }
 }
 
-// In-leaf rank-1 update of positions u+1..kLeaf-1: x[c] -= l * ur[c].
+// x[c] -= l * ur[c] for the leaf positions c >= c0 (c0 is a constant once
+// the caller's step loop is unrolled).
 template <typename T, int NB>
-__device__ __forceinline__ void leaf_rank1(T (&x)[NB], T l, const T* __restrict__ ur, int u)
+__device__ __forceinline__ void leaf_axpy(T (&x)[NB], T l, const T* __restrict__ ur, int c0)
 {
-    if constexpr (std::is_same<T, float>::value) {
 #pragma unroll
-        for (int c = 0; c < kLeaf; c += 2) {
-            if (c > u) {
-                const float2 r = __ffma2_rn(make_float2(-l, -l), make_float2(ur[c], ur[c + 1]),
-                                            make_float2(x[c], x[c + 1]));
-                x[c] = r.x;
-                x[c + 1] = r.y;
-            } else if (c + 1 > u) {
-                x[c + 1] = fmaf(-l, ur[c + 1], x[c + 1]);
-            }
-        }
-    } else {
-#pragma unroll
-        for (int c = 0; c < kLeaf; ++c)
-            if (c > u) x[c] = fma(-l, ur[c], x[c]);
-    }
+    for (int c = 0; c < kLeaf; ++c)
+        if (c >= c0) x[c] = fma(-l, ur[c], x[c]);
 }
 
-// End-of-leaf update of positions [kLeaf, kLeaf + rcv) of an active row:
-// x[c] -= x[t] * U[t][c] for the leaf's steps t in order (steps whose
-// column underflowed did no update and are skipped).
-template <typename T, int NB>
-__device__ __forceinline__ void leaf_block_update(T (&x)[NB], const T* __restrict__ U, int ldu, int steps,
-                                                  unsigned ufmask, int rcv)
+// Rank-8 update of positions [kLeaf, pend) of a row: x[p] -= x[LP + t] *
+// U[t][p + SHIFT] for the leaf's steps t in order (steps whose column
+// underflowed did no update and are skipped).
+template <typename T, int NB, int LP, int SHIFT, int PMAX>
+__device__ __forceinline__ void leaf_rank8(T (&x)[NB], const T* __restrict__ U, unsigned ufmask, int pend)
 {
     using V = Vec16<T>;
 #pragma unroll
-    for (int t = 0; t < kLeaf; ++t) {
-        if (t >= steps) break;
-        if ((ufmask >> t) & 1u) continue;
-        const T l = x[t];
-        const T* ut = U + t * ldu;
+    for (int v = kLeaf / V::E; v < PMAX / V::E; ++v) {
+        const int p = v * V::E;
+        if (p >= pend) break;
 #pragma unroll
-        for (int v = kLeaf / V::E; v < NB / V::E; ++v) {
-            const int c = v * V::E;
-            if (c >= kLeaf + rcv) break;
-            const typename V::type uv = reinterpret_cast<const typename V::type*>(ut)[v];
+        for (int t = 0; t < kLeaf; ++t) {
+            if ((ufmask >> t) & 1u) continue;
+            const T l = x[LP + t];
+            const typename V::type uv = *reinterpret_cast<const typename V::type*>(U + t * NB + p + SHIFT);
             if constexpr (std::is_same<T, float>::value) {
-                const float2 a = __ffma2_rn(make_float2(-l, -l), make_float2(uv.x, uv.y), make_float2(x[c], x[c + 1]));
-                const float2 b = __ffma2_rn(make_float2(-l, -l), make_float2(uv.z, uv.w), make_float2(x[c + 2], x[c + 3]));
-                x[c] = a.x;
-                x[c + 1] = a.y;
-                x[c + 2] = b.x;
-                x[c + 3] = b.y;
+                const float2 a = __ffma2_rn(make_float2(-l, -l), make_float2(uv.x, uv.y), make_float2(x[p], x[p + 1]));
+                const float2 b = __ffma2_rn(make_float2(-l, -l), make_float2(uv.z, uv.w), make_float2(x[p + 2], x[p + 3]));
+                x[p] = a.x;
+                x[p + 1] = a.y;
+                x[p + 2] = b.x;
+                x[p + 3] = b.y;
             } else {
-                x[c] = fma(-l, uv.x, x[c]);
-                x[c + 1] = fma(-l, uv.y, x[c + 1]);
+                x[p] = fma(-l, uv.x, x[p]);
+                x[p + 1] = fma(-l, uv.y, x[p + 1]);
             }
         }
     }
 }
 
-// Positions [kLeaf, kLeaf + rcv) of a row that became the leaf's pivot at
-// step t take their final (U) values.
+// Positions [kLeaf, pend) of a row that became a pivot row in the leaf take
+// their final (U) values.
 template <typename T, int NB>
-__device__ __forceinline__ void leaf_take_u(T (&x)[NB], const T* __restrict__ ut, int rcv)
+__device__ __forceinline__ void leaf_take_u(T (&x)[NB], const T* __restrict__ ut, int pend)
 {
     using V = Vec16<T>;
 #pragma unroll
     for (int v = kLeaf / V::E; v < NB / V::E; ++v) {
-        const int c = v * V::E;
-        if (c >= kLeaf + rcv) break;
+        const int p = v * V::E;
+        if (p >= pend) break;
         const typename V::type uv = reinterpret_cast<const typename V::type*>(ut)[v];
 #pragma unroll
-        for (int e = 0; e < V::E; ++e) x[c + e] = V::get(uv, e);
+        for (int e = 0; e < V::E; ++e) x[p + e] = V::get(uv, e);
     }
 }
 
@@ -904,37 +892,52 @@ __device__ __forceinline__ void leaf_rotate(T (&x)[NB])
     for (int c = 0; c < kLeaf; ++c) x[NB - kLeaf + c] = t[c];
 }
 
+// A pivot row's positions [0, pw) into every CTA's receive buffer `dst_row`
+// (one CTA: written there directly).
 template <typename T, int NB>
-__global__ void __launch_bounds__(kReg2Threads, 1)
+__device__ __forceinline__ void leaf_send_row(const T (&x)[NB], int pw, int G, T* stage, T* dst_row,
+                                              uint64_t* bar)
+{
+    if (G == 1) {
+        leaf_stage_row<T, NB>(dst_row, x, pw);
+        return;
+    }
+    leaf_stage_row<T, NB>(stage, x, pw);
+    fence_proxy_async_smem();
+    for (int d = 0; d < G; ++d)
+        bulk_s2cluster(cluster_addr(dst_row, d), stage, (uint32_t)(pw * sizeof(T)), cluster_addr(bar, d));
+}
+
+template <typename T, int NB>
+__global__ void __launch_bounds__(kLeafThreads, 1)
 lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int nb,
                      int64_t* __restrict__ P, const unsigned char* __restrict__ modes,
                      int rows_per_cta, int* pairs, int* err, float* __restrict__ ahi,
                      float* __restrict__ alo, const T* __restrict__ Sp, int64_t lds)
 {
-    static_assert(NB % kLeaf == 0, "whole leaves");
+    static_assert(NB % kLeaf == 0 && NB >= 2 * kLeaf, "whole leaves");
     static_assert(NB * sizeof(T) == 256, "a row is 16 vectors of 16 bytes");
     using V = Vec16<T>;
-    constexpr int kRem = NB - kLeaf;                          // widest remainder of a leaf
-    constexpr int kMsgVecs = (int)(sizeof(LeafMsg<T>) / 16);  // 16-byte pieces of a message
+    constexpr int kMsgVecs = (int)(sizeof(LeafMsg<T>) / 16);
     static_assert(sizeof(LeafMsg<T>) % 16 == 0, "message in 16-byte pieces");
+    constexpr int kLast = kLeaf - 1;
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
 
-    __shared__ unsigned long long s_key[kReg2Warps];
-    __shared__ int s_idx[kReg2Warps];
-    __shared__ int s_loc[kReg2Warps];
-    __shared__ __align__(16) T warp_leaf[kReg2Warps][kLeaf];      // each warp's candidate's leaf part
-    __shared__ __align__(16) LeafMsg<T> msg[2][kClusterCtas];    // messages, by column parity
-    __shared__ __align__(16) T urow[kLeaf];                       // the pivot row's leaf part
-    __shared__ __align__(16) T s_rem[kLeaf][NB];                  // pivot rows' unfinished parts, then U
-    __shared__ __align__(16) T s_stage[kLeaf][NB];                // this CTA's pivot rows, staged
+    __shared__ unsigned long long s_key[kLeafWarps];
+    __shared__ int s_idx[kLeafWarps];
+    __shared__ int s_loc[kLeafWarps];
+    __shared__ __align__(16) T warp_leaf[kLeafWarps][kLeaf];     // each warp's candidate's leaf part
+    __shared__ __align__(16) LeafMsg<T> msg[2][kClusterCtas];   // messages, by column parity
+    __shared__ __align__(16) T s_urow[kLeaf][kLeaf];             // the leaf's pivot rows, leaf part
+    __shared__ __align__(16) T s_rem[2][kLeaf][NB];              // pivot rows, then U (by leaf parity)
+    __shared__ __align__(16) T s_stage[kLeaf][NB];               // this CTA's pivot rows, staged
     __shared__ __align__(8) uint64_t mbar[2];
     __shared__ __align__(8) uint64_t mbar_leaf;
     __shared__ unsigned long long s_wk;
     __shared__ int s_wi, s_wloc;
     __shared__ unsigned char s_mode[kPanelMax];
     __shared__ int s_piv[kPanelMax];
-    __shared__ unsigned char s_staged[kLeaf];  // this CTA holds the leaf step's pivot row
     __shared__ int s_abort;
 
     const int G = (int)cluster.num_blocks();
@@ -943,10 +946,9 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
     const int m = (int)(n - k);
     const int r0 = cta * rows_per_cta;
     const int nr = max(0, min(rows_per_cta, m - r0));
-    const bool ha = tid < nr, hb = tid + kReg2Threads < nr;
+    const bool have = tid < nr;
     T* Ap = A + k + k * lda;
 
-    if (tid < kLeaf) s_staged[tid] = 0;
     if (tid == 0) {
         mbar_init(&mbar[0], 1u);
         mbar_init(&mbar[1], 1u);
@@ -954,79 +956,66 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
         s_abort = 0;
         mbar_fence_init();
     }
-    for (int j = tid; j < nb; j += kReg2Threads) s_mode[j] = modes[j];
+    for (int j = tid; j < nb; j += kLeafThreads) s_mode[j] = modes[j];
     const T* Xp = Sp ? Sp : Ap;
     const int64_t ldx = Sp ? lds : lda;
-    T x[NB], y[NB];
+    T x[NB];
 #pragma unroll
-    for (int c = 0; c < NB; ++c) {
-        x[c] = (ha && c < nb) ? Xp[r0 + tid + c * ldx] : T(0);
-        y[c] = (hb && c < nb) ? Xp[r0 + tid + kReg2Threads + c * ldx] : T(0);
-    }
-    // current positions of this thread's rows, whether they still take part,
-    // and the leaf step at which they became a pivot row (-1: not this leaf)
-    int pos_a = r0 + tid, pos_b = r0 + tid + kReg2Threads;
-    bool act_a = ha, act_b = hb;
-    const int loc_a = (cta << 16) | (2 * tid), loc_b = loc_a + 1;
+    for (int c = 0; c < NB; ++c) x[c] = (have && c < nb) ? Xp[r0 + tid + c * ldx] : T(0);
+    int pos = r0 + tid;  // this row's current position
+    bool act = have;     // still a candidate (not yet a pivot row)
+    const int loc = (cta << 16) | tid;
     cluster.sync();  // every CTA's mbarriers are initialised before any message
 
     bool prev_uf = false;
     unsigned leaf_uses = 0;
-    for (int jb = 0; jb < nb; jb += kLeaf) {
+    int prev_end = 0;  // the previous leaf's rank-8 update still owed: positions [kLeaf, prev_end)
+    unsigned prev_ufmask = 0;
+    for (int jb = 0, leaf = 0; jb < nb; jb += kLeaf, ++leaf) {
+        const int lpar = leaf & 1;
         const int steps = min(kLeaf, nb - jb);
-        const int lim = NB - jb;                          // unfinished positions
-        const int rc = max(0, nb - jb - kLeaf);           // remainder columns still to factor
-        const int rcv = (rc + V::E - 1) / V::E * V::E;    // in whole vectors (<= lim - kLeaf)
-        const int pw = kLeaf + rcv;                       // positions a pivot row sends
+        const int rc = max(0, nb - jb - kLeaf);          // columns after the leaf still to factor
+        const int rcv = (rc + V::E - 1) / V::E * V::E;   // in whole vectors
+        const int pw = kLeaf + rcv;                      // positions a pivot row sends
         const bool block = rc > 0;
         if (block && G > 1 && tid == 0)
             mbar_expect_tx(&mbar_leaf, (uint32_t)(steps * pw * (int)sizeof(T)));
-        int dstep_a = -1, dstep_b = -1;
+        int dstep = -1;       // leaf step at which this row became a pivot row
+        int send_step = -1;   // this thread's pivot row, not yet sent
         unsigned ufmask = 0;
+        T lprev = T(0);       // the previous step's multiplier, owed on positions > step + 1
+        bool owe = false;
 #pragma unroll
         for (int u = 0; u < kLeaf; ++u) {
             if (u >= steps) break;
             const int j = jb + u;
             const int par = j & 1;
             const bool r2 = s_mode[j] && !prev_uf;
-            // 1. this warp's candidate: the larger key, the lower position on a tie
-            unsigned long long bk = 0;
-            int bi = INT_MAX;
-            if (act_a) {
-                bk = reg_pivot_key(x[u], pos_a == j, r2);
-                bi = pos_a;
-            }
-            if (act_b) {
-                const unsigned long long kb = reg_pivot_key(y[u], pos_b == j, r2);
-                if (bi == INT_MAX || kb > bk || (kb == bk && pos_b < bi)) {
-                    bk = kb;
-                    bi = pos_b;
-                }
-            }
+            // 1. this warp's candidate; the winner's leaf part with the owed update applied
+            unsigned long long bk = act ? reg_pivot_key(x[u], pos == j, r2) : 0ull;
+            int bi = act ? pos : INT_MAX;
             reg_key_reduce<T>(bk, bi);
-            if (bi != INT_MAX) {
-                if (act_a && pos_a == bi) {
-                    leaf_stage_row<T, NB>(warp_leaf[warp], x, kLeaf);
-                    s_loc[warp] = loc_a;
-                } else if (act_b && pos_b == bi) {
-                    leaf_stage_row<T, NB>(warp_leaf[warp], y, kLeaf);
-                    s_loc[warp] = loc_b;
-                }
+            if (act && pos == bi) {
+                T lp[kLeaf];
+#pragma unroll
+                for (int c = 0; c < kLeaf; ++c)
+                    lp[c] = (u > 0 && owe && c > u) ? fma(-lprev, s_urow[u > 0 ? u - 1 : 0][c], x[c]) : x[c];
+#pragma unroll
+                for (int q = 0; q < kLeaf / V::E; ++q)
+                    reinterpret_cast<typename V::type*>(warp_leaf[warp])[q] = V::make(&lp[q * V::E]);
+                s_loc[warp] = loc;
             }
             if (lane == 0) {
                 s_key[warp] = bk;
                 s_idx[warp] = bi;
             }
             __syncthreads();
-            if (block && G > 1 && u > 0 && warp == kReg2Warps - 1 && lane < G && s_staged[u - 1])
-                bulk_s2cluster(cluster_addr(&s_rem[u - 1][0], lane), s_stage[u - 1],
-                               (uint32_t)(pw * sizeof(T)), cluster_addr(&mbar_leaf, lane));
             if (warp == 0) {
-                // 2. this CTA's candidate
-                bk = lane < kReg2Warps ? s_key[lane] : 0ull;
-                bi = lane < kReg2Warps ? s_idx[lane] : INT_MAX;
+                // 2. this CTA's candidate; with a cluster, one message into every CTA
+                bk = lane < kLeafWarps ? s_key[lane] : 0ull;
+                bi = lane < kLeafWarps ? s_idx[lane] : INT_MAX;
                 reg_key_reduce<T>(bk, bi);
-                const unsigned wm = __ballot_sync(0xffffffffu, lane < kReg2Warps && bi != INT_MAX && s_idx[lane] == bi);
+                const unsigned wm = __ballot_sync(0xffffffffu, lane < kLeafWarps && bi != INT_MAX && s_idx[lane] == bi);
                 const int ww = wm ? __ffs(wm) - 1 : -1;
                 if (G == 1) {
                     if (lane == 0) {
@@ -1035,17 +1024,15 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
                         s_wloc = ww >= 0 ? s_loc[ww] : -1;
                     }
                     if (ww >= 0 && lane < kLeaf / V::E)
-                        reinterpret_cast<typename V::type*>(urow)[lane] =
+                        reinterpret_cast<typename V::type*>(s_urow[u])[lane] =
                             reinterpret_cast<const typename V::type*>(warp_leaf[ww])[lane];
                 } else {
-                    // 3. one message into every CTA; its arrival completes
-                    //    that CTA's mbarrier for this column
                     if (lane == 0) mbar_expect_tx(&mbar[par], (uint32_t)(G * sizeof(LeafMsg<T>)));
                     if (lane < G) {
                         const uint32_t dst = cluster_addr(&msg[par][cta], lane);
                         const uint32_t bar = cluster_addr(&mbar[par], lane);
-                        const int loc = ww >= 0 ? s_loc[ww] : -1;
-                        st_async16(dst, make_uint4((unsigned)bk, (unsigned)(bk >> 32), (unsigned)bi, (unsigned)loc), bar);
+                        const int wl = ww >= 0 ? s_loc[ww] : -1;
+                        st_async16(dst, make_uint4((unsigned)bk, (unsigned)(bk >> 32), (unsigned)bi, (unsigned)wl), bar);
 #pragma unroll
                         for (int q = 1; q < kMsgVecs; ++q) {
                             const uint4 v = ww >= 0 ? reinterpret_cast<const uint4*>(warp_leaf[ww])[q - 1]
@@ -1053,102 +1040,90 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
                             st_async16(dst + 16 * q, v, bar);
                         }
                     }
-                    const bool got = __all_sync(0xffffffffu, mbar_wait(&mbar[par], (uint32_t)((j >> 1) & 1)));
-                    if (!got) {
-                        if (lane == 0) {
-                            s_abort = 1;
-                            atomicCAS(err, (int)kDevOk, (int)kDevTimeout);
-                        }
-                    } else {
-                        unsigned long long wk = lane < G ? msg[par][lane].key : 0ull;
-                        int wi = lane < G ? msg[par][lane].pos : INT_MAX;
-                        reg_key_reduce<T>(wk, wi);
-                        const unsigned om = __ballot_sync(0xffffffffu, lane < G && wi != INT_MAX && msg[par][lane].pos == wi);
-                        const int wo = om ? __ffs(om) - 1 : -1;
-                        if (lane == 0) {
-                            s_wk = wk;
-                            s_wi = wi;
-                            s_wloc = wo >= 0 ? msg[par][wo].loc : -1;
-                        }
-                        if (wo >= 0 && lane < kLeaf / V::E)
-                            reinterpret_cast<typename V::type*>(urow)[lane] =
-                                reinterpret_cast<const typename V::type*>(msg[par][wo].leaf)[lane];
+                }
+            }
+            // 3. the shadow: work this row owes, while the messages travel
+            if (u > 0 && owe) leaf_axpy<T, NB>(x, lprev, s_urow[u > 0 ? u - 1 : 0], u + 1);
+            owe = false;
+            if (u == 0 && act && prev_end > kLeaf)
+                leaf_rank8<T, NB, NB - kLeaf, kLeaf, NB - kLeaf>(x, &s_rem[lpar ^ 1][0][0], prev_ufmask, prev_end);
+            if (send_step >= 0) {
+                leaf_send_row<T, NB>(x, pw, G, s_stage[send_step], s_rem[lpar][send_step], &mbar_leaf);
+                send_step = -1;
+            }
+            if (warp == 0 && G > 1) {
+                // 4. every CTA's message (bounded wait), reduced here
+                const bool got = __all_sync(0xffffffffu, mbar_wait(&mbar[par], (uint32_t)((j >> 1) & 1)));
+                if (!got) {
+                    if (lane == 0) {
+                        s_abort = 1;
+                        atomicCAS(err, (int)kDevOk, (int)kDevTimeout);
                     }
+                } else {
+                    unsigned long long wk = lane < G ? msg[par][lane].key : 0ull;
+                    int wi = lane < G ? msg[par][lane].pos : INT_MAX;
+                    reg_key_reduce<T>(wk, wi);
+                    const unsigned om = __ballot_sync(0xffffffffu, lane < G && wi != INT_MAX && msg[par][lane].pos == wi);
+                    const int wo = om ? __ffs(om) - 1 : -1;
+                    if (lane == 0) {
+                        s_wk = wk;
+                        s_wi = wi;
+                        s_wloc = wo >= 0 ? msg[par][wo].loc : -1;
+                    }
+                    if (wo >= 0 && lane < kLeaf / V::E)
+                        reinterpret_cast<typename V::type*>(s_urow[u])[lane] =
+                            reinterpret_cast<const typename V::type*>(msg[par][wo].leaf)[lane];
                 }
             }
             __syncthreads();
             if (s_abort) break;
-            const unsigned long long wk = s_wk;
-            const int wi = s_wi;
-            const bool uf = reg_key_underflows<T>(wk);
-            // the row that becomes position j's final row: the pivot, or on
-            // underflow the row already at position j (no interchange)
-            bool own_a, own_b;
+            // 5. the decision: bookkeeping, the column's scaling and the next column
+            const bool uf = reg_key_underflows<T>(s_wk);
+            bool own;
             if (uf) {
-                own_a = act_a && pos_a == j;
-                own_b = act_b && pos_b == j;
-                if (act_a) x[u] = T(0);
-                if (act_b) y[u] = T(0);
+                own = act && pos == j;
+                if (act) x[u] = T(0);
                 if (tid == 0) s_piv[j] = (int)(k + j);
                 ufmask |= 1u << u;
                 prev_uf = true;
             } else {
-                const int wloc = s_wloc;
-                own_a = act_a && loc_a == wloc;
-                own_b = act_b && loc_b == wloc;
+                const int wi = s_wi;
+                own = act && loc == s_wloc;
                 if (tid == 0) s_piv[j] = (int)(k + wi);
                 prev_uf = false;
-                // the interchange: the row at position j moves to position wi
-                if (act_a && !own_a && pos_a == j) pos_a = wi;
-                if (act_b && !own_b && pos_b == j) pos_b = wi;
+                if (act && !own && pos == j) pos = wi;  // the interchange
             }
-            if (own_a) {
-                act_a = false;
-                pos_a = j;
-                dstep_a = u;
+            if (own) {
+                act = false;
+                pos = j;
+                dstep = u;
+                if (block) send_step = u;
             }
-            if (own_b) {
-                act_b = false;
-                pos_b = j;
-                dstep_b = u;
-            }
-            // the pivot row's unfinished part goes to every CTA for the leaf's end
-            // (staged here; the last warp bulk-copies it while warp 0 runs
-            // the next column's exchange, or at the leaf's end)
-            if (block && (own_a || own_b)) {
-                // one CTA: straight into the receive buffer
-                T* st = G == 1 ? s_rem[u] : s_stage[u];
-                if (own_a) leaf_stage_row<T, NB>(st, x, pw);
-                else leaf_stage_row<T, NB>(st, y, pw);
-                if (G > 1) {
-                    fence_proxy_async_smem();
-                    s_staged[u] = 1;
-                }
-            }
-            if (!uf) {
+            if (!uf && act) {
                 // TMV scales the column by the reciprocal of the pivot
-                const T rp = recip_rn(urow[u]);
-                if (act_a) {
-                    const T l = x[u] * rp;
-                    x[u] = l;
-                    leaf_rank1<T, NB>(x, l, urow, u);
+                const T l = x[u] * recip_rn(s_urow[u][u]);
+                x[u] = l;
+                if (u < kLast) {
+                    const int c1 = u < kLast ? u + 1 : u;
+                    x[c1] = fma(-l, s_urow[u][c1], x[c1]);
                 }
-                if (act_b) {
-                    const T l = y[u] * rp;
-                    y[u] = l;
-                    leaf_rank1<T, NB>(y, l, urow, u);
+                if (u + 2 < kLeaf) {
+                    lprev = l;
+                    owe = true;
                 }
             }
         }
         if (s_abort) break;
+        prev_end = 0;
         if (block) {
-            // 4. the leaf's pivot rows: U12 = L11^-1 A12 (every CTA the same),
-            //    then the rank-8 update of the columns after the leaf
+            // 6. the leaf's end: the last pivot row out, the leaf's U12 (every
+            //    CTA the same), the next leaf's columns, and the final values
+            //    of the leaf's pivot rows
+            if (send_step >= 0) {
+                leaf_send_row<T, NB>(x, pw, G, s_stage[send_step], s_rem[lpar][send_step], &mbar_leaf);
+                send_step = -1;
+            }
             if (G > 1) {
-                __syncthreads();  // the last step's pivot row is staged
-                if (warp == kReg2Warps - 1 && lane < G && s_staged[steps - 1])
-                    bulk_s2cluster(cluster_addr(&s_rem[steps - 1][0], lane), s_stage[steps - 1],
-                                   (uint32_t)(pw * sizeof(T)), cluster_addr(&mbar_leaf, lane));
                 if (!mbar_wait(&mbar_leaf, leaf_uses & 1u)) {
                     if (tid == 0) atomicCAS(err, (int)kDevOk, (int)kDevTimeout);
                     s_abort = 1;  // every thread of the CTA reaches this
@@ -1157,33 +1132,29 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
             }
             __syncthreads();
             if (s_abort) break;
-            if (tid < kLeaf) s_staged[tid] = 0;  // read again only after the next leaf's barriers
-            // forward substitution per column, in registers, steps in order
-            for (int c = kLeaf + tid; c < kLeaf + rcv; c += kReg2Threads) {
+            T(*Ur)[NB] = s_rem[lpar];
+            for (int p = kLeaf + tid; p < pw; p += kLeafThreads) {
                 T uc[kLeaf];
 #pragma unroll
-                for (int t = 0; t < kLeaf; ++t) uc[t] = t < steps ? s_rem[t][c] : T(0);
+                for (int t = 0; t < kLeaf; ++t) uc[t] = Ur[t][p];
 #pragma unroll
                 for (int t = 1; t < kLeaf; ++t) {
-                    if (t >= steps) break;
 #pragma unroll
                     for (int q = 0; q < t; ++q)
-                        if (!((ufmask >> q) & 1u)) uc[t] = fma(-s_rem[t][q], uc[q], uc[t]);
+                        if (!((ufmask >> q) & 1u)) uc[t] = fma(-Ur[t][q], uc[q], uc[t]);
                 }
 #pragma unroll
-                for (int t = 0; t < kLeaf; ++t)
-                    if (t < steps) s_rem[t][c] = uc[t];
+                for (int t = 0; t < kLeaf; ++t) Ur[t][p] = uc[t];
             }
             __syncthreads();
-            if (act_a) leaf_block_update<T, NB>(x, &s_rem[0][0], NB, steps, ufmask, rcv);
-            else if (dstep_a >= 0) leaf_take_u<T, NB>(x, s_rem[dstep_a], rcv);
-            if (act_b) leaf_block_update<T, NB>(y, &s_rem[0][0], NB, steps, ufmask, rcv);
-            else if (dstep_b >= 0) leaf_take_u<T, NB>(y, s_rem[dstep_b], rcv);
+            if (act) leaf_rank8<T, NB, 0, 0, 2 * kLeaf>(x, &Ur[0][0], ufmask, min(pw, 2 * kLeaf));
+            else if (dstep >= 0) leaf_take_u<T, NB>(x, Ur[dstep], pw);
+            // positions [2 kLeaf, pw) are owed; after the rotation below they
+            // are [kLeaf, pw - kLeaf)
+            prev_end = pw - kLeaf;
+            prev_ufmask = ufmask;
         }
-        if (jb + kLeaf < nb) {
-            leaf_rotate<T, NB>(x);
-            leaf_rotate<T, NB>(y);
-        }
+        if (jb + kLeaf < nb) leaf_rotate<T, NB>(x);
     }
 
     if (!s_abort) {
@@ -1191,30 +1162,25 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
         // rows below the panel block also as the TF32 hi/lo split of L21
         // (row-major, nb wide) that the step's tensor-core update reads
         const int rot = ((nb - 1) / kLeaf) * kLeaf;  // x[p] holds column (p + rot) mod NB
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const bool have = h == 0 ? ha : hb;
-            const int pr = h == 0 ? pos_a : pos_b;
-            if (!have) continue;
-            const bool split = std::is_same<T, float>::value && ahi != nullptr && pr >= nb;
+        if (have) {
+            const bool split = std::is_same<T, float>::value && ahi != nullptr && pos >= nb;
 #pragma unroll
             for (int p = 0; p < NB; ++p) {
                 const int col = (p + rot) % NB;
                 if (col < nb) {
-                    const T v = h == 0 ? x[p] : y[p];
-                    Ap[pr + col * lda] = v;
+                    Ap[pos + col * lda] = x[p];
                     if (split) {
-                        const float f = (float)v;
+                        const float f = (float)x[p];
                         const float hi = tf32_round(f);
-                        ahi[(int64_t)(pr - nb) * nb + col] = hi;
-                        alo[(int64_t)(pr - nb) * nb + col] = tf32_round(f - hi);
+                        ahi[(int64_t)(pos - nb) * nb + col] = hi;
+                        alo[(int64_t)(pos - nb) * nb + col] = tf32_round(f - hi);
                     }
                 }
             }
         }
         __syncthreads();
         if (cta == 0) {
-            for (int j = tid; j < nb; j += kReg2Threads) P[k + j] = s_piv[j];
+            for (int j = tid; j < nb; j += kLeafThreads) P[k + j] = s_piv[j];
             if (warp == 0) panel_row_pairs(k, nb, s_piv, pairs);
         }
     }
@@ -2088,7 +2054,7 @@ static bool reg_panel_ok(Context* c)
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.gridDim = dim3(kClusterCtas);
-    cfg.blockDim = dim3(kReg2Threads);
+    cfg.blockDim = dim3(c->panel_reg2 ? kReg2Threads : kLeafThreads);
     cfg.dynamicSmemBytes = 0;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
@@ -2119,7 +2085,7 @@ static tmvg_status launch_panel_cluster_reg(Context* c, cudaStream_t s, T* A, in
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.gridDim = dim3(G);
-    cfg.blockDim = dim3(kReg2Threads);
+    cfg.blockDim = dim3(c->panel_reg2 ? kReg2Threads : kLeafThreads);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = s;
     cfg.attrs = attr;
