@@ -779,14 +779,16 @@ lu_panel_cluster_reg2_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t 
 // exchange, while warp 0 waits for the other CTAs.
 //
 // * One panel row per thread, 512 threads per CTA (16 CTAs: m <= 8192).
-// * Columns are factored in leaves of kLeaf = 8.  After a pivot decision a
-//   thread scales its row's column j and updates column j+1 (the next key);
+// * Columns are factored in leaves of kLeaf = 8; the step loop is not
+//   unrolled (every column runs the same instructions: a large unrolled body
+//   misses in the instruction cache), and the leaf's eight registers rotate
+//   by one position per step so that column j is always x[0].  After a pivot
+//   decision a thread scales its row's column j and updates column j+1 (the next key);
 //   the rest of the step's rank-1 update on the leaf is owed and paid in the
 //   next column's shadow.  A leaf's effect on the later columns is a rank-8
-//   update A2 -= L1 U12 with U12 = L11^-1 A12 solved from the leaf's pivot
-//   rows: on the next leaf's eight columns at the end of the leaf, on the
-//   rest in the first shadow of the next leaf.  Every entry still receives
-//   TMV's subtractions in TMV's order, one fused multiply-add each.
+//   update A2 -= L1 U12 at the end of the leaf, with U12 = L11^-1 A12 solved
+//   from the leaf's pivot rows.  Every entry still receives TMV's
+//   subtractions in TMV's order, one fused multiply-add each.
 // * Rows never move: each thread tracks its row's current position; an
 //   interchange swaps two positions, a pivot row is marked done, and rows
 //   are written to their final positions at the end.  Ties go to the lowest
@@ -821,16 +823,6 @@ __device__ __forceinline__ void leaf_stage_row(T* __restrict__ dst, const T (&x)
         if (v * V::E >= pw) break;
         reinterpret_cast<typename V::type*>(dst)[v] = V::make(&x[v * V::E]);
     }
-}
-
-// x[c] -= l * ur[c] for the leaf positions c >= c0 (c0 is a constant once
-// the caller's step loop is unrolled).
-template <typename T, int NB>
-__device__ __forceinline__ void leaf_axpy(T (&x)[NB], T l, const T* __restrict__ ur, int c0)
-{
-#pragma unroll
-    for (int c = 0; c < kLeaf; ++c)
-        if (c >= c0) x[c] = fma(-l, ur[c], x[c]);
 }
 
 // Rank-8 update of positions [kLeaf, pend) of a row: x[p] -= x[LP + t] *
@@ -892,17 +884,33 @@ __device__ __forceinline__ void leaf_rotate(T (&x)[NB])
     for (int c = 0; c < kLeaf; ++c) x[NB - kLeaf + c] = t[c];
 }
 
-// A pivot row's positions [0, pw) into every CTA's receive buffer `dst_row`
-// (one CTA: written there directly).
+// The leaf part by one position: x[q] <- x[q + 1], x[kLeaf - 1] <- x[0].
 template <typename T, int NB>
-__device__ __forceinline__ void leaf_send_row(const T (&x)[NB], int pw, int G, T* stage, T* dst_row,
+__device__ __forceinline__ void leaf_rotate1(T (&x)[NB])
+{
+    const T t = x[0];
+#pragma unroll
+    for (int q = 0; q < kLeaf - 1; ++q) x[q] = x[q + 1];
+    x[kLeaf - 1] = t;
+}
+
+// A pivot row's columns [0, pw) into every CTA's receive buffer `dst_row`
+// (one CTA: written there directly); its leaf part is rotated by `rot`
+// (position q holds leaf column (rot + q) mod kLeaf).
+template <typename T, int NB>
+__device__ __forceinline__ void leaf_send_row(const T (&x)[NB], int rot, int pw, int G, T* stage, T* dst_row,
                                               uint64_t* bar)
 {
-    if (G == 1) {
-        leaf_stage_row<T, NB>(dst_row, x, pw);
-        return;
+    T* buf = G == 1 ? dst_row : stage;
+#pragma unroll
+    for (int q = 0; q < kLeaf; ++q) buf[(rot + q) & (kLeaf - 1)] = x[q];
+    using V = Vec16<T>;
+#pragma unroll
+    for (int v = kLeaf / V::E; v < NB / V::E; ++v) {
+        if (v * V::E >= pw) break;
+        reinterpret_cast<typename V::type*>(buf)[v] = V::make(&x[v * V::E]);
     }
-    leaf_stage_row<T, NB>(stage, x, pw);
+    if (G == 1) return;
     fence_proxy_async_smem();
     for (int d = 0; d < G; ++d)
         bulk_s2cluster(cluster_addr(dst_row, d), stage, (uint32_t)(pw * sizeof(T)), cluster_addr(bar, d));
@@ -969,8 +977,6 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
 
     bool prev_uf = false;
     unsigned leaf_uses = 0;
-    int prev_end = 0;  // the previous leaf's rank-8 update still owed: positions [kLeaf, prev_end)
-    unsigned prev_ufmask = 0;
     for (int jb = 0, leaf = 0; jb < nb; jb += kLeaf, ++leaf) {
         const int lpar = leaf & 1;
         const int steps = min(kLeaf, nb - jb);
@@ -985,21 +991,24 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
         unsigned ufmask = 0;
         T lprev = T(0);       // the previous step's multiplier, owed on positions > step + 1
         bool owe = false;
-#pragma unroll
-        for (int u = 0; u < kLeaf; ++u) {
-            if (u >= steps) break;
+#pragma unroll 1
+        for (int u = 0; u < steps; ++u) {
+            // the leaf's registers are rotated one position per step:
+            // position q holds column (u + q) mod kLeaf of the leaf
             const int j = jb + u;
             const int par = j & 1;
             const bool r2 = s_mode[j] && !prev_uf;
             // 1. this warp's candidate; the winner's leaf part with the owed update applied
-            unsigned long long bk = act ? reg_pivot_key(x[u], pos == j, r2) : 0ull;
+            unsigned long long bk = act ? reg_pivot_key(x[0], pos == j, r2) : 0ull;
             int bi = act ? pos : INT_MAX;
             reg_key_reduce<T>(bk, bi);
             if (act && pos == bi) {
+                // (in position order; positions 1..7-u owe step u-1's update,
+                // whose pivot row s_urow[u-1] is in step u-1's position order)
                 T lp[kLeaf];
 #pragma unroll
-                for (int c = 0; c < kLeaf; ++c)
-                    lp[c] = (u > 0 && owe && c > u) ? fma(-lprev, s_urow[u > 0 ? u - 1 : 0][c], x[c]) : x[c];
+                for (int q = 0; q < kLeaf; ++q)
+                    lp[q] = (owe && q >= 1 && q <= kLast - u) ? fma(-lprev, s_urow[u - 1][q + 1 < kLeaf ? q + 1 : q], x[q]) : x[q];
 #pragma unroll
                 for (int q = 0; q < kLeaf / V::E; ++q)
                     reinterpret_cast<typename V::type*>(warp_leaf[warp])[q] = V::make(&lp[q * V::E]);
@@ -1043,12 +1052,14 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
                 }
             }
             // 3. the shadow: work this row owes, while the messages travel
-            if (u > 0 && owe) leaf_axpy<T, NB>(x, lprev, s_urow[u > 0 ? u - 1 : 0], u + 1);
+            if (owe) {
+#pragma unroll
+                for (int q = 1; q < kLeaf; ++q)
+                    if (q <= kLast - u) x[q] = fma(-lprev, s_urow[u - 1][q + 1 < kLeaf ? q + 1 : q], x[q]);
+            }
             owe = false;
-            if (u == 0 && act && prev_end > kLeaf)
-                leaf_rank8<T, NB, NB - kLeaf, kLeaf, NB - kLeaf>(x, &s_rem[lpar ^ 1][0][0], prev_ufmask, prev_end);
             if (send_step >= 0) {
-                leaf_send_row<T, NB>(x, pw, G, s_stage[send_step], s_rem[lpar][send_step], &mbar_leaf);
+                leaf_send_row<T, NB>(x, u, pw, G, s_stage[send_step], s_rem[lpar][send_step], &mbar_leaf);
                 send_step = -1;
             }
             if (warp == 0 && G > 1) {
@@ -1082,7 +1093,7 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
             bool own;
             if (uf) {
                 own = act && pos == j;
-                if (act) x[u] = T(0);
+                if (act) x[0] = T(0);
                 if (tid == 0) s_piv[j] = (int)(k + j);
                 ufmask |= 1u << u;
                 prev_uf = true;
@@ -1101,26 +1112,24 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
             }
             if (!uf && act) {
                 // TMV scales the column by the reciprocal of the pivot
-                const T l = x[u] * recip_rn(s_urow[u][u]);
-                x[u] = l;
-                if (u < kLast) {
-                    const int c1 = u < kLast ? u + 1 : u;
-                    x[c1] = fma(-l, s_urow[u][c1], x[c1]);
-                }
+                const T l = x[0] * recip_rn(s_urow[u][0]);
+                x[0] = l;
+                if (u < kLast) x[1] = fma(-l, s_urow[u][1], x[1]);
                 if (u + 2 < kLeaf) {
                     lprev = l;
                     owe = true;
                 }
             }
+            leaf_rotate1<T, NB>(x);
         }
         if (s_abort) break;
-        prev_end = 0;
+        for (int r = steps; r < kLeaf; ++r) leaf_rotate1<T, NB>(x);  // back to column order
         if (block) {
             // 6. the leaf's end: the last pivot row out, the leaf's U12 (every
-            //    CTA the same), the next leaf's columns, and the final values
-            //    of the leaf's pivot rows
+            //    CTA the same), the rank-8 update of the columns after the
+            //    leaf, and the final values of the leaf's pivot rows
             if (send_step >= 0) {
-                leaf_send_row<T, NB>(x, pw, G, s_stage[send_step], s_rem[lpar][send_step], &mbar_leaf);
+                leaf_send_row<T, NB>(x, 0, pw, G, s_stage[send_step], s_rem[lpar][send_step], &mbar_leaf);
                 send_step = -1;
             }
             if (G > 1) {
@@ -1147,12 +1156,8 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
                 for (int t = 0; t < kLeaf; ++t) Ur[t][p] = uc[t];
             }
             __syncthreads();
-            if (act) leaf_rank8<T, NB, 0, 0, 2 * kLeaf>(x, &Ur[0][0], ufmask, min(pw, 2 * kLeaf));
+            if (act) leaf_rank8<T, NB, 0, 0, NB>(x, &Ur[0][0], ufmask, pw);
             else if (dstep >= 0) leaf_take_u<T, NB>(x, Ur[dstep], pw);
-            // positions [2 kLeaf, pw) are owed; after the rotation below they
-            // are [kLeaf, pw - kLeaf)
-            prev_end = pw - kLeaf;
-            prev_ufmask = ufmask;
         }
         if (jb + kLeaf < nb) leaf_rotate<T, NB>(x);
     }
