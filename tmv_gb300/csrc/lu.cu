@@ -946,6 +946,7 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
     __shared__ int s_wi, s_wloc;
     __shared__ unsigned char s_mode[kPanelMax];
     __shared__ int s_piv[kPanelMax];
+    __shared__ int s_npairs;  // row pairs written so far (used in CTA 0)
     __shared__ int s_abort;
 
     const int G = (int)cluster.num_blocks();
@@ -962,6 +963,7 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
         mbar_init(&mbar[1], 1u);
         mbar_init(&mbar_leaf, 1u);
         s_abort = 0;
+        s_npairs = 0;
         mbar_fence_init();
     }
     for (int j = tid; j < nb; j += kLeafThreads) s_mode[j] = modes[j];
@@ -1165,31 +1167,63 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
     if (!s_abort) {
         // rows to their final positions; with ahi (FP32 factorisation) the
         // rows below the panel block also as the TF32 hi/lo split of L21
-        // (row-major, nb wide) that the step's tensor-core update reads
+        // (row-major, nb wide; 16-byte stores when nb allows) that the step's
+        // tensor-core update reads
         const int rot = ((nb - 1) / kLeaf) * kLeaf;  // x[p] holds column (p + rot) mod NB
         if (have) {
-            const bool split = std::is_same<T, float>::value && ahi != nullptr && pos >= nb;
 #pragma unroll
             for (int p = 0; p < NB; ++p) {
                 const int col = (p + rot) % NB;
-                if (col < nb) {
-                    Ap[pos + col * lda] = x[p];
-                    if (split) {
-                        const float f = (float)x[p];
-                        const float hi = tf32_round(f);
-                        ahi[(int64_t)(pos - nb) * nb + col] = hi;
-                        alo[(int64_t)(pos - nb) * nb + col] = tf32_round(f - hi);
+                if (col < nb) Ap[pos + col * lda] = x[p];
+            }
+            if (std::is_same<T, float>::value && ahi != nullptr && pos >= nb) {
+                float* hrow = ahi + (int64_t)(pos - nb) * nb;
+                float* lrow = alo + (int64_t)(pos - nb) * nb;
+                if ((nb & 3) == 0) {
+#pragma unroll
+                    for (int p = 0; p < NB; p += 4) {
+                        const int col = (p + rot) % NB;  // rot is a multiple of 4: no wrap
+                        if (col < nb) {
+                            float hi[4], lo[4];
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) {
+                                const float f = (float)x[p + e];
+                                hi[e] = tf32_round(f);
+                                lo[e] = tf32_round(f - hi[e]);
+                            }
+                            *reinterpret_cast<float4*>(hrow + col) = make_float4(hi[0], hi[1], hi[2], hi[3]);
+                            *reinterpret_cast<float4*>(lrow + col) = make_float4(lo[0], lo[1], lo[2], lo[3]);
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int p = 0; p < NB; ++p) {
+                        const int col = (p + rot) % NB;
+                        if (col < nb) {
+                            const float f = (float)x[p];
+                            const float hi = tf32_round(f);
+                            hrow[col] = hi;
+                            lrow[col] = tf32_round(f - hi);
+                        }
                     }
                 }
             }
+            // the interchanges as a row gather: a row that moved is one pair,
+            // "row k + pos receives the old row k + r0 + tid" (slots handed
+            // out by a counter in CTA 0's shared memory; consumers read the
+            // pairs as a set)
+            if (pos != r0 + tid) {
+                int* cnt = cluster.map_shared_rank(&s_npairs, 0);
+                const int q = atomicAdd(cnt, 1);
+                pairs[1 + q] = (int)(k + pos);
+                pairs[1 + kMaxPairs + q] = (int)(k + r0 + tid);
+            }
         }
-        __syncthreads();
-        if (cta == 0) {
+        if (cta == 0)
             for (int j = tid; j < nb; j += kLeafThreads) P[k + j] = s_piv[j];
-            if (warp == 0) panel_row_pairs(k, nb, s_piv, pairs);
-        }
     }
     cluster.sync();  // no CTA leaves while another may still store into it
+    if (cta == 0 && tid == 0 && !s_abort) pairs[0] = s_npairs;
 }
 
 // ---------------------------------------------------------------------
