@@ -1165,48 +1165,15 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
     }
 
     if (!s_abort) {
-        // rows to their final positions; with ahi (FP32 factorisation) the
-        // rows below the panel block also as the TF32 hi/lo split of L21
-        // (row-major, nb wide; 16-byte stores when nb allows) that the step's
-        // tensor-core update reads
+        // rows to their final positions (the TF32 split of L21 that the
+        // tensor-core update reads is made by its own kernel; ahi and alo are
+        // not written here)
         const int rot = ((nb - 1) / kLeaf) * kLeaf;  // x[p] holds column (p + rot) mod NB
         if (have) {
 #pragma unroll
             for (int p = 0; p < NB; ++p) {
                 const int col = (p + rot) % NB;
                 if (col < nb) Ap[pos + col * lda] = x[p];
-            }
-            if (std::is_same<T, float>::value && ahi != nullptr && pos >= nb) {
-                float* hrow = ahi + (int64_t)(pos - nb) * nb;
-                float* lrow = alo + (int64_t)(pos - nb) * nb;
-                if ((nb & 3) == 0) {
-#pragma unroll
-                    for (int p = 0; p < NB; p += 4) {
-                        const int col = (p + rot) % NB;  // rot is a multiple of 4: no wrap
-                        if (col < nb) {
-                            float hi[4], lo[4];
-#pragma unroll
-                            for (int e = 0; e < 4; ++e) {
-                                const float f = (float)x[p + e];
-                                hi[e] = tf32_round(f);
-                                lo[e] = tf32_round(f - hi[e]);
-                            }
-                            *reinterpret_cast<float4*>(hrow + col) = make_float4(hi[0], hi[1], hi[2], hi[3]);
-                            *reinterpret_cast<float4*>(lrow + col) = make_float4(lo[0], lo[1], lo[2], lo[3]);
-                        }
-                    }
-                } else {
-#pragma unroll
-                    for (int p = 0; p < NB; ++p) {
-                        const int col = (p + rot) % NB;
-                        if (col < nb) {
-                            const float f = (float)x[p];
-                            const float hi = tf32_round(f);
-                            hrow[col] = hi;
-                            lrow[col] = tf32_round(f - hi);
-                        }
-                    }
-                }
             }
             // the interchanges as a row gather: a row that moved is one pair,
             // "row k + pos receives the old row k + r0 + tid" (slots handed
@@ -2246,12 +2213,10 @@ tmvg_status lu_factor(Context* c, int64_t n, T* A, int64_t lda, int64_t* P)
         // written by its fused narrow update
         auto panel = [&](int64_t kk, int w, int64_t step, bool from_scratch = false) -> tmvg_status {
             ScopedTimer timer(c, kClsPanel, 2.0 * sizeof(T) * (n - kk) * w, panel_flops(n - kk, w), side);
+            // (the register panel writes no L21 split: tf32x3_split_a makes it
+            // below, on the main stream, off the chain of panels)
             float* ahi = nullptr;
             float* alo = nullptr;
-            if (reg && tc_for(kk, w)) {
-                ahi = arena[step & 1].Ahi;
-                alo = arena[step & 1].Alo;
-            }
             int* pp = pairs_of(step);
             tmvg_status s2 =
                 reg ? (from_scratch
@@ -2298,8 +2263,10 @@ tmvg_status lu_factor(Context* c, int64_t n, T* A, int64_t lda, int64_t* P)
             T* Sk = Sbuf[step & 1];
             const bool fused = Sk != nullptr && nb == kNarrowNB;
             if constexpr (std::is_same<T, float>::value) {
-                // the register panel kernel writes the L21 split itself
-                if (!st && tc && !reg) st = tf32x3_split_a(c, rest, nb, A + (k + nb) + k * lda, lda, b);
+                // the L21 split here when the narrow update reads it; with the
+                // fused narrow update (exact FP32) only the wide update does,
+                // and the main stream makes it
+                if (!st && tc && !fused) st = tf32x3_split_a(c, rest, nb, A + (k + nb) + k * lda, lda, b);
                 if (!st && fused) st = narrow_update_f32(c, A, lda, n, k, k + nb, nb2, pk, Sk, n);
             }
             if (!st && !fused) st = update_columns<T>(c, n, A, lda, k, nb, k + nb, nb2, tc, b, pk);
@@ -2315,6 +2282,8 @@ tmvg_status lu_factor(Context* c, int64_t n, T* A, int64_t lda, int64_t* P)
             // first nb rows) into A: the next panel reads the scratch panel
             // and writes only rows below these, and the scratch panel is
             // reused two steps later, after this step's wide update
+            if constexpr (std::is_same<T, float>::value)
+                if (!st && tc && fused) st = tf32x3_split_a(c, rest, nb, A + (k + nb) + k * lda, lda, b);
             if (!st && fused)
                 st = check_cuda(c,
                                 cudaMemcpy2DAsync(A + k + (k + nb) * lda, sizeof(T) * lda, Sk, sizeof(T) * n,
