@@ -786,10 +786,9 @@ lu_panel_cluster_reg2_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t 
 //   decision a thread scales its row's column j and updates column j+1 (the next key);
 //   the rest of the step's rank-1 update on the leaf is owed and paid in the
 //   next column's shadow.  A leaf's effect on the later columns is a rank-8
-//   update A2 -= L1 U12, with U12 = L11^-1 A12 solved from the leaf's pivot
-//   rows: on the next leaf's eight columns at the end of the leaf, on the
-//   rest in the shadow of the next leaf's first column.  Every entry still
-//   receives TMV's subtractions in TMV's order, one fused multiply-add each.
+//   update A2 -= L1 U12 at the end of the leaf, with U12 = L11^-1 A12 solved
+//   from the leaf's pivot rows.  Every entry still receives TMV's
+//   subtractions in TMV's order, one fused multiply-add each.
 // * Warp 0 hands each decision to the CTA as one record: pivot position and
 //   location, underflow, and the reciprocal of the pivot (taken once).
 // * Rows never move: each thread tracks its row's current position; an
@@ -991,8 +990,6 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
 
     bool prev_uf = false;
     unsigned leaf_uses = 0;
-    int prev_end = 0;  // the previous leaf's rank-8 update still owed: positions [kLeaf, prev_end)
-    unsigned prev_ufmask = 0;
     for (int jb = 0, leaf = 0; jb < nb; jb += kLeaf, ++leaf) {
         const int lpar = leaf & 1;
         const int steps = min(kLeaf, nb - jb);
@@ -1010,9 +1007,8 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
 
         // One column: the leaf's registers are rotated one position per
         // step, position q holding column (u + q) mod kLeaf of the leaf.
-        // FIRST (step 0) also pays the previous leaf's owed rank-8 update in
-        // the exchange's shadow.  Returns false when a wait gave up.
-        auto column = [&](const int u, auto first) -> bool {
+        // Returns false when a wait gave up.
+        auto column = [&](const int u) -> bool {
             const int j = jb + u;
             const int par = j & 1;
             const bool r2 = s_mode[j] && !prev_uf;
@@ -1077,11 +1073,6 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
                     if (q <= kLast - u) x[q] = fma(-lprev, s_urow[u - 1][q + 1 < kLeaf ? q + 1 : q], x[q]);
             }
             owe = false;
-            if constexpr (decltype(first)::value) {
-                if (act && prev_end > kLeaf)
-                    leaf_rank8<T, NB, NB - kLeaf, kLeaf, NB - kLeaf>(x, &s_rem[lpar ^ 1][0][0], prev_ufmask,
-                                                                     prev_end);
-            }
             if (send_step >= 0) {
                 leaf_send_row<T, NB>(x, u, pw, G, s_stage[send_step], s_rem[lpar][send_step], &mbar_leaf);
                 send_step = -1;
@@ -1149,16 +1140,15 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
             return true;
         };
 
-        bool ok = column(0, std::true_type{});
+        bool ok = true;
 #pragma unroll 1
-        for (int u = 1; u < steps && ok; ++u) ok = column(u, std::false_type{});
+        for (int u = 0; u < steps && ok; ++u) ok = column(u);
         if (!ok) break;
         for (int r = steps; r < kLeaf; ++r) leaf_rotate1<T, NB>(x);  // back to column order
-        prev_end = 0;
         if (block) {
             // 6. the leaf's end: the last pivot row out, the leaf's U12 (every
-            //    CTA the same), the next leaf's columns, and the final values
-            //    of the leaf's pivot rows
+            //    CTA the same), the rank-8 update of the columns after the
+            //    leaf, and the final values of the leaf's pivot rows
             if (send_step >= 0) {
                 leaf_send_row<T, NB>(x, 0, pw, G, s_stage[send_step], s_rem[lpar][send_step], &mbar_leaf);
                 send_step = -1;
@@ -1187,12 +1177,8 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
                 for (int t = 0; t < kLeaf; ++t) Ur[t][p] = uc[t];
             }
             __syncthreads();
-            if (act) leaf_rank8<T, NB, 0, 0, 2 * kLeaf>(x, &Ur[0][0], ufmask, min(pw, 2 * kLeaf));
+            if (act) leaf_rank8<T, NB, 0, 0, NB>(x, &Ur[0][0], ufmask, pw);
             else if (dstep >= 0) leaf_take_u<T, NB>(x, Ur[dstep], pw);
-            // positions [2 kLeaf, pw) are owed; after the rotation below they
-            // are [kLeaf, pw - kLeaf), paid in the next leaf's first shadow
-            prev_end = pw - kLeaf;
-            prev_ufmask = ufmask;
         }
         if (jb + kLeaf < nb) leaf_rotate<T, NB>(x);
     }
