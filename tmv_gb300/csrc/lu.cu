@@ -789,8 +789,6 @@ lu_panel_cluster_reg2_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t 
 //   update A2 -= L1 U12 at the end of the leaf, with U12 = L11^-1 A12 solved
 //   from the leaf's pivot rows.  Every entry still receives TMV's
 //   subtractions in TMV's order, one fused multiply-add each.
-// * Warp 0 hands each decision to the CTA as one record: pivot position and
-//   location, underflow, and the reciprocal of the pivot (taken once).
 // * Rows never move: each thread tracks its row's current position; an
 //   interchange swaps two positions, a pivot row is marked done, and rows
 //   are written to their final positions at the end.  Ties go to the lowest
@@ -925,8 +923,6 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
                      int rows_per_cta, int* pairs, int* err, float* __restrict__ ahi,
                      float* __restrict__ alo, const T* __restrict__ Sp, int64_t lds)
 {
-    // (the TF32 split of L21 that the tensor-core update reads is made by its
-    // own kernel: ahi and alo are not written here)
     static_assert(NB % kLeaf == 0 && NB >= 2 * kLeaf, "whole leaves");
     static_assert(NB * sizeof(T) == 256, "a row is 16 vectors of 16 bytes");
     using V = Vec16<T>;
@@ -936,14 +932,6 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
 
-    // the decision of a column, as warp 0 hands it to the CTA
-    struct Decision {
-        int wi;    // pivot position
-        int wloc;  // pivot row's location (cta << 16 | thread)
-        int uf;    // the column underflowed
-        int pad;
-        T rp;      // reciprocal of the pivot
-    };
     __shared__ unsigned long long s_key[kLeafWarps];
     __shared__ int s_idx[kLeafWarps];
     __shared__ int s_loc[kLeafWarps];
@@ -952,9 +940,10 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
     __shared__ __align__(16) T s_urow[kLeaf][kLeaf];             // the leaf's pivot rows, leaf part
     __shared__ __align__(16) T s_rem[2][kLeaf][NB];              // pivot rows, then U (by leaf parity)
     __shared__ __align__(16) T s_stage[kLeaf][NB];               // this CTA's pivot rows, staged
-    __shared__ __align__(16) Decision s_dec;
     __shared__ __align__(8) uint64_t mbar[2];
     __shared__ __align__(8) uint64_t mbar_leaf;
+    __shared__ unsigned long long s_wk;
+    __shared__ int s_wi, s_wloc;
     __shared__ unsigned char s_mode[kPanelMax];
     __shared__ int s_piv[kPanelMax];
     __shared__ int s_npairs;  // row pairs written so far (used in CTA 0)
@@ -1004,20 +993,20 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
         unsigned ufmask = 0;
         T lprev = T(0);       // the previous step's multiplier, owed on positions > step + 1
         bool owe = false;
-
-        // One column: the leaf's registers are rotated one position per
-        // step, position q holding column (u + q) mod kLeaf of the leaf.
-        // Returns false when a wait gave up.
-        auto column = [&](const int u) -> bool {
+#pragma unroll 1
+        for (int u = 0; u < steps; ++u) {
+            // the leaf's registers are rotated one position per step:
+            // position q holds column (u + q) mod kLeaf of the leaf
             const int j = jb + u;
             const int par = j & 1;
             const bool r2 = s_mode[j] && !prev_uf;
-            // 1. this warp's candidate; the winner's leaf part (position
-            //    order) with the owed update applied
+            // 1. this warp's candidate; the winner's leaf part with the owed update applied
             unsigned long long bk = act ? reg_pivot_key(x[0], pos == j, r2) : 0ull;
             int bi = act ? pos : INT_MAX;
             reg_key_reduce<T>(bk, bi);
             if (act && pos == bi) {
+                // (in position order; positions 1..7-u owe step u-1's update,
+                // whose pivot row s_urow[u-1] is in step u-1's position order)
                 T lp[kLeaf];
 #pragma unroll
                 for (int q = 0; q < kLeaf; ++q)
@@ -1040,16 +1029,14 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
                 const unsigned wm = __ballot_sync(0xffffffffu, lane < kLeafWarps && bi != INT_MAX && s_idx[lane] == bi);
                 const int ww = wm ? __ffs(wm) - 1 : -1;
                 if (G == 1) {
+                    if (lane == 0) {
+                        s_wk = bk;
+                        s_wi = bi;
+                        s_wloc = ww >= 0 ? s_loc[ww] : -1;
+                    }
                     if (ww >= 0 && lane < kLeaf / V::E)
                         reinterpret_cast<typename V::type*>(s_urow[u])[lane] =
                             reinterpret_cast<const typename V::type*>(warp_leaf[ww])[lane];
-                    if (lane == 0) {
-                        const bool uf = reg_key_underflows<T>(bk);
-                        s_dec.wi = bi;
-                        s_dec.wloc = ww >= 0 ? s_loc[ww] : -1;
-                        s_dec.uf = uf;
-                        s_dec.rp = (!uf && ww >= 0) ? recip_rn(warp_leaf[ww][0]) : T(0);
-                    }
                 } else {
                     if (lane == 0) mbar_expect_tx(&mbar[par], (uint32_t)(G * sizeof(LeafMsg<T>)));
                     if (lane < G) {
@@ -1091,34 +1078,33 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
                     reg_key_reduce<T>(wk, wi);
                     const unsigned om = __ballot_sync(0xffffffffu, lane < G && wi != INT_MAX && msg[par][lane].pos == wi);
                     const int wo = om ? __ffs(om) - 1 : -1;
+                    if (lane == 0) {
+                        s_wk = wk;
+                        s_wi = wi;
+                        s_wloc = wo >= 0 ? msg[par][wo].loc : -1;
+                    }
                     if (wo >= 0 && lane < kLeaf / V::E)
                         reinterpret_cast<typename V::type*>(s_urow[u])[lane] =
                             reinterpret_cast<const typename V::type*>(msg[par][wo].leaf)[lane];
-                    if (lane == 0) {
-                        const bool uf = reg_key_underflows<T>(wk);
-                        s_dec.wi = wi;
-                        s_dec.wloc = wo >= 0 ? msg[par][wo].loc : -1;
-                        s_dec.uf = uf;
-                        s_dec.rp = (!uf && wo >= 0) ? recip_rn(msg[par][wo].leaf[0]) : T(0);
-                    }
                 }
             }
             __syncthreads();
-            if (s_abort) return false;
+            if (s_abort) break;
             // 5. the decision: bookkeeping, the column's scaling and the next column
-            const Decision d = s_dec;
+            const bool uf = reg_key_underflows<T>(s_wk);
             bool own;
-            if (d.uf) {
+            if (uf) {
                 own = act && pos == j;
                 if (act) x[0] = T(0);
                 if (tid == 0) s_piv[j] = (int)(k + j);
                 ufmask |= 1u << u;
                 prev_uf = true;
             } else {
-                own = act && loc == d.wloc;
-                if (tid == 0) s_piv[j] = (int)(k + d.wi);
+                const int wi = s_wi;
+                own = act && loc == s_wloc;
+                if (tid == 0) s_piv[j] = (int)(k + wi);
                 prev_uf = false;
-                if (act && !own && pos == j) pos = d.wi;  // the interchange
+                if (act && !own && pos == j) pos = wi;  // the interchange
             }
             if (own) {
                 act = false;
@@ -1126,9 +1112,9 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
                 dstep = u;
                 if (block) send_step = u;
             }
-            if (!d.uf && act) {
+            if (!uf && act) {
                 // TMV scales the column by the reciprocal of the pivot
-                const T l = x[0] * d.rp;
+                const T l = x[0] * recip_rn(s_urow[u][0]);
                 x[0] = l;
                 if (u < kLast) x[1] = fma(-l, s_urow[u][1], x[1]);
                 if (u + 2 < kLeaf) {
@@ -1137,13 +1123,8 @@ lu_panel_leaf_kernel(T* __restrict__ A, int64_t lda, int64_t n, int64_t k, int n
                 }
             }
             leaf_rotate1<T, NB>(x);
-            return true;
-        };
-
-        bool ok = true;
-#pragma unroll 1
-        for (int u = 0; u < steps && ok; ++u) ok = column(u);
-        if (!ok) break;
+        }
+        if (s_abort) break;
         for (int r = steps; r < kLeaf; ++r) leaf_rotate1<T, NB>(x);  // back to column order
         if (block) {
             // 6. the leaf's end: the last pivot row out, the leaf's U12 (every
