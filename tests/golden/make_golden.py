@@ -3,12 +3,11 @@
 Runs the reference library compiled from the TMV sources (oracle/_ref, built
 by ``make -C oracle ref``) on the known-answer inputs of TMV's own tests and
 on seeded inputs, and stores inputs and TMV's outputs as compressed .npz
-files.  It needs the TMV source tree (default /root/reference, or
-$TMV_REFERENCE) because it reads the BIGN=100 system's data out of
-tests/TMV_TestMatrixDiv.cpp; the fixtures it writes are committed so that the
-tests run without it.
+files.  It needs the TMV source tree, given as $TMV_REFERENCE, because it
+reads the BIGN=100 system's data out of tests/TMV_TestMatrixDiv.cpp; the
+fixtures it writes are committed so that the tests run without it.
 
-    python tests/golden/make_golden.py
+    TMV_REFERENCE=<TMV 0.76 tree> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -28,7 +27,9 @@ sys.path.insert(0, str(ROOT / "tests"))
 import oracle  # noqa: E402
 from helpers import arith8_operands, tmv_decomp_matrix, tmv_square4  # noqa: E402
 
-REFERENCE = Path(os.environ.get("TMV_REFERENCE", "/root/reference"))
+if not os.environ.get("TMV_REFERENCE"):
+    sys.exit("make_golden.py: set TMV_REFERENCE to the TMV 0.76 source tree")
+REFERENCE = Path(os.environ["TMV_REFERENCE"])
 
 
 def sha(a: np.ndarray) -> str:

@@ -1,9 +1,9 @@
 // gemm_simt.cu -- FP64 (DFMA) and FP32 (FFMA) tiled products.
 //
-// GB300 executes FP64 at about 2 DFMA per SM per clock (measured 1.19
-// TFLOP/s for DFMA, 1.05 TFLOP/s for the m8n8k4 DMMA), so a register-tiled
-// DFMA kernel is the native FP64 engine: it keeps the FP64 pipe issuing every
-// cycle without needing the tensor path.  The FP32 variant (about 70 TFLOP/s
+// GB300 executes FP64 at about 2 DFMA per SM per clock (the library's DFMA
+// rate probe, tmvg_probe_fp64_rate, reads about 1.25 TFLOP/s at 2070 MHz),
+// so a register-tiled DFMA kernel is the native FP64 engine: it keeps the
+// FP64 pipe issuing every cycle without needing the tensor path.  The FP32 variant (about 70 TFLOP/s
 // FFMA) serves the mixed-precision trailing updates.
 //
 // Layouts: op(A)(i,k) is A[i + k*lda] (column-major) or A[i*lda + k]
