@@ -293,6 +293,50 @@ tmvg_status tmvg_lu_rdiveq_z64(tmvg_handle h, int64_t n, const double* LU, int64
  *           (src/TMV_LUInverse.cpp:236). */
 tmvg_status tmvg_lu_inverse_z64(tmvg_handle h, int64_t n, const double* LU, int64_t lda,
                                 const int64_t* P, double* Minv, int64_t ldm);
+/* Host-view variants of the four complex<double> entries above, as the
+ * link-time drop-in calls them: A, B and Minv are host views with TMV's
+ * (stepi, stepj) in complex elements (column- or row-major), LU is a
+ * column-major host matrix with leading dimension lda, P a host vector.
+ * Each copies its operands to the device, runs the entry above and copies
+ * the results back; synchronous, as TMV's calls are. */
+tmvg_status tmvg_lu_decompose_z64_host(tmvg_handle h, int64_t n, double* A, int64_t sAi,
+                                       int64_t sAj, int64_t* P);
+tmvg_status tmvg_lu_ldiveq_z64_host(tmvg_handle h, int64_t n, const double* LU, int64_t lda,
+                                    const int64_t* P, int64_t nrhs, double* B, int64_t sBi,
+                                    int64_t sBj);
+tmvg_status tmvg_lu_rdiveq_z64_host(tmvg_handle h, int64_t n, const double* LU, int64_t lda,
+                                    const int64_t* P, int64_t nrows, double* B, int64_t sBi,
+                                    int64_t sBj);
+tmvg_status tmvg_lu_inverse_z64_host(tmvg_handle h, int64_t n, const double* LU, int64_t lda,
+                                     const int64_t* P, double* Minv, int64_t msi, int64_t msj);
+
+/* ---- float: MultMM, LU_Decompose, LU_LDivEq / LU_RDivEq, LU_Inverse ----
+ * Host views (TMV's (stepi, stepj); LU column-major with lda), synchronous,
+ * with the conventions of the double entries: the product (FP32 FMA tiles)
+ * C (+)= alpha A B; the factorisation P A = L U with TMV's pivot rule on FP32
+ * values (its trailing updates are 3xTF32 tensor-core products, FP32-accurate
+ * but not FP32-rounded step by step); B := B / (P L U) and B (P L U)^-1 with
+ * TMVG_SINGULAR where TMV throws SingularUpperTriMatrix<float>; Minv :=
+ * (P L U)^-1.
+ * Replace: template void tmv::MultMM<add,float,float,float>
+ *          (src/TMV_MultMM.cpp:405-477), tmv::LU_Decompose<float>
+ *          (src/TMV_LUDecompose.cpp:514-559), tmv::LU_LDivEq / LU_RDivEq
+ *          <float,float> (src/TMV_LUDiv.cpp:186-226, 370-411) and
+ *          tmv::LU_Inverse<float,float> (src/TMV_LUInverse.cpp:236-299). */
+tmvg_status tmvg_multmm_f32_host(tmvg_handle h, int add, float alpha, int64_t m, int64_t n,
+                                 int64_t k, const float* A, int64_t sAi, int64_t sAj,
+                                 const float* B, int64_t sBi, int64_t sBj, float* C,
+                                 int64_t sCi, int64_t sCj);
+tmvg_status tmvg_lu_decompose_f32_host(tmvg_handle h, int64_t n, float* A, int64_t sAi,
+                                       int64_t sAj, int64_t* P);
+tmvg_status tmvg_lu_ldiveq_f32_host(tmvg_handle h, int64_t n, const float* LU, int64_t lda,
+                                    const int64_t* P, int64_t nrhs, float* B, int64_t sBi,
+                                    int64_t sBj);
+tmvg_status tmvg_lu_rdiveq_f32_host(tmvg_handle h, int64_t n, const float* LU, int64_t lda,
+                                    const int64_t* P, int64_t nrows, float* B, int64_t sBi,
+                                    int64_t sBj);
+tmvg_status tmvg_lu_inverse_f32_host(tmvg_handle h, int64_t n, const float* LU, int64_t lda,
+                                     const int64_t* P, float* Minv, int64_t msi, int64_t msj);
 /* det (re, im), logdet = sum log|U_jj| and sign (re, im) from the factors,
  * host outputs.  Replaces: LUDiv<std::complex<double> >::det / logDet
  * (src/TMV_LUD.cpp:132-156). */

@@ -7,7 +7,9 @@
 //   tmv_surface <dir>
 //     in:  <dir>/in.bin   int64 n, k, p, then column-major doubles
 //                         A (n x k), B (k x p), M (n x n), R (n x p),
-//                         W (p x n), b (n), S (n x n, singular)
+//                         W (p x n), b (n), S (n x n, singular), then
+//                         complex<double> (real, imaginary interleaved)
+//                         Mz (n x n), Rz (n x p), Wz (p x n)
 //     out: <dir>/<name>.bin for each result, <dir>/results.txt with one line
 //          "<name> ok" or "<name> throw <exception kind>" per step.
 //
@@ -17,9 +19,11 @@
 // C -= A*B; a product of strided views; m.divideUsing(tmv::LU), saveDiv,
 // X = R/m, x = b/m, Y = W%m, X /= m, det, logDet, inverse, isSingular, the LU
 // factors and pivots; the same solves on a row-major m (TMV's istrans path);
-// LU_Decompose of a tall and a wide matrix (include/tmv/TMV_LUD.h:79); and
-// the solve of a singular m, which must throw.
+// LU_Decompose of a tall and a wide matrix (include/tmv/TMV_LUD.h:79); the
+// solve of a singular m, which must throw; and the same product and LU
+// surface for tmv::Matrix<float> and tmv::Matrix<std::complex<double> >.
 #include <algorithm>
+#include <complex>
 #include <cstdint>
 #include <cstdio>
 #include <fstream>
@@ -51,6 +55,30 @@ void save_v(const std::string& name, const tmv::Vector<double>& x)
     std::vector<double> v(x.size());
     for (ptrdiff_t i = 0; i < (ptrdiff_t)x.size(); ++i) v[i] = x(i);
     save_vec(name, v);
+}
+
+template <class M>
+void save_z(const std::string& name, const M& m)
+{
+    std::vector<double> v;
+    for (ptrdiff_t j = 0; j < (ptrdiff_t)m.rowsize(); ++j)
+        for (ptrdiff_t i = 0; i < (ptrdiff_t)m.colsize(); ++i) {
+            const std::complex<double> z = m(i, j);
+            v.push_back(z.real());
+            v.push_back(z.imag());
+        }
+    std::ofstream f(g_dir + "/" + name + ".bin", std::ios::binary);
+    f.write(reinterpret_cast<const char*>(v.data()), v.size() * sizeof(double));
+}
+
+template <class M>
+void save_f(const std::string& name, const M& m)
+{
+    std::vector<double> v;
+    for (ptrdiff_t j = 0; j < (ptrdiff_t)m.rowsize(); ++j)
+        for (ptrdiff_t i = 0; i < (ptrdiff_t)m.colsize(); ++i) v.push_back((double)m(i, j));
+    std::ofstream f(g_dir + "/" + name + ".bin", std::ios::binary);
+    f.write(reinterpret_cast<const char*>(v.data()), v.size() * sizeof(double));
 }
 
 void save_vec(const std::string& name, const std::vector<double>& v)
@@ -98,6 +126,16 @@ int main(int argc, char** argv)
     };
     const tmv::Matrix<double> A = read(n, k), B = read(k, p), M = read(n, n), R = read(n, p),
                               W = read(p, n), bm = read(n, 1), S = read(n, n);
+    auto readz = [&](ptrdiff_t rows, ptrdiff_t cols) {
+        tmv::Matrix<std::complex<double> > m(rows, cols);
+        std::vector<double> v(2 * rows * cols);
+        in.read(reinterpret_cast<char*>(v.data()), v.size() * sizeof(double));
+        for (ptrdiff_t j = 0; j < cols; ++j)
+            for (ptrdiff_t i = 0; i < rows; ++i)
+                m(i, j) = std::complex<double>(v[2 * (i + j * rows)], v[2 * (i + j * rows) + 1]);
+        return m;
+    };
+    const tmv::Matrix<std::complex<double> > Mz = readz(n, n), Rz = readz(n, p), Wz = readz(p, n);
     if (!in) {
         std::fprintf(stderr, "short input\n");
         return 2;
@@ -182,5 +220,49 @@ int main(int argc, char** argv)
     s.divideUsing(tmv::LU);
     step("singular_ldiv", [&] { tmv::Vector<double> x = b / s; save_v("singular_ldiv", x); });
     step("singular_det", [&] { save_vec("singular_det", {s.det(), s.isSingular() ? 1.0 : 0.0}); });
+
+    // float: MultMM<float> and the LU surface on the same data, rounded
+    auto tofloat = [](const tmv::Matrix<double>& d) {
+        tmv::Matrix<float> f(d.colsize(), d.rowsize());
+        for (ptrdiff_t j = 0; j < (ptrdiff_t)d.rowsize(); ++j)
+            for (ptrdiff_t i = 0; i < (ptrdiff_t)d.colsize(); ++i) f(i, j) = (float)d(i, j);
+        return f;
+    };
+    const tmv::Matrix<float> Af = tofloat(A), Bf = tofloat(B), Mf = tofloat(M), Rf = tofloat(R),
+                             Wf = tofloat(W);
+    step("f_prod", [&] {
+        tmv::Matrix<float> C = Af * Bf;
+        C += 0.5f * Af * Bf;
+        save_f("f_prod", C);
+    });
+    tmv::Matrix<float> mf = Mf;
+    mf.divideUsing(tmv::LU);
+    mf.saveDiv();
+    step("f_ldiv", [&] { tmv::Matrix<float> X = Rf / mf; save_f("f_ldiv", X); });
+    step("f_rdiv", [&] { tmv::Matrix<float> Y = Wf % mf; save_f("f_rdiv", Y); });
+    step("f_inverse", [&] { tmv::Matrix<float> Mi = mf.inverse(); save_f("f_inverse", Mi); });
+    step("f_factors", [&] {
+        save_f("f_factors", mf.lud().getLU());
+        const ptrdiff_t* pv = mf.lud().getP().getValues();
+        save_vec("f_pivots", std::vector<double>(pv, pv + n));
+    });
+
+    // complex<double>: LU_Decompose, LU_LDivEq, LU_RDivEq, LU_Inverse, det
+    tmv::Matrix<std::complex<double> > mz = Mz;
+    mz.divideUsing(tmv::LU);
+    mz.saveDiv();
+    step("z_ldiv", [&] { tmv::Matrix<std::complex<double> > X = Rz / mz; save_z("z_ldiv", X); });
+    step("z_rdiv", [&] { tmv::Matrix<std::complex<double> > Y = Wz % mz; save_z("z_rdiv", Y); });
+    step("z_inverse", [&] { tmv::Matrix<std::complex<double> > Mi = mz.inverse(); save_z("z_inverse", Mi); });
+    step("z_factors", [&] {
+        save_z("z_factors", mz.lud().getLU());
+        const ptrdiff_t* pv = mz.lud().getP().getValues();
+        save_vec("z_pivots", std::vector<double>(pv, pv + n));
+        const std::complex<double> d = mz.det();
+        save_vec("z_det", {d.real(), d.imag()});
+    });
+    tmv::Matrix<std::complex<double>, tmv::RowMajor> mzr = Mz;
+    mzr.divideUsing(tmv::LU);
+    step("z_rm_ldiv", [&] { tmv::Matrix<std::complex<double> > X = Rz / mzr; save_z("z_rm_ldiv", X); });
     return 0;
 }

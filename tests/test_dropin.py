@@ -89,6 +89,10 @@ def test_surface_program_runs_on_stock_tmv(dropin, tmp_path):
     assert np.abs(C - A @ B).max() <= 1e-13 * np.abs(A @ B).max()
     for name, shape in T.result_shapes(n, k, p).items():  # every result has its size
         assert T.load(tmp_path, name, shape).shape == shape
+    for name, shape in T.float_shapes(n, k, p).items():
+        assert T.load(tmp_path, name, shape).shape == shape
+    for name, shape in T.complex_shapes(n, k, p).items():
+        assert T.load_z(tmp_path, name, shape).shape == shape
 
 
 def test_stock_tmv_wide_lu_differs_only_in_its_last_row(dropin, tmp_path):

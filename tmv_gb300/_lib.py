@@ -77,6 +77,16 @@ _SIGS = {
     "tmvg_lu_rdiveq_z64": (C.c_int, [vp, i64, vp, i64, vp, i64, vp, i64]),
     "tmvg_lu_inverse_z64": (C.c_int, [vp, i64, vp, i64, vp, vp, i64]),
     "tmvg_lu_det_z64": (C.c_int, [vp, i64, vp, i64, vp, vp, C.POINTER(dbl), vp]),
+    "tmvg_lu_decompose_z64_host": (C.c_int, [vp, i64, vp, i64, i64, vp]),
+    "tmvg_lu_ldiveq_z64_host": (C.c_int, [vp, i64, vp, i64, vp, i64, vp, i64, i64]),
+    "tmvg_lu_rdiveq_z64_host": (C.c_int, [vp, i64, vp, i64, vp, i64, vp, i64, i64]),
+    "tmvg_lu_inverse_z64_host": (C.c_int, [vp, i64, vp, i64, vp, vp, i64, i64]),
+    "tmvg_multmm_f32_host": (C.c_int, [vp, C.c_int, C.c_float, i64, i64, i64, vp, i64, i64, vp, i64,
+                                       i64, vp, i64, i64]),
+    "tmvg_lu_decompose_f32_host": (C.c_int, [vp, i64, vp, i64, i64, vp]),
+    "tmvg_lu_ldiveq_f32_host": (C.c_int, [vp, i64, vp, i64, vp, i64, vp, i64, i64]),
+    "tmvg_lu_rdiveq_f32_host": (C.c_int, [vp, i64, vp, i64, vp, i64, vp, i64, i64]),
+    "tmvg_lu_inverse_f32_host": (C.c_int, [vp, i64, vp, i64, vp, vp, i64, i64]),
     "tmvg_lu_rdiveq_f64": (C.c_int, [vp, i64, vp, i64, vp, i64, vp, i64]),
     "tmvg_lu_ldiveq_f64_host": (C.c_int, [vp, i64, vp, i64, vp, i64, vp, i64, i64]),
     "tmvg_lu_rdiveq_f64_host": (C.c_int, [vp, i64, vp, i64, vp, i64, vp, i64, i64]),

@@ -219,15 +219,16 @@ static tmvg_status transpose(Context* c, int64_t rows, int64_t cols, const T* in
 // Copy a strided host matrix (rows x cols, element (i,j) at p[i*si + j*sj])
 // into a dense column-major device buffer, and back.  Column- and row-major
 // host layouts move with one 2-D copy; anything else is packed on the host.
-static tmvg_status h2d_matrix(Context* c, double* dst, const double* src, int64_t rows,
-                              int64_t cols, int64_t si, int64_t sj, double* tmp_dev)
+template <typename T>
+static tmvg_status h2d_matrix(Context* c, T* dst, const T* src, int64_t rows, int64_t cols,
+                              int64_t si, int64_t sj, T* tmp_dev)
 {
     if (rows <= 0 || cols <= 0) return TMVG_OK;
     if (si == 1 || cols == 1) {
         const int64_t ld = cols == 1 ? rows : sj;
         return check_cuda(c,
-                          cudaMemcpy2DAsync(dst, rows * sizeof(double), src, ld * sizeof(double),
-                                            rows * sizeof(double), cols, cudaMemcpyHostToDevice,
+                          cudaMemcpy2DAsync(dst, rows * sizeof(T), src, ld * sizeof(T),
+                                            rows * sizeof(T), cols, cudaMemcpyHostToDevice,
                                             c->stream),
                           "h2d");
     }
@@ -235,38 +236,113 @@ static tmvg_status h2d_matrix(Context* c, double* dst, const double* src, int64_
         const int64_t ld = rows == 1 ? cols : si;
         tmvg_status st = check_cuda(
             c,
-            cudaMemcpy2DAsync(tmp_dev, cols * sizeof(double), src, ld * sizeof(double),
-                              cols * sizeof(double), rows, cudaMemcpyHostToDevice, c->stream),
+            cudaMemcpy2DAsync(tmp_dev, cols * sizeof(T), src, ld * sizeof(T),
+                              cols * sizeof(T), rows, cudaMemcpyHostToDevice, c->stream),
             "h2d");
         if (st) return st;
-        return transpose<double>(c, cols, rows, tmp_dev, cols, dst, rows);
+        return transpose<T>(c, cols, rows, tmp_dev, cols, dst, rows);
     }
     return set_error(c, TMVG_BAD_ARG, "host matrix must be column- or row-major");
 }
 
-static tmvg_status d2h_matrix(Context* c, double* dst, const double* src, int64_t rows,
-                              int64_t cols, int64_t si, int64_t sj, double* tmp_dev)
+template <typename T>
+static tmvg_status d2h_matrix(Context* c, T* dst, const T* src, int64_t rows, int64_t cols,
+                              int64_t si, int64_t sj, T* tmp_dev)
 {
     if (rows <= 0 || cols <= 0) return TMVG_OK;
     if (si == 1 || cols == 1) {
         const int64_t ld = cols == 1 ? rows : sj;
         return check_cuda(c,
-                          cudaMemcpy2DAsync(dst, ld * sizeof(double), src, rows * sizeof(double),
-                                            rows * sizeof(double), cols, cudaMemcpyDeviceToHost,
+                          cudaMemcpy2DAsync(dst, ld * sizeof(T), src, rows * sizeof(T),
+                                            rows * sizeof(T), cols, cudaMemcpyDeviceToHost,
                                             c->stream),
                           "d2h");
     }
     if (sj == 1 || rows == 1) {
         const int64_t ld = rows == 1 ? cols : si;
-        tmvg_status st = transpose<double>(c, rows, cols, src, rows, tmp_dev, cols);
+        tmvg_status st = transpose<T>(c, rows, cols, src, rows, tmp_dev, cols);
         if (st) return st;
         return check_cuda(c,
-                          cudaMemcpy2DAsync(dst, ld * sizeof(double), tmp_dev, cols * sizeof(double),
-                                            cols * sizeof(double), rows, cudaMemcpyDeviceToHost,
+                          cudaMemcpy2DAsync(dst, ld * sizeof(T), tmp_dev, cols * sizeof(T),
+                                            cols * sizeof(T), rows, cudaMemcpyDeviceToHost,
                                             c->stream),
                           "d2h");
     }
     return set_error(c, TMVG_BAD_ARG, "host matrix must be column- or row-major");
+}
+
+
+// ---- host-view entry points for float and complex<double> ---------------
+// The same transfers as the double ones: dense column-major device copies in
+// the context's arena, the device routine, the results back, synchronous.
+template <typename T, typename Factor>
+static tmvg_status lu_decompose_host(Context* c, int64_t n, T* A, int64_t sAi, int64_t sAj,
+                                     int64_t* P, Factor factor)
+{
+    if (n < 0) return set_error(c, TMVG_BAD_ARG, "lu: negative n");
+    if (n == 0) return TMVG_OK;
+    IoBufs io(c, {sizeof(T) * n * n, sizeof(T) * n * n, sizeof(int64_t) * n});
+    if (!io.ok) return set_error(c, TMVG_OOM, "lu: device buffers");
+    DevBuf &dA = io[0], &tmp = io[1], &dP = io[2];
+    tmvg_status st = h2d_matrix<T>(c, dA.as<T>(), A, n, n, sAi, sAj, tmp.as<T>());
+    if (!st) st = factor(dA.as<T>(), dP.as<int64_t>());
+    if (!st) st = d2h_matrix<T>(c, A, dA.as<T>(), n, n, sAi, sAj, tmp.as<T>());
+    if (!st)
+        st = check_cuda(c, cudaMemcpyAsync(P, dP.p, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, c->stream),
+                        "lu: pivots d2h");
+    if (!st) st = check_cuda(c, cudaStreamSynchronize(c->stream), "lu sync");
+    return st;
+}
+
+// B := B / (P L U) (left) or B (P L U)^-1 (right) on host views; Div(dLU,
+// dP, other, dB, ldb) runs the device solve.
+template <typename T, typename Div>
+static tmvg_status lu_div_host(Context* c, bool right, int64_t n, const T* LU, int64_t lda,
+                               const int64_t* P, int64_t other, T* B, int64_t sBi, int64_t sBj, Div div)
+{
+    if (n < 0 || other < 0 || lda < std::max<int64_t>(n, 1)) return set_error(c, TMVG_BAD_ARG, "div: bad sizes");
+    if (n == 0 || other == 0) return TMVG_OK;
+    const int64_t rows = right ? other : n, cols = right ? n : other;
+    IoBufs io(c, {sizeof(T) * n * n, sizeof(int64_t) * n, sizeof(T) * rows * cols, sizeof(T) * rows * cols});
+    if (!io.ok) return set_error(c, TMVG_OOM, "div: device buffers");
+    DevBuf &dLU = io[0], &dP = io[1], &dB = io[2], &tmp = io[3];
+    tmvg_status st = check_cuda(c,
+                                cudaMemcpy2DAsync(dLU.p, n * sizeof(T), LU, lda * sizeof(T), n * sizeof(T), n,
+                                                  cudaMemcpyHostToDevice, c->stream),
+                                "div: LU h2d");
+    if (!st)
+        st = check_cuda(c, cudaMemcpyAsync(dP.p, P, sizeof(int64_t) * n, cudaMemcpyHostToDevice, c->stream),
+                        "div: P h2d");
+    if (!st) st = h2d_matrix<T>(c, dB.as<T>(), B, rows, cols, sBi, sBj, tmp.as<T>());
+    if (!st) st = div(dLU.as<T>(), dP.as<int64_t>(), other, dB.as<T>(), rows);
+    if (st == TMVG_OK || st == TMVG_SINGULAR) {
+        tmvg_status st2 = d2h_matrix<T>(c, B, dB.as<T>(), rows, cols, sBi, sBj, tmp.as<T>());
+        if (!st2) st2 = check_cuda(c, cudaStreamSynchronize(c->stream), "div sync");
+        if (st2) return st2;
+    }
+    return st;
+}
+
+template <typename T, typename Inv>
+static tmvg_status lu_inverse_host(Context* c, int64_t n, const T* LU, int64_t lda, const int64_t* P,
+                                   T* Minv, int64_t msi, int64_t msj, Inv inv)
+{
+    if (n < 0 || lda < std::max<int64_t>(n, 1)) return set_error(c, TMVG_BAD_ARG, "inverse: bad sizes");
+    if (n == 0) return TMVG_OK;
+    IoBufs io(c, {sizeof(T) * n * n, sizeof(int64_t) * n, sizeof(T) * n * n, sizeof(T) * n * n});
+    if (!io.ok) return set_error(c, TMVG_OOM, "inverse: device buffers");
+    DevBuf &dLU = io[0], &dP = io[1], &dM = io[2], &tmp = io[3];
+    tmvg_status st = check_cuda(c,
+                                cudaMemcpy2DAsync(dLU.p, n * sizeof(T), LU, lda * sizeof(T), n * sizeof(T), n,
+                                                  cudaMemcpyHostToDevice, c->stream),
+                                "inverse: LU h2d");
+    if (!st)
+        st = check_cuda(c, cudaMemcpyAsync(dP.p, P, sizeof(int64_t) * n, cudaMemcpyHostToDevice, c->stream),
+                        "inverse: P h2d");
+    if (!st) st = inv(dLU.as<T>(), dP.as<int64_t>(), dM.as<T>());
+    if (!st) st = d2h_matrix<T>(c, Minv, dM.as<T>(), n, n, msi, msj, tmp.as<T>());
+    if (!st) st = check_cuda(c, cudaStreamSynchronize(c->stream), "inverse sync");
+    return st;
 }
 
 }  // namespace tmvg
@@ -831,6 +907,108 @@ tmvg_status tmvg_lu_inverse_z64(tmvg_handle h, int64_t n, const double* LU, int6
 {
     CTX_OR_BAIL(h);
     return zlu_inverse(c, n, reinterpret_cast<const double2*>(LU), lda, P, reinterpret_cast<double2*>(Minv), ldm);
+}
+
+
+tmvg_status tmvg_multmm_f32_host(tmvg_handle h, int add, float alpha, int64_t m, int64_t n, int64_t k,
+                                 const float* A, int64_t sAi, int64_t sAj, const float* B, int64_t sBi,
+                                 int64_t sBj, float* C, int64_t sCi, int64_t sCj)
+{
+    CTX_OR_BAIL(h);
+    if (m < 0 || n < 0 || k < 0) return set_error(c, TMVG_BAD_ARG, "multmm: negative size");
+    if (m == 0 || n == 0) return TMVG_OK;
+    IoBufs io(c, {sizeof(float) * m * k, sizeof(float) * k * n, sizeof(float) * m * n,
+                  sizeof(float) * std::max(std::max(m * k, k * n), m * n)});
+    if (!io.ok) return set_error(c, TMVG_OOM, "multmm: device buffers");
+    DevBuf &dA = io[0], &dB = io[1], &dC = io[2], &tmp = io[3];
+    tmvg_status st = h2d_matrix<float>(c, dA.as<float>(), A, m, k, sAi, sAj, tmp.as<float>());
+    if (!st) st = h2d_matrix<float>(c, dB.as<float>(), B, k, n, sBi, sBj, tmp.as<float>());
+    if (!st && add) st = h2d_matrix<float>(c, dC.as<float>(), C, m, n, sCi, sCj, tmp.as<float>());
+    if (!st)
+        st = gemm<float>(c, m, n, k, alpha, Mat<const float>{dA.as<float>(), 1, m},
+                         Mat<const float>{dB.as<float>(), 1, k}, add ? 1.0f : 0.0f, Mat<float>{dC.as<float>(), 1, m});
+    if (!st) st = d2h_matrix<float>(c, C, dC.as<float>(), m, n, sCi, sCj, tmp.as<float>());
+    if (!st) st = check_cuda(c, cudaStreamSynchronize(c->stream), "multmm sync");
+    return st;
+}
+
+tmvg_status tmvg_lu_decompose_f32_host(tmvg_handle h, int64_t n, float* A, int64_t sAi, int64_t sAj,
+                                       int64_t* P)
+{
+    CTX_OR_BAIL(h);
+    return lu_decompose_host<float>(c, n, A, sAi, sAj, P,
+                                    [&](float* dA, int64_t* dP) { return lu_factor<float>(c, n, dA, n, dP); });
+}
+
+tmvg_status tmvg_lu_ldiveq_f32_host(tmvg_handle h, int64_t n, const float* LU, int64_t lda, const int64_t* P,
+                                    int64_t nrhs, float* B, int64_t sBi, int64_t sBj)
+{
+    CTX_OR_BAIL(h);
+    return lu_div_host<float>(c, false, n, LU, lda, P, nrhs, B, sBi, sBj,
+                              [&](const float* dLU, const int64_t* dP, int64_t o, float* dB, int64_t ldb) {
+                                  return lu_ldiveq<float>(c, n, dLU, n, dP, o, dB, 1, ldb);
+                              });
+}
+
+tmvg_status tmvg_lu_rdiveq_f32_host(tmvg_handle h, int64_t n, const float* LU, int64_t lda, const int64_t* P,
+                                    int64_t nrows, float* B, int64_t sBi, int64_t sBj)
+{
+    CTX_OR_BAIL(h);
+    return lu_div_host<float>(c, true, n, LU, lda, P, nrows, B, sBi, sBj,
+                              [&](const float* dLU, const int64_t* dP, int64_t o, float* dB, int64_t ldb) {
+                                  return lu_rdiveq<float>(c, n, dLU, n, dP, o, dB, 1, ldb);
+                              });
+}
+
+tmvg_status tmvg_lu_inverse_f32_host(tmvg_handle h, int64_t n, const float* LU, int64_t lda, const int64_t* P,
+                                     float* Minv, int64_t msi, int64_t msj)
+{
+    CTX_OR_BAIL(h);
+    return lu_inverse_host<float>(c, n, LU, lda, P, Minv, msi, msj,
+                                  [&](const float* dLU, const int64_t* dP, float* dM) {
+                                      return lu_inverse<float>(c, n, dLU, n, dP, dM, n);
+                                  });
+}
+
+tmvg_status tmvg_lu_decompose_z64_host(tmvg_handle h, int64_t n, double* A, int64_t sAi, int64_t sAj,
+                                       int64_t* P)
+{
+    CTX_OR_BAIL(h);
+    return lu_decompose_host<double2>(c, n, reinterpret_cast<double2*>(A), sAi, sAj, P,
+                                      [&](double2* dA, int64_t* dP) { return zlu_factor(c, n, dA, n, dP); });
+}
+
+tmvg_status tmvg_lu_ldiveq_z64_host(tmvg_handle h, int64_t n, const double* LU, int64_t lda, const int64_t* P,
+                                    int64_t nrhs, double* B, int64_t sBi, int64_t sBj)
+{
+    CTX_OR_BAIL(h);
+    return lu_div_host<double2>(c, false, n, reinterpret_cast<const double2*>(LU), lda, P, nrhs,
+                                reinterpret_cast<double2*>(B), sBi, sBj,
+                                [&](const double2* dLU, const int64_t* dP, int64_t o, double2* dB, int64_t ldb) {
+                                    return zlu_ldiveq(c, n, dLU, n, dP, o, dB, ldb);
+                                });
+}
+
+tmvg_status tmvg_lu_rdiveq_z64_host(tmvg_handle h, int64_t n, const double* LU, int64_t lda, const int64_t* P,
+                                    int64_t nrows, double* B, int64_t sBi, int64_t sBj)
+{
+    CTX_OR_BAIL(h);
+    return lu_div_host<double2>(c, true, n, reinterpret_cast<const double2*>(LU), lda, P, nrows,
+                                reinterpret_cast<double2*>(B), sBi, sBj,
+                                [&](const double2* dLU, const int64_t* dP, int64_t o, double2* dB, int64_t ldb) {
+                                    return zlu_rdiveq(c, n, dLU, n, dP, o, dB, ldb);
+                                });
+}
+
+tmvg_status tmvg_lu_inverse_z64_host(tmvg_handle h, int64_t n, const double* LU, int64_t lda, const int64_t* P,
+                                     double* Minv, int64_t msi, int64_t msj)
+{
+    CTX_OR_BAIL(h);
+    return lu_inverse_host<double2>(c, n, reinterpret_cast<const double2*>(LU), lda, P,
+                                    reinterpret_cast<double2*>(Minv), msi, msj,
+                                    [&](const double2* dLU, const int64_t* dP, double2* dM) {
+                                        return zlu_inverse(c, n, dLU, n, dP, dM, n);
+                                    });
 }
 
 tmvg_status tmvg_lu_det_z64(tmvg_handle h, int64_t n, const double* LU, int64_t lda, const int64_t* P,

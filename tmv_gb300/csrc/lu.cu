@@ -2515,6 +2515,10 @@ template tmvg_status tri_ldiveq<double>(Context*, int64_t, const double*, int64_
                                         int64_t, double*, int64_t, int64_t);
 template tmvg_status lu_inverse_ata<double>(Context*, int64_t, const double*, int64_t, double*, int64_t);
 template tmvg_status lu_factor<float>(Context*, int64_t, float*, int64_t, int64_t*);
+template tmvg_status lu_inverse<float>(Context*, int64_t, const float*, int64_t, const int64_t*, float*,
+                                       int64_t);
+template tmvg_status lu_rdiveq<float>(Context*, int64_t, const float*, int64_t, const int64_t*,
+                                      int64_t, float*, int64_t, int64_t);
 template tmvg_status tri_solve<double>(Context*, int64_t, const double*, int64_t, int64_t, bool,
                                        bool, int64_t, double*, int64_t, int64_t, bool);
 template tmvg_status tri_solve<float>(Context*, int64_t, const float*, int64_t, int64_t, bool,
