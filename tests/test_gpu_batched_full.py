@@ -67,7 +67,7 @@ def test_full_batch_fp64_pivots_and_solutions(dev, orc, full):
     p_off = np.concatenate([[0], np.cumsum(n)[:-1]])
     for s in range(COUNT):
         ns = int(n[s])
-        lu = np.asfortranarray(A[a_off[s]:a_off[s] + ns * ns].reshape(ns, ns, order="F"))
+        lu = A[a_off[s]:a_off[s] + ns * ns].reshape(ns, ns, order="F").copy(order="F")
         p_o = orc.lu_decompose(lu)
         assert np.array_equal(Pg[p_off[s]:p_off[s] + ns], p_o), s
 
