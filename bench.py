@@ -553,14 +553,15 @@ def batched_bench(dev, args, with_cpu: bool) -> dict:
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic
 # byte of each kernel class, from one ncu capture of the class's main kernel
 # on the n = 8192 workload (commands and figures in profiles/):
-#   panel: lu_panel_cluster_reg2_kernel, k = 256: 2.19 MB / 4.06 MB
+#   panel: lu_panel_leaf_kernel, k = 320: 2.08 MB / 4.03 MB
 #   trailing_update: tf32x3_update_kernel, k = 256: 432.1 MB / 495.7 MB
 #   tri_solve: trsv_pub_kernel: 139.6 MB / 138.5 MB
 # The traffic of a span is its algorithmic bytes times the ratio.
-NCU_TRAFFIC_PER_ALG_BYTE: dict = {"panel": 0.540, "trailing_update": 0.872, "tri_solve": 1.008}
+NCU_TRAFFIC_PER_ALG_BYTE: dict = {"panel": 0.516, "trailing_update": 0.872, "tri_solve": 1.008}
 
 KERNEL_NAMES = {
-    "panel": "lu_panel_cluster_reg2_kernel (16-CTA cluster, two register-resident FP32 panel rows per thread)",
+    "panel": "lu_panel_leaf_kernel (16-CTA cluster, 512 threads, one register-resident FP32 panel row "
+             "per thread, 8-column leaves)",
     "trailing_update": "U12 solve + A22 -= L21 U12 (FP32: u12_reg_kernel + tf32x3_update_kernel "
                        "on tcgen05; FP64: u12_reg_kernel + gemm_simt_kernel<double>)",
     "tri_solve": "trsv_pub_kernel (FP32 inverse-block triangular solve)",
@@ -653,17 +654,20 @@ def e2e_host(args, Acm, B, n, nrhs, mixed=False) -> dict:
             h.check(h.call("tmvg_divide_f64_host", n, C.c_void_p(hA.data_ptr()), nrhs,
                            C.c_void_p(hB.data_ptr()), C.c_void_p(hX.data_ptr()), None, None))
     call()
-    steps = max(1, min(args.steps, 5))
+    steps = max(3, min(args.steps, 7))
     per_call = []
     t0 = time.perf_counter()
     for _ in range(steps):
         t1 = time.perf_counter()
         call()  # synchronous: returns after X is back in host memory
         per_call.append((time.perf_counter() - t1) * 1e3)
-    dt = (time.perf_counter() - t0) / steps
+    # the median call: one synchronous call is one step, and a host-side
+    # stall in one call (seen as a single 4x outlier) says nothing of the path
+    dt = float(np.median(per_call)) * 1e-3
     return {"value": round(lu_solve_flops(n, nrhs) / dt / 1e12, 4), "unit": "TFLOP/s",
             "h2d_bytes_per_step": 8 * n * n + 8 * n * nrhs, "d2h_bytes_per_step": 8 * n * nrhs,
-            "ms_per_step": round(dt * 1e3, 3), "steps": steps,
+            "ms_per_step": round(dt * 1e3, 3), "steps": steps, "statistic": "median call",
+            "ms_mean": round((time.perf_counter() - t0) / steps * 1e3, 3),
             "ms_per_call": [round(t, 3) for t in per_call]}
 
 
@@ -829,7 +833,7 @@ def main():
     ap.add_argument("--no-sweep", action="store_true",
                     help="skip the condition-number / equal-accuracy sweep")
     ap.add_argument("--batch-count", type=int, default=20000)
-    ap.add_argument("--batch-cpu-sample", type=int, default=2000)
+    ap.add_argument("--batch-cpu-sample", type=int, default=20000)
     ap.add_argument("--no-extras", action="store_true",
                     help="time the step only (no FP64 comparison, e2e, roofline or CPU leg)")
     args = ap.parse_args()
