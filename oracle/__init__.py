@@ -202,6 +202,36 @@ class _Backend:
         f(cnt, _p(n), _p(nrhs), _p(a_off), _p(b_off), _p(A), _p(B), _p(st))
         return st
 
+    # band LU: TMV's column-major band storage, element (i,j) at ab[i + j*ldab]
+    def band_lu_decompose(self, ab: np.ndarray, n: int, lo: int, hi: int, ldab: int,
+                          algo: int = 0) -> np.ndarray:
+        """LU_Decompose of the band matrix in the float64 buffer ab (in place,
+        (0,0) at ab[0]); algo 0 is TMV's general band algorithm, 1 its
+        tridiagonal one.  Returns P (int64)."""
+        assert ab.dtype == np.float64 and ab.flags.c_contiguous
+        P = np.zeros(max(n, 0), dtype=np.int64)
+        f = self._f("band_lu_decompose", C.c_int, [i64, i64, i64, C.c_int, vp, i64, vp])
+        rc = f(n, lo, hi, algo, _p(ab), ldab, _p(P))
+        if rc:
+            raise RuntimeError(f"band_lu_decompose rc={rc}")
+        return P
+
+    def band_lu_ldiveq(self, lu: np.ndarray, n: int, lo: int, hi: int, ldab: int, P: np.ndarray,
+                       B: np.ndarray, algo: int = 0, ldb: int | None = None) -> None:
+        """B (n x nrhs, column-major in a flat or Fortran-order float64 array)
+        := (P L U)^-1 B in place from band factors."""
+        assert B.dtype == np.float64
+        nrhs = 1 if B.ndim == 1 else B.shape[1]
+        if ldb is None:
+            ldb = n if B.ndim == 1 else B.strides[1] // 8
+        f = self._f("band_lu_ldiveq", C.c_int, [i64, i64, i64, C.c_int, vp, i64, vp, i64, vp, i64])
+        rc = f(n, lo, hi, algo, _p(lu), ldab, _p(np.ascontiguousarray(P, dtype=np.int64)), nrhs,
+               _p(B), ldb)
+        if rc == SINGULAR:
+            raise OracleSingular("singular")
+        if rc:
+            raise RuntimeError(f"band_lu_ldiveq rc={rc}")
+
     def set_threads(self, t: int) -> None:
         self._f("set_threads", None, [C.c_int])(t)
 

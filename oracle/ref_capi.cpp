@@ -18,6 +18,11 @@
 //   tmvref_rdivide       X = B % m (LUDiv::doRDiv, src/TMV_LUD.cpp:122-130)
 //   tmvref_det           m.det(), m.logDet(&s) (src/TMV_LUD.cpp:132-190)
 //   tmvref_batched_divide  one B_i/A_i per system, OpenMP over systems.
+//   tmvref_band_lu_decompose, tmvref_band_lu_ldiveq
+//                        LU_Decompose(BandMatrixView<T>, ptrdiff_t*, ptrdiff_t)
+//                        (src/TMV_BandLUDecompose.cpp:383) and LU_LDivEq on band
+//                        factors (src/TMV_BandLUDiv.cpp:139) over TMV's
+//                        column-major band storage.
 //   tmvref_lu_decompose_z, tmvref_lu_ldiveq_z, tmvref_lu_rdiveq_z, tmvref_det_z,
 //   tmvref_inverse_z, tmvref_multmm_z
 //                        the same for std::complex<double> (column-major,
@@ -26,8 +31,11 @@
 // Status: 0 ok, 1 tmv::Singular thrown, 2 other tmv::Error, 3 other exception.
 
 #include "TMV.h"
+#include "TMV_Band.h"
+#include "TMV_BandLUDiv.h"
 #include "TMV_LUDiv.h"
 #include <omp.h>
+#include <algorithm>
 #include <cstring>
 
 namespace {
@@ -129,6 +137,68 @@ int tmvref_det_z(ptrdiff_t n, const double* A, double* det, double* logdet, doub
         det[1] = d.imag();
         sign[0] = s.real();
         sign[1] = s.imag();
+    });
+}
+
+// Band LU over TMV's column-major band storage: element (i,j) at a[i + j*ldab]
+// for j-hu <= i <= j+lo, hu = min(lo+hi, n-1).  The fill diagonals hi+1..hu
+// are zeroed first, as BandLUDiv's copy of A into its wider band leaves them.
+// algo 0 factors the column-major view (NonLapBandLU_Decompose); algo 1
+// (lo = hi = 1) copies the matrix into the diagonal-major storage BandLUDiv
+// gives a tridiagonal matrix, so that TMV runs NonLapTriDiagLU_Decompose and
+// the row-oriented upper solve, and copies the factors back.
+static void band_zero_fill(ptrdiff_t n, ptrdiff_t hi, ptrdiff_t hu, double* a, ptrdiff_t ldab)
+{
+    for (ptrdiff_t j = 0; j < n; ++j)
+        for (ptrdiff_t d = hi + 1; d <= hu; ++d)
+            if (j - d >= 0) a[(j - d) + j * ldab] = 0.0;
+}
+
+static void band_to_dm(ptrdiff_t n, ptrdiff_t hu, const double* a, ptrdiff_t ldab,
+                       tmv::BandMatrix<double, tmv::DiagMajor>& D)
+{
+    for (ptrdiff_t j = 0; j < n; ++j)
+        for (ptrdiff_t i = std::max<ptrdiff_t>(0, j - hu); i <= std::min(n - 1, j + 1); ++i)
+            D(i, j) = a[i + j * ldab];
+}
+
+int tmvref_band_lu_decompose(ptrdiff_t n, ptrdiff_t lo, ptrdiff_t hi, int algo, double* a,
+                             ptrdiff_t ldab, ptrdiff_t* P)
+{
+    return guarded([&] {
+        if (n == 0) return;
+        const ptrdiff_t hu = std::min(lo + hi, n - 1);
+        band_zero_fill(n, hi, hu, a, ldab);
+        if (algo == 1) {
+            tmv::BandMatrix<double, tmv::DiagMajor> D(n, n, 1, hu, 0.0);
+            band_to_dm(n, hu, a, ldab, D);
+            tmv::LU_Decompose(D.view(), P, hi);
+            for (ptrdiff_t j = 0; j < n; ++j)
+                for (ptrdiff_t i = std::max<ptrdiff_t>(0, j - hu); i <= std::min(n - 1, j + 1); ++i)
+                    a[i + j * ldab] = D(i, j);
+            return;
+        }
+        tmv::BandMatrixView<double> A(a, n, n, lo, hu, 1, ldab, ldab + 1, tmv::NonConj);
+        tmv::LU_Decompose(A, P, hi);
+    });
+}
+
+int tmvref_band_lu_ldiveq(ptrdiff_t n, ptrdiff_t lo, ptrdiff_t hi, int algo, const double* lu,
+                          ptrdiff_t ldab, const ptrdiff_t* P, ptrdiff_t nrhs, double* B,
+                          ptrdiff_t ldb)
+{
+    return guarded([&] {
+        if (n == 0 || nrhs == 0) return;
+        const ptrdiff_t hu = std::min(lo + hi, n - 1);
+        tmv::MatrixView<double> Bv = tmv::MatrixViewOf(B, n, nrhs, 1, ldb);
+        if (algo == 1) {
+            tmv::BandMatrix<double, tmv::DiagMajor> D(n, n, 1, hu, 0.0);
+            band_to_dm(n, hu, lu, ldab, D);
+            tmv::LU_LDivEq(D, P, Bv);
+            return;
+        }
+        tmv::ConstBandMatrixView<double> LU(lu, n, n, lo, hu, 1, ldab, ldab + 1, tmv::NonConj);
+        tmv::LU_LDivEq(LU, P, Bv);
     });
 }
 

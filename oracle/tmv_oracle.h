@@ -88,6 +88,20 @@ int oracle_batched_divide(ptrdiff_t count, const ptrdiff_t* n,
                           const ptrdiff_t* b_off, const double* A, double* B,
                           int* status);
 
+/* Band LU (tmv_oracle_band.c): TMV's column-major band storage, element
+ * (i,j) at a[i + j*ldab] for j-hu <= i <= j+lo, hu = min(lo+hi, n-1)
+ * superdiagonals (the interchanges fill them; ldab >= lo + hu).
+ * LU_Decompose(BandMatrixView) in place, P[0..n); and LU_LDivEq on the
+ * factors for B (n x nrhs, leading dimension ldb).  algo picks TMV's general
+ * band algorithm or its tridiagonal one (lo = hi = 1). */
+#define ORACLE_BAND_GENERAL 0
+#define ORACLE_BAND_TRIDIAG 1
+int oracle_band_lu_decompose(ptrdiff_t n, ptrdiff_t lo, ptrdiff_t hi, int algo, double* a,
+                             ptrdiff_t ldab, ptrdiff_t* P);
+int oracle_band_lu_ldiveq(ptrdiff_t n, ptrdiff_t lo, ptrdiff_t hi, int algo, const double* lu,
+                          ptrdiff_t ldab, const ptrdiff_t* P, ptrdiff_t nrhs, double* B,
+                          ptrdiff_t ldb);
+
 /* complex<double> (tmv_oracle_z.c): column-major, entries interleaved
  * (re, im), leading dimensions in complex elements. */
 int oracle_lu_decompose_z(ptrdiff_t n, double* A, ptrdiff_t lda, ptrdiff_t* P);

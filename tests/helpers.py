@@ -74,3 +74,60 @@ def diag_shift_matrix(rng, n: int, shift: float) -> np.ndarray:
     a = rng.standard_normal((n, n))
     a[np.arange(n), np.arange(n)] += shift
     return a
+
+
+# --- band storage -----------------------------------------------------------
+# TMV's column-major band layout: element (i,j) of an n x n band matrix at
+# ab[i + j*ldab] from the (0,0) slot, for j-hu <= i <= j+lo; a batch puts
+# system s at ab[s*sab + ...].
+
+def band_hu(n: int, lo: int, hi: int) -> int:
+    return min(lo + hi, n - 1) if n > 0 else 0
+
+
+def band_len(n: int, ldab: int) -> int:
+    """Slots from (0,0) to (n-1,n-1), inclusive."""
+    return (n - 1) * (ldab + 1) + 1 if n > 0 else 0
+
+
+def band_pack(a: np.ndarray, lo: int, hi: int, ldab: int, out: np.ndarray | None = None,
+              fill: float = 0.0) -> np.ndarray:
+    """The band of the dense a (entries outside -lo..hi ignored) in band
+    storage; the fill diagonals hi+1..hu and any gap slots hold `fill`."""
+    n = a.shape[0]
+    hu = band_hu(n, lo, hi)
+    ab = np.full(band_len(n, ldab), fill) if out is None else out
+    for j in range(n):
+        for i in range(max(0, j - hi), min(n, j + lo + 1)):
+            ab[i + j * ldab] = a[i, j]
+    return ab
+
+
+def band_unpack(ab: np.ndarray, n: int, lo: int, hu: int, ldab: int) -> np.ndarray:
+    a = np.zeros((n, n))
+    for j in range(n):
+        for i in range(max(0, j - hu), min(n, j + lo + 1)):
+            a[i, j] = ab[i + j * ldab]
+    return a
+
+
+def band_matrix(rng, n: int, lo: int, hi: int, kind: str = "normal") -> np.ndarray:
+    """A dense n x n matrix with lo subdiagonals and hi superdiagonals.
+    kind: normal (N(0,1)), int (integers in -2..2: exact zeros, ties and unit
+    pivots), dom (N(0,1) + (lo+hi+1) on the diagonal), tiny (normal with
+    subnormal columns that take TMV's underflow branch)."""
+    if kind == "int":
+        a = rng.integers(-2, 3, size=(n, n)).astype(np.float64)
+    else:
+        a = rng.standard_normal((n, n))
+    if kind == "dom":
+        a += (lo + hi + 1) * np.eye(n)
+    if kind == "tiny" and n > 2:
+        for j in rng.choice(n - 1, size=max(1, n // 8), replace=False):
+            a[:, j] *= 1e-310
+    return np.triu(np.tril(a, hi), -lo)
+
+
+def bits(x: np.ndarray) -> np.ndarray:
+    """Bit patterns, so that equality also sees signed zeros and NaNs."""
+    return np.ascontiguousarray(x, dtype=np.float64).view(np.int64)
