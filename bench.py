@@ -752,6 +752,86 @@ def other_workloads(dev, with_cpu: bool) -> dict:
         "workload": "X = A^-1 B (n = 2048, 64 right-hand sides), backward gB = A^-T G and gA = -gB X^T "
                     "from the stored factors"}
     del flush
+    out["band_lu_65536x1024"] = band_workloads(dev, with_cpu)
+    return out
+
+
+def band_workloads(dev, with_cpu: bool) -> dict:
+    """The batched band LU (x = b / A per system, TMV's LU_Decompose and
+    LU_LDivEq on band storage, one thread per system): 65536 systems of
+    n = 1024 with one right-hand side, entries N(0,1) with lo + hi + 2 added to
+    the diagonal, seeded; tridiagonal (lo = hi = 1, TMV's tridiagonal
+    algorithm) and pentadiagonal (lo = hi = 2, the general algorithm).  The
+    factorisation is in place, so every timed launch gets a fresh copy of the
+    inputs (copied before its events); the band and right-hand sides (2.1 and
+    3.8 GB) exceed L2.  Rooflines: the FP64 pipe, counting one pipe slot per
+    product, difference and reciprocal (division) -- half the DFMA TFLOP/s
+    rate in operations -- and HBM for the bytes read and written once."""
+    import torch
+
+    from tmv_gb300.band import band_layout, band_lu_solve, band_lu_solve_count
+
+    count, n = 65536, 1024
+    stream = torch.cuda.current_stream(dev)
+    hbm = peaks()["hbm_gbs"]
+    out = {}
+    for lo, hi, algo in [(1, 1, "tridiag"), (2, 2, "general")]:
+        lay = band_layout(n, lo, hi)
+        g = torch.Generator(device=dev).manual_seed(11)
+        ab0 = torch.randn(count * lay.stride_ab, dtype=torch.float64, device=dev, generator=g)
+        i = torch.arange(n, device=dev)
+        ab0.view(count, lay.stride_ab)[:, i * (lay.ldab + 1)] += lo + hi + 2.0
+        b0 = torch.randn(count * n, dtype=torch.float64, device=dev, generator=g)
+        ab, X = torch.empty_like(ab0), torch.empty_like(b0)
+        P = torch.empty(count * n, dtype=torch.int64, device=dev)
+        st = torch.empty(count, dtype=torch.int32, device=dev)
+        times = []
+        for rep in range(6):
+            ab.copy_(ab0)
+            X.copy_(b0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            band_lu_solve(ab, count, lay, X, 1, algo=algo, P=P, status=st)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if rep >= 2:
+                times.append(e0.elapsed_time(e1))
+        ms = float(np.median(times))
+        assert int(st.abs().sum().item()) == 0
+        work = band_lu_solve_count(count, lay, 1)
+        ops = work["flops"] / (ms * 1e-3) / 1e12  # T operations / s
+        pipe = FP64_PEAK["tflops"] / 2 if FP64_PEAK["tflops"] else None
+        gbs = work["bytes"] / (ms * 1e-3) / 1e9
+        key = f"{'tridiag' if algo == 'tridiag' else 'general'}_lo{lo}_hi{hi}"
+        out[key] = {
+            "value": round(count / (ms * 1e-3), 1), "unit": "systems/s", "ms": round(ms, 4),
+            "kernel": f"band_lu_kernel<{lo},{2 * lo},{'true' if algo == 'tridiag' else 'false'}>",
+            "fp64_ops_per_launch": work["flops"], "bytes_per_launch": work["bytes"],
+            "roofline_fp64_pipe": {"bound": "fp64", "achieved": round(ops, 4), "unit": "Top/s",
+                                   "peak": round(pipe, 4) if pipe else None,
+                                   "frac": round(ops / pipe, 4) if pipe else None,
+                                   "peak_source": "DFMA rate / 2 (one pipe slot per op)"},
+            "roofline_hbm": {"bound": "hbm", "achieved": round(gbs, 1), "peak": hbm, "unit": "GB/s",
+                             "frac": round(gbs / hbm, 4)},
+            "workload": f"{count} systems, n = {n}, lo = {lo}, hi = {hi}, 1 right-hand side, "
+                        f"algorithm {algo}"}
+        if with_cpu:
+            orc, kind, what = cpu_reference()
+            cores = os.cpu_count() or 1
+            orc.set_threads(cores)
+            sample = count  # the whole batch: about a second on 16 cores
+            hab = ab0[:sample * lay.stride_ab].cpu().numpy().copy()
+            hb = b0[:sample * n].cpu().numpy().copy()
+            t0 = time.perf_counter()
+            Ph, sth = orc.band_batched_solve(sample, n, lo, hi, 1 if algo == "tridiag" else 0, hab,
+                                             lay.ldab, lay.stride_ab, 1, hb, n, n)
+            dt = time.perf_counter() - t0
+            ok = bool(np.array_equal(hb.view(np.int64), X[:sample * n].cpu().numpy().view(np.int64)))
+            out[key]["cpu_baseline"] = {
+                "value": round(sample / dt, 1), "unit": "systems/s", "cores": cores, "kind": kind,
+                "sample": f"all {sample} systems ({dt:.2f} s, OpenMP over systems); {what}",
+                "solutions_bitwise_equal_gpu": ok}
+        del ab0, b0, ab, X, P, st
     return out
 
 

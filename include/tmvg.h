@@ -433,6 +433,53 @@ tmvg_status tmvg_batched_lu_solve_mixed_f64(tmvg_batch_plan plan, const double* 
                                             int32_t* iters, double* berr);
 tmvg_status tmvg_batch_plan_destroy(tmvg_batch_plan plan);
 
+/* ---------------------------------------------------------------------
+ * Batched band LU: count n x n band systems of one shape (lo subdiagonals,
+ * hi superdiagonals), one GPU thread per system.  Replaces, per system,
+ * tmv::LU_Decompose(BandMatrixView<double>, ptrdiff_t* P, ptrdiff_t Anhi)
+ * (include/tmv/TMV_BandLUD.h:61, src/TMV_BandLUDecompose.cpp:383-425) and
+ * tmv::LU_LDivEq(const GenBandMatrix<double>&, const ptrdiff_t*,
+ * MatrixView<double>) (src/TMV_BandLUDiv.h:52, src/TMV_BandLUDiv.cpp:811),
+ * the two steps of BandLUDiv (x = b / A for a tmv::BandMatrix); results are
+ * TMV's bit for bit.
+ *
+ * Storage is TMV's column-major band layout: system s's element (i,j) at
+ * AB[s*stride_ab + i + j*ldab] for j-hu <= i <= j+lo, hu = min(lo+hi, n-1)
+ * (the superdiagonals the interchanges fill), ldab >= lo + hu, stride_ab >=
+ * (n-1)(ldab+1)+1.  The factors replace A in those slots (the fill diagonals
+ * hi+1..hu are written, never read); P[s*stride_p + j] receives the row
+ * interchanged with row j (TMV's ptrdiff_t P).  B is n x nrhs column-major
+ * per system at B[s*stride_b + i + q*ldb], ldb >= n.
+ *
+ * algo: TMVG_BAND_GENERAL, TMV's general band algorithm (the column-major
+ * BandMatrixView above), or TMVG_BAND_TRIDIAG (lo == hi == 1), the
+ * tridiagonal algorithm BandLUDiv runs on its diagonal-major copy of a
+ * tridiagonal matrix (src/TMV_BandLUDecompose.cpp:144-200,
+ * src/TMV_BandTriDiv_V.cpp:63-135), here on the same column-major storage.
+ *
+ * status[s] (solves): 0; 1 a zero U(j,j) met where TMV throws
+ * SingularBandLU (B then holds a partial result); 2 an interchange P[j]
+ * outside rows j..min(j+lo, n-1), not applied (factors not made by this
+ * factorisation).  Device pointers, stream-ordered on the handle's stream;
+ * no synchronisation.
+ * --------------------------------------------------------------------- */
+#define TMVG_BAND_GENERAL 0
+#define TMVG_BAND_TRIDIAG 1
+tmvg_status tmvg_band_lu_decompose_batched_f64(tmvg_handle h, int64_t count, int64_t n, int64_t lo,
+                                               int64_t hi, int algo, double* AB, int64_t ldab,
+                                               int64_t stride_ab, int64_t* P, int64_t stride_p);
+tmvg_status tmvg_band_lu_ldiveq_batched_f64(tmvg_handle h, int64_t count, int64_t n, int64_t lo,
+                                            int64_t hi, int algo, const double* AB, int64_t ldab,
+                                            int64_t stride_ab, const int64_t* P, int64_t stride_p,
+                                            int64_t nrhs, double* B, int64_t ldb, int64_t stride_b,
+                                            int32_t* status);
+/* Both in one launch (the factors and P are written as by the decompose). */
+tmvg_status tmvg_band_lu_solve_batched_f64(tmvg_handle h, int64_t count, int64_t n, int64_t lo,
+                                           int64_t hi, int algo, double* AB, int64_t ldab,
+                                           int64_t stride_ab, int64_t* P, int64_t stride_p,
+                                           int64_t nrhs, double* B, int64_t ldb, int64_t stride_b,
+                                           int32_t* status);
+
 #if defined(__GNUC__)
 #pragma GCC visibility pop
 #endif

@@ -232,6 +232,17 @@ class _Backend:
         if rc:
             raise RuntimeError(f"band_lu_ldiveq rc={rc}")
 
+    def band_batched_solve(self, count: int, n: int, lo: int, hi: int, algo: int, ab: np.ndarray,
+                           ldab: int, sab: int, nrhs: int, B: np.ndarray, ldb: int, sb: int):
+        """The batched band workload in place on the host cores (OpenMP over
+        systems); returns (P, status)."""
+        P = np.zeros(count * max(n, 1), dtype=np.int64)
+        st = np.zeros(count, dtype=np.int32)
+        f = self._f("band_batched_solve", C.c_int, [i64, i64, i64, i64, C.c_int, vp, i64, i64, vp,
+                                                    i64, i64, vp, i64, i64, vp])
+        f(count, n, lo, hi, algo, _p(ab), ldab, sab, _p(P), max(n, 1), nrhs, _p(B), ldb, sb, _p(st))
+        return P, st
+
     def set_threads(self, t: int) -> None:
         self._f("set_threads", None, [C.c_int])(t)
 

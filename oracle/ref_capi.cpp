@@ -22,7 +22,8 @@
 //                        LU_Decompose(BandMatrixView<T>, ptrdiff_t*, ptrdiff_t)
 //                        (src/TMV_BandLUDecompose.cpp:383) and LU_LDivEq on band
 //                        factors (src/TMV_BandLUDiv.cpp:139) over TMV's
-//                        column-major band storage.
+//                        column-major band storage; tmvref_band_batched_solve
+//                        both over a batch, OpenMP over systems.
 //   tmvref_lu_decompose_z, tmvref_lu_ldiveq_z, tmvref_lu_rdiveq_z, tmvref_det_z,
 //   tmvref_inverse_z, tmvref_multmm_z
 //                        the same for std::complex<double> (column-major,
@@ -200,6 +201,21 @@ int tmvref_band_lu_ldiveq(ptrdiff_t n, ptrdiff_t lo, ptrdiff_t hi, int algo, con
         tmv::ConstBandMatrixView<double> LU(lu, n, n, lo, hu, 1, ldab, ldab + 1, tmv::NonConj);
         tmv::LU_LDivEq(LU, P, Bv);
     });
+}
+
+// The batched band workload through TMV, OpenMP over systems.
+int tmvref_band_batched_solve(ptrdiff_t count, ptrdiff_t n, ptrdiff_t lo, ptrdiff_t hi, int algo,
+                              double* ab, ptrdiff_t ldab, ptrdiff_t sab, ptrdiff_t* P, ptrdiff_t sp,
+                              ptrdiff_t nrhs, double* B, ptrdiff_t ldb, ptrdiff_t sb, int* status)
+{
+#pragma omp parallel for schedule(static)
+    for (ptrdiff_t s = 0; s < count; ++s) {
+        int rc = tmvref_band_lu_decompose(n, lo, hi, algo, ab + s * sab, ldab, P + s * sp);
+        if (rc == 0)
+            rc = tmvref_band_lu_ldiveq(n, lo, hi, algo, ab + s * sab, ldab, P + s * sp, nrhs, B + s * sb, ldb);
+        status[s] = rc;
+    }
+    return 0;
 }
 
 int tmvref_lu_ldiveq(ptrdiff_t n, const double* LU, ptrdiff_t lda,

@@ -101,6 +101,11 @@ int oracle_band_lu_decompose(ptrdiff_t n, ptrdiff_t lo, ptrdiff_t hi, int algo, 
 int oracle_band_lu_ldiveq(ptrdiff_t n, ptrdiff_t lo, ptrdiff_t hi, int algo, const double* lu,
                           ptrdiff_t ldab, const ptrdiff_t* P, ptrdiff_t nrhs, double* B,
                           ptrdiff_t ldb);
+/* count systems of one shape, OpenMP over systems (system s at ab + s*sab,
+ * P + s*sp, B + s*sb); status[s] per system. */
+int oracle_band_batched_solve(ptrdiff_t count, ptrdiff_t n, ptrdiff_t lo, ptrdiff_t hi, int algo,
+                              double* ab, ptrdiff_t ldab, ptrdiff_t sab, ptrdiff_t* P, ptrdiff_t sp,
+                              ptrdiff_t nrhs, double* B, ptrdiff_t ldb, ptrdiff_t sb, int* status);
 
 /* complex<double> (tmv_oracle_z.c): column-major, entries interleaved
  * (re, im), leading dimensions in complex elements. */

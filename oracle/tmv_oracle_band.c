@@ -259,3 +259,22 @@ int oracle_band_lu_ldiveq(ptrdiff_t n, ptrdiff_t lo, ptrdiff_t hi, int algo, con
     }
     return ORACLE_OK;
 }
+
+/* The batched band workload on the host cores: for each system s (OpenMP
+ * over systems) LU_Decompose and LU_LDivEq in place, system s's band at
+ * ab + s*sab, interchanges at P + s*sp, right-hand sides at B + s*sb;
+ * status[s] as oracle_band_lu_ldiveq returns it. */
+int oracle_band_batched_solve(ptrdiff_t count, ptrdiff_t n, ptrdiff_t lo, ptrdiff_t hi, int algo,
+                              double* ab, ptrdiff_t ldab, ptrdiff_t sab, ptrdiff_t* P, ptrdiff_t sp,
+                              ptrdiff_t nrhs, double* B, ptrdiff_t ldb, ptrdiff_t sb, int* status)
+{
+#pragma omp parallel for schedule(static)
+    for (idx s = 0; s < count; ++s) {
+        int rc = oracle_band_lu_decompose(n, lo, hi, algo, ab + s * sab, ldab, P + s * sp);
+        if (rc == ORACLE_OK)
+            rc = oracle_band_lu_ldiveq(n, lo, hi, algo, ab + s * sab, ldab, P + s * sp, nrhs, B + s * sb,
+                                       ldb);
+        status[s] = rc;
+    }
+    return ORACLE_OK;
+}

@@ -129,5 +129,8 @@ def band_matrix(rng, n: int, lo: int, hi: int, kind: str = "normal") -> np.ndarr
 
 
 def bits(x: np.ndarray) -> np.ndarray:
-    """Bit patterns, so that equality also sees signed zeros and NaNs."""
-    return np.ascontiguousarray(x, dtype=np.float64).view(np.int64)
+    """Bit patterns, so that equality also sees signed zeros and infinities;
+    every NaN maps to one pattern (the sign and payload of a NaN that an
+    operation creates differ between x86, aarch64 and the GPU)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    return np.where(np.isnan(x), np.float64(np.nan), x).view(np.int64)

@@ -115,6 +115,12 @@ _SIGS = {
     "tmvg_batched_lu_solve_f64": (C.c_int, [vp, vp, vp, vp, vp]),
     "tmvg_batched_lu_solve_mixed_f64": (C.c_int, [vp, vp, vp, vp, vp, C.c_int, dbl, vp, vp]),
     "tmvg_batch_plan_destroy": (C.c_int, [vp]),
+    "tmvg_band_lu_decompose_batched_f64": (C.c_int, [vp, i64, i64, i64, i64, C.c_int, vp, i64, i64,
+                                                   vp, i64]),
+    "tmvg_band_lu_ldiveq_batched_f64": (C.c_int, [vp, i64, i64, i64, i64, C.c_int, vp, i64, i64, vp,
+                                                i64, i64, vp, i64, i64, vp]),
+    "tmvg_band_lu_solve_batched_f64": (C.c_int, [vp, i64, i64, i64, i64, C.c_int, vp, i64, i64, vp,
+                                               i64, i64, vp, i64, i64, vp]),
 }
 
 _lib = None

@@ -1,0 +1,572 @@
+// band.cu -- batched band LU: TMV's LU_Decompose(BandMatrixView<double>)
+// (src/TMV_BandLUDecompose.cpp:383-425) and LU_LDivEq on band factors
+// (src/TMV_BandLUDiv.cpp:811-831) for many systems of one shape, one thread
+// per system.
+//
+// A band LU is a chain of n dependent steps, each touching a window of at
+// most (lo+1) x (hu+1) entries, so one system offers no parallelism worth a
+// CTA.  The GPU form is a batch: thousands of same-shaped band systems (line
+// solves of a PDE grid, spline and filter systems), each run by one thread
+// that keeps its window in registers.  The work is FP64 arithmetic (one IEEE
+// division and about 2 lo hu products and differences per step), so the FP64
+// pipe bounds it.
+//
+// Storage is TMV's column-major band layout per system: element (i,j) at
+// ab[s*sab + i + j*ldab] for j-hu <= i <= j+lo, hu = min(lo+hi, n-1), with
+// ldab >= lo + hu.  The fill diagonals hi+1..hu are outputs (the kernel writes
+// every band slot once, as it leaves the window) and are never read.
+//
+// Results are TMV's bit for bit: the same pivot rule, the same operations in
+// the same order, products and differences rounded separately (__dmul_rn,
+// __dsub_rn: no contraction into FMA), true IEEE divisions.  Two algorithms,
+// as TMV picks them by storage:
+//   TMVG_BAND_GENERAL  NonLapBandLU_Decompose (:49-143) and the
+//                      column-oriented upper solve (src/TMV_BandTriDiv_V.cpp:
+//                      148-235);
+//   TMVG_BAND_TRIDIAG  NonLapTriDiagLU_Decompose (:144-200), which BandLUDiv
+//                      uses for a tridiagonal matrix (src/TMV_BandLUD.cpp:
+//                      61-63), and the row-oriented upper solve
+//                      (src/TMV_BandTriDiv_V.cpp:63-135).
+#include <float.h>
+
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace tmvg {
+
+namespace {
+
+constexpr int kBandThreads = 128;
+
+struct BandArgs {
+    double* ab;
+    int64_t sab, ldab;
+    int64_t* P;
+    int64_t sp;
+    double* B;
+    int64_t ldb, sb;
+    int32_t* status;
+    int64_t count;
+    int64_t n;
+    int lo, hi, hu, nrhs;
+    int factor, solve;
+};
+
+__host__ __device__ __forceinline__ int64_t lmin(int64_t x, int64_t y) { return x < y ? x : y; }
+__host__ __device__ __forceinline__ int64_t lmax(int64_t x, int64_t y) { return x > y ? x : y; }
+
+// a - b*c with the product rounded first, as TMV's C++ evaluates it.
+__device__ __forceinline__ double msub(double a, double b, double c)
+{
+    return __dsub_rn(a, __dmul_rn(b, c));
+}
+
+// v *= x as MultXV does it (src/TMV_MultXV.cpp:150-153): unchanged for
+// x == 1, zero for x == 0.
+__device__ __forceinline__ double scale_by(double v, double x)
+{
+    return x == 1.0 ? v : (x == 0.0 ? 0.0 : __dmul_rn(x, v));
+}
+
+// ---------------------------------------------------------------------------
+// Factorisation with the window W[r][c] = A(j+r, j+c), r <= lo, c <= hu, in
+// registers.  LOC >= lo and HUC >= hu are the compile-time capacities;
+// entries outside the runtime window stay zero.  At step j the column j
+// (rows j..j+lo) and the row j (columns j+1..j+hu) are final and stored; the
+// window then moves one step down the diagonal and takes in row j+1+lo,
+// which no earlier step touched.  Its new column j+1+hu holds fill above
+// row j+1+lo (zero).
+// ---------------------------------------------------------------------------
+template <int LOC, int HUC, bool TRID>
+__device__ void band_factor(double* __restrict__ a, int64_t ldab, int64_t* __restrict__ P, int64_t n,
+                            int lo, int hi, int hu)
+{
+    if (lo == 0) {  // already U (src/TMV_BandLUDecompose.cpp:417-421); no fill
+        for (int64_t i = 0; i < n; ++i) P[i] = i;
+        return;
+    }
+    double W[LOC + 1][HUC + 1];
+#pragma unroll
+    for (int r = 0; r <= LOC; ++r)
+#pragma unroll
+        for (int c = 0; c <= HUC; ++c) {
+            const bool in = r <= lo && c <= hu && r < n && c < n && c - r <= hi;
+            W[r][c] = in ? a[r + c * ldab] : 0.0;
+        }
+    for (int64_t j = 0; j < n; ++j) {
+        const int rlim = (int)lmin(lo + 1, n - j);  // rows j..j+rlim-1
+        const int clim = (int)lmin(hu + 1, n - j);  // columns j..j+clim-1
+        if (j + 1 < n) {
+            if (TRID) {
+                const bool pivot = fabs(W[1][0]) > fabs(W[0][0]);
+                if (pivot) {
+#pragma unroll
+                    for (int c = 0; c <= 2; ++c) {
+                        const double t = W[0][c];
+                        W[0][c] = W[1][c];
+                        W[1][c] = t;
+                    }
+                }
+                P[j] = j + (pivot ? 1 : 0);
+                if (fabs(W[0][0]) < DBL_MIN) {
+                    W[0][0] = 0.0;
+                    W[1][0] = 0.0;
+                } else {
+                    W[1][0] = W[1][0] / W[0][0];
+                }
+                W[1][1] = msub(W[1][1], W[1][0], W[0][1]);
+                if (pivot && j + 2 < n) W[1][2] = msub(W[1][2], W[1][0], W[0][2]);
+            } else {
+                // first strict maximum of |A(j..j+rlim-1, j)|
+                double piv = fabs(W[0][0]);
+                int ip = 0;
+#pragma unroll
+                for (int r = 1; r <= LOC; ++r) {
+                    const double v = fabs(W[r][0]);
+                    if (r < rlim && v > piv) {
+                        piv = v;
+                        ip = r;
+                    }
+                }
+                if (piv < DBL_MIN) {  // TMV_Underflow: zero the column, no interchange
+                    ip = 0;
+#pragma unroll
+                    for (int r = 0; r <= LOC; ++r)
+                        if (r < rlim) W[r][0] = 0.0;
+                }
+#pragma unroll
+                for (int r = 1; r <= LOC; ++r)
+                    if (r == ip)
+#pragma unroll
+                        for (int c = 0; c <= HUC; ++c) {
+                            const double t = W[0][c];
+                            W[0][c] = W[r][c];
+                            W[r][c] = t;
+                        }
+                P[j] = j + ip;
+                const double ujj = W[0][0];
+                if (ujj != 0.0) {
+                    const double inv = 1.0 / ujj;
+#pragma unroll
+                    for (int r = 1; r <= LOC; ++r)
+                        if (r < rlim) W[r][0] = scale_by(W[r][0], inv);
+                }
+                // outer-product update, a column with a zero U(j,c) left alone
+#pragma unroll
+                for (int c = 1; c <= HUC; ++c) {
+                    const double u = W[0][c];
+                    if (c < clim && u != 0.0)
+#pragma unroll
+                        for (int r = 1; r <= LOC; ++r)
+                            if (r < rlim) W[r][c] = msub(W[r][c], W[r][0], u);
+                }
+            }
+        } else {
+            P[j] = j;
+        }
+        // column j (L and U(j,j)) and row j of U leave the window
+#pragma unroll
+        for (int r = 0; r <= LOC; ++r)
+            if (r < rlim) a[(j + r) + j * ldab] = W[r][0];
+#pragma unroll
+        for (int c = 1; c <= HUC; ++c)
+            if (c < clim) a[j + (j + c) * ldab] = W[0][c];
+        if (j + 1 == n) break;
+#pragma unroll
+        for (int r = 0; r <= LOC; ++r)
+#pragma unroll
+            for (int c = 0; c <= HUC; ++c) W[r][c] = (r < LOC && c < HUC) ? W[r + 1][c + 1] : 0.0;
+        const int64_t nr = j + 1 + lo;
+#pragma unroll
+        for (int r = 0; r <= LOC; ++r)
+            if (r == lo)
+#pragma unroll
+                for (int c = 0; c <= HUC; ++c)
+                    if (c <= hu) W[r][c] = (nr < n && j + 1 + c < n) ? a[nr + (j + 1 + c) * ldab] : 0.0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// One right-hand side: the packed P L solve (LU_PackedPL_LDivEq,
+// src/TMV_BandLUDiv.cpp:79-118) with the window y[r] = b[j+r] in registers,
+// then the upper solve on the leading i2 rows, i2 = one past the last nonzero
+// (NonBlasTriLDivEq trims trailing zeros, src/TMV_BandTriDiv_V.cpp:455-466):
+// a diagonal U (hu == 0) divides every row < i2 after checking its U(i,i)
+// (DoDiagLDivEq1, src/TMV_DiagMatrix.cpp:296-341); otherwise the column form
+// (zero entries skipped) or, for the tridiagonal algorithm, the row form,
+// each with its window x[k] = b[j-k] (column) or b[i+k] (row) in registers.
+// Returns 0, 1 for a zero U(j,j) where TMV throws SingularBandLU, or 2 for
+// an interchange P[j] outside rows j..min(j+lo, n-1) (factors not made by
+// the band LU), which is not applied.
+// ---------------------------------------------------------------------------
+template <int LOC, int HUC, bool TRID>
+__device__ int band_solve_one(const double* __restrict__ a, int64_t ldab, const int64_t* __restrict__ P,
+                               int64_t n, int lo, int hu, double* __restrict__ b)
+{
+    int64_t last_nz = -1;
+    if (lo == 0) {
+        for (int64_t j = n - 1; j >= 0; --j)
+            if (b[j] != 0.0) {
+                last_nz = j;
+                break;
+            }
+    } else {
+        double y[LOC + 1];
+#pragma unroll
+        for (int r = 0; r <= LOC; ++r) y[r] = (r <= lo && r < n) ? b[r] : 0.0;
+        for (int64_t j = 0; j < n; ++j) {
+            if (j + 1 < n) {
+                const int64_t pj = P[j];
+                if (pj < j || pj > j + lo || pj >= n) return 2;
+                const int d = (int)(pj - j);
+#pragma unroll
+                for (int r = 1; r <= LOC; ++r)
+                    if (r == d) {
+                        const double t = y[0];
+                        y[0] = y[r];
+                        y[r] = t;
+                    }
+                const double bj = y[0];
+                if (bj != 0.0)
+#pragma unroll
+                    for (int r = 1; r <= LOC; ++r)
+                        if (r <= lo && j + r < n) y[r] = msub(y[r], a[(j + r) + j * ldab], bj);
+            }
+            b[j] = y[0];
+            if (y[0] != 0.0) last_nz = j;
+#pragma unroll
+            for (int r = 0; r < LOC; ++r) y[r] = y[r + 1];
+            y[LOC] = 0.0;
+            const int64_t nr = j + 1 + lo;
+#pragma unroll
+            for (int r = 0; r <= LOC; ++r)
+                if (r == lo) y[r] = nr < n ? b[nr] : 0.0;
+        }
+    }
+    const int64_t i2 = last_nz + 1;
+    if (i2 == 0) return 0;
+    if (hu == 0) {
+        for (int64_t i = 0; i < i2; ++i) {
+            const double d = a[i + i * ldab];
+            if (d == 0.0) return 1;
+            b[i] = b[i] / d;
+        }
+        return 0;
+    }
+    if (TRID) {
+        const int64_t nh = lmin(hu, i2 - 1);
+        double x1 = 0.0, x2 = 0.0;  // b[i+1], b[i+2], solved
+        for (int64_t i = i2 - 1; i >= 0; --i) {
+            const int64_t len = lmin(i2 - 1 - i, nh);
+            double v = b[i];
+            if (len >= 1) v = msub(v, x1, a[i + (i + 1) * ldab]);
+            if (len >= 2) v = msub(v, x2, a[i + (i + 2) * ldab]);
+            const double d = a[i + i * ldab];
+            if (d == 0.0) return 1;
+            v = v / d;
+            b[i] = v;
+            x2 = x1;
+            x1 = v;
+        }
+        return 0;
+    }
+    double x[HUC + 1];
+    {
+        const int64_t j = i2 - 1;
+#pragma unroll
+        for (int k = 0; k <= HUC; ++k) x[k] = (k <= hu && j - k >= 0) ? b[j - k] : 0.0;
+    }
+    for (int64_t j = i2 - 1; j >= 0; --j) {
+        const double bj0 = x[0];
+        if (bj0 != 0.0) {
+            const double d = a[j + j * ldab];
+            if (d == 0.0) return 1;
+            const double bj = bj0 / d;
+            x[0] = bj;
+#pragma unroll
+            for (int k = 1; k <= HUC; ++k)
+                if (k <= hu && j - k >= 0) x[k] = msub(x[k], bj, a[(j - k) + j * ldab]);
+        }
+        b[j] = x[0];
+#pragma unroll
+        for (int k = 0; k < HUC; ++k) x[k] = x[k + 1];
+        x[HUC] = 0.0;
+        const int64_t nr = j - 1 - hu;
+#pragma unroll
+        for (int k = 0; k <= HUC; ++k)
+            if (k == hu) x[k] = nr >= 0 ? b[nr] : 0.0;
+    }
+    return 0;
+}
+
+template <int LOC, int HUC, bool TRID>
+__global__ void __launch_bounds__(kBandThreads) band_lu_kernel(const BandArgs g)
+{
+    const int64_t s = (int64_t)blockIdx.x * kBandThreads + threadIdx.x;
+    if (s >= g.count) return;
+    double* a = g.ab + s * g.sab;
+    int64_t* P = g.P + s * g.sp;
+    if (g.factor) band_factor<LOC, HUC, TRID>(a, g.ldab, P, g.n, g.lo, g.hi, g.hu);
+    if (!g.solve) return;
+    int st = 0;
+    if (g.nrhs > 0) {
+        double* B = g.B + s * g.sb;
+        if (g.n == 1 && g.nrhs > 1 && g.ldb == 1) {
+            // a 1 x nrhs B with ldb == 1 is row-major to TMV: ColUpperTriLDivEq
+            // (src/TMV_BandTriDiv_M.cpp:87-125) checks U(0,0) and scales the
+            // row by its reciprocal
+            const double d = a[0];
+            if (d == 0.0) {
+                st = 1;
+            } else {
+                const double inv = 1.0 / d;
+                for (int q = 0; q < g.nrhs; ++q) B[q] = scale_by(B[q], inv);
+            }
+        } else {
+            for (int q = 0; q < g.nrhs && st == 0; ++q)
+                st = band_solve_one<LOC, HUC, TRID>(a, g.ldab, P, g.n, g.lo, g.hu, B + q * g.ldb);
+        }
+    }
+    g.status[s] = st;
+}
+
+// The same algorithm for bands wider than the register kernels hold: the
+// window stays in the band storage itself (the thread's own slots, cached in
+// L1/L2), each step a direct transcription of the loops of
+// NonLapBandLU_Decompose and of the solves above.
+__global__ void __launch_bounds__(kBandThreads) band_lu_wide_kernel(const BandArgs g)
+{
+    const int64_t s = (int64_t)blockIdx.x * kBandThreads + threadIdx.x;
+    if (s >= g.count) return;
+    double* a = g.ab + s * g.sab;
+    int64_t* P = g.P + s * g.sp;
+    const int64_t n = g.n, ld = g.ldab;
+    const int lo = g.lo, hi = g.hi, hu = g.hu;
+    if (g.factor) {
+        for (int64_t j = 0; j < n; ++j)
+            for (int d = hi + 1; d <= hu; ++d)
+                if (j - d >= 0) a[(j - d) + j * ld] = 0.0;
+        if (lo == 0) {
+            for (int64_t i = 0; i < n; ++i) P[i] = i;
+        } else {
+            int64_t endcol = lmin(lo + 1, n), endrow = lmin(hu + 1, n);
+            for (int64_t j = 0; j + 1 < n; ++j) {
+                int64_t ip = 0;
+                double piv = fabs(a[j + j * ld]);
+                for (int64_t i = 1; i < endcol - j; ++i) {
+                    const double v = fabs(a[(j + i) + j * ld]);
+                    if (v > piv) {
+                        piv = v;
+                        ip = i;
+                    }
+                }
+                if (piv < DBL_MIN) {
+                    ip = 0;
+                    for (int64_t i = j; i < endcol; ++i) a[i + j * ld] = 0.0;
+                }
+                if (ip != 0) {
+                    ip += j;
+                    for (int64_t c = j; c < endrow; ++c) {
+                        const double t = a[ip + c * ld];
+                        a[ip + c * ld] = a[j + c * ld];
+                        a[j + c * ld] = t;
+                    }
+                }
+                P[j] = ip != 0 ? ip : j;
+                const double ujj = a[j + j * ld];
+                if (ujj != 0.0) {
+                    const double inv = 1.0 / ujj;
+                    for (int64_t i = j + 1; i < endcol; ++i) a[i + j * ld] = scale_by(a[i + j * ld], inv);
+                }
+                for (int64_t c = j + 1; c < endrow; ++c) {
+                    const double u = a[j + c * ld];
+                    if (u == 0.0) continue;
+                    for (int64_t i = j + 1; i < endcol; ++i)
+                        a[i + c * ld] = msub(a[i + c * ld], a[i + j * ld], u);
+                }
+                if (endcol < n) ++endcol;
+                if (endrow < n) ++endrow;
+            }
+            P[n - 1] = n - 1;
+        }
+    }
+    if (!g.solve) return;
+    int st = 0;
+    const bool row_b = n == 1 && g.nrhs > 1 && g.ldb == 1;
+    double* B = g.nrhs > 0 ? g.B + s * g.sb : nullptr;
+    if (row_b) {
+        const double d = a[0];
+        if (d == 0.0) {
+            st = 1;
+        } else {
+            const double inv = 1.0 / d;
+            for (int q = 0; q < g.nrhs; ++q) B[q] = scale_by(B[q], inv);
+        }
+    }
+    for (int q = 0; q < g.nrhs && st == 0 && !row_b; ++q) {
+        double* b = B + q * g.ldb;
+        if (lo > 0) {
+            int64_t jn = lmin(lo + 1, n);
+            for (int64_t j = 0; j + 1 < n && st == 0; ++j) {
+                const int64_t pj = P[j];
+                if (pj < j || pj > j + lo || pj >= n) {
+                    st = 2;
+                    break;
+                }
+                if (pj != j) {
+                    const double t = b[j];
+                    b[j] = b[pj];
+                    b[pj] = t;
+                }
+                const double bj = b[j];
+                if (bj != 0.0)
+                    for (int64_t i = j + 1; i < jn; ++i) b[i] = msub(b[i], a[i + j * ld], bj);
+                if (jn < n) ++jn;
+            }
+        }
+        if (st) break;
+        int64_t i2 = n;
+        while (i2 > 0 && b[i2 - 1] == 0.0) --i2;
+        if (i2 == 0) continue;
+        if (hu == 0) {
+            for (int64_t i = 0; i < i2 && st == 0; ++i) {
+                const double d = a[i + i * ld];
+                if (d == 0.0) st = 1;
+                else b[i] = b[i] / d;
+            }
+            continue;
+        }
+        for (int64_t j = i2 - 1; j >= 0; --j) {
+            if (b[j] == 0.0) continue;
+            const double d = a[j + j * ld];
+            if (d == 0.0) {
+                st = 1;
+                break;
+            }
+            const double bj = b[j] / d;
+            b[j] = bj;
+            for (int64_t i = lmax(0, j - hu); i < j; ++i) b[i] = msub(b[i], bj, a[i + j * ld]);
+        }
+    }
+    g.status[s] = st;
+}
+
+// The register kernel's window capacity for (lo, hu), or -1 for the wide kernel.
+int band_class(int lo, int hu, int algo)
+{
+    if (algo == TMVG_BAND_TRIDIAG) return 0;
+    if (lo <= 1 && hu <= 2) return 1;
+    if (lo <= 2 && hu <= 4) return 2;
+    if (lo <= 4 && hu <= 8) return 3;
+    return -1;
+}
+
+tmvg_status band_run(Context* c, int64_t count, int64_t n, int64_t lo, int64_t hi, int algo, double* AB,
+                     int64_t ldab, int64_t sab, int64_t* P, int64_t sp, int64_t nrhs, double* B, int64_t ldb,
+                     int64_t sb, int32_t* status, bool factor, bool solve, const char* what)
+{
+    std::string w(what);
+    if (count < 0 || n < 0 || lo < 0 || hi < 0 || nrhs < 0) return set_error(c, TMVG_BAD_ARG, w + ": negative size");
+    if (algo != TMVG_BAND_GENERAL && algo != TMVG_BAND_TRIDIAG)
+        return set_error(c, TMVG_BAD_ARG, w + ": unknown algorithm");
+    if (count == 0 || n == 0) return TMVG_OK;
+    if (lo > n - 1 || hi > n - 1) return set_error(c, TMVG_BAD_ARG, w + ": lo and hi must be < n");
+    if (algo == TMVG_BAND_TRIDIAG && (lo != 1 || hi != 1))
+        return set_error(c, TMVG_BAD_ARG, w + ": the tridiagonal algorithm needs lo == hi == 1");
+    if (lo > 1 << 20 || hi > 1 << 20) return set_error(c, TMVG_BAD_ARG, w + ": band too wide");
+    const int64_t hu = std::min(lo + hi, n - 1);
+    if (ldab < lo + hu || ldab < 1) return set_error(c, TMVG_BAD_ARG, w + ": ldab < lo + min(lo+hi, n-1)");
+    const int64_t len = (n - 1) * (ldab + 1) + 1;
+    if (count > 1 && sab < len) return set_error(c, TMVG_BAD_ARG, w + ": band systems overlap (stride_ab)");
+    if (count > 1 && sp < n) return set_error(c, TMVG_BAD_ARG, w + ": stride_p < n");
+    if (!AB || !P) return set_error(c, TMVG_BAD_ARG, w + ": null band or pivot pointer");
+    if (solve) {
+        if (nrhs > (1 << 30)) return set_error(c, TMVG_BAD_ARG, w + ": too many right-hand sides");
+        if (!status) return set_error(c, TMVG_BAD_ARG, w + ": null status pointer");
+        if (nrhs > 0) {
+            if (!B) return set_error(c, TMVG_BAD_ARG, w + ": null right-hand side pointer");
+            if (ldb < n) return set_error(c, TMVG_BAD_ARG, w + ": ldb < n");
+            if (count > 1 && sb < ldb * (nrhs - 1) + n)
+                return set_error(c, TMVG_BAD_ARG, w + ": right-hand sides overlap (stride_b)");
+        }
+    }
+    BandArgs g;
+    g.ab = AB;
+    g.sab = sab;
+    g.ldab = ldab;
+    g.P = P;
+    g.sp = sp;
+    g.B = B;
+    g.ldb = ldb;
+    g.sb = sb;
+    g.status = status;
+    g.count = count;
+    g.n = n;
+    g.lo = (int)lo;
+    g.hi = (int)hi;
+    g.hu = (int)hu;
+    g.nrhs = solve ? (int)nrhs : 0;
+    g.factor = factor;
+    g.solve = solve;
+    const int64_t blocks = (count + kBandThreads - 1) / kBandThreads;
+    if (blocks > INT32_MAX) return set_error(c, TMVG_BAD_ARG, w + ": too many systems");
+    const dim3 grid((unsigned)blocks);
+    switch (band_class((int)lo, (int)hu, algo)) {
+        case 0: band_lu_kernel<1, 2, true><<<grid, kBandThreads, 0, c->stream>>>(g); break;
+        case 1: band_lu_kernel<1, 2, false><<<grid, kBandThreads, 0, c->stream>>>(g); break;
+        case 2: band_lu_kernel<2, 4, false><<<grid, kBandThreads, 0, c->stream>>>(g); break;
+        case 3: band_lu_kernel<4, 8, false><<<grid, kBandThreads, 0, c->stream>>>(g); break;
+        default: band_lu_wide_kernel<<<grid, kBandThreads, 0, c->stream>>>(g); break;
+    }
+    c->launches += 1;
+    return check_cuda(c, cudaGetLastError(), what);
+}
+
+}  // namespace
+
+}  // namespace tmvg
+
+using namespace tmvg;
+
+extern "C" {
+
+tmvg_status tmvg_band_lu_decompose_batched_f64(tmvg_handle h, int64_t count, int64_t n, int64_t lo,
+                                               int64_t hi, int algo, double* AB, int64_t ldab,
+                                               int64_t stride_ab, int64_t* P, int64_t stride_p)
+{
+    Context* c = reinterpret_cast<Context*>(h);
+    if (!c) return TMVG_BAD_ARG;
+    c->last_error.clear();
+    if (cudaSetDevice(c->device) != cudaSuccess) return set_error(c, TMVG_CUDA_ERROR, "cudaSetDevice failed");
+    return band_run(c, count, n, lo, hi, algo, AB, ldab, stride_ab, P, stride_p, 0, nullptr, 1, 0, nullptr, true,
+                    false, "band_lu_decompose");
+}
+
+tmvg_status tmvg_band_lu_ldiveq_batched_f64(tmvg_handle h, int64_t count, int64_t n, int64_t lo, int64_t hi,
+                                            int algo, const double* AB, int64_t ldab, int64_t stride_ab,
+                                            const int64_t* P, int64_t stride_p, int64_t nrhs, double* B,
+                                            int64_t ldb, int64_t stride_b, int32_t* status)
+{
+    Context* c = reinterpret_cast<Context*>(h);
+    if (!c) return TMVG_BAD_ARG;
+    c->last_error.clear();
+    if (cudaSetDevice(c->device) != cudaSuccess) return set_error(c, TMVG_CUDA_ERROR, "cudaSetDevice failed");
+    return band_run(c, count, n, lo, hi, algo, const_cast<double*>(AB), ldab, stride_ab, const_cast<int64_t*>(P),
+                    stride_p, nrhs, B, ldb, stride_b, status, false, true, "band_lu_ldiveq");
+}
+
+tmvg_status tmvg_band_lu_solve_batched_f64(tmvg_handle h, int64_t count, int64_t n, int64_t lo, int64_t hi,
+                                           int algo, double* AB, int64_t ldab, int64_t stride_ab, int64_t* P,
+                                           int64_t stride_p, int64_t nrhs, double* B, int64_t ldb,
+                                           int64_t stride_b, int32_t* status)
+{
+    Context* c = reinterpret_cast<Context*>(h);
+    if (!c) return TMVG_BAD_ARG;
+    c->last_error.clear();
+    if (cudaSetDevice(c->device) != cudaSuccess) return set_error(c, TMVG_CUDA_ERROR, "cudaSetDevice failed");
+    return band_run(c, count, n, lo, hi, algo, AB, ldab, stride_ab, P, stride_p, nrhs, B, ldb, stride_b, status,
+                    true, true, "band_lu_solve");
+}
+
+}  // extern "C"
