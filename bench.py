@@ -751,7 +751,43 @@ def other_workloads(dev, with_cpu: bool) -> dict:
         "backward_roofline": fp64_roofline(4.0 * n * n * 64 / (bwd_ms * 1e-3) / 1e12),
         "workload": "X = A^-1 B (n = 2048, 64 right-hand sides), backward gB = A^-T G and gA = -gB X^T "
                     "from the stored factors"}
-    del flush
+    # complex<double> LU + solve at n = 4096 (8 right-hand sides): A, B with
+    # N(0,1) real and imaginary parts, 4 sqrt(n) added to the diagonal
+    n = 4096
+    Az = torch.complex(torch.randn((n, n), dtype=torch.float64, device=dev, generator=g),
+                       torch.randn((n, n), dtype=torch.float64, device=dev, generator=g))
+    Az += 4.0 * np.sqrt(n) * torch.eye(n, dtype=torch.complex128, device=dev)
+    Az = Az.t().contiguous().t()
+    Bz = torch.complex(torch.randn((n, 8), dtype=torch.float64, device=dev, generator=g),
+                       torch.randn((n, 8), dtype=torch.float64, device=dev, generator=g)).t().contiguous().t()
+    LUz, Xz = torch.empty_like(Az), torch.empty_like(Bz)
+
+    def zsolve():
+        LUz.copy_(Az)
+        Xz.copy_(Bz)
+        Pz = linalg.lu_decompose_z(LUz)
+        linalg.lu_ldiveq_z(LUz, Pz, Xz)
+
+    ms = ev_time(zsolve, reps=3, warm=1)
+    zfl = 8.0 * n ** 3 / 3.0 + 8.0 * n * n * 8  # real flops: 4 real FMAs per complex FMA
+    tf = zfl / (ms * 1e-3) / 1e12
+    res = (Az @ Xz - Bz).abs().max().item() / (Az.abs().sum(dim=1).max().item() * Xz.abs().max().item())
+    out["complex_lu_solve_4096"] = {
+        "value": round(tf, 4), "unit": "TFLOP/s", "ms": round(ms, 3), "roofline": fp64_roofline(tf),
+        "normwise_backward_error": res,
+        "workload": "complex<double> X = B/A, n = 4096, 8 right-hand sides, A ~ CN(0,1) + 4 sqrt(n) I; "
+                    "flops 8n^3/3 + 8 n^2 nrhs (timed region includes the two device copies of A and B)"}
+    if with_cpu:
+        orc, kind, what = cpu_reference()
+        nc = 1024
+        ah = (Az[:nc, :nc]).cpu().numpy().copy(order="F")
+        t0 = time.perf_counter()
+        orc.lu_decompose_z(ah)
+        dt = time.perf_counter() - t0
+        out["complex_lu_solve_4096"]["cpu_baseline"] = {
+            "value": round(8.0 * nc ** 3 / 3.0 / dt / 1e12, 5), "unit": "TFLOP/s", "cores": 1, "kind": kind,
+            "sample": f"one complex LU_Decompose at n = {nc} ({dt:.2f} s, one core); {what}"}
+    del Az, Bz, LUz, Xz, flush
     out["band_lu_65536x1024"] = band_workloads(dev, with_cpu)
     return out
 

@@ -17,7 +17,7 @@ def _host(t):
     return np.asfortranarray(t.cpu().numpy())
 
 
-@pytest.mark.parametrize("n", [1, 2, 3, 5, 17, 64, 65, 130, 300])
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 17, 64, 65, 127, 128, 130, 300, 1024, 1500])
 def test_complex_lu_and_solve_match_oracle(dev, orc, n):
     import torch
 
@@ -172,3 +172,30 @@ def test_complex_inverse_matches_tmv(dev):
     P = linalg.lu_decompose_z(A)
     with pytest.raises(_lib.SingularError):
         linalg.lu_inverse_z(A, P)
+
+
+def test_complex_lu_narrow_panel_large(dev):
+    """n = 6400 takes the 16-column panels (a 32-column panel's rows exceed
+    shared memory): P L U = A to rounding, |L| <= 1 (partial pivoting), and a
+    solve's normwise backward error at most 1e-14."""
+    import torch
+
+    from tmv_gb300 import linalg
+
+    n = 6400
+    g = torch.Generator(device=dev).manual_seed(21)
+    A = torch.complex(torch.randn((n, n), dtype=torch.float64, device=dev, generator=g),
+                      torch.randn((n, n), dtype=torch.float64, device=dev, generator=g))
+    A = A.t().contiguous().t()
+    LU = A.clone()
+    P = linalg.lu_decompose_z(LU)
+    b = torch.complex(torch.randn((n, 2), dtype=torch.float64, device=dev, generator=g),
+                      torch.randn((n, 2), dtype=torch.float64, device=dev, generator=g)).t().contiguous().t()
+    x = b.clone()
+    linalg.lu_ldiveq_z(LU, P, x)
+    Pc = P.cpu().numpy()
+    assert (Pc >= np.arange(n)).all() and (Pc < n).all()
+    L = torch.tril(LU, -1)
+    assert float(L.abs().max()) <= 1.0 + 1e-12
+    berr = float((A @ x - b).abs().max() / (A.abs().sum(dim=1).max() * x.abs().max()))
+    assert berr <= 1e-14, berr

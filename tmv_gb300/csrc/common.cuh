@@ -76,6 +76,8 @@ struct Context {
     int cluster_ok[2] = {-1, -1};
     // The same for the register-resident panel kernel.
     int reg_cluster_ok[2] = {-1, -1};
+    // The same for the complex LU's panel cluster, per panel width (32, 16).
+    int zpanel_ok[2] = {-1, -1};
     // Third grow-only workspace: operand copies of the tensor-core update.
     void* work3 = nullptr;
     size_t work3_bytes = 0;

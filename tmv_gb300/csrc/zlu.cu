@@ -14,14 +14,18 @@
 // Complex products are (ac - bd, ad + bc) with separately rounded products
 // (no fused multiply-add), as the host computes them.
 //
-// A first GPU form: right-looking, one column per step (pivot search in one
-// CTA, row interchange, scaling, rank-1 update over the grid), the left
-// solve one CTA per right-hand side, the right solve (LU_RDivEq) one row per
-// CTA substituted in TMV's order.  Values agree with TMV's recursive factorisation
-// to rounding; pivots are TMV's wherever rounding does not decide a tie.
+// Small matrices (n < 128) factor one column per step (pivot search in one
+// CTA, row interchange, scaling, rank-1 update over the grid); larger ones
+// by panels (zlu_factor_blocked below).  The left solve runs one CTA per
+// right-hand side, the right solve (LU_RDivEq) one row per CTA substituted
+// in TMV's order.  Values agree with TMV's recursive factorisation to
+// rounding; pivots are TMV's wherever rounding does not decide a tie.
 #include "zlu.cuh"
 
+#include <cooperative_groups.h>
+
 #include <algorithm>
+#include <climits>
 
 namespace tmvg {
 
@@ -155,10 +159,489 @@ zlu_update_kernel(int64_t n, double2* A, int64_t lda, int64_t k)
     A[i + j * lda] = zsub(A[i + j * lda], zmul(A[i + k * lda], A[k + j * lda]));
 }
 
+// ---------------------------------------------------------------------------
+// Blocked factorisation (n >= kZBlockedMin): right-looking over panels of KB
+// columns (32, or 16 where a 32-wide panel's rows exceed shared memory).
+// Each panel is factored by one 16-CTA cluster with the rows dealt
+// cyclically to the CTAs and held in their shared memory; the column steps
+// are the column path's (pivot, interchange within the panel, scaling by
+// TMV_InverseOf, rank-1 update of the panel's later columns).  The panel's
+// interchanges are then applied to the other columns, U12 = L11^-1 A12 is
+// solved, and A22 -= L21 U12 runs as a register-tiled complex DFMA product.
+// Column values differ from the unblocked updates only by rounding, so the
+// pivots are the column path's (TMV's) wherever rounding does not decide a
+// tie.
+//
+// Pivot search in two stages, so that TMV_ABS (two divisions and a square
+// root) is evaluated only where it can decide: a proxy key per row, the bits
+// of |z|^2 computed after scaling z by a power of two (two FP64 operations,
+// relative error below 2^-51), selects the rows within 256 ulps of |z|^2 of
+// the CTA's largest key; those get TMV_ABS and the largest TMV_ABS (lowest
+// row on ties) is the CTA's candidate.  TMV_ABS differs from |z| by at most a few
+// ulps, so no row outside the margin can hold the maximum.  Infinite and NaN
+// entries follow TMV_ABS (NaN): chosen only as the column's first entry.
+// ---------------------------------------------------------------------------
+constexpr int kZPanelCtas = 16;
+constexpr int kZPanelThreads = 512;
+constexpr int64_t kZBlockedMin = 128;
+constexpr size_t kZPanelSmemMax = 200 * 1024;
+constexpr long long kZKeyNaNFirst = 0x7fffffffffffffffLL;  // NaN/inf as row j
+constexpr long long kZKeyNaN = -0x7fffffffffffffffLL;      // NaN/inf elsewhere
+constexpr long long kZKeyZero = -(1LL << 62);
+constexpr long long kZAbsBits = 0x7fffffffffffffffLL;
+constexpr long long kZInfBits = 0x7ff0000000000000LL;
+
+// Proxy key of z: increasing in |z| up to its rounding.  Comparisons and
+// scaling run on the integer pipe (a double comparison occupies the FP64
+// pipe, which GB300 issues at 2 per SM per clock); |z|^2 itself takes one
+// DMUL and one DFMA.
+__device__ __forceinline__ long long zproxy_key(double2 z, bool first)
+{
+    const long long ur = __double_as_longlong(z.x) & kZAbsBits;
+    const long long ui = __double_as_longlong(z.y) & kZAbsBits;
+    const long long us = ur > ui ? ur : ui;
+    if (us >= kZInfBits) return first ? kZKeyNaNFirst : kZKeyNaN;  // inf or NaN
+    if (us == 0) return kZKeyZero;
+    const int eb = (int)(us >> 52);  // biased exponent of the larger part
+    double r, t;
+    int e2;  // |z|^2 = K 4^e2
+    if (eb == 0) {  // subnormal: scale by 2^600 first (exact)
+        const double ar = fabs(z.x) * 0x1p600, ai = fabs(z.y) * 0x1p600;
+        const long long vs = __double_as_longlong(fmax(ar, ai));
+        const int e = (int)(vs >> 52) - 1023;
+        const double sc = __longlong_as_double((long long)(1023 - e) << 52);
+        r = ar * sc;
+        t = ai * sc;
+        e2 = e - 600;
+    } else {
+        // both parts scaled by 2^-(eb-1023) through their exponent fields; a
+        // smaller part pushed below the normal range counts as zero (its
+        // square is below 2^-1000 of K's); a subnormal smaller part is scaled
+        // by a multiplication (exact)
+        const long long shift = (long long)(eb - 1023) << 52;
+        const long long ul = ur > ui ? ui : ur;
+        const double big = __longlong_as_double(us - shift);
+        const int lb = (int)(ul >> 52);
+        double small;
+        if (lb == 0)
+            small = ul == 0 ? 0.0 : __longlong_as_double(ul) * __longlong_as_double((long long)(2046 - eb) << 52);
+        else
+            small = lb - (eb - 1023) >= 1 ? __longlong_as_double(ul - shift) : 0.0;
+        r = big;
+        t = small;
+        e2 = eb - 1023;
+    }
+    const double K = fma(r, r, t * t);  // in [1, 8)
+    // exponent 2 e2 in [-2148, 2046] above K's bits less 1.0's (K's binade
+    // offset 0..2 and mantissa), the mantissa's last two bits dropped so that
+    // the sum fits 64 bits; one key unit is 4 ulps of K
+    const long long kb = (__double_as_longlong(K) - __double_as_longlong(1.0)) >> 2;
+    return ((long long)(2 * e2) << 50) + kb;
+}
+
+// TMV_ABS as an ordered integer key: its bits (non-negative), a NaN as the
+// column's first entry above everything, elsewhere below everything.
+__device__ __forceinline__ long long zabs_key(double raw, bool first)
+{
+    const long long b = __double_as_longlong(raw);
+    if ((b & kZAbsBits) > kZInfBits) return first ? kZKeyNaNFirst : -1;
+    return b;
+}
+
+template <int KB>
+struct ZPanelShared {
+    long long cand_key[2];     // this CTA's candidate: zabs_key (-2: none)
+    double cand_abs[2];        // its TMV_ABS (NaN kept)
+    long long cand_row[2];     // its global row (LLONG_MAX: none)
+    double2 cand_inv[2];       // TMV_InverseOf of its entry
+    double2 cand_rowv[2][KB];  // its row's panel entries
+    double2 diag_rowv[2][KB];  // row j's panel entries (the CTA owning row j)
+    double2 prow[KB];          // the pivot row after the interchange: U's row j
+    double2 inv;
+    int under;
+    long long wkey[kZPanelThreads / 32];
+    int wrow[kZPanelThreads / 32];
+};
+
+template <int KB>
+__global__ void __launch_bounds__(kZPanelThreads)
+zlu_panel_smem_kernel(int64_t n, double2* __restrict__ A, int64_t lda, int64_t k, int kb, int64_t* __restrict__ P,
+                      int rpc)
+{
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    extern __shared__ double2 s_rows[];  // rpc rows, stride KB + 1
+    __shared__ ZPanelShared<KB> sh;
+    constexpr int RS = KB + 1;
+    const int cta = (int)cluster.block_rank();
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // local row r is global row k + cta + 16 r
+    for (int t = tid; t < rpc * kb; t += kZPanelThreads) {
+        const int r = t % rpc, c = t / rpc;
+        const int64_t i = k + cta + (int64_t)kZPanelCtas * r;
+        s_rows[r * RS + c] = i < n ? A[i + (k + c) * lda] : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    for (int jj = 0; jj < kb; ++jj) {
+        const int par = jj & 1;
+        const int64_t j = k + jj;
+        // rows of this CTA at or below j: r >= r0
+        const int64_t d0 = j - k - cta;
+        const int r0 = d0 <= 0 ? 0 : (int)((d0 + kZPanelCtas - 1) / kZPanelCtas);
+        const int lj = (d0 >= 0 && d0 % kZPanelCtas == 0) ? (int)(d0 / kZPanelCtas) : -1;
+        // stage 1: largest proxy key (the first row's key kept for stage 2)
+        long long bk = LLONG_MIN, key0 = LLONG_MIN;
+        for (int r = r0 + tid; r < rpc; r += kZPanelThreads) {
+            const int64_t i = k + cta + (int64_t)kZPanelCtas * r;
+            if (i >= n) break;
+            const long long key = zproxy_key(s_rows[r * RS + jj], i == j);
+            if (r == r0 + tid) key0 = key;
+            bk = key > bk ? key : bk;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const long long ok = __shfl_xor_sync(0xffffffffu, bk, o);
+            bk = ok > bk ? ok : bk;
+        }
+        if (lane == 0) sh.wkey[warp] = bk;
+        __syncthreads();
+        long long mk = sh.wkey[0];
+#pragma unroll
+        for (int w = 1; w < kZPanelThreads / 32; ++w) mk = sh.wkey[w] > mk ? sh.wkey[w] : mk;
+        // stage 2: TMV_ABS (and TMV_InverseOf) of the rows within 64 key units
+        // (256 ulps of |z|^2) of the largest
+        const long long thr = mk <= LLONG_MIN + 64 ? LLONG_MIN + 1 : mk - 64;
+        long long ba = -2;
+        int br = INT_MAX;
+        double braw = 0.0;
+        double2 binv = make_double2(0.0, 0.0);
+        for (int r = r0 + tid; r < rpc && mk != LLONG_MIN; r += kZPanelThreads) {
+            const int64_t i = k + cta + (int64_t)kZPanelCtas * r;
+            if (i >= n) break;
+            const double2 z = s_rows[r * RS + jj];
+            const long long key = r == r0 + tid ? key0 : zproxy_key(z, i == j);
+            if (key < thr) continue;
+            const double raw = tmv_abs(z);
+            const long long a = zabs_key(raw, i == j);
+            if (a > ba || (a == ba && r < br)) {
+                ba = a;
+                br = r;
+                braw = raw;
+                binv = tmv_inverse_of(z);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const long long oa = __shfl_xor_sync(0xffffffffu, ba, o);
+            const int orow = __shfl_xor_sync(0xffffffffu, br, o);
+            if (oa > ba || (oa == ba && orow < br)) { ba = oa; br = orow; }
+        }
+        if (lane == 0) { sh.wkey[warp] = ba; sh.wrow[warp] = br; }
+        __syncthreads();
+        ba = sh.wkey[0];
+        br = sh.wrow[0];
+#pragma unroll
+        for (int w = 1; w < kZPanelThreads / 32; ++w)
+            if (sh.wkey[w] > ba || (sh.wkey[w] == ba && sh.wrow[w] < br)) { ba = sh.wkey[w]; br = sh.wrow[w]; }
+        // stage the candidate (its owner thread writes its TMV_ABS and
+        // inverse) and, where owned, row j
+        if (tid < kb) {
+            if (br != INT_MAX) sh.cand_rowv[par][tid] = s_rows[br * RS + tid];
+            if (lj >= 0) sh.diag_rowv[par][tid] = s_rows[lj * RS + tid];
+        }
+        if (br != INT_MAX && (br - r0) % kZPanelThreads == tid && br >= r0) {
+            sh.cand_abs[par] = braw;
+            sh.cand_inv[par] = binv;
+        }
+        if (tid == 0) {
+            sh.cand_key[par] = ba;
+            sh.cand_row[par] = br == INT_MAX ? LLONG_MAX : k + cta + (long long)kZPanelCtas * br;
+        }
+        cluster.sync();
+        // the winner over the cluster: lanes 0..15 of every warp read one CTA each
+        long long wa = -3, wr = LLONG_MAX;
+        int wc = 0;
+        if (lane < kZPanelCtas) {
+            ZPanelShared<KB>* o = cluster.map_shared_rank(&sh, lane);
+            wa = o->cand_key[par];
+            wr = o->cand_row[par];
+            wc = lane;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const long long oa = __shfl_xor_sync(0xffffffffu, wa, o);
+            const long long orow = __shfl_xor_sync(0xffffffffu, wr, o);
+            const int oc = __shfl_xor_sync(0xffffffffu, wc, o);
+            if (oa > wa || (oa == wa && orow < wr)) { wa = oa; wr = orow; wc = oc; }
+        }
+        const int owner_j = (int)((j - k) % kZPanelCtas);
+        // U's row j: the pivot row (or row j with its column zeroed)
+        if (tid < kb) {
+            ZPanelShared<KB>* w = cluster.map_shared_rank(&sh, wc);
+            // the pivot's own modulus (a NaN stays NaN: no underflow)
+            const long long rb = __double_as_longlong(w->cand_abs[par]) & kZAbsBits;
+            const bool under = rb < __double_as_longlong(DBL_MIN);
+            const int64_t p = under ? j : (int64_t)wr;
+            double2 v;
+            if (under) {
+                v = cluster.map_shared_rank(&sh.diag_rowv[par][0], owner_j)[tid];
+                if (tid == jj) v = make_double2(0.0, 0.0);
+            } else {
+                v = w->cand_rowv[par][tid];
+            }
+            sh.prow[tid] = v;
+            if (lj >= 0) s_rows[lj * RS + tid] = v;
+            if (p != j && (int)((p - k) % kZPanelCtas) == cta)
+                s_rows[(int)((p - k) / kZPanelCtas) * RS + tid] =
+                    cluster.map_shared_rank(&sh.diag_rowv[par][0], owner_j)[tid];
+            if (tid == 0) {
+                sh.under = under ? 1 : 0;
+                sh.inv = under ? make_double2(0.0, 0.0) : w->cand_inv[par];
+                if (cta == 0) P[j] = p;
+            }
+        }
+        __syncthreads();
+        // scale and update this CTA's rows below j
+        const double2 inv = sh.inv;
+        const bool und = sh.under != 0;
+        for (int r = r0 + tid; r < rpc; r += kZPanelThreads) {
+            const int64_t i = k + cta + (int64_t)kZPanelCtas * r;
+            if (i >= n) break;
+            if (i == j) continue;
+            double2* row = &s_rows[r * RS];
+            const double2 l = und ? make_double2(0.0, 0.0) : zmul(row[jj], inv);
+            row[jj] = l;
+            for (int c = jj + 1; c < kb; ++c) {
+                const double2 u = sh.prow[c];
+                double2 a = row[c];
+                a.x = fma(-l.x, u.x, a.x);
+                a.x = fma(l.y, u.y, a.x);
+                a.y = fma(-l.x, u.y, a.y);
+                a.y = fma(-l.y, u.x, a.y);
+                row[c] = a;
+            }
+        }
+        // (the next column reads only this thread's rows until its first
+        // __syncthreads; sh.prow is rewritten only after the next cluster.sync)
+    }
+    __syncthreads();
+    for (int t = tid; t < rpc * kb; t += kZPanelThreads) {
+        const int r = t % rpc, c = t / rpc;
+        const int64_t i = k + cta + (int64_t)kZPanelCtas * r;
+        if (i < n) A[i + (k + c) * lda] = s_rows[r * RS + c];
+    }
+    cluster.sync();  // no CTA leaves while another may still read its shared memory
+}
+
+// The panel's interchanges P[k..k+kb) applied in order to every column
+// outside [k, k+kb), one column per thread.
+__global__ void zlu_swap_rest_kernel(int64_t n, double2* A, int64_t lda, int64_t k, int kb,
+                                     const int64_t* __restrict__ P)
+{
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t col = t < k ? t : t + kb;
+    if (col >= n) return;
+    double2* a = A + col * lda;
+    for (int jj = 0; jj < kb; ++jj) {
+        const int64_t j = k + jj, p = P[j];
+        if (p != j) {
+            const double2 x = a[j];
+            a[j] = a[p];
+            a[p] = x;
+        }
+    }
+}
+
+// U12 = L11^-1 A12 (L11 unit lower, KB x KB), one column of A12 per thread,
+// the column held in registers.
+template <int KB>
+__global__ void __launch_bounds__(64) zlu_trsm_kernel(int64_t n, double2* A, int64_t lda, int64_t k)
+{
+    __shared__ double2 s_l[KB][KB + 1];
+    for (int t = threadIdx.x; t < KB * KB; t += blockDim.x) {
+        const int r = t % KB, q = t / KB;
+        s_l[r][q] = A[(k + r) + (k + q) * lda];
+    }
+    __syncthreads();
+    const int64_t col = k + KB + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (col >= n) return;
+    double2* a = A + k + col * lda;
+    double2 x[KB];
+#pragma unroll
+    for (int r = 0; r < KB; ++r) x[r] = a[r];
+#pragma unroll
+    for (int q = 0; q < KB; ++q)
+#pragma unroll
+        for (int r = q + 1; r < KB; ++r) {
+            const double2 l = s_l[r][q];
+            x[r].x = fma(-l.x, x[q].x, x[r].x);
+            x[r].x = fma(l.y, x[q].y, x[r].x);
+            x[r].y = fma(-l.x, x[q].y, x[r].y);
+            x[r].y = fma(-l.y, x[q].x, x[r].y);
+        }
+#pragma unroll
+    for (int r = 0; r < KB; ++r) a[r] = x[r];
+}
+
+// A22 -= L21 U12 (K = KB): 64 x 64 complex tiles, each of the 256 threads a
+// 4 x 4 block, complex products on the DFMA pipe.
+constexpr int kZgBM = 64, kZgBN = 64, kZgBK = 8;
+template <int KB>
+__global__ void __launch_bounds__(256)
+zlu_gemm_kernel(int64_t n, double2* A, int64_t lda, int64_t k)
+{
+    __shared__ double2 s_a[kZgBK][kZgBM];
+    __shared__ double2 s_b[kZgBK][kZgBN + 1];
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const int64_t r0 = k + KB + (int64_t)blockIdx.x * kZgBM;  // rows of A22
+    const int64_t c0 = k + KB + (int64_t)blockIdx.y * kZgBN;  // columns of A22
+    double2 acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = make_double2(0.0, 0.0);
+    for (int kk = 0; kk < KB; kk += kZgBK) {
+        for (int t = tid; t < kZgBK * kZgBM; t += 256) {
+            const int r = t % kZgBM, q = t / kZgBM;
+            const int64_t gi = r0 + r;
+            s_a[q][r] = gi < n ? A[gi + (k + kk + q) * lda] : make_double2(0.0, 0.0);
+        }
+        for (int t = tid; t < kZgBK * kZgBN; t += 256) {
+            const int q = t % kZgBK, cc = t / kZgBK;
+            const int64_t gj = c0 + cc;
+            s_b[q][cc] = gj < n ? A[(k + kk + q) + gj * lda] : make_double2(0.0, 0.0);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < kZgBK; ++q) {
+            double2 av[4], bv[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) av[a] = s_a[q][tx + 16 * a];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) bv[b] = s_b[q][ty + 16 * b];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                    acc[a][b].x = fma(av[a].x, bv[b].x, acc[a][b].x);
+                    acc[a][b].x = fma(-av[a].y, bv[b].y, acc[a][b].x);
+                    acc[a][b].y = fma(av[a].x, bv[b].y, acc[a][b].y);
+                    acc[a][b].y = fma(av[a].y, bv[b].x, acc[a][b].y);
+                }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        const int64_t gj = c0 + ty + 16 * b;
+        if (gj >= n) continue;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int64_t gi = r0 + tx + 16 * a;
+            if (gi < n) {
+                double2* p = &A[gi + gj * lda];
+                *p = make_double2(p->x - acc[a][b].x, p->y - acc[a][b].y);
+            }
+        }
+    }
+}
+
+// The panel width for n: 32 where ceil(n/16) rows of 33 entries fit the
+// shared memory, else 16; 0 (column path) beyond.
+static int zpanel_width(int64_t n)
+{
+    const int64_t rpc = ceil_div(n, kZPanelCtas);
+    if ((size_t)rpc * 33 * sizeof(double2) <= kZPanelSmemMax) return 32;
+    if ((size_t)rpc * 17 * sizeof(double2) <= kZPanelSmemMax) return 16;
+    return 0;
+}
+
+// Whether the 16-CTA panel cluster of width KB can run here with the most
+// shared memory it may ask for (checked once per context and width).
+template <int KB>
+static bool zpanel_cluster_ok(Context* c)
+{
+    static_assert(kZPanelCtas == 16, "non-portable cluster size");
+    int& ok = c->zpanel_ok[KB == 32 ? 0 : 1];
+    if (ok >= 0) return ok == 1;
+    ok = 0;
+    if (cudaFuncSetAttribute(zlu_panel_smem_kernel<KB>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(zlu_panel_smem_kernel<KB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kZPanelSmemMax) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kZPanelCtas;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(kZPanelCtas);
+    cfg.blockDim = dim3(kZPanelThreads);
+    cfg.dynamicSmemBytes = kZPanelSmemMax;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, zlu_panel_smem_kernel<KB>, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    ok = clusters >= 1 ? 1 : 0;
+    return ok == 1;
+}
+
+template <int KB>
+static tmvg_status zlu_factor_blocked(Context* c, int64_t n, double2* A, int64_t lda, int64_t* P)
+{
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kZPanelCtas;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(kZPanelCtas);
+    cfg.blockDim = dim3(kZPanelThreads);
+    cfg.stream = c->stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    for (int64_t k = 0; k < n; k += KB) {
+        const int kb = (int)std::min<int64_t>(KB, n - k);
+        const int rpc = (int)ceil_div(n - k, kZPanelCtas);
+        cfg.dynamicSmemBytes = (size_t)rpc * (KB + 1) * sizeof(double2);
+        tmvg_status st = check_cuda(
+            c, cudaLaunchKernelEx(&cfg, zlu_panel_smem_kernel<KB>, n, A, lda, k, kb, P, rpc),
+            "lu_z: panel launch");
+        if (st) return st;
+        ++c->launches;
+        const int64_t rest_cols = n - kb;
+        if (rest_cols > 0) {
+            zlu_swap_rest_kernel<<<(unsigned)ceil_div(rest_cols, 128), 128, 0, c->stream>>>(n, A, lda, k, kb, P);
+            ++c->launches;
+        }
+        const int64_t m2 = n - k - kb;
+        if (m2 > 0) {  // kb == KB here
+            zlu_trsm_kernel<KB><<<(unsigned)ceil_div(m2, 64), 64, 0, c->stream>>>(n, A, lda, k);
+            const dim3 grid((unsigned)ceil_div(m2, kZgBM), (unsigned)ceil_div(m2, kZgBN));
+            zlu_gemm_kernel<KB><<<grid, 256, 0, c->stream>>>(n, A, lda, k);
+            c->launches += 2;
+        }
+        st = check_cuda(c, cudaGetLastError(), "lu_z: blocked launch");
+        if (st) return st;
+    }
+    return TMVG_OK;
+}
+
 tmvg_status zlu_factor(Context* c, int64_t n, double2* A, int64_t lda, int64_t* P)
 {
     if (n < 0 || lda < std::max<int64_t>(n, 1)) return set_error(c, TMVG_BAD_ARG, "lu_z: bad n/lda");
     if (n == 0) return TMVG_OK;
+    if (n >= kZBlockedMin) {
+        const int w = zpanel_width(n);
+        if (w == 32 && zpanel_cluster_ok<32>(c)) return zlu_factor_blocked<32>(c, n, A, lda, P);
+        if (w == 16 && zpanel_cluster_ok<16>(c)) return zlu_factor_blocked<16>(c, n, A, lda, P);
+    }
     int* flag = (int*)workspace(c, 256);
     if (!flag) return TMVG_OOM;
     const unsigned gcols = (unsigned)std::min<int64_t>(ceil_div(n, kZThreads), 4 * c->num_sms);
