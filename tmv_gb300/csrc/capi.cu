@@ -56,6 +56,7 @@ void* workspace(Context* c, size_t bytes) { return grow(c, c->work, c->work_byte
 void* workspace2(Context* c, size_t bytes) { return grow(c, c->work2, c->work2_bytes, bytes); }
 void* workspace3(Context* c, size_t bytes) { return grow(c, c->work3, c->work3_bytes, bytes); }
 void* perm_lists_buffer(Context* c, size_t bytes) { return grow(c, c->perm_lists, c->perm_lists_bytes, bytes); }
+void* trsv_dinv_buffer(Context* c, size_t bytes) { return grow(c, c->trsv_dinv, c->trsv_dinv_bytes, bytes); }
 
 static cudaEvent_t pooled_event(Context* c)
 {
@@ -432,6 +433,7 @@ tmvg_status tmvg_destroy(tmvg_handle h)
     if (c->perm_lists) cudaFree(c->perm_lists);
     if (c->trsv_flags) cudaFree(c->trsv_flags);
     if (c->trsv_pub) cudaFree(c->trsv_pub);
+    if (c->trsv_dinv) cudaFree(c->trsv_dinv);
     if (c->dflags) cudaFree(c->dflags);
     if (c->hflags) cudaFreeHost(c->hflags);
     for (const TimedSpan& sp : c->spans) {

@@ -71,6 +71,10 @@ struct Context {
     // word (epoch << 32 | value bits); grow-only, never needs clearing.
     unsigned long long* trsv_pub = nullptr;
     size_t trsv_pub_len = 0;
+    // Inverted 64 x 64 diagonal blocks of the many-column sync-free solve
+    // (grow-only) and their per-block zero-diagonal flags.
+    void* trsv_dinv = nullptr;
+    size_t trsv_dinv_bytes = 0;
     // Whether a 16-CTA cluster of the panel kernel can be launched, per
     // element type (-1 unknown, 0 no, 1 yes): [0] double, [1] float.
     int cluster_ok[2] = {-1, -1};
@@ -149,6 +153,7 @@ tmvg_status probe_fp64_rate(Context* c, double* tflops);
 void* workspace2(Context* c, size_t bytes);
 void* workspace3(Context* c, size_t bytes);
 void* perm_lists_buffer(Context* c, size_t bytes);
+void* trsv_dinv_buffer(Context* c, size_t bytes);
 // Reads and clears the device error word (synchronises the stream).
 tmvg_status collect_device_error(Context* c, const char* what);
 

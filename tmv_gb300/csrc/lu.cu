@@ -2336,13 +2336,14 @@ tmvg_status lu_factor(Context* c, int64_t n, T* A, int64_t lda, int64_t* P)
 }
 
 // Triangular solve of the pivoted right-hand sides: the single-launch
-// sync-free kernel for few columns, the blocked product-based solve for many.
+// sync-free kernel (one CTA per 64-row block and group of right-hand sides)
+// up to 256 columns, the blocked product-based solve for more.
 template <typename T>
 static tmvg_status tri_any(Context* c, int64_t n, const T* tri, int64_t tsi, int64_t tsj,
                            bool upper, bool unit, int64_t nrhs, T* B, int64_t bsi, int64_t bsj,
                            bool skip_zero)
 {
-    if (nrhs <= 8)
+    if (nrhs <= 256 && ceil_div(n, (int64_t)64) * ceil_div(nrhs, (int64_t)4) <= kTrsvFlagCap)
         return trsm_sync_free<T>(c, n, tri, tsi, tsj, upper, unit, nrhs, B, bsi, bsj, skip_zero);
     return tri_solve<T>(c, n, tri, tsi, tsj, upper, unit, nrhs, B, bsi, bsj, skip_zero);
 }

@@ -44,14 +44,67 @@ __device__ __forceinline__ void st_release(unsigned* p, unsigned v)
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// Inverse of each 64 x 64 lower diagonal block (an upper triangle arrives
+// index-reversed), for the many-column solve: one CTA per block, thread j
+// builds column j by forward substitution with the diagonal's reciprocals
+// (taken once per block).  dinv[b] is row-major 64 x 64; sing[b] = 1 when
+// the block has a zero diagonal (that block keeps the substitution, with
+// TMV's zero-skipping and singular semantics).
+template <typename T>
+__global__ void __launch_bounds__(kTrsvBlock)
+tri_inv64_kernel(int64_t n, const T* __restrict__ tri, int64_t tsi, int64_t tsj, bool unit,
+                 T* __restrict__ dinv, int* __restrict__ sing)
+{
+    // dynamic shared memory: D and X, each kTrsvBlock x (kTrsvBlock + 1)
+    extern __shared__ __align__(16) unsigned char inv_smem[];
+    T(*D)[kTrsvBlock + 1] = reinterpret_cast<T(*)[kTrsvBlock + 1]>(inv_smem);
+    T(*X)[kTrsvBlock + 1] = D + kTrsvBlock;
+    __shared__ T rd[kTrsvBlock];
+    __shared__ int s_sing;
+    const int tid = threadIdx.x;
+    const int64_t b = blockIdx.x, r0 = b * kTrsvBlock;
+    const int rows = (int)min((int64_t)kTrsvBlock, n - r0);
+    if (tid == 0) s_sing = 0;
+    for (int t = tid; t < kTrsvBlock * kTrsvBlock; t += kTrsvBlock) {
+        const int rr = t % kTrsvBlock, cc = t / kTrsvBlock;
+        D[rr][cc] = (rr < rows && cc <= rr) ? tri[(r0 + rr) * tsi + (r0 + cc) * tsj] : T(0);
+    }
+    __syncthreads();
+    if (!unit && tid < rows) {
+        if (D[tid][tid] == T(0)) s_sing = 1;
+        else rd[tid] = T(1) / D[tid][tid];
+    }
+    __syncthreads();
+    if (tid == 0) sing[b] = s_sing;
+    if (s_sing) return;
+    const int j = tid;
+    for (int i = 0; i < kTrsvBlock; ++i) {
+        T v = T(0);
+        if (i < rows && j < rows && i >= j) {
+            T acc = i == j ? T(1) : T(0);
+            for (int k = j; k < i; ++k) acc -= D[i][k] * X[k][j];
+            v = unit ? acc : acc * rd[i];
+        }
+        X[i][j] = v;
+    }
+    __syncthreads();
+    T* out = dinv + b * kTrsvBlock * kTrsvBlock;
+    for (int t = tid; t < kTrsvBlock * kTrsvBlock; t += kTrsvBlock) out[t] = X[t / kTrsvBlock][t % kTrsvBlock];
+}
+
+// One CTA per (row block, group of NR right-hand sides); tickets hand the
+// pairs out block by block (all groups of block b before block b+1), and a
+// CTA waits only on earlier blocks of its own group, so every wait is on a
+// ticket already handed out.  flags[g * nblk + b] publishes (b, g).
 template <typename T, int NR>
 __global__ void __launch_bounds__(kTrsvThreads)
 trsm_sync_free_kernel(int64_t n, const T* __restrict__ tri, int64_t tsi, int64_t tsj, bool unit,
-                      int nr, T* B, int64_t bsi, int64_t bsj, bool skip_zero,
+                      int64_t nrhs, int groups, T* B, int64_t bsi, int64_t bsj, bool skip_zero,
                       unsigned* flags, unsigned epoch, unsigned long long* ticket,
-                      unsigned long long tbase, unsigned spin_limit, int* err)
+                      unsigned long long tbase, unsigned spin_limit, int* err,
+                      const T* __restrict__ dinv, const int* __restrict__ dinv_sing)
 {
-    __shared__ int s_blk;
+    __shared__ long long s_tk;
     __shared__ T xs[kTrsvBlock][NR];
     __shared__ T xj[kTrsvBlock][NR];
     __shared__ T Td[kTrsvBlock][kTrsvBlock + 1];
@@ -61,20 +114,31 @@ trsm_sync_free_kernel(int64_t n, const T* __restrict__ tri, int64_t tsi, int64_t
     const int tid = threadIdx.x;
     const int i = tid & 63, g = tid >> 6;
     if (tid == 0) {
-        s_blk = (int)(atomicAdd(ticket, 1ull) - tbase);
+        s_tk = (long long)(atomicAdd(ticket, 1ull) - tbase);
         s_abort = 0;
     }
     __syncthreads();
-    const int64_t b = s_blk;
     const int64_t nblk = (n + kTrsvBlock - 1) / kTrsvBlock;
-    if (b < 0 || b >= nblk) return;
+    if (s_tk < 0 || s_tk >= nblk * groups) return;
+    const int64_t b = s_tk / groups;
+    const int grp = (int)(s_tk % groups);
+    const int nr = (int)min((int64_t)NR, nrhs - (int64_t)grp * NR);
+    B += (int64_t)grp * NR * bsj;
+    flags += (int64_t)grp * nblk;
     const int64_t r0 = b * kTrsvBlock;
     const int rows = (int)min((int64_t)kTrsvBlock, n - r0);
 
-    // diagonal block and right-hand side
-    for (int t = tid; t < kTrsvBlock * kTrsvBlock; t += kTrsvThreads) {
-        const int rr = t % kTrsvBlock, cc = t / kTrsvBlock;
-        Td[rr][cc] = (rr < rows && cc <= rr) ? tri[(r0 + rr) * tsi + (r0 + cc) * tsj] : T(0);
+    // diagonal block (or its inverse) and right-hand side
+    const bool use_inv = dinv != nullptr && dinv_sing[b] == 0;
+    if (use_inv) {
+        const T* di = dinv + b * kTrsvBlock * kTrsvBlock;
+        for (int t = tid; t < kTrsvBlock * kTrsvBlock; t += kTrsvThreads)
+            Td[t / kTrsvBlock][t % kTrsvBlock] = di[t];
+    } else {
+        for (int t = tid; t < kTrsvBlock * kTrsvBlock; t += kTrsvThreads) {
+            const int rr = t % kTrsvBlock, cc = t / kTrsvBlock;
+            Td[rr][cc] = (rr < rows && cc <= rr) ? tri[(r0 + rr) * tsi + (r0 + cc) * tsj] : T(0);
+        }
     }
     for (int t = tid; t < kTrsvBlock * NR; t += kTrsvThreads) {
         const int rr = t % kTrsvBlock, q = t / kTrsvBlock;
@@ -124,10 +188,28 @@ trsm_sync_free_kernel(int64_t n, const T* __restrict__ tri, int64_t tsi, int64_t
     }
     __syncthreads();
 
-    // diagonal block: warp q substitutes right-hand side q (2 rows per lane)
+    // diagonal block: x_b = D_b^-1 x_b as a product (thread (i, q) one entry),
+    // or warp q substitutes right-hand side q (2 rows per lane)
     const int warp = tid >> 5, lane = tid & 31;
     bool sing = false;
-    for (int q = warp; q < nr; q += kTrsvThreads / 32) {
+    if (use_inv) {
+        constexpr int PER = (NR * kTrsvBlock + kTrsvThreads - 1) / kTrsvThreads;
+        T v[PER];
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+            const int t = tid + u * kTrsvThreads, ii = t % kTrsvBlock, q = t / kTrsvBlock;
+            v[u] = T(0);
+            if (q < nr && ii < rows)
+                for (int kk = 0; kk <= ii; ++kk) v[u] += Td[ii][kk] * xs[kk][q];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+            const int t = tid + u * kTrsvThreads, ii = t % kTrsvBlock, q = t / kTrsvBlock;
+            if (q < nr && ii < rows) xs[ii][q] = v[u];
+        }
+    }
+    for (int q = warp; q < nr && !use_inv; q += kTrsvThreads / 32) {
         for (int jj = 0; jj < rows; ++jj) {
             __syncwarp();
             T v = xs[jj][q];
@@ -178,40 +260,59 @@ tmvg_status trsm_sync_free(Context* c, int64_t n, const T* tri, int64_t tsi, int
         bsi = -bsi;
     }
     const int64_t nblk = ceil_div(n, kTrsvBlock);
-    if (nblk > (int64_t)kTrsvFlagCap)
-        return set_error(c, TMVG_UNSUPPORTED, "trsv: n too large for the flag array");
     constexpr int NRM = kTrsvMaxRhs<T>;
-    for (int64_t q0 = 0; q0 < nrhs; q0 += NRM) {
-        const int nr = (int)std::min<int64_t>(NRM, nrhs - q0);
-        const unsigned epoch = ++c->trsv_epoch;
-        // tickets restart at 0 for every launch
-        tmvg_status st = check_cuda(
-            c, cudaMemsetAsync(c->trsv_ticket, 0, sizeof(unsigned long long), c->stream),
-            "trsv ticket reset");
-        if (st) return st;
-        T* Bq = B + q0 * bsj;
-        // tickets map to blocks (ticket - tbase); the failure-path test hook
-        // starts them at block test_skip_blocks, so the blocks before it are
-        // never solved and the first waiting block's bounded wait gives up
-        unsigned long long tbase = 0ull;
-        if (c->test_skip_blocks > 0) {
-            tbase = 0ull - (unsigned long long)c->test_skip_blocks;
-            c->test_skip_blocks = 0;
-        }
-        const unsigned limit = c->poll_limit ? c->poll_limit : kSpinLimit;
-        if (nr == 1)
-            trsm_sync_free_kernel<T, 1><<<(unsigned)nblk, kTrsvThreads, 0, c->stream>>>(
-                n, tri, tsi, tsj, unit, nr, Bq, bsi, bsj, skip_zero, c->trsv_flags, epoch,
-                c->trsv_ticket, tbase, limit, c->dflags);
-        else
-            trsm_sync_free_kernel<T, NRM><<<(unsigned)nblk, kTrsvThreads, 0, c->stream>>>(
-                n, tri, tsi, tsj, unit, nr, Bq, bsi, bsj, skip_zero, c->trsv_flags, epoch,
-                c->trsv_ticket, tbase, limit, c->dflags);
-        ++c->launches;
-        st = check_cuda(c, cudaGetLastError(), "trsv launch");
-        if (st) return st;
+    const int64_t groups = nrhs == 1 ? 1 : ceil_div(nrhs, NRM);
+    if (nblk * groups > (int64_t)kTrsvFlagCap)
+        return set_error(c, TMVG_UNSUPPORTED, "trsv: n x nrhs too large for the flag array");
+    const unsigned epoch = ++c->trsv_epoch;
+    // tickets restart at 0 for every launch
+    tmvg_status st = check_cuda(
+        c, cudaMemsetAsync(c->trsv_ticket, 0, sizeof(unsigned long long), c->stream),
+        "trsv ticket reset");
+    if (st) return st;
+    // tickets map to (block, group) pairs (ticket - tbase); the failure-path
+    // test hook starts them at block test_skip_blocks, so the blocks before
+    // it are never solved and the first waiting block's bounded wait gives up
+    unsigned long long tbase = 0ull;
+    if (c->test_skip_blocks > 0) {
+        tbase = 0ull - (unsigned long long)c->test_skip_blocks * (unsigned long long)groups;
+        c->test_skip_blocks = 0;
     }
-    return TMVG_OK;
+    const unsigned limit = c->poll_limit ? c->poll_limit : kSpinLimit;
+    const unsigned grid = (unsigned)(nblk * groups);
+    // Beyond two groups (more than 2 NR columns) the diagonal blocks are
+    // inverted first, so that a block's step on the chain is a short product
+    // instead of a 64-step substitution with a division per step.
+    const T* dinv = nullptr;
+    const int* dsing = nullptr;
+    if (groups > 2) {
+        const size_t ib = sizeof(T) * (size_t)nblk * kTrsvBlock * kTrsvBlock;
+        unsigned char* w = (unsigned char*)trsv_dinv_buffer(c, ib + sizeof(int) * (size_t)nblk);
+        if (!w) return set_error(c, TMVG_OOM, "trsv: inverse blocks");
+        T* dv = (T*)w;
+        int* ds = (int*)(w + ib);
+        const size_t smem = sizeof(T) * 2 * kTrsvBlock * (kTrsvBlock + 1);
+        st = check_cuda(c, cudaFuncSetAttribute(tri_inv64_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)smem),
+                        "trsv inverse blocks: smem attribute");
+        if (st) return st;
+        tri_inv64_kernel<T><<<(unsigned)nblk, kTrsvBlock, smem, c->stream>>>(n, tri, tsi, tsj, unit, dv, ds);
+        ++c->launches;
+        st = check_cuda(c, cudaGetLastError(), "trsv inverse blocks");
+        if (st) return st;
+        dinv = dv;
+        dsing = ds;
+    }
+    if (nrhs == 1)
+        trsm_sync_free_kernel<T, 1><<<grid, kTrsvThreads, 0, c->stream>>>(
+            n, tri, tsi, tsj, unit, nrhs, 1, B, bsi, bsj, skip_zero, c->trsv_flags, epoch,
+            c->trsv_ticket, tbase, limit, c->dflags, nullptr, nullptr);
+    else
+        trsm_sync_free_kernel<T, NRM><<<grid, kTrsvThreads, 0, c->stream>>>(
+            n, tri, tsi, tsj, unit, nrhs, (int)groups, B, bsi, bsj, skip_zero, c->trsv_flags, epoch,
+            c->trsv_ticket, tbase, limit, c->dflags, dinv, dsing);
+    ++c->launches;
+    return check_cuda(c, cudaGetLastError(), "trsv launch");
 }
 
 // ---------------------------------------------------------------------
