@@ -21,6 +21,7 @@
 // in TMV's order.  Values agree with TMV's recursive factorisation to
 // rounding; pivots are TMV's wherever rounding does not decide a tie.
 #include "zlu.cuh"
+#include "trsv.cuh"
 
 #include <cooperative_groups.h>
 
@@ -717,12 +718,224 @@ zlu_solve_kernel(int64_t n, const double2* __restrict__ LU, int64_t lda, const i
     }
 }
 
+// ---------------------------------------------------------------------------
+// Blocked left solve (n >= kZBlockedMin): B is gathered into a scratch copy in
+// the pivoted row order, then solved by 64-row blocks: each diagonal block by
+// one CTA per 4 right-hand sides, a thread per (row, column) and one barrier
+// per step (the column-oriented solve: a zero entry is skipped; a nonzero
+// entry meeting a zero U(j,j) is singular; division as b * TMV_InverseOf(d),
+// the inverses taken once for the whole diagonal), the rows beyond the block
+// updated by a complex product; then the result is copied back.  Values agree
+// with the column-by-column solve to rounding.
+// ---------------------------------------------------------------------------
+constexpr int kZSolveBlock = 64;
+constexpr int kZSolveCols = 4;
+
+__global__ void zlu_gather_rows_kernel(int64_t n, int64_t nrhs, const int* __restrict__ perm,
+                                       const double2* __restrict__ B, int64_t ldb, double2* __restrict__ X)
+{
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= n * nrhs) return;
+    const int64_t i = t % n, q = t / n;
+    X[i + q * n] = B[(int64_t)perm[i] + q * ldb];
+}
+
+__global__ void zlu_copy_back_kernel(int64_t n, int64_t nrhs, const double2* __restrict__ X,
+                                     double2* __restrict__ B, int64_t ldb)
+{
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= n * nrhs) return;
+    const int64_t i = t % n, q = t / n;
+    B[i + q * ldb] = X[i + q * n];
+}
+
+__global__ void zlu_diag_inverse_kernel(int64_t n, const double2* __restrict__ LU, int64_t lda,
+                                        double2* __restrict__ dinv)
+{
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const double2 d = LU[j + j * lda];
+    dinv[j] = znonzero(d) ? tmv_inverse_of(d) : make_double2(0.0, 0.0);
+}
+
+// One 64-row diagonal block [k, k+w) of the unit lower (upper = false) or
+// non-unit upper triangle for columns [q0, q0 + 4) of X (n x nrhs, ld n).
+__global__ void __launch_bounds__(kZSolveBlock * kZSolveCols)
+zlu_diag_solve_kernel(int64_t n, const double2* __restrict__ LU, int64_t lda, const double2* __restrict__ dinv,
+                      int64_t k, int w, bool upper, int64_t nrhs, double2* X, int* err)
+{
+    __shared__ double2 xs[kZSolveBlock][kZSolveCols];
+    const int i = threadIdx.x % kZSolveBlock, ql = threadIdx.x / kZSolveBlock;
+    const int64_t q = (int64_t)blockIdx.x * kZSolveCols + ql;
+    const bool mine = i < w && q < nrhs;
+    double2* x = X + k + q * n;
+    xs[i][ql] = mine ? x[i] : make_double2(0.0, 0.0);
+    bool sing = false;
+    __syncthreads();
+    for (int s = 0; s < w; ++s) {
+        const int j = upper ? w - 1 - s : s;
+        if (upper) {
+            if (i == j && mine) {
+                const double2 v = xs[j][ql];
+                if (znonzero(v)) {
+                    const double2 d = LU[(k + j) + (k + j) * lda];
+                    if (!znonzero(d)) sing = true;
+                    else xs[j][ql] = zmul(v, dinv[k + j]);
+                }
+            }
+            __syncthreads();
+        }
+        const double2 xj = xs[j][ql];
+        const bool below = upper ? i < j : i > j;
+        if (mine && below && znonzero(xj)) xs[i][ql] = zsub(xs[i][ql], zmul(xj, LU[(k + i) + (k + j) * lda]));
+        __syncthreads();
+    }
+    if (sing) atomicCAS(err, (int)kDevOk, (int)kDevSingular);
+    if (mine) x[i] = xs[i][ql];
+}
+
+// C -= A B for a few columns (N <= 16): a thread per entry of C.
+__global__ void zlu_gemm_skinny_kernel(int64_t M, int64_t N, int K, const double2* __restrict__ A, int64_t lda,
+                                       const double2* __restrict__ B, int64_t ldb, double2* __restrict__ C,
+                                       int64_t ldc)
+{
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= M * N) return;
+    const int64_t i = t % M, q = t / M;
+    double re = 0.0, im = 0.0;
+    for (int kk = 0; kk < K; ++kk) {
+        const double2 a = A[i + kk * lda], b = B[kk + q * ldb];
+        re = fma(a.x, b.x, re);
+        re = fma(-a.y, b.y, re);
+        im = fma(a.x, b.y, im);
+        im = fma(a.y, b.x, im);
+    }
+    double2* cp = &C[i + q * ldc];
+    *cp = make_double2(cp->x - re, cp->y - im);
+}
+
+// C -= A B, general: 64 x 64 tiles, each of the 256 threads a 4 x 4 block.
+__global__ void __launch_bounds__(256)
+zlu_gemm_tiled_kernel(int64_t M, int64_t N, int K, const double2* __restrict__ A, int64_t lda,
+                      const double2* __restrict__ B, int64_t ldb, double2* __restrict__ C, int64_t ldc)
+{
+    __shared__ double2 s_a[kZgBK][kZgBM];
+    __shared__ double2 s_b[kZgBK][kZgBN + 1];
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const int64_t r0 = (int64_t)blockIdx.x * kZgBM, c0 = (int64_t)blockIdx.y * kZgBN;
+    double2 acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = make_double2(0.0, 0.0);
+    for (int kk = 0; kk < K; kk += kZgBK) {
+        for (int t = tid; t < kZgBK * kZgBM; t += 256) {
+            const int r = t % kZgBM, q = t / kZgBM;
+            s_a[q][r] = (r0 + r < M && kk + q < K) ? A[(r0 + r) + (kk + q) * lda] : make_double2(0.0, 0.0);
+        }
+        for (int t = tid; t < kZgBK * kZgBN; t += 256) {
+            const int q = t % kZgBK, cc = t / kZgBK;
+            s_b[q][cc] = (c0 + cc < N && kk + q < K) ? B[(kk + q) + (c0 + cc) * ldb] : make_double2(0.0, 0.0);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < kZgBK; ++q) {
+            double2 av[4], bv[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) av[a] = s_a[q][tx + 16 * a];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) bv[b] = s_b[q][ty + 16 * b];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                    acc[a][b].x = fma(av[a].x, bv[b].x, acc[a][b].x);
+                    acc[a][b].x = fma(-av[a].y, bv[b].y, acc[a][b].x);
+                    acc[a][b].y = fma(av[a].x, bv[b].y, acc[a][b].y);
+                    acc[a][b].y = fma(av[a].y, bv[b].x, acc[a][b].y);
+                }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        const int64_t gj = c0 + ty + 16 * b;
+        if (gj >= N) continue;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int64_t gi = r0 + tx + 16 * a;
+            if (gi < M) {
+                double2* cp = &C[gi + gj * ldc];
+                *cp = make_double2(cp->x - acc[a][b].x, cp->y - acc[a][b].y);
+            }
+        }
+    }
+}
+
+static tmvg_status zgemm_sub(Context* c, int64_t M, int64_t N, int K, const double2* A, int64_t lda,
+                             const double2* B, int64_t ldb, double2* C, int64_t ldc)
+{
+    if (M <= 0 || N <= 0 || K <= 0) return TMVG_OK;
+    if (N <= 16) {
+        zlu_gemm_skinny_kernel<<<(unsigned)ceil_div(M * N, 128), 128, 0, c->stream>>>(M, N, K, A, lda, B, ldb, C,
+                                                                                        ldc);
+    } else {
+        const dim3 grid((unsigned)ceil_div(M, kZgBM), (unsigned)ceil_div(N, kZgBN));
+        zlu_gemm_tiled_kernel<<<grid, 256, 0, c->stream>>>(M, N, K, A, lda, B, ldb, C, ldc);
+    }
+    ++c->launches;
+    return check_cuda(c, cudaGetLastError(), "lu_ldiveq_z: product");
+}
+
+static tmvg_status zlu_ldiveq_blocked(Context* c, int64_t n, const double2* LU, int64_t lda, const int64_t* P,
+                                      int64_t nrhs, double2* B, int64_t ldb)
+{
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t o_perm = 0, o_dinv = al(sizeof(int) * n), o_x = o_dinv + al(sizeof(double2) * n);
+    unsigned char* ws = (unsigned char*)workspace(c, o_x + sizeof(double2) * (size_t)n * nrhs);
+    if (!ws) return set_error(c, TMVG_OOM, "lu_ldiveq_z: workspace");
+    int* perm = (int*)(ws + o_perm);
+    double2* dinv = (double2*)(ws + o_dinv);
+    double2* X = (double2*)(ws + o_x);
+    tmvg_status st = pivots_to_perm(c, n, P, perm);
+    if (st) return st;
+    const unsigned ge = (unsigned)ceil_div(n * nrhs, 256);
+    zlu_gather_rows_kernel<<<ge, 256, 0, c->stream>>>(n, nrhs, perm, B, ldb, X);
+    zlu_diag_inverse_kernel<<<(unsigned)ceil_div(n, 256), 256, 0, c->stream>>>(n, LU, lda, dinv);
+    c->launches += 2;
+    if ((st = check_cuda(c, cudaGetLastError(), "lu_ldiveq_z: gather"))) return st;
+    const unsigned gq = (unsigned)ceil_div(nrhs, kZSolveCols);
+    // L (unit lower), blocks in order
+    for (int64_t k = 0; k < n; k += kZSolveBlock) {
+        const int w = (int)std::min<int64_t>(kZSolveBlock, n - k);
+        zlu_diag_solve_kernel<<<gq, kZSolveBlock * kZSolveCols, 0, c->stream>>>(n, LU, lda, dinv, k, w, false,
+                                                                                 nrhs, X, c->dflags);
+        ++c->launches;
+        if ((st = check_cuda(c, cudaGetLastError(), "lu_ldiveq_z: diagonal block"))) return st;
+        if ((st = zgemm_sub(c, n - k - w, nrhs, w, LU + (k + w) + k * lda, lda, X + k, n, X + k + w, n))) return st;
+    }
+    // U (non-unit upper), blocks from the last
+    for (int64_t k = ((n - 1) / kZSolveBlock) * kZSolveBlock; k >= 0; k -= kZSolveBlock) {
+        const int w = (int)std::min<int64_t>(kZSolveBlock, n - k);
+        zlu_diag_solve_kernel<<<gq, kZSolveBlock * kZSolveCols, 0, c->stream>>>(n, LU, lda, dinv, k, w, true,
+                                                                                 nrhs, X, c->dflags);
+        ++c->launches;
+        if ((st = check_cuda(c, cudaGetLastError(), "lu_ldiveq_z: diagonal block"))) return st;
+        if ((st = zgemm_sub(c, k, nrhs, w, LU + k * lda, lda, X + k, n, X, n))) return st;
+    }
+    zlu_copy_back_kernel<<<ge, 256, 0, c->stream>>>(n, nrhs, X, B, ldb);
+    ++c->launches;
+    if ((st = check_cuda(c, cudaGetLastError(), "lu_ldiveq_z: copy back"))) return st;
+    return collect_device_error(c, "lu_ldiveq_z");
+}
+
 tmvg_status zlu_ldiveq(Context* c, int64_t n, const double2* LU, int64_t lda, const int64_t* P, int64_t nrhs,
                        double2* B, int64_t ldb)
 {
     if (n < 0 || nrhs < 0 || lda < std::max<int64_t>(n, 1) || ldb < std::max<int64_t>(n, 1))
         return set_error(c, TMVG_BAD_ARG, "lu_ldiveq_z: bad sizes");
     if (n == 0 || nrhs == 0) return TMVG_OK;
+    if (n >= kZBlockedMin && n <= (int64_t)INT32_MAX) return zlu_ldiveq_blocked(c, n, LU, lda, P, nrhs, B, ldb);
     if (nrhs > 65535) return set_error(c, TMVG_UNSUPPORTED, "lu_ldiveq_z: too many right-hand sides");
     zlu_solve_kernel<<<(unsigned)nrhs, kZThreads, 0, c->stream>>>(n, LU, lda, P, B, ldb, c->dflags);
     ++c->launches;
