@@ -434,14 +434,13 @@ zlu_panel_smem_kernel(int64_t n, double2* __restrict__ A, int64_t lda, int64_t k
     cluster.sync();  // no CTA leaves while another may still read its shared memory
 }
 
-// The panel's interchanges P[k..k+kb) applied in order to every column
-// outside [k, k+kb), one column per thread.
-__global__ void zlu_swap_rest_kernel(int64_t n, double2* A, int64_t lda, int64_t k, int kb,
+// The panel's interchanges P[k..k+kb) applied in order to the columns
+// [c0, c1), one column per thread.
+__global__ void zlu_swap_rest_kernel(int64_t c0, int64_t c1, double2* A, int64_t lda, int64_t k, int kb,
                                      const int64_t* __restrict__ P)
 {
-    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int64_t col = t < k ? t : t + kb;
-    if (col >= n) return;
+    const int64_t col = c0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (col >= c1) return;
     double2* a = A + col * lda;
     for (int jj = 0; jj < kb; ++jj) {
         const int64_t j = k + jj, p = P[j];
@@ -456,7 +455,7 @@ __global__ void zlu_swap_rest_kernel(int64_t n, double2* A, int64_t lda, int64_t
 // U12 = L11^-1 A12 (L11 unit lower, KB x KB), one column of A12 per thread,
 // the column held in registers.
 template <int KB>
-__global__ void __launch_bounds__(64) zlu_trsm_kernel(int64_t n, double2* A, int64_t lda, int64_t k)
+__global__ void __launch_bounds__(64) zlu_trsm_kernel(int64_t c1, double2* A, int64_t lda, int64_t k, int64_t c0)
 {
     __shared__ double2 s_l[KB][KB + 1];
     for (int t = threadIdx.x; t < KB * KB; t += blockDim.x) {
@@ -464,8 +463,8 @@ __global__ void __launch_bounds__(64) zlu_trsm_kernel(int64_t n, double2* A, int
         s_l[r][q] = A[(k + r) + (k + q) * lda];
     }
     __syncthreads();
-    const int64_t col = k + KB + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (col >= n) return;
+    const int64_t col = c0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (col >= c1) return;
     double2* a = A + k + col * lda;
     double2 x[KB];
 #pragma unroll
@@ -489,13 +488,13 @@ __global__ void __launch_bounds__(64) zlu_trsm_kernel(int64_t n, double2* A, int
 constexpr int kZgBM = 64, kZgBN = 64, kZgBK = 8;
 template <int KB>
 __global__ void __launch_bounds__(256)
-zlu_gemm_kernel(int64_t n, double2* A, int64_t lda, int64_t k)
+zlu_gemm_kernel(int64_t n, double2* A, int64_t lda, int64_t k, int64_t cbeg, int64_t cend)
 {
     __shared__ double2 s_a[kZgBK][kZgBM];
     __shared__ double2 s_b[kZgBK][kZgBN + 1];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     const int64_t r0 = k + KB + (int64_t)blockIdx.x * kZgBM;  // rows of A22
-    const int64_t c0 = k + KB + (int64_t)blockIdx.y * kZgBN;  // columns of A22
+    const int64_t c0 = cbeg + (int64_t)blockIdx.y * kZgBN;    // columns [cbeg, cend) of A22
     double2 acc[4][4];
 #pragma unroll
     for (int a = 0; a < 4; ++a)
@@ -510,7 +509,7 @@ zlu_gemm_kernel(int64_t n, double2* A, int64_t lda, int64_t k)
         for (int t = tid; t < kZgBK * kZgBN; t += 256) {
             const int q = t % kZgBK, cc = t / kZgBK;
             const int64_t gj = c0 + cc;
-            s_b[q][cc] = gj < n ? A[(k + kk + q) + gj * lda] : make_double2(0.0, 0.0);
+            s_b[q][cc] = gj < cend ? A[(k + kk + q) + gj * lda] : make_double2(0.0, 0.0);
         }
         __syncthreads();
 #pragma unroll
@@ -535,7 +534,7 @@ zlu_gemm_kernel(int64_t n, double2* A, int64_t lda, int64_t k)
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
         const int64_t gj = c0 + ty + 16 * b;
-        if (gj >= n) continue;
+        if (gj >= cend) continue;
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
             const int64_t gi = r0 + tx + 16 * a;
@@ -593,9 +592,17 @@ static bool zpanel_cluster_ok(Context* c)
     return ok == 1;
 }
 
+// Look-ahead: panel k+1 runs on the high-priority side stream as soon as
+// step k has updated its columns (the "narrow" update: interchanges, U12 and
+// the product for those KB columns, on the main stream), beside step k's
+// update of every other column (the "wide" update); the main stream waits for
+// panel k+1 before step k+1.  The panel and the wide update touch disjoint
+// columns.
 template <int KB>
 static tmvg_status zlu_factor_blocked(Context* c, int64_t n, double2* A, int64_t lda, int64_t* P)
 {
+    tmvg_status st = ensure_side_stream(c);
+    if (st) return st;
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -604,32 +611,54 @@ static tmvg_status zlu_factor_blocked(Context* c, int64_t n, double2* A, int64_t
     attr[0].val.clusterDim.z = 1;
     cfg.gridDim = dim3(kZPanelCtas);
     cfg.blockDim = dim3(kZPanelThreads);
-    cfg.stream = c->stream;
+    cfg.stream = c->side;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    for (int64_t k = 0; k < n; k += KB) {
+    auto panel = [&](int64_t k) -> tmvg_status {
         const int kb = (int)std::min<int64_t>(KB, n - k);
         const int rpc = (int)ceil_div(n - k, kZPanelCtas);
         cfg.dynamicSmemBytes = (size_t)rpc * (KB + 1) * sizeof(double2);
-        tmvg_status st = check_cuda(
-            c, cudaLaunchKernelEx(&cfg, zlu_panel_smem_kernel<KB>, n, A, lda, k, kb, P, rpc),
-            "lu_z: panel launch");
-        if (st) return st;
         ++c->launches;
-        const int64_t rest_cols = n - kb;
-        if (rest_cols > 0) {
-            zlu_swap_rest_kernel<<<(unsigned)ceil_div(rest_cols, 128), 128, 0, c->stream>>>(n, A, lda, k, kb, P);
-            ++c->launches;
+        return check_cuda(c, cudaLaunchKernelEx(&cfg, zlu_panel_smem_kernel<KB>, n, A, lda, k, kb, P, rpc),
+                          "lu_z: panel launch");
+    };
+    auto swap = [&](int64_t c0, int64_t c1, int64_t k, int kb) {
+        if (c1 <= c0) return;
+        zlu_swap_rest_kernel<<<(unsigned)ceil_div(c1 - c0, 128), 128, 0, c->stream>>>(c0, c1, A, lda, k, kb, P);
+        ++c->launches;
+    };
+    // step k's U12 and product for the columns [c0, c1) (k + KB <= c0)
+    auto update = [&](int64_t k, int64_t c0, int64_t c1) {
+        if (c1 <= c0 || k + KB >= n) return;
+        zlu_trsm_kernel<KB><<<(unsigned)ceil_div(c1 - c0, 64), 64, 0, c->stream>>>(c1, A, lda, k, c0);
+        const dim3 grid((unsigned)ceil_div(n - k - KB, kZgBM), (unsigned)ceil_div(c1 - c0, kZgBN));
+        zlu_gemm_kernel<KB><<<grid, 256, 0, c->stream>>>(n, A, lda, k, c0, c1);
+        c->launches += 2;
+    };
+    if ((st = check_cuda(c, cudaEventRecord(c->ev_fork, c->stream), "lu_z: fork"))) return st;
+    if ((st = check_cuda(c, cudaStreamWaitEvent(c->side, c->ev_fork, 0), "lu_z: fork wait"))) return st;
+    if ((st = panel(0))) return st;
+    if ((st = check_cuda(c, cudaEventRecord(c->ev_panel, c->side), "lu_z: panel event"))) return st;
+    for (int64_t k = 0; k < n; k += KB) {
+        const int kb = (int)std::min<int64_t>(KB, n - k);
+        if ((st = check_cuda(c, cudaStreamWaitEvent(c->stream, c->ev_panel, 0), "lu_z: panel wait"))) return st;
+        const int64_t kn = k + kb, kn1 = std::min<int64_t>(n, kn + KB);
+        if (kn < n) {
+            // narrow: the next panel's columns, then that panel on the side stream
+            swap(kn, kn1, k, kb);
+            update(k, kn, kn1);
+            if ((st = check_cuda(c, cudaGetLastError(), "lu_z: narrow update"))) return st;
+            if ((st = check_cuda(c, cudaEventRecord(c->ev_wide, c->stream), "lu_z: narrow event"))) return st;
+            if ((st = check_cuda(c, cudaStreamWaitEvent(c->side, c->ev_wide, 0), "lu_z: narrow wait"))) return st;
+            if ((st = panel(kn))) return st;
+            if ((st = check_cuda(c, cudaEventRecord(c->ev_panel, c->side), "lu_z: panel event"))) return st;
         }
-        const int64_t m2 = n - k - kb;
-        if (m2 > 0) {  // kb == KB here
-            zlu_trsm_kernel<KB><<<(unsigned)ceil_div(m2, 64), 64, 0, c->stream>>>(n, A, lda, k);
-            const dim3 grid((unsigned)ceil_div(m2, kZgBM), (unsigned)ceil_div(m2, kZgBN));
-            zlu_gemm_kernel<KB><<<grid, 256, 0, c->stream>>>(n, A, lda, k);
-            c->launches += 2;
-        }
-        st = check_cuda(c, cudaGetLastError(), "lu_z: blocked launch");
-        if (st) return st;
+        // wide: the factored columns before the panel and the columns beyond
+        // the next panel
+        swap(0, k, k, kb);
+        swap(kn1, n, k, kb);
+        update(k, kn1, n);
+        if ((st = check_cuda(c, cudaGetLastError(), "lu_z: wide update"))) return st;
     }
     return TMVG_OK;
 }
