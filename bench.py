@@ -225,6 +225,14 @@ def run_gpu(args) -> dict:
 
         dist.init_process_group("nccl", device_id=dev)
 
+    if args.path in ("band", "complex"):
+        h = linalg.handle(local)
+        FP64_PEAK.update({"tflops": round(h.fp64_rate(), 4), "source": "tmvg_probe_fp64_rate in this run"})
+        with_cpu = rank == 0 and not args.no_cpu_baseline
+        w = (band_workloads(dev, with_cpu, args.band_count) if args.path == "band"
+             else complex_workload(dev, with_cpu))
+        return {"path": args.path, "fp64_peak": dict(FP64_PEAK), "workloads": w} if rank == 0 else None
+
     if args.path == "batched":
         b = batched_bench(dev, args, with_cpu=(rank == 0 and not args.no_cpu_baseline))
         out = {"metric": "batched uneven FP64 LU solves/s", "value": b["value"], "unit": "solves/s",
@@ -751,6 +759,38 @@ def other_workloads(dev, with_cpu: bool) -> dict:
         "backward_roofline": fp64_roofline(4.0 * n * n * 64 / (bwd_ms * 1e-3) / 1e12),
         "workload": "X = A^-1 B (n = 2048, 64 right-hand sides), backward gB = A^-T G and gA = -gB X^T "
                     "from the stored factors"}
+    del flush
+    out["complex_lu_solve_4096"] = complex_workload(dev, with_cpu)
+    out["band_lu_65536x1024"] = band_workloads(dev, with_cpu)
+    return out
+
+
+def complex_workload(dev, with_cpu: bool) -> dict:
+    """complex<double> X = B/A at n = 4096 with 8 right-hand sides (A, B with
+    N(0,1) real and imaginary parts, 4 sqrt(n) added to A's diagonal, seeded),
+    timed with CUDA events (best of three after one warm-up), the two device
+    copies of A and B inside each timed call."""
+    import torch
+
+    from tmv_gb300 import linalg
+
+    stream = torch.cuda.current_stream(dev)
+
+    def ev_time(fn, reps=3, warm=1):
+        for _ in range(warm):
+            fn()
+        best = float("inf")
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        return best
+
+    g = torch.Generator(device=dev)
+    g.manual_seed(7)
     # complex<double> LU + solve at n = 4096 (8 right-hand sides): A, B with
     # N(0,1) real and imaginary parts, 4 sqrt(n) added to the diagonal
     n = 4096
@@ -772,27 +812,26 @@ def other_workloads(dev, with_cpu: bool) -> dict:
     zfl = 8.0 * n ** 3 / 3.0 + 8.0 * n * n * 8  # real flops: 4 real FMAs per complex FMA
     tf = zfl / (ms * 1e-3) / 1e12
     res = (Az @ Xz - Bz).abs().max().item() / (Az.abs().sum(dim=1).max().item() * Xz.abs().max().item())
-    out["complex_lu_solve_4096"] = {
+    out = {
         "value": round(tf, 4), "unit": "TFLOP/s", "ms": round(ms, 3), "roofline": fp64_roofline(tf),
         "normwise_backward_error": res,
         "workload": "complex<double> X = B/A, n = 4096, 8 right-hand sides, A ~ CN(0,1) + 4 sqrt(n) I; "
                     "flops 8n^3/3 + 8 n^2 nrhs (timed region includes the two device copies of A and B)"}
     if with_cpu:
         orc, kind, what = cpu_reference()
-        nc = 1024
+        nc = 2048
         ah = (Az[:nc, :nc]).cpu().numpy().copy(order="F")
         t0 = time.perf_counter()
         orc.lu_decompose_z(ah)
         dt = time.perf_counter() - t0
-        out["complex_lu_solve_4096"]["cpu_baseline"] = {
+        out["cpu_baseline"] = {
             "value": round(8.0 * nc ** 3 / 3.0 / dt / 1e12, 5), "unit": "TFLOP/s", "cores": 1, "kind": kind,
             "sample": f"one complex LU_Decompose at n = {nc} ({dt:.2f} s, one core); {what}"}
-    del Az, Bz, LUz, Xz, flush
-    out["band_lu_65536x1024"] = band_workloads(dev, with_cpu)
+    del Az, Bz, LUz, Xz
     return out
 
 
-def band_workloads(dev, with_cpu: bool) -> dict:
+def band_workloads(dev, with_cpu: bool, count: int = 65536) -> dict:
     """The batched band LU (x = b / A per system, TMV's LU_Decompose and
     LU_LDivEq on band storage, one thread per system): 65536 systems of
     n = 1024 with one right-hand side, entries N(0,1) with lo + hi + 2 added to
@@ -807,7 +846,7 @@ def band_workloads(dev, with_cpu: bool) -> dict:
 
     from tmv_gb300.band import band_layout, band_lu_solve, band_lu_solve_count
 
-    count, n = 65536, 1024
+    n = 1024
     stream = torch.cuda.current_stream(dev)
     hbm = peaks()["hbm_gbs"]
     out = {}
@@ -939,9 +978,11 @@ def main():
     ap.add_argument("--n", type=int, default=8192)
     ap.add_argument("--cond", type=float, default=1e6)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--path", default="mixed", choices=["mixed", "fp64", "batched"],
+    ap.add_argument("--path", default="mixed", choices=["mixed", "fp64", "batched", "band", "complex"],
                     help="mixed: the headline solve; fp64: the FP64 LU solve alone; batched: "
-                         "only the batched uneven solver (for profiling it)")
+                         "only the batched uneven solver; band: only the batched band LU "
+                         "workloads; complex: only the complex<double> LU solve (the last "
+                         "three for profiling them)")
     ap.add_argument("--matrix-cache", default=None,
                     help="load the workload matrix from this file if present, else save it "
                          "there (lets a profiler run skip the QR-based generation)")
@@ -949,6 +990,8 @@ def main():
     ap.add_argument("--no-sweep", action="store_true",
                     help="skip the condition-number / equal-accuracy sweep")
     ap.add_argument("--batch-count", type=int, default=20000)
+    ap.add_argument("--band-count", type=int, default=65536,
+                    help="systems of the band workload with --path band (smaller for a profiler)")
     ap.add_argument("--batch-cpu-sample", type=int, default=20000)
     ap.add_argument("--no-extras", action="store_true",
                     help="time the step only (no FP64 comparison, e2e, roofline or CPU leg)")

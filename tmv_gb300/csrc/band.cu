@@ -62,11 +62,51 @@ __device__ __forceinline__ double msub(double a, double b, double c)
     return __dsub_rn(a, __dmul_rn(b, c));
 }
 
+// Comparisons on the integer pipe: on GB300 a double comparison occupies the
+// FP64 pipe (2 operations per SM per clock), the pipe this kernel is bound by.
+// Non-negative doubles order like their bit patterns; |x| > |y| (false when
+// either is NaN) is absbits(x) > absbits(y) with absbits(x) <= inf.
+constexpr long long kAbs = 0x7fffffffffffffffLL;
+constexpr long long kInfBits = 0x7ff0000000000000LL;
+constexpr long long kDblMinBits = 0x0010000000000000LL;  // DBL_MIN
+constexpr long long kOneBits = 0x3ff0000000000000LL;     // 1.0
+__device__ __forceinline__ long long absbits(double x) { return __double_as_longlong(x) & kAbs; }
+__device__ __forceinline__ bool nonzero(double x) { return absbits(x) != 0; }
+__device__ __forceinline__ bool abs_greater(double x, double y)
+{
+    const long long bx = absbits(x);
+    return bx > absbits(y) && bx <= kInfBits;
+}
+__device__ __forceinline__ bool underflows(double x) { return absbits(x) < kDblMinBits; }
+
 // v *= x as MultXV does it (src/TMV_MultXV.cpp:150-153): unchanged for
 // x == 1, zero for x == 0.
 __device__ __forceinline__ double scale_by(double v, double x)
 {
-    return x == 1.0 ? v : (x == 0.0 ? 0.0 : __dmul_rn(x, v));
+    const long long b = __double_as_longlong(x);
+    return b == kOneBits ? v : ((b & kAbs) == 0 ? 0.0 : __dmul_rn(x, v));
+}
+
+// Steps whose loads are issued ahead (the loop is unrolled by this many so
+// that each prefetch has a register slot of its own).  One: the next step's
+// loads are issued as a step ends.  Deeper prefetching (2 and 4 steps) was
+// measured on the 65536-system benchmark batch and gained nothing for the
+// tridiagonal kernel (6.1 ms) and cost the (2,4) one occupancy (152
+// registers: 8.7 -> 12.8 ms); the kernel is bound by the FP64 issue of its
+// two IEEE divisions and few products per step, not by load latency.
+template <int LOC, int HUC>
+__host__ __device__ constexpr int band_prefetch() { return 1; }
+
+// Row j+1+lo of the band, columns j+1..j+1+hu: the row that enters the window
+// at the end of step j (zero outside the matrix).
+template <int HUC>
+__device__ __forceinline__ void band_load_row(const double* __restrict__ a, int64_t ldab, int64_t n, int lo,
+                                              int hu, int64_t j, double (&dst)[HUC + 1])
+{
+    const int64_t nr = j + 1 + lo;
+#pragma unroll
+    for (int c = 0; c <= HUC; ++c)
+        dst[c] = (c <= hu && nr < n && j + 1 + c < n) ? a[nr + (j + 1 + c) * ldab] : 0.0;
 }
 
 // ---------------------------------------------------------------------------
@@ -75,8 +115,8 @@ __device__ __forceinline__ double scale_by(double v, double x)
 // entries outside the runtime window stay zero.  At step j the column j
 // (rows j..j+lo) and the row j (columns j+1..j+hu) are final and stored; the
 // window then moves one step down the diagonal and takes in row j+1+lo,
-// which no earlier step touched.  Its new column j+1+hu holds fill above
-// row j+1+lo (zero).
+// which no earlier step touched (its loads were issued PD steps earlier).
+// Its new column j+1+hu holds fill above row j+1+lo (zero).
 // ---------------------------------------------------------------------------
 template <int LOC, int HUC, bool TRID>
 __device__ void band_factor(double* __restrict__ a, int64_t ldab, int64_t* __restrict__ P, int64_t n,
@@ -86,6 +126,7 @@ __device__ void band_factor(double* __restrict__ a, int64_t ldab, int64_t* __res
         for (int64_t i = 0; i < n; ++i) P[i] = i;
         return;
     }
+    constexpr int PD = band_prefetch<LOC, HUC>();
     double W[LOC + 1][HUC + 1];
 #pragma unroll
     for (int r = 0; r <= LOC; ++r)
@@ -94,96 +135,102 @@ __device__ void band_factor(double* __restrict__ a, int64_t ldab, int64_t* __res
             const bool in = r <= lo && c <= hu && r < n && c < n && c - r <= hi;
             W[r][c] = in ? a[r + c * ldab] : 0.0;
         }
-    for (int64_t j = 0; j < n; ++j) {
-        const int rlim = (int)lmin(lo + 1, n - j);  // rows j..j+rlim-1
-        const int clim = (int)lmin(hu + 1, n - j);  // columns j..j+clim-1
-        if (j + 1 < n) {
-            if (TRID) {
-                const bool pivot = fabs(W[1][0]) > fabs(W[0][0]);
-                if (pivot) {
+    double pre[PD][HUC + 1];
 #pragma unroll
-                    for (int c = 0; c <= 2; ++c) {
-                        const double t = W[0][c];
-                        W[0][c] = W[1][c];
-                        W[1][c] = t;
-                    }
-                }
-                P[j] = j + (pivot ? 1 : 0);
-                if (fabs(W[0][0]) < DBL_MIN) {
-                    W[0][0] = 0.0;
-                    W[1][0] = 0.0;
-                } else {
-                    W[1][0] = W[1][0] / W[0][0];
-                }
-                W[1][1] = msub(W[1][1], W[1][0], W[0][1]);
-                if (pivot && j + 2 < n) W[1][2] = msub(W[1][2], W[1][0], W[0][2]);
-            } else {
-                // first strict maximum of |A(j..j+rlim-1, j)|
-                double piv = fabs(W[0][0]);
-                int ip = 0;
+    for (int u = 0; u < PD; ++u) band_load_row<HUC>(a, ldab, n, lo, hu, u, pre[u]);
+    for (int64_t j0 = 0; j0 < n; j0 += PD) {
 #pragma unroll
-                for (int r = 1; r <= LOC; ++r) {
-                    const double v = fabs(W[r][0]);
-                    if (r < rlim && v > piv) {
-                        piv = v;
-                        ip = r;
-                    }
-                }
-                if (piv < DBL_MIN) {  // TMV_Underflow: zero the column, no interchange
-                    ip = 0;
+        for (int u = 0; u < PD; ++u) {
+            const int64_t j = j0 + u;
+            if (j >= n) break;
+            const int rlim = (int)lmin(lo + 1, n - j);  // rows j..j+rlim-1
+            const int clim = (int)lmin(hu + 1, n - j);  // columns j..j+clim-1
+            if (j + 1 < n) {
+                if (TRID) {
+                    const bool pivot = abs_greater(W[1][0], W[0][0]);
+                    if (pivot) {
 #pragma unroll
-                    for (int r = 0; r <= LOC; ++r)
-                        if (r < rlim) W[r][0] = 0.0;
-                }
-#pragma unroll
-                for (int r = 1; r <= LOC; ++r)
-                    if (r == ip)
-#pragma unroll
-                        for (int c = 0; c <= HUC; ++c) {
+                        for (int c = 0; c <= 2; ++c) {
                             const double t = W[0][c];
-                            W[0][c] = W[r][c];
-                            W[r][c] = t;
+                            W[0][c] = W[1][c];
+                            W[1][c] = t;
                         }
-                P[j] = j + ip;
-                const double ujj = W[0][0];
-                if (ujj != 0.0) {
-                    const double inv = 1.0 / ujj;
+                    }
+                    P[j] = j + (pivot ? 1 : 0);
+                    if (underflows(W[0][0])) {
+                        W[0][0] = 0.0;
+                        W[1][0] = 0.0;
+                    } else {
+                        W[1][0] = W[1][0] / W[0][0];
+                    }
+                    W[1][1] = msub(W[1][1], W[1][0], W[0][1]);
+                    if (pivot && j + 2 < n) W[1][2] = msub(W[1][2], W[1][0], W[0][2]);
+                } else {
+                    // first strict maximum of |A(j..j+rlim-1, j)|
+                    double piv = W[0][0];
+                    int ip = 0;
 #pragma unroll
                     for (int r = 1; r <= LOC; ++r)
-                        if (r < rlim) W[r][0] = scale_by(W[r][0], inv);
-                }
-                // outer-product update, a column with a zero U(j,c) left alone
+                        if (r < rlim && abs_greater(W[r][0], piv)) {
+                            piv = W[r][0];
+                            ip = r;
+                        }
+                    if (underflows(piv)) {  // TMV_Underflow: zero the column, no interchange
+                        ip = 0;
 #pragma unroll
-                for (int c = 1; c <= HUC; ++c) {
-                    const double u = W[0][c];
-                    if (c < clim && u != 0.0)
+                        for (int r = 0; r <= LOC; ++r)
+                            if (r < rlim) W[r][0] = 0.0;
+                    }
+#pragma unroll
+                    for (int r = 1; r <= LOC; ++r)
+                        if (r == ip)
+#pragma unroll
+                            for (int c = 0; c <= HUC; ++c) {
+                                const double t = W[0][c];
+                                W[0][c] = W[r][c];
+                                W[r][c] = t;
+                            }
+                    P[j] = j + ip;
+                    const double ujj = W[0][0];
+                    if (nonzero(ujj)) {
+                        const double inv = 1.0 / ujj;
 #pragma unroll
                         for (int r = 1; r <= LOC; ++r)
-                            if (r < rlim) W[r][c] = msub(W[r][c], W[r][0], u);
+                            if (r < rlim) W[r][0] = scale_by(W[r][0], inv);
+                    }
+                    // outer-product update, a column with a zero U(j,c) left alone
+#pragma unroll
+                    for (int c = 1; c <= HUC; ++c) {
+                        const double uc = W[0][c];
+                        if (c < clim && nonzero(uc))
+#pragma unroll
+                            for (int r = 1; r <= LOC; ++r)
+                                if (r < rlim) W[r][c] = msub(W[r][c], W[r][0], uc);
+                    }
                 }
+            } else {
+                P[j] = j;
             }
-        } else {
-            P[j] = j;
+            // column j (L and U(j,j)) and row j of U leave the window
+#pragma unroll
+            for (int r = 0; r <= LOC; ++r)
+                if (r < rlim) a[(j + r) + j * ldab] = W[r][0];
+#pragma unroll
+            for (int c = 1; c <= HUC; ++c)
+                if (c < clim) a[j + (j + c) * ldab] = W[0][c];
+            if (j + 1 == n) break;
+#pragma unroll
+            for (int r = 0; r <= LOC; ++r)
+#pragma unroll
+                for (int c = 0; c <= HUC; ++c) W[r][c] = (r < LOC && c < HUC) ? W[r + 1][c + 1] : 0.0;
+#pragma unroll
+            for (int r = 0; r <= LOC; ++r)
+                if (r == lo)
+#pragma unroll
+                    for (int c = 0; c <= HUC; ++c)
+                        if (c <= hu) W[r][c] = pre[u][c];
+            band_load_row<HUC>(a, ldab, n, lo, hu, j + PD, pre[u]);
         }
-        // column j (L and U(j,j)) and row j of U leave the window
-#pragma unroll
-        for (int r = 0; r <= LOC; ++r)
-            if (r < rlim) a[(j + r) + j * ldab] = W[r][0];
-#pragma unroll
-        for (int c = 1; c <= HUC; ++c)
-            if (c < clim) a[j + (j + c) * ldab] = W[0][c];
-        if (j + 1 == n) break;
-#pragma unroll
-        for (int r = 0; r <= LOC; ++r)
-#pragma unroll
-            for (int c = 0; c <= HUC; ++c) W[r][c] = (r < LOC && c < HUC) ? W[r + 1][c + 1] : 0.0;
-        const int64_t nr = j + 1 + lo;
-#pragma unroll
-        for (int r = 0; r <= LOC; ++r)
-            if (r == lo)
-#pragma unroll
-                for (int c = 0; c <= HUC; ++c)
-                    if (c <= hu) W[r][c] = (nr < n && j + 1 + c < n) ? a[nr + (j + 1 + c) * ldab] : 0.0;
     }
 }
 
@@ -196,18 +243,55 @@ __device__ void band_factor(double* __restrict__ a, int64_t ldab, int64_t* __res
 // (DoDiagLDivEq1, src/TMV_DiagMatrix.cpp:296-341); otherwise the column form
 // (zero entries skipped) or, for the tridiagonal algorithm, the row form,
 // each with its window x[k] = b[j-k] (column) or b[i+k] (row) in registers.
-// Returns 0, 1 for a zero U(j,j) where TMV throws SingularBandLU, or 2 for
-// an interchange P[j] outside rows j..min(j+lo, n-1) (factors not made by
-// the band LU), which is not applied.
+// The loads of each step (interchange, L or U column, entering b) are issued
+// PD steps ahead.  Returns 0, 1 for a zero U(j,j) where TMV throws
+// SingularBandLU, or 2 for an interchange P[j] outside rows
+// j..min(j+lo, n-1) (factors not made by the band LU), which is not applied.
 // ---------------------------------------------------------------------------
+template <int LOC>
+struct FwdLoads {
+    int64_t p;
+    double l[LOC + 1];  // L(j+r, j), r = 1..lo
+    double bn;          // b[j+1+lo]
+};
+
+template <int LOC>
+__device__ __forceinline__ void band_fwd_load(const double* __restrict__ a, int64_t ldab,
+                                              const int64_t* __restrict__ P, const double* __restrict__ b,
+                                              int64_t n, int lo, int64_t j, FwdLoads<LOC>& f)
+{
+    f.p = j + 1 < n ? P[j] : j;
+#pragma unroll
+    for (int r = 1; r <= LOC; ++r) f.l[r] = (r <= lo && j + r < n) ? a[(j + r) + j * ldab] : 0.0;
+    const int64_t nr = j + 1 + lo;
+    f.bn = nr < n ? b[nr] : 0.0;
+}
+
+template <int HUC>
+struct BwdLoads {
+    double u[HUC + 1];  // U(j-k, j), k = 0..hu (u[0] = U(j,j))
+    double bn;          // b[j-1-hu]
+};
+
+template <int HUC>
+__device__ __forceinline__ void band_bwd_load(const double* __restrict__ a, int64_t ldab,
+                                              const double* __restrict__ b, int hu, int64_t j, BwdLoads<HUC>& f)
+{
+#pragma unroll
+    for (int k = 0; k <= HUC; ++k) f.u[k] = (k <= hu && j - k >= 0 && j >= 0) ? a[(j - k) + j * ldab] : 0.0;
+    const int64_t nr = j - 1 - hu;
+    f.bn = (nr >= 0 && j >= 0) ? b[nr] : 0.0;
+}
+
 template <int LOC, int HUC, bool TRID>
 __device__ int band_solve_one(const double* __restrict__ a, int64_t ldab, const int64_t* __restrict__ P,
-                               int64_t n, int lo, int hu, double* __restrict__ b)
+                              int64_t n, int lo, int hu, double* __restrict__ b)
 {
+    constexpr int PD = band_prefetch<LOC, HUC>();
     int64_t last_nz = -1;
     if (lo == 0) {
         for (int64_t j = n - 1; j >= 0; --j)
-            if (b[j] != 0.0) {
+            if (nonzero(b[j])) {
                 last_nz = j;
                 break;
             }
@@ -215,33 +299,43 @@ __device__ int band_solve_one(const double* __restrict__ a, int64_t ldab, const 
         double y[LOC + 1];
 #pragma unroll
         for (int r = 0; r <= LOC; ++r) y[r] = (r <= lo && r < n) ? b[r] : 0.0;
-        for (int64_t j = 0; j < n; ++j) {
-            if (j + 1 < n) {
-                const int64_t pj = P[j];
-                if (pj < j || pj > j + lo || pj >= n) return 2;
-                const int d = (int)(pj - j);
+        FwdLoads<LOC> f[PD];
 #pragma unroll
-                for (int r = 1; r <= LOC; ++r)
-                    if (r == d) {
-                        const double t = y[0];
-                        y[0] = y[r];
-                        y[r] = t;
-                    }
-                const double bj = y[0];
-                if (bj != 0.0)
+        for (int u = 0; u < PD; ++u) band_fwd_load<LOC>(a, ldab, P, b, n, lo, u, f[u]);
+        for (int64_t j0 = 0; j0 < n; j0 += PD) {
+#pragma unroll
+            for (int u = 0; u < PD; ++u) {
+                const int64_t j = j0 + u;
+                if (j >= n) break;
+                if (j + 1 < n) {
+                    const int64_t pj = f[u].p;
+                    if (pj < j || pj > j + lo || pj >= n) return 2;
+                    const int d = (int)(pj - j);
 #pragma unroll
                     for (int r = 1; r <= LOC; ++r)
-                        if (r <= lo && j + r < n) y[r] = msub(y[r], a[(j + r) + j * ldab], bj);
+                        if (r == d) {
+                            const double t = y[0];
+                            y[0] = y[r];
+                            y[r] = t;
+                        }
+                    const double bj = y[0];
+                    if (nonzero(bj))
+#pragma unroll
+                        for (int r = 1; r <= LOC; ++r)
+                            if (r <= lo && j + r < n) y[r] = msub(y[r], f[u].l[r], bj);
+                }
+                b[j] = y[0];
+                if (nonzero(y[0])) last_nz = j;
+                const double bn = f[u].bn;
+#pragma unroll
+                for (int r = 0; r < LOC; ++r) y[r] = y[r + 1];
+                y[LOC] = 0.0;
+#pragma unroll
+                for (int r = 0; r <= LOC; ++r)
+                    if (r == lo) y[r] = bn;
+                // b[j+1+lo+PD] is not yet touched: the window covers rows up to j+1+lo
+                band_fwd_load<LOC>(a, ldab, P, b, n, lo, j + PD, f[u]);
             }
-            b[j] = y[0];
-            if (y[0] != 0.0) last_nz = j;
-#pragma unroll
-            for (int r = 0; r < LOC; ++r) y[r] = y[r + 1];
-            y[LOC] = 0.0;
-            const int64_t nr = j + 1 + lo;
-#pragma unroll
-            for (int r = 0; r <= LOC; ++r)
-                if (r == lo) y[r] = nr < n ? b[nr] : 0.0;
         }
     }
     const int64_t i2 = last_nz + 1;
@@ -249,7 +343,7 @@ __device__ int band_solve_one(const double* __restrict__ a, int64_t ldab, const 
     if (hu == 0) {
         for (int64_t i = 0; i < i2; ++i) {
             const double d = a[i + i * ldab];
-            if (d == 0.0) return 1;
+            if (!nonzero(d)) return 1;
             b[i] = b[i] / d;
         }
         return 0;
@@ -263,7 +357,7 @@ __device__ int band_solve_one(const double* __restrict__ a, int64_t ldab, const 
             if (len >= 1) v = msub(v, x1, a[i + (i + 1) * ldab]);
             if (len >= 2) v = msub(v, x2, a[i + (i + 2) * ldab]);
             const double d = a[i + i * ldab];
-            if (d == 0.0) return 1;
+            if (!nonzero(d)) return 1;
             v = v / d;
             b[i] = v;
             x2 = x1;
@@ -277,25 +371,35 @@ __device__ int band_solve_one(const double* __restrict__ a, int64_t ldab, const 
 #pragma unroll
         for (int k = 0; k <= HUC; ++k) x[k] = (k <= hu && j - k >= 0) ? b[j - k] : 0.0;
     }
-    for (int64_t j = i2 - 1; j >= 0; --j) {
-        const double bj0 = x[0];
-        if (bj0 != 0.0) {
-            const double d = a[j + j * ldab];
-            if (d == 0.0) return 1;
-            const double bj = bj0 / d;
-            x[0] = bj;
+    BwdLoads<HUC> f[PD];
 #pragma unroll
-            for (int k = 1; k <= HUC; ++k)
-                if (k <= hu && j - k >= 0) x[k] = msub(x[k], bj, a[(j - k) + j * ldab]);
+    for (int u = 0; u < PD; ++u) band_bwd_load<HUC>(a, ldab, b, hu, i2 - 1 - u, f[u]);
+    for (int64_t j0 = i2 - 1; j0 >= 0; j0 -= PD) {
+#pragma unroll
+        for (int u = 0; u < PD; ++u) {
+            const int64_t j = j0 - u;
+            if (j < 0) break;
+            const double bj0 = x[0];
+            if (nonzero(bj0)) {
+                const double d = f[u].u[0];
+                if (!nonzero(d)) return 1;
+                const double bj = bj0 / d;
+                x[0] = bj;
+#pragma unroll
+                for (int k = 1; k <= HUC; ++k)
+                    if (k <= hu && j - k >= 0) x[k] = msub(x[k], bj, f[u].u[k]);
+            }
+            b[j] = x[0];
+            const double bn = f[u].bn;
+#pragma unroll
+            for (int k = 0; k < HUC; ++k) x[k] = x[k + 1];
+            x[HUC] = 0.0;
+#pragma unroll
+            for (int k = 0; k <= HUC; ++k)
+                if (k == hu) x[k] = bn;
+            // b[j-1-hu-PD] is below the window: not yet touched by this pass
+            band_bwd_load<HUC>(a, ldab, b, hu, j - PD, f[u]);
         }
-        b[j] = x[0];
-#pragma unroll
-        for (int k = 0; k < HUC; ++k) x[k] = x[k + 1];
-        x[HUC] = 0.0;
-        const int64_t nr = j - 1 - hu;
-#pragma unroll
-        for (int k = 0; k <= HUC; ++k)
-            if (k == hu) x[k] = nr >= 0 ? b[nr] : 0.0;
     }
     return 0;
 }

@@ -452,35 +452,41 @@ __global__ void zlu_swap_rest_kernel(int64_t c0, int64_t c1, double2* A, int64_t
     }
 }
 
-// U12 = L11^-1 A12 (L11 unit lower, KB x KB), one column of A12 per thread,
-// the column held in registers.
+// U12 = L11^-1 A12 (L11 unit lower, KB x KB) for the columns [c0, c1): a
+// warp per column, lane r holding row r; at step q lane q's entry is final and
+// is broadcast by shuffle, and the lanes below subtract L(r, q) x_q.  (One
+// column per thread kept the 32-step chain of four dependent DFMA per step in
+// one lane: about 60 us for a 32-column narrow update on the look-ahead
+// chain; a warp per column takes a few.)
+constexpr int kZTrsmWarps = 4;
 template <int KB>
-__global__ void __launch_bounds__(64) zlu_trsm_kernel(int64_t c1, double2* A, int64_t lda, int64_t k, int64_t c0)
+__global__ void __launch_bounds__(32 * kZTrsmWarps)
+zlu_trsm_kernel(int64_t c1, double2* A, int64_t lda, int64_t k, int64_t c0)
 {
+    static_assert(KB <= 32, "a lane per row");
     __shared__ double2 s_l[KB][KB + 1];
     for (int t = threadIdx.x; t < KB * KB; t += blockDim.x) {
         const int r = t % KB, q = t / KB;
         s_l[r][q] = A[(k + r) + (k + q) * lda];
     }
     __syncthreads();
-    const int64_t col = c0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t col = c0 + (int64_t)blockIdx.x * kZTrsmWarps + warp;
     if (col >= c1) return;
     double2* a = A + k + col * lda;
-    double2 x[KB];
+    double2 x = lane < KB ? a[lane] : make_double2(0.0, 0.0);
 #pragma unroll
-    for (int r = 0; r < KB; ++r) x[r] = a[r];
-#pragma unroll
-    for (int q = 0; q < KB; ++q)
-#pragma unroll
-        for (int r = q + 1; r < KB; ++r) {
-            const double2 l = s_l[r][q];
-            x[r].x = fma(-l.x, x[q].x, x[r].x);
-            x[r].x = fma(l.y, x[q].y, x[r].x);
-            x[r].y = fma(-l.x, x[q].y, x[r].y);
-            x[r].y = fma(-l.y, x[q].x, x[r].y);
+    for (int q = 0; q < KB; ++q) {
+        const double xr = __shfl_sync(0xffffffffu, x.x, q), xi = __shfl_sync(0xffffffffu, x.y, q);
+        if (lane > q && lane < KB) {
+            const double2 l = s_l[lane][q];
+            x.x = fma(-l.x, xr, x.x);
+            x.x = fma(l.y, xi, x.x);
+            x.y = fma(-l.x, xi, x.y);
+            x.y = fma(-l.y, xr, x.y);
         }
-#pragma unroll
-    for (int r = 0; r < KB; ++r) a[r] = x[r];
+    }
+    if (lane < KB) a[lane] = x;
 }
 
 // A22 -= L21 U12 (K = KB): 64 x 64 complex tiles, each of the 256 threads a
@@ -630,7 +636,8 @@ static tmvg_status zlu_factor_blocked(Context* c, int64_t n, double2* A, int64_t
     // step k's U12 and product for the columns [c0, c1) (k + KB <= c0)
     auto update = [&](int64_t k, int64_t c0, int64_t c1) {
         if (c1 <= c0 || k + KB >= n) return;
-        zlu_trsm_kernel<KB><<<(unsigned)ceil_div(c1 - c0, 64), 64, 0, c->stream>>>(c1, A, lda, k, c0);
+        zlu_trsm_kernel<KB><<<(unsigned)ceil_div(c1 - c0, kZTrsmWarps), 32 * kZTrsmWarps, 0, c->stream>>>(
+            c1, A, lda, k, c0);
         const dim3 grid((unsigned)ceil_div(n - k - KB, kZgBM), (unsigned)ceil_div(c1 - c0, kZgBN));
         zlu_gemm_kernel<KB><<<grid, 256, 0, c->stream>>>(n, A, lda, k, c0, c1);
         c->launches += 2;
@@ -788,17 +795,24 @@ __global__ void zlu_diag_inverse_kernel(int64_t n, const double2* __restrict__ L
 }
 
 // One 64-row diagonal block [k, k+w) of the unit lower (upper = false) or
-// non-unit upper triangle for columns [q0, q0 + 4) of X (n x nrhs, ld n).
+// non-unit upper triangle for columns [q0, q0 + 4) of X (n x nrhs, ld n); the
+// block's triangle is staged in shared memory first (dynamic, 64 x 65
+// entries), so that the 64 steps read it at shared-memory latency.
 __global__ void __launch_bounds__(kZSolveBlock * kZSolveCols)
 zlu_diag_solve_kernel(int64_t n, const double2* __restrict__ LU, int64_t lda, const double2* __restrict__ dinv,
                       int64_t k, int w, bool upper, int64_t nrhs, double2* X, int* err)
 {
     __shared__ double2 xs[kZSolveBlock][kZSolveCols];
+    extern __shared__ double2 s_tri[];  // [kZSolveBlock][kZSolveBlock + 1]
     const int i = threadIdx.x % kZSolveBlock, ql = threadIdx.x / kZSolveBlock;
     const int64_t q = (int64_t)blockIdx.x * kZSolveCols + ql;
     const bool mine = i < w && q < nrhs;
     double2* x = X + k + q * n;
     xs[i][ql] = mine ? x[i] : make_double2(0.0, 0.0);
+    for (int t = threadIdx.x; t < w * w; t += kZSolveBlock * kZSolveCols) {
+        const int r = t % w, cc = t / w;
+        s_tri[r * (kZSolveBlock + 1) + cc] = LU[(k + r) + (k + cc) * lda];
+    }
     bool sing = false;
     __syncthreads();
     for (int s = 0; s < w; ++s) {
@@ -807,7 +821,7 @@ zlu_diag_solve_kernel(int64_t n, const double2* __restrict__ LU, int64_t lda, co
             if (i == j && mine) {
                 const double2 v = xs[j][ql];
                 if (znonzero(v)) {
-                    const double2 d = LU[(k + j) + (k + j) * lda];
+                    const double2 d = s_tri[j * (kZSolveBlock + 1) + j];
                     if (!znonzero(d)) sing = true;
                     else xs[j][ql] = zmul(v, dinv[k + j]);
                 }
@@ -816,7 +830,8 @@ zlu_diag_solve_kernel(int64_t n, const double2* __restrict__ LU, int64_t lda, co
         }
         const double2 xj = xs[j][ql];
         const bool below = upper ? i < j : i > j;
-        if (mine && below && znonzero(xj)) xs[i][ql] = zsub(xs[i][ql], zmul(xj, LU[(k + i) + (k + j) * lda]));
+        if (mine && below && znonzero(xj))
+            xs[i][ql] = zsub(xs[i][ql], zmul(xj, s_tri[i * (kZSolveBlock + 1) + j]));
         __syncthreads();
     }
     if (sing) atomicCAS(err, (int)kDevOk, (int)kDevSingular);
@@ -934,11 +949,16 @@ static tmvg_status zlu_ldiveq_blocked(Context* c, int64_t n, const double2* LU, 
     c->launches += 2;
     if ((st = check_cuda(c, cudaGetLastError(), "lu_ldiveq_z: gather"))) return st;
     const unsigned gq = (unsigned)ceil_div(nrhs, kZSolveCols);
+    const size_t tri_smem = sizeof(double2) * kZSolveBlock * (kZSolveBlock + 1);
+    if ((st = check_cuda(c, cudaFuncSetAttribute(zlu_diag_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)tri_smem),
+                         "lu_ldiveq_z: smem attribute")))
+        return st;
     // L (unit lower), blocks in order
     for (int64_t k = 0; k < n; k += kZSolveBlock) {
         const int w = (int)std::min<int64_t>(kZSolveBlock, n - k);
-        zlu_diag_solve_kernel<<<gq, kZSolveBlock * kZSolveCols, 0, c->stream>>>(n, LU, lda, dinv, k, w, false,
-                                                                                 nrhs, X, c->dflags);
+        zlu_diag_solve_kernel<<<gq, kZSolveBlock * kZSolveCols, tri_smem, c->stream>>>(n, LU, lda, dinv, k, w,
+                                                                                        false, nrhs, X, c->dflags);
         ++c->launches;
         if ((st = check_cuda(c, cudaGetLastError(), "lu_ldiveq_z: diagonal block"))) return st;
         if ((st = zgemm_sub(c, n - k - w, nrhs, w, LU + (k + w) + k * lda, lda, X + k, n, X + k + w, n))) return st;
@@ -946,8 +966,8 @@ static tmvg_status zlu_ldiveq_blocked(Context* c, int64_t n, const double2* LU, 
     // U (non-unit upper), blocks from the last
     for (int64_t k = ((n - 1) / kZSolveBlock) * kZSolveBlock; k >= 0; k -= kZSolveBlock) {
         const int w = (int)std::min<int64_t>(kZSolveBlock, n - k);
-        zlu_diag_solve_kernel<<<gq, kZSolveBlock * kZSolveCols, 0, c->stream>>>(n, LU, lda, dinv, k, w, true,
-                                                                                 nrhs, X, c->dflags);
+        zlu_diag_solve_kernel<<<gq, kZSolveBlock * kZSolveCols, tri_smem, c->stream>>>(n, LU, lda, dinv, k, w,
+                                                                                        true, nrhs, X, c->dflags);
         ++c->launches;
         if ((st = check_cuda(c, cudaGetLastError(), "lu_ldiveq_z: diagonal block"))) return st;
         if ((st = zgemm_sub(c, k, nrhs, w, LU + k * lda, lda, X + k, n, X, n))) return st;
