@@ -234,6 +234,8 @@ def run_gpu(args) -> dict:
         return {"path": args.path, "fp64_peak": dict(FP64_PEAK), "workloads": w} if rank == 0 else None
 
     if args.path == "batched":
+        h = linalg.handle(local)
+        FP64_PEAK.update({"tflops": round(h.fp64_rate(), 4), "source": "tmvg_probe_fp64_rate in this run"})
         b = batched_bench(dev, args, with_cpu=(rank == 0 and not args.no_cpu_baseline))
         out = {"metric": "batched uneven FP64 LU solves/s", "value": b["value"], "unit": "solves/s",
                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,

@@ -22,6 +22,8 @@
 // FP64 FMA throughput (about 2 per SM per clock on GB300) bounds the kernel.
 // PW (8 or 16) is chosen per size class by the plan's tuner.
 #include "batched.cuh"
+
+#include <type_traits>
 #include "lu.cuh"
 #include "pivots.cuh"
 
@@ -97,6 +99,11 @@ constexpr bool kStageU12 = sizeof(T) == 4;
 // The blocked LU of one system in place (A n x n column-major, element type
 // T), pivots to P; the interchanges are also applied to the r columns of B
 // (B may be null with r = 0).  Pivot keys compare in FP64 for either T.
+// x != 0 on the integer pipe (a double comparison takes an FP64 issue slot,
+// which the substitutions' products need): the bits without the sign.
+__device__ __forceinline__ bool nz(double x) { return (__double_as_longlong(x) << 1) != 0; }
+__device__ __forceinline__ bool nz(float x) { return (__float_as_uint(x) << 1) != 0u; }
+
 template <typename T, int PW>
 __device__ void factor_one(int64_t n, int64_t r, T* __restrict__ A, T* __restrict__ B,
                            int64_t* __restrict__ P, T* smem)
@@ -104,9 +111,9 @@ __device__ void factor_one(int64_t n, int64_t r, T* __restrict__ A, T* __restric
     constexpr int LDP = PW + 1;
     T* pan = smem;  // [256][LDP]
     T* u12s = smem + kBatchMaxN * LDP;  // FP32 only: U12 rows [PW][256]
-    __shared__ double s_key[kBatchThreads / 32];
+    __shared__ long long s_key[kBatchThreads / 32];
     __shared__ long long s_idx[kBatchThreads / 32];
-    __shared__ double w_key;
+    __shared__ long long w_key;
     __shared__ long long w_idx;
     __shared__ int s_piv[PW];
     __shared__ int s_pairs[1 + 2 * kMaxPairs];
@@ -134,23 +141,25 @@ __device__ void factor_one(int64_t n, int64_t r, T* __restrict__ A, T* __restric
         __syncthreads();
         for (int j = 0; j < w; ++j) {
             const bool r2 = r2_column(n, k0 + j) && !prev_uf;
-            double bk = -INFINITY;
+            long long bk = LLONG_MIN;
             long long bi = LLONG_MAX;
             for (int rr = j + tid; rr < m; rr += kBatchThreads)
-                pivot_combine(bk, bi, pivot_key(pan[rr * LDP + j], rr == j, r2), (long long)rr);
-            warp_pivot_reduce(bk, bi);
+                pivot_icombine(bk, bi, pivot_ikey(pan[rr * LDP + j], rr == j, r2), (long long)rr);
+            warp_pivot_ireduce(bk, bi);
             if (lane == 0) { s_key[warp] = bk; s_idx[warp] = bi; }
             __syncthreads();
             if (warp == 0) {
-                bk = lane < kBatchThreads / 32 ? s_key[lane] : -INFINITY;
+                bk = lane < kBatchThreads / 32 ? s_key[lane] : LLONG_MIN;
                 bi = lane < kBatchThreads / 32 ? s_idx[lane] : LLONG_MAX;
-                warp_pivot_reduce(bk, bi);
+                warp_pivot_ireduce(bk, bi);
                 if (lane == 0) { w_key = bk; w_idx = bi; }
             }
             __syncthreads();
-            const double wk = w_key;
             const int wi = (int)w_idx;
-            if (underflows<T>(wk)) {
+            // the winning key is the bits of |pivot| (0 or inf bits for a NaN
+            // first element): TMV_Underflow is a comparison of bit patterns
+            if (w_key < __double_as_longlong(std::is_same<T, double>::value ? 2.2250738585072014e-308
+                                                                            : 1.1754943508222875e-38)) {
                 if (tid == 0) s_piv[j] = (int)(k0 + j);
                 for (int rr = j + tid; rr < m; rr += kBatchThreads) pan[rr * LDP + j] = T(0);
                 prev_uf = true;
@@ -332,7 +341,7 @@ __device__ void lu_solve_staged(int64_t n, int64_t r, const T* __restrict__ LU, 
                 T* xq = xs + lane * XS + j0;
                 for (int k = 0; k < jb; ++k) {
                     const T xk = xq[k];
-                    if (xk != T(0))
+                    if (nz(xk))
                         for (int i = k + 1; i < jb; ++i) xq[i] -= dg[i * DS + k] * xk;
                 }
             }
@@ -350,7 +359,7 @@ __device__ void lu_solve_staged(int64_t n, int64_t r, const T* __restrict__ LU, 
 #pragma unroll
                     for (int u = 0; u < PF; ++u) {
                         const T xk = k0 + u < jb ? xq[k0 + u] : T(0);
-                        if (xk != T(0)) v -= lv[u] * xk;
+                        if (nz(xk)) v -= lv[u] * xk;
                     }
                 }
                 xs[q * XS + i] = v;
@@ -366,12 +375,12 @@ __device__ void lu_solve_staged(int64_t n, int64_t r, const T* __restrict__ LU, 
                 T* xq = xs + lane * XS + j0;
                 for (int k = jb - 1; k >= 0; --k) {
                     T v = xq[k];
-                    if (v != T(0)) {
+                    if (nz(v)) {
                         const T d = dg[k * DS + k];
-                        if (d == T(0)) *sing = 1;
+                        if (!nz(d)) *sing = 1;
                         else xq[k] = v = v / d;
                     }
-                    if (v != T(0))
+                    if (nz(v))
                         for (int i = 0; i < k; ++i) xq[i] -= dg[i * DS + k] * v;
                 }
             }
@@ -394,7 +403,7 @@ __device__ void lu_solve_staged(int64_t n, int64_t r, const T* __restrict__ LU, 
                     for (int u = 0; u < PF; ++u) {
                         const int k = kt - 1 - u;
                         const T xk = k >= 0 ? xq[k] : T(0);
-                        if (xk != T(0)) v -= uv[u] * xk;
+                        if (nz(xk)) v -= uv[u] * xk;
                     }
                 }
                 xs[q * XS + i] = v;

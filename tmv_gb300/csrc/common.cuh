@@ -199,6 +199,37 @@ __device__ __forceinline__ void warp_pivot_reduce(double& k, I& i)
     }
 }
 
+// The same keys as ordered 64-bit integers, for reductions that should not
+// take FP64 issue slots (a double comparison occupies the FP64 pipe, which
+// GB300 issues at 2 per SM per clock): the bits of |v| (non-negative doubles
+// order like their bit patterns), the bits of +inf or 0 for a NaN first
+// element, -1 for a NaN elsewhere.
+template <typename T>
+__device__ __forceinline__ long long pivot_ikey(T v, bool first, bool r2mode)
+{
+    const long long b = __double_as_longlong((double)v) & 0x7fffffffffffffffLL;
+    if (b > 0x7ff0000000000000LL) return first ? (r2mode ? 0LL : 0x7ff0000000000000LL) : -1LL;
+    return b;
+}
+
+__device__ __forceinline__ void pivot_icombine(long long& k, long long& i, long long k2, long long i2)
+{
+    if (k2 > k || (k2 == k && i2 < i)) {
+        k = k2;
+        i = i2;
+    }
+}
+
+__device__ __forceinline__ void warp_pivot_ireduce(long long& k, long long& i)
+{
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const long long k2 = __shfl_xor_sync(0xffffffffu, k, off);
+        const long long i2 = __shfl_xor_sync(0xffffffffu, i, off);
+        pivot_icombine(k, i, k2, i2);
+    }
+}
+
 // TMV_Underflow for a real pivot magnitude a = |piv| (include/tmv/TMV_Base.h:
 // 692-696, where TMV_ABS2 of a real is its absolute value, :330-331):
 // a < numeric_limits<T>::min().  NaN never underflows.
