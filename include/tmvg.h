@@ -163,7 +163,8 @@ tmvg_status tmvg_lu_decompose_f64_host(tmvg_handle h, int64_t n, double* A,
  * this library holds until the process exits; each call looks up the array's
  * device address in the current context.  Runs on the current device and
  * the given cudaStream_t (NULL: legacy default stream) and synchronises that
- * stream before it returns.  Limit: n <= 16384, and a panel CTA's rows must
+ * stream before it returns (so it cannot be called while the stream is being
+ * captured into a CUDA graph).  Limit: n <= 16384, and a panel CTA's rows must
  * fit in 200 KiB of shared memory (every n <= 16384 does on a GPU with at
  * least 40 SMs); other sizes return TMVG_UNSUPPORTED before any device work.
  * Calls share the array, so calls that overlap on the GPU (other threads or

@@ -2079,15 +2079,23 @@ static tmvg_status launch_panel_cluster_reg(Context* c, cudaStream_t s, T* A, in
                                             int* pairs, float* ahi, float* alo, const T* Sp = nullptr,
                                             int64_t lds = 0)
 {
-    // the leaf panel: one row per thread, in the smallest power-of-two
+    // FP32 leaf panel: one row per thread, in the smallest power-of-two
     // cluster whose CTAs hold the panel's rows (16 at m = 8192, 8 from 4096
     // rows down, ... one CTA, with no cluster exchange, at 512 rows): the
-    // exchange of a column costs less with fewer CTAs.  The two-rows-per-
-    // thread panel keeps 16 CTAs (a panel of at most 512 rows in one CTA).
+    // exchange of a column costs less with fewer CTAs.  FP64 panels spread
+    // their rows over 16 CTAs from 128 rows up: their in-panel products run
+    // on the FP64 pipe (2 per SM per clock), which fewer SMs would make the
+    // limit (n = 2048: 12.4 ms for the LU with the FP32 rule).  The
+    // two-rows-per-thread panel keeps 16 CTAs (a panel of at most 512 rows in
+    // one CTA).
     const int64_t m = n - k;
     int G = m <= 2 * kReg2Threads ? 1 : kClusterCtas;
-    if (!c->panel_reg2)
-        while (G > 1 && (int64_t)(G / 2) * kLeafThreads >= m) G /= 2;
+    if (!c->panel_reg2) {
+        if (sizeof(T) == 4)
+            while (G > 1 && (int64_t)(G / 2) * kLeafThreads >= m) G /= 2;
+        else
+            G = m <= 128 ? 1 : kClusterCtas;
+    }
     const int rpc = (int)ceil_div(m, G);
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
