@@ -103,3 +103,29 @@ def test_autotuned_plan_and_workload_properties(dev, orc):
     Xo = B.copy()
     assert not orc.batched_divide(n, r, a_off, b_off, A.copy(), Xo).any()
     assert np.abs(X - Xo).max() <= 1e-12 * np.abs(Xo).max()
+
+
+def test_tuned_widths_persist_per_device(dev, tmp_path, monkeypatch):
+    """The tuner writes its widths to the table named by TMVG_TUNE_CACHE
+    (keyed by SM count, size class and device name) and a later plan on the
+    same device takes them from there without timing."""
+    from tmv_gb300.batched import BatchPlan
+
+    table = tmp_path / "tune.txt"
+    monkeypatch.setenv("TMVG_TUNE_CACHE", str(table))
+    n = np.array([20, 40, 100, 200] * 8)
+    r = np.ones_like(n)
+    plan = BatchPlan(n, r, tune=True)
+    widths = plan.panel_widths
+    plan.close()
+    lines = [l.split() for l in table.read_text().splitlines() if l.strip()]
+    assert len(lines) == 4  # one entry per size class present
+    for l in lines:
+        assert int(l[2]) in (8, 16) and int(l[2]) == widths[int(l[1])]
+    # rewrite the table: the next plan must take these widths, untimed
+    forced = [(l[0], l[1], "8" if l[2] == "16" else "16", l[3], " ".join(l[4:])) for l in lines]
+    table.write_text("".join(" ".join(f) + "\n" for f in forced))
+    plan = BatchPlan(n, r, tune=True)
+    assert plan.panel_widths == [int(f[2]) for f in sorted(forced, key=lambda f: int(f[1]))]
+    plan.close()
+    monkeypatch.setenv("TMVG_TUNE_CACHE", "off")

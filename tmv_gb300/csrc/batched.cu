@@ -22,16 +22,20 @@
 // FP64 FMA throughput (about 2 per SM per clock on GB300) bounds the kernel.
 // PW (8 or 16) is chosen per size class by the plan's tuner.
 #include "batched.cuh"
-
-#include <type_traits>
 #include "lu.cuh"
 #include "pivots.cuh"
+
+#include <dlfcn.h>
 
 #include <algorithm>
 #include <chrono>
 #include <climits>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
+#include <string>
+#include <type_traits>
 #include <vector>
 
 namespace tmvg {
@@ -852,16 +856,91 @@ static tmvg_status run_plan(BatchPlan* p, double* A, double* B, int64_t* P, int*
     return check_cuda(c, cudaStreamSynchronize(c->stream), "batched: sync");
 }
 
+// The tuner's results persist in a small text table keyed by the device
+// (name and SM count) and the size class, so that a plan on the same kind of
+// GPU takes its panel widths without timing them again: one line
+// "<sms> <class> <width> <ms> <device name>" per entry.  The file is
+// $TMVG_TUNE_CACHE ("off" or empty: no table), by default tmvg_tune_cache.txt
+// beside this library.
+static std::string tune_cache_path()
+{
+    if (const char* e = std::getenv("TMVG_TUNE_CACHE")) {
+        if (!*e || std::strcmp(e, "off") == 0) return std::string();
+        return std::string(e);
+    }
+    Dl_info info;
+    if (dladdr((void*)&tune_cache_path, &info) && info.dli_fname) {
+        std::string lib(info.dli_fname);
+        const size_t slash = lib.rfind('/');
+        return (slash == std::string::npos ? std::string(".") : lib.substr(0, slash)) + "/tmvg_tune_cache.txt";
+    }
+    return std::string();
+}
+
+struct TuneEntry {
+    int sms, cls, width;
+    float ms;
+    std::string device;
+};
+
+static std::vector<TuneEntry> read_tune_cache(const std::string& path)
+{
+    std::vector<TuneEntry> out;
+    if (path.empty()) return out;
+    FILE* f = std::fopen(path.c_str(), "r");
+    if (!f) return out;
+    char line[512];
+    while (std::fgets(line, sizeof(line), f)) {
+        TuneEntry e;
+        int used = 0;
+        if (std::sscanf(line, "%d %d %d %f %n", &e.sms, &e.cls, &e.width, &e.ms, &used) < 4) continue;
+        if (e.cls < 0 || e.cls >= kNumClasses || (e.width != 8 && e.width != 16)) continue;
+        e.device = std::string(line + used);
+        while (!e.device.empty() && (e.device.back() == '\n' || e.device.back() == '\r')) e.device.pop_back();
+        out.push_back(e);
+    }
+    std::fclose(f);
+    return out;
+}
+
+static void write_tune_cache(const std::string& path, const std::vector<TuneEntry>& es)
+{
+    if (path.empty()) return;
+    const std::string tmp = path + ".tmp";
+    FILE* f = std::fopen(tmp.c_str(), "w");
+    if (!f) return;  // a read-only location: the table is an optimisation only
+    for (const TuneEntry& e : es) std::fprintf(f, "%d %d %d %.4f %s\n", e.sms, e.cls, e.width, e.ms, e.device.c_str());
+    const bool ok = std::fclose(f) == 0;
+    if (ok) std::rename(tmp.c_str(), path.c_str());
+    else std::remove(tmp.c_str());
+}
+
 // Time each panel width on the systems of each size class (a sample of at
-// most 256 of them, on scratch copies) and keep the fastest.
+// most 256 of them, on scratch copies) and keep the fastest; a class already
+// in the persisted table for this device takes its width from there.
 static tmvg_status tune(BatchPlan* p)
 {
     Context* c = p->c;
     const int cand[2] = {8, 16};
+    const std::string cache = tune_cache_path();
+    std::vector<TuneEntry> table = read_tune_cache(cache);
+    cudaDeviceProp prop;
+    std::string dev_name = "unknown";
+    if (cudaGetDeviceProperties(&prop, c->device) == cudaSuccess) dev_name = prop.name;
+    else cudaGetLastError();
+    bool table_changed = false;
     std::vector<std::vector<int64_t>> members(kNumClasses);
     for (int64_t s = 0; s < p->count; ++s) members[size_class(p->hn[s])].push_back(s);
     for (int k = 0; k < kNumClasses; ++k) {
         if (members[k].empty()) continue;
+        bool cached = false;
+        for (const TuneEntry& e : table)
+            if (e.sms == c->num_sms && e.cls == k && e.device == dev_name) {
+                p->pw[k] = e.width;
+                cached = true;
+                break;
+            }
+        if (cached) continue;
         const size_t take = std::min<size_t>(members[k].size(), 256);
         // scratch sub-batch: packed copies of the sampled systems
         std::vector<int64_t> n(take), r(take), ao(take), bo(take), po(take);
@@ -937,6 +1016,10 @@ static tmvg_status tune(BatchPlan* p)
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
             p->pw[k] = best;
+            if (!st) {
+                table.push_back({c->num_sms, k, best, best_ms, dev_name});
+                table_changed = true;
+            }
         }
         if (sub.exec) cudaGraphExecDestroy(sub.exec);
         if (sub.graph) cudaGraphDestroy(sub.graph);
@@ -945,6 +1028,7 @@ static tmvg_status tune(BatchPlan* p)
         cudaFree(sub.d_queue); cudaFree(dA); cudaFree(dB); cudaFree(dP); cudaFree(dS);
         if (st) return st;
     }
+    if (table_changed) write_tune_cache(cache, table);
     return TMVG_OK;
 }
 
