@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 namespace tmvg {
 
@@ -104,10 +105,11 @@ __global__ void gather_to_f32_kernel(int64_t n, const int* __restrict__ perm,
     if (i < n) v[i] = (float)b[(int64_t)perm[i] * inc];
 }
 
-// x (+)= (double) v32
+// x (+)= (double) v32 (nothing once *stop is set)
 __global__ void update_kernel(int64_t n, const float* __restrict__ v, double* __restrict__ x,
-                              int64_t inc, bool add)
+                              int64_t inc, bool add, const int* stop)
 {
+    if (stop && *stop) return;
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i < n) x[i * inc] = add ? x[i * inc] + (double)v[i] : (double)v[i];
 }
@@ -115,8 +117,10 @@ __global__ void update_kernel(int64_t n, const float* __restrict__ v, double* __
 // Residual partial sums: part[chunk][i] = sum_{c in chunk} A[i,c] x[c] (FP64).
 __global__ void __launch_bounds__(256)
 residual_partial_kernel(int64_t n, const double* __restrict__ A, int64_t lda,
-                        const double* __restrict__ x, int64_t incx, double* __restrict__ part)
+                        const double* __restrict__ x, int64_t incx, double* __restrict__ part,
+                        const int* stop)
 {
+    if (*stop) return;
     __shared__ double xs[kChunk];
     const int64_t c0 = (int64_t)blockIdx.y * kChunk;
     const int cn = (int)min((int64_t)kChunk, n - c0);
@@ -143,8 +147,10 @@ __global__ void residual_final_kernel(int64_t n, int nchunks, const double* __re
                                       const double* __restrict__ b, int64_t incb,
                                       const double* __restrict__ x, int64_t incx,
                                       const int* __restrict__ inv, float* __restrict__ rp,
-                                      unsigned long long* rmax, unsigned long long* xmax)
+                                      unsigned long long* rmax, unsigned long long* xmax,
+                                      const int* stop)
 {
+    if (*stop) return;
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     double s = 0.0;
@@ -153,6 +159,71 @@ __global__ void residual_final_kernel(int64_t n, int nchunks, const double* __re
     rp[inv[i]] = (float)r;
     atomic_max_abs(rmax, r);
     atomic_max_abs(xmax, x[i * incx]);
+}
+
+// The refinement loop's state on the device, so that the loop runs without
+// a host round trip per step: the host enqueues max_iter steps, each step's
+// kernels return at once when `done` is set, and one copy at the end reads
+// the summary.
+struct IrState {
+    int done;       // this right-hand side has stopped
+    int conv;       // ... with the backward error at or below tol
+    int iters;      // corrections applied to this right-hand side
+    int pad;
+    double berr;    // its last backward error
+    // over all right-hand sides
+    int worst_iters;
+    int all_conv;
+    double worst_berr;
+    double anorm;
+};
+
+// After step it's residual: the normwise backward error
+// ||r|| / (||A|| ||x|| + ||b||) from the reduced norms sc = (||A||, ||b||,
+// ||r||, ||x||) (bit patterns of non-negative doubles); stop on tol, on
+// max_iter corrections or on NaN (recording in *iters_q the corrections this
+// right-hand side received); fold a stopped right-hand side into the
+// summary; clear ||r|| and ||x|| for the next residual.
+__global__ void ir_check_kernel(unsigned long long* sc, double tol, int it, int max_iter, IrState* st,
+                                int* iters_q)
+{
+    if (st->done) return;
+    const double an = __longlong_as_double((long long)sc[0]);
+    const double bn = __longlong_as_double((long long)sc[1]);
+    const double rn = __longlong_as_double((long long)sc[2]);
+    const double xn = __longlong_as_double((long long)sc[3]);
+    const double denom = an * xn + bn;
+    const double berr = denom > 0 ? rn / denom : (rn == 0 ? 0.0 : INFINITY);
+    st->berr = berr;
+    st->iters = it;
+    st->anorm = an;
+    const bool conv = berr <= tol;
+    if (conv || it >= max_iter || !(berr == berr)) {
+        st->done = 1;
+        *iters_q = it;
+        st->conv = conv ? 1 : 0;
+        st->worst_iters = max(st->worst_iters, it);
+        st->worst_berr = fmax(st->worst_berr, berr);  // NaN-free unless berr is NaN
+        if (!(berr == berr)) st->worst_berr = berr;
+        st->all_conv = st->all_conv && conv;
+    }
+    sc[2] = 0ull;
+    sc[3] = 0ull;
+}
+
+// A new right-hand side: clear its stop flag (the summary carries over).
+__global__ void ir_begin_kernel(IrState* st, int first)
+{
+    st->done = 0;
+    st->conv = 0;
+    st->iters = 0;
+    st->berr = 0.0;
+    if (first) {
+        st->worst_iters = 0;
+        st->all_conv = 1;
+        st->worst_berr = 0.0;
+        st->anorm = 0.0;
+    }
 }
 
 static inline unsigned blocks_for(int64_t n, int t) { return (unsigned)ceil_div(n, t); }
@@ -180,7 +251,9 @@ tmvg_status lu_solve_mixed(Context* c, int64_t n, const double* A, int64_t lda, 
     const size_t o_dl = o_sc + 256;
     const size_t o_du = o_dl + al(sizeof(float) * (size_t)nib * kInvBlock * kInvBlock);
     const size_t o_sg = o_du + al(sizeof(float) * (size_t)nib * kInvBlock * kInvBlock);
-    const size_t bytes = o_sg + al(sizeof(int) * 2 * nib);
+    const size_t o_ir = o_sg + al(sizeof(int) * 2 * nib);
+    const size_t o_iq = o_ir + al(sizeof(IrState));
+    const size_t bytes = o_iq + al(sizeof(int) * (size_t)nrhs);
     unsigned char* ws = (unsigned char*)workspace2(c, bytes);
     if (!ws) return TMVG_OOM;
     float* As = (float*)(ws + o_As);
@@ -190,7 +263,17 @@ tmvg_status lu_solve_mixed(Context* c, int64_t n, const double* A, int64_t lda, 
     float* v = (float*)(ws + o_v);
     double* part = (double*)(ws + o_part);
     unsigned long long* sc = (unsigned long long*)(ws + o_sc);  // anorm, bmax, rmax, xmax
-    unsigned long long hsc[4];
+    IrState* irs = (IrState*)(ws + o_ir);
+    int* iters_q = (int*)(ws + o_iq);  // corrections applied, per right-hand side
+    const int* stop = &irs->done;
+    // With kernel timing on, the spans of each enqueued step, so that the
+    // steps the device skipped can be dropped once the loop is known.
+    struct StepSpans {
+        int64_t q;
+        int it;
+        size_t res0, res1, cor0, cor1;
+    };
+    std::vector<StepSpans> step_spans;
     float* dinvL = (float*)(ws + o_dl);
     float* dinvU = (float*)(ws + o_du);
     int* singL = (int*)(ws + o_sg);
@@ -225,25 +308,27 @@ tmvg_status lu_solve_mixed(Context* c, int64_t n, const double* A, int64_t lda, 
     // and the vector (in and out)
     const double fn = (double)n;
     const double tri_bytes = 4.0 * (fn * (fn + 1) / 2 + fn * kInvBlock + 2 * fn);
-    auto solve32 = [&](float* vec) -> tmvg_status {
+    auto solve32 = [&](float* vec, const int* stp) -> tmvg_status {
         tmvg_status s2;
         {
             ScopedTimer timer(c, kClsTriSolve, tri_bytes, fn * fn);
             s2 = trsv_with_inverse_blocks<float>(c, n, As, 1, n, false, true, dinvL, singL, vec, 1,
-                                                 true);
+                                                 true, stp);
         }
         if (s2) return s2;
         ScopedTimer timer(c, kClsTriSolve, tri_bytes, fn * fn);
         return trsv_with_inverse_blocks<float>(c, n, As, 1, n, true, false, dinvU, singU, vec, 1,
-                                               true);
+                                               true, stp);
     };
 
-    int worst_iters = 0;
-    bool all_conv = true;
-    double worst_berr = 0.0, anorm = 0.0;
+    // All steps of all right-hand sides are enqueued without a host round
+    // trip: ir_check_kernel decides on the device after each residual, and
+    // the kernels of the steps after it return at once.
     for (int64_t q = 0; q < nrhs; ++q) {
         const double* b = B + q * ldb;
         double* x = X + q * ldx;
+        ir_begin_kernel<<<1, 1, 0, c->stream>>>(irs, q == 0 ? 1 : 0);
+        if ((st = launched("ir begin"))) return st;
         st = check_cuda(c, cudaMemsetAsync(sc + 1, 0, 3 * sizeof(unsigned long long), c->stream),
                         "memset");
         if (st) return st;
@@ -253,60 +338,75 @@ tmvg_status lu_solve_mixed(Context* c, int64_t n, const double* A, int64_t lda, 
         // 3. initial solve
         gather_to_f32_kernel<<<blocks_for(n, 256), 256, 0, c->stream>>>(n, perm, b, 1, v);
         if ((st = launched("gather"))) return st;
-        st = solve32(v);
+        st = solve32(v, nullptr);
         if (st) return st;
-        update_kernel<<<blocks_for(n, 256), 256, 0, c->stream>>>(n, v, x, 1, false);
+        update_kernel<<<blocks_for(n, 256), 256, 0, c->stream>>>(n, v, x, 1, false, nullptr);
         if ((st = launched("update"))) return st;
-
-        int it = 0;
-        double berr = INFINITY;
-        bool conv = false;
-        for (;;) {
-            // 4. FP64 residual, pivoted FP32 copy, norms
-            st = check_cuda(c, cudaMemsetAsync(sc + 2, 0, 2 * sizeof(unsigned long long), c->stream),
-                            "memset");
-            if (st) return st;
+        for (int it = 0; it <= max_iter; ++it) {
+            StepSpans ss{q, it, c->spans.size(), 0, 0, 0};
+            // 4. FP64 residual, pivoted FP32 copy, norms, stopping test
             {
                 // reads A (FP64) once, x per column chunk, b; writes the FP32 residual
                 ScopedTimer timer(c, kClsResidual, 8.0 * fn * fn + 8.0 * fn * (nchunks + 1) + 4.0 * fn,
                                   2.0 * fn * fn);
                 residual_partial_kernel<<<dim3(blocks_for(n, 256), nchunks), 256, 0, c->stream>>>(
-                    n, A, lda, x, 1, part);
+                    n, A, lda, x, 1, part, stop);
                 if ((st = launched("residual"))) return st;
                 residual_final_kernel<<<blocks_for(n, 256), 256, 0, c->stream>>>(
-                    n, nchunks, part, b, 1, x, 1, inv, v, sc + 2, sc + 3);
+                    n, nchunks, part, b, 1, x, 1, inv, v, sc + 2, sc + 3, stop);
                 if ((st = launched("residual_final"))) return st;
             }
-            st = check_cuda(c,
-                            cudaMemcpyAsync(hsc, sc, sizeof(hsc), cudaMemcpyDeviceToHost, c->stream),
-                            "norms d2h");
-            if (st) return st;
-            st = collect_device_error(c, "lu_solve_mixed");
-            if (st) return st;
-            double d[4];
-            for (int k = 0; k < 4; ++k) {
-                long long bits = (long long)hsc[k];
-                std::memcpy(&d[k], &bits, sizeof(double));
+            ss.res1 = c->spans.size();
+            ir_check_kernel<<<1, 1, 0, c->stream>>>(sc, tol, it, max_iter, irs, iters_q + q);
+            if ((st = launched("ir check"))) return st;
+            ss.cor0 = c->spans.size();
+            if (it < max_iter) {
+                // 5. correction
+                st = solve32(v, stop);
+                if (st) return st;
+                update_kernel<<<blocks_for(n, 256), 256, 0, c->stream>>>(n, v, x, 1, true, stop);
+                if ((st = launched("update"))) return st;
             }
-            anorm = d[0];
-            const double denom = d[0] * d[3] + d[1];
-            berr = denom > 0 ? d[2] / denom : (d[2] == 0 ? 0.0 : INFINITY);
-            if (berr <= tol) {
-                conv = true;
-                break;
-            }
-            if (it >= max_iter || !(berr == berr)) break;
-            // 5. correction
-            st = solve32(v);
-            if (st) return st;
-            update_kernel<<<blocks_for(n, 256), 256, 0, c->stream>>>(n, v, x, 1, true);
-            if ((st = launched("update"))) return st;
-            ++it;
+            ss.cor1 = c->spans.size();
+            if (c->timing) step_spans.push_back(ss);
         }
-        worst_iters = std::max(worst_iters, it);
-        worst_berr = std::max(worst_berr, berr);
-        all_conv = all_conv && conv;
     }
+    IrState hs;
+    st = check_cuda(c, cudaMemcpyAsync(&hs, irs, sizeof(hs), cudaMemcpyDeviceToHost, c->stream),
+                    "ir state d2h");
+    if (st) return st;
+    st = collect_device_error(c, "lu_solve_mixed");  // synchronises the stream
+    if (st) return st;
+    if (!step_spans.empty()) {
+        // drop the timed spans of the steps the device skipped: the residual
+        // of step it ran iff it <= iters, its correction iff it < iters
+        std::vector<int> iq((size_t)nrhs);
+        st = check_cuda(c, cudaMemcpy(iq.data(), iters_q, sizeof(int) * (size_t)nrhs, cudaMemcpyDeviceToHost),
+                        "ir iterations d2h");
+        if (st) return st;
+        std::vector<char> drop(c->spans.size(), 0);
+        for (const StepSpans& ss : step_spans) {
+            const int done_at = iq[(size_t)ss.q];
+            if (ss.it > done_at)
+                for (size_t k = ss.res0; k < ss.res1; ++k) drop[k] = 1;
+            if (ss.it >= done_at)
+                for (size_t k = ss.cor0; k < ss.cor1; ++k) drop[k] = 1;
+        }
+        std::vector<TimedSpan> kept;
+        kept.reserve(c->spans.size());
+        for (size_t k = 0; k < c->spans.size(); ++k) {
+            if (drop[k]) {
+                c->event_pool.push_back(c->spans[k].a);
+                c->event_pool.push_back(c->spans[k].b);
+            } else {
+                kept.push_back(c->spans[k]);
+            }
+        }
+        c->spans.swap(kept);
+    }
+    const int worst_iters = hs.worst_iters;
+    const bool all_conv = hs.all_conv != 0;
+    const double worst_berr = hs.worst_berr, anorm = hs.anorm;
     if (info) *info = tmvg_ir_info{worst_iters, all_conv ? 1 : 0, worst_berr, anorm};
     if (!all_conv)
         return set_error(c, TMVG_NOT_CONVERGED,

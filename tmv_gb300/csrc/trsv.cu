@@ -413,8 +413,9 @@ __global__ void __launch_bounds__(256)
 trsv_invdiag_kernel(int64_t n, const T* __restrict__ tri, int64_t tsi, int64_t tsj,
                     const T* __restrict__ dinv, const int* __restrict__ singular, bool unit,
                     T* x, int64_t incx, bool skip_zero, unsigned* flags, unsigned epoch,
-                    unsigned long long* ticket, int* err)
+                    unsigned long long* ticket, int* err, const int* stop)
 {
+    if (stop && *stop) return;  // a device-side loop has finished: no work, no waits
     __shared__ int s_blk, s_abort;
     __shared__ T xj[kIB];
     __shared__ T rhs[kIB];
@@ -534,8 +535,9 @@ __global__ void __launch_bounds__(kPubThreads)
 trsv_pub_kernel(int64_t n, const float* __restrict__ tri, int64_t tsi, int64_t tsj,
                 const float* __restrict__ dinv, const int* __restrict__ singular, bool unit,
                 float* x, int64_t incx, bool skip_zero, unsigned long long* pub, unsigned epoch,
-                unsigned long long* ticket, int* err)
+                unsigned long long* ticket, int* err, const int* stop)
 {
+    if (stop && *stop) return;  // a device-side loop has finished: no work, no waits
     __shared__ int s_blk, s_abort;
     __shared__ float xj[2][kIB];
     __shared__ float rhs[kIB];
@@ -710,7 +712,7 @@ tmvg_status trsv_lu_inverse_blocks(Context* c, int64_t n, const T* LU, int64_t l
 template <typename T>
 tmvg_status trsv_with_inverse_blocks(Context* c, int64_t n, const T* tri, int64_t tsi, int64_t tsj,
                                      bool upper, bool unit, const T* dinv, const int* singular,
-                                     T* x, int64_t incx, bool skip_zero)
+                                     T* x, int64_t incx, bool skip_zero, const int* stop)
 {
     if (n <= 0) return TMVG_OK;
     if (upper) {
@@ -747,13 +749,13 @@ tmvg_status trsv_with_inverse_blocks(Context* c, int64_t n, const T* tri, int64_
         if (epoch == 0) ++c->trsv_epoch;  // skip the clear value on wrap-around
         trsv_pub_kernel<<<(unsigned)nblk, kPubThreads, 0, c->stream>>>(
             n, tri, tsi, tsj, dinv, singular, unit, x, incx, skip_zero, c->trsv_pub,
-            c->trsv_epoch, c->trsv_ticket, c->dflags);
+            c->trsv_epoch, c->trsv_ticket, c->dflags, stop);
         ++c->launches;
         return check_cuda(c, cudaGetLastError(), "trsv pub launch");
     }
     trsv_invdiag_kernel<T><<<(unsigned)nblk, 256, 0, c->stream>>>(
         n, tri, tsi, tsj, dinv, singular, unit, x, incx, skip_zero, c->trsv_flags, epoch,
-        c->trsv_ticket, c->dflags);
+        c->trsv_ticket, c->dflags, stop);
     ++c->launches;
     return check_cuda(c, cudaGetLastError(), "trsv invdiag launch");
 }
@@ -766,10 +768,10 @@ template tmvg_status trsv_factor_inverse_blocks<double>(Context*, int64_t, const
                                                         int64_t, bool, bool, double*, int*);
 template tmvg_status trsv_with_inverse_blocks<float>(Context*, int64_t, const float*, int64_t,
                                                      int64_t, bool, bool, const float*, const int*,
-                                                     float*, int64_t, bool);
+                                                     float*, int64_t, bool, const int*);
 template tmvg_status trsv_with_inverse_blocks<double>(Context*, int64_t, const double*, int64_t,
                                                       int64_t, bool, bool, const double*,
-                                                      const int*, double*, int64_t, bool);
+                                                      const int*, double*, int64_t, bool, const int*);
 
 // ---------------------------------------------------------------------
 // Interchanges -> gather permutation: perm = identity, then for i in order

@@ -23,6 +23,9 @@ constexpr int64_t kInvBlock = 128;
 template <typename T>
 tmvg_status trsv_factor_inverse_blocks(Context* c, int64_t n, const T* tri, int64_t tsi,
                                        int64_t tsj, bool upper, bool unit, T* dinv, int* singular);
+// (trsv_with_inverse_blocks: stop, when given, is a device word; a nonzero
+// value makes the launch return at once, for solves enqueued ahead by a loop
+// that decides on the device when to stop.)
 // Both triangles of a packed LU factor (column-major, leading dimension ld)
 // in one launch: unit lower L into (dinvL, singL), upper U into (dinvU, singU).
 template <typename T>
@@ -31,7 +34,7 @@ tmvg_status trsv_lu_inverse_blocks(Context* c, int64_t n, const T* LU, int64_t l
 template <typename T>
 tmvg_status trsv_with_inverse_blocks(Context* c, int64_t n, const T* tri, int64_t tsi, int64_t tsj,
                                      bool upper, bool unit, const T* dinv, const int* singular,
-                                     T* x, int64_t incx, bool skip_zero);
+                                     T* x, int64_t incx, bool skip_zero, const int* stop = nullptr);
 
 // Interchange vector P (TMV/LAPACK form) -> gather permutation perm with
 // (P B)[i] = B[perm[i]].
