@@ -11,15 +11,18 @@
 //   - the solves divide by U(j,j) as TMV_Divide = b * TMV_InverseOf(d) and
 //     skip zero entries, as TMV's column-oriented vector solves do
 //     (src/TMV_TriDiv_V.cpp:148-236, 322-398), one right-hand side at a time.
-// Complex products are (ac - bd, ad + bc) with separately rounded products
-// (no fused multiply-add), as the host computes them.
+// The scaling and the solves' complex products are (ac - bd, ad + bc) with
+// separately rounded products (no fused multiply-add), as the host computes
+// them; the blocked trailing products and solves' off-diagonal products use
+// fused multiply-adds (values to rounding).
 //
 // Small matrices (n < 128) factor one column per step (pivot search in one
-// CTA, row interchange, scaling, rank-1 update over the grid); larger ones
-// by panels (zlu_factor_blocked below).  The left solve runs one CTA per
-// right-hand side, the right solve (LU_RDivEq) one row per CTA substituted
-// in TMV's order.  Values agree with TMV's recursive factorisation to
-// rounding; pivots are TMV's wherever rounding does not decide a tie.
+// CTA, row interchange, scaling, rank-1 update over the grid) and solve one
+// CTA per right-hand side; larger ones factor by panels with look-ahead
+// (zlu_factor_blocked) and solve by 64-row blocks (zlu_ldiveq_blocked).  The
+// right solve (LU_RDivEq) runs one row per CTA substituted in TMV's order.
+// Values agree with TMV's recursive factorisation to rounding; pivots are
+// TMV's wherever rounding does not decide a tie.
 #include "zlu.cuh"
 #include "trsv.cuh"
 
