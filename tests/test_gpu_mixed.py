@@ -146,3 +146,24 @@ def test_full_size_8192_cond1e6(dev):
     X64, _, _ = linalg.divide(A, b)
     fe = float((X - X64).norm() / X64.norm())
     assert fe <= 50 * cond * (info.backward_error + np.finfo(float).eps)
+
+
+@pytest.mark.parametrize("n", [512, 500])
+def test_zero_column_reports_singular(dev, n):
+    # a zero column of A gives the FP32 factor an exact zero U(j,j); the
+    # refinement's triangular solve meets it in a diagonal block (the
+    # substitution branch of both solve forms: n = 512 streams whole 128-row
+    # blocks, n = 500 takes the register form) and the call reports SINGULAR,
+    # as TMV's solve throws on a singular U; the handle stays usable
+    from tmv_gb300 import TmvgError, linalg
+
+    a, b = haar(n, 1e2, seed=41)
+    a[:, 300] = 0.0
+    A = to_dev(a, dev, "F")
+    B = to_dev(b.reshape(n, 1), dev, "F")
+    with pytest.raises(TmvgError) as ei:
+        linalg.solve_mixed(A, B, max_iter=3, tol=1e-12)
+    assert ei.value.status == 1
+    a2, b2 = haar(n, 1e2, seed=42)
+    X, info = linalg.solve_mixed(to_dev(a2, dev, "F"), to_dev(b2.reshape(n, 1), dev, "F"))
+    assert info.converged == 1 and backward_error(a2, to_host(X)[:, 0], b2) <= 1e-14

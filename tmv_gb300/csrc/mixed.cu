@@ -251,7 +251,9 @@ tmvg_status lu_solve_mixed(Context* c, int64_t n, const double* A, int64_t lda, 
     const size_t o_dl = o_sc + 256;
     const size_t o_du = o_dl + al(sizeof(float) * (size_t)nib * kInvBlock * kInvBlock);
     const size_t o_sg = o_du + al(sizeof(float) * (size_t)nib * kInvBlock * kInvBlock);
-    const size_t o_ir = o_sg + al(sizeof(int) * 2 * nib);
+    const size_t o_ml = o_sg + al(sizeof(int) * 2 * nib);
+    const size_t o_mu = o_ml + al(sizeof(float) * (size_t)nib * kInvBlock * kInvBlock);
+    const size_t o_ir = o_mu + al(sizeof(float) * (size_t)nib * kInvBlock * kInvBlock);
     const size_t o_iq = o_ir + al(sizeof(IrState));
     const size_t bytes = o_iq + al(sizeof(int) * (size_t)nrhs);
     unsigned char* ws = (unsigned char*)workspace2(c, bytes);
@@ -278,6 +280,8 @@ tmvg_status lu_solve_mixed(Context* c, int64_t n, const double* A, int64_t lda, 
     float* dinvU = (float*)(ws + o_du);
     int* singL = (int*)(ws + o_sg);
     int* singU = singL + nib;
+    float* mlinkL = (float*)(ws + o_ml);
+    float* mlinkU = (float*)(ws + o_mu);
 
     tmvg_status st;
     auto launched = [&](const char* what) {
@@ -304,6 +308,9 @@ tmvg_status lu_solve_mixed(Context* c, int64_t n, const double* A, int64_t lda, 
     // solve of the refinement loop
     st = trsv_lu_inverse_blocks<float>(c, n, As, n, dinvL, singL, dinvU, singU);
     if (st) return st;
+    // and the link blocks M_b = Dinv_b T[b, b-1] of both triangles
+    st = trsv_lu_link_blocks(c, n, As, n, dinvL, singL, mlinkL, dinvU, singU, mlinkU);
+    if (st) return st;
     // one triangular solve reads its triangle, the inverted diagonal blocks
     // and the vector (in and out)
     const double fn = (double)n;
@@ -313,12 +320,12 @@ tmvg_status lu_solve_mixed(Context* c, int64_t n, const double* A, int64_t lda, 
         {
             ScopedTimer timer(c, kClsTriSolve, tri_bytes, fn * fn);
             s2 = trsv_with_inverse_blocks<float>(c, n, As, 1, n, false, true, dinvL, singL, vec, 1,
-                                                 true, stp);
+                                                 true, stp, mlinkL);
         }
         if (s2) return s2;
         ScopedTimer timer(c, kClsTriSolve, tri_bytes, fn * fn);
         return trsv_with_inverse_blocks<float>(c, n, As, 1, n, true, false, dinvU, singU, vec, 1,
-                                               true, stp);
+                                               true, stp, mlinkU);
     };
 
     // All steps of all right-hand sides are enqueued without a host round

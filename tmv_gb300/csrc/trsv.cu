@@ -16,6 +16,7 @@
 // column-oriented vector solve (src/TMV_TriDiv_V.cpp:148-236, 322-398):
 // x_i = b_i - sum_j T_ij x_j over j in dependency order.
 #include "trsv.cuh"
+#include "async.cuh"
 #include "pivots.cuh"
 
 #include <type_traits>
@@ -538,7 +539,7 @@ trsv_pub_kernel(int64_t n, const float* __restrict__ tri, int64_t tsi, int64_t t
                 unsigned long long* ticket, int* err, const int* stop)
 {
     if (stop && *stop) return;  // a device-side loop has finished: no work, no waits
-    __shared__ int s_blk, s_abort;
+    __shared__ int s_blk, s_abort[2];  // one per parity of the wait: a single barrier separates two waits
     __shared__ float xj[2][kIB];
     __shared__ float rhs[kIB];
     __shared__ float part[4][kIB];
@@ -546,7 +547,7 @@ trsv_pub_kernel(int64_t n, const float* __restrict__ tri, int64_t tsi, int64_t t
     const int i = tid & (kIB - 1), q = tid >> 7;  // row of the block, quarter of the columns
     if (tid == 0) {
         s_blk = (int)atomicAdd(ticket, 1ull);
-        s_abort = 0;
+        s_abort[0] = s_abort[1] = 0;
     }
     __syncthreads();
     const int64_t b = s_blk;
@@ -587,7 +588,7 @@ trsv_pub_kernel(int64_t n, const float* __restrict__ tri, int64_t tsi, int64_t t
             while ((v & 0xffffffff00000000ull) != tag) {
                 if (++spins > kSpinLimit || *((volatile int*)err) == kDevTimeout) {
                     atomicCAS(err, (int)kDevOk, (int)kDevTimeout);
-                    s_abort = 1;
+                    s_abort[j & 1] = 1;
                     break;
                 }
                 if (spins > 32) __nanosleep(32);
@@ -597,7 +598,7 @@ trsv_pub_kernel(int64_t n, const float* __restrict__ tri, int64_t tsi, int64_t t
             if (j + 1 < b) vpre = ld_relaxed_u64(w + kIB);
         }
         __syncthreads();  // xb complete; the other buffer is free again
-        if (s_abort) return false;
+        if (s_abort[j & 1]) return false;
 #pragma unroll
         for (int c = 0; c < kPubCols; c += 2) {
             acc0 -= a[c] * xb[q * kPubCols + c];
@@ -709,11 +710,264 @@ tmvg_status trsv_lu_inverse_blocks(Context* c, int64_t n, const T* LU, int64_t l
     return launch_inv_blocks<T>(c, n, jl, ju, 2);
 }
 
+// ---------------------------------------------------------------------
+// The refinement's FP32 solve with its tiles streamed through shared memory
+// (n a multiple of 128).  Timestamps per block showed the register form
+// bound by streaming: a block's CTA spends about 2.2 us per 64 KB tile with
+// one tile in flight.  Here each CTA keeps two tiles in flight in a ring of
+// three shared-memory slots filled by cp.async (no register cost), and the
+// last tile enters through a link block M_b = Dinv_b T[b, b-1] precomputed
+// once per factor: y_b = Dinv_b (r_b - sum_{j<b-1} T[b,j] x_j) is formed
+// before x_{b-1} arrives and the step on the chain is x_b = y_b - M_b x_{b-1}
+// (Dinv_b and M_b rows in registers).  Blocks with a zero diagonal keep the
+// substitution.
+// ---------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+link_blocks_kernel(int64_t n, int64_t nblk, InvBlocksJob<float> j0, InvBlocksJob<float> j1, float* ml0,
+                   float* ml1)
+{
+    extern __shared__ __align__(16) float lk_smem[];
+    float* Ds = lk_smem;                    // Dinv_b, [kIB][kIB+1] by row
+    float* Ts = lk_smem + kIB * (kIB + 1);  // T[b, b-1], [kIB][kIB+1] by row
+    const int job = (int)(blockIdx.x / (nblk - 1));
+    const int64_t b = 1 + blockIdx.x % (nblk - 1);
+    const InvBlocksJob<float>& J = job ? j1 : j0;
+    float* ml = job ? ml1 : ml0;
+    if (J.singular[b]) return;
+    const int64_t r0 = b * kIB, c0 = (b - 1) * kIB;
+    const int rows = (int)min((int64_t)kIB, n - r0);
+    const float* Di = J.dinv + b * (int64_t)kIB * kIB;
+    for (int t = threadIdx.x; t < kIB * kIB; t += 256) {
+        const int i = t % kIB, k = t / kIB;  // coalesced along i
+        Ds[i * (kIB + 1) + k] = Di[i + k * kIB];
+        Ts[i * (kIB + 1) + k] = i < rows ? J.tri[(r0 + i) * J.tsi + (c0 + k) * J.tsj] : 0.0f;
+    }
+    __syncthreads();
+    const int i0 = (threadIdx.x & 31) * 4, cc0 = (threadIdx.x >> 5) * 16;
+    float acc[4][16];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int c = 0; c < 16; ++c) acc[a][c] = 0.0f;
+    for (int k = 0; k < kIB; ++k) {
+        float d[4], tt[16];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) d[a] = Ds[(i0 + a) * (kIB + 1) + k];
+#pragma unroll
+        for (int c = 0; c < 16; ++c) tt[c] = Ts[k * (kIB + 1) + cc0 + c];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int c = 0; c < 16; ++c) acc[a][c] = fmaf(d[a], tt[c], acc[a][c]);
+    }
+    float* out = ml + b * (int64_t)kIB * kIB;
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int c = 0; c < 16; ++c) out[(i0 + a) + (cc0 + c) * kIB] = acc[a][c];
+}
+
+tmvg_status trsv_lu_link_blocks(Context* c, int64_t n, const float* LU, int64_t ld, const float* dinvL,
+                                const int* singL, float* mlinkL, const float* dinvU, const int* singU,
+                                float* mlinkU)
+{
+    const int64_t nblk = ceil_div(n, kIB);
+    if (nblk < 2) return TMVG_OK;
+    const InvBlocksJob<float> jl =
+        inv_blocks_job<float>(n, LU, 1, ld, false, true, const_cast<float*>(dinvL), const_cast<int*>(singL));
+    const InvBlocksJob<float> ju =
+        inv_blocks_job<float>(n, LU, 1, ld, true, false, const_cast<float*>(dinvU), const_cast<int*>(singU));
+    const size_t smem = sizeof(float) * 2 * kIB * (kIB + 1);
+    tmvg_status st = check_cuda(
+        c, cudaFuncSetAttribute(link_blocks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+        "link blocks: smem attribute");
+    if (st) return st;
+    link_blocks_kernel<<<(unsigned)(2 * (nblk - 1)), 256, smem, c->stream>>>(n, nblk, jl, ju, mlinkL, mlinkU);
+    ++c->launches;
+    return check_cuda(c, cudaGetLastError(), "link blocks launch");
+}
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+constexpr int kRing = 3;  // shared-memory tile slots: two tiles in flight beside the one in use
+
+__global__ void __launch_bounds__(kPubThreads)
+trsv_pub_async_kernel(int64_t n, const float* __restrict__ tri, int64_t tsi, int64_t tsj, bool upper,
+                      const float* __restrict__ dinv, const int* __restrict__ singular,
+                      const float* __restrict__ mlink, bool unit, float* x, int64_t incx, bool skip_zero,
+                      unsigned long long* pub, unsigned epoch, unsigned long long* ticket, int* err,
+                      const int* stop)
+{
+    if (stop && *stop) return;  // a device-side loop has finished: no work, no waits
+    extern __shared__ __align__(16) float ring[];  // [kRing][kIB columns][kIB]
+    __shared__ int s_blk, s_abort[2];  // one per parity of the wait: a single barrier separates two waits
+    __shared__ float xj[2][kIB];
+    __shared__ float rhs[kIB];
+    __shared__ float part[4][kIB];
+    const int tid = threadIdx.x;
+    const int i = tid & (kIB - 1), q = tid >> 7;  // row of the block, quarter of the columns
+    if (tid == 0) {
+        s_blk = (int)atomicAdd(ticket, 1ull);
+        s_abort[0] = s_abort[1] = 0;
+    }
+    __syncthreads();
+    const int64_t b = s_blk;
+    const int64_t nblk = n / kIB;
+    if (b >= nblk) return;
+    const int64_t r0 = b * kIB;
+    const unsigned long long tag = (unsigned long long)epoch << 32;
+    // a tile column's 128 entries are contiguous in memory, from view row
+    // r0 (lower) or r0 + 127 (upper: the view is index-reversed)
+    const int64_t rbase = upper ? (r0 + kIB - 1) * tsi : r0 * tsi;
+    const int pos = upper ? kIB - 1 - i : i;  // this row's place in a slot column
+
+    // independent of the other blocks: right-hand side, inverse and link rows
+    const float b_i = tid < kIB ? x[(r0 + tid) * incx] : 0.0f;
+    const bool sing = singular[b] != 0;
+    const bool use_link = b >= 1 && !sing;
+    const int64_t ntiles = use_link ? b - 1 : b;
+    float di[kPubCols], mi[kPubCols];
+    {
+        const float* Di = dinv + b * (int64_t)kIB * kIB;
+        const float* Mb = use_link ? mlink + b * (int64_t)kIB * kIB : nullptr;
+#pragma unroll
+        for (int l = 0; l < kPubCols; ++l) {
+            di[l] = sing ? 0.0f : Di[i + (q * kPubCols + l) * kIB];
+            mi[l] = use_link ? Mb[i + (q * kPubCols + l) * kIB] : 0.0f;
+        }
+    }
+    // tile j into slot s: 4096 pieces of 16 bytes, 8 per thread
+    auto fetch = [&](int64_t j, int s) {
+        if (j < ntiles) {
+            float* slot = ring + (size_t)s * kIB * kIB;
+#pragma unroll
+            for (int u = 0; u < (kIB * kIB / 4) / kPubThreads; ++u) {
+                const int t = tid + u * kPubThreads;
+                const int c = t / (kIB / 4), k = t % (kIB / 4);
+                cp_async16(slot + c * kIB + 4 * k, tri + rbase + (j * kIB + c) * tsj + 4 * k);
+            }
+        }
+        cp_async_commit();  // one group per tile, empty past the last
+    };
+    unsigned long long vpre = 0;
+    if (b > 0 && tid < kIB) vpre = ld_relaxed_u64(pub + tid);
+    auto wait_x = [&](int64_t j) -> bool {
+        float* xb = xj[j & 1];
+        if (tid < kIB) {
+            const unsigned long long* w = pub + j * kIB + tid;
+            unsigned long long v = vpre;
+            unsigned spins = 0;
+            while ((v & 0xffffffff00000000ull) != tag) {
+                if (++spins > kSpinLimit || *((volatile int*)err) == kDevTimeout) {
+                    atomicCAS(err, (int)kDevOk, (int)kDevTimeout);
+                    s_abort[j & 1] = 1;
+                    break;
+                }
+                if (spins > 32) __nanosleep(32);
+                v = ld_relaxed_u64(w);
+            }
+            xb[tid] = __uint_as_float((unsigned)v);
+            if (j + 1 < b) vpre = ld_relaxed_u64(w + kIB);
+        }
+        __syncthreads();  // xb complete (and every thread's landed tile copies visible)
+        return !s_abort[j & 1];
+    };
+    float acc0 = 0.0f, acc1 = 0.0f;
+    fetch(0, 0);
+    fetch(1, 1);
+    for (int64_t j = 0; j < ntiles; ++j) {
+        cp_async_wait1();  // this thread's pieces of tile j have landed
+        if (!wait_x(j)) {
+            asm volatile("cp.async.wait_all;" ::: "memory");
+            return;
+        }
+        // slot (j + 2) % 3 held tile j - 1, which every thread finished
+        // before the barrier above
+        fetch(j + 2, (int)((j + 2) % kRing));
+        const float* slot = ring + (size_t)(j % kRing) * kIB * kIB;
+        const float* xb = xj[j & 1];
+#pragma unroll
+        for (int l = 0; l < kPubCols; l += 2) {
+            acc0 -= slot[(q * kPubCols + l) * kIB + pos] * xb[q * kPubCols + l];
+            acc1 -= slot[(q * kPubCols + l + 1) * kIB + pos] * xb[q * kPubCols + l + 1];
+        }
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");  // the empty groups past the last tile
+    part[q][i] = acc0 + acc1;
+    __syncthreads();
+    if (tid < kIB) rhs[tid] = b_i + ((part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]));
+    __syncthreads();
+    if (!sing) {
+        float sum = 0.0f;
+#pragma unroll
+        for (int l = 0; l < kPubCols; ++l) sum += di[l] * rhs[q * kPubCols + l];
+        part[q][i] = sum;
+        __syncthreads();
+        float v = tid < kIB ? (part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]) : 0.0f;
+        if (use_link) {
+            if (!wait_x(b - 1)) return;  // its barrier also orders the reads of part above
+            const float* xb = xj[(b - 1) & 1];
+            float m0 = 0.0f, m1 = 0.0f;
+#pragma unroll
+            for (int l = 0; l < kPubCols; l += 2) {
+                m0 = fmaf(mi[l], xb[q * kPubCols + l], m0);
+                m1 = fmaf(mi[l + 1], xb[q * kPubCols + l + 1], m1);
+            }
+            part[q][i] = m0 + m1;
+            __syncthreads();
+            if (tid < kIB) v -= (part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]);
+        }
+        if (tid < kIB) {
+            x[(r0 + tid) * incx] = v;
+            st_relaxed_u64(pub + r0 + tid, tag | __float_as_uint(v));
+        }
+    } else if (tid < 32) {
+        // zero diagonal somewhere: substitution with TMV's zero skipping
+        bool sg = false;
+        for (int jj = 0; jj < kIB; ++jj) {
+            __syncwarp();
+            float v = rhs[jj];
+            if (!unit) {
+                const float d = tri[(r0 + jj) * tsi + (r0 + jj) * tsj];
+                if (skip_zero) {
+                    if (v != 0.0f) {
+                        if (d == 0.0f) sg = true;
+                        else v = v / d;
+                    }
+                } else {
+                    if (d == 0.0f) sg = true;
+                    else v = v * (1.0f / d);
+                }
+            }
+            __syncwarp();
+            if (tid == 0) rhs[jj] = v;
+            if (v != 0.0f || !skip_zero)
+                for (int k2 = jj + 1 + tid; k2 < kIB; k2 += 32)
+                    rhs[k2] -= tri[(r0 + k2) * tsi + (r0 + jj) * tsj] * v;
+        }
+        if (sg) atomicCAS(err, (int)kDevOk, (int)kDevSingular);
+        __syncwarp();
+        for (int k2 = tid; k2 < kIB; k2 += 32) {
+            x[(r0 + k2) * incx] = rhs[k2];
+            st_relaxed_u64(pub + r0 + k2, tag | __float_as_uint(rhs[k2]));
+        }
+    }
+}
+
 template <typename T>
 tmvg_status trsv_with_inverse_blocks(Context* c, int64_t n, const T* tri, int64_t tsi, int64_t tsj,
                                      bool upper, bool unit, const T* dinv, const int* singular,
-                                     T* x, int64_t incx, bool skip_zero, const int* stop)
+                                     T* x, int64_t incx, bool skip_zero, const int* stop,
+                                     const T* mlink)
 {
+    const bool is_upper = upper;
+    const T* tri_in = tri;  // the triangle's storage, before an upper view is reversed
+    const int64_t tsi_in = tsi;
     if (n <= 0) return TMVG_OK;
     if (upper) {
         tri = tri + (n - 1) * (tsi + tsj);
@@ -747,6 +1001,19 @@ tmvg_status trsv_with_inverse_blocks(Context* c, int64_t n, const T* tri, int64_
             c->trsv_pub_len = (size_t)n;
         }
         if (epoch == 0) ++c->trsv_epoch;  // skip the clear value on wrap-around
+        // the streamed form: whole 128-row blocks, 16-byte aligned tile columns
+        if (mlink && n % kIB == 0 && tsi_in == 1 && (tsj % 4) == 0 && ((uintptr_t)tri_in % 16) == 0) {
+            const size_t smem = sizeof(float) * kRing * kIB * kIB;
+            st = check_cuda(c, cudaFuncSetAttribute(trsv_pub_async_kernel,
+                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                            "trsv async: smem attribute");
+            if (st) return st;
+            trsv_pub_async_kernel<<<(unsigned)nblk, kPubThreads, smem, c->stream>>>(
+                n, tri, tsi, tsj, is_upper, dinv, singular, mlink, unit, x, incx, skip_zero, c->trsv_pub,
+                c->trsv_epoch, c->trsv_ticket, c->dflags, stop);
+            ++c->launches;
+            return check_cuda(c, cudaGetLastError(), "trsv async launch");
+        }
         trsv_pub_kernel<<<(unsigned)nblk, kPubThreads, 0, c->stream>>>(
             n, tri, tsi, tsj, dinv, singular, unit, x, incx, skip_zero, c->trsv_pub,
             c->trsv_epoch, c->trsv_ticket, c->dflags, stop);
@@ -768,10 +1035,11 @@ template tmvg_status trsv_factor_inverse_blocks<double>(Context*, int64_t, const
                                                         int64_t, bool, bool, double*, int*);
 template tmvg_status trsv_with_inverse_blocks<float>(Context*, int64_t, const float*, int64_t,
                                                      int64_t, bool, bool, const float*, const int*,
-                                                     float*, int64_t, bool, const int*);
+                                                     float*, int64_t, bool, const int*, const float*);
 template tmvg_status trsv_with_inverse_blocks<double>(Context*, int64_t, const double*, int64_t,
                                                       int64_t, bool, bool, const double*,
-                                                      const int*, double*, int64_t, bool, const int*);
+                                                      const int*, double*, int64_t, bool, const int*,
+                                                      const double*);
 
 // ---------------------------------------------------------------------
 // Interchanges -> gather permutation: perm = identity, then for i in order

@@ -34,7 +34,15 @@ tmvg_status trsv_lu_inverse_blocks(Context* c, int64_t n, const T* LU, int64_t l
 template <typename T>
 tmvg_status trsv_with_inverse_blocks(Context* c, int64_t n, const T* tri, int64_t tsi, int64_t tsj,
                                      bool upper, bool unit, const T* dinv, const int* singular,
-                                     T* x, int64_t incx, bool skip_zero, const int* stop = nullptr);
+                                     T* x, int64_t incx, bool skip_zero, const int* stop = nullptr,
+                                     const T* mlink = nullptr);
+// Link blocks of an FP32 factor for trsv_with_inverse_blocks (mlink, FP32
+// only; used when n is a multiple of 128): M_b = Dinv_b T[b, b-1] for both
+// triangles (ceil(n/128)*128*128 floats each), computed once per factor
+// after trsv_lu_inverse_blocks.
+tmvg_status trsv_lu_link_blocks(Context* c, int64_t n, const float* LU, int64_t ld, const float* dinvL,
+                                const int* singL, float* mlinkL, const float* dinvU, const int* singU,
+                                float* mlinkU);
 
 // Interchange vector P (TMV/LAPACK form) -> gather permutation perm with
 // (P B)[i] = B[perm[i]].
