@@ -474,6 +474,18 @@ tmvg_status tmvg_band_lu_ldiveq_batched_f64(tmvg_handle h, int64_t count, int64_
                                             int64_t stride_ab, const int64_t* P, int64_t stride_p,
                                             int64_t nrhs, double* B, int64_t ldb, int64_t stride_b,
                                             int32_t* status);
+/* x P L U = m for every system from its band factors: replaces
+ * tmv::LU_RDivEq(const GenBandMatrix<double>&, const ptrdiff_t*,
+ * MatrixView<double>) (src/TMV_BandLUDiv.h:55, src/TMV_BandLUDiv.cpp:834-851),
+ * the step of BandLUDiv behind m %= A (and behind b / A when BandLUDiv
+ * factors the transpose), bit for bit.  m is nrhs x n per system, row q at
+ * B[s*stride_b + q*ldb] (unit step, ldb >= n: a row-major m to TMV); the
+ * memory layout is ldiveq's B.  Same status values. */
+tmvg_status tmvg_band_lu_rdiveq_batched_f64(tmvg_handle h, int64_t count, int64_t n, int64_t lo,
+                                            int64_t hi, int algo, const double* AB, int64_t ldab,
+                                            int64_t stride_ab, const int64_t* P, int64_t stride_p,
+                                            int64_t nrhs, double* B, int64_t ldb, int64_t stride_b,
+                                            int32_t* status);
 /* Both in one launch (the factors and P are written as by the decompose). */
 tmvg_status tmvg_band_lu_solve_batched_f64(tmvg_handle h, int64_t count, int64_t n, int64_t lo,
                                            int64_t hi, int algo, double* AB, int64_t ldab,

@@ -232,6 +232,22 @@ class _Backend:
         if rc:
             raise RuntimeError(f"band_lu_ldiveq rc={rc}")
 
+    def band_lu_rdiveq(self, lu: np.ndarray, n: int, lo: int, hi: int, ldab: int, P: np.ndarray,
+                       M: np.ndarray, algo: int = 0, ldb: int | None = None) -> None:
+        """M (nrhs x n, each row contiguous: a flat or C-order float64 array)
+        := M (P L U)^-1 in place from band factors (LU_RDivEq)."""
+        assert M.dtype == np.float64
+        nrhs = 1 if M.ndim == 1 else M.shape[0]
+        if ldb is None:
+            ldb = n if M.ndim == 1 else M.strides[0] // 8
+        f = self._f("band_lu_rdiveq", C.c_int, [i64, i64, i64, C.c_int, vp, i64, vp, i64, vp, i64])
+        rc = f(n, lo, hi, algo, _p(lu), ldab, _p(np.ascontiguousarray(P, dtype=np.int64)), nrhs,
+               _p(M), ldb)
+        if rc == SINGULAR:
+            raise OracleSingular("singular")
+        if rc:
+            raise RuntimeError(f"band_lu_rdiveq rc={rc}")
+
     def band_batched_solve(self, count: int, n: int, lo: int, hi: int, algo: int, ab: np.ndarray,
                            ldab: int, sab: int, nrhs: int, B: np.ndarray, ldb: int, sb: int):
         """The batched band workload in place on the host cores (OpenMP over

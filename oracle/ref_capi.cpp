@@ -18,10 +18,11 @@
 //   tmvref_rdivide       X = B % m (LUDiv::doRDiv, src/TMV_LUD.cpp:122-130)
 //   tmvref_det           m.det(), m.logDet(&s) (src/TMV_LUD.cpp:132-190)
 //   tmvref_batched_divide  one B_i/A_i per system, OpenMP over systems.
-//   tmvref_band_lu_decompose, tmvref_band_lu_ldiveq
+//   tmvref_band_lu_decompose, tmvref_band_lu_ldiveq, tmvref_band_lu_rdiveq
 //                        LU_Decompose(BandMatrixView<T>, ptrdiff_t*, ptrdiff_t)
-//                        (src/TMV_BandLUDecompose.cpp:383) and LU_LDivEq on band
-//                        factors (src/TMV_BandLUDiv.cpp:139) over TMV's
+//                        (src/TMV_BandLUDecompose.cpp:383) and LU_LDivEq /
+//                        LU_RDivEq on band factors (src/TMV_BandLUDiv.cpp:
+//                        811-851; m row-major for RDivEq) over TMV's
 //                        column-major band storage; tmvref_band_batched_solve
 //                        both over a batch, OpenMP over systems.
 //   tmvref_lu_decompose_z, tmvref_lu_ldiveq_z, tmvref_lu_rdiveq_z, tmvref_det_z,
@@ -200,6 +201,25 @@ int tmvref_band_lu_ldiveq(ptrdiff_t n, ptrdiff_t lo, ptrdiff_t hi, int algo, con
         }
         tmv::ConstBandMatrixView<double> LU(lu, n, n, lo, hu, 1, ldab, ldab + 1, tmv::NonConj);
         tmv::LU_LDivEq(LU, P, Bv);
+    });
+}
+
+int tmvref_band_lu_rdiveq(ptrdiff_t n, ptrdiff_t lo, ptrdiff_t hi, int algo, const double* lu,
+                          ptrdiff_t ldab, const ptrdiff_t* P, ptrdiff_t nrhs, double* B,
+                          ptrdiff_t ldb)
+{
+    return guarded([&] {
+        if (n == 0 || nrhs == 0) return;
+        const ptrdiff_t hu = std::min(lo + hi, n - 1);
+        tmv::MatrixView<double> Mv = tmv::MatrixViewOf(B, nrhs, n, ldb, 1);
+        if (algo == 1) {
+            tmv::BandMatrix<double, tmv::DiagMajor> D(n, n, 1, hu, 0.0);
+            band_to_dm(n, hu, lu, ldab, D);
+            tmv::LU_RDivEq(D, P, Mv);
+            return;
+        }
+        tmv::ConstBandMatrixView<double> LU(lu, n, n, lo, hu, 1, ldab, ldab + 1, tmv::NonConj);
+        tmv::LU_RDivEq(LU, P, Mv);
     });
 }
 

@@ -101,6 +101,10 @@ int oracle_band_lu_decompose(ptrdiff_t n, ptrdiff_t lo, ptrdiff_t hi, int algo, 
 int oracle_band_lu_ldiveq(ptrdiff_t n, ptrdiff_t lo, ptrdiff_t hi, int algo, const double* lu,
                           ptrdiff_t ldab, const ptrdiff_t* P, ptrdiff_t nrhs, double* B,
                           ptrdiff_t ldb);
+/* x P L U = m for the nrhs rows of m (row q at B + q*ldb), in place. */
+int oracle_band_lu_rdiveq(ptrdiff_t n, ptrdiff_t lo, ptrdiff_t hi, int algo, const double* lu,
+                          ptrdiff_t ldab, const ptrdiff_t* P, ptrdiff_t nrhs, double* B,
+                          ptrdiff_t ldb);
 /* count systems of one shape, OpenMP over systems (system s at ab + s*sab,
  * P + s*sp, B + s*sb); status[s] per system. */
 int oracle_band_batched_solve(ptrdiff_t count, ptrdiff_t n, ptrdiff_t lo, ptrdiff_t hi, int algo,

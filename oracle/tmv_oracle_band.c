@@ -260,6 +260,95 @@ int oracle_band_lu_ldiveq(ptrdiff_t n, ptrdiff_t lo, ptrdiff_t hi, int algo, con
     return ORACLE_OK;
 }
 
+/* LU_RDivEq for band factors, NonLapLU_RDivEq (src/TMV_BandLUDiv.cpp:
+ * 244-290, 834-851): x P L U = m for each row of m (nrhs x n, row q at
+ * B + q*ldb, unit step), in two passes per row b:
+ *
+ * 1. y U = b, i.e. TriLDivEq(Transpose(U), b) (src/TMV_BandTriDiv_M.cpp:
+ *    391-425 with one column at a time, NonBlasTriLDivEq of
+ *    src/TMV_BandTriDiv_V.cpp:445-468).  For hu == 0 the transpose is
+ *    diagonal and the solve is upper_solve's diagonal one (trailing zeros
+ *    trimmed, every U(i,i) of the leading part checked).  Otherwise leading
+ *    zeros are trimmed (i1 = the first nonzero; nothing to do when b is
+ *    zero) and the row form runs forward (DoRowLowerTriLDivEq, :240-313):
+ *    b[i] -= b[j] U(j,i) for j = max(i1, i-hu) .. i-1 in that order, then
+ *    b[i] / U(i,i), every U(i,i) from i1 on checked.
+ * 2. z L = y (LU_PackedPL_RDivEq, :190-222): for j = n-2 down to 0,
+ *    b[j] -= sum_k b[j+k] L(j+k, j) over k = 1..min(lo, n-1-j), then swap
+ *    b[j] and b[P[j]].  The sum is MultMV's (src/TMV_MultMV.cpp:298-380 and
+ *    the row form :80-122): a product into a temporary from 0.0, added into
+ *    b[j] with alpha = -1.  The column-major factors give it x with unit
+ *    step: t = 0.0 + L b ... and b[j] - t; the diagonal-major storage of
+ *    the tridiagonal algorithm gives a strided x, which MultMV copies as
+ *    alpha x: t' = 0.0 + (-L) b ... and b[j] + t' (the same value but for
+ *    the sign of a zero).
+ *
+ * ORACLE_SINGULAR for a zero U(i,i) where TMV throws SingularBandLU;
+ * ORACLE_BAD_ARG for an interchange P[j] outside rows j..min(j+lo, n-1)
+ * (factors not made by the band LU), not applied.  The
+ * 1 x nrhs special case with ldb == 1 is LDivEq's (the two passes see the
+ * same one-entry transpose). */
+static int rdiv_row(idx n, idx lo, idx hu, int algo, const double* lu, idx ldab, const idx* P, double* b)
+{
+    if (hu == 0) {
+        const int rc = upper_solve(n, hu, algo, lu, ldab, b);
+        if (rc) return rc;
+    } else {
+        idx i1 = 0;
+        while (i1 < n && b[i1] == 0.0) ++i1;
+        for (idx i = i1; i < n; ++i) {
+            double v = b[i];
+            for (idx j = imax(i1, i - hu); j < i; ++j) v -= b[j] * BA(lu, ldab, j, i);
+            const double d = BA(lu, ldab, i, i);
+            if (d == 0.0) return ORACLE_SINGULAR;
+            b[i] = v / d;
+        }
+    }
+    if (lo == 0) return ORACLE_OK;
+    for (idx j = n - 2; j >= 0; --j) {
+        const idx len = imin(lo, n - 1 - j);
+        if (algo == ORACLE_BAND_TRIDIAG) {
+            double t = 0.0;
+            for (idx k = 1; k <= len; ++k) t += (-BA(lu, ldab, j + k, j)) * b[j + k];
+            b[j] = b[j] + t;
+        } else {
+            double t = 0.0;
+            for (idx k = 1; k <= len; ++k) t += BA(lu, ldab, j + k, j) * b[j + k];
+            b[j] = b[j] - t;
+        }
+        const idx pj = P[j];
+        if (pj < j || pj > j + lo || pj >= n) return ORACLE_BAD_ARG;
+        if (pj != j) {
+            const double t = b[j];
+            b[j] = b[pj];
+            b[pj] = t;
+        }
+    }
+    return ORACLE_OK;
+}
+
+int oracle_band_lu_rdiveq(ptrdiff_t n, ptrdiff_t lo, ptrdiff_t hi, int algo, const double* lu,
+                          ptrdiff_t ldab, const ptrdiff_t* P, ptrdiff_t nrhs, double* B,
+                          ptrdiff_t ldb)
+{
+    if (n < 0 || lo < 0 || hi < 0 || nrhs < 0) return ORACLE_BAD_ARG;
+    if (n == 0 || nrhs == 0) return ORACLE_OK;
+    if (lo > n - 1 || hi > n - 1) return ORACLE_BAD_ARG;
+    if (algo == ORACLE_BAND_TRIDIAG && (lo != 1 || hi != 1)) return ORACLE_BAD_ARG;
+    const idx hu = imin(lo + hi, n - 1);
+    if (n == 1 && nrhs > 1 && ldb == 1) {
+        const double d = lu[0];
+        if (d == 0.0) return ORACLE_SINGULAR;
+        scale(B, nrhs, 1.0 / d);
+        return ORACLE_OK;
+    }
+    for (idx q = 0; q < nrhs; ++q) {
+        const int rc = rdiv_row(n, lo, hu, algo, lu, ldab, P, B + q * ldb);
+        if (rc) return rc;
+    }
+    return ORACLE_OK;
+}
+
 /* The batched band workload on the host cores: for each system s (OpenMP
  * over systems) LU_Decompose and LU_LDivEq in place, system s's band at
  * ab + s*sab, interchanges at P + s*sp, right-hand sides at B + s*sb;

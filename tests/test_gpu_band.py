@@ -259,3 +259,170 @@ def test_band_benchmark_size(dev, orc, lo, hi, algo):
         assert np.array_equal(P[s * n:(s + 1) * n].cpu().numpy(), Po)
         assert np.array_equal(bits(ab[seg].cpu().numpy()[sl]), bits(sys_ab[sl]))
         assert np.array_equal(bits(X[s * n:(s + 1) * n].cpu().numpy()), bits(xo))
+
+
+def rdiv_rows(rng, count, n, nrhs):
+    """Each system's nrhs rows (contiguous, ldb = n) with zeros and negative
+    zeros, leading and trailing runs in some rows: the trims and signed-zero
+    paths of both passes."""
+    M = rng.standard_normal((count, nrhs, n))
+    M[rng.random(M.shape) < 0.15] = 0.0
+    M[rng.random(M.shape) < 0.05] = -0.0
+    if n > 3:
+        M[::3, 0, : n // 3] = 0.0
+        M[1::3, -1, -(n // 3):] = -0.0
+    return M.reshape(-1)
+
+
+def oracle_rdiv(orc, lay, ab, M, count, nrhs, algo):
+    """Per system: factors and P from the oracle's decompose, then its
+    LU_RDivEq of the rows; returns (P, status, X)."""
+    ab, X = ab.copy(), M.copy()
+    n = lay.n
+    P = np.zeros((count, n), dtype=np.int64)
+    st = np.zeros(count, dtype=np.int32)
+    for s in range(count):
+        sys_ab = ab[s * lay.stride_ab:(s + 1) * lay.stride_ab]
+        P[s] = orc.band_lu_decompose(sys_ab, n, lay.lo, lay.hi, lay.ldab, ALGO[algo])
+        Xs = X[s * n * nrhs:(s + 1) * n * nrhs].reshape(nrhs, n)
+        try:
+            orc.band_lu_rdiveq(sys_ab, n, lay.lo, lay.hi, lay.ldab, P[s], Xs, ALGO[algo], ldb=n)
+        except oracle.OracleSingular:
+            st[s] = 1
+    return P, st, X
+
+
+def gpu_rdiv(dev, lay, ab, M, count, nrhs, algo):
+    import torch
+
+    from tmv_gb300.band import band_lu_decompose, band_lu_rdiveq
+
+    dab = torch.from_numpy(ab).to(dev)
+    dM = torch.from_numpy(M).to(dev)
+    P = torch.empty(count * lay.n, dtype=torch.int64, device=dev)
+    band_lu_decompose(dab, count, lay, P, algo=algo)
+    st = band_lu_rdiveq(dab, count, lay, P, dM, nrhs, algo=algo)
+    torch.cuda.synchronize()
+    return P.cpu().numpy().reshape(count, lay.n), st.cpu().numpy(), dM.cpu().numpy()
+
+
+@pytest.mark.parametrize("lo,hi,algo", SHAPES)
+@pytest.mark.parametrize("kind", ["normal", "int", "tiny"])
+def test_band_rdiveq_matches_oracle_bitwise(dev, orc, lo, hi, algo, kind):
+    """LU_RDivEq (x P L U = m) for every kernel class: solutions (signed zeros
+    included) and statuses bit for bit against the oracle."""
+    rng = np.random.default_rng(200 + 10 * lo + hi)
+    count, nrhs = 37, 3
+    for n in [1, 2, 3, 8, 65, 300]:
+        if lo > n - 1 or hi > n - 1:
+            continue
+        lay, ab, _ = make_batch(rng, count, n, lo, hi, kind, 1)
+        M = rdiv_rows(rng, count, n, nrhs)
+        o_P, o_st, o_X = oracle_rdiv(orc, lay, ab, M, count, nrhs, algo)
+        g_P, g_st, g_X = gpu_rdiv(dev, lay, ab, M, count, nrhs, algo)
+        assert np.array_equal(g_P, o_P)
+        assert np.array_equal(g_st, o_st), f"n={n}"
+        for s in range(count):
+            if o_st[s] == 0:
+                xs = slice(s * n * nrhs, (s + 1) * n * nrhs)
+                assert np.array_equal(bits(g_X[xs]), bits(o_X[xs])), f"n={n} system {s}"
+
+
+def test_band_rdiveq_singular_and_bad_interchange(dev, orc):
+    import torch
+
+    from tmv_gb300.band import band_lu_decompose, band_lu_rdiveq
+
+    rng = np.random.default_rng(17)
+    for lo, hi in [(2, 1), (6, 6)]:  # register and wide kernels
+        count, n, nrhs = 6, 30, 2
+        lay, ab, _ = make_batch(rng, count, n, lo, hi, "normal", 1)
+        # a zero column in system 3: a zero U(j,j), met by the forward pass
+        for i in range(max(0, 12 - hi), min(n, 12 + lo + 1)):
+            ab[3 * lay.stride_ab + i + 12 * lay.ldab] = 0.0
+        M = rdiv_rows(rng, count, n, nrhs)
+        o_P, o_st, o_X = oracle_rdiv(orc, lay, ab, M, count, nrhs, "general")
+        assert o_st[3] == 1
+        g_P, g_st, g_X = gpu_rdiv(dev, lay, ab, M, count, nrhs, "general")
+        assert np.array_equal(g_st, o_st)
+        dab = torch.from_numpy(ab).to(dev)
+        P = torch.empty(count * n, dtype=torch.int64, device=dev)
+        band_lu_decompose(dab, count, lay, P)
+        P[1 * n + 5] = 5 + lo + 1  # beyond the band
+        P[2 * n + 7] = 3           # above the diagonal
+        st = band_lu_rdiveq(dab, count, lay, P, torch.from_numpy(M).to(dev), nrhs)
+        assert st.cpu().tolist() == [0, 2, 2, 1, 0, 0]
+
+
+def test_band_rdiveq_one_unknown_rows(dev, orc):
+    """n = 1 with several rows stored at unit stride (ldb = 1): TMV scales the
+    whole row by the reciprocal, as for ldiveq's 1 x nrhs B."""
+    import torch
+
+    from tmv_gb300.band import band_layout, band_lu_decompose, band_lu_rdiveq
+
+    lay = band_layout(1, 0, 0)
+    for d in [3.0, 0.0]:
+        o_ab = np.array([d])
+        o_P = orc.band_lu_decompose(o_ab, 1, 0, 0, 1)
+        Mo = np.array([[1.0], [-2.0], [7.0]])
+        try:
+            orc.band_lu_rdiveq(o_ab, 1, 0, 0, 1, o_P, Mo, ldb=1)
+            o_st = 0
+        except oracle.OracleSingular:
+            o_st = 1
+        dab = torch.tensor([d], dtype=torch.float64, device=dev)
+        P = torch.empty(1, dtype=torch.int64, device=dev)
+        band_lu_decompose(dab, 1, lay, P)
+        dM = torch.tensor([1.0, -2.0, 7.0], dtype=torch.float64, device=dev)
+        st = band_lu_rdiveq(dab, 1, lay, P, dM, 3, ldb=1, stride_b=3)
+        assert int(st.item()) == o_st
+        if o_st == 0:
+            assert np.array_equal(bits(dM.cpu().numpy()), bits(Mo.ravel()))
+
+
+@pytest.mark.parametrize("lo,hi,algo", [(1, 1, "tridiag"), (2, 2, "general")])
+def test_band_rdiveq_benchmark_size(dev, orc, lo, hi, algo):
+    """65536 systems of n = 1024 (the band benchmark's batch): x A = m solved
+    from the factors; every system's normwise backward error of x A = m at
+    most 1e-14, 16 sampled systems bit for bit against the oracle."""
+    import torch
+
+    from tmv_gb300.band import band_layout, band_lu_decompose, band_lu_rdiveq
+
+    count, n = 65536, 1024
+    lay = band_layout(n, lo, hi)
+    g = torch.Generator(device=dev).manual_seed(6)
+    ab0 = torch.randn(count * lay.stride_ab, dtype=torch.float64, device=dev, generator=g)
+    A = ab0.view(count, lay.stride_ab)
+    i = torch.arange(n, device=dev)
+    A[:, i * (lay.ldab + 1)] += lo + hi + 2.0
+    m = torch.randn(count, n, dtype=torch.float64, device=dev, generator=g)
+    ab = ab0.clone()
+    P = torch.empty(count * n, dtype=torch.int64, device=dev)
+    band_lu_decompose(ab, count, lay, P, algo=algo)
+    X = m.clone().reshape(-1)
+    st = band_lu_rdiveq(ab, count, lay, P, X, 1, algo=algo)
+    torch.cuda.synchronize()
+    assert int(st.abs().sum().item()) == 0
+    x = X.view(count, n)
+    # x A: column j of A against x (the band of the input, diagonals -lo..hi)
+    n_, ld = lay.n, lay.ldab
+    xa = torch.zeros(count, n, dtype=torch.float64, device=dev)
+    na = torch.zeros(count, n, dtype=torch.float64, device=dev)
+    for d in range(-lo, hi + 1):
+        r = torch.arange(max(0, -d), min(n_, n_ - d), device=dev)  # rows r, columns r + d
+        xa[:, r + d] += x[:, r] * A[:, r * (ld + 1) + d * ld]
+        na[:, r + d] += A[:, r * (ld + 1) + d * ld].abs()
+    res = (xa - m).abs().amax(dim=1)
+    # for rows x A the bound is ||x||_inf ||A||_1 (column sums of |A|)
+    berr = res / (na.amax(dim=1) * x.abs().amax(dim=1) + m.abs().amax(dim=1))
+    assert float(berr.max()) <= 1e-14
+    for s in np.random.default_rng(2).choice(count, size=16, replace=False):
+        s = int(s)
+        seg = slice(s * lay.stride_ab, (s + 1) * lay.stride_ab)
+        sys_ab = ab0[seg].cpu().numpy().copy()
+        Po = orc.band_lu_decompose(sys_ab, n, lo, hi, lay.ldab, ALGO[algo])
+        xo = m[s].cpu().numpy().copy()
+        orc.band_lu_rdiveq(sys_ab, n, lo, hi, lay.ldab, Po, xo, ALGO[algo])
+        assert np.array_equal(bits(x[s].cpu().numpy()), bits(xo))

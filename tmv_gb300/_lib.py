@@ -119,6 +119,8 @@ _SIGS = {
                                                    vp, i64]),
     "tmvg_band_lu_ldiveq_batched_f64": (C.c_int, [vp, i64, i64, i64, i64, C.c_int, vp, i64, i64, vp,
                                                 i64, i64, vp, i64, i64, vp]),
+    "tmvg_band_lu_rdiveq_batched_f64": (C.c_int, [vp, i64, i64, i64, i64, C.c_int, vp, i64, i64, vp,
+                                                i64, i64, vp, i64, i64, vp]),
     "tmvg_band_lu_solve_batched_f64": (C.c_int, [vp, i64, i64, i64, i64, C.c_int, vp, i64, i64, vp,
                                                i64, i64, vp, i64, i64, vp]),
 }

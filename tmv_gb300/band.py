@@ -7,9 +7,10 @@ at ``ab[s*stride_ab + i + j*ldab]`` for ``j-hu <= i <= j+lo`` with
 ``ldab >= lo + hu``.  ``band_layout`` gives the packed defaults.
 
 The calls mirror, per system, tmv::LU_Decompose(BandMatrixView<double>, P,
-Anhi) (src/TMV_BandLUDecompose.cpp:383-425) and tmv::LU_LDivEq on band
-factors (src/TMV_BandLUDiv.cpp:811-831), bit for bit; ``algo="tridiag"``
-runs TMV's tridiagonal algorithm, the one BandLUDiv uses for lo == hi == 1.
+Anhi) (src/TMV_BandLUDecompose.cpp:383-425) and tmv::LU_LDivEq / LU_RDivEq
+on band factors (src/TMV_BandLUDiv.cpp:811-851), bit for bit;
+``algo="tridiag"`` runs TMV's tridiagonal algorithm, the one BandLUDiv uses
+for lo == hi == 1.
 """
 from __future__ import annotations
 
@@ -92,6 +93,29 @@ def band_lu_ldiveq(ab: torch.Tensor, count: int, lay: BandLayout, P: torch.Tenso
     return status
 
 
+def band_lu_rdiveq(ab: torch.Tensor, count: int, lay: BandLayout, P: torch.Tensor,
+                   M: torch.Tensor, nrhs: int, ldb: int | None = None, stride_b: int | None = None,
+                   stride_p: int | None = None, algo: str = "general",
+                   status: torch.Tensor | None = None) -> torch.Tensor:
+    """M := M (P L U)^-1 for every system from its band factors (x A = m,
+    TMV's LU_RDivEq); M holds system s's nrhs x n block with row q at
+    M[s*stride_b + q*ldb ...] (each row contiguous).  Returns the per-system
+    status as band_lu_ldiveq does."""
+    _check(ab, torch.float64, "ab")
+    _check(P, torch.int64, "P")
+    _check(M, torch.float64, "M")
+    ldb = lay.n if ldb is None else ldb
+    stride_b = ldb * nrhs if stride_b is None else stride_b
+    if status is None:
+        status = torch.empty(count, dtype=torch.int32, device=ab.device)
+    h = handle(ab.device.index)
+    h.check(h.lib.tmvg_band_lu_rdiveq_batched_f64(
+        h.h, count, lay.n, lay.lo, lay.hi, _algo(algo), _ptr(ab), lay.ldab, lay.stride_ab,
+        _ptr(P), lay.n if stride_p is None else stride_p, nrhs, _ptr(M), ldb, stride_b,
+        _ptr(status)), "band_lu_rdiveq")
+    return status
+
+
 def band_lu_solve(ab: torch.Tensor, count: int, lay: BandLayout, B: torch.Tensor, nrhs: int,
                   ldb: int | None = None, stride_b: int | None = None, algo: str = "general",
                   P: torch.Tensor | None = None,
@@ -127,5 +151,5 @@ def band_lu_solve_count(count: int, lay: BandLayout, nrhs: int) -> dict:
     return {"flops": float(flops), "bytes": float(byts)}
 
 
-__all__ = ["BandLayout", "band_layout", "band_lu_decompose", "band_lu_ldiveq", "band_lu_solve",
-           "band_lu_solve_count"]
+__all__ = ["BandLayout", "band_layout", "band_lu_decompose", "band_lu_ldiveq", "band_lu_rdiveq",
+           "band_lu_solve", "band_lu_solve_count"]

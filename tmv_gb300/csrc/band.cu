@@ -1,7 +1,7 @@
 // band.cu -- batched band LU: TMV's LU_Decompose(BandMatrixView<double>)
-// (src/TMV_BandLUDecompose.cpp:383-425) and LU_LDivEq on band factors
-// (src/TMV_BandLUDiv.cpp:811-831) for many systems of one shape, one thread
-// per system.
+// (src/TMV_BandLUDecompose.cpp:383-425), LU_LDivEq and LU_RDivEq on band
+// factors (src/TMV_BandLUDiv.cpp:811-851) for many systems of one shape, one
+// thread per system.
 //
 // A band LU is a chain of n dependent steps, each touching a window of at
 // most (lo+1) x (hu+1) entries, so one system offers no parallelism worth a
@@ -51,6 +51,7 @@ struct BandArgs {
     int64_t n;
     int lo, hi, hu, nrhs;
     int factor, solve;
+    int trans;  // the solve is LU_RDivEq: each right-hand side is a row x of x P L U = m
 };
 
 __host__ __device__ __forceinline__ int64_t lmin(int64_t x, int64_t y) { return x < y ? x : y; }
@@ -404,7 +405,169 @@ __device__ int band_solve_one(const double* __restrict__ a, int64_t ldab, const 
     return 0;
 }
 
+// ---------------------------------------------------------------------------
+// One row of LU_RDivEq (NonLapLU_RDivEq, src/TMV_BandLUDiv.cpp:244-290):
+// x P L U = m, b a row of m with unit step.
+//  1. y U = b, TriLDivEq(Transpose(U), b) (NonBlasTriLDivEq,
+//     src/TMV_BandTriDiv_V.cpp:445-468): for hu == 0 the diagonal solve of the
+//     leading part up to the last nonzero (every U(i,i) there checked);
+//     otherwise, from the first nonzero i1 on, the forward row form
+//     (DoRowLowerTriLDivEq, :240-313): b[i] -= b[j] U(j,i) for j =
+//     max(i1, i-hu) .. i-1 in that order, then b[i] / U(i,i), every U(i,i)
+//     checked.  Window x[k] = solved b[i-1-k] in registers; the loads of
+//     step i (U's column i, b[i]) are issued PD steps ahead.
+//  2. z L = y (LU_PackedPL_RDivEq, :190-222): for j = n-2 down to 0,
+//     b[j] -= sum_k L(j+k, j) b[j+k], k = 1..min(lo, n-1-j), the sum formed
+//     from 0.0 as MultMV forms it (src/TMV_MultMV.cpp:298-380, row form
+//     :80-122); the diagonal-major factors of the tridiagonal algorithm give
+//     MultMV a strided x, which it copies scaled by -1, so there the sum is of
+//     (-L) b and is added.  Then b[j] and b[P[j]] are swapped.  Window
+//     y[r] = b[j+r] in registers; b[j+lo] is final once step j is done.
+// Returns 0, 1 for a zero U(i,i) where TMV throws SingularBandLU, or 2 for
+// an interchange outside rows j..min(j+lo, n-1), which is not applied.
+// ---------------------------------------------------------------------------
+template <int HUC>
+struct RFwdLoads {
+    double u[HUC + 1];  // U(i-k, i), k = 0..hu (u[0] = U(i,i))
+    double bn;          // b[i]
+};
+
+template <int HUC>
+__device__ __forceinline__ void band_rfwd_load(const double* __restrict__ a, int64_t ldab,
+                                               const double* __restrict__ b, int64_t n, int hu, int64_t i,
+                                               RFwdLoads<HUC>& f)
+{
+#pragma unroll
+    for (int k = 0; k <= HUC; ++k) f.u[k] = (k <= hu && i - k >= 0 && i < n) ? a[(i - k) + i * ldab] : 0.0;
+    f.bn = i < n ? b[i] : 0.0;
+}
+
+template <int LOC>
+struct RBwdLoads {
+    int64_t p;
+    double l[LOC + 1];  // L(j+r, j), r = 1..lo
+    double bn;          // b[j]
+};
+
+template <int LOC>
+__device__ __forceinline__ void band_rbwd_load(const double* __restrict__ a, int64_t ldab,
+                                               const int64_t* __restrict__ P, const double* __restrict__ b,
+                                               int64_t n, int lo, int64_t j, RBwdLoads<LOC>& f)
+{
+    f.p = j >= 0 ? P[j] : 0;
+#pragma unroll
+    for (int r = 1; r <= LOC; ++r) f.l[r] = (r <= lo && j >= 0 && j + r < n) ? a[(j + r) + j * ldab] : 0.0;
+    f.bn = j >= 0 ? b[j] : 0.0;
+}
+
+// b[i] / U(i,i) for i below one past the last nonzero, every U(i,i) there
+// checked (the diagonal solve of both directions, DoDiagLDivEq1,
+// src/TMV_DiagMatrix.cpp:296-341).
+__device__ __forceinline__ int band_diag_solve(const double* __restrict__ a, int64_t ldab, int64_t n,
+                                               double* __restrict__ b)
+{
+    int64_t i2 = n;
+    while (i2 > 0 && !nonzero(b[i2 - 1])) --i2;
+    for (int64_t i = 0; i < i2; ++i) {
+        const double d = a[i + i * ldab];
+        if (!nonzero(d)) return 1;
+        b[i] = b[i] / d;
+    }
+    return 0;
+}
+
 template <int LOC, int HUC, bool TRID>
+__device__ int band_rsolve_one(const double* __restrict__ a, int64_t ldab, const int64_t* __restrict__ P,
+                               int64_t n, int lo, int hu, double* __restrict__ b)
+{
+    constexpr int PD = band_prefetch<LOC, HUC>();
+    if (hu == 0) {
+        const int st = band_diag_solve(a, ldab, n, b);
+        if (st) return st;
+    } else {
+        int64_t i1 = 0;
+        while (i1 < n && !nonzero(b[i1])) ++i1;
+        double x[HUC];
+#pragma unroll
+        for (int k = 0; k < HUC; ++k) x[k] = 0.0;
+        RFwdLoads<HUC> f[PD];
+#pragma unroll
+        for (int u = 0; u < PD; ++u) band_rfwd_load<HUC>(a, ldab, b, n, hu, i1 + u, f[u]);
+        for (int64_t i0 = i1; i0 < n; i0 += PD) {
+#pragma unroll
+            for (int u = 0; u < PD; ++u) {
+                const int64_t i = i0 + u;
+                if (i >= n) break;
+                double v = f[u].bn;
+#pragma unroll
+                for (int k = HUC - 1; k >= 0; --k)
+                    if (k < hu && i - 1 - k >= i1) v = msub(v, x[k], f[u].u[k + 1]);
+                const double d = f[u].u[0];
+                if (!nonzero(d)) return 1;
+                v = v / d;
+                b[i] = v;
+#pragma unroll
+                for (int k = HUC - 1; k > 0; --k) x[k] = x[k - 1];
+                x[0] = v;
+                // b[i+PD] is not yet written: this pass writes b[i] in order
+                band_rfwd_load<HUC>(a, ldab, b, n, hu, i + PD, f[u]);
+            }
+        }
+    }
+    if (lo == 0) return 0;
+    double y[LOC + 1];
+    y[0] = 0.0;
+#pragma unroll
+    for (int r = 1; r <= LOC; ++r) y[r] = (r <= lo && n - 2 + r < n) ? b[n - 2 + r] : 0.0;
+    RBwdLoads<LOC> g[PD];
+#pragma unroll
+    for (int u = 0; u < PD; ++u) band_rbwd_load<LOC>(a, ldab, P, b, n, lo, n - 2 - u, g[u]);
+    for (int64_t j0 = n - 2; j0 >= 0; j0 -= PD) {
+#pragma unroll
+        for (int u = 0; u < PD; ++u) {
+            const int64_t j = j0 - u;
+            if (j < 0) break;
+            y[0] = g[u].bn;
+            double t = 0.0;
+            if (TRID) {
+#pragma unroll
+                for (int r = 1; r <= LOC; ++r)
+                    if (r <= lo && j + r < n) t = __dadd_rn(t, __dmul_rn(-g[u].l[r], y[r]));
+                y[0] = __dadd_rn(y[0], t);
+            } else {
+#pragma unroll
+                for (int r = 1; r <= LOC; ++r)
+                    if (r <= lo && j + r < n) t = __dadd_rn(t, __dmul_rn(g[u].l[r], y[r]));
+                y[0] = __dsub_rn(y[0], t);
+            }
+            const int64_t pj = g[u].p;
+            if (pj < j || pj > j + lo || pj >= n) return 2;
+            const int dd = (int)(pj - j);
+#pragma unroll
+            for (int r = 1; r <= LOC; ++r)
+                if (r == dd) {
+                    const double w = y[0];
+                    y[0] = y[r];
+                    y[r] = w;
+                }
+            // b[j+lo] is final: later steps reach rows below j+lo only
+#pragma unroll
+            for (int r = 1; r <= LOC; ++r)
+                if (r == lo && j + r < n) b[j + r] = y[r];
+#pragma unroll
+            for (int r = LOC; r > 0; --r) y[r] = y[r - 1];
+            // b[j-PD] is below every row this pass has written
+            band_rbwd_load<LOC>(a, ldab, P, b, n, lo, j - PD, g[u]);
+        }
+    }
+    // rows 0..lo-1, still in the window (y[r] = b[r-1])
+#pragma unroll
+    for (int r = 1; r <= LOC; ++r)
+        if (r <= lo) b[r - 1] = y[r];
+    return 0;
+}
+
+template <int LOC, int HUC, bool TRID, bool TRANS>
 __global__ void __launch_bounds__(kBandThreads) band_lu_kernel(const BandArgs g)
 {
     const int64_t s = (int64_t)blockIdx.x * kBandThreads + threadIdx.x;
@@ -427,6 +590,9 @@ __global__ void __launch_bounds__(kBandThreads) band_lu_kernel(const BandArgs g)
                 const double inv = 1.0 / d;
                 for (int q = 0; q < g.nrhs; ++q) B[q] = scale_by(B[q], inv);
             }
+        } else if (TRANS) {
+            for (int q = 0; q < g.nrhs && st == 0; ++q)
+                st = band_rsolve_one<LOC, HUC, TRID>(a, g.ldab, P, g.n, g.lo, g.hu, B + q * g.ldb);
         } else {
             for (int q = 0; q < g.nrhs && st == 0; ++q)
                 st = band_solve_one<LOC, HUC, TRID>(a, g.ldab, P, g.n, g.lo, g.hu, B + q * g.ldb);
@@ -438,7 +604,8 @@ __global__ void __launch_bounds__(kBandThreads) band_lu_kernel(const BandArgs g)
 // The same algorithm for bands wider than the register kernels hold: the
 // window stays in the band storage itself (the thread's own slots, cached in
 // L1/L2), each step a direct transcription of the loops of
-// NonLapBandLU_Decompose and of the solves above.
+// NonLapBandLU_Decompose and of the solves above (the general algorithm
+// only: the tridiagonal one always fits the register kernel).
 __global__ void __launch_bounds__(kBandThreads) band_lu_wide_kernel(const BandArgs g)
 {
     const int64_t s = (int64_t)blockIdx.x * kBandThreads + threadIdx.x;
@@ -508,7 +675,43 @@ __global__ void __launch_bounds__(kBandThreads) band_lu_wide_kernel(const BandAr
             for (int q = 0; q < g.nrhs; ++q) B[q] = scale_by(B[q], inv);
         }
     }
-    for (int q = 0; q < g.nrhs && st == 0 && !row_b; ++q) {
+    for (int q = 0; q < g.nrhs && st == 0 && !row_b && g.trans; ++q) {
+        double* b = B + q * g.ldb;
+        if (hu == 0) {
+            st = band_diag_solve(a, ld, n, b);
+        } else {
+            int64_t i1 = 0;
+            while (i1 < n && b[i1] == 0.0) ++i1;
+            for (int64_t i = i1; i < n; ++i) {
+                double v = b[i];
+                for (int64_t j = lmax(i1, i - hu); j < i; ++j) v = msub(v, b[j], a[j + i * ld]);
+                const double d = a[i + i * ld];
+                if (d == 0.0) {
+                    st = 1;
+                    break;
+                }
+                b[i] = v / d;
+            }
+        }
+        if (st || lo == 0) continue;
+        for (int64_t j = n - 2; j >= 0; --j) {
+            const int64_t len = lmin(lo, n - 1 - j);
+            double t = 0.0;
+            for (int64_t k = 1; k <= len; ++k) t = __dadd_rn(t, __dmul_rn(a[(j + k) + j * ld], b[j + k]));
+            b[j] = __dsub_rn(b[j], t);
+            const int64_t pj = P[j];
+            if (pj < j || pj > j + lo || pj >= n) {
+                st = 2;
+                break;
+            }
+            if (pj != j) {
+                const double w = b[j];
+                b[j] = b[pj];
+                b[pj] = w;
+            }
+        }
+    }
+    for (int q = 0; q < g.nrhs && st == 0 && !row_b && !g.trans; ++q) {
         double* b = B + q * g.ldb;
         if (lo > 0) {
             int64_t jn = lmin(lo + 1, n);
@@ -568,7 +771,8 @@ int band_class(int lo, int hu, int algo)
 
 tmvg_status band_run(Context* c, int64_t count, int64_t n, int64_t lo, int64_t hi, int algo, double* AB,
                      int64_t ldab, int64_t sab, int64_t* P, int64_t sp, int64_t nrhs, double* B, int64_t ldb,
-                     int64_t sb, int32_t* status, bool factor, bool solve, const char* what)
+                     int64_t sb, int32_t* status, bool factor, bool solve, const char* what,
+                     bool trans = false)
 {
     std::string w(what);
     if (count < 0 || n < 0 || lo < 0 || hi < 0 || nrhs < 0) return set_error(c, TMVG_BAD_ARG, w + ": negative size");
@@ -613,14 +817,22 @@ tmvg_status band_run(Context* c, int64_t count, int64_t n, int64_t lo, int64_t h
     g.nrhs = solve ? (int)nrhs : 0;
     g.factor = factor;
     g.solve = solve;
+    g.trans = trans;
     const int64_t blocks = (count + kBandThreads - 1) / kBandThreads;
     if (blocks > INT32_MAX) return set_error(c, TMVG_BAD_ARG, w + ": too many systems");
     const dim3 grid((unsigned)blocks);
-    switch (band_class((int)lo, (int)hu, algo)) {
-        case 0: band_lu_kernel<1, 2, true><<<grid, kBandThreads, 0, c->stream>>>(g); break;
-        case 1: band_lu_kernel<1, 2, false><<<grid, kBandThreads, 0, c->stream>>>(g); break;
-        case 2: band_lu_kernel<2, 4, false><<<grid, kBandThreads, 0, c->stream>>>(g); break;
-        case 3: band_lu_kernel<4, 8, false><<<grid, kBandThreads, 0, c->stream>>>(g); break;
+    // the row solve (LU_RDivEq) has kernels of its own, so that the factor
+    // and column-solve kernels keep their register budget
+    const int cls = band_class((int)lo, (int)hu, algo);
+    switch (cls < 0 ? -1 : cls + (trans ? 4 : 0)) {
+        case 0: band_lu_kernel<1, 2, true, false><<<grid, kBandThreads, 0, c->stream>>>(g); break;
+        case 1: band_lu_kernel<1, 2, false, false><<<grid, kBandThreads, 0, c->stream>>>(g); break;
+        case 2: band_lu_kernel<2, 4, false, false><<<grid, kBandThreads, 0, c->stream>>>(g); break;
+        case 3: band_lu_kernel<4, 8, false, false><<<grid, kBandThreads, 0, c->stream>>>(g); break;
+        case 4: band_lu_kernel<1, 2, true, true><<<grid, kBandThreads, 0, c->stream>>>(g); break;
+        case 5: band_lu_kernel<1, 2, false, true><<<grid, kBandThreads, 0, c->stream>>>(g); break;
+        case 6: band_lu_kernel<2, 4, false, true><<<grid, kBandThreads, 0, c->stream>>>(g); break;
+        case 7: band_lu_kernel<4, 8, false, true><<<grid, kBandThreads, 0, c->stream>>>(g); break;
         default: band_lu_wide_kernel<<<grid, kBandThreads, 0, c->stream>>>(g); break;
     }
     c->launches += 1;
@@ -658,6 +870,19 @@ tmvg_status tmvg_band_lu_ldiveq_batched_f64(tmvg_handle h, int64_t count, int64_
     if (cudaSetDevice(c->device) != cudaSuccess) return set_error(c, TMVG_CUDA_ERROR, "cudaSetDevice failed");
     return band_run(c, count, n, lo, hi, algo, const_cast<double*>(AB), ldab, stride_ab, const_cast<int64_t*>(P),
                     stride_p, nrhs, B, ldb, stride_b, status, false, true, "band_lu_ldiveq");
+}
+
+tmvg_status tmvg_band_lu_rdiveq_batched_f64(tmvg_handle h, int64_t count, int64_t n, int64_t lo, int64_t hi,
+                                            int algo, const double* AB, int64_t ldab, int64_t stride_ab,
+                                            const int64_t* P, int64_t stride_p, int64_t nrhs, double* B,
+                                            int64_t ldb, int64_t stride_b, int32_t* status)
+{
+    Context* c = reinterpret_cast<Context*>(h);
+    if (!c) return TMVG_BAD_ARG;
+    c->last_error.clear();
+    if (cudaSetDevice(c->device) != cudaSuccess) return set_error(c, TMVG_CUDA_ERROR, "cudaSetDevice failed");
+    return band_run(c, count, n, lo, hi, algo, const_cast<double*>(AB), ldab, stride_ab, const_cast<int64_t*>(P),
+                    stride_p, nrhs, B, ldb, stride_b, status, false, true, "band_lu_rdiveq", true);
 }
 
 tmvg_status tmvg_band_lu_solve_batched_f64(tmvg_handle h, int64_t count, int64_t n, int64_t lo, int64_t hi,

@@ -796,28 +796,39 @@ __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_g
 
 constexpr int kRing = 3;  // shared-memory tile slots: two tiles in flight beside the one in use
 
+// Rows of blocks b >= b0 are split between two CTAs: a helper takes the
+// tiles j < b/2 (their x_j are published first) and publishes its partial
+// row sums as tagged words in hpub; the block's own CTA takes the tiles from
+// b/2 on and adds the helper's sums before its diagonal block.  Tickets run
+// 0 .. b0-1 for the unsplit blocks, then helper(b), block(b) for b = b0, ...,
+// so that every CTA waits only on CTAs with lower tickets.
 __global__ void __launch_bounds__(kPubThreads)
 trsv_pub_async_kernel(int64_t n, const float* __restrict__ tri, int64_t tsi, int64_t tsj, bool upper,
                       const float* __restrict__ dinv, const int* __restrict__ singular,
                       const float* __restrict__ mlink, bool unit, float* x, int64_t incx, bool skip_zero,
-                      unsigned long long* pub, unsigned epoch, unsigned long long* ticket, int* err,
-                      const int* stop)
+                      unsigned long long* pub, unsigned long long* hpub, int64_t b0, unsigned epoch,
+                      unsigned long long* ticket, int* err, const int* stop)
 {
     if (stop && *stop) return;  // a device-side loop has finished: no work, no waits
     extern __shared__ __align__(16) float ring[];  // [kRing][kIB columns][kIB]
-    __shared__ int s_blk, s_abort[2];  // one per parity of the wait: a single barrier separates two waits
+    __shared__ int64_t s_tk;
+    __shared__ int s_abort[2];  // one per parity of the wait: a single barrier separates two waits
     __shared__ float xj[2][kIB];
     __shared__ float rhs[kIB];
+    __shared__ float hp[kIB];
     __shared__ float part[4][kIB];
     const int tid = threadIdx.x;
     const int i = tid & (kIB - 1), q = tid >> 7;  // row of the block, quarter of the columns
     if (tid == 0) {
-        s_blk = (int)atomicAdd(ticket, 1ull);
+        s_tk = (int64_t)atomicAdd(ticket, 1ull);
         s_abort[0] = s_abort[1] = 0;
     }
     __syncthreads();
-    const int64_t b = s_blk;
+    const int64_t tk = s_tk;
     const int64_t nblk = n / kIB;
+    const int64_t b = tk < b0 ? tk : b0 + (tk - b0) / 2;
+    const bool helper = tk >= b0 && ((tk - b0) & 1) == 0;
+    const bool split = b >= b0;
     if (b >= nblk) return;
     const int64_t r0 = b * kIB;
     const unsigned long long tag = (unsigned long long)epoch << 32;
@@ -827,23 +838,24 @@ trsv_pub_async_kernel(int64_t n, const float* __restrict__ tri, int64_t tsi, int
     const int pos = upper ? kIB - 1 - i : i;  // this row's place in a slot column
 
     // independent of the other blocks: right-hand side, inverse and link rows
-    const float b_i = tid < kIB ? x[(r0 + tid) * incx] : 0.0f;
     const bool sing = singular[b] != 0;
-    const bool use_link = b >= 1 && !sing;
-    const int64_t ntiles = use_link ? b - 1 : b;
+    const bool use_link = !helper && b >= 1 && !sing;
+    const int64_t jbeg = split && !helper ? b / 2 : 0;
+    const int64_t jend = helper ? b / 2 : (use_link ? b - 1 : b);
+    const float b_i = !helper && tid < kIB ? x[(r0 + tid) * incx] : 0.0f;
     float di[kPubCols], mi[kPubCols];
     {
         const float* Di = dinv + b * (int64_t)kIB * kIB;
         const float* Mb = use_link ? mlink + b * (int64_t)kIB * kIB : nullptr;
 #pragma unroll
         for (int l = 0; l < kPubCols; ++l) {
-            di[l] = sing ? 0.0f : Di[i + (q * kPubCols + l) * kIB];
+            di[l] = sing || helper ? 0.0f : Di[i + (q * kPubCols + l) * kIB];
             mi[l] = use_link ? Mb[i + (q * kPubCols + l) * kIB] : 0.0f;
         }
     }
     // tile j into slot s: 4096 pieces of 16 bytes, 8 per thread
     auto fetch = [&](int64_t j, int s) {
-        if (j < ntiles) {
+        if (j < jend) {
             float* slot = ring + (size_t)s * kIB * kIB;
 #pragma unroll
             for (int u = 0; u < (kIB * kIB / 4) / kPubThreads; ++u) {
@@ -854,43 +866,50 @@ trsv_pub_async_kernel(int64_t n, const float* __restrict__ tri, int64_t tsi, int
         }
         cp_async_commit();  // one group per tile, empty past the last
     };
-    unsigned long long vpre = 0;
-    if (b > 0 && tid < kIB) vpre = ld_relaxed_u64(pub + tid);
-    auto wait_x = [&](int64_t j) -> bool {
-        float* xb = xj[j & 1];
+    int waits = 0;  // waits so far: the parity of the next one's buffers
+    // poll 128 tagged words from w into dst (the first value already loaded)
+    auto wait_words = [&](const unsigned long long* w, unsigned long long v, float* dst) -> bool {
+        const int par = waits++ & 1;
         if (tid < kIB) {
-            const unsigned long long* w = pub + j * kIB + tid;
-            unsigned long long v = vpre;
             unsigned spins = 0;
             while ((v & 0xffffffff00000000ull) != tag) {
                 if (++spins > kSpinLimit || *((volatile int*)err) == kDevTimeout) {
                     atomicCAS(err, (int)kDevOk, (int)kDevTimeout);
-                    s_abort[j & 1] = 1;
+                    s_abort[par] = 1;
                     break;
                 }
                 if (spins > 32) __nanosleep(32);
-                v = ld_relaxed_u64(w);
+                v = ld_relaxed_u64(w + tid);
             }
-            xb[tid] = __uint_as_float((unsigned)v);
-            if (j + 1 < b) vpre = ld_relaxed_u64(w + kIB);
+            dst[tid] = __uint_as_float((unsigned)v);
         }
-        __syncthreads();  // xb complete (and every thread's landed tile copies visible)
-        return !s_abort[j & 1];
+        __syncthreads();  // dst complete (and every thread's landed tile copies visible)
+        return !s_abort[par];
+    };
+    // the word of x_j a thread polls is loaded one wait ahead
+    unsigned long long vpre = 0;
+    if (b > 0 && tid < kIB) vpre = ld_relaxed_u64(pub + jbeg * kIB + tid);
+    auto wait_x = [&](int64_t j) -> const float* {
+        float* xb = xj[waits & 1];
+        const unsigned long long v = vpre;
+        if (tid < kIB && j + 1 < b) vpre = ld_relaxed_u64(pub + (j + 1) * kIB + tid);
+        return wait_words(pub + j * kIB, v, xb) ? xb : nullptr;
     };
     float acc0 = 0.0f, acc1 = 0.0f;
-    fetch(0, 0);
-    fetch(1, 1);
-    for (int64_t j = 0; j < ntiles; ++j) {
+    fetch(jbeg, 0);
+    fetch(jbeg + 1, 1);
+    for (int64_t j = jbeg; j < jend; ++j) {
+        const int64_t k = j - jbeg;
         cp_async_wait1();  // this thread's pieces of tile j have landed
-        if (!wait_x(j)) {
+        const float* xb = wait_x(j);
+        if (!xb) {
             asm volatile("cp.async.wait_all;" ::: "memory");
             return;
         }
-        // slot (j + 2) % 3 held tile j - 1, which every thread finished
+        // slot (k + 2) % 3 held tile j - 1, which every thread finished
         // before the barrier above
-        fetch(j + 2, (int)((j + 2) % kRing));
-        const float* slot = ring + (size_t)(j % kRing) * kIB * kIB;
-        const float* xb = xj[j & 1];
+        fetch(j + 2, (int)((k + 2) % kRing));
+        const float* slot = ring + (size_t)(k % kRing) * kIB * kIB;
 #pragma unroll
         for (int l = 0; l < kPubCols; l += 2) {
             acc0 -= slot[(q * kPubCols + l) * kIB + pos] * xb[q * kPubCols + l];
@@ -899,8 +918,24 @@ trsv_pub_async_kernel(int64_t n, const float* __restrict__ tri, int64_t tsi, int
     }
     asm volatile("cp.async.wait_all;" ::: "memory");  // the empty groups past the last tile
     part[q][i] = acc0 + acc1;
-    __syncthreads();
-    if (tid < kIB) rhs[tid] = b_i + ((part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]));
+    if (helper) {
+        __syncthreads();
+        if (tid < kIB) {
+            const float p = (part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]);
+            st_relaxed_u64(hpub + r0 + tid, tag | __float_as_uint(p));
+        }
+        return;
+    }
+    if (split) {
+        const unsigned long long v = tid < kIB ? ld_relaxed_u64(hpub + r0 + tid) : 0ull;
+        if (!wait_words(hpub + r0, v, hp)) return;  // its barrier also completes part
+    } else {
+        __syncthreads();
+    }
+    if (tid < kIB) {
+        const float h = split ? hp[tid] : 0.0f;
+        rhs[tid] = b_i + (((part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid])) + h);
+    }
     __syncthreads();
     if (!sing) {
         float sum = 0.0f;
@@ -910,8 +945,8 @@ trsv_pub_async_kernel(int64_t n, const float* __restrict__ tri, int64_t tsi, int
         __syncthreads();
         float v = tid < kIB ? (part[0][tid] + part[1][tid]) + (part[2][tid] + part[3][tid]) : 0.0f;
         if (use_link) {
-            if (!wait_x(b - 1)) return;  // its barrier also orders the reads of part above
-            const float* xb = xj[(b - 1) & 1];
+            const float* xb = wait_x(b - 1);  // its barrier also orders the reads of part above
+            if (!xb) return;
             float m0 = 0.0f, m1 = 0.0f;
 #pragma unroll
             for (int l = 0; l < kPubCols; l += 2) {
@@ -990,12 +1025,13 @@ tmvg_status trsv_with_inverse_blocks(Context* c, int64_t n, const T* tri, int64_
             if (c->trsv_pub) cudaFree(c->trsv_pub);
             c->trsv_pub = nullptr;
             c->trsv_pub_len = 0;
-            if (cudaMalloc(&c->trsv_pub, sizeof(unsigned long long) * (size_t)n) != cudaSuccess) {
+            // x's words, then the split rows' partial sums
+            if (cudaMalloc(&c->trsv_pub, 2 * sizeof(unsigned long long) * (size_t)n) != cudaSuccess) {
                 cudaGetLastError();
                 return set_error(c, TMVG_OOM, "trsv: publication buffer");
             }
             // epoch 0 is never used by a solve
-            st = check_cuda(c, cudaMemset(c->trsv_pub, 0, sizeof(unsigned long long) * (size_t)n),
+            st = check_cuda(c, cudaMemset(c->trsv_pub, 0, 2 * sizeof(unsigned long long) * (size_t)n),
                             "trsv pub clear");
             if (st) return st;
             c->trsv_pub_len = (size_t)n;
@@ -1008,9 +1044,12 @@ tmvg_status trsv_with_inverse_blocks(Context* c, int64_t n, const T* tri, int64_
                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                             "trsv async: smem attribute");
             if (st) return st;
-            trsv_pub_async_kernel<<<(unsigned)nblk, kPubThreads, smem, c->stream>>>(
+            // split rows from b0 on while every CTA has an SM of its own
+            // (one 197 KB CTA per SM)
+            const int64_t b0 = std::min<int64_t>(nblk, std::max<int64_t>(4, 2 * nblk - c->num_sms));
+            trsv_pub_async_kernel<<<(unsigned)(2 * nblk - b0), kPubThreads, smem, c->stream>>>(
                 n, tri, tsi, tsj, is_upper, dinv, singular, mlink, unit, x, incx, skip_zero, c->trsv_pub,
-                c->trsv_epoch, c->trsv_ticket, c->dflags, stop);
+                c->trsv_pub + c->trsv_pub_len, b0, c->trsv_epoch, c->trsv_ticket, c->dflags, stop);
             ++c->launches;
             return check_cuda(c, cudaGetLastError(), "trsv async launch");
         }
