@@ -565,16 +565,17 @@ def batched_bench(dev, args, with_cpu: bool) -> dict:
 # on the n = 8192 workload (commands and figures in profiles/):
 #   panel: lu_panel_leaf_kernel, k = 320: 2.08 MB / 4.03 MB
 #   trailing_update: tf32x3_update_kernel, k = 256: 432.1 MB / 495.7 MB
-#   tri_solve: trsv_pub_kernel: 139.6 MB / 138.5 MB
+#   tri_solve: trsv_pub_async_kernel: 140.4 MB / 138.5 MB
 # The traffic of a span is its algorithmic bytes times the ratio.
-NCU_TRAFFIC_PER_ALG_BYTE: dict = {"panel": 0.516, "trailing_update": 0.872, "tri_solve": 1.008}
+NCU_TRAFFIC_PER_ALG_BYTE: dict = {"panel": 0.516, "trailing_update": 0.872, "tri_solve": 1.014}
 
 KERNEL_NAMES = {
     "panel": "lu_panel_leaf_kernel (16-CTA cluster, 512 threads, one register-resident FP32 panel row "
              "per thread, 8-column leaves)",
     "trailing_update": "U12 solve + A22 -= L21 U12 (FP32: u12_reg_kernel + tf32x3_update_kernel "
                        "on tcgen05; FP64: u12_reg_kernel + gemm_simt_kernel<double>)",
-    "tri_solve": "trsv_pub_kernel (FP32 inverse-block triangular solve)",
+    "tri_solve": "trsv_pub_async_kernel (FP32 inverse-block triangular solve, tiles staged in "
+                 "shared memory by cp.async, link blocks, helper CTAs for long block rows)",
     "residual": "residual_partial_kernel + residual_final_kernel (FP64 b - A x)",
 }
 
