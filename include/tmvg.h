@@ -486,6 +486,21 @@ tmvg_status tmvg_band_lu_rdiveq_batched_f64(tmvg_handle h, int64_t count, int64_
                                             int64_t stride_ab, const int64_t* P, int64_t stride_p,
                                             int64_t nrhs, double* B, int64_t ldb, int64_t stride_b,
                                             int32_t* status);
+/* X = A^-1 B for every system as tmv::BandLUDiv computes it (B /= A for a
+ * column-major tmv::BandMatrix, src/TMV_BandLUD.cpp:60-146, 217-222), bit for
+ * bit: A's band (lo, hi) at AB[s*stride_ab + i + j*ldab], j-hi <= i <= j+lo,
+ * ldab >= lo + hi (not modified) is copied into LU (min(lo,hi)
+ * subdiagonals, hu = min(lo+hi, n-1) superdiagonals, ldlu >= min(lo,hi) +
+ * hu; must not overlap AB), transposed when hi < lo, and factored with the
+ * tridiagonal algorithm when lo == hi == 1; B (n x nrhs column-major, as for
+ * ldiveq) is then solved with LU_LDivEq, or with LU_RDivEq on the
+ * transpose's factors (its rows are B's columns).  LU and P keep the
+ * factors (of A^T when hi < lo).  Same status values. */
+tmvg_status tmvg_band_divide_batched_f64(tmvg_handle h, int64_t count, int64_t n, int64_t lo, int64_t hi,
+                                         const double* AB, int64_t ldab, int64_t stride_ab, double* LU,
+                                         int64_t ldlu, int64_t stride_lu, int64_t* P, int64_t stride_p,
+                                         int64_t nrhs, double* B, int64_t ldb, int64_t stride_b,
+                                         int32_t* status);
 /* Both in one launch (the factors and P are written as by the decompose). */
 tmvg_status tmvg_band_lu_solve_batched_f64(tmvg_handle h, int64_t count, int64_t n, int64_t lo,
                                            int64_t hi, int algo, double* AB, int64_t ldab,

@@ -248,6 +248,20 @@ class _Backend:
         if rc:
             raise RuntimeError(f"band_lu_rdiveq rc={rc}")
 
+    def band_divide(self, ab: np.ndarray, n: int, lo: int, hi: int, ldab: int, B: np.ndarray) -> None:
+        """B := A^-1 B through TMV's BandLUDiv (B /= A for a tmv::BandMatrix;
+        TMV itself only): A's band (lo, hi) at ab[i + j*ldab], j-hi <= i <= j+lo;
+        B n x nrhs column-major."""
+        assert B.dtype == np.float64
+        nrhs = 1 if B.ndim == 1 else B.shape[1]
+        ldb = n if B.ndim == 1 else B.strides[1] // 8
+        f = self._f("band_divide", C.c_int, [i64, i64, i64, vp, i64, i64, vp, i64])
+        rc = f(n, lo, hi, _p(np.ascontiguousarray(ab, dtype=np.float64)), ldab, nrhs, _p(B), ldb)
+        if rc == SINGULAR:
+            raise OracleSingular("singular")
+        if rc:
+            raise RuntimeError(f"band_divide rc={rc}")
+
     def band_batched_solve(self, count: int, n: int, lo: int, hi: int, algo: int, ab: np.ndarray,
                            ldab: int, sab: int, nrhs: int, B: np.ndarray, ldb: int, sb: int):
         """The batched band workload in place on the host cores (OpenMP over

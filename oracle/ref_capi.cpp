@@ -223,6 +223,24 @@ int tmvref_band_lu_rdiveq(ptrdiff_t n, ptrdiff_t lo, ptrdiff_t hi, int algo, con
     });
 }
 
+// B /= A for a tmv::BandMatrix A (lo, hi; column-major storage), through
+// BandLUDiv as TMV's division operators run it (src/TMV_BandLUD.cpp:85-146,
+// 217-222): A's band given in the layout above with hu = hi (no fill slots
+// needed), B n x nrhs column-major.
+int tmvref_band_divide(ptrdiff_t n, ptrdiff_t lo, ptrdiff_t hi, const double* a, ptrdiff_t ldab,
+                       ptrdiff_t nrhs, double* B, ptrdiff_t ldb)
+{
+    return guarded([&] {
+        if (n == 0 || nrhs == 0) return;
+        tmv::BandMatrix<double> A(n, n, lo, hi, 0.0);
+        for (ptrdiff_t j = 0; j < n; ++j)
+            for (ptrdiff_t i = std::max<ptrdiff_t>(0, j - hi); i <= std::min(n - 1, j + lo); ++i)
+                A(i, j) = a[i + j * ldab];
+        tmv::MatrixView<double> Bv = tmv::MatrixViewOf(B, n, nrhs, 1, ldb);
+        Bv /= A;
+    });
+}
+
 // The batched band workload through TMV, OpenMP over systems.
 int tmvref_band_batched_solve(ptrdiff_t count, ptrdiff_t n, ptrdiff_t lo, ptrdiff_t hi, int algo,
                               double* ab, ptrdiff_t ldab, ptrdiff_t sab, ptrdiff_t* P, ptrdiff_t sp,

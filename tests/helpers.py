@@ -134,3 +134,32 @@ def bits(x: np.ndarray) -> np.ndarray:
     operation creates differ between x86, aarch64 and the GPU)."""
     x = np.ascontiguousarray(x, dtype=np.float64)
     return np.where(np.isnan(x), np.float64(np.nan), x).view(np.int64)
+
+
+def band_divide_plan(lo: int, hi: int) -> tuple[int, bool]:
+    """BandLUDiv's choices for a column-major tmv::BandMatrix (src/
+    TMV_BandLUD.cpp:60-93): the tridiagonal algorithm for lo == hi == 1, the
+    transpose factored (and the solve a right division) when hi < lo."""
+    return (1 if lo == 1 and hi == 1 else 0), hi < lo
+
+
+def oracle_band_divide(orc, a: np.ndarray, lo: int, hi: int, B: np.ndarray):
+    """X = A^-1 B as BandLUDiv computes it, composed from the oracle's band
+    LU_Decompose and LU_LDivEq / LU_RDivEq.  Returns (X, status)."""
+    import oracle
+
+    n = a.shape[0]
+    algo, trans = band_divide_plan(lo, hi)
+    lo2, hi2 = (hi, lo) if trans else (lo, hi)
+    ldab = max(lo2 + band_hu(n, lo2, hi2), 1)
+    ab = band_pack(a.T if trans else a, lo2, hi2, ldab)
+    P = orc.band_lu_decompose(ab, n, lo2, hi2, ldab, algo)
+    X = np.asfortranarray(B.copy())
+    try:
+        if trans:
+            orc.band_lu_rdiveq(ab, n, lo2, hi2, ldab, P, X.T, algo)
+        else:
+            orc.band_lu_ldiveq(ab, n, lo2, hi2, ldab, P, X, algo)
+        return X, 0
+    except oracle.OracleSingular:
+        return X, 1

@@ -193,3 +193,33 @@ def test_band_rdiveq_edge_cases():
     M = np.zeros((2, 25))
     M[:, :20] = rng.standard_normal((2, 20))
     rcheck(a, 2, 3, 0, M, ldab=9, ldb=25)
+
+
+def test_band_divide_composition_matches_bandludiv():
+    """TMV's B /= A for a band matrix (BandLUDiv: the tridiagonal algorithm
+    for lo == hi == 1, A's transpose factored and LU_RDivEq when hi < lo)
+    equals the composition of the restated steps, bit for bit."""
+    from tests.helpers import oracle_band_divide
+
+    orc, ref = oracle.port(), oracle.ref()
+    rng = np.random.default_rng(31)
+    shapes = SHAPES + [(3, 1), (5, 2), (2, 0), (6, 1)]
+    for kind in ["normal", "int", "tiny"]:
+        for n in [1, 2, 3, 7, 40, 150]:
+            for lo, hi in shapes:
+                if lo > n - 1 or hi > n - 1:
+                    continue
+                a = band_matrix(rng, n, lo, hi, kind)
+                B = rng.standard_normal((n, 3))
+                B[rng.random((n, 3)) < 0.2] = 0.0
+                X1, s1 = oracle_band_divide(orc, a, lo, hi, B)
+                X2 = np.asfortranarray(B.copy())
+                try:
+                    ref.band_divide(band_pack(a, lo, hi, max(lo + hi, 1)), n, lo, hi, max(lo + hi, 1), X2)
+                    s2 = 0
+                except oracle.OracleSingular:
+                    s2 = 1
+                ctx = f"n={n} lo={lo} hi={hi} {kind}"
+                assert s1 == s2, ctx
+                if s1 == 0:
+                    assert np.array_equal(bits(X1), bits(X2)), ctx

@@ -426,3 +426,56 @@ def test_band_rdiveq_benchmark_size(dev, orc, lo, hi, algo):
         xo = m[s].cpu().numpy().copy()
         orc.band_lu_rdiveq(sys_ab, n, lo, hi, lay.ldab, Po, xo, ALGO[algo])
         assert np.array_equal(bits(x[s].cpu().numpy()), bits(xo))
+
+
+@pytest.mark.parametrize("lo,hi", [(1, 1), (2, 2), (0, 3), (3, 0), (1, 0), (2, 1), (3, 1), (5, 2),
+                                   (4, 4), (7, 3), (6, 1)])
+@pytest.mark.parametrize("kind", ["normal", "int"])
+def test_band_divide_matches_bandludiv_composition(dev, orc, lo, hi, kind):
+    """B /= A as BandLUDiv runs it (tridiagonal algorithm for lo == hi == 1,
+    the transpose factored and solved by rows when hi < lo), for the register
+    and wide kernels: solutions, factors and statuses bit for bit against the
+    oracle's composition (pinned to TMV's BandLUDiv by test_band_oracle.py)."""
+    import torch
+
+    from tests.helpers import band_divide_plan, band_hu, band_pack, oracle_band_divide
+    from tmv_gb300.band import band_divide, band_layout
+
+    rng = np.random.default_rng(300 + 10 * lo + hi)
+    count, nrhs = 23, 2
+    for n in [1, 2, 5, 64, 257]:
+        if lo > n - 1 or hi > n - 1:
+            continue
+        lay = band_layout(n, lo, hi)
+        ab = np.full(count * lay.stride_ab, np.nan)  # slots outside the band are never read
+        mats = []
+        for s in range(count):
+            a = band_matrix(rng, n, lo, hi, kind)
+            band_pack(a, lo, hi, lay.ldab, out=ab[s * lay.stride_ab:(s + 1) * lay.stride_ab])
+            mats.append(a)
+        B = rng.standard_normal((count, nrhs, n))
+        B[rng.random(B.shape) < 0.15] = 0.0
+        dab = torch.from_numpy(ab).to(dev)
+        dB = torch.from_numpy(B.reshape(-1).copy()).to(dev)
+        lu, lay_lu, P, st, trans = band_divide(dab, count, lay, dB, nrhs)
+        torch.cuda.synchronize()
+        assert trans == band_divide_plan(lo, hi)[1]
+        assert torch.equal(dab.cpu(), torch.from_numpy(ab)) or np.array_equal(
+            bits(dab.cpu().numpy()), bits(ab))  # A is not modified
+        g_X = dB.cpu().numpy().reshape(count, nrhs, n)
+        g_st = st.cpu().numpy()
+        g_lu = lu.cpu().numpy()
+        for s in range(count):
+            Xo, so = oracle_band_divide(orc, mats[s], lo, hi, B[s].T)
+            assert g_st[s] == so, f"n={n} system {s}"
+            if so == 0:
+                assert np.array_equal(bits(g_X[s].T), bits(Xo)), f"n={n} system {s}"
+            # the factors: the oracle's decompose of A (or A^T)
+            algo, tr = band_divide_plan(lo, hi)
+            lo2, hi2 = (hi, lo) if tr else (lo, hi)
+            ob = band_pack(mats[s].T if tr else mats[s], lo2, hi2, lay_lu.ldab)
+            orc.band_lu_decompose(ob, n, lo2, hi2, lay_lu.ldab, algo)
+            hu = band_hu(n, lo2, hi2)
+            sl = [i + j * lay_lu.ldab for j in range(n) for i in range(max(0, j - hu), min(n, j + lo2 + 1))]
+            seg = g_lu[s * lay_lu.stride_ab:(s + 1) * lay_lu.stride_ab]
+            assert np.array_equal(bits(seg[sl]), bits(ob[sl])), f"n={n} system {s} factors"

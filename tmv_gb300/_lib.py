@@ -121,6 +121,8 @@ _SIGS = {
                                                 i64, i64, vp, i64, i64, vp]),
     "tmvg_band_lu_rdiveq_batched_f64": (C.c_int, [vp, i64, i64, i64, i64, C.c_int, vp, i64, i64, vp,
                                                 i64, i64, vp, i64, i64, vp]),
+    "tmvg_band_divide_batched_f64": (C.c_int, [vp, i64, i64, i64, i64, vp, i64, i64, vp, i64, i64, vp,
+                                             i64, i64, vp, i64, i64, vp]),
     "tmvg_band_lu_solve_batched_f64": (C.c_int, [vp, i64, i64, i64, i64, C.c_int, vp, i64, i64, vp,
                                                i64, i64, vp, i64, i64, vp]),
 }

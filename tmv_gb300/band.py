@@ -137,6 +137,36 @@ def band_lu_solve(ab: torch.Tensor, count: int, lay: BandLayout, B: torch.Tensor
     return P, status
 
 
+def band_divide(ab: torch.Tensor, count: int, lay: BandLayout, B: torch.Tensor, nrhs: int,
+                ldb: int | None = None, stride_b: int | None = None, lu: torch.Tensor | None = None,
+                P: torch.Tensor | None = None, status: torch.Tensor | None = None):
+    """X = A^-1 B per system as TMV's BandLUDiv computes it (B /= A for a
+    tmv::BandMatrix): the tridiagonal algorithm for lo == hi == 1, A's
+    transpose factored and the columns of B solved as rows (LU_RDivEq) when
+    hi < lo.  ab holds A's band in lay (only diagonals -lo..hi are read; ab
+    is not modified); B is solved in place.  Returns (lu, lu_layout, P,
+    status, transposed): the factors (of A^T when transposed)."""
+    _check(ab, torch.float64, "ab")
+    _check(B, torch.float64, "B")
+    n, lo, hi = lay.n, lay.lo, lay.hi
+    trans = hi < lo
+    lay_lu = band_layout(n, min(lo, hi), lo if trans else hi)
+    if lu is None:
+        lu = torch.empty(max(count * lay_lu.stride_ab, 1), dtype=torch.float64, device=ab.device)
+    _check(lu, torch.float64, "lu")
+    ldb = n if ldb is None else ldb
+    stride_b = ldb * nrhs if stride_b is None else stride_b
+    if P is None:
+        P = torch.empty(count * max(n, 1), dtype=torch.int64, device=ab.device)
+    if status is None:
+        status = torch.empty(count, dtype=torch.int32, device=ab.device)
+    h = handle(ab.device.index)
+    h.check(h.lib.tmvg_band_divide_batched_f64(
+        h.h, count, n, lo, hi, _ptr(ab), lay.ldab, lay.stride_ab, _ptr(lu), lay_lu.ldab,
+        lay_lu.stride_ab, _ptr(P), n, nrhs, _ptr(B), ldb, stride_b, _ptr(status)), "band_divide")
+    return lu, lay_lu, P, status, trans
+
+
 def band_lu_solve_count(count: int, lay: BandLayout, nrhs: int) -> dict:
     """Algorithmic work of one band_lu_solve over the batch: FP64 operations
     of the general algorithm (per step a reciprocal, lo scalings, lo hu
@@ -151,5 +181,5 @@ def band_lu_solve_count(count: int, lay: BandLayout, nrhs: int) -> dict:
     return {"flops": float(flops), "bytes": float(byts)}
 
 
-__all__ = ["BandLayout", "band_layout", "band_lu_decompose", "band_lu_ldiveq", "band_lu_rdiveq",
-           "band_lu_solve", "band_lu_solve_count"]
+__all__ = ["BandLayout", "band_divide", "band_layout", "band_lu_decompose", "band_lu_ldiveq",
+           "band_lu_rdiveq", "band_lu_solve", "band_lu_solve_count"]

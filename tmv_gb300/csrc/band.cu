@@ -759,6 +759,26 @@ __global__ void __launch_bounds__(kBandThreads) band_lu_wide_kernel(const BandAr
     g.status[s] = st;
 }
 
+// BandLUDiv's copy of A into its factor storage (src/TMV_BandLUD.cpp:60-93,
+// 133-137): lo' = min(lo, hi) subdiagonals, hu = min(lo+hi, n-1)
+// superdiagonals, A itself or, when hi < lo, its transpose; the slots outside
+// A's band are zero.  One thread per column of one system.
+__global__ void __launch_bounds__(kBandThreads)
+band_copy_kernel(int64_t count, int64_t n, int lo, int hi, int lo2, int hu, bool trans,
+                 const double* __restrict__ ab, int64_t ldab, int64_t sab, double* __restrict__ lu,
+                 int64_t ldlu, int64_t slu)
+{
+    const int64_t t = (int64_t)blockIdx.x * kBandThreads + threadIdx.x;
+    if (t >= count * n) return;
+    const int64_t s = t / n, j = t % n;
+    const double* a = ab + s * sab;
+    double* o = lu + s * slu;
+    for (int64_t i = lmax(0, j - hu); i <= lmin(n - 1, j + lo2); ++i) {
+        const int64_t r = trans ? j : i, c = trans ? i : j;  // the entry of A
+        o[i + j * ldlu] = (r >= c - hi && r <= c + lo) ? a[r + c * ldab] : 0.0;
+    }
+}
+
 // The register kernel's window capacity for (lo, hu), or -1 for the wide kernel.
 int band_class(int lo, int hu, int algo)
 {
@@ -883,6 +903,46 @@ tmvg_status tmvg_band_lu_rdiveq_batched_f64(tmvg_handle h, int64_t count, int64_
     if (cudaSetDevice(c->device) != cudaSuccess) return set_error(c, TMVG_CUDA_ERROR, "cudaSetDevice failed");
     return band_run(c, count, n, lo, hi, algo, const_cast<double*>(AB), ldab, stride_ab, const_cast<int64_t*>(P),
                     stride_p, nrhs, B, ldb, stride_b, status, false, true, "band_lu_rdiveq", true);
+}
+
+tmvg_status tmvg_band_divide_batched_f64(tmvg_handle h, int64_t count, int64_t n, int64_t lo, int64_t hi,
+                                         const double* AB, int64_t ldab, int64_t stride_ab, double* LU,
+                                         int64_t ldlu, int64_t stride_lu, int64_t* P, int64_t stride_p,
+                                         int64_t nrhs, double* B, int64_t ldb, int64_t stride_b,
+                                         int32_t* status)
+{
+    Context* c = reinterpret_cast<Context*>(h);
+    if (!c) return TMVG_BAD_ARG;
+    c->last_error.clear();
+    if (cudaSetDevice(c->device) != cudaSuccess) return set_error(c, TMVG_CUDA_ERROR, "cudaSetDevice failed");
+    if (count < 0 || n < 0 || lo < 0 || hi < 0 || nrhs < 0)
+        return set_error(c, TMVG_BAD_ARG, "band_divide: negative size");
+    if (count == 0 || n == 0) return TMVG_OK;
+    if (lo > n - 1 || hi > n - 1) return set_error(c, TMVG_BAD_ARG, "band_divide: lo and hi must be < n");
+    if (!AB || !LU) return set_error(c, TMVG_BAD_ARG, "band_divide: null band pointer");
+    if (ldab < std::max<int64_t>(lo + hi, 1)) return set_error(c, TMVG_BAD_ARG, "band_divide: ldab < lo + hi");
+    if (count > 1 && stride_ab < (n - 1) * (ldab + 1) + 1)
+        return set_error(c, TMVG_BAD_ARG, "band_divide: band systems overlap (stride_ab)");
+    // BandLUDiv: the tridiagonal algorithm for lo == hi == 1; the transpose
+    // factored when hi < lo (src/TMV_BandLUD.cpp:60-93)
+    const bool trans = hi < lo;
+    const int algo = (lo == 1 && hi == 1) ? TMVG_BAND_TRIDIAG : TMVG_BAND_GENERAL;
+    const int64_t lo2 = trans ? hi : lo, hi2 = trans ? lo : hi;
+    const int64_t hu = std::min(lo + hi, n - 1);
+    if (ldlu < std::max<int64_t>(lo2 + hu, 1)) return set_error(c, TMVG_BAD_ARG, "band_divide: ldlu < min(lo,hi) + hu");
+    if (count > 1 && stride_lu < (n - 1) * (ldlu + 1) + 1)
+        return set_error(c, TMVG_BAD_ARG, "band_divide: factor systems overlap (stride_lu)");
+    const int64_t threads = count * n;
+    const int64_t blocks = (threads + kBandThreads - 1) / kBandThreads;
+    if (blocks > INT32_MAX) return set_error(c, TMVG_BAD_ARG, "band_divide: too many systems");
+    band_copy_kernel<<<(unsigned)blocks, kBandThreads, 0, c->stream>>>(count, n, (int)lo, (int)hi, (int)lo2,
+                                                                     (int)hu, trans, AB, ldab, stride_ab, LU,
+                                                                     ldlu, stride_lu);
+    c->launches += 1;
+    tmvg_status st = check_cuda(c, cudaGetLastError(), "band_divide: copy");
+    if (st) return st;
+    return band_run(c, count, n, lo2, hi2, algo, LU, ldlu, stride_lu, P, stride_p, nrhs, B, ldb, stride_b, status,
+                    true, true, "band_divide", trans);
 }
 
 tmvg_status tmvg_band_lu_solve_batched_f64(tmvg_handle h, int64_t count, int64_t n, int64_t lo, int64_t hi,
