@@ -119,15 +119,33 @@ __device__ __forceinline__ void band_load_row(const double* __restrict__ a, int6
 // which no earlier step touched (its loads were issued PD steps earlier).
 // Its new column j+1+hu holds fill above row j+1+lo (zero).
 // ---------------------------------------------------------------------------
-template <int LOC, int HUC, bool TRID>
+//
+// With FUSE, the packed P L solve of one right-hand side b (the forward part
+// of band_solve_one, LU_PackedPL_LDivEq) runs inside the same loop: step j's
+// interchange and L column are final when the step ends (TMV's band LU never
+// swaps L's earlier columns), so b's window y[r] = b[j+r] takes the same
+// operations in the same order as in a separate pass, without reloading L,
+// P and b.  *last_nz receives the last nonzero row of the result (-1: none).
+// Needs lo >= 1.
+template <int LOC, int HUC, bool TRID, bool FUSE = false>
 __device__ void band_factor(double* __restrict__ a, int64_t ldab, int64_t* __restrict__ P, int64_t n,
-                            int lo, int hi, int hu)
+                            int lo, int hi, int hu, double* __restrict__ b = nullptr,
+                            int64_t* last_nz = nullptr)
 {
     if (lo == 0) {  // already U (src/TMV_BandLUDecompose.cpp:417-421); no fill
         for (int64_t i = 0; i < n; ++i) P[i] = i;
         return;
     }
     constexpr int PD = band_prefetch<LOC, HUC>();
+    double y[LOC + 1];
+    double ypre[PD];
+    int64_t lnz = -1;
+    if (FUSE) {
+#pragma unroll
+        for (int r = 0; r <= LOC; ++r) y[r] = (r <= lo && r < n) ? b[r] : 0.0;
+#pragma unroll
+        for (int u = 0; u < PD; ++u) ypre[u] = (u + 1 + lo < n) ? b[u + 1 + lo] : 0.0;
+    }
     double W[LOC + 1][HUC + 1];
 #pragma unroll
     for (int r = 0; r <= LOC; ++r)
@@ -166,6 +184,14 @@ __device__ void band_factor(double* __restrict__ a, int64_t ldab, int64_t* __res
                     }
                     W[1][1] = msub(W[1][1], W[1][0], W[0][1]);
                     if (pivot && j + 2 < n) W[1][2] = msub(W[1][2], W[1][0], W[0][2]);
+                    if (FUSE) {
+                        if (pivot) {
+                            const double t = y[0];
+                            y[0] = y[1];
+                            y[1] = t;
+                        }
+                        if (nonzero(y[0])) y[1] = msub(y[1], W[1][0], y[0]);
+                    }
                 } else {
                     // first strict maximum of |A(j..j+rlim-1, j)|
                     double piv = W[0][0];
@@ -208,6 +234,20 @@ __device__ void band_factor(double* __restrict__ a, int64_t ldab, int64_t* __res
                             for (int r = 1; r <= LOC; ++r)
                                 if (r < rlim) W[r][c] = msub(W[r][c], W[r][0], uc);
                     }
+                    if (FUSE) {
+#pragma unroll
+                        for (int r = 1; r <= LOC; ++r)
+                            if (r == ip) {
+                                const double t = y[0];
+                                y[0] = y[r];
+                                y[r] = t;
+                            }
+                        const double bj = y[0];
+                        if (nonzero(bj))
+#pragma unroll
+                            for (int r = 1; r <= LOC; ++r)
+                                if (r < rlim) y[r] = msub(y[r], W[r][0], bj);
+                    }
                 }
             } else {
                 P[j] = j;
@@ -219,7 +259,21 @@ __device__ void band_factor(double* __restrict__ a, int64_t ldab, int64_t* __res
 #pragma unroll
             for (int c = 1; c <= HUC; ++c)
                 if (c < clim) a[j + (j + c) * ldab] = W[0][c];
+            if (FUSE) {
+                b[j] = y[0];
+                if (nonzero(y[0])) lnz = j;
+            }
             if (j + 1 == n) break;
+            if (FUSE) {
+                // b[j+1+lo] enters (untouched so far: the window reached row j+lo)
+#pragma unroll
+                for (int r = 0; r < LOC; ++r) y[r] = y[r + 1];
+                y[LOC] = 0.0;
+#pragma unroll
+                for (int r = 0; r <= LOC; ++r)
+                    if (r == lo) y[r] = ypre[u];
+                ypre[u] = (j + 1 + lo + PD < n) ? b[j + 1 + lo + PD] : 0.0;
+            }
 #pragma unroll
             for (int r = 0; r <= LOC; ++r)
 #pragma unroll
@@ -233,6 +287,7 @@ __device__ void band_factor(double* __restrict__ a, int64_t ldab, int64_t* __res
             band_load_row<HUC>(a, ldab, n, lo, hu, j + PD, pre[u]);
         }
     }
+    if (FUSE) *last_nz = lnz;
 }
 
 // ---------------------------------------------------------------------------
@@ -284,62 +339,13 @@ __device__ __forceinline__ void band_bwd_load(const double* __restrict__ a, int6
     f.bn = (nr >= 0 && j >= 0) ? b[nr] : 0.0;
 }
 
-template <int LOC, int HUC, bool TRID>
-__device__ int band_solve_one(const double* __restrict__ a, int64_t ldab, const int64_t* __restrict__ P,
-                              int64_t n, int lo, int hu, double* __restrict__ b)
+// The upper solve of band_solve_one on rows below i2 (one past the last
+// nonzero after the P L solve).
+template <int HUC, bool TRID>
+__device__ int band_upper_solve(const double* __restrict__ a, int64_t ldab, int64_t n, int hu,
+                                double* __restrict__ b, int64_t i2)
 {
-    constexpr int PD = band_prefetch<LOC, HUC>();
-    int64_t last_nz = -1;
-    if (lo == 0) {
-        for (int64_t j = n - 1; j >= 0; --j)
-            if (nonzero(b[j])) {
-                last_nz = j;
-                break;
-            }
-    } else {
-        double y[LOC + 1];
-#pragma unroll
-        for (int r = 0; r <= LOC; ++r) y[r] = (r <= lo && r < n) ? b[r] : 0.0;
-        FwdLoads<LOC> f[PD];
-#pragma unroll
-        for (int u = 0; u < PD; ++u) band_fwd_load<LOC>(a, ldab, P, b, n, lo, u, f[u]);
-        for (int64_t j0 = 0; j0 < n; j0 += PD) {
-#pragma unroll
-            for (int u = 0; u < PD; ++u) {
-                const int64_t j = j0 + u;
-                if (j >= n) break;
-                if (j + 1 < n) {
-                    const int64_t pj = f[u].p;
-                    if (pj < j || pj > j + lo || pj >= n) return 2;
-                    const int d = (int)(pj - j);
-#pragma unroll
-                    for (int r = 1; r <= LOC; ++r)
-                        if (r == d) {
-                            const double t = y[0];
-                            y[0] = y[r];
-                            y[r] = t;
-                        }
-                    const double bj = y[0];
-                    if (nonzero(bj))
-#pragma unroll
-                        for (int r = 1; r <= LOC; ++r)
-                            if (r <= lo && j + r < n) y[r] = msub(y[r], f[u].l[r], bj);
-                }
-                b[j] = y[0];
-                if (nonzero(y[0])) last_nz = j;
-                const double bn = f[u].bn;
-#pragma unroll
-                for (int r = 0; r < LOC; ++r) y[r] = y[r + 1];
-                y[LOC] = 0.0;
-#pragma unroll
-                for (int r = 0; r <= LOC; ++r)
-                    if (r == lo) y[r] = bn;
-                // b[j+1+lo+PD] is not yet touched: the window covers rows up to j+1+lo
-                band_fwd_load<LOC>(a, ldab, P, b, n, lo, j + PD, f[u]);
-            }
-        }
-    }
-    const int64_t i2 = last_nz + 1;
+    constexpr int PD = band_prefetch<1, HUC>();
     if (i2 == 0) return 0;
     if (hu == 0) {
         for (int64_t i = 0; i < i2; ++i) {
@@ -403,6 +409,64 @@ __device__ int band_solve_one(const double* __restrict__ a, int64_t ldab, const 
         }
     }
     return 0;
+}
+
+template <int LOC, int HUC, bool TRID>
+__device__ int band_solve_one(const double* __restrict__ a, int64_t ldab, const int64_t* __restrict__ P,
+                              int64_t n, int lo, int hu, double* __restrict__ b)
+{
+    constexpr int PD = band_prefetch<LOC, HUC>();
+    int64_t last_nz = -1;
+    if (lo == 0) {
+        for (int64_t j = n - 1; j >= 0; --j)
+            if (nonzero(b[j])) {
+                last_nz = j;
+                break;
+            }
+    } else {
+        double y[LOC + 1];
+#pragma unroll
+        for (int r = 0; r <= LOC; ++r) y[r] = (r <= lo && r < n) ? b[r] : 0.0;
+        FwdLoads<LOC> f[PD];
+#pragma unroll
+        for (int u = 0; u < PD; ++u) band_fwd_load<LOC>(a, ldab, P, b, n, lo, u, f[u]);
+        for (int64_t j0 = 0; j0 < n; j0 += PD) {
+#pragma unroll
+            for (int u = 0; u < PD; ++u) {
+                const int64_t j = j0 + u;
+                if (j >= n) break;
+                if (j + 1 < n) {
+                    const int64_t pj = f[u].p;
+                    if (pj < j || pj > j + lo || pj >= n) return 2;
+                    const int d = (int)(pj - j);
+#pragma unroll
+                    for (int r = 1; r <= LOC; ++r)
+                        if (r == d) {
+                            const double t = y[0];
+                            y[0] = y[r];
+                            y[r] = t;
+                        }
+                    const double bj = y[0];
+                    if (nonzero(bj))
+#pragma unroll
+                        for (int r = 1; r <= LOC; ++r)
+                            if (r <= lo && j + r < n) y[r] = msub(y[r], f[u].l[r], bj);
+                }
+                b[j] = y[0];
+                if (nonzero(y[0])) last_nz = j;
+                const double bn = f[u].bn;
+#pragma unroll
+                for (int r = 0; r < LOC; ++r) y[r] = y[r + 1];
+                y[LOC] = 0.0;
+#pragma unroll
+                for (int r = 0; r <= LOC; ++r)
+                    if (r == lo) y[r] = bn;
+                // b[j+1+lo+PD] is not yet touched: the window covers rows up to j+1+lo
+                band_fwd_load<LOC>(a, ldab, P, b, n, lo, j + PD, f[u]);
+            }
+        }
+    }
+    return band_upper_solve<HUC, TRID>(a, ldab, n, hu, b, last_nz + 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -574,6 +638,16 @@ __global__ void __launch_bounds__(kBandThreads) band_lu_kernel(const BandArgs g)
     if (s >= g.count) return;
     double* a = g.ab + s * g.sab;
     int64_t* P = g.P + s * g.sp;
+    if (!TRANS && LOC <= 2 && g.factor && g.solve && g.nrhs == 1 && g.lo > 0) {
+        // factor and solve of one right-hand side: the P L solve inside the
+        // factorisation's loop, then the upper solve (not for the widest
+        // register class, whose window already takes most registers)
+        double* B = g.B + s * g.sb;
+        int64_t lnz = -1;
+        band_factor<LOC, HUC, TRID, true>(a, g.ldab, P, g.n, g.lo, g.hi, g.hu, B, &lnz);
+        g.status[s] = band_upper_solve<HUC, TRID>(a, g.ldab, g.n, g.hu, B, lnz + 1);
+        return;
+    }
     if (g.factor) band_factor<LOC, HUC, TRID>(a, g.ldab, P, g.n, g.lo, g.hi, g.hu);
     if (!g.solve) return;
     int st = 0;
