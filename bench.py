@@ -847,7 +847,20 @@ def band_workloads(dev, with_cpu: bool, count: int = 65536) -> dict:
     rate in operations -- and HBM for the bytes read and written once."""
     import torch
 
-    from tmv_gb300.band import band_layout, band_lu_solve, band_lu_solve_count
+    from tmv_gb300.band import band_divide, band_layout, band_lu_rdiveq, band_lu_solve, band_lu_solve_count
+
+    def timed(fn, reset) -> float:
+        ts = []
+        for rep in range(6):
+            reset()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if rep >= 2:
+                ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts))
 
     n = 1024
     stream = torch.cuda.current_stream(dev)
@@ -893,6 +906,14 @@ def band_workloads(dev, with_cpu: bool, count: int = 65536) -> dict:
                              "frac": round(gbs / hbm, 4)},
             "workload": f"{count} systems, n = {n}, lo = {lo}, hi = {hi}, 1 right-hand side, "
                         f"algorithm {algo}"}
+        # x A = b from the same factors (LU_RDivEq), one row per system
+        X2 = torch.empty_like(b0)
+        ms_r = timed(lambda: band_lu_rdiveq(ab, count, lay, P, X2, 1, algo=algo, status=st),
+                     lambda: X2.copy_(b0))
+        assert int(st.abs().sum().item()) == 0
+        out[key]["rdiveq"] = {"value": round(count / (ms_r * 1e-3), 1), "unit": "systems/s",
+                              "ms": round(ms_r, 4),
+                              "what": "x A = b per system from the factors above (LU_RDivEq)"}
         if with_cpu:
             orc, kind, what = cpu_reference()
             cores = os.cpu_count() or 1
@@ -919,6 +940,24 @@ def band_workloads(dev, with_cpu: bool, count: int = 65536) -> dict:
                             "tests); g++ -O2 on aarch64 contracts a - b*c into fused "
                             "multiply-adds by default, so TMV built there differs by rounding"}}
         del ab0, b0, ab, X, P, st
+    lo, hi = 2, 1
+    lay = band_layout(n, lo, hi)
+    g = torch.Generator(device=dev).manual_seed(12)
+    ab0 = torch.randn(count * lay.stride_ab, dtype=torch.float64, device=dev, generator=g)
+    i = torch.arange(n, device=dev)
+    ab0.view(count, lay.stride_ab)[:, i * (lay.ldab + 1)] += lo + hi + 2.0
+    b0 = torch.randn(count * n, dtype=torch.float64, device=dev, generator=g)
+    X = torch.empty_like(b0)
+    lay_lu = band_layout(n, min(lo, hi), lo)
+    lu = torch.empty(count * lay_lu.stride_ab, dtype=torch.float64, device=dev)
+    P = torch.empty(count * n, dtype=torch.int64, device=dev)
+    st = torch.empty(count, dtype=torch.int32, device=dev)
+    ms_d = timed(lambda: band_divide(ab0, count, lay, X, 1, lu=lu, P=P, status=st), lambda: X.copy_(b0))
+    assert int(st.abs().sum().item()) == 0
+    out["divide_lo2_hi1"] = {
+        "value": round(count / (ms_d * 1e-3), 1), "unit": "systems/s", "ms": round(ms_d, 4),
+        "workload": f"{count} systems, n = {n}, lo = 2, hi = 1, 1 right-hand side: B /= A as "
+                    "BandLUDiv runs it (A^T copied and factored, then LU_RDivEq), A not modified"}
     return out
 
 
