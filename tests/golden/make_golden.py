@@ -291,8 +291,60 @@ def complex_lu(ref):
     np.savez_compressed(HERE / "complex_lu.npz", **out)
 
 
+def band_lu(ref):
+    # TMV's band LU_Decompose (general and tridiagonal algorithms), band
+    # LU_LDivEq / LU_RDivEq from those factors, and BandLUDiv's B /= A (the
+    # transpose factored when hi < lo), on seeded inputs with exact zeros
+    from helpers import band_hu, band_matrix, band_pack
+
+    rng = np.random.default_rng(2024)
+    out = {}
+    cases = [(n, lo, hi, algo, kind)
+             for n in (1, 2, 5, 33)
+             for lo, hi, algo in ((0, 0, 0), (0, 2, 0), (1, 0, 0), (1, 1, 0), (1, 1, 1), (2, 1, 0),
+                                  (1, 3, 0), (2, 2, 0), (4, 3, 0), (7, 7, 0))
+             for kind in ("normal", "int")
+             if lo <= n - 1 and hi <= n - 1]
+    for c, (n, lo, hi, algo, kind) in enumerate(cases):
+        a = band_matrix(rng, n, lo, hi, kind)
+        hu = band_hu(n, lo, hi)
+        ldab = max(lo + hu, 1)
+        ab = band_pack(a, lo, hi, ldab)
+        lu = ab.copy()
+        P = ref.band_lu_decompose(lu, n, lo, hi, ldab, algo)
+        B = rng.standard_normal((n, 2))
+        B[rng.random((n, 2)) < 0.2] = 0.0
+        X = np.asfortranarray(B.copy())
+        try:
+            ref.band_lu_ldiveq(lu, n, lo, hi, ldab, P, X, algo)
+            xst = 0
+        except oracle.OracleSingular:
+            xst = 1
+        M = rng.standard_normal((2, n))
+        M[rng.random((2, n)) < 0.2] = 0.0
+        M[rng.random((2, n)) < 0.1] = -0.0
+        Y = M.copy()
+        try:
+            ref.band_lu_rdiveq(lu, n, lo, hi, ldab, P, Y, algo)
+            yst = 0
+        except oracle.OracleSingular:
+            yst = 1
+        D = np.asfortranarray(B.copy())
+        ldd = max(lo + hi, 1)
+        try:
+            ref.band_divide(band_pack(a, lo, hi, ldd), n, lo, hi, ldd, D)
+            dst = 0
+        except oracle.OracleSingular:
+            dst = 1
+        out.update({f"c{c}_meta": np.array([n, lo, hi, algo, ldab, xst, yst, dst]), f"c{c}_ab": ab,
+                    f"c{c}_lu": lu, f"c{c}_P": P, f"c{c}_B": B, f"c{c}_X": X, f"c{c}_M": M,
+                    f"c{c}_Y": Y, f"c{c}_D": D})
+    out["count"] = np.array([len(cases)])
+    np.savez_compressed(HERE / "band_lu.npz", **out)
+
+
 FIXTURES = [arith8, square4, decomp200, bign, random_lu, special, batched_small, inverse,
-            multmv_tri, complex_lu]
+            multmv_tri, complex_lu, band_lu]
 
 
 def main(names: list[str]):

@@ -208,3 +208,45 @@ def test_complex_lu_fixtures(orc):
         P = orc.lu_decompose_z(A)
         assert np.array_equal(P, g[f"sP{q}"])
         np.testing.assert_array_equal(A, g[f"sLU{q}"])
+
+
+def test_band_lu_fixtures(orc):
+    # TMV's own band LU_Decompose, LU_LDivEq, LU_RDivEq and BandLUDiv's
+    # B /= A (band_lu.npz), bit for bit: pivots, factors, solutions (signed
+    # zeros included) and singular statuses
+    import oracle
+    from helpers import band_hu, band_unpack, bits, oracle_band_divide
+
+    g = load("band_lu.npz")
+    for c in range(int(g["count"][0])):
+        n, lo, hi, algo, ldab, xst, yst, dst = (int(v) for v in g[f"c{c}_meta"])
+        lu = g[f"c{c}_ab"].copy()  # the input band (fill slots zero)
+        a = band_unpack(lu, n, lo, band_hu(n, lo, hi), ldab)
+        P = orc.band_lu_decompose(lu, n, lo, hi, ldab, algo)
+        ctx = f"case {c}: n={n} lo={lo} hi={hi} algo={algo}"
+        assert np.array_equal(P, g[f"c{c}_P"]), ctx
+        hu = band_hu(n, lo, hi)
+        sl = [i + j * ldab for j in range(n) for i in range(max(0, j - hu), min(n, j + lo + 1))]
+        assert np.array_equal(bits(lu[sl]), bits(g[f"c{c}_lu"][sl])), ctx
+        X = np.asfortranarray(g[f"c{c}_B"].copy())
+        try:
+            orc.band_lu_ldiveq(lu, n, lo, hi, ldab, P, X, algo)
+            st = 0
+        except oracle.OracleSingular:
+            st = 1
+        assert st == xst, ctx
+        if st == 0:
+            assert np.array_equal(bits(X), bits(g[f"c{c}_X"])), ctx
+        Y = g[f"c{c}_M"].copy()
+        try:
+            orc.band_lu_rdiveq(lu, n, lo, hi, ldab, P, Y, algo)
+            st = 0
+        except oracle.OracleSingular:
+            st = 1
+        assert st == yst, ctx
+        if st == 0:
+            assert np.array_equal(bits(Y), bits(g[f"c{c}_Y"])), ctx
+        D, st = oracle_band_divide(orc, a, lo, hi, g[f"c{c}_B"])
+        assert st == dst, ctx
+        if st == 0:
+            assert np.array_equal(bits(D), bits(g[f"c{c}_D"])), ctx
