@@ -97,13 +97,14 @@ tmvg_status tmvg_probe_fp64_rate(tmvg_handle h, double* tflops);
 /* Failure-path test hook, no counterpart in TMV.  poll_limit sets how many
  * polls the block-flag waits of the sync-free triangular solve (the solve of
  * up to 8 right-hand sides behind tmvg_tri_ldiveq_f64, tmvg_lu_ldiveq_f64 and
- * the FP64 solves) make before they give up (0 restores the default, 2^24
- * polls with back-off).  skip_blocks > 0 makes the next such solve hand its
- * 64-row blocks out from block skip_blocks on, so blocks [0, skip_blocks)
- * are never solved and their flags never published: the first block that
- * waits on one gives up after poll_limit polls, the others stop in turn, and
- * the call returns TMVG_TIMEOUT with the handle still usable (the hook
- * resets itself after that one launch).  Nothing traps or hangs. */
+ * the FP64 solves) and of the mixed solve's streamed FP32 triangular solve
+ * (n a multiple of 128) make before they give up (0 restores the default,
+ * 2^24 polls with back-off).  skip_blocks > 0 makes the next such solve hand
+ * its blocks out from ticket skip_blocks on, so the first blocks are never
+ * solved and their results never published: the first block that waits on
+ * one gives up after poll_limit polls, the others stop in turn, and the call
+ * returns TMVG_TIMEOUT with the handle still usable (the hook resets itself
+ * after that one launch).  Nothing traps or hangs. */
 tmvg_status tmvg_test_set_wait(tmvg_handle h, uint32_t poll_limit, int32_t skip_blocks);
 
 /* ---- MultMM ----------------------------------------------------------

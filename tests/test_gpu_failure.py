@@ -73,3 +73,35 @@ def test_test_hook_rejects_negative_skip(dev):
 
     h = linalg.handle(dev.index or 0)
     assert h.call("tmvg_test_set_wait", 0, -1) == 3  # TMVG_BAD_ARG
+
+
+def test_refinement_solve_wait_times_out_and_handle_recovers(dev):
+    """The same hook on the mixed solve's streamed FP32 triangular solve
+    (n = 512: whole 128-row blocks, each CTA waiting on tagged words of the
+    blocks before it): its first launch starts at ticket 1, block 0 never
+    publishes, the wait on it gives up after 2000 polls, the solve returns
+    TMVG_TIMEOUT, and the next solve on the same handle converges."""
+    from tmv_gb300 import TmvgError, linalg
+
+    rng = np.random.default_rng(92)
+    n = 512
+    a = rng.standard_normal((n, n)) + 4.0 * np.sqrt(n) * np.eye(n)
+    b = rng.standard_normal(n)
+    h = linalg.handle(dev.index or 0)
+    A = to_dev(a, dev, "F")
+    B = to_dev(b.reshape(n, 1), dev, "F")
+    h.check(h.call("tmvg_test_set_wait", 2000, 1), "test_set_wait")
+    try:
+        t0 = time.perf_counter()
+        with pytest.raises(TmvgError) as ei:
+            linalg.solve_mixed(A, B)
+        dt = time.perf_counter() - t0
+    finally:
+        h.check(h.call("tmvg_test_set_wait", 0, 0), "test_set_wait")
+    assert ei.value.status == TIMEOUT
+    assert "timed out" in str(ei.value)
+    assert dt < 10.0
+    X, info = linalg.solve_mixed(A, B)
+    assert info.converged == 1
+    x = to_host(X)[:, 0]
+    assert np.abs(a @ x - b).max() <= 1e-12 * (np.abs(a).sum(axis=1).max() * np.abs(x).max())

@@ -807,7 +807,7 @@ trsv_pub_async_kernel(int64_t n, const float* __restrict__ tri, int64_t tsi, int
                       const float* __restrict__ dinv, const int* __restrict__ singular,
                       const float* __restrict__ mlink, bool unit, float* x, int64_t incx, bool skip_zero,
                       unsigned long long* pub, unsigned long long* hpub, int64_t b0, unsigned epoch,
-                      unsigned long long* ticket, int* err, const int* stop)
+                      unsigned long long* ticket, int64_t tk0, unsigned limit, int* err, const int* stop)
 {
     if (stop && *stop) return;  // a device-side loop has finished: no work, no waits
     extern __shared__ __align__(16) float ring[];  // [kRing][kIB columns][kIB]
@@ -820,7 +820,8 @@ trsv_pub_async_kernel(int64_t n, const float* __restrict__ tri, int64_t tsi, int
     const int tid = threadIdx.x;
     const int i = tid & (kIB - 1), q = tid >> 7;  // row of the block, quarter of the columns
     if (tid == 0) {
-        s_tk = (int64_t)atomicAdd(ticket, 1ull);
+        // tickets from tk0 on (tk0 > 0 only for the failure-path test hook)
+        s_tk = (int64_t)atomicAdd(ticket, 1ull) + tk0;
         s_abort[0] = s_abort[1] = 0;
     }
     __syncthreads();
@@ -873,7 +874,7 @@ trsv_pub_async_kernel(int64_t n, const float* __restrict__ tri, int64_t tsi, int
         if (tid < kIB) {
             unsigned spins = 0;
             while ((v & 0xffffffff00000000ull) != tag) {
-                if (++spins > kSpinLimit || *((volatile int*)err) == kDevTimeout) {
+                if (++spins > limit || *((volatile int*)err) == kDevTimeout) {
                     atomicCAS(err, (int)kDevOk, (int)kDevTimeout);
                     s_abort[par] = 1;
                     break;
@@ -1047,9 +1048,16 @@ tmvg_status trsv_with_inverse_blocks(Context* c, int64_t n, const T* tri, int64_
             // split rows from b0 on while every CTA has an SM of its own
             // (one 197 KB CTA per SM)
             const int64_t b0 = std::min<int64_t>(nblk, std::max<int64_t>(4, 2 * nblk - c->num_sms));
+            // the failure-path test hook: tickets start at test_skip_blocks,
+            // so the blocks before it are never solved and the waits on them
+            // give up after poll_limit polls
+            const int64_t tk0 = c->test_skip_blocks > 0 ? c->test_skip_blocks : 0;
+            c->test_skip_blocks = 0;
+            const unsigned limit = c->poll_limit ? c->poll_limit : kSpinLimit;
             trsv_pub_async_kernel<<<(unsigned)(2 * nblk - b0), kPubThreads, smem, c->stream>>>(
                 n, tri, tsi, tsj, is_upper, dinv, singular, mlink, unit, x, incx, skip_zero, c->trsv_pub,
-                c->trsv_pub + c->trsv_pub_len, b0, c->trsv_epoch, c->trsv_ticket, c->dflags, stop);
+                c->trsv_pub + c->trsv_pub_len, b0, c->trsv_epoch, c->trsv_ticket, tk0, limit, c->dflags,
+                stop);
             ++c->launches;
             return check_cuda(c, cudaGetLastError(), "trsv async launch");
         }
